@@ -1,0 +1,198 @@
+"""ctypes front-end of the CPU oracle (oracle/xpsi_oracle.c + gslsub).
+
+TEST INFRASTRUCTURE.  The functions below mirror the reference's module-level
+callables (same argument meaning, numpy in / numpy out) so tests read like
+the reference's own: they are the checker for the CUDA path and the timed CPU
+baseline, never the product.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SOURCES = [os.path.join(HERE, "xpsi_oracle.c"),
+           os.path.join(HERE, "gslsub", "gslsub.c")]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle shared library (gcc, OpenMP, no FMA contraction)."""
+    os.makedirs(BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in SOURCES + [
+        os.path.join(HERE, "gslsub", "include", "gslsub.h"),
+        os.path.join(HERE, "gslsub", "include", "gk_nodes.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-fopenmp",
+                           "-ffp-contract=off", "-std=c11", "-D_GNU_SOURCE",
+                           "-I", os.path.join(HERE, "gslsub", "include"),
+                           *SOURCES, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class Atmos4D(C.Structure):
+    _fields_ = [("logT", C.c_void_p), ("logg", C.c_void_p), ("mu", C.c_void_p),
+                ("logE", C.c_void_p), ("I", C.c_void_p),
+                ("nT", C.c_size_t), ("ng", C.c_size_t), ("nmu", C.c_size_t),
+                ("nE", C.c_size_t)]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(LIB)
+            P = C.c_void_p
+            L.xo_compute_rays.restype = C.c_int
+            L.xo_compute_rays.argtypes = [C.c_int, C.c_size_t, C.c_double, P, P,
+                                          C.c_size_t, P, P, P, P]
+            L.xo_integrate.restype = C.c_int
+            L.xo_integrate.argtypes = [
+                C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P,
+                C.c_size_t, P, P, P, P, P, C.c_size_t, P, C.c_size_t, P,
+                C.c_size_t, P, C.c_int, P, C.c_int, P]
+            L.xo_energy_integrator.restype = None
+            L.xo_energy_integrator.argtypes = [C.c_int, C.c_size_t, C.c_size_t, P,
+                                               P, C.c_size_t, P, P]
+            L.xo_precomputation.restype = None
+            L.xo_precomputation.argtypes = [C.c_size_t, C.c_size_t, P, P]
+            L.xo_eval_marginal_likelihood.restype = C.c_int
+            L.xo_eval_marginal_likelihood.argtypes = [
+                C.c_double, C.c_size_t, P, C.c_size_t, P, C.c_size_t, P, P, P, P,
+                P, P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                P, C.c_double, P, C.c_uint, P, P, P, P]
+            L.xo_lnfact.restype = C.c_double
+            L.xo_lnfact.argtypes = [C.c_uint]
+            _lib = L
+    return _lib
+
+
+def _c(a, dtype=np.float64):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def compute_rays(N_T, N_u, r_s, r_s_over_R, maxAlpha, N_R):
+    """rays.compute_rays (rays.pyx:249-390); maxAlpha is clamped in place."""
+    u = _c(r_s_over_R)
+    assert maxAlpha.dtype == np.float64 and maxAlpha.flags.c_contiguous
+    D = np.empty((N_u, N_R)); CA = np.empty((N_u, N_R)); L = np.empty((N_u, N_R))
+    MD = np.empty(N_u)
+    t = lib().xo_compute_rays(int(N_T), N_u, float(r_s), _p(u), _p(maxAlpha), N_R,
+                              _p(D), _p(CA), _p(L), _p(MD))
+    return t, D, CA, L, MD
+
+
+def _atmos_struct(hot_atmosphere):
+    if not hot_atmosphere:
+        return None, ()
+    keep = tuple(_c(a) for a in hot_atmosphere)
+    s = Atmos4D(*(_p(a).value for a in keep), keep[0].size, keep[1].size,
+                keep[2].size, keep[3].size)
+    return s, keep
+
+
+def integrate(numThreads, R, omega, r_s, inclination, cellArea,
+              radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+              CELL_RADIATES, correction_srcCellParams, numRays, deflection,
+              cos_alpha, lag, maxDeflection, cos_gammaArray, energies, leaves,
+              phases, hot_atmosphere, elsewhere_atmosphere, hot_atm_ext,
+              else_atm_ext, beam_opt, image_order_limit=None, R_in=1e6):
+    """integrator_for_azimuthal_invariance.integrate (:70-665) for the
+    uniform BB / Num4D hot regions the likelihood path uses."""
+    if correction_srcCellParams is not None or beam_opt != 0 or R_in < 1e6:
+        raise NotImplementedError("oracle covers the default hot-region path")
+    A = _c(cellArea); S0, S1 = A.shape
+    par = _c(srcCellParams)
+    rad = _c(CELL_RADIATES, np.int32)
+    E = _c(energies); Lv = _c(leaves); P = _c(phases)
+    out = np.zeros((E.size, P.size))
+    st, keep = _atmos_struct(hot_atmosphere)
+    arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
+            _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
+            _c(cos_gammaArray)]
+    status = lib().xo_integrate(
+        int(numThreads), float(R), float(omega), float(r_s), float(inclination),
+        S0, S1, _p(A), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
+        _p(par), par.shape[2], _p(rad), int(numRays), _p(arrs[4]), _p(arrs[5]),
+        _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
+        P.size, _p(P), int(hot_atm_ext),
+        C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
+        int(image_order_limit or 0), _p(out))
+    del keep
+    if status != 0:
+        return (1, None)
+    return (0, out)
+
+
+def energy_integrator(N_Ts, signal, energies, energy_edges):
+    """tools.energy_integrator (energy_integrator.pyx:27-114)."""
+    S = _c(signal); E = _c(energies); ed = _c(energy_edges)
+    out = np.zeros((ed.size - 1, S.shape[1]))
+    lib().xo_energy_integrator(int(N_Ts), E.size, S.shape[1], _p(S), _p(E), ed.size,
+                               _p(ed), _p(out))
+    return out
+
+
+def precomputation(data):
+    d = _c(data, np.int32)
+    out = np.zeros(d.shape[0])
+    lib().xo_precomputation(d.shape[0], d.shape[1], _p(d), _p(out))
+    return out
+
+
+def eval_marginal_likelihood(exposure_time, phases, counts, components,
+                             component_phases, phase_shifts,
+                             neg_sum_ln_data_factorial, support,
+                             workspace_intervals, epsabs, epsrel, epsilon, sigmas,
+                             llzero, allow_negative=False, slim=20.0,
+                             background=None, seed=12345, return_status=False):
+    """default_background_marginalisation.eval_marginal_likelihood (:450-734)."""
+    ph = _c(phases); cnt = _c(counts)
+    comps = [_c(c) for c in components]
+    cph = [_c(c) for c in component_phases]
+    H = len(comps)
+    K, B = cnt.shape
+    sup = _c(support)
+    if sup.shape[0] != K:
+        raise TypeError('The number of energy channels in the background support '
+                        'does not match to that of the data.')
+    for i in range(K):
+        if sup[i, 1] == 0:
+            raise TypeError('Background upper limit cannot be set to 0.')
+        if sup[i, 1] > 0 and sup[i, 1] - sup[i, 0] < 0:
+            raise TypeError('Background upper limit must be higher than the lower limit.')
+    if isinstance(allow_negative, bool):
+        an = np.full(H, int(allow_negative), dtype=np.int32)
+    else:
+        an = _c([int(x) for x in allow_negative], np.int32)
+    ptrs = (C.c_void_p * H)(*[_p(c).value for c in comps])
+    pptrs = (C.c_void_p * H)(*[_p(c).value for c in cph])
+    nph = np.array([c.shape[1] for c in comps], dtype=np.uint64)
+    sh = _c(phase_shifts)
+    pre = _c(neg_sum_ln_data_factorial)
+    bg = _c(background) if background is not None else None
+    STAR = np.zeros((K, B)); mb = np.zeros(K); mbs = np.zeros(K)
+    ll = C.c_double(0.0)
+    st = lib().xo_eval_marginal_likelihood(
+        float(exposure_time), B, _p(ph), K, _p(cnt), H, C.cast(ptrs, C.c_void_p),
+        _p(nph), C.cast(pptrs, C.c_void_p), _p(sh), _p(pre), _p(sup), float(epsabs),
+        float(epsrel), float(epsilon), float(sigmas), float(llzero), _p(an),
+        float(slim), _p(bg) if bg is not None else None, int(seed), C.byref(ll),
+        _p(STAR), _p(mb), _p(mbs))
+    res = (ll.value, STAR, mb, mbs)
+    return (res, st) if return_status else res

@@ -1,0 +1,844 @@
+/*
+ * xpsi_oracle.c -- CPU restatement of X-PSI's pulse-likelihood path (FP64).
+ *
+ * TEST INFRASTRUCTURE: this is the oracle.  Only tests/, the smoke check and
+ * bench.py's CPU-baseline leg may load it, and only as the checker or the
+ * timed CPU baseline -- never as the product path.  It follows the reference
+ * Cython line by line (citations are file:line in the xpsi source tree) and
+ * uses the oracle's GSL-API subset (gslsub) for splines and quadrature, as
+ * the reference uses GSL.  Parity of this file with the reference modules
+ * (built by build_ref.py) is checked in tests/test_oracle_vs_reference.py
+ * and through the committed golden fixtures.
+ *
+ * Stages:
+ *   xo_compute_rays          cellmesh/rays.pyx:249-390 (+ rayIntegrator :90-247)
+ *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665
+ *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
+ *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
+ *   xo_precomputation        likelihoods/default_background_marginalisation.pyx:38-68
+ *   xo_eval_marginal_likelihood   same file :176-734 and
+ *                            tools/compute_expected_counts.pyx:66-197
+ */
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "gslsub.h"
+
+#define XO_PI 3.14159265358979323846
+static const double kPi = XO_PI;
+static const double kHalfPi = XO_PI / 2.0;
+static const double kTwoPi = 2.0 * XO_PI;
+static const double kC = 2.99792458e8;            /* global_imports.py _c */
+static const double kKeV = 1.60217662e-16;        /* global_imports.py _keV */
+static const double kKB = 1.38064852e-23;         /* global_imports.py _k_B */
+static const double kHKeV = 4.135667662e-18;      /* global_imports.py _h_keV */
+static const double kErg = 1.0e-7;                /* hot_BB.pyx:23 */
+static const double kPlanck = 5.040366110812353e22; /* hot_BB.pyx:24 */
+
+/* tools/core.pyx:118-122 */
+static int are_equal(double x, double y) { return fabs(x - y) < 1.0e-12; }
+
+/* ================================================================== */
+/* rays                                                               */
+/* ================================================================== */
+static const double kBPhotonSphere = 2.598076211353316; /* 3 sqrt(3) / 2, rays.pyx:59 */
+
+/* rays.pyx:53-57 */
+static double image_deflection(int order, double psi) {
+  if (order % 2 != 0)
+    return (double)(order + 1) * kPi + pow(-1.0, (double)order) * psi;
+  return (double)order * kPi + pow(-1.0, (double)order) * psi;
+}
+
+/* rays.pyx:61-88 */
+static double f_in_def(double x, void *p) {
+  double rc = ((double *)p)[0];
+  return 1.0 / sqrt(2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (rc - 1.0));
+}
+static double f_in_lag(double x, void *p) {
+  double rc = ((double *)p)[0];
+  double X = 1.0 / sqrt(2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (rc - 1.0));
+  return X * X / (x + X);
+}
+static double f_out_def(double x, void *p) {
+  double sas = ((double *)p)[0], Rr = ((double *)p)[1];
+  return x / sqrt(1.0 - sas + x * x * sas * (2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (Rr - 1.0)));
+}
+static double f_out_lag(double x, void *p) {
+  double sas = ((double *)p)[0], Rr = ((double *)p)[1];
+  double f = sqrt(1.0 - sas + x * x * sas * (2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (Rr - 1.0)));
+  return x / (f + f * f);
+}
+
+/* rays.pyx:90-247: out[0] = deflection, out[2] = lag (s) */
+static void ray_integrator(gsl_integration_workspace *w, double cos_alpha,
+                           double r_s, double u, double out[4]) {
+  int status = GSL_SUCCESS;
+  double outp[2], inp[1];
+  gsl_function fd, fl;
+  double sas = 1.0 - cos_alpha * cos_alpha;
+  double sa = sqrt(sas);
+  double alpha = acos(cos_alpha);
+  double b = sa / (u * sqrt(1.0 - u));
+  if (b <= kBPhotonSphere) {
+    outp[0] = sas;
+    outp[1] = 1.0 / u;
+    fd.function = f_out_def; fd.params = outp;
+    fl.function = f_out_lag; fl.params = outp;
+    status = gsl_integration_qag(&fd, 0.0, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &out[0], &out[1]);
+    if (status == GSL_EFAILED) out[0] = NAN;
+    if (status != GSL_EFAILED) {
+      status = gsl_integration_qag(&fl, 0.0, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &out[2], &out[3]);
+      if (status == GSL_EFAILED) out[0] = NAN;
+    }
+    if (status != GSL_EFAILED) {
+      out[0] *= 2.0 * b * u;
+      out[2] *= 2.0 * b * b * u * r_s;
+    }
+  } else if (alpha <= kPi / 2.0) {
+    double rc, wR;
+    if (are_equal(sa, 1.0)) {
+      rc = 1.0 / u;
+      wR = 0.0;
+    } else {
+      rc = 2.0 * b * cos((atan(sqrt(4.0 * b * b / 27.0 - 1.0)) - kPi) / 3.0) / sqrt(3.0);
+      wR = sqrt(1.0 - rc * u);
+    }
+    inp[0] = rc;
+    fd.function = f_in_def; fd.params = inp;
+    fl.function = f_in_lag; fl.params = inp;
+    if (isnan(wR)) wR = 0.0;
+    status = gsl_integration_qag(&fd, wR, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &out[0], &out[1]);
+    if (status == GSL_EFAILED) out[0] = NAN;
+    if (status != GSL_EFAILED) {
+      status = gsl_integration_qag(&fl, wR, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &out[2], &out[3]);
+      if (status == GSL_EFAILED) out[0] = NAN;
+    }
+    if (status != GSL_EFAILED) {
+      out[0] *= 2.0 * b / rc;
+      out[2] *= 2.0 * b * b * r_s / rc;
+    }
+  } else if (alpha > kPi / 2.0) {
+    double dd[2], dl[2], e;
+    double rc = 2.0 * b * cos((atan(sqrt(4.0 * b * b / 27.0 - 1.0)) - kPi) / 3.0) / sqrt(3.0);
+    inp[0] = rc;
+    fd.function = f_in_def; fd.params = inp;
+    fl.function = f_in_lag; fl.params = inp;
+    double wR = sqrt(1.0 - rc * u);
+    if (isnan(wR)) wR = 0.0;
+    status = gsl_integration_qag(&fd, 0.0, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &dd[1], &e);
+    if (status == GSL_EFAILED) out[0] = NAN;
+    if (status != GSL_EFAILED) {
+      status = gsl_integration_qag(&fd, wR, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &dd[0], &e);
+      if (status == GSL_EFAILED) out[0] = NAN;
+    }
+    if (status != GSL_EFAILED) {
+      status = gsl_integration_qag(&fl, 0.0, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &dl[1], &e);
+      if (status == GSL_EFAILED) out[0] = NAN;
+    }
+    if (status != GSL_EFAILED) {
+      status = gsl_integration_qag(&fl, wR, 1.0, 0, 1.0e-12, 100, GSL_INTEG_GAUSS61, w, &dl[0], &e);
+      if (status == GSL_EFAILED) out[0] = NAN;
+    }
+    if (status != GSL_EFAILED) {
+      out[0] = 2.0 * b * (2.0 * dd[1] - dd[0]) / rc;
+      out[2] = 2.0 * b * b * r_s * (2.0 * dl[1] - dl[0]) / rc;
+      double cor = 1.0 / u - rc + log((1.0 / u - 1.0) / (rc - 1.0));
+      out[2] += 2.0 * r_s * cor;
+    }
+  }
+  if (status != GSL_EFAILED) out[2] /= kC;
+}
+
+/* rays.pyx:249-390.  Rows are independent; the NaN-repair counter is kept
+ * per row (the reference keeps it per OpenMP thread, which is equivalent
+ * whenever a row finishes without a fatal flag). */
+int xo_compute_rays(int n_threads, size_t N_u, double r_s,
+                    const double *u_arr, double *maxAlpha, size_t N_R,
+                    double *deflection, double *cos_alpha, double *lag,
+                    double *maxDeflection) {
+  int terminate = 0;
+  gsl_error_handler_t *prev = gsl_set_error_handler_off();
+  const double eps = 1.0e-8;
+#pragma omp parallel num_threads(n_threads > 0 ? n_threads : 1) reduction(| : terminate)
+  {
+    gsl_integration_workspace *w = gsl_integration_workspace_alloc(100);
+    int term = 0;
+#pragma omp for schedule(static, 1)
+    for (long ii = 0; ii < (long)N_u; ii++) {
+      size_t i = (size_t)ii;
+      double u = u_arr[i], extreme = 0.0;
+      double *D = deflection + i * N_R, *CA = cos_alpha + i * N_R, *L = lag + i * N_R;
+      size_t icount = 0, iidx = 0;
+      if (u < 2.0 / 3.0)
+        extreme = kPi - asin(sqrt(1.0 - u) * kBPhotonSphere * u);
+      else if (are_equal(u, 2.0 / 3.0))
+        extreme = kPi / 2.0;
+      else if (2.0 / 3.0 < u && u < 1.0)
+        extreme = asin(sqrt(1.0 - u) * kBPhotonSphere * u);
+      if (maxAlpha[i] >= (1.0 - eps) * extreme) maxAlpha[i] = (1.0 - eps) * extreme;
+      double inc = (1.0 - cos(maxAlpha[i])) / ((double)N_R - 1.0);
+      for (size_t j = 0; j < N_R; j++) {
+        CA[j] = 1.0 - (double)j * inc;
+        if (j == 0) {
+          CA[j] = 1.0;
+          D[j] = 0.0;
+          L[j] = 0.0;
+          continue;
+        }
+        if (term) continue;
+        double rp[4] = {0, 0, 0, 0};
+        ray_integrator(w, CA[j], r_s, u, rp);
+        if (j == N_R - 1 && (isnan(rp[0]) || rp[0] <= D[j - 1])) {
+          term = 1;
+        } else if (icount > 0 && !isnan(rp[0]) && 0.0 <= rp[0] && rp[0] < 100.0 * kPi &&
+                   rp[0] > D[iidx]) {
+          D[j] = rp[0];
+          L[j] = rp[2];
+          double delta = (double)icount + 1.0;
+          for (size_t k = 1; k <= icount; k++) {
+            D[iidx + k] = D[j] * (double)k;
+            D[iidx + k] += D[iidx] * (delta - (double)k);
+            D[iidx + k] /= delta;
+            L[iidx + k] = L[j] * (double)k;
+            L[iidx + k] += L[iidx] * (delta - (double)k);
+            L[iidx + k] /= delta;
+          }
+          icount = 0;
+        } else if (isnan(rp[0]) || rp[0] < 0.0 || rp[0] > 100.0 * kPi) {
+          if (icount == 0) iidx = j - 1;
+          icount++;
+        } else {
+          D[j] = rp[0];
+          L[j] = rp[2];
+        }
+      }
+      maxDeflection[i] = D[N_R - 1];
+    }
+    if (term) terminate = 1;
+    gsl_integration_workspace_free(w);
+  }
+  gsl_set_error_handler(prev);
+  return terminate;
+}
+
+/* ================================================================== */
+/* atmospheres                                                        */
+/* ================================================================== */
+typedef struct {
+  /* numerical 4-D table, dims (logT, logg, mu, log10(E/kT)), row major */
+  const double *logT, *logg, *mu, *logE, *I;
+  size_t nT, ng, nmu, nE;
+} xo_atmos4d;
+
+/* hot_BB.pyx:54-82 (times the norm :84-98 applied by the caller) */
+static double eval_bb(double E, const double *vec) {
+  double temp = (kKB / kKeV) * pow(10.0, vec[0]);
+  return E * E * E / (exp(E / temp) - 1.0);
+}
+
+/* Per-thread state of the reference's Num4D evaluator
+ * (hot_Num4D.pyx:66-199, ACCELERATE): the base node of each dimension's
+ * 4-point stencil persists between calls.  The evaluator only moves a base
+ * node when the query leaves the stencil's central interval, and it clamps an
+ * out-of-table query only on the call that moves the node, so its output for
+ * out-of-range arguments depends on the call history.  The oracle keeps that
+ * state exactly as the reference does (one state per OpenMP thread, reset at
+ * every integrator call). */
+typedef struct {
+  size_t BN[4];
+  double node[8];
+} num4d_state;
+
+static void num4d_reset(num4d_state *st, const xo_atmos4d *A) {
+  const double *g[4] = {A->logT, A->logg, A->mu, A->logE};
+  for (int d = 0; d < 4; d++) {
+    st->BN[d] = 0;
+    st->node[2 * d] = g[d][1];
+    st->node[2 * d + 1] = g[d][2];
+  }
+}
+
+/* hot_Num4D.pyx:248-439 */
+static double eval_num4d(const xo_atmos4d *A, num4d_state *st, double E,
+                         double mu, const double *vec) {
+  double v[4];
+  double E_eff = (kKB / kKeV) * pow(10.0, vec[0]);
+  v[0] = vec[0];
+  v[1] = vec[1];
+  v[2] = mu;
+  v[3] = log10(E / E_eff);
+  const double *g[4] = {A->logT, A->logg, A->mu, A->logE};
+  size_t n[4] = {A->nT, A->ng, A->nmu, A->nE};
+  size_t *BN = st->BN;
+  double *node = st->node;
+  for (int i = 0; i < 4; i++) {
+    const double *P = g[i];
+    if (v[i] < node[2 * i] && BN[i] != 0) {
+      while (v[i] < P[BN[i] + 1]) {
+        if (BN[i] > 0) BN[i] -= 1;
+        else if (v[i] <= P[0]) { v[i] = P[0]; break; }
+        else break;
+      }
+      node[2 * i] = P[BN[i] + 1];
+      node[2 * i + 1] = P[BN[i] + 2];
+    } else if (v[i] > node[2 * i + 1] && BN[i] != n[i] - 4) {
+      while (v[i] > P[BN[i] + 2]) {
+        if (BN[i] < n[i] - 4) BN[i] += 1;
+        else if (v[i] >= P[n[i] - 1]) { v[i] = P[n[i] - 1]; break; }
+        else break;
+      }
+      node[2 * i] = P[BN[i] + 1];
+      node[2 * i + 1] = P[BN[i] + 2];
+    }
+  }
+  double w[4][4];
+  for (int d = 0; d < 4; d++) {
+    const double *P = g[d];
+    size_t b = BN[d];
+    double x = v[d];
+    double d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
+    double d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
+    double d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
+    double d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
+    double s0 = 1.0 / (P[b] - P[b + 1]); s0 /= P[b] - P[b + 2]; s0 /= P[b] - P[b + 3];
+    double s1 = 1.0 / (P[b + 1] - P[b]); s1 /= P[b + 1] - P[b + 2]; s1 /= P[b + 1] - P[b + 3];
+    double s2 = 1.0 / (P[b + 2] - P[b]); s2 /= P[b + 2] - P[b + 1]; s2 /= P[b + 2] - P[b + 3];
+    double s3 = 1.0 / (P[b + 3] - P[b]); s3 /= P[b + 3] - P[b + 1]; s3 /= P[b + 3] - P[b + 2];
+    w[d][0] = d0 * s0; w[d][1] = d1 * s1; w[d][2] = d2 * s2; w[d][3] = d3 * s3;
+  }
+  size_t S0 = A->ng * A->nmu * A->nE, S1 = A->nmu * A->nE, S2 = A->nE;
+  double I = 0.0;
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++)
+      for (int k = 0; k < 4; k++)
+        for (int l = 0; l < 4; l++) {
+          double t = w[0][i] * w[1][j] * w[2][k] * w[3][l];
+          I += t * A->I[(BN[0] + i) * S0 + (BN[1] + j) * S1 + (BN[2] + k) * S2 + BN[3] + l];
+        }
+  if (I < 0.0) return 0.0;
+  return I * pow(10.0, 3.0 * v[0]);
+}
+
+/* ================================================================== */
+/* cell-mesh integrator, azimuthal invariance                         */
+/* ================================================================== */
+int xo_integrate(int n_threads, double R, double omega, double r_s,
+                 double inclination, size_t S0, size_t S1,
+                 const double *cellArea, const double *radius_arr,
+                 const double *u_arr, const double *theta, const double *phi,
+                 const double *srcCellParams, size_t n_params,
+                 const int *radiates, size_t N_R, const double *deflection,
+                 const double *cos_alpha, const double *lag,
+                 const double *maxDeflection, const double *cos_gammaArray,
+                 size_t N_E, const double *energies, size_t N_L,
+                 const double *leaves, size_t N_P, const double *phases,
+                 int atm_ext, const xo_atmos4d *atmos, int image_order_limit,
+                 double *flux) {
+  (void)R;
+  const double sin_i = sin(inclination), cos_i = cos(inclination);
+  const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
+  const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
+  int nt = n_threads > 0 ? n_threads : 1;
+  int terminate_any = 0;
+  double *priv = (double *)calloc((size_t)nt * N_E * N_P, sizeof(double));
+  /* integrator_for_azimuthal_invariance.pyx:213-226 */
+  double *cos_defl = (double *)malloc(S0 * N_R * sizeof(double));
+  double *ca_alt = (double *)malloc(S0 * N_R * sizeof(double));
+  for (size_t i = 0; i < S0; i++)
+    for (size_t j = 0; j < N_R; j++) {
+      cos_defl[i * N_R + j] = cos(deflection[i * N_R + N_R - j - 1]);
+      ca_alt[i * N_R + j] = cos_alpha[i * N_R + N_R - j - 1];
+    }
+  gsl_error_handler_t *prev = gsl_set_error_handler_off();
+
+#pragma omp parallel num_threads(nt) reduction(| : terminate_any)
+  {
+    int T = 0;
+#ifdef _OPENMP
+    T = omp_get_thread_num();
+#endif
+    double *pflux = priv + (size_t)T * N_E * N_P;
+    gsl_interp_accel *acc_a = gsl_interp_accel_alloc(), *acc_alt = gsl_interp_accel_alloc();
+    gsl_interp_accel *acc_l = gsl_interp_accel_alloc(), *acc_p = gsl_interp_accel_alloc();
+    gsl_interp *ia = gsl_interp_alloc(gsl_interp_steffen, N_R);
+    gsl_interp *il = gsl_interp_alloc(gsl_interp_steffen, N_R);
+    gsl_interp *ip = gsl_interp_alloc(gsl_interp_akima_periodic, N_L);
+    double *PHASE = (double *)malloc(N_L * sizeof(double));
+    double *PROFILE = (double *)malloc(N_E * N_L * sizeof(double));
+    num4d_state nst;
+    if (atm_ext == 2) num4d_reset(&nst, atmos);
+    int terminate = 0;
+#pragma omp for schedule(static, 1)
+    for (long ii = 0; ii < (long)S0; ii++) {
+      size_t i = (size_t)ii, J = 0, j;
+      if (terminate) continue;
+      for (j = 0; j < S1; j++)
+        if (radiates[i * S1 + j] == 1) { J = j; break; }
+      if (j == S1) continue;
+      const double *defl = deflection + i * N_R;
+      gsl_interp_accel_reset(acc_a);
+      gsl_interp_accel_reset(acc_l);
+      j = 0;
+      while (defl[j] <= kHalfPi) j++;
+      const double *xalt = cos_defl + i * N_R + (N_R - j - 1);
+      const double *yalt = ca_alt + i * N_R + (N_R - j - 1);
+      gsl_interp *ialt = gsl_interp_alloc(gsl_interp_steffen, j + 1);
+      gsl_interp_init(ialt, xalt, yalt, j + 1);
+      gsl_interp_accel_reset(acc_alt);
+      gsl_interp_init(ia, defl, cos_alpha + i * N_R, N_R);
+      gsl_interp_init(il, defl, lag + i * N_R, N_R);
+      const double *ya = cos_alpha + i * N_R, *yl = lag + i * N_R;
+
+      double radius = radius_arr[i];
+      double Grav_z = sqrt(1.0 - u_arr[i]);
+      double cos_gamma = cos_gammaArray[i];
+      double sin_gamma = sqrt(1.0 - cos_gamma * cos_gamma);
+      double cos_th = cos(theta[i * S1]), sin_th = sin(theta[i * S1]);
+      double th_over_pi = theta[i * S1] / kPi;
+      double beta = radius * omega * sin_th / (kC * Grav_z);
+      double Lorentz = sqrt(1.0 - beta * beta);
+      double cos_a = -1.0, deriv = -1.0;
+      int IO = image_order_limit > 0 ? image_order_limit
+                                     : (int)ceil(maxDeflection[i] / kPi);
+      const double *VEC = srcCellParams + (i * S1 + J) * n_params;
+      for (int I = 0; I < IO; I++) {
+        int InvisFlag = 2, CalcRays = 0;
+        size_t InvisPhase = 0;
+        double InvisStep;
+        for (size_t k = 0; k < leaf_lim; k++) {
+          double cos_psi = cos_i * cos_th + sin_i * sin_th * cos(leaves[k]);
+          double psi = image_deflection(I, acos(cos_psi));
+          double sin_psi = sin(psi);
+          if (!are_equal(psi, 0.0) && are_equal(sin_psi, 0.0)) {
+            double _i = (cos_i >= 0.0) ? inclination + inclination * 1.0e-6
+                                       : inclination - inclination * 1.0e-6;
+            cos_psi = cos(_i) * cos_th + sin(_i) * sin_th * cos(leaves[k]);
+            psi = image_deflection(I, acos(cos_psi));
+            sin_psi = sin(psi);
+          }
+          double sin_alpha = 0.0, mu = 0.0;
+          if (psi <= maxDeflection[i]) {
+            if (psi < ia->xmin || psi > ia->xmax) { terminate = 1; break; }
+            if (psi <= kHalfPi && cos_psi >= ialt->xmin)
+              cos_a = gsl_interp_eval(ialt, xalt, yalt, cos_psi, acc_alt);
+            else
+              cos_a = gsl_interp_eval(ia, defl, ya, psi, acc_a);
+            sin_alpha = sqrt(1.0 - cos_a * cos_a);
+            mu = cos_a * cos_gamma;
+            if (!are_equal(psi, 0.0)) {
+              double cos_delta = (cos_i - cos_th * cos_psi) / (sin_th * sin_psi);
+              if (th_over_pi < 0.5) mu = mu + sin_alpha * sin_gamma * cos_delta;
+              else mu = mu - sin_alpha * sin_gamma * cos_delta;
+            }
+            CalcRays = (mu > 0.0) ? 1 : 0; /* R_in = 1e6: no disk */
+          } else {
+            CalcRays = 0;
+          }
+          if (CalcRays == 1) {
+            if (psi <= kHalfPi && cos_psi >= ialt->xmin) {
+              deriv = gsl_interp_eval_deriv(ialt, xalt, yalt, cos_psi, acc_alt);
+            } else {
+              deriv = gsl_interp_eval_deriv(ia, defl, ya, psi, acc_a);
+              deriv = exp(log(fabs(deriv)) - log(fabs(sin_psi)));
+            }
+            if (psi < il->xmin || psi > il->xmax) { terminate = 1; break; }
+            double plag = gsl_interp_eval(il, defl, yl, psi, acc_l);
+            for (int ks = 0; ks < 2; ks++) {
+              if ((0 < k && k < leaf_lim - 1) || (k == 0 && ks == 0) ||
+                  (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
+                  (k == leaf_lim - 1 && N_L % 2 == 0)) {
+                size_t kdx = (ks == 0) ? k : N_L - 1 - k;
+                double superlum, eta;
+                if (!are_equal(psi, 0.0)) {
+                  double cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
+                  superlum = 1.0 + beta * cos_xi;
+                  eta = Lorentz / superlum;
+                } else {
+                  superlum = 1.0;
+                  eta = Lorentz;
+                }
+                double Z = eta * Grav_z;
+                double ABB = mu * eta;
+                double GEOM = mu * fabs(deriv) * Grav_z * eta * eta * eta / superlum;
+                PHASE[kdx] = leaves[kdx] + plag;
+                for (size_t p = 0; p < N_E; p++) {
+                  double Ep = energies[p] / Z;
+                  double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
+                                              : eval_bb(Ep, VEC);
+                  PROFILE[p * N_L + kdx] = (I_E * norm - 0.0) * GEOM;
+                }
+              }
+            }
+            if (k == 0) {
+              PHASE[N_L - 1] = PHASE[0] + kTwoPi;
+              for (size_t p = 0; p < N_E; p++) PROFILE[p * N_L + N_L - 1] = PROFILE[p * N_L];
+            } else if (k > 0 && InvisFlag == 2) {
+              InvisStep = leaves[k] / (double)k;
+              for (size_t m = N_L - k; m < N_L; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
+              for (size_t p = 0; p < N_E; p++)
+                for (size_t m = N_L - k; m < N_L; m++) PROFILE[p * N_L + m] = 0.0;
+              PHASE[0] = PHASE[N_L - 1] - kTwoPi;
+              for (size_t m = 1; m < k; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
+              for (size_t p = 0; p < N_E; p++) {
+                PROFILE[p * N_L] = 0.0;
+                for (size_t m = 1; m < k; m++) PROFILE[p * N_L + m] = 0.0;
+              }
+            } else if (InvisFlag == 1) {
+              InvisStep = PHASE[k] - PHASE[InvisPhase - 1];
+              InvisStep = InvisStep / (double)(k - InvisPhase + 1);
+              for (size_t m = InvisPhase; m < k; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
+              InvisStep = PHASE[N_L - InvisPhase] - PHASE[N_L - 1 - k];
+              InvisStep = InvisStep / (double)(k - InvisPhase + 1);
+              for (size_t m = N_L - k; m < N_L - InvisPhase; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
+            }
+            InvisFlag = 0;
+          } else {
+            if (InvisFlag == 0) {
+              InvisStep = PHASE[N_L - k] - PHASE[k - 1];
+              InvisStep = InvisStep / (double)(N_L - 2 * k + 1);
+              for (size_t m = k; m < N_L - k; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
+              for (size_t p = 0; p < N_E; p++)
+                for (size_t m = k; m < N_L - k; m++) PROFILE[p * N_L + m] = 0.0;
+              InvisFlag = 1;
+              InvisPhase = k;
+            }
+          }
+        }
+        if (terminate) break;
+        if (InvisFlag == 2) break;
+        for (size_t m = 1; m < N_L; m++)
+          if (PHASE[m] <= PHASE[m - 1]) { terminate = 1; break; }
+        if (terminate) break;
+        for (size_t p = 0; p < N_E && !terminate; p++) {
+          const double *prof = PROFILE + p * N_L;
+          gsl_interp_accel_reset(acc_p);
+          gsl_interp_init(ip, PHASE, prof, N_L);
+          for (j = 0; j < S1 && !terminate; j++) {
+            if (radiates[i * S1 + j] != 1) continue;
+            double shift = phi[i * S1 + j];
+            double A = cellArea[i * S1 + j];
+            for (size_t k = 0; k < N_P; k++) {
+              double x = phases[k] + shift;
+              if (x > PHASE[N_L - 1]) {
+                while (x > PHASE[N_L - 1]) x = x - kTwoPi;
+              } else if (x < PHASE[0]) {
+                while (x < PHASE[0]) x = x + kTwoPi;
+              }
+              if (x < ip->xmin || x > ip->xmax) { terminate = 1; break; }
+              double s = gsl_interp_eval(ip, PHASE, prof, x, acc_p);
+              if (s > 0.0) pflux[p * N_P + k] += A * s;
+            }
+          }
+        }
+        if (terminate) break;
+      }
+      gsl_interp_free(ialt);
+    }
+    if (terminate) terminate_any = 1;
+    gsl_interp_free(ia); gsl_interp_free(il); gsl_interp_free(ip);
+    gsl_interp_accel_free(acc_a); gsl_interp_accel_free(acc_alt);
+    gsl_interp_accel_free(acc_l); gsl_interp_accel_free(acc_p);
+    free(PHASE); free(PROFILE);
+  }
+  gsl_set_error_handler(prev);
+  /* :605-612 */
+  for (size_t p = 0; p < N_E; p++)
+    for (size_t k = 0; k < N_P; k++) {
+      double s = 0.0;
+      for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_E * N_P + p * N_P + k];
+      flux[p * N_P + k] = s / (energies[p] * kKeV);
+    }
+  free(priv); free(cos_defl); free(ca_alt);
+  return terminate_any ? 1 : 0;
+}
+
+/* ================================================================== */
+/* energy integrator: tools/energy_integrator.pyx:27-114              */
+/* out[n_edges-1][N_P] (the reference returns binned.T)               */
+/* ================================================================== */
+void xo_energy_integrator(int n_threads, size_t N_E, size_t N_P,
+                          const double *signal, const double *logE,
+                          size_t n_edges, const double *logEdges, double *out) {
+  const double maxE = logE[N_E - 1];
+  memset(out, 0, (n_edges - 1) * N_P * sizeof(double));
+#pragma omp parallel num_threads(n_threads > 0 ? n_threads : 1)
+  {
+    gsl_interp *ip = gsl_interp_alloc(gsl_interp_akima_periodic, N_E);
+    gsl_interp_accel *acc = gsl_interp_accel_alloc();
+    double *cpy = (double *)malloc(N_E * sizeof(double));
+#pragma omp for schedule(static, 1)
+    for (long ii = 0; ii < (long)N_P; ii++) {
+      size_t i = (size_t)ii;
+      for (size_t j = 0; j < N_E; j++) cpy[j] = pow(10.0, logE[j]) * signal[j * N_P + i] * log(10.0);
+      gsl_interp_accel_reset(acc);
+      gsl_interp_init(ip, logE, cpy, N_E);
+      for (size_t j = 0; j + 1 < n_edges; j++) {
+        double up = logEdges[j + 1] > maxE ? maxE : logEdges[j + 1];
+        out[j * N_P + i] = gsl_interp_eval_integ(ip, logE, cpy, logEdges[j], up, acc);
+        if (logEdges[j + 1] > maxE) break;
+      }
+    }
+    free(cpy);
+    gsl_interp_accel_free(acc);
+    gsl_interp_free(ip);
+  }
+}
+
+/* ================================================================== */
+/* background-marginalised Poisson likelihood                          */
+/* ================================================================== */
+/* default_background_marginalisation.pyx:38-68 */
+void xo_precomputation(size_t K, size_t B, const int *counts, double *out) {
+  for (size_t i = 0; i < K; i++) {
+    double s = 0.0;
+    for (size_t j = 0; j < B; j++) s += gsl_sf_lnfact((unsigned)counts[i * B + j]);
+    out[i] = -s;
+  }
+}
+
+typedef struct {
+  size_t n;
+  double SCALE, T_exp, A, std;
+  const double *data;
+  double *star;
+} marg_args;
+
+/* :84-138 */
+static double marginal_integrand(double B, void *params) {
+  marg_args *a = (marg_args *)params;
+  double x = 0.0;
+  for (size_t j = 0; j < a->n; j++) {
+    double c = a->SCALE * (a->star[j] + B);
+    if (c > 0.0) x += a->data[j] * log(c) - c;
+    else if (are_equal(c, 0.0) && are_equal(a->data[j], 0.0)) {}
+    else return 0.0;
+  }
+  return exp(x - a->A);
+}
+
+/* :140-173 */
+static double newton_delta(double B, marg_args *a) {
+  double x = 0.0, y = 0.0;
+  for (size_t j = 0; j < a->n; j++) {
+    y += a->data[j] / (a->star[j] + B);
+    x += a->data[j] / pow(a->star[j] + B, 2.0);
+  }
+  y = 2.0 * a->T_exp - 2.0 * y;
+  x *= 2.0;
+  a->std = sqrt(2.0 / x);
+  return -1.0 * y / x;
+}
+
+/* :176-447; returns 1 on success, 0 when the integral vanished (LOGLIKE
+ * then holds the llzero draw, the caller stops) */
+static int channel_marginal(marg_args *a, double precomp_i, double *LOGLIKE,
+                            double av_DATA, double av_STAR, double epsabs,
+                            double epsrel, double epsilon, double sigmas,
+                            double llzero, const double *support,
+                            double *mcl_bg, double *mcl_bg_s,
+                            gsl_integration_cquad_workspace *w,
+                            unsigned *rng_state) {
+  double T = a->T_exp, B, lower, upper;
+  if (are_equal(av_DATA, 0.0) && are_equal(av_STAR, 0.0)) {
+    lower = 0.0;
+    if (lower < support[0]) lower = support[0];
+    upper = 10.0 / T;
+    if (upper > support[1] && support[1] > 0.0) upper = support[1];
+    B = 0.0;
+    LOGLIKE[0] += log((exp(-1.0 * lower * T) - exp(-1.0 * upper * T)) / T);
+  } else {
+    double B_min = 0.0;
+    B = av_DATA - av_STAR;
+    if (B <= B_min) {
+      double min_counts = -1.0;
+      for (size_t j = 0; j < a->n; j++)
+        if (are_equal(a->star[j], 0.0)) { min_counts = -2.0; break; }
+      if (are_equal(min_counts, -2.0)) {
+        for (size_t j = 0; j < a->n; j++)
+          if ((are_equal(min_counts, -2.0) && a->data[j] > 0.0) ||
+              (0.0 < a->data[j] && a->data[j] < min_counts))
+            min_counts = a->data[j];
+      }
+      if (!are_equal(min_counts, -1.0)) {
+        if (are_equal(min_counts, -2.0)) { B = 0.0; B_min = 0.0; }
+        else { B = 0.01 * min_counts / a->SCALE; B_min = 0.1 * B; }
+      } else {
+        B = B_min;
+      }
+    }
+    double dB = newton_delta(B, a);
+    int counter = 0;
+    while (fabs(dB) > epsilon * a->std && counter < 2) {
+      B += dB;
+      if (B < B_min) {
+        if (B_min > 0.0) counter += 1;
+        else counter = 2;
+        B = B_min;
+      }
+      dB = newton_delta(B, a);
+    }
+    double std_est = 0.0;
+    for (size_t j = 0; j < a->n; j++) std_est += a->data[j] / pow(a->star[j] + B, 2.0);
+    if (std_est > 0.0) std_est = sqrt(1.0 / std_est);
+    else std_est = 1e90;
+    lower = B - sigmas * std_est;
+    upper = B + sigmas * std_est;
+    if (lower < B_min) lower = B_min;
+    double Bi = B;
+    if (lower < support[0]) {
+      lower = support[0];
+      if (upper < support[0] && support[1] > 0.0) { upper = support[1]; Bi = support[0]; }
+      else if (upper < support[0]) { upper = support[0] + sigmas * std_est; Bi = support[0]; }
+    }
+    if (upper > support[1] && support[1] > 0.0) {
+      upper = support[1];
+      if (lower > support[1]) { lower = support[0]; Bi = support[1]; }
+    }
+    if (Bi < lower) Bi = lower;
+    else if (Bi > upper) Bi = upper;
+    a->A = 0.0;
+    for (size_t j = 0; j < a->n; j++) {
+      double c = a->SCALE * (a->star[j] + Bi);
+      if (c > 0.0) a->A += a->data[j] * log(c) - c;
+      else if (are_equal(c, 0.0) && are_equal(a->data[j], 0.0)) {}
+      else a->A += llzero;
+    }
+    gsl_function f;
+    f.function = marginal_integrand;
+    f.params = a;
+    double result, abserr;
+    size_t nev;
+    gsl_integration_cquad(&f, lower, upper, epsabs, epsrel, w, &result, &abserr, &nev);
+    if (result > 0.0) {
+      LOGLIKE[0] += log(result) + a->A + precomp_i;
+    } else {
+      *rng_state = *rng_state * 1103515245u + 12345u;
+      LOGLIKE[0] = llzero * (0.1 + 0.9 * ((*rng_state >> 8) & 0xffffff) / 16777215.0);
+      return 0;
+    }
+  }
+  mcl_bg[0] = B * T;
+  if (B < support[0]) B = support[0];
+  else if (B > support[1] && support[1] > 0.0) B = support[1];
+  mcl_bg_s[0] = B * T;
+  for (size_t j = 0; j < a->n; j++) a->star[j] = a->SCALE * (a->star[j] + B);
+  return 1;
+}
+
+/* compute_expected_counts.pyx:66-197 for one channel */
+static void star_rate_channel(size_t B, const double *phase_edges, size_t H,
+                              const double *const *components,
+                              const size_t *n_phase,
+                              const double *const *component_phases,
+                              const double *shifts, gsl_interp **ip,
+                              gsl_interp_accel **acc, double *STAR,
+                              size_t channel, const int *allow_negative) {
+  for (size_t p = 0; p < H; p++) {
+    size_t np = n_phase[p];
+    const double *pulse = components[p] + channel * np;
+    if (np > 1) {
+      gsl_interp_init(ip[p], component_phases[p], pulse, np);
+      for (size_t j = 0; j < B; j++) {
+        double pa = phase_edges[j] + shifts[p];
+        double pb = phase_edges[j + 1] + shifts[p];
+        if (are_equal(pb - pa, 1.0)) { pa = 0.0; pb = 1.0; }
+        else { pa -= floor(pa); pb -= floor(pb); }
+        double v;
+        if (pa < pb) {
+          v = gsl_interp_eval_integ(ip[p], component_phases[p], pulse, pa, pb, acc[p]);
+          if (v > 0.0 || allow_negative[p] == 1) STAR[j] += v;
+        } else {
+          v = gsl_interp_eval_integ(ip[p], component_phases[p], pulse, pa, 1.0, acc[p]);
+          if (v > 0.0 || allow_negative[p] == 1) STAR[j] += v;
+          v = gsl_interp_eval_integ(ip[p], component_phases[p], pulse, 0.0, pb, acc[p]);
+          if (v > 0.0 || allow_negative[p] == 1) STAR[j] += v;
+        }
+      }
+    } else {
+      STAR[0] = pulse[0];
+    }
+  }
+  for (size_t j = 0; j < B; j++)
+    if (STAR[j] < 0.0) STAR[j] = 0.0;
+}
+
+/* default_background_marginalisation.pyx:450-734.  Returns 0 normally,
+ * 1 when the slim cut fired, 2 when a channel integral vanished. */
+int xo_eval_marginal_likelihood(
+    double exposure_time, size_t B, const double *phase_edges, size_t K,
+    const double *counts, size_t H, const double *const *components,
+    const size_t *n_phase, const double *const *component_phases,
+    const double *shifts, const double *precomp, const double *support,
+    double epsabs, double epsrel, double epsilon, double sigmas,
+    double llzero, const int *allow_negative, double slim,
+    const double *background, unsigned rng_seed, double *loglike,
+    double *STAR, double *mcl_bg, double *mcl_bg_s) {
+  double n = (double)B;
+  double SCALE = exposure_time / n;
+  double LOGLIKE = 0.0;
+  int status = 0;
+  unsigned rng = rng_seed;
+  gsl_interp **ip = (gsl_interp **)calloc(H, sizeof(gsl_interp *));
+  gsl_interp_accel **acc = (gsl_interp_accel **)calloc(H, sizeof(gsl_interp_accel *));
+  for (size_t p = 0; p < H; p++) {
+    if (n_phase[p] > 1) {
+      ip[p] = gsl_interp_alloc(gsl_interp_akima_periodic, n_phase[p]);
+      acc[p] = gsl_interp_accel_alloc();
+    }
+  }
+  gsl_integration_cquad_workspace *w = gsl_integration_cquad_workspace_alloc(1000);
+  memset(STAR, 0, K * B * sizeof(double));
+  memset(mcl_bg, 0, K * sizeof(double));
+  memset(mcl_bg_s, 0, K * sizeof(double));
+  marg_args a;
+  a.n = B;
+  a.SCALE = SCALE;
+  a.T_exp = exposure_time;
+  for (size_t i = 0; i < K; i++) {
+    double *row = STAR + i * B;
+    star_rate_channel(B, phase_edges, H, components, n_phase, component_phases,
+                      shifts, ip, acc, row, i, allow_negative);
+    double av_DATA = 0.0, av_STAR = 0.0;
+    for (size_t j = 0; j < B; j++) {
+      if (background) row[j] += background[i * B + j];
+      row[j] *= n;
+      av_STAR += row[j];
+      av_DATA += counts[i * B + j];
+    }
+    if (slim >= 0.0) {
+      double limit = av_STAR * SCALE - slim * sqrt(av_STAR * SCALE) - av_DATA;
+      if (limit > 0.0) {
+        rng = rng * 1103515245u + 12345u;
+        LOGLIKE = llzero * (0.1 + 0.9 * ((rng >> 8) & 0xffffff) / 16777215.0);
+        status = 1;
+        break;
+      }
+    }
+    av_STAR /= n;
+    av_DATA /= exposure_time;
+    a.data = counts + i * B;
+    a.star = row;
+    int out = channel_marginal(&a, precomp[i], &LOGLIKE, av_DATA, av_STAR, epsabs,
+                               epsrel, epsilon, sigmas, llzero, support + 2 * i,
+                               mcl_bg + i, mcl_bg_s + i, w, &rng);
+    if (out == 0) { status = 2; break; }
+  }
+  for (size_t p = 0; p < H; p++) {
+    if (ip[p]) gsl_interp_free(ip[p]);
+    if (acc[p]) gsl_interp_accel_free(acc[p]);
+  }
+  free(ip); free(acc);
+  gsl_integration_cquad_workspace_free(w);
+  *loglike = LOGLIKE;
+  return status;
+}
+
+/* ---- oracle-side exposure of the quadrature subset for tests ---- */
+double xo_lnfact(unsigned n) { return gsl_sf_lnfact(n); }
