@@ -1,0 +1,199 @@
+/*
+ * xpsi_gb300.h -- C ABI of the GB300 pulse-likelihood kernels.
+ *
+ * Plain C types only: pointers, sizes, doubles and int32 flags.  Two layers:
+ *
+ *  1. Drop-in entry points, one per native callable on X-PSI's likelihood
+ *     path.  They take HOST arrays with the reference's layouts (C-contiguous
+ *     float64, int32 flags), copy them to the GPU, run the kernels and copy the
+ *     result back before returning.  Return value: >= 0 is the reference's own
+ *     status word; < 0 is a CUDA or usage failure (xgpu_last_error() says why).
+ *
+ *  2. Batched entry points that take DEVICE pointers and a cudaStream_t
+ *     (passed as void*), for many parameter vectors per launch.
+ *
+ * No entry point raises; errors are return codes, as in the reference
+ * (HotRegion.py:12-19 maps the integer statuses to exceptions).
+ */
+#ifndef XPSI_GB300_H
+#define XPSI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XGPU_ABI_VERSION 1
+
+/* Status words of the batched layer (per parameter vector). */
+enum {
+  XGPU_OK = 0,
+  XGPU_RAY_FAIL = 1,      /* rays.pyx:331-339 -> HotRegion.RayError */
+  XGPU_PULSE_FAIL = 2,    /* integrator terminate -> HotRegion.PulseError */
+  XGPU_ATMOS_BOUNDS = 3,  /* Photosphere.py:486-507 */
+  XGPU_QUAD_FAIL = 4,     /* vanished marginal integral -> random llzero */
+  XGPU_SLIM_CUT = 5,      /* slim early exit */
+  XGPU_BAD_INPUT = 6
+};
+
+int xgpu_abi_version(void);
+/* Text of the last failure on the calling thread ("" if none). */
+const char *xgpu_last_error(void);
+
+/* Numerical 4-D atmosphere (hot_Num4D.pyx), the tuple X-PSI preloads:
+ * grids logT[nT], logg[ng], mu[nmu], logE[nE] and the row-major intensity
+ * table [nT][ng][nmu][nE] (preload.pyx:6-35). */
+typedef struct {
+  const double *logT, *logg, *mu, *logE, *intensity;
+  size_t nT, ng, nmu, nE;
+} xgpu_atmos4d;
+
+/* ---------------------------------------------------------------------- */
+/* 1. drop-in entry points (host arrays)                                  */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces xpsi.cellmesh.rays.compute_rays (xpsi/cellmesh/rays.pyx:249-390).
+ * maxAlpha[N_u] is clamped in place as the reference does (:317-318).
+ * Outputs deflection, cos_alpha, lag [N_u][N_R] and maxDeflection[N_u].
+ * Returns the reference's terminate flag (0 or 1). */
+int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R,
+                      double *maxAlpha, size_t N_R, double *deflection,
+                      double *cos_alpha, double *lag, double *maxDeflection);
+
+/* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance.integrate
+ * (xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-98) for uniform
+ * hot regions: no correction field, beam_opt 0, no disk (R_in >= 1e6).
+ * atm_ext 1 = blackbody, 2 = Num4D (atmos required).  image_order_limit 0
+ * means "infer" (the reference's None).  flux[N_E][N_P] is written on
+ * success.  Returns 0 (SUCCESS) or 1 (ERROR, :657-665). */
+int xgpu_integrate(double R, double omega, double r_s, double inclination,
+                   size_t S0, size_t S1, const double *cellArea,
+                   const double *radialCoords_of_parallels,
+                   const double *r_s_over_r, const double *theta,
+                   const double *phi, const double *srcCellParams,
+                   size_t n_params, const int32_t *cell_radiates, size_t N_R,
+                   const double *deflection, const double *cos_alpha,
+                   const double *lag, const double *maxDeflection,
+                   const double *cos_gammaArray, size_t N_E,
+                   const double *energies, size_t N_L, const double *leaves,
+                   size_t N_P, const double *phases, int atm_ext,
+                   const xgpu_atmos4d *atmos, int image_order_limit,
+                   double *flux);
+
+/* Replaces xpsi.tools.energy_integrator.energy_integrator
+ * (xpsi/tools/energy_integrator.pyx:27-31).  signal[N_E][N_P]; log10 energies
+ * and log10 interval edges; out[n_edges-1][N_P] (the reference's return,
+ * already transposed). */
+int xgpu_energy_integrator(size_t N_E, size_t N_P, const double *signal,
+                           const double *log10_energies, size_t n_edges,
+                           const double *log10_edges, double *out);
+
+/* Replaces Instrument.__call__'s fold (xpsi/Instrument.py:192-197):
+ * out[K][N] = matrix[K][0:q] @ signal[q][N]; ld is the matrix row stride. */
+int xgpu_response_fold(size_t K, size_t q, size_t N, const double *matrix,
+                       size_t ld, const double *signal, double *out);
+
+/* Replaces default_background_marginalisation.precomputation (:38-68). */
+int xgpu_precomputation(size_t K, size_t B, const int32_t *counts,
+                        double *out);
+
+/* Replaces default_background_marginalisation.eval_marginal_likelihood
+ * (:450-734).  H components (hot regions), each components[h] is [K][n_phases]
+ * with phases component_phases[h][n_phases]; all components must share one
+ * phase grid.  support[K][2]; background[K][B] or NULL.  Outputs: *loglike,
+ * star[K][B], mcl_bg[K], mcl_bg_support[K].  Returns 0, or XGPU_SLIM_CUT /
+ * XGPU_QUAD_FAIL when the reference would return a random llzero draw (the
+ * draw is in *loglike). */
+int xgpu_eval_marginal_likelihood(
+    double exposure_time, size_t B, const double *phase_edges, size_t K,
+    const double *counts, size_t H, const double *const *components,
+    const size_t *n_phases, const double *const *component_phases,
+    const double *phase_shifts, const double *neg_sum_ln_data_factorial,
+    const double *support, double epsabs, double epsrel, double epsilon,
+    double sigmas, double llzero, const int32_t *allow_negative, double slim,
+    const double *background, double *loglike, double *star, double *mcl_bg,
+    double *mcl_bg_support);
+
+/* ---------------------------------------------------------------------- */
+/* 2. batched entry points (device pointers, asynchronous on `stream`)    */
+/* ---------------------------------------------------------------------- */
+
+/* One cell mesh of one parameter vector (a hot region's superseding or
+ * ceding member).  Rows of all meshes are packed: mesh m owns rows
+ * [row_off, row_off+S0) and cells [cell_off, cell_off+S0*S1). */
+typedef struct {
+  int32_t S0, S1;
+  int64_t row_off, cell_off;
+  double omega, inclination;
+  int32_t image_order_limit, atm_ext;
+  int64_t flux_off;
+} xgpu_mesh;
+
+/* Ray tables for n_rows packed rows (per-row u and r_s).  When lag_C and
+ * lag_scale are non-NULL the lag is calibrated in place as
+ * HotRegion.py:880-901 does: lag = (lag - lag_C[row]) * lag_scale[row].
+ * row_status[row] gets XGPU_RAY_FAIL where the reference would terminate. */
+int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u,
+                    const double *r_s, double *maxAlpha, double *deflection,
+                    double *cos_alpha, double *lag, double *maxDeflection,
+                    int32_t *row_status, const double *lag_C,
+                    const double *lag_scale, void *stream);
+
+/* Integrator over n_meshes packed meshes.  `meshes` is a HOST array; every
+ * other pointer is device memory.  flux receives [N_E][N_P] per mesh at
+ * meshes[m].flux_off; mesh_status[m] gets XGPU_PULSE_FAIL on terminate. */
+typedef struct {
+  const int32_t *row_mesh;
+  const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;
+  const double *deflection, *cos_alpha, *lag;
+  const double *cellArea, *phi, *params;
+  int32_t n_params;
+  const int32_t *radiates;
+  const double *energies, *leaves, *phases;
+  xgpu_atmos4d atmos; /* device pointers; intensity NULL when no mesh is Num4D */
+  double *flux;
+  int32_t *mesh_status;
+} xgpu_integrate_batch_data;
+
+int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows,
+                         int N_R, int N_E, int N_L, int N_P,
+                         const xgpu_integrate_batch_data *d, int target_ctas,
+                         void *stream);
+
+/* Energy integration of n_signals [N_E][N_P] signals at in_off[s] (device
+ * int64 offsets) into [n_edges-1][N_P] at out_off[s]; d_sq[s] divides the
+ * signal first (Likelihood.py:361-364); accumulate adds into out. */
+int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges,
+                      const double *signal, const int64_t *in_off,
+                      const double *log10_energies, const double *log10_edges,
+                      const double *d_sq, double *out, const int64_t *out_off,
+                      int accumulate, void *stream);
+
+/* out[b][K][N] = matrix[K][0:q] @ in[b][q][N] for b < batch (FP64). */
+int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix,
+                    int ld, const double *in, double *out, void *stream);
+
+/* Background-marginalised log-likelihood for n_vec evaluations sharing one
+ * data set: signals[n_vec][H][K][N_P], shifts[n_vec][H]; chan_ll and
+ * chan_flag are [n_vec][K] scratch; star [n_vec][K][B] and the background
+ * estimates [n_vec][K] may be NULL.  loglike[n_vec], status[n_vec]. */
+typedef struct {
+  int32_t n_vec, K, B, H, N_P;
+  double exposure, epsabs, epsrel, epsilon, sigmas, llzero, slim;
+  const double *phase_edges, *comp_phases, *counts, *precomp, *support;
+  const double *background, *signals, *shifts;
+  const int32_t *allow_negative;
+  double *chan_ll;
+  int32_t *chan_flag;
+  double *star, *mcl_bg, *mcl_bg_support, *loglike;
+  int32_t *status;
+} xgpu_likelihood_batch_data;
+
+int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XPSI_GB300_H */

@@ -19,7 +19,11 @@
  * smooth or piecewise-smooth integrands; here the same QAG machinery with the
  * 21-point rule is run to epsrel min(epsrel, 1e-13), which converges to the
  * same integral with a smaller error.  Differences from a GSL build are thus
- * bounded by that GSL routine's own quadrature error.
+ * bounded by that GSL routine's own quadrature error.  When every interior
+ * node sees zero but an endpoint does not (a channel without counts gives a
+ * window of width ~1e91 whose integrand decays on a scale 1 / exposure),
+ * the window is cut into dyadic pieces toward that endpoint, mirroring how a
+ * Clenshaw-Curtis rule, whose nodes include the endpoints, finds the mass.
  */
 #include "gslsub.h"
 
@@ -708,6 +712,35 @@ void gsl_integration_cquad_workspace_free(gsl_integration_cquad_workspace *ws) {
   free(ws);
 }
 
+/* Dyadic pieces toward an endpoint where all the integrand's mass sits: the
+ * window [lo, hi] is cut at lo + L 2^-k (toward lo) or hi - L 2^-k (toward
+ * hi), each piece integrated adaptively, until the pieces stop contributing.
+ * This is what a Clenshaw-Curtis scheme does implicitly for a spike at an
+ * endpoint (its nodes include the endpoints); an interior Gauss-Kronrod rule
+ * would otherwise see only zeros. */
+static double dyadic_to_end(const gsl_function *f, double lo, double hi, int toward_lo,
+                            double er, gsl_integration_workspace *w, size_t *nev) {
+  const double L = hi - lo;
+  double sum = 0.0;
+  int seen = 0, quiet_after = 0;
+  for (int k = 0; k < 2100; k++) {
+    double s1 = ldexp(L, -(k + 1)), s0 = ldexp(L, -k);
+    double p0 = toward_lo ? lo + s1 : hi - s0;
+    double p1 = toward_lo ? lo + s0 : hi - s1;
+    if (!(p0 < p1) || (toward_lo ? p0 <= lo : p1 >= hi)) break;
+    double r, e;
+    qag_core(f, p0, p1, 0.0, er, CQUAD_SUB_LIMIT, &RULE21, w, &r, &e, nev, 1);
+    sum += r;
+    if (r != 0.0) seen = 1;
+    if (seen && fabs(r) <= 1.0e-17 * fabs(sum)) {
+      if (++quiet_after >= 4) break;
+    } else {
+      quiet_after = 0;
+    }
+  }
+  return sum;
+}
+
 int gsl_integration_cquad(const gsl_function *f, double a, double b,
                           double epsabs, double epsrel,
                           gsl_integration_cquad_workspace *ws, double *result,
@@ -727,6 +760,18 @@ int gsl_integration_cquad(const gsl_function *f, double a, double b,
   double r, e;
   /* quiet: a panel that stalls on round-off still returns its best sum */
   qag_core(f, a, b, epsabs, er, CQUAD_SUB_LIMIT, &RULE21, ws->w, &r, &e, &nev, 1);
+  if (r == 0.0) {
+    double fa = GSL_FN_EVAL(f, a), fb = GSL_FN_EVAL(f, b);
+    nev += 2;
+    if (fa != 0.0 || fb != 0.0) {
+      double m = 0.5 * (a + b), rl, rr;
+      if (fa != 0.0) rl = dyadic_to_end(f, a, m, 1, er, ws->w, &nev);
+      else qag_core(f, a, m, 0.0, er, CQUAD_SUB_LIMIT, &RULE21, ws->w, &rl, &e, &nev, 1);
+      if (fb != 0.0) rr = dyadic_to_end(f, m, b, 0, er, ws->w, &nev);
+      else qag_core(f, m, b, 0.0, er, CQUAD_SUB_LIMIT, &RULE21, ws->w, &rr, &e, &nev, 1);
+      r = rl + rr;
+    }
+  }
   *result = sign * r;
   *abserr = e;
   if (nevals) *nevals = nev;

@@ -1,0 +1,226 @@
+"""Generate the golden fixtures under tests/golden/ from the REFERENCE itself.
+
+Runs where the reference checkout and its extension build exist
+(`python oracle/build_ref.py` first).  Every array saved here is an input or
+an output of the reference's own code (X-PSI's Cython compiled by
+oracle/build_ref.py, Python model classes imported from the checkout), so
+the GPU tests compare against the reference, not against a restatement.
+
+Cases
+  examples_fast  the model of xpsi/tests/test_likelihood.py (blackbody spot,
+                 golden log L -47881.27817666349); all stage inputs/outputs.
+  num4d_omit     a spot with an omitted (crescent) region and a small seeded
+                 numerical 4-D atmosphere; fast spin so that mu*eta > 1 and the
+                 reference's history-dependent clamp is exercised.
+  config1        the blackbody workload of the small plain configuration
+                 (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
+                 32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
+                 32 phase bins, 1e6 s, seeded Poisson data) with a reduced
+                 phase/energy grid only where noted.
+
+Usage:  python tests/golden/make_fixtures.py
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_harness as H  # noqa: E402
+from xpsi_gb300 import synthetic  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", path, "%.0f kB" % (os.path.getsize(path) / 1024))
+
+
+def examples_fast(xpsi):
+    H.examples_fast_modules()
+    src = open(os.path.join(H.REF, "xpsi", "tests", "test_likelihood.py")).read()
+    src = src.replace(
+        "assert np.isclose(-47881.27817666349, likelihood(p,force=True,reinitialise=True), rtol=1.0e-5)",
+        "G['v'] = likelihood(p,force=True,reinitialise=True); G['lik'] = likelihood")
+    g = {"__file__": os.path.join(H.REF, "xpsi", "tests", "test_likelihood.py"),
+         "__name__": "tl", "G": {}}
+    exec(compile(src, "test_likelihood.py", "exec"), g)
+    g["TestLikelihoodCheck"]().test_likelihood_is_correct()
+    lik, v = g["G"]["lik"], g["G"]["v"]
+    st = lik._star.spacetime
+    hot = lik._star.photospheres[0].hot
+    sig = lik._signals[0][0]
+    from xpsi.cellmesh.rays import compute_rays
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate
+    from xpsi.tools.energy_integrator import energy_integrator
+    from xpsi.likelihoods.default_background_marginalisation import (
+        eval_marginal_likelihood, precomputation)
+    u = np.ascontiguousarray(st.r_s / hot._super_r)
+    maxAlpha_in = np.pi / 2.0 + np.arccos(hot._super_cos_gamma)
+    ma = maxAlpha_in.copy()
+    S = int(hot._super_sqrt_num_cells)
+    rt = compute_rays(1, S, st.r_s, u, ma, hot._num_rays)
+    E = sig.energies
+    fl = integrate(1, st.R, st.Omega, st.r_s, st.i, hot._super_cellArea, hot._super_r,
+                   hot._super_r_s_over_r, hot._super_theta, hot._super_phi,
+                   hot._super_cellParamVecs, hot._super_radiates, None, hot._num_rays,
+                   hot._super_deflection, hot._super_cos_alpha, hot._super_lag,
+                   hot._super_maxDeflection, hot._super_cos_gamma, E, hot.leaves,
+                   hot.phases, (), None, hot.atm_ext, None, hot.beam_opt,
+                   hot._image_order_limit)
+    sflux = fl[1] / st.d_sq
+    logE, logEd = np.log10(E), np.log10(sig._energy_edges)
+    ei = energy_integrator(1, sflux, logE, logEd)
+    matrix = sig._instrument.construct_matrix()
+    folded = np.dot(matrix, ei)
+    counts = sig._data.counts
+    pre = precomputation(counts.astype(np.int32))
+    ml = eval_marginal_likelihood(sig._data.exposure_time, sig._data.phases, counts,
+                                  sig.signals, [hot.phases_in_cycles], sig.shifts, pre,
+                                  sig._support, 1000, 0.0, 1.0e-8, 1.0e-3, 10.0, -1.0e90)
+    save("examples_fast",
+         golden_logL=-47881.27817666349, ref_logL=v,
+         R=st.R, Omega=st.Omega, r_s=st.r_s, inclination=st.i, d_sq=st.d_sq,
+         cellArea=hot._super_cellArea, radius=hot._super_r, u=hot._super_r_s_over_r,
+         theta=hot._super_theta, phi=hot._super_phi, params=hot._super_cellParamVecs,
+         radiates=hot._super_radiates, N_R=hot._num_rays,
+         maxAlpha_in=maxAlpha_in, rays_u=u, rays_maxAlpha_out=ma,
+         rays_deflection=rt[1], rays_cos_alpha=rt[2], rays_lag=rt[3], rays_maxDefl=rt[4],
+         deflection=hot._super_deflection, cos_alpha=hot._super_cos_alpha,
+         lag=hot._super_lag, maxDeflection=hot._super_maxDeflection,
+         cos_gamma=hot._super_cos_gamma, energies=E, leaves=hot.leaves, phases=hot.phases,
+         atm_ext=hot.atm_ext, image_order_limit=hot._image_order_limit, flux=fl[1],
+         log10_energies=logE, log10_edges=logEd, signal_in=sflux, energy_out=ei,
+         matrix=matrix, folded=folded, registered=sig.signals[0],
+         exposure=sig._data.exposure_time, phase_edges=sig._data.phases, counts=counts,
+         comp_phases=hot.phases_in_cycles, shifts=sig.shifts, precomp=pre,
+         support=sig._support, logL=ml[0], star=ml[1], mcl_bg=ml[2], mcl_bg_s=ml[3])
+
+
+def mesh_member(xpsi, *, M_sun, R_km, f_hz, cos_i, colat, radius, logT, omit=None,
+                sqrt_num_cells, min_cells, max_cells, N_R, antiphased=False):
+    """Mesh, rays and source parameters of one hot region via the reference's
+    own cellmesh functions, with the glue HotRegion applies
+    (HotRegion.py:774-1017)."""
+    from xpsi.global_imports import _GM, _csq, _G, _km, _2pi, _c
+    from xpsi.cellmesh.mesh_tools import allocate_cells
+    from xpsi.cellmesh.mesh import construct_spot_cellMesh
+    from xpsi.cellmesh.rays import compute_rays
+    r_g = M_sun * _GM
+    r_s = 2.0 * r_g
+    R = R_km * _km
+    Mkg = M_sun * _GM * _csq / _G
+    Omega = _2pi * f_hz
+    zeta = r_g / R
+    eps = Omega ** 2.0 * R ** 3.0 / (_G * Mkg)
+    o_r, o_c, o_a = omit if omit is not None else (0.0, 0.0, 0.0)
+    S, N, _, _ = allocate_cells(sqrt_num_cells ** 2, min_cells, max_cells, Mkg, r_s, R, Omega,
+                                zeta, eps, 0, radius, 0.0, colat, colat, -0.0, o_c, o_r, o_a)
+    S = int(S)
+    th, ph, r, A, maxA, cg, g = construct_spot_cellMesh(1, int(N), S, Mkg, r_s, R, zeta, eps,
+                                                        0, radius, colat, o_r, o_c, o_a)
+    ph = ph - o_a
+    if antiphased:
+        ph = ph + math.pi
+    u = np.ascontiguousarray(r_s / r)
+    ma_in = np.array(maxA, copy=True)
+    ma = ma_in.copy()
+    t, D, CA, L, MD = compute_rays(1, S, r_s, u, ma, N_R)
+    assert t == 0
+    raw_lag = L.copy()
+    R_i = R / r_s
+    C = (1.0 / u - R_i)
+    C += np.log((1.0 / u - 1.0) / (R_i - 1.0))
+    C *= r_s / _c
+    for j in range(L.shape[1]):
+        L[:, j] -= C
+    L *= f_hz * _2pi
+    radiates = np.greater(A, 0.0).astype(np.int32)
+    params = np.ones((S, S, 2))
+    params[..., :-1] *= logT
+    for j in range(S):
+        params[:, j, -1] *= g
+    return dict(R=R, Omega=Omega, r_s=r_s, inclination=math.acos(cos_i), S=S,
+                cellArea=A, radius=r, u=u, theta=th, phi=ph, params=params,
+                radiates=radiates, maxAlpha_in=ma_in, rays_maxAlpha_out=ma,
+                deflection=D, cos_alpha=CA, raw_lag=raw_lag, lag=L, maxDeflection=MD,
+                cos_gamma=cg, effGrav=g, N_R=N_R)
+
+
+def num4d_omit(xpsi):
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate
+    atm = synthetic.num4d_table(shape=(12, 8, 20, 40), seed=2)
+    m = mesh_member(xpsi, M_sun=1.6, R_km=14.0, f_hz=600.0, cos_i=0.55, colat=1.2,
+                    radius=0.3, logT=6.3, omit=(0.12, 1.25, 0.1), sqrt_num_cells=20,
+                    min_cells=10, max_cells=40, N_R=256)
+    E = np.logspace(-1.0, 1.0, 48)
+    leaves = np.linspace(0.0, 2 * math.pi, 40)
+    phases = 2 * math.pi * np.linspace(0.0, 1.0, 40)
+    args = lambda nt: (nt, m["R"], m["Omega"], m["r_s"], m["inclination"], m["cellArea"],
+                       m["radius"], m["u"], m["theta"], m["phi"], m["params"],
+                       m["radiates"], None, m["N_R"], m["deflection"], m["cos_alpha"],
+                       m["lag"], m["maxDeflection"], m["cos_gamma"], E, leaves, phases,
+                       atm, None, 2, None, 0, None)
+    st1, flux1 = integrate(*args(1))
+    st4, flux4 = integrate(*args(4))
+    assert st1 == 0
+    save("num4d_omit", **{k: v for k, v in m.items()}, energies=E, leaves=leaves,
+         phases=phases, atm_logT=atm[0], atm_logg=atm[1], atm_mu=atm[2], atm_logE=atm[3],
+         atm_I=atm[4], atm_ext=2, image_order_limit=0, flux=flux1,
+         flux_threads4=flux4 if st4 == 0 else np.zeros(0))
+
+
+def config1(xpsi):
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate
+    from xpsi.tools.energy_integrator import energy_integrator
+    from xpsi.likelihoods.default_background_marginalisation import (
+        eval_marginal_likelihood, precomputation)
+    w = synthetic.config1_workload()
+    m = mesh_member(xpsi, M_sun=w["mass"], R_km=w["radius_km"], f_hz=w["frequency"],
+                    cos_i=math.cos(w["inclination"]), colat=w["colatitude"],
+                    radius=w["spot_radius"], logT=w["logT"], sqrt_num_cells=32,
+                    min_cells=10, max_cells=80, N_R=512)
+    E = w["energies"]
+    leaves = np.linspace(0.0, 2 * math.pi, 64)
+    phases = 2 * math.pi * np.linspace(0.0, 1.0, 64)
+    st, flux = integrate(1, m["R"], m["Omega"], m["r_s"], m["inclination"], m["cellArea"],
+                         m["radius"], m["u"], m["theta"], m["phi"], m["params"],
+                         m["radiates"], None, m["N_R"], m["deflection"], m["cos_alpha"],
+                         m["lag"], m["maxDeflection"], m["cos_gamma"], E, leaves, phases,
+                         (), None, 1, None, 0, None)
+    assert st == 0
+    d_sq = w["d_sq"]
+    sflux = flux / d_sq
+    logE, logEd = np.log10(E), np.log10(w["input_edges"])
+    ei = energy_integrator(1, sflux, logE, logEd)
+    folded = np.dot(w["matrix"], ei)
+    comp_phases = np.linspace(0.0, 1.0, 64)
+    counts = synthetic.poisson_data(folded, comp_phases, w["phase_edges"], w["exposure"],
+                                    seed=20261203)
+    pre = precomputation(counts.astype(np.int32))
+    support = -1.0 * np.ones((counts.shape[0], 2))
+    support[:, 0] = 0.0
+    ml = eval_marginal_likelihood(w["exposure"], w["phase_edges"], counts.astype(np.float64),
+                                  [folded], [comp_phases], np.array([0.0]), pre, support,
+                                  1000, 0.0, 1.0e-8, 1.0e-3, 10.0, -1.0e90)
+    save("config1", **{k: v for k, v in m.items()}, energies=E, leaves=leaves, phases=phases,
+         atm_ext=1, image_order_limit=0, flux=flux, d_sq=d_sq, signal_in=sflux,
+         log10_energies=logE, log10_edges=logEd, energy_out=ei, matrix=w["matrix"],
+         folded=folded, exposure=w["exposure"], phase_edges=w["phase_edges"],
+         counts=counts, comp_phases=comp_phases, shifts=np.array([0.0]), precomp=pre,
+         support=support, logL=ml[0], star=ml[1], mcl_bg=ml[2], mcl_bg_s=ml[3])
+
+
+def main():
+    xpsi = H.load()
+    examples_fast(xpsi)
+    num4d_omit(xpsi)
+    config1(xpsi)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,66 @@
+"""GB300-native pulse-likelihood hot path for X-PSI.
+
+Drop-in replacements for the native callables on X-PSI's likelihood path
+(same names, arguments, return values and error statuses), backed by
+hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
+
+    xpsi_gb300.cellmesh.rays.compute_rays
+    xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
+    xpsi_gb300.tools.energy_integrator.energy_integrator
+    xpsi_gb300.likelihoods.default_background_marginalisation.{precomputation,
+                                                              eval_marginal_likelihood}
+    xpsi_gb300.instrument.fold        (Instrument.__call__'s matrix product)
+
+`install(xpsi)` rebinds them inside an imported X-PSI package, and
+`xpsi_gb300.batch` evaluates many parameter vectors per launch.
+"""
+from ._native import GPUError, build, lib  # noqa: F401
+
+__version__ = "0.1.0"
+
+
+def install(xpsi_module):
+    """Route an imported X-PSI package's likelihood path through the GPU.
+
+    Rebinds the module-level callables that X-PSI's model classes import
+    (HotRegion.py:3-6 and :557-572, Signal.py:10, CustomSignal modules) so
+    that Likelihood.__call__ runs the CUDA kernels.  Returns the list of
+    rebound names.
+    """
+    import importlib
+    from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
+    from .tools import energy_integrator as ei
+    from .likelihoods import default_background_marginalisation as dbm
+    done = []
+    targets = [
+        ("xpsi.cellmesh.rays", "compute_rays", rays.compute_rays),
+        ("xpsi.cellmesh.integrator_for_azimuthal_invariance", "integrate", integ.integrate),
+        ("xpsi.tools.energy_integrator", "energy_integrator", ei.energy_integrator),
+        ("xpsi.likelihoods.default_background_marginalisation", "eval_marginal_likelihood",
+         dbm.eval_marginal_likelihood),
+        ("xpsi.likelihoods.default_background_marginalisation", "precomputation",
+         dbm.precomputation),
+    ]
+    for modname, attr, fn in targets:
+        try:
+            mod = importlib.import_module(modname)
+        except ImportError:
+            continue
+        setattr(mod, attr, fn)
+        done.append(modname + "." + attr)
+    # names bound at import time by the model classes
+    for modname, attr, fn in (("xpsi.HotRegion", "_compute_rays", rays.compute_rays),
+                              ("xpsi.Signal", "energy_integrator", ei.energy_integrator)):
+        mod = importlib.import_module(modname)
+        setattr(mod, attr, fn)
+        done.append(modname + "." + attr)
+    HotRegion = importlib.import_module("xpsi.HotRegion").HotRegion
+    orig = HotRegion.symmetry.fset
+
+    def _symmetry(self, declaration, _orig=orig):
+        _orig(self, declaration)
+        if declaration and not getattr(self, "_split", False):
+            self._integrator = integ.integrate
+    HotRegion.symmetry = property(HotRegion.symmetry.fget, _symmetry)
+    done.append("xpsi.HotRegion.HotRegion.symmetry")
+    return done

@@ -1,0 +1,164 @@
+"""Build and load the in-tree CUDA library (libxpsi_gb300.so) and bind the
+C ABI declared in include/xpsi_gb300.h with ctypes.
+
+The library is compiled for sm_103a only.  Every compute entry point of this
+package goes through it; when it cannot be loaded (no CUDA device, build
+missing) calls fail loudly -- there is no CPU fallback.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libxpsi_gb300.so")
+UNITS = ["rays", "integrator", "energy", "fold", "likelihood", "abi"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+              "--expt-relaxed-constexpr", "-diag-suppress", "177"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _sources_mtime():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+             if f.endswith((".cu", ".cuh", ".h"))]
+    files.append(os.path.join(ROOT, "include", "xpsi_gb300.h"))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def build(force=False, verbose=False):
+    """Compile every CUDA unit for sm_103a (in parallel) and link the library."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+        return LIB
+    nvcc = _nvcc()
+
+    def compile_unit(u):
+        obj = os.path.join(BUILD, u + ".o")
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, u + ".cu"), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s%s" % (u, r.stdout, r.stderr))
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout + r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(len(UNITS)) as ex:
+        objs = list(ex.map(compile_unit, UNITS))
+    tmp = LIB + ".tmp%d" % os.getpid()
+    r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lock = threading.Lock()
+_lib = None
+
+P = C.c_void_p
+D = C.c_double
+SZ = C.c_size_t
+I32 = C.c_int32
+I64 = C.c_int64
+
+
+class Atmos4D(C.Structure):
+    _fields_ = [("logT", P), ("logg", P), ("mu", P), ("logE", P), ("intensity", P),
+                ("nT", SZ), ("ng", SZ), ("nmu", SZ), ("nE", SZ)]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("S0", I32), ("S1", I32), ("row_off", I64), ("cell_off", I64),
+                ("omega", D), ("inclination", D), ("image_order_limit", I32),
+                ("atm_ext", I32), ("flux_off", I64)]
+
+
+class IntegrateBatchData(C.Structure):
+    _fields_ = [("row_mesh", P), ("radius", P), ("u", P), ("cos_gamma", P),
+                ("theta0", P), ("maxDeflection", P), ("deflection", P),
+                ("cos_alpha", P), ("lag", P), ("cellArea", P), ("phi", P),
+                ("params", P), ("n_params", I32), ("radiates", P), ("energies", P),
+                ("leaves", P), ("phases", P), ("atmos", Atmos4D), ("flux", P),
+                ("mesh_status", P)]
+
+
+class LikelihoodBatchData(C.Structure):
+    _fields_ = [("n_vec", I32), ("K", I32), ("B", I32), ("H", I32), ("N_P", I32),
+                ("exposure", D), ("epsabs", D), ("epsrel", D), ("epsilon", D),
+                ("sigmas", D), ("llzero", D), ("slim", D),
+                ("phase_edges", P), ("comp_phases", P), ("counts", P), ("precomp", P),
+                ("support", P), ("background", P), ("signals", P), ("shifts", P),
+                ("allow_negative", P), ("chan_ll", P), ("chan_flag", P), ("star", P),
+                ("mcl_bg", P), ("mcl_bg_support", P), ("loglike", P), ("status", P)]
+
+
+def _bind(L):
+    sig = {
+        "xgpu_abi_version": (C.c_int, []),
+        "xgpu_last_error": (C.c_char_p, []),
+        "xgpu_compute_rays": (C.c_int, [SZ, D, P, P, SZ, P, P, P, P]),
+        "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, SZ,
+                                     P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
+                                     C.POINTER(Atmos4D), C.c_int, P]),
+        "xgpu_energy_integrator": (C.c_int, [SZ, SZ, P, P, SZ, P, P]),
+        "xgpu_response_fold": (C.c_int, [SZ, SZ, SZ, P, SZ, P, P]),
+        "xgpu_precomputation": (C.c_int, [SZ, SZ, P, P]),
+        "xgpu_eval_marginal_likelihood": (C.c_int, [D, SZ, P, SZ, P, SZ, P, P, P, P, P,
+                                                    P, D, D, D, D, D, P, D, P, P, P, P,
+                                                    P]),
+        "xgpu_rays_batch": (C.c_int, [I64, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
+        "xgpu_integrate_batch": (C.c_int, [C.c_int, C.POINTER(Mesh), I64, C.c_int,
+                                           C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(IntegrateBatchData), C.c_int, P]),
+        "xgpu_energy_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P,
+                                        P, P, P, C.c_int, P]),
+        "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
+                                      P, P]),
+        "xgpu_likelihood_batch": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_integrate",
+            "xgpu_energy_integrator", "xgpu_response_fold", "xgpu_precomputation",
+            "xgpu_eval_marginal_likelihood", "xgpu_rays_batch", "xgpu_integrate_batch",
+            "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch"]
+
+
+def lib():
+    """The loaded C ABI (built on first use if the sources are newer)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB) or os.path.getmtime(LIB) < _sources_mtime():
+                build()
+            _lib = _bind(C.CDLL(LIB))
+    return _lib
+
+
+class GPUError(RuntimeError):
+    """A CUDA or usage failure reported by the C ABI."""
+
+
+def check(rc):
+    """Raise GPUError for negative return codes; pass statuses through."""
+    if rc < 0:
+        msg = lib().xgpu_last_error().decode(errors="replace")
+        raise GPUError(msg or ("C ABI call failed with %d" % rc))
+    return rc

@@ -1,0 +1,494 @@
+// abi.cu -- the C ABI (include/xpsi_gb300.h): host staging for the drop-in
+// entry points and argument plumbing for the batched ones.  Device scratch
+// comes from the stream-ordered allocator (cudaMallocAsync), so a drop-in
+// call costs one H2D burst, the kernels and one D2H burst.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/xpsi_gb300.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(const char *what, cudaError_t e) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return -1;
+}
+int fail_msg(const std::string &m) {
+  g_err = m;
+  return -2;
+}
+
+#define CK(x)                              \
+  do {                                     \
+    cudaError_t e_ = (x);                  \
+    if (e_ != cudaSuccess) return fail(#x, e_); \
+  } while (0)
+
+// one library stream per device for the drop-in calls
+std::mutex g_mu;
+cudaStream_t g_stream[64] = {};
+
+int lib_stream(cudaStream_t *st) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail_msg("device index out of range");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_stream[dev]) CK(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
+  *st = g_stream[dev];
+  return 0;
+}
+
+// stream-ordered device buffer
+struct Dev {
+  void *p = nullptr;
+  cudaStream_t st = nullptr;
+  ~Dev() {
+    if (p) cudaFreeAsync(p, st);
+  }
+  template <typename T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+int dalloc(Dev &d, size_t bytes, cudaStream_t st) {
+  d.st = st;
+  if (bytes == 0) bytes = 16;
+  CK(cudaMallocAsync(&d.p, bytes, st));
+  return 0;
+}
+
+template <typename T>
+int upload(Dev &d, const T *h, size_t n, cudaStream_t st) {
+  int r = dalloc(d, n * sizeof(T), st);
+  if (r) return r;
+  if (n) CK(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+// device copy of the most recent Num4D table passed to the drop-in layer,
+// keyed by its host pointers, sizes and a strided content sample
+struct AtmosCache {
+  const double *host_I = nullptr;
+  size_t nT = 0, ng = 0, nmu = 0, nE = 0;
+  uint64_t sample = 0;
+  int dev = -1;
+  void *buf = nullptr;
+  xg::Atmos4D view{};
+} g_atmos;
+
+uint64_t sample_table(const xgpu_atmos4d *A) {
+  size_t n = A->nT * A->ng * A->nmu * A->nE;
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](const double *p, size_t m, size_t stride) {
+    for (size_t i = 0; i < m; i += stride) {
+      uint64_t b;
+      std::memcpy(&b, p + i, 8);
+      h = (h ^ b) * 1099511628211ull;
+    }
+  };
+  mix(A->intensity, n, std::max<size_t>(1, n / 65536));
+  mix(A->logT, A->nT, 1);
+  mix(A->logg, A->ng, 1);
+  mix(A->mu, A->nmu, 1);
+  mix(A->logE, A->nE, 1);
+  return h;
+}
+
+int atmos_device(const xgpu_atmos4d *A, cudaStream_t st, xg::Atmos4D *out) {
+  if (A->nT < 4 || A->ng < 4 || A->nmu < 4 || A->nE < 4)
+    return fail_msg("Num4D grids need at least 4 nodes per dimension");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  uint64_t smp = sample_table(A);
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_atmos.buf && g_atmos.dev == dev && g_atmos.host_I == A->intensity &&
+      g_atmos.nT == A->nT && g_atmos.ng == A->ng && g_atmos.nmu == A->nmu &&
+      g_atmos.nE == A->nE && g_atmos.sample == smp) {
+    *out = g_atmos.view;
+    return 0;
+  }
+  if (g_atmos.buf) {
+    CK(cudaStreamSynchronize(st));
+    cudaFree(g_atmos.buf);
+    g_atmos.buf = nullptr;
+  }
+  size_t nI = A->nT * A->ng * A->nmu * A->nE;
+  size_t tot = A->nT + A->ng + A->nmu + A->nE + nI;
+  CK(cudaMalloc(&g_atmos.buf, tot * sizeof(double)));
+  double *b = static_cast<double *>(g_atmos.buf);
+  double *pT = b, *pg = pT + A->nT, *pm = pg + A->ng, *pE = pm + A->nmu, *pI = pE + A->nE;
+  CK(cudaMemcpyAsync(pT, A->logT, A->nT * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pg, A->logg, A->ng * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pm, A->mu, A->nmu * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pE, A->logE, A->nE * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pI, A->intensity, nI * 8, cudaMemcpyHostToDevice, st));
+  g_atmos.host_I = A->intensity;
+  g_atmos.nT = A->nT; g_atmos.ng = A->ng; g_atmos.nmu = A->nmu; g_atmos.nE = A->nE;
+  g_atmos.sample = smp;
+  g_atmos.dev = dev;
+  g_atmos.view = xg::Atmos4D{pT, pg, pm, pE, pI, (int)A->nT, (int)A->ng, (int)A->nmu,
+                             (int)A->nE};
+  *out = g_atmos.view;
+  return 0;
+}
+
+static_assert(sizeof(xgpu_mesh) == sizeof(xg::MemberDesc), "mesh descriptor layout");
+
+}  // namespace
+
+extern "C" {
+
+int xgpu_abi_version(void) { return XGPU_ABI_VERSION; }
+const char *xgpu_last_error(void) { return g_err.c_str(); }
+
+// ------------------------------------------------------------------ batched
+int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u, const double *r_s,
+                    double *maxAlpha, double *deflection, double *cos_alpha, double *lag,
+                    double *maxDeflection, int32_t *row_status, const double *lag_C,
+                    const double *lag_scale, void *stream) {
+  if (N_R < 3) return fail_msg("num_rays must be at least 3");
+  if (n_rows > INT32_MAX) return fail_msg("too many rows in one launch");
+  xg::RaysArgs a{(int)n_rows, N_R, u, r_s, maxAlpha, deflection, cos_alpha, lag,
+                 maxDeflection, row_status, lag_C, lag_scale};
+  xg::launch_rays(a, static_cast<cudaStream_t>(stream));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
+                         int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
+                         int target_ctas, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_meshes <= 0) return 0;
+  if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
+  if (N_R < 3) return fail_msg("num_rays must be at least 3");
+  for (int m = 0; m < n_meshes; m++) {
+    if (meshes[m].atm_ext == 2 && d->atmos.intensity == nullptr)
+      return fail_msg("a Num4D mesh needs the atmosphere table");
+    if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2)
+      return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+  }
+  if (target_ctas <= 0) target_ctas = 4 * 152;
+  int64_t rpc = std::max<int64_t>(1, n_rows / target_ctas);
+  std::vector<int64_t> r0, r1;
+  std::vector<int32_t> first(n_meshes + 1);
+  for (int m = 0; m < n_meshes; m++) {
+    first[m] = (int32_t)r0.size();
+    for (int64_t s = 0; s < meshes[m].S0; s += rpc) {
+      r0.push_back(meshes[m].row_off + s);
+      r1.push_back(meshes[m].row_off + std::min<int64_t>(meshes[m].S0, s + rpc));
+    }
+  }
+  first[n_meshes] = (int32_t)r0.size();
+  int n_chunks = (int)r0.size();
+  Dev dm, dr0, dr1, dfirst, dpart, dstate;
+  int rc;
+  if ((rc = upload(dm, reinterpret_cast<const xg::MemberDesc *>(meshes), n_meshes, st))) return rc;
+  if ((rc = upload(dr0, r0.data(), r0.size(), st))) return rc;
+  if ((rc = upload(dr1, r1.data(), r1.size(), st))) return rc;
+  if ((rc = upload(dfirst, first.data(), first.size(), st))) return rc;
+  size_t part_n = (size_t)n_chunks * N_E * N_P;
+  if ((rc = dalloc(dpart, part_n * sizeof(double), st))) return rc;
+  CK(cudaMemsetAsync(dpart.p, 0, part_n * sizeof(double), st));
+  if ((rc = dalloc(dstate, (size_t)3 * n_rows + 16, st))) return rc;
+  CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
+
+  xg::IntegrateArgs a{};
+  a.n_members = n_meshes;
+  a.n_rows = n_rows;
+  a.members = dm.as<xg::MemberDesc>();
+  a.row_member = d->row_mesh;
+  a.radius = d->radius; a.u = d->u; a.cos_gamma = d->cos_gamma; a.theta0 = d->theta0;
+  a.maxDeflection = d->maxDeflection;
+  a.deflection = d->deflection; a.cos_alpha = d->cos_alpha; a.lag = d->lag;
+  a.N_R = N_R;
+  a.cellArea = d->cellArea; a.phi = d->phi; a.params = d->params; a.n_params = d->n_params;
+  a.radiates = d->radiates;
+  a.N_E = N_E; a.N_L = N_L; a.N_P = N_P;
+  a.energies = d->energies; a.leaves = d->leaves; a.phases = d->phases;
+  a.atmos = xg::Atmos4D{d->atmos.logT, d->atmos.logg, d->atmos.mu, d->atmos.logE,
+                        d->atmos.intensity, (int)d->atmos.nT, (int)d->atmos.ng,
+                        (int)d->atmos.nmu, (int)d->atmos.nE};
+  a.n_chunks = n_chunks;
+  a.chunk_r0 = dr0.as<int64_t>();
+  a.chunk_r1 = dr1.as<int64_t>();
+  a.partial = dpart.as<double>();
+  a.chunk_first = dfirst.as<int32_t>();
+  uint8_t *sb = dstate.as<uint8_t>();
+  a.row_has_eval = sb; a.row_last_top = sb + n_rows; a.row_entry_top = sb + 2 * n_rows;
+  a.member_status = d->mesh_status;
+  a.flux = d->flux;
+  xg::launch_integrate(a, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges, const double *signal,
+                      const int64_t *in_off, const double *log10_energies,
+                      const double *log10_edges, const double *d_sq, double *out,
+                      const int64_t *out_off, int accumulate, void *stream) {
+  if (N_E < 5) return fail_msg("at least 5 energies are needed (Akima spline)");
+  xg::EnergyArgs a{n_signals, N_E, N_P, n_edges, signal, in_off, log10_energies,
+                   log10_edges, 1.0, d_sq, out, out_off, accumulate};
+  xg::launch_energy(a, static_cast<cudaStream_t>(stream));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix, int ld,
+                    const double *in, double *out, void *stream) {
+  xg::FoldArgs a{batch, K, q, N, matrix, ld, in, out};
+  xg::launch_fold_f64(a, static_cast<cudaStream_t>(stream));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream) {
+  if (d->B > 64) return fail_msg("at most 64 phase bins per channel");
+  if (d->N_P < 5) return fail_msg("at least 5 signal phases are needed (Akima spline)");
+  xg::LikeArgs a{};
+  a.n_vec = d->n_vec; a.K = d->K; a.B = d->B; a.H = d->H; a.N_P = d->N_P;
+  a.exposure = d->exposure; a.epsabs = d->epsabs; a.epsrel = d->epsrel;
+  a.epsilon = d->epsilon; a.sigmas = d->sigmas; a.llzero = d->llzero; a.slim = d->slim;
+  a.phase_edges = d->phase_edges; a.comp_phases = d->comp_phases; a.counts = d->counts;
+  a.precomp = d->precomp; a.support = d->support; a.background = d->background;
+  a.signals = d->signals; a.shifts = d->shifts; a.allow_negative = d->allow_negative;
+  a.chan_ll = d->chan_ll; a.chan_flag = d->chan_flag; a.star = d->star;
+  a.mcl_bg = d->mcl_bg; a.mcl_bg_s = d->mcl_bg_support; a.loglike = d->loglike;
+  a.status = d->status;
+  xg::launch_likelihood(a, static_cast<cudaStream_t>(stream));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// ------------------------------------------------------------------ drop-in
+int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R, double *maxAlpha,
+                      size_t N_R, double *deflection, double *cos_alpha, double *lag,
+                      double *maxDeflection) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (N_u == 0) return 0;
+  std::vector<double> rs(N_u, r_s);
+  Dev du, drs, dma, dD, dCA, dL, dMD, dstat;
+  size_t tab = N_u * N_R;
+  if ((rc = upload(du, r_s_over_R, N_u, st))) return rc;
+  if ((rc = upload(drs, rs.data(), N_u, st))) return rc;
+  if ((rc = upload(dma, maxAlpha, N_u, st))) return rc;
+  if ((rc = dalloc(dD, tab * 8, st)) || (rc = dalloc(dCA, tab * 8, st)) ||
+      (rc = dalloc(dL, tab * 8, st)) || (rc = dalloc(dMD, N_u * 8, st)) ||
+      (rc = dalloc(dstat, N_u * 4, st)))
+    return rc;
+  rc = xgpu_rays_batch((int64_t)N_u, (int)N_R, du.as<double>(), drs.as<double>(),
+                       dma.as<double>(), dD.as<double>(), dCA.as<double>(), dL.as<double>(),
+                       dMD.as<double>(), dstat.as<int32_t>(), nullptr, nullptr, st);
+  if (rc) return rc;
+  std::vector<int32_t> stat(N_u);
+  CK(cudaMemcpyAsync(maxAlpha, dma.p, N_u * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(deflection, dD.p, tab * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(cos_alpha, dCA.p, tab * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(lag, dL.p, tab * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(maxDeflection, dMD.p, N_u * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(stat.data(), dstat.p, N_u * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (size_t i = 0; i < N_u; i++)
+    if (stat[i] != 0) return 1;
+  return 0;
+}
+
+int xgpu_integrate(double R, double omega, double r_s, double inclination, size_t S0,
+                   size_t S1, const double *cellArea, const double *radius,
+                   const double *r_s_over_r, const double *theta, const double *phi,
+                   const double *srcCellParams, size_t n_params, const int32_t *radiates,
+                   size_t N_R, const double *deflection, const double *cos_alpha,
+                   const double *lag, const double *maxDeflection, const double *cos_gamma,
+                   size_t N_E, const double *energies, size_t N_L, const double *leaves,
+                   size_t N_P, const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
+                   int image_order_limit, double *flux) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (n_params < 2) return fail_msg("srcCellParams needs at least 2 parameters per cell");
+  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
+  xg::Atmos4D A{};
+  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  const size_t cells = S0 * S1;
+  std::vector<double> theta0(S0);
+  for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
+  std::vector<int32_t> row_mesh(S0, 0);
+  Dev dA, drad, du, dth0, dphi, dpar, dR, dD, dCA, dL, dMD, dcg, dE, dLv, dP, dF, dst, drm;
+  if ((rc = upload(dA, cellArea, cells, st)) || (rc = upload(drad, radius, S0, st)) ||
+      (rc = upload(du, r_s_over_r, S0, st)) || (rc = upload(dth0, theta0.data(), S0, st)) ||
+      (rc = upload(dphi, phi, cells, st)) || (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
+      (rc = upload(dR, radiates, cells, st)) || (rc = upload(dD, deflection, S0 * N_R, st)) ||
+      (rc = upload(dCA, cos_alpha, S0 * N_R, st)) || (rc = upload(dL, lag, S0 * N_R, st)) ||
+      (rc = upload(dMD, maxDeflection, S0, st)) || (rc = upload(dcg, cos_gamma, S0, st)) ||
+      (rc = upload(dE, energies, N_E, st)) || (rc = upload(dLv, leaves, N_L, st)) ||
+      (rc = upload(dP, phases, N_P, st)) || (rc = dalloc(dF, N_E * N_P * 8, st)) ||
+      (rc = dalloc(dst, 16, st)) || (rc = upload(drm, row_mesh.data(), S0, st)))
+    return rc;
+  xgpu_mesh mesh{(int32_t)S0, (int32_t)S1, 0, 0, omega, inclination, image_order_limit,
+                 atm_ext, 0};
+  xgpu_integrate_batch_data d{};
+  d.row_mesh = drm.as<int32_t>();
+  d.radius = drad.as<double>(); d.u = du.as<double>(); d.cos_gamma = dcg.as<double>();
+  d.theta0 = dth0.as<double>(); d.maxDeflection = dMD.as<double>();
+  d.deflection = dD.as<double>(); d.cos_alpha = dCA.as<double>(); d.lag = dL.as<double>();
+  d.cellArea = dA.as<double>(); d.phi = dphi.as<double>(); d.params = dpar.as<double>();
+  d.n_params = (int32_t)n_params; d.radiates = dR.as<int32_t>();
+  d.energies = dE.as<double>(); d.leaves = dLv.as<double>(); d.phases = dP.as<double>();
+  if (atm_ext == 2) {
+    d.atmos = xgpu_atmos4d{A.logT, A.logg, A.mu, A.logE, A.I, (size_t)A.nT, (size_t)A.ng,
+                           (size_t)A.nmu, (size_t)A.nE};
+  }
+  d.flux = dF.as<double>();
+  d.mesh_status = dst.as<int32_t>();
+  rc = xgpu_integrate_batch(1, &mesh, (int64_t)S0, (int)N_R, (int)N_E, (int)N_L, (int)N_P, &d,
+                            0, st);
+  if (rc) return rc;
+  int32_t status = 0;
+  CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux, dF.p, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return status != 0 ? 1 : 0;
+}
+
+int xgpu_energy_integrator(size_t N_E, size_t N_P, const double *signal,
+                           const double *log10_energies, size_t n_edges,
+                           const double *log10_edges, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (n_edges < 2) return 0;
+  int64_t zero = 0;
+  Dev ds, dE, ded, dout, doff;
+  size_t nout = (n_edges - 1) * N_P;
+  if ((rc = upload(ds, signal, N_E * N_P, st)) || (rc = upload(dE, log10_energies, N_E, st)) ||
+      (rc = upload(ded, log10_edges, n_edges, st)) || (rc = dalloc(dout, nout * 8, st)) ||
+      (rc = upload(doff, &zero, 1, st)))
+    return rc;
+  CK(cudaMemsetAsync(dout.p, 0, nout * 8, st));
+  rc = xgpu_energy_batch(1, (int)N_E, (int)N_P, (int)n_edges, ds.as<double>(),
+                         doff.as<int64_t>(), dE.as<double>(), ded.as<double>(), nullptr,
+                         dout.as<double>(), doff.as<int64_t>(), 0, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, dout.p, nout * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_response_fold(size_t K, size_t q, size_t N, const double *matrix, size_t ld,
+                       const double *signal, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  Dev dM, ds, dout;
+  if ((rc = upload(dM, matrix, K * ld, st)) || (rc = upload(ds, signal, q * N, st)) ||
+      (rc = dalloc(dout, K * N * 8, st)))
+    return rc;
+  rc = xgpu_fold_batch(1, (int)K, (int)q, (int)N, dM.as<double>(), (int)ld, ds.as<double>(),
+                       dout.as<double>(), st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, dout.p, K * N * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_precomputation(size_t K, size_t B, const int32_t *counts, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  Dev dc, dout;
+  if ((rc = upload(dc, counts, K * B, st)) || (rc = dalloc(dout, K * 8, st))) return rc;
+  xg::launch_precomputation((int)K, (int)B, dc.as<int32_t>(), dout.as<double>(), st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout.p, K * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_eval_marginal_likelihood(double exposure_time, size_t B, const double *phase_edges,
+                                  size_t K, const double *counts, size_t H,
+                                  const double *const *components, const size_t *n_phases,
+                                  const double *const *component_phases,
+                                  const double *phase_shifts, const double *precomp,
+                                  const double *support, double epsabs, double epsrel,
+                                  double epsilon, double sigmas, double llzero,
+                                  const int32_t *allow_negative, double slim,
+                                  const double *background, double *loglike, double *star,
+                                  double *mcl_bg, double *mcl_bg_support) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (H == 0) return fail_msg("at least one component is needed");
+  const size_t N_P = n_phases[0];
+  for (size_t h = 1; h < H; h++) {
+    if (n_phases[h] != N_P ||
+        std::memcmp(component_phases[h], component_phases[0], N_P * sizeof(double)) != 0)
+      return fail_msg("components must share one phase grid");
+  }
+  std::vector<double> sig(H * K * N_P);
+  for (size_t h = 0; h < H; h++)
+    std::memcpy(sig.data() + h * K * N_P, components[h], K * N_P * sizeof(double));
+  Dev dpe, dcp, dcnt, dpre, dsup, dbg, dsig, dsh, dan, dll, dfl, dstar, dmb, dmbs, dL, dS;
+  if ((rc = upload(dpe, phase_edges, B + 1, st)) ||
+      (rc = upload(dcp, component_phases[0], N_P, st)) || (rc = upload(dcnt, counts, K * B, st)) ||
+      (rc = upload(dpre, precomp, K, st)) || (rc = upload(dsup, support, 2 * K, st)) ||
+      (rc = upload(dsig, sig.data(), sig.size(), st)) || (rc = upload(dsh, phase_shifts, H, st)) ||
+      (rc = upload(dan, allow_negative, H, st)) || (rc = dalloc(dll, K * 8, st)) ||
+      (rc = dalloc(dfl, K * 4, st)) || (rc = dalloc(dstar, K * B * 8, st)) ||
+      (rc = dalloc(dmb, K * 8, st)) || (rc = dalloc(dmbs, K * 8, st)) ||
+      (rc = dalloc(dL, 8, st)) || (rc = dalloc(dS, 4, st)))
+    return rc;
+  if (background && (rc = upload(dbg, background, K * B, st))) return rc;
+  CK(cudaMemsetAsync(dmb.p, 0, K * 8, st));
+  CK(cudaMemsetAsync(dmbs.p, 0, K * 8, st));
+  xgpu_likelihood_batch_data d{};
+  d.n_vec = 1; d.K = (int32_t)K; d.B = (int32_t)B; d.H = (int32_t)H; d.N_P = (int32_t)N_P;
+  d.exposure = exposure_time; d.epsabs = epsabs; d.epsrel = epsrel; d.epsilon = epsilon;
+  d.sigmas = sigmas; d.llzero = llzero; d.slim = slim;
+  d.phase_edges = dpe.as<double>(); d.comp_phases = dcp.as<double>();
+  d.counts = dcnt.as<double>(); d.precomp = dpre.as<double>(); d.support = dsup.as<double>();
+  d.background = background ? dbg.as<double>() : nullptr;
+  d.signals = dsig.as<double>(); d.shifts = dsh.as<double>();
+  d.allow_negative = dan.as<int32_t>();
+  d.chan_ll = dll.as<double>(); d.chan_flag = dfl.as<int32_t>();
+  d.star = dstar.as<double>(); d.mcl_bg = dmb.as<double>(); d.mcl_bg_support = dmbs.as<double>();
+  d.loglike = dL.as<double>(); d.status = dS.as<int32_t>();
+  rc = xgpu_likelihood_batch(&d, st);
+  if (rc) return rc;
+  int32_t status = 0;
+  std::vector<int32_t> flags(K);
+  CK(cudaMemcpyAsync(loglike, dL.p, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&status, dS.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flags.data(), dfl.p, K * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(star, dstar.p, K * B * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(mcl_bg, dmb.p, K * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(mcl_bg_support, dmbs.p, K * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  // channels after an early exit are left as the reference leaves them (zero)
+  for (size_t ch = 0; ch < K; ch++) {
+    if (flags[ch] != 0) {
+      size_t first_zero = (flags[ch] == 1) ? ch + 1 : ch + 1;
+      for (size_t c2 = first_zero; c2 < K; c2++) {
+        std::memset(star + c2 * B, 0, B * sizeof(double));
+        mcl_bg[c2] = 0.0;
+        mcl_bg_support[c2] = 0.0;
+      }
+      break;
+    }
+  }
+  return status;
+}
+
+}  // extern "C"

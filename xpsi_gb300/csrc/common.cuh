@@ -1,0 +1,265 @@
+// common.cuh -- device-side building blocks shared by the pulse-likelihood
+// kernels: physical constants, status codes, spline pieces (Steffen, Akima
+// with periodic ends) and a QUADPACK-style adaptive Gauss-Kronrod integrator.
+//
+// The numerical semantics follow the X-PSI reference path (cited per item);
+// the spline and quadrature algorithms are the published ones the reference
+// reaches through GSL (Steffen 1990; Akima 1970 with periodic end chords;
+// QUADPACK QAG, Piessens et al. 1983).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gk_nodes.h"
+
+namespace xg {
+
+// xpsi/global_imports.py constants
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kHalfPi = kPi / 2.0;
+constexpr double kTwoPi = 2.0 * kPi;
+constexpr double kC = 2.99792458e8;
+constexpr double kKeV = 1.60217662e-16;
+constexpr double kKB = 1.38064852e-23;
+constexpr double kHKeV = 4.135667662e-18;
+constexpr double kErg = 1.0e-7;                  // hot_BB.pyx:23
+constexpr double kPlanck = 5.040366110812353e22; // hot_BB.pyx:24
+constexpr double kBPhotonSphere = 2.598076211353316;  // 3 sqrt(3)/2, rays.pyx:59
+
+// status words shared by every batched entry point
+enum Status : int32_t {
+  kOk = 0,
+  kRayFail = 1,     // rays.pyx:331-339 -> HotRegion.RayError
+  kPulseFail = 2,   // integrator terminate -> HotRegion.PulseError
+  kAtmosBounds = 3, // Photosphere.py:486-507
+  kQuadFail = 4,    // marginal integral vanished -> random llzero
+  kSlimCut = 5,     // slim early exit (default_background_marginalisation.pyx:677-684)
+  kBadInput = 6,
+};
+
+// tools/core.pyx:118-122
+__host__ __device__ __forceinline__ bool are_equal(double x, double y) {
+  return fabs(x - y) < 1.0e-12;
+}
+
+// rays.pyx:53-57
+__device__ __forceinline__ double image_deflection(int order, double psi) {
+  double s = (order % 2 == 0) ? 1.0 : -1.0;
+  return (order % 2 != 0) ? (double)(order + 1) * kPi + s * psi
+                          : (double)order * kPi + s * psi;
+}
+
+// largest i in [0, n-2] with x[i] <= v (v inside [x[0], x[n-1]])
+template <typename T>
+__device__ __forceinline__ int locate(const T *x, int n, T v) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (x[mid] > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------
+// Steffen (1990) monotone cubic, evaluated without a coefficient table: the
+// node slopes of interval i need only y[i-1..i+2].  End slopes are the end
+// chords (Steffen sect. 2.2, the choice GSL's steffen type makes).
+// ---------------------------------------------------------------------
+template <typename XF, typename YF>
+__device__ __forceinline__ double steffen_slope(const XF &x, const YF &y, int n, int i) {
+  if (i == 0) return (y(1) - y(0)) / (x(1) - x(0));
+  if (i == n - 1) return (y(n - 1) - y(n - 2)) / (x(n - 1) - x(n - 2));
+  double hl = x(i) - x(i - 1), hr = x(i + 1) - x(i);
+  double sl = (y(i) - y(i - 1)) / hl, sr = (y(i + 1) - y(i)) / hr;
+  double p = (sl * hr + sr * hl) / (hl + hr);
+  double mag = fmin(fabs(sl), fmin(fabs(sr), 0.5 * fabs(p)));
+  return (copysign(1.0, sl) + copysign(1.0, sr)) * mag;
+}
+
+struct Cubic {
+  double y0, k1, k2, k3, x0;
+};
+
+template <typename XF, typename YF>
+__device__ __forceinline__ Cubic steffen_piece(const XF &x, const YF &y, int n, int i) {
+  double h = x(i + 1) - x(i);
+  double s = (y(i + 1) - y(i)) / h;
+  double d0 = steffen_slope(x, y, n, i), d1 = steffen_slope(x, y, n, i + 1);
+  Cubic c;
+  c.x0 = x(i);
+  c.y0 = y(i);
+  c.k1 = d0;
+  c.k2 = (3.0 * s - 2.0 * d0 - d1) / h;
+  c.k3 = (d0 + d1 - 2.0 * s) / (h * h);
+  return c;
+}
+
+__device__ __forceinline__ double cubic_eval(const Cubic &c, double v) {
+  double t = v - c.x0;
+  return c.y0 + t * (c.k1 + t * (c.k2 + t * c.k3));
+}
+
+__device__ __forceinline__ double cubic_deriv(const Cubic &c, double v) {
+  double t = v - c.x0;
+  return c.k1 + t * (2.0 * c.k2 + 3.0 * c.k3 * t);
+}
+
+// exact integral of a cubic piece over [x0 + u, x0 + w]
+__host__ __device__ __forceinline__ double piece_integral(double y0, double k1, double k2,
+                                                          double k3, double u, double w) {
+  double Fw = w * (y0 + w * (0.5 * k1 + w * (k2 / 3.0 + 0.25 * k3 * w)));
+  double Fu = u * (y0 + u * (0.5 * k1 + u * (k2 / 3.0 + 0.25 * k3 * u)));
+  return Fw - Fu;
+}
+
+// ---------------------------------------------------------------------
+// Akima (1970) piece coefficients for interval i from the chord slopes
+// m[i-2..i+2]; a segment whose two weights vanish is the chord.
+// ---------------------------------------------------------------------
+template <typename Real>
+__device__ __forceinline__ void akima_piece(Real mm2, Real mm1, Real m0, Real mp1, Real mp2,
+                                            Real h, Real &k1, Real &k2, Real &k3) {
+  Real wl = fabs(mp1 - m0) + fabs(mm1 - mm2);
+  if (wl == Real(0)) {
+    k1 = m0; k2 = Real(0); k3 = Real(0);
+    return;
+  }
+  Real wr = fabs(mp2 - mp1) + fabs(m0 - mm1);
+  Real f = fabs(mm1 - mm2) / wl;
+  Real tl = (Real(1) - f) * mm1 + f * m0;
+  Real tr;
+  if (wr == Real(0)) {
+    tr = m0;
+  } else {
+    Real g = fabs(m0 - mm1) / wr;
+    tr = (Real(1) - g) * m0 + g * mp1;
+  }
+  k1 = tl;
+  k2 = (Real(3) * m0 - Real(2) * tl - tr) / h;
+  k3 = (tl + tr - Real(2) * m0) / (h * h);
+}
+
+// periodic chord index: chords 0..n-2, ghosts -2,-1 -> n-3,n-2; n-1,n -> 0,1
+__device__ __forceinline__ int periodic_chord(int j, int n) {
+  if (j < 0) return j + (n - 1);
+  if (j > n - 2) return j - (n - 1);
+  return j;
+}
+
+// ---------------------------------------------------------------------
+// QUADPACK QAG with a Gauss-Kronrod rule, one thread per integral.  The
+// interval list lives in the caller-provided arrays (local memory).
+// Returns a GSL-compatible status: 0 ok, 5 failed, 11 max iterations,
+// 18 round-off, 21 singularity.  Result semantics match the reference's
+// GSL call (best estimate returned on every status).
+// ---------------------------------------------------------------------
+template <int HALF>
+struct GKRule {
+  const double *x, *wk, *wg;
+};
+
+template <int HALF, typename F>
+__device__ __forceinline__ void gk_panel(const F &f, const double *X, const double *WK,
+                                         const double *WG, double a, double b, double &res,
+                                         double &err, double &rabs, double &rasc) {
+  constexpr int NH = HALF - 1;
+  double c = 0.5 * (a + b), h = 0.5 * (b - a), ah = fabs(h);
+  double fv1[NH], fv2[NH];
+  double fc = f(c);
+  double rk = WK[NH] * fc;
+  double rg = WG[NH] * fc;
+  double ra = fabs(rk);
+#pragma unroll
+  for (int j = 0; j < NH; j++) {
+    double dx = h * X[j];
+    double f1 = f(c - dx), f2 = f(c + dx);
+    fv1[j] = f1;
+    fv2[j] = f2;
+    rk += WK[j] * (f1 + f2);
+    rg += WG[j] * (f1 + f2);
+    ra += WK[j] * (fabs(f1) + fabs(f2));
+  }
+  double mean = 0.5 * rk;
+  double rc = WK[NH] * fabs(fc - mean);
+#pragma unroll
+  for (int j = 0; j < NH; j++) rc += WK[j] * (fabs(fv1[j] - mean) + fabs(fv2[j] - mean));
+  res = rk * h;
+  ra *= ah;
+  rc *= ah;
+  double e = fabs((rk - rg) * h);
+  if (rc != 0.0 && e != 0.0) {
+    double sc = pow(200.0 * e / rc, 1.5);
+    e = sc < 1.0 ? rc * sc : rc;
+  }
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  if (ra > dmin / (50.0 * eps)) {
+    double fl = 50.0 * eps * ra;
+    if (fl > e) e = fl;
+  }
+  err = e;
+  rabs = ra;
+  rasc = rc;
+}
+
+template <int HALF, int LIMIT, typename F>
+__device__ int qag(const F &f, const double *X, const double *WK, const double *WG, double a,
+                   double b, double epsabs, double epsrel, double &result, double &abserr) {
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  double al[LIMIT], bl[LIMIT], rl[LIMIT], el[LIMIT];
+  double r0, e0, ra0, rc0;
+  gk_panel<HALF>(f, X, WK, WG, a, b, r0, e0, ra0, rc0);
+  int size = 1;
+  al[0] = a; bl[0] = b; rl[0] = r0; el[0] = e0;
+  double tol = fmax(epsabs, epsrel * fabs(r0));
+  double rfloor = 50.0 * eps * ra0;
+  if (e0 <= rfloor && e0 > tol) { result = r0; abserr = e0; return 18; }
+  if ((e0 <= tol && e0 != rc0) || e0 == 0.0) { result = r0; abserr = e0; return 0; }
+  if (LIMIT == 1) { result = r0; abserr = e0; return 11; }
+  double area = r0, errsum = e0;
+  int rnd1 = 0, rnd2 = 0, fail = 0, iter = 1, k = 0;
+  do {
+    double ai = al[k], bi = bl[k], ri = rl[k], ei = el[k];
+    double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
+    double r1, e1, ra1, rc1, r2, e2, ra2, rc2;
+    gk_panel<HALF>(f, X, WK, WG, a1, b1, r1, e1, ra1, rc1);
+    gk_panel<HALF>(f, X, WK, WG, a2, b2, r2, e2, ra2, rc2);
+    double r12 = r1 + r2, e12 = e1 + e2;
+    errsum += e12 - ei;
+    area += r12 - ri;
+    if (rc1 != e1 && rc2 != e2) {
+      double delta = ri - r12;
+      if (fabs(delta) <= 1.0e-5 * fabs(r12) && e12 >= 0.99 * ei) rnd1++;
+      if (iter >= 10 && e12 > ei) rnd2++;
+    }
+    tol = fmax(epsabs, epsrel * fabs(area));
+    if (errsum > tol) {
+      if (rnd1 >= 6 || rnd2 >= 20) fail = 2;
+      double edge = (1.0 + 100.0 * eps) * (fabs(a2) + 1000.0 * dmin);
+      if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
+    }
+    int nw = size++;
+    if (e2 > e1) {
+      al[k] = a2; bl[k] = b2; rl[k] = r2; el[k] = e2;
+      al[nw] = a1; bl[nw] = b1; rl[nw] = r1; el[nw] = e1;
+    } else {
+      al[k] = a1; bl[k] = b1; rl[k] = r1; el[k] = e1;
+      al[nw] = a2; bl[nw] = b2; rl[nw] = r2; el[nw] = e2;
+    }
+    k = 0;
+    for (int i = 1; i < size; i++)
+      if (el[i] > el[k]) k = i;
+    iter++;
+  } while (iter < LIMIT && !fail && errsum > tol);
+  double sum = 0.0;
+  for (int i = 0; i < size; i++) sum += rl[i];
+  result = sum;
+  abserr = errsum;
+  if (errsum <= tol) return 0;
+  if (fail == 2) return 18;
+  if (fail == 3) return 21;
+  if (iter == LIMIT) return 11;
+  return 5;
+}
+
+}  // namespace xg

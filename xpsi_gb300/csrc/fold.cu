@@ -1,0 +1,69 @@
+// fold.cu -- K5 (FP64 form): the instrument-response fold
+// signals[K][N] = M[K][q] @ integrated[q][N], replacing Instrument.__call__
+// (xpsi/Instrument.py:163-197, a numpy dot).  All likelihood evaluations in a
+// batch share M, so the batch is one GEMM over N = batch * phases columns.
+// FP64 tiles of 64 x 64 in shared memory, 4 x 4 outputs per thread.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace xg {
+namespace {
+
+constexpr int TM = 64, TN = 64, TK = 16;
+
+__global__ void __launch_bounds__(256) fold_f64_kernel(FoldArgs a) {
+  __shared__ double sA[TK][TM + 1];
+  __shared__ double sB[TK][TN + 1];
+  const int b = blockIdx.z;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const double *In = a.in + (size_t)b * a.q * a.N;
+  double *Out = a.out + (size_t)b * a.K * a.N;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < a.q; k0 += TK) {
+    for (int t = threadIdx.x; t < TK * TM; t += 256) {
+      int kk = t % TK, mm = t / TK;
+      int gm = m0 + mm, gk = k0 + kk;
+      sA[kk][mm] = (gm < a.K && gk < a.q) ? a.M[(size_t)gm * a.ldM + gk] : 0.0;
+    }
+    for (int t = threadIdx.x; t < TK * TN; t += 256) {
+      int nn = t % TN, kk = t / TN;
+      int gn = n0 + nn, gk = k0 + kk;
+      sB[kk][nn] = (gn < a.N && gk < a.q) ? In[(size_t)gk * a.N + gn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; kk++) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) av[i] = sA[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) bv[j] = sB[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] += av[i] * bv[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int gm = m0 + ty + 16 * i;
+    if (gm >= a.K) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int gn = n0 + tx + 16 * j;
+      if (gn < a.N) Out[(size_t)gm * a.N + gn] = acc[i][j];
+    }
+  }
+}
+
+}  // namespace
+
+void launch_fold_f64(const FoldArgs &a, cudaStream_t st) {
+  if (a.batch <= 0) return;
+  dim3 grid((a.N + TN - 1) / TN, (a.K + TM - 1) / TM, a.batch);
+  fold_f64_kernel<<<grid, 256, 0, st>>>(a);
+}
+
+}  // namespace xg

@@ -1,0 +1,633 @@
+// integrator.cu -- K2+K3: the cell-mesh integrator for azimuthally invariant
+// hot regions, replacing
+// xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-665 with the
+// blackbody (hot_BB.pyx:54-98) and numerical 4-D (hot_Num4D.pyx:248-461)
+// atmospheres.
+//
+// Work decomposition (one CTA per chunk of consecutive parallels of one mesh):
+//   1. leaf geometry, one thread per leaf pair (k, N_L-1-k): image deflection,
+//      cos alpha / lag / d cos alpha from the Steffen ray tables, Doppler and
+//      aberration factors (:342-441);
+//   2. one thread runs the sequential visibility state machine that fills the
+//      phase knots through invisible intervals (:480-549) and records, per
+//      profile column, which leaf's radiation it carries (or zero);
+//   3. per chunk of energies: the specific intensities of every column
+//      (:445-478) -> Akima-periodic piece coefficients in shared memory
+//      (:566-569) -> every (phase, cell) thread-task evaluates the piece once
+//      per energy and accumulates A_ij * max(S, 0) (:571-598) in registers;
+//   4. per-chunk partial sums are reduced in a fixed order and divided by
+//      E keV (:605-612), so results are bitwise reproducible run to run.
+//
+// Num4D call history.  The reference evaluator keeps its stencil base node
+// between calls and clamps an out-of-table cos(emission angle) only on the
+// call that moves the node (hot_Num4D.pyx:300-351).  mu * eta exceeds the
+// table's mu range on the approaching limb, so for such leaves the first
+// energy is evaluated at the clamped mu = mu_max when the previously
+// evaluated leaf sat below the table's third-to-last mu node, and every
+// other energy extrapolates the last stencil.  The kernels reproduce the
+// reference's single-thread call order exactly: a geometry pre-pass and a
+// per-mesh scan hand each parallel the state its first evaluation sees.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kEPT = 8;  // energies per accumulation task
+
+// Akima piece of one energy row: value at the left knot and the three
+// polynomial coefficients; 32 bytes, read as two 16-byte shared loads.
+struct __align__(16) Piece {
+  double y, k1, k2, k3;
+};
+
+struct RowCtx {
+  int S1, N_R, J, IO;
+  const double *D, *CA, *LG;  // ray tables of the row
+  int jalt;                   // first ray with deflection > pi/2
+  double radius, Grav_z, cos_gamma, sin_gamma, cos_th, sin_th, th_over_pi, beta, Lorentz;
+  double maxDefl, cos_i, sin_i, inclination;
+  double vec0, vec1;
+};
+
+struct GeoSmem {
+  double *phase, *leafphase, *Z, *ABB, *GEOM;
+  int *src, *calc, *term, *clamp0;
+  int *flags;  // [0] terminate, [1] invisible image, [2] any evaluation, [3] last_top
+};
+
+
+struct MainX { const double *D; __device__ double operator()(int j) const { return D[j]; } };
+struct ArrY { const double *Y; __device__ double operator()(int j) const { return Y[j]; } };
+struct AltX {
+  const double *D; int jalt;
+  __device__ double operator()(int t) const { return cos(D[jalt - t]); }
+};
+struct AltY {
+  const double *Y; int jalt;
+  __device__ double operator()(int t) const { return Y[jalt - t]; }
+};
+
+template <typename XF>
+__device__ __forceinline__ int locate_f(const XF &x, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (x(mid) > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+template <typename XF, typename YF>
+__device__ __forceinline__ void steffen_eval(const XF &x, const YF &y, int n, double v,
+                                             double *val, double *der) {
+  int i = locate_f(x, n, v);
+  Cubic c = steffen_piece(x, y, n, i);
+  if (val) *val = cubic_eval(c, v);
+  if (der) *der = cubic_deriv(c, v);
+}
+
+// per-leaf geometry, integrator_for_azimuthal_invariance.pyx:342-441
+__device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_lim,
+                              const double *leaves, GeoSmem &g) {
+  double cos_psi = c.cos_i * c.cos_th + c.sin_i * c.sin_th * cos(leaves[k]);
+  double psi = image_deflection(I, acos(cos_psi));
+  double sin_psi = sin(psi);
+  if (!are_equal(psi, 0.0) && are_equal(sin_psi, 0.0)) {
+    double _i = (c.cos_i >= 0.0) ? c.inclination + c.inclination * 1.0e-6
+                                 : c.inclination - c.inclination * 1.0e-6;
+    cos_psi = cos(_i) * c.cos_th + sin(_i) * c.sin_th * cos(leaves[k]);
+    psi = image_deflection(I, acos(cos_psi));
+    sin_psi = sin(psi);
+  }
+  const int N_R = c.N_R;
+  MainX mx{c.D};
+  AltX ax{c.D, c.jalt};
+  AltY ay{c.CA, c.jalt};
+  const double alt_xmin = cos(c.D[c.jalt]);
+  int calc = 0, term = 0;
+  double sin_alpha = 0.0, mu = 0.0, cos_a;
+  if (psi <= c.maxDefl) {
+    if (psi < c.D[0] || psi > c.D[N_R - 1]) {
+      term = 1;
+    } else {
+      if (psi <= kHalfPi && cos_psi >= alt_xmin)
+        steffen_eval(ax, ay, c.jalt + 1, cos_psi, &cos_a, nullptr);
+      else
+        steffen_eval(mx, ArrY{c.CA}, N_R, psi, &cos_a, nullptr);
+      sin_alpha = sqrt(1.0 - cos_a * cos_a);
+      mu = cos_a * c.cos_gamma;
+      if (!are_equal(psi, 0.0)) {
+        double cos_delta = (c.cos_i - c.cos_th * cos_psi) / (c.sin_th * sin_psi);
+        if (c.th_over_pi < 0.5) mu = mu + sin_alpha * c.sin_gamma * cos_delta;
+        else mu = mu - sin_alpha * c.sin_gamma * cos_delta;
+      }
+      calc = (mu > 0.0) ? 1 : 0;
+    }
+  }
+  if (calc && !term) {
+    double deriv;
+    if (psi <= kHalfPi && cos_psi >= alt_xmin) {
+      steffen_eval(ax, ay, c.jalt + 1, cos_psi, nullptr, &deriv);
+    } else {
+      steffen_eval(mx, ArrY{c.CA}, N_R, psi, nullptr, &deriv);
+      deriv = exp(log(fabs(deriv)) - log(fabs(sin_psi)));
+    }
+    double plag;
+    steffen_eval(mx, ArrY{c.LG}, N_R, psi, &plag, nullptr);
+    for (int ks = 0; ks < 2; ks++) {
+      if ((0 < k && k < leaf_lim - 1) || (k == 0 && ks == 0) ||
+          (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
+          (k == leaf_lim - 1 && N_L % 2 == 0)) {
+        int kdx = (ks == 0) ? k : N_L - 1 - k;
+        double superlum, eta;
+        if (!are_equal(psi, 0.0)) {
+          double cos_xi = sin_alpha * c.sin_i * sin(leaves[kdx]) / sin_psi;
+          superlum = 1.0 + c.beta * cos_xi;
+          eta = c.Lorentz / superlum;
+        } else {
+          superlum = 1.0;
+          eta = c.Lorentz;
+        }
+        g.Z[kdx] = eta * c.Grav_z;
+        g.ABB[kdx] = mu * eta;
+        g.GEOM[kdx] = mu * fabs(deriv) * c.Grav_z * eta * eta * eta / superlum;
+        g.leafphase[kdx] = leaves[kdx] + plag;
+      }
+    }
+  }
+  g.calc[k] = calc;
+  g.term[k] = term;
+}
+
+// sequential visibility state machine, :480-563.  Runs on one thread.
+// Returns through g.flags: [0] terminate, [1] no visibility in this image.
+// Tracks the Num4D call-history flag `top` (last evaluated mu*eta above the
+// table's third-to-last mu node) and marks columns whose first energy sees a
+// clamped mu.
+__device__ void state_machine(int N_L, int leaf_lim, const double *leaves, GeoSmem &g,
+                              bool num4d, double mu_top3, double mu_max, int &top,
+                              int &any_eval) {
+  int InvisFlag = 2, InvisPhase = 0;
+  double step;
+  int term = 0;
+  for (int m = 0; m < N_L; m++) g.src[m] = -1;
+  for (int k = 0; k < leaf_lim; k++) {
+    if (g.term[k]) { term = 1; break; }
+    if (g.calc[k]) {
+      for (int ks = 0; ks < 2; ks++) {
+        if ((0 < k && k < leaf_lim - 1) || (k == 0 && ks == 0) ||
+            (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
+            (k == leaf_lim - 1 && N_L % 2 == 0)) {
+          int kdx = (ks == 0) ? k : N_L - 1 - k;
+          // the reference writes the knot when it reaches this leaf (:441);
+          // earlier gap fills may have passed over this position
+          g.phase[kdx] = g.leafphase[kdx];
+          g.src[kdx] = kdx;
+          if (num4d) {
+            double a = g.ABB[kdx];
+            g.clamp0[kdx] = (a > mu_max && !top) ? 1 : 0;
+            top = (a > mu_top3) ? 1 : 0;
+          }
+          any_eval = 1;
+        }
+      }
+      if (k == 0) {
+        g.phase[N_L - 1] = g.phase[0] + kTwoPi;
+        g.src[N_L - 1] = g.src[0];
+      } else if (k > 0 && InvisFlag == 2) {
+        step = leaves[k] / (double)k;
+        for (int m = N_L - k; m < N_L; m++) g.phase[m] = g.phase[m - 1] + step;
+        for (int m = N_L - k; m < N_L; m++) g.src[m] = -1;
+        g.phase[0] = g.phase[N_L - 1] - kTwoPi;
+        for (int m = 1; m < k; m++) g.phase[m] = g.phase[m - 1] + step;
+        g.src[0] = -1;
+        for (int m = 1; m < k; m++) g.src[m] = -1;
+      } else if (InvisFlag == 1) {
+        step = g.phase[k] - g.phase[InvisPhase - 1];
+        step = step / (double)(k - InvisPhase + 1);
+        for (int m = InvisPhase; m < k; m++) g.phase[m] = g.phase[m - 1] + step;
+        step = g.phase[N_L - InvisPhase] - g.phase[N_L - 1 - k];
+        step = step / (double)(k - InvisPhase + 1);
+        for (int m = N_L - k; m < N_L - InvisPhase; m++) g.phase[m] = g.phase[m - 1] + step;
+      }
+      InvisFlag = 0;
+    } else {
+      if (InvisFlag == 0) {
+        step = g.phase[N_L - k] - g.phase[k - 1];
+        step = step / (double)(N_L - 2 * k + 1);
+        for (int m = k; m < N_L - k; m++) g.phase[m] = g.phase[m - 1] + step;
+        for (int m = k; m < N_L - k; m++) g.src[m] = -1;
+        InvisFlag = 1;
+        InvisPhase = k;
+      }
+    }
+  }
+  int invis = 0;
+  if (!term) {
+    if (InvisFlag == 2) {
+      invis = 1;
+    } else {
+      for (int m = 1; m < N_L; m++)
+        if (g.phase[m] <= g.phase[m - 1]) { term = 1; break; }
+    }
+  }
+  g.flags[0] = term;
+  g.flags[1] = invis;
+}
+
+__device__ bool load_row(const IntegrateArgs &a, const MemberDesc &M, int64_t row, int i,
+                         RowCtx &c, int *s_J) {
+  // first radiating cell of the parallel (:286-296), found by the first warp
+  const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
+  if (threadIdx.x < 32) {
+    int best = M.S1;
+    for (int j = threadIdx.x; j < M.S1; j += 32)
+      if (rad[j] == 1) { best = min(best, j); break; }
+    for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (threadIdx.x == 0) *s_J = best;
+  }
+  __syncthreads();
+  int J = *s_J;
+  __syncthreads();
+  if (J >= M.S1) return false;
+  c.S1 = M.S1;
+  c.N_R = a.N_R;
+  c.J = J;
+  c.D = a.deflection + row * a.N_R;
+  c.CA = a.cos_alpha + row * a.N_R;
+  c.LG = a.lag + row * a.N_R;
+  // first ray deflected beyond pi/2 (:301-303); the reference's loop is
+  // unbounded, here it stops at the row's last ray
+  int j = 0;
+  while (j < a.N_R - 1 && c.D[j] <= kHalfPi) j++;
+  c.jalt = j;
+  c.radius = a.radius[row];
+  c.Grav_z = sqrt(1.0 - a.u[row]);
+  c.cos_gamma = a.cos_gamma[row];
+  c.sin_gamma = sqrt(1.0 - c.cos_gamma * c.cos_gamma);
+  double th = a.theta0[row];
+  c.cos_th = cos(th);
+  c.sin_th = sin(th);
+  c.th_over_pi = th / kPi;
+  c.beta = c.radius * M.omega * c.sin_th / (kC * c.Grav_z);
+  c.Lorentz = sqrt(1.0 - c.beta * c.beta);
+  c.maxDefl = a.maxDeflection[row];
+  c.inclination = M.inclination;
+  c.cos_i = cos(M.inclination);
+  c.sin_i = sin(M.inclination);
+  c.IO = M.image_order_limit > 0 ? M.image_order_limit : (int)ceil(c.maxDefl / kPi);
+  const double *vec = a.params + (M.cell_off + (int64_t)i * M.S1 + J) * a.n_params;
+  c.vec0 = vec[0];
+  c.vec1 = vec[1];
+  return true;
+}
+
+__device__ __forceinline__ double eval_bb(double E, double vec0) {
+  double temp = (kKB / kKeV) * pow(10.0, vec0);
+  return E * E * E / (exp(E / temp) - 1.0);
+}
+
+__device__ __forceinline__ int stencil_base(const double *g, int n, double v) {
+  // base node of the 4-point stencil around the interval holding v
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (g[mid] > v) hi = mid; else lo = mid;
+  }
+  int b = lo - 1;
+  if (b < 0) b = 0;
+  if (b > n - 4) b = n - 4;
+  return b;
+}
+
+__device__ __forceinline__ void lagrange4(const double *P, int b, double x, double w[4]) {
+  double d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
+  double d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
+  double s0 = 1.0 / (P[b] - P[b + 1]); s0 /= P[b] - P[b + 2]; s0 /= P[b] - P[b + 3];
+  double s1 = 1.0 / (P[b + 1] - P[b]); s1 /= P[b + 1] - P[b + 2]; s1 /= P[b + 1] - P[b + 3];
+  double s2 = 1.0 / (P[b + 2] - P[b]); s2 /= P[b + 2] - P[b + 1]; s2 /= P[b + 2] - P[b + 3];
+  double s3 = 1.0 / (P[b + 3] - P[b]); s3 /= P[b + 3] - P[b + 1]; s3 /= P[b + 3] - P[b + 2];
+  w[0] = d0 * s0; w[1] = d1 * s1; w[2] = d2 * s2; w[3] = d3 * s3;
+}
+
+// hot_Num4D.pyx:248-439 with the stencil the reference's cached walk lands on
+__device__ double eval_num4d(const Atmos4D &A, double E, double mu, bool clamp_mu,
+                             double vec0, double vec1) {
+  double v[4];
+  double E_eff = (kKB / kKeV) * pow(10.0, vec0);
+  v[0] = vec0;
+  v[1] = vec1;
+  v[2] = mu;
+  v[3] = log10(E / E_eff);
+  const double *g[4] = {A.logT, A.logg, A.mu, A.logE};
+  const int n[4] = {A.nT, A.ng, A.nmu, A.nE};
+  int b[4];
+  double w[4][4];
+#pragma unroll
+  for (int d = 0; d < 4; d++) {
+    double x = v[d];
+    if (d != 2) {  // in-table by construction; clamp as the walk would
+      if (x < g[d][0]) x = g[d][0];
+      if (x > g[d][n[d] - 1]) x = g[d][n[d] - 1];
+    } else {
+      if (x > g[2][n[2] - 1] && clamp_mu) x = g[2][n[2] - 1];
+    }
+    v[d] = x;
+    b[d] = stencil_base(g[d], n[d], x);
+    lagrange4(g[d], b[d], x, w[d]);
+  }
+  const int64_t S2 = A.nE, S1 = (int64_t)A.nmu * A.nE, S0 = (int64_t)A.ng * S1;
+  double I = 0.0;
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++)
+      for (int k = 0; k < 4; k++) {
+        const double *row = A.I + (b[0] + i) * S0 + (b[1] + j) * S1 + (b[2] + k) * S2 + b[3];
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+          double t = w[0][i] * w[1][j] * w[2][k] * w[3][l];
+          I += t * __ldg(row + l);
+        }
+      }
+  if (I < 0.0) return 0.0;
+  return I * pow(10.0, 3.0 * v[0]);
+}
+
+struct Layout {
+  int N_L, EC;
+  size_t bytes;
+};
+
+__host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E) {
+  Layout L;
+  L.N_L = N_L;
+  int ec = 8;
+  while (ec < 32 && (long)N_P * (ec * 2 / kEPT) <= kThreads && ec * 2 <= N_E + kEPT) ec *= 2;
+  while (ec > 8 && (size_t)ec * N_L * 32 > 96 * 1024) ec /= 2;
+  L.EC = ec;
+  L.bytes = (size_t)5 * N_L * sizeof(double)      // phase, leafphase, Z, ABB, GEOM
+            + (size_t)ec * N_L * 4 * sizeof(double)  // coefficients
+            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 16;
+  return L;
+}
+
+__device__ GeoSmem carve(char *base, int N_L, int EC, double **coef) {
+  GeoSmem g;
+  double *d = reinterpret_cast<double *>(base);
+  g.phase = d; d += N_L;
+  g.leafphase = d; d += N_L;
+  g.Z = d; d += N_L;
+  g.ABB = d; d += N_L;
+  g.GEOM = d; d += N_L;
+  d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(d) + 15) & ~uintptr_t(15));
+  *coef = d; d += (size_t)EC * N_L * 4;
+  int *ip = reinterpret_cast<int *>(d);
+  g.src = ip; ip += N_L;
+  g.calc = ip; ip += N_L;
+  g.term = ip; ip += N_L;
+  g.clamp0 = ip; ip += N_L;
+  g.flags = ip;
+  return g;
+}
+
+// ---------------------------------------------------------------------------
+// Pre-pass for Num4D: per parallel, does it evaluate the atmosphere, and does
+// its last evaluation leave the mu stencil at the top of the table?
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) num4d_prepass_kernel(IntegrateArgs a) {
+  extern __shared__ __align__(16) char smem[];
+  const int64_t row = blockIdx.x;
+  const int m = a.row_member[row];
+  const MemberDesc M = a.members[m];
+  const int i = (int)(row - M.row_off);
+  const int N_L = a.N_L;
+  const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
+  Layout L = make_layout(N_L, a.N_P, a.N_E);
+  double *coef;
+  GeoSmem g = carve(smem, N_L, 0, &coef);
+  __shared__ int s_J, s_any, s_top;
+  RowCtx c;
+  if (threadIdx.x == 0) { s_any = 0; s_top = 0; }
+  if (!load_row(a, M, row, i, c, &s_J)) {
+    if (threadIdx.x == 0) { a.row_has_eval[row] = 0; a.row_last_top[row] = 0; }
+    return;
+  }
+  (void)L;
+  const double mu_max = a.atmos.mu[a.atmos.nmu - 1], mu_top3 = a.atmos.mu[a.atmos.nmu - 3];
+  for (int I = 0; I < c.IO; I++) {
+    for (int k = threadIdx.x; k < leaf_lim; k += blockDim.x)
+      leaf_geometry(c, I, k, N_L, leaf_lim, a.leaves, g);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int top = s_top, any = s_any;
+      state_machine(N_L, leaf_lim, a.leaves, g, true, mu_top3, mu_max, top, any);
+      s_top = top;
+      s_any = any;
+    }
+    __syncthreads();
+    int stop = g.flags[0] | g.flags[1];
+    __syncthreads();
+    if (stop) break;
+  }
+  if (threadIdx.x == 0) {
+    a.row_has_eval[row] = (uint8_t)s_any;
+    a.row_last_top[row] = (uint8_t)s_top;
+  }
+}
+
+// serial over the parallels of each mesh, in the reference's call order
+__global__ void num4d_scan_kernel(IntegrateArgs a) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.n_members) return;
+  const MemberDesc M = a.members[m];
+  if (M.atm != 2) return;
+  uint8_t carry = 0;
+  for (int i = 0; i < M.S0; i++) {
+    int64_t row = M.row_off + i;
+    a.row_entry_top[row] = carry;
+    if (a.row_has_eval[row]) carry = a.row_last_top[row];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// main integrator kernel: one CTA per chunk of parallels of one mesh
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
+  extern __shared__ __align__(16) char smem[];
+  const int chunk = blockIdx.x;
+  const int64_t r0 = a.chunk_r0[chunk], r1 = a.chunk_r1[chunk];
+  const int m = a.row_member[r0];
+  const MemberDesc M = a.members[m];
+  const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
+  const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
+  const Layout L = make_layout(N_L, N_P, N_E);
+  const int EC = L.EC;
+  double *coef;
+  GeoSmem g = carve(smem, N_L, EC, &coef);
+  Piece *co4 = reinterpret_cast<Piece *>(coef);
+  __shared__ int s_J, s_top, s_any;
+  const bool num4d = (M.atm == 2);
+  const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
+  double *part = a.partial + (size_t)chunk * N_E * N_P;
+  const double mu_max = num4d ? a.atmos.mu[a.atmos.nmu - 1] : 0.0;
+  const double mu_top3 = num4d ? a.atmos.mu[a.atmos.nmu - 3] : 0.0;
+  const int groups = EC / kEPT;
+  const int ntasks = N_P * groups;
+
+  for (int64_t row = r0; row < r1; row++) {
+    const int i = (int)(row - M.row_off);
+    RowCtx c;
+    if (!load_row(a, M, row, i, c, &s_J)) continue;
+    if (threadIdx.x == 0) {
+      s_top = num4d ? (int)a.row_entry_top[row] : 0;
+      s_any = 0;
+    }
+    __syncthreads();
+    const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
+    const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
+    const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
+    for (int I = 0; I < c.IO; I++) {
+      for (int k = threadIdx.x; k < leaf_lim; k += blockDim.x)
+        leaf_geometry(c, I, k, N_L, leaf_lim, a.leaves, g);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int top = s_top, any = s_any;
+        state_machine(N_L, leaf_lim, a.leaves, g, num4d, mu_top3, mu_max, top, any);
+        s_top = top;
+        s_any = any;
+      }
+      __syncthreads();
+      const int term = g.flags[0], invis = g.flags[1];
+      if (term) {
+        if (threadIdx.x == 0) atomicExch(&a.member_status[m], (int)kPulseFail);
+        return;
+      }
+      if (invis) break;
+
+      for (int e0 = 0; e0 < N_E; e0 += EC) {
+        const int ne = min(EC, N_E - e0);
+        // specific intensities of every profile column (:445-478)
+        for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+          const int pl = t / N_L, col = t - pl * N_L;
+          const int p = e0 + pl;
+          const int s = g.src[col];
+          double y = 0.0;
+          if (s >= 0) {
+            const double Ep = a.energies[p] / g.Z[s];
+            double I_E;
+            if (num4d)
+              I_E = eval_num4d(a.atmos, Ep, g.ABB[s], p == 0 && g.clamp0[s], c.vec0, c.vec1);
+            else
+              I_E = eval_bb(Ep, c.vec0);
+            y = (I_E * norm - 0.0) * g.GEOM[s];
+          }
+          co4[pl * N_L + col].y = y;
+        }
+        __syncthreads();
+        // Akima-periodic piece coefficients (:566-569)
+        for (int t = threadIdx.x; t < ne * (N_L - 1); t += blockDim.x) {
+          const int pl = t / (N_L - 1), iv = t - pl * (N_L - 1);
+          const Piece *yr = co4 + pl * N_L;
+          double mch[5];
+#pragma unroll
+          for (int d = 0; d < 5; d++) {
+            int q = periodic_chord(iv - 2 + d, N_L);
+            mch[d] = (yr[q + 1].y - yr[q].y) / (g.phase[q + 1] - g.phase[q]);
+          }
+          double k1, k2, k3;
+          akima_piece(mch[0], mch[1], mch[2], mch[3], mch[4], g.phase[iv + 1] - g.phase[iv], k1,
+                      k2, k3);
+          Piece *o = co4 + pl * N_L + iv;
+          o->k1 = k1;
+          o->k2 = k2;
+          o->k3 = k3;
+        }
+        __syncthreads();
+        // cell x phase accumulation (:571-598)
+        const double x_lo = g.phase[0], x_hi = g.phase[N_L - 1];
+        for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
+          const int k = task % N_P, grp = task / N_P;
+          const int pb = grp * kEPT;
+          if (pb >= ne) continue;
+          double acc[kEPT];
+#pragma unroll
+          for (int e = 0; e < kEPT; e++) acc[e] = 0.0;
+          const double ph = a.phases[k];
+          int bad = 0;
+          for (int j = 0; j < M.S1; j++) {
+            if (rad[j] != 1) continue;
+            double x = ph + cellPhi[j];
+            if (x > x_hi) {
+              while (x > x_hi) x = x - kTwoPi;
+            } else if (x < x_lo) {
+              while (x < x_lo) x = x + kTwoPi;
+            }
+            if (x < x_lo || x > x_hi) { bad = 1; break; }
+            const int iv = locate(g.phase, N_L, x);
+            const double t = x - g.phase[iv];
+            const double A = cellA[j];
+#pragma unroll
+            for (int e = 0; e < kEPT; e++) {
+              if (pb + e < ne) {
+                const Piece q = co4[(pb + e) * N_L + iv];
+                const double s = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
+                if (s > 0.0) acc[e] += A * s;
+              }
+            }
+          }
+          if (bad) {
+            atomicExch(&a.member_status[m], (int)kPulseFail);
+            continue;
+          }
+#pragma unroll
+          for (int e = 0; e < kEPT; e++)
+            if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += acc[e];
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// ordered reduction of the chunk partials and the 1/(E keV) factor (:605-612)
+__global__ void reduce_flux_kernel(IntegrateArgs a) {
+  const int m = blockIdx.y;
+  const MemberDesc M = a.members[m];
+  const int n = a.N_E * a.N_P;
+  const int c0 = a.chunk_first[m], c1 = a.chunk_first[m + 1];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = c0; c < c1; c++) s += a.partial[(size_t)c * n + t];
+    const int p = t / a.N_P;
+    a.flux[M.flux_off + t] = s / (a.energies[p] * kKeV);
+  }
+}
+
+}  // namespace
+
+void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
+  if (a.n_members <= 0) return;
+  Layout L = make_layout(a.N_L, a.N_P, a.N_E);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+    attr_set = true;
+  }
+  bool any_num4d = a.atmos.I != nullptr;
+  if (any_num4d) {
+    size_t pre_smem = (size_t)5 * a.N_L * sizeof(double) + (size_t)4 * a.N_L * sizeof(int) +
+                      8 * sizeof(int) + 16;
+    num4d_prepass_kernel<<<(unsigned)a.n_rows, 128, pre_smem, st>>>(a);
+    num4d_scan_kernel<<<(a.n_members + 127) / 128, 128, 0, st>>>(a);
+  }
+  integrate_kernel<<<a.n_chunks, kThreads, L.bytes, st>>>(a);
+  dim3 grid((a.N_E * a.N_P + 255) / 256, a.n_members);
+  reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
+}
+
+}  // namespace xg

@@ -1,0 +1,125 @@
+// kernels.h -- argument blocks and launchers of the pulse-likelihood kernels.
+// Every pointer here is a DEVICE pointer; host staging lives in abi.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xg {
+
+constexpr int kMaxImages = 8;  // image orders tracked per parallel
+
+// ---- K1 rays ----------------------------------------------------------
+struct RaysArgs {
+  int n_rows, N_R;
+  const double *u;        // [rows] r_s / r of the parallel
+  const double *r_s_row;  // [rows] Schwarzschild radius (m)
+  double *maxAlpha;       // [rows] in/out (clamped, rays.pyx:317-318)
+  double *deflection, *cos_alpha, *lag;  // [rows][N_R]
+  double *maxDeflection;  // [rows]
+  int32_t *row_status;    // [rows] or null
+  const double *lag_C;     // [rows] lag calibration offset (s) or null
+  const double *lag_scale; // [rows] 2 pi f_mode
+};
+void launch_rays(const RaysArgs &a, cudaStream_t st);
+
+// ---- K2/K3 integrator ----------------------------------------------------
+// One "member" is one cell mesh (a hot region's superseding or ceding part)
+// of one parameter vector.  Rows of all members are packed: member m owns
+// global rows [row_off, row_off + S0) and cells [cell_off, cell_off + S0*S1).
+struct MemberDesc {
+  int32_t S0, S1;
+  int64_t row_off, cell_off;
+  double omega, inclination;
+  int32_t image_order_limit;  // 0: infer from the maximum deflection
+  int32_t atm;                // 1 blackbody, 2 numerical 4-D table
+  int64_t flux_off;           // offset of this member's [N_E][N_P] flux
+};
+
+struct Atmos4D {
+  const double *logT, *logg, *mu, *logE, *I;
+  int nT, ng, nmu, nE;
+};
+
+struct IntegrateArgs {
+  int n_members;
+  int64_t n_rows;
+  const MemberDesc *members;
+  // per packed row
+  const int32_t *row_member;
+  const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;
+  const double *deflection, *cos_alpha, *lag;  // [rows][N_R], lag calibrated
+  int N_R;
+  // per packed cell
+  const double *cellArea, *phi, *params;  // params [cells][n_params]
+  int n_params;
+  const int32_t *radiates;
+  // shared grids
+  int N_E, N_L, N_P;
+  const double *energies, *leaves, *phases;
+  Atmos4D atmos;
+  // work chunks: chunk c covers rows [chunk_r0[c], chunk_r1[c]) of one member
+  int n_chunks;
+  const int64_t *chunk_r0, *chunk_r1;
+  double *partial;          // [n_chunks][N_E][N_P]
+  const int32_t *chunk_first;  // [n_members + 1] first chunk of each member
+  // Num4D call-history state (see integrator.cu)
+  uint8_t *row_has_eval, *row_last_top, *row_entry_top;  // [rows]
+  int32_t *member_status;   // [n_members]
+  double *flux;             // [..] at members[m].flux_off
+};
+void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
+
+// ---- K4 energy integrator ------------------------------------------------
+struct EnergyArgs {
+  int n_signals;        // number of [N_E][N_P] inputs
+  int N_E, N_P, n_edges;
+  const double *signal;      // [n_signals][N_E][N_P]
+  const int64_t *in_off;     // [n_signals] element offset of each signal
+  const double *logE;        // [N_E]
+  const double *logEdges;    // [n_edges]
+  double scale;              // multiplies the signal (1 / d^2 folded in)
+  const double *scale_per;   // [n_signals] or null
+  double *out;               // [n_signals][n_edges-1][N_P] at out_off
+  const int64_t *out_off;
+  int accumulate;            // add into out instead of storing
+};
+void launch_energy(const EnergyArgs &a, cudaStream_t st);
+
+// ---- K5 response fold -----------------------------------------------------
+// out[b][K][N] = M[K][q] @ in[b][q][N] in FP64
+struct FoldArgs {
+  int batch, K, q, N;
+  const double *M;  // [K][ldM], columns [0, q)
+  int ldM;
+  const double *in;  // [batch][q][N]
+  double *out;       // [batch][K][N]
+};
+void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
+
+// ---- K6 likelihood ----------------------------------------------------------
+struct LikeArgs {
+  int n_vec;             // likelihood evaluations
+  int K, B, H;           // channels, phase bins, components (hot regions)
+  int N_P;               // phases per component signal
+  double exposure, epsabs, epsrel, epsilon, sigmas, llzero, slim;
+  const double *phase_edges;  // [B+1]
+  const double *comp_phases;  // [N_P] phases (cycles) of every component
+  const double *counts;       // [K][B]
+  const double *precomp;      // [K]
+  const double *support;      // [K][2]
+  const double *background;   // [K][B] or null
+  const double *signals;      // [n_vec][H][K][N_P]
+  const double *shifts;       // [n_vec][H]
+  const int32_t *allow_negative;  // [H]
+  double *chan_ll;            // [n_vec][K] per-channel log-likelihood terms
+  int32_t *chan_flag;         // [n_vec][K] 0 ok, 1 slim cut, 2 vanished integral
+  double *star;               // [n_vec][K][B] or null
+  double *mcl_bg, *mcl_bg_s;  // [n_vec][K] or null
+  double *loglike;            // [n_vec]
+  int32_t *status;            // [n_vec]
+};
+void launch_likelihood(const LikeArgs &a, cudaStream_t st);
+void launch_precomputation(int K, int B, const int32_t *counts, double *out, cudaStream_t st);
+
+}  // namespace xg

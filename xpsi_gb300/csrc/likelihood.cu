@@ -1,0 +1,461 @@
+// likelihood.cu -- K6: expected counts per phase bin and the background-
+// marginalised Poisson log-likelihood, replacing
+//   xpsi/tools/compute_expected_counts.pyx:66-197 and
+//   xpsi/likelihoods/default_background_marginalisation.pyx:38-734.
+//
+// One warp per (likelihood evaluation, channel).  Lanes integrate the
+// Akima-periodic phase interpolant of each component over their phase bins;
+// the scalar Newton / window logic is replicated in every lane (all lanes see
+// identical values, so control flow stays warp-uniform) and the marginal
+// integral is a QUADPACK-style adaptive Gauss-Kronrod-21 quadrature run to
+// relative 1e-13 whose 21 node evaluations per panel are spread over the
+// lanes.  The reference's CQUAD call (:416-419) asks for relative 1e-8 on
+// this smooth integrand, so both converge to the same integral.  The channel
+// terms are summed per evaluation in channel order by a second kernel, which
+// also applies the reference's early exits (slim cut :677-684, vanished
+// integral :423-429).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace xg {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kMaxB = 64;      // phase bins per channel held in shared memory
+constexpr int kQagLimit = 256; // interval list of the marginal quadrature
+
+struct WarpSmem {
+  double star[kMaxB];
+  double data[kMaxB];
+  double fv[42];
+  double al[kQagLimit], bl[kQagLimit], rl[kQagLimit], el[kQagLimit];
+};
+
+// integral of the Akima-periodic interpolant through (x[i], y[i]) over [lo, hi]
+__device__ double akima_periodic_integral(const double *x, const double *y, int n, double lo,
+                                          double hi) {
+  if (lo > hi || lo < x[0] || hi > x[n - 1]) return nan("");
+  if (lo == hi) return 0.0;
+  auto chord = [&](int j) -> double {
+    int q = periodic_chord(j, n);
+    return (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
+  };
+  int ia = locate(x, n, lo), ib = locate(x, n, hi);
+  double acc = 0.0;
+  for (int i = ia; i <= ib; i++) {
+    double h = x[i + 1] - x[i];
+    double k1, k2, k3;
+    akima_piece(chord(i - 2), chord(i - 1), chord(i), chord(i + 1), chord(i + 2), h, k1, k2, k3);
+    double u = (i == ia) ? lo - x[i] : 0.0;
+    double w = (i == ib) ? hi - x[i] : h;
+    acc += piece_integral(y[i], k1, k2, k3, u, w);
+  }
+  return acc;
+}
+
+struct Marg {
+  int n;
+  double SCALE, T, A;
+  const double *data, *star;
+};
+
+// :84-138
+__device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
+  double x = 0.0;
+  for (int j = 0; j < m.n; j++) {
+    double c = m.SCALE * (m.star[j] + B);
+    if (c > 0.0) x += m.data[j] * log(c) - c;
+    else if (are_equal(c, 0.0) && are_equal(m.data[j], 0.0)) {}
+    else return 0.0;
+  }
+  return exp(x - m.A);
+}
+
+// :140-173 (returns the step; writes the Gaussian width)
+__device__ __forceinline__ double newton_delta(const Marg &m, double B, double &std) {
+  double x = 0.0, y = 0.0;
+  for (int j = 0; j < m.n; j++) {
+    y += m.data[j] / (m.star[j] + B);
+    x += m.data[j] / pow(m.star[j] + B, 2.0);
+  }
+  y = 2.0 * m.T - 2.0 * y;
+  x *= 2.0;
+  std = sqrt(2.0 / x);
+  return -1.0 * y / x;
+}
+
+// panel sums of the 21-point rule from the node values fv[0..20]:
+// nodes 0..9 at c - h X[j], 10 at c, 11..20 at c + h X[j]
+__device__ void gk21_sums(const double *fv, double a, double b, double &res, double &err,
+                          double &rabs, double &rasc) {
+  const int NH = XG_K21_HALF - 1;
+  double h = 0.5 * (b - a), ah = fabs(h);
+  double fc = fv[NH];
+  double rk = XG_K21_WK[NH] * fc, rg = XG_K21_WG[NH] * fc, ra = fabs(rk);
+  for (int j = 0; j < NH; j++) {
+    double f1 = fv[j], f2 = fv[NH + 1 + j];
+    rk += XG_K21_WK[j] * (f1 + f2);
+    rg += XG_K21_WG[j] * (f1 + f2);
+    ra += XG_K21_WK[j] * (fabs(f1) + fabs(f2));
+  }
+  double mean = 0.5 * rk;
+  double rc = XG_K21_WK[NH] * fabs(fc - mean);
+  for (int j = 0; j < NH; j++)
+    rc += XG_K21_WK[j] * (fabs(fv[j] - mean) + fabs(fv[NH + 1 + j] - mean));
+  res = rk * h;
+  ra *= ah;
+  rc *= ah;
+  double e = fabs((rk - rg) * h);
+  if (rc != 0.0 && e != 0.0) {
+    double sc = pow(200.0 * e / rc, 1.5);
+    e = sc < 1.0 ? rc * sc : rc;
+  }
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  if (ra > dmin / (50.0 * eps)) {
+    double fl = 50.0 * eps * ra;
+    if (fl > e) e = fl;
+  }
+  err = e;
+  rabs = ra;
+  rasc = rc;
+}
+
+__device__ __forceinline__ double gk21_node(double a, double b, int n) {
+  const int NH = XG_K21_HALF - 1;
+  double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  if (n < NH) return c - h * XG_K21_X[n];
+  if (n == NH) return c;
+  return c + h * XG_K21_X[n - NH - 1];
+}
+
+// two panels [a1,b1], [a2,b2] (the second optional) evaluated by the warp
+__device__ void warp_panels(const Marg &m, WarpSmem &w, int lane, double a1, double b1,
+                            double a2, double b2, bool two) {
+  const int total = two ? 42 : 21;
+  for (int t = lane; t < total; t += 32) {
+    double x = (t < 21) ? gk21_node(a1, b1, t) : gk21_node(a2, b2, t - 21);
+    w.fv[t] = marginal_integrand(m, x);
+  }
+  __syncwarp();
+}
+
+// adaptive GK21 (same scheme as the rays' QAG), warp-cooperative; a < b
+__device__ double warp_qag21_core(const Marg &m, WarpSmem &w, int lane, double a, double b,
+                                  double epsabs, double er) {
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  double r0, e0, ra0, rc0;
+  warp_panels(m, w, lane, a, b, 0, 0, false);
+  gk21_sums(w.fv, a, b, r0, e0, ra0, rc0);
+  __syncwarp();
+  double tol = fmax(epsabs, er * fabs(r0));
+  double rfloor = 50.0 * eps * ra0;
+  if ((e0 <= rfloor && e0 > tol) || (e0 <= tol && e0 != rc0) || e0 == 0.0) return r0;
+  if (lane == 0) { w.al[0] = a; w.bl[0] = b; w.rl[0] = r0; w.el[0] = e0; }
+  __syncwarp();
+  int size = 1, iter = 1, k = 0, rnd1 = 0, rnd2 = 0, fail = 0;
+  double area = r0, errsum = e0;
+  do {
+    double ai = w.al[k], bi = w.bl[k], ri = w.rl[k], ei = w.el[k];
+    double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
+    warp_panels(m, w, lane, a1, b1, a2, b2, true);
+    double r1, e1, ra1, rc1, r2, e2, ra2, rc2;
+    gk21_sums(w.fv, a1, b1, r1, e1, ra1, rc1);
+    gk21_sums(w.fv + 21, a2, b2, r2, e2, ra2, rc2);
+    __syncwarp();
+    double r12 = r1 + r2, e12 = e1 + e2;
+    errsum += e12 - ei;
+    area += r12 - ri;
+    if (rc1 != e1 && rc2 != e2) {
+      double delta = ri - r12;
+      if (fabs(delta) <= 1.0e-5 * fabs(r12) && e12 >= 0.99 * ei) rnd1++;
+      if (iter >= 10 && e12 > ei) rnd2++;
+    }
+    tol = fmax(epsabs, er * fabs(area));
+    if (errsum > tol) {
+      if (rnd1 >= 6 || rnd2 >= 20) fail = 2;
+      double edge = (1.0 + 100.0 * eps) * (fabs(a2) + 1000.0 * dmin);
+      if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
+    }
+    int nw = size++;
+    if (lane == 0) {
+      if (e2 > e1) {
+        w.al[k] = a2; w.bl[k] = b2; w.rl[k] = r2; w.el[k] = e2;
+        w.al[nw] = a1; w.bl[nw] = b1; w.rl[nw] = r1; w.el[nw] = e1;
+      } else {
+        w.al[k] = a1; w.bl[k] = b1; w.rl[k] = r1; w.el[k] = e1;
+        w.al[nw] = a2; w.bl[nw] = b2; w.rl[nw] = r2; w.el[nw] = e2;
+      }
+    }
+    __syncwarp();
+    k = 0;
+    for (int i = 1; i < size; i++)
+      if (w.el[i] > w.el[k]) k = i;
+    iter++;
+  } while (iter < kQagLimit && !fail && errsum > tol);
+  double sum = 0.0;
+  for (int i = 0; i < size; i++) sum += w.rl[i];
+  __syncwarp();
+  return sum;
+}
+
+// dyadic pieces toward an endpoint holding all the mass (see warp_marginal)
+__device__ double warp_dyadic(const Marg &m, WarpSmem &w, int lane, double lo, double hi,
+                              bool toward_lo, double er) {
+  const double L = hi - lo;
+  double sum = 0.0;
+  int seen = 0, quiet_after = 0;
+  for (int k = 0; k < 2100; k++) {
+    double s1 = ldexp(L, -(k + 1)), s0 = ldexp(L, -k);
+    double p0 = toward_lo ? lo + s1 : hi - s0;
+    double p1 = toward_lo ? lo + s0 : hi - s1;
+    if (!(p0 < p1) || (toward_lo ? p0 <= lo : p1 >= hi)) break;
+    double r = warp_qag21_core(m, w, lane, p0, p1, 0.0, er);
+    sum += r;
+    if (r != 0.0) seen = 1;
+    if (seen && fabs(r) <= 1.0e-17 * fabs(sum)) {
+      if (++quiet_after >= 4) break;
+    } else {
+      quiet_after = 0;
+    }
+  }
+  return sum;
+}
+
+// the marginal integral over [a, b]: adaptive GK21 at relative
+// min(epsrel, 1e-13); when every interior node sees zero but an endpoint
+// does not (a channel without counts has a window ~1e91 wide whose integrand
+// decays on the scale 1 / exposure), the window is cut into dyadic pieces
+// toward that endpoint, as a Clenshaw-Curtis rule with endpoint nodes would
+// resolve it.
+__device__ double warp_marginal(const Marg &m, WarpSmem &w, int lane, double a, double b,
+                                double epsabs, double epsrel) {
+  const double eps = 2.220446049250313e-16;
+  double sign = 1.0;
+  if (b < a) { double t = a; a = b; b = t; sign = -1.0; }
+  if (a == b) return 0.0;
+  double er = epsrel < 1.0e-13 ? epsrel : 1.0e-13;
+  if (epsabs <= 0.0 && er < 50.0 * eps) er = 50.0 * eps;
+  double r = warp_qag21_core(m, w, lane, a, b, epsabs, er);
+  if (r == 0.0) {
+    double fa = marginal_integrand(m, a), fb = marginal_integrand(m, b);
+    if (fa != 0.0 || fb != 0.0) {
+      double mid = 0.5 * (a + b);
+      double rl = (fa != 0.0) ? warp_dyadic(m, w, lane, a, mid, true, er)
+                              : warp_qag21_core(m, w, lane, a, mid, 0.0, er);
+      double rr = (fb != 0.0) ? warp_dyadic(m, w, lane, mid, b, false, er)
+                              : warp_qag21_core(m, w, lane, mid, b, 0.0, er);
+      r = rl + rr;
+    }
+  }
+  return sign * r;
+}
+
+__global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
+  __shared__ WarpSmem ws[kWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long gw = (long)blockIdx.x * kWarps + wid;
+  if (gw >= (long)a.n_vec * a.K) return;
+  const int v = (int)(gw / a.K), ch = (int)(gw % a.K);
+  WarpSmem &w = ws[wid];
+  const int B = a.B, N_P = a.N_P;
+  const double n = (double)B;
+  const double SCALE = a.exposure / n;
+  const double T = a.exposure;
+  // expected star count rate per phase bin (compute_expected_counts.pyx:66-197)
+  for (int j = lane; j < B; j += 32) {
+    double st = 0.0;
+    for (int h = 0; h < a.H; h++) {
+      const double *pulse = a.signals + (((size_t)v * a.H + h) * a.K + ch) * N_P;
+      const double sh = a.shifts[(size_t)v * a.H + h];
+      const bool neg = a.allow_negative[h] == 1;
+      if (N_P > 1) {
+        double pa = a.phase_edges[j] + sh, pb = a.phase_edges[j + 1] + sh;
+        if (are_equal(pb - pa, 1.0)) { pa = 0.0; pb = 1.0; }
+        else { pa -= floor(pa); pb -= floor(pb); }
+        double val;
+        if (pa < pb) {
+          val = akima_periodic_integral(a.comp_phases, pulse, N_P, pa, pb);
+          if (val > 0.0 || neg) st += val;
+        } else {
+          val = akima_periodic_integral(a.comp_phases, pulse, N_P, pa, 1.0);
+          if (val > 0.0 || neg) st += val;
+          val = akima_periodic_integral(a.comp_phases, pulse, N_P, 0.0, pb);
+          if (val > 0.0 || neg) st += val;
+        }
+      } else if (j == 0) {
+        st = pulse[0];
+      }
+    }
+    if (st < 0.0) st = 0.0;
+    if (a.background) st += a.background[(size_t)ch * B + j];
+    st *= n;
+    w.star[j] = st;
+    w.data[j] = a.counts[(size_t)ch * B + j];
+  }
+  __syncwarp();
+  double av_STAR = 0.0, av_DATA = 0.0;
+  for (int j = 0; j < B; j++) {
+    av_STAR += w.star[j];
+    av_DATA += w.data[j];
+  }
+  const size_t o = (size_t)v * a.K + ch;
+  int flag = 0;
+  double term = 0.0, Bout = 0.0;
+  if (a.slim >= 0.0) {
+    double limit = av_STAR * SCALE - a.slim * sqrt(av_STAR * SCALE) - av_DATA;
+    if (limit > 0.0) flag = 1;
+  }
+  const double *support = a.support + 2 * (size_t)ch;
+  Marg m{B, SCALE, T, 0.0, w.data, w.star};
+  double Bfinal = 0.0;
+  if (!flag) {
+    av_STAR /= n;
+    av_DATA /= T;
+    double Bv;
+    if (are_equal(av_DATA, 0.0) && are_equal(av_STAR, 0.0)) {
+      double lower = 0.0;
+      if (lower < support[0]) lower = support[0];
+      double upper = 10.0 / T;
+      if (upper > support[1] && support[1] > 0.0) upper = support[1];
+      Bv = 0.0;
+      term = log((exp(-1.0 * lower * T) - exp(-1.0 * upper * T)) / T);
+    } else {
+      double B_min = 0.0;
+      Bv = av_DATA - av_STAR;
+      if (Bv <= B_min) {
+        double min_counts = -1.0;
+        for (int j = 0; j < B; j++)
+          if (are_equal(w.star[j], 0.0)) { min_counts = -2.0; break; }
+        if (are_equal(min_counts, -2.0)) {
+          for (int j = 0; j < B; j++)
+            if ((are_equal(min_counts, -2.0) && w.data[j] > 0.0) ||
+                (0.0 < w.data[j] && w.data[j] < min_counts))
+              min_counts = w.data[j];
+        }
+        if (!are_equal(min_counts, -1.0)) {
+          if (are_equal(min_counts, -2.0)) { Bv = 0.0; B_min = 0.0; }
+          else { Bv = 0.01 * min_counts / SCALE; B_min = 0.1 * Bv; }
+        } else {
+          Bv = B_min;
+        }
+      }
+      double stdv;
+      double dB = newton_delta(m, Bv, stdv);
+      int counter = 0, steps = 0;
+      // the reference's Newton loop (:336-352) has no step limit; 10000 steps
+      // bound it here (convergence takes a handful)
+      while (fabs(dB) > a.epsilon * stdv && counter < 2 && steps++ < 10000) {
+        Bv += dB;
+        if (Bv < B_min) {
+          if (B_min > 0.0) counter += 1;
+          else counter = 2;
+          Bv = B_min;
+        }
+        dB = newton_delta(m, Bv, stdv);
+      }
+      double std_est = 0.0;
+      for (int j = 0; j < B; j++) std_est += w.data[j] / pow(w.star[j] + Bv, 2.0);
+      if (std_est > 0.0) std_est = sqrt(1.0 / std_est);
+      else std_est = 1e90;
+      double lower = Bv - a.sigmas * std_est, upper = Bv + a.sigmas * std_est;
+      if (lower < B_min) lower = B_min;
+      double Bi = Bv;
+      if (lower < support[0]) {
+        lower = support[0];
+        if (upper < support[0] && support[1] > 0.0) { upper = support[1]; Bi = support[0]; }
+        else if (upper < support[0]) { upper = support[0] + a.sigmas * std_est; Bi = support[0]; }
+      }
+      if (upper > support[1] && support[1] > 0.0) {
+        upper = support[1];
+        if (lower > support[1]) { lower = support[0]; Bi = support[1]; }
+      }
+      if (Bi < lower) Bi = lower;
+      else if (Bi > upper) Bi = upper;
+      double A = 0.0;
+      for (int j = 0; j < B; j++) {
+        double c = SCALE * (w.star[j] + Bi);
+        if (c > 0.0) A += w.data[j] * log(c) - c;
+        else if (are_equal(c, 0.0) && are_equal(w.data[j], 0.0)) {}
+        else A += a.llzero;
+      }
+      m.A = A;
+      double result = warp_marginal(m, w, lane, lower, upper, a.epsabs, a.epsrel);
+      if (result > 0.0) term = log(result) + A + a.precomp[ch];
+      else flag = 2;
+    }
+    Bfinal = Bv;
+    Bout = Bv;
+  }
+  if (lane == 0) {
+    a.chan_ll[o] = term;
+    a.chan_flag[o] = flag;
+    if (a.mcl_bg && flag == 0) {
+      a.mcl_bg[o] = Bout * T;
+      double Bs = Bout;
+      if (Bs < support[0]) Bs = support[0];
+      else if (Bs > support[1] && support[1] > 0.0) Bs = support[1];
+      a.mcl_bg_s[o] = Bs * T;
+    }
+  }
+  if (a.star) {
+    for (int j = lane; j < B; j += 32) {
+      double s = w.star[j];
+      if (flag == 0) s = SCALE * (s + Bfinal);
+      a.star[o * B + j] = s;
+    }
+  }
+}
+
+// channel-ordered sum and the reference's early exits
+__global__ void like_finalize_kernel(LikeArgs a) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.n_vec) return;
+  double LL = 0.0;
+  int st = kOk;
+  for (int ch = 0; ch < a.K; ch++) {
+    size_t o = (size_t)v * a.K + ch;
+    int f = a.chan_flag[o];
+    if (f != 0) {
+      // llzero * (0.1 + 0.9 U): U from a hash of (evaluation, channel)
+      uint32_t hsh = (uint32_t)v * 2654435761u ^ (uint32_t)ch * 40503u ^ 0x9e3779b9u;
+      hsh ^= hsh >> 16; hsh *= 0x7feb352du; hsh ^= hsh >> 15; hsh *= 0x846ca68bu; hsh ^= hsh >> 16;
+      double U = (double)(hsh >> 8) / 16777215.0;
+      LL = a.llzero * (0.1 + 0.9 * U);
+      st = (f == 1) ? kSlimCut : kQuadFail;
+      break;
+    }
+    LL += a.chan_ll[o];
+  }
+  a.loglike[v] = LL;
+  a.status[v] = st;
+}
+
+}  // namespace
+
+void launch_likelihood(const LikeArgs &a, cudaStream_t st) {
+  long warps = (long)a.n_vec * a.K;
+  if (warps <= 0) return;
+  unsigned blocks = (unsigned)((warps + kWarps - 1) / kWarps);
+  like_channel_kernel<<<blocks, 32 * kWarps, 0, st>>>(a);
+  like_finalize_kernel<<<(a.n_vec + 127) / 128, 128, 0, st>>>(a);
+}
+
+}  // namespace xg
+
+namespace xg {
+namespace {
+// default_background_marginalisation.pyx:38-68: -sum_j ln(d_ij!)
+__global__ void precomp_kernel(int K, int B, const int32_t *counts, double *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  double s = 0.0;
+  for (int j = 0; j < B; j++) s += lgamma((double)(uint32_t)counts[(size_t)i * B + j] + 1.0);
+  out[i] = -s;
+}
+}  // namespace
+
+void launch_precomputation(int K, int B, const int32_t *counts, double *out, cudaStream_t st) {
+  if (K <= 0) return;
+  precomp_kernel<<<(K + 127) / 128, 128, 0, st>>>(K, B, counts, out);
+}
+}  // namespace xg
