@@ -1,0 +1,344 @@
+"""Throughput benchmark of the pulse-signal likelihood hot path.
+
+Workload (the batched configuration): V parameter vectors drawn from the
+prior (M U(1,3) Msun, R U(3 r_g, 16 km), spin U(200,600) Hz, cos i U(0,1),
+D 1 kpc; two Num4D hot regions, one circular and one with an omitted
+crescent; colatitudes U(0,pi), radii U(0.01,0.5), log T U(5.8,6.6)), model
+resolution sqrt_num_cells 64 (max 128), num_leaves 128, num_rays 1024,
+128 energies; 35x14x67x166 FP64 atmosphere table; 1500 x 128 response;
+32 phase bins; counts drawn from the model of the full-size configuration's
+vector.  A step is one pass of the hot path -- rays, integrator, energy
+integration, response fold, background-marginalised likelihood -- over the
+batch.  Meshes are built on the host before the timed region (both arms).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--vectors V]
+                    [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  --impl reference times the CPU restatement
+of the reference path (oracle/) on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "likelihood evals/s at |ΔlogL|≤1e-3 vs FP64, batched vs plain GPU; p50/p99 latency"
+UNIT = "likelihood evals/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.cmd = ["nvidia-smi", "-i", str(gpu_index),
+                    "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                    "clocks_event_reasons.hw_thermal_slowdown,"
+                    "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                    "--format=csv,noheader,nounits", "-lms", "200"]
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(V, seed_vectors=3):
+    from xpsi_gb300 import synthetic as SY
+    model = SY.config2_model()
+    params = SY.config3_vectors(V, seed=seed_vectors)
+    return model, params
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("XPSI_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gb300(args):
+    import torch
+    from xpsi_gb300 import batch as BT
+    from xpsi_gb300 import synthetic as SY
+    from xpsi_gb300._native import lib
+    rank, world = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    V = args.vectors
+    model, _ = build_workload(1)
+    # data: Poisson draws from the model of the full-size configuration's vector
+    ev = BT.BatchEvaluator(model, device=local)
+    P0 = BT.prepare(model, SY.config2_vector(seed=1)[None, :])
+    B0 = ev.upload(P0)
+    ev.run(B0)
+    torch.cuda.synchronize()
+    folded = B0["folded"].cpu().numpy()
+    SY.attach_data(model, [folded[0], folded[1]], P0.shifts[0])
+    ev = BT.BatchEvaluator(model, device=local)
+    # each rank evaluates its own V vectors (independent parameter vectors)
+    params = SY.config3_vectors(V * world, seed=3)[rank * V:(rank + 1) * V]
+    t0 = time.time()
+    P = BT.prepare(model, params)
+    t_mesh = time.time() - t0
+    B = ev.upload(P)
+    flops = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    # warm-up
+    for _ in range(args.warmup):
+        ev.run(B)
+    torch.cuda.synchronize()
+    # integrator time (CUDA events on the launching stream) and its
+    # algorithmic FLOPs for one step
+    probe = {"flops": flops}
+    ev.run(B, probe=probe)
+    torch.cuda.synchronize()
+    int_ms = probe["start"].elapsed_time(probe["end"])
+    int_flops = float(flops.item())
+    # timed region
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    with clocks:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ev.run(B)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world)
+    st = ev.statuses(B)
+    value = V * world / (ms / 1e3)
+    # end to end through the public API with host buffers: H2D of the packed
+    # inputs (pinned), the five stages, D2H of log L and statuses
+    h2d = ev.h2d_bytes(P)
+    d2h = V * (8 + 4)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Bx = ev.upload(P, pinned=True)
+        ev.run(Bx)
+        ll = Bx["loglike"].cpu()
+        stx = Bx["status"].cpu()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = max_over_ranks(e2e_s, world)
+    pk, pk_kind = peaks()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded prior draws, "
+        "Poisson counts from the model)",
+        "config": {"workload": "batched prior vectors of the full-size plain model "
+                   "(2 Num4D hot regions, one omitted crescent; 64/128 cells, 128 leaves, "
+                   "1024 rays, 128 energies, 1500x128 response, 32 bins)",
+                   "vectors_per_gpu": V, "precision": "plain FP64",
+                   "l2": "inputs and ray tables larger than L2 (129 MB) every step",
+                   "mesh_build_host_s": round(t_mesh, 3),
+                   "status_counts": {str(k): int(v) for k, v in
+                                     zip(*np.unique(st, return_counts=True))}},
+        "e2e": {"value": V * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+    }
+    # kernels launched per step: rays 1, integrator 2 (+2 Num4D pre-pass/scan),
+    # energy 1, fold 1, likelihood 2
+    out["gpu_launches"] = args.steps * (1 + 4 + 1 + 1 + 2)
+    peak64 = fp64_peak(local)
+    achieved = int_flops / (int_ms / 1e3) / 1e12
+    out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64,
+                       "unit": "TFLOP/s", "frac": achieved / peak64 if peak64 else None,
+                       "traffic": None, "kernel": "integrate_kernel",
+                       "kernel_ms": int_ms, "flops_per_launch": int_flops,
+                       "peak_source": "measured FP64 FMA probe on this GPU (not in "
+                       "MEASURED_PEAKS.json)", "hbm_peak_gbs": pk.get("hbm_gbs"),
+                       "hbm_peak_source": pk_kind}
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args, model, params)
+        print(json.dumps(out))
+
+
+def fp64_peak(device):
+    import torch
+    from xpsi_gb300._native import lib
+    buf = torch.zeros(1, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    L = lib()
+    L.xgpu_peak_probe(1, 152 * 8, 256, 64, buf.data_ptr(), st)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fl = L.xgpu_peak_probe(1, 152 * 8, 256, 4096, buf.data_ptr(), st)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, fl / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
+# ------------------------------------------------------------------ CPU legs
+def oracle_evals(model, params, n_threads, budget_s):
+    """Run the oracle over successive vectors until the time budget is used;
+    returns (evaluations, seconds)."""
+    from xpsi_gb300 import batch as BT
+    from oracle import pipeline as OP
+    done, t_total = 0, 0.0
+    for v in range(params.shape[0]):
+        P = BT.prepare(model, params[v:v + 1], n_threads=n_threads)
+        t0 = time.perf_counter()
+        OP.loglike(model, P, n_threads=n_threads)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total >= budget_s:
+            break
+    return done, t_total
+
+
+def cpu_baseline(args, model, params):
+    cores = os.cpu_count() or 1
+    n, t = oracle_evals(model, params, cores, args.cpu_budget)
+    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} of the benchmark's prior vectors through the CPU restatement "
+                      f"(oracle/, OpenMP over parallels, {cores} threads), meshes excluded, "
+                      f"{t:.1f} s"}
+
+
+def run_reference(args):
+    rank, world = dist_init()
+    if rank != 0:
+        return
+    from oracle import oracle as O  # noqa: F401
+    from oracle import pipeline as OP
+    from xpsi_gb300 import batch as BT
+    from xpsi_gb300 import synthetic as SY
+    model, _ = build_workload(1)
+    P0 = BT.prepare(model, SY.config2_vector(seed=1)[None, :])
+    _, _, stages = OP.loglike(model, P0, n_threads=os.cpu_count() or 1, return_stages=True)
+    SY.attach_data(model, [stages[0]["folded"], stages[1]["folded"]], P0.shifts[0])
+    params = SY.config3_vectors(args.vectors, seed=3)
+    cores = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_budget / max(1, args.steps))
+    for _ in range(args.warmup):
+        oracle_evals(model, params[:1], cores, 0.0)
+    n_tot, t_tot = 0, 0.0
+    for s in range(args.steps):
+        n, t = oracle_evals(model, params[s:], cores, per_step)
+        n_tot += n
+        t_tot += t
+    value = n_tot / t_tot
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_tot / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded prior draws, Poisson counts from the model)",
+           "config": {"workload": "batched prior vectors of the full-size plain model",
+                      "vectors_sampled": n_tot},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{n_tot} prior vectors through the CPU restatement "
+                                      f"(OpenMP, {cores} threads), meshes excluded"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--vectors", type=int, default=256)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

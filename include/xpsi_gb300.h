@@ -155,6 +155,7 @@ typedef struct {
   xgpu_atmos4d atmos; /* device pointers; intensity NULL when no mesh is Num4D */
   double *flux;
   int32_t *mesh_status;
+  double *flop_counter; /* optional: algorithmic FLOPs of the launch are added */
 } xgpu_integrate_batch_data;
 
 int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows,
@@ -192,6 +193,54 @@ typedef struct {
 } xgpu_likelihood_batch_data;
 
 int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream);
+
+/* Measurement helper (no counterpart in the reference): launches an FMA
+ * throughput probe (fp64 != 0: FP64, else FP32) and returns the FLOPs it
+ * issues, so that kernel rates can be quoted against the device's own FP64 /
+ * FP32 issue peaks.  out: device scratch of 8 bytes. */
+double xgpu_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
+                       void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* 3. host-side cell meshes for the batched path (CPU, multithreaded)     */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces xpsi.cellmesh.mesh_tools.allocate_cells
+ * (xpsi/cellmesh/mesh_tools.pyx:892-1099); out4 = (super_sqrt_num_cells,
+ * super_num_cells, cede_sqrt_num_cells, cede_num_cells). */
+int xgpu_allocate_cells(size_t num_cells, size_t min_sqrt, size_t max_sqrt,
+                        double R_eq, double Omega, double zeta, double epsilon,
+                        int star_shape_ind, double super_radius,
+                        double cede_radius, double super_colatitude,
+                        double cede_colatitude, double super_azimuth,
+                        double hole_colatitude, double hole_radius,
+                        double hole_azimuth, double *out4);
+
+/* Replaces construct_spot_cellMesh (xpsi/cellmesh/mesh.pyx:23-417, polar 0)
+ * and construct_polar_cellMesh (xpsi/cellmesh/polar_mesh.pyx:23-430,
+ * polar 1).  Arguments follow the reference (ceding = enclosing region,
+ * superseding = omitted/superseding region inside it).  Outputs:
+ * theta, phi, area [S][S]; r, maxAlpha, cos_gamma, effGrav [S]. */
+int xgpu_cell_mesh(int polar, size_t num_cells, size_t S, double R_eq,
+                   double zeta, double epsilon, int star_shape_ind,
+                   double cede_radius, double cede_colatitude,
+                   double super_radius, double super_colatitude,
+                   double super_azimuth, double *theta, double *phi, double *r,
+                   double *area, double *maxAlpha, double *cos_gamma,
+                   double *effGrav);
+
+typedef struct {
+  int32_t polar;
+  size_t num_cells, S;
+  double R_eq, zeta, epsilon;
+  int32_t star_shape_ind;
+  double cede_radius, cede_colatitude, super_radius, super_colatitude,
+      super_azimuth;
+  double *theta, *phi, *r, *area, *maxAlpha, *cos_gamma, *effGrav;
+} xgpu_mesh_request;
+
+/* Many meshes at once on n_threads host threads (0: all cores). */
+int xgpu_cell_mesh_many(int n, const xgpu_mesh_request *req, int n_threads);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
-UNITS = ["rays", "integrator", "energy", "fold", "likelihood", "abi"]
+UNITS = ["rays", "integrator", "energy", "fold", "likelihood", "abi", "mesh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -31,7 +31,7 @@ def _nvcc():
 
 def _sources_mtime():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
-             if f.endswith((".cu", ".cuh", ".h"))]
+             if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
     files.append(os.path.join(ROOT, "include", "xpsi_gb300.h"))
     return max(os.path.getmtime(f) for f in files)
 
@@ -45,7 +45,12 @@ def build(force=False, verbose=False):
 
     def compile_unit(u):
         obj = os.path.join(BUILD, u + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, u + ".cu"), "-o", obj]
+        src = os.path.join(CSRC, u + ".cu")
+        if os.path.exists(src):
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        else:  # host C++ unit
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c",
+                   os.path.join(CSRC, u + ".cpp"), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s%s" % (u, r.stdout, r.stderr))
@@ -56,7 +61,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp%d" % os.getpid()
-    r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"],
+    r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
@@ -91,7 +96,15 @@ class IntegrateBatchData(C.Structure):
                 ("cos_alpha", P), ("lag", P), ("cellArea", P), ("phi", P),
                 ("params", P), ("n_params", I32), ("radiates", P), ("energies", P),
                 ("leaves", P), ("phases", P), ("atmos", Atmos4D), ("flux", P),
-                ("mesh_status", P)]
+                ("mesh_status", P), ("flop_counter", P)]
+
+
+class MeshRequest(C.Structure):
+    _fields_ = [("polar", I32), ("num_cells", SZ), ("S", SZ), ("R_eq", D), ("zeta", D),
+                ("epsilon", D), ("star_shape_ind", I32), ("cede_radius", D),
+                ("cede_colatitude", D), ("super_radius", D), ("super_colatitude", D),
+                ("super_azimuth", D), ("theta", P), ("phi", P), ("r", P), ("area", P),
+                ("maxAlpha", P), ("cos_gamma", P), ("effGrav", P)]
 
 
 class LikelihoodBatchData(C.Structure):
@@ -127,6 +140,12 @@ def _bind(L):
         "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
                                       P, P]),
         "xgpu_likelihood_batch": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
+        "xgpu_allocate_cells": (C.c_int, [SZ, SZ, SZ, D, D, D, D, C.c_int, D, D, D, D, D, D,
+                                          D, D, P]),
+        "xgpu_cell_mesh": (C.c_int, [C.c_int, SZ, SZ, D, D, D, C.c_int, D, D, D, D, D, P, P,
+                                     P, P, P, P, P]),
+        "xgpu_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(MeshRequest), C.c_int]),
+        "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -138,7 +157,8 @@ def _bind(L):
 EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_integrate",
             "xgpu_energy_integrator", "xgpu_response_fold", "xgpu_precomputation",
             "xgpu_eval_marginal_likelihood", "xgpu_rays_batch", "xgpu_integrate_batch",
-            "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch"]
+            "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
+            "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe"]
 
 
 def lib():

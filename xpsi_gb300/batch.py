@@ -1,0 +1,428 @@
+"""Batched likelihood evaluation: many parameter vectors per launch.
+
+The model mirrors X-PSI's Likelihood/Star/Photosphere/HotRegion/Signal stack
+for uniform-temperature hot regions (HotRegion.py, Signal.py, Likelihood.py),
+with the per-vector geometry prepared on the host and every numerical stage
+on the GPU:
+
+    host   Spacetime derived quantities (Spacetime.py:110-187), cell budget and
+           meshes (mesh_tools.pyx:892-1099, mesh.pyx, polar_mesh.pyx), lag
+           calibration constants (HotRegion.py:880-901), source parameters
+           (HotRegion.py:953-1017)
+    GPU    rays (K1) -> integrator (K2/K3) -> energy integration over the
+           instrument's input intervals with the 1/d^2 factor (K4,
+           Likelihood.py:361-364) -> response fold (K5) -> background-
+           marginalised log-likelihood of every vector (K6)
+
+PyTorch supplies device buffers and the stream; the kernels are reached
+through the C ABI only.
+"""
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from ._native import (Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh, check, lib)
+from .cellmesh import mesh as _mesh
+
+# xpsi/global_imports.py
+_GM = 0.5 * 2.95325024e3
+_C = 2.99792458e8
+_CSQ = _C * _C
+_G = 6.6740831e-11
+_KM = 1.0e3
+_KPC = 3.08567758e19
+_2PI = 2.0 * math.pi
+
+STATUS_NAMES = {0: "ok", 1: "RayError", 2: "PulseError", 3: "AtmosError", 4: "QuadFail",
+                5: "SlimCut", 6: "BadInput"}
+
+
+@dataclass
+class HotRegionSpec:
+    """Resolution and kind of one hot region (HotRegion.__init__ arguments)."""
+    atm_ext: int = 1                 # 1 blackbody, 2 numerical 4-D
+    sqrt_num_cells: int = 32
+    min_sqrt_num_cells: int = 10
+    max_sqrt_num_cells: int = 80
+    num_leaves: int = 64
+    num_rays: int = 512
+    image_order_limit: Optional[int] = None
+    omit: bool = False
+    is_antiphased: bool = False
+
+
+@dataclass
+class Instrument:
+    matrix: np.ndarray               # [K, q] response (channels x input intervals)
+    energy_edges: np.ndarray         # [q + 1] keV
+
+
+@dataclass
+class Data:
+    counts: np.ndarray               # [K, B]
+    phase_edges: np.ndarray          # [B + 1] cycles
+    exposure: float
+    support: Optional[np.ndarray] = None  # [K, 2]; default unbounded
+
+
+@dataclass
+class Model:
+    regions: List[HotRegionSpec]
+    instrument: Instrument
+    data: Data
+    num_energies: int = 64
+    atmosphere: Optional[tuple] = None   # (logT, logg, mu, logE, I) for Num4D
+    llzero: float = -1.0e90
+    epsrel: float = 1.0e-8
+    epsilon: float = 1.0e-3
+    sigmas: float = 10.0
+    slim: float = 20.0
+    energies: np.ndarray = field(default=None)
+
+    def __post_init__(self):
+        if self.energies is None:
+            e = self.instrument.energy_edges
+            # construct_energy_array for one waveband (Signal.py:1092-1197)
+            self.energies = np.logspace(math.log10(e[0]), math.log10(e[-1]),
+                                        int(math.ceil(self.num_energies)))
+        leaves = {r.num_leaves for r in self.regions}
+        rays = {r.num_rays for r in self.regions}
+        if len(leaves) != 1 or len(rays) != 1:
+            raise ValueError("all hot regions of one model share num_leaves and num_rays")
+
+
+# parameter vector layout per vector:
+#   mass, radius_km, frequency, cos_inclination, distance_kpc,
+#   then per region: colatitude, angular radius, log10 T, phase shift,
+#   and for an omit region additionally omit radius, omit colatitude, omit azimuth
+def param_names(model):
+    names = ["mass", "radius", "frequency", "cos_inclination", "distance"]
+    for h, r in enumerate(model.regions):
+        names += [f"h{h}_colatitude", f"h{h}_radius", f"h{h}_temperature", f"h{h}_phase_shift"]
+        if r.omit:
+            names += [f"h{h}_omit_radius", f"h{h}_omit_colatitude", f"h{h}_omit_azimuth"]
+    return names
+
+
+def _effective_gravity_bounds(R, zeta, eps):
+    c = _C
+    out = []
+    for mu in (1.0, 0.0):
+        x = zeta
+        g0 = x * c * c / (R * math.sqrt(1.0 - 2.0 * x))
+        c_e, c_p = -0.791 + 0.776 * x, 1.138 - 1.431 * x
+        d_e, d_p = (-1.315 + 2.431 * x) * eps * x, (0.653 - 2.864 * x) * eps * x
+        d_60 = (13.47 - 27.13 * x) * eps * x
+        f_e, f_p = -1.172 * x * eps * eps, 0.975 * x * eps * eps
+        g = 1.0 + (c_e + d_e + f_e) * eps * (1.0 - mu * mu)
+        g += (c_p + d_p + f_p - d_60) * eps * mu * mu + d_60 * eps * abs(mu)
+        out.append(math.log10(g * g0) + 2.0)
+    return out
+
+
+class Prepared:
+    """Host-packed inputs of one batch (numpy), ready to upload."""
+
+
+def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
+    """Derived quantities and meshes of every (vector, hot region) member,
+    packed into the flat arrays the kernels read."""
+    params = np.atleast_2d(np.asarray(params, dtype=np.float64))
+    V = params.shape[0]
+    H = len(model.regions)
+    names = param_names(model)
+    if params.shape[1] != len(names):
+        raise ValueError("expected %d parameters per vector: %s" % (len(names), names))
+    col = {n: i for i, n in enumerate(names)}
+    reqs, members, status = [], [], np.zeros(V, dtype=np.int32)
+    atm = model.atmosphere
+    for v in range(V):
+        p = params[v]
+        Msun, Rkm, f, cosi, Dkpc = (p[col[k]] for k in ("mass", "radius", "frequency",
+                                                         "cos_inclination", "distance"))
+        r_g = Msun * _GM
+        r_s = 2.0 * r_g
+        R = Rkm * _KM
+        Mkg = Msun * _GM * _CSQ / _G
+        Om = _2PI * f
+        zeta = r_g / R
+        eps = Om ** 2.0 * R ** 3.0 / (_G * Mkg)
+        star = dict(r_s=r_s, R=R, Omega=Om, zeta=zeta, eps=eps, inclination=math.acos(cosi),
+                    d_sq=(Dkpc * _KPC) ** 2, f=f)
+        if atm is not None and any(r.atm_ext == 2 for r in model.regions):
+            # Photosphere.py:486-507
+            gl = _effective_gravity_bounds(R, zeta, eps)
+            for h, r in enumerate(model.regions):
+                T = p[col[f"h{h}_temperature"]]
+                if r.atm_ext == 2 and not (atm[0][0] <= T <= atm[0][-1]):
+                    status[v] = 3
+            if any(not (atm[1][0] <= g <= atm[1][-1]) for g in gl):
+                status[v] = 3
+        for h, r in enumerate(model.regions):
+            colat, rad = p[col[f"h{h}_colatitude"]], p[col[f"h{h}_radius"]]
+            logT, shift = p[col[f"h{h}_temperature"]], p[col[f"h{h}_phase_shift"]]
+            if r.omit:
+                o_r = p[col[f"h{h}_omit_radius"]]
+                o_c = p[col[f"h{h}_omit_colatitude"]]
+                o_a = p[col[f"h{h}_omit_azimuth"]]
+            else:
+                o_r = o_c = o_a = 0.0
+            a = _mesh.allocate_cells(r.sqrt_num_cells ** 2, r.min_sqrt_num_cells,
+                                     r.max_sqrt_num_cells, Mkg, r_s, R, Om, zeta, eps, 0, rad,
+                                     0.0, colat, colat, -0.0, o_c, o_r, o_a)
+            S = int(a[0])
+            polar = (colat - rad < 0.0) or (colat + rad > math.pi)
+            reqs.append(dict(polar=polar, num_cells=int(a[1]), S=S, R_eq=R, zeta=zeta,
+                             epsilon=eps, star_shape_ind=0, cede_radius=rad,
+                             cede_colatitude=colat, super_radius=o_r, super_colatitude=o_c,
+                             super_azimuth=o_a))
+            members.append(dict(v=v, h=h, S=S, logT=logT, shift=shift, omit_azimuth=o_a,
+                                antiphased=r.is_antiphased, spec=r, **star))
+    _mesh.build_many(reqs, n_threads)
+    n_rows = sum(m["S"] for m in members)
+    n_cells = sum(m["S"] * m["S"] for m in members)
+    P = Prepared()
+    P.V, P.H, P.n_rows, P.n_cells = V, H, n_rows, n_cells
+    P.status = status
+    P.row = {k: np.empty(n_rows) for k in ("u", "r_s", "maxAlpha", "radius", "cos_gamma",
+                                           "theta0", "lag_C", "lag_scale")}
+    P.row_mesh = np.empty(n_rows, dtype=np.int32)
+    P.cellArea = np.empty(n_cells)
+    P.phi = np.empty(n_cells)
+    P.params = np.empty((n_cells, 2))
+    P.radiates = np.empty(n_cells, dtype=np.int32)
+    P.meshes = (Mesh * len(members))()
+    P.d_sq = np.empty(len(members))
+    P.shifts = np.empty((V, H))
+    N_E, N_P = len(model.energies), model.regions[0].num_leaves
+    ro = co = 0
+    for m_i, (m, q) in enumerate(zip(members, reqs)):
+        S = m["S"]
+        sl = slice(ro, ro + S)
+        u = m["r_s"] / q["r"]
+        P.row["u"][sl] = u
+        P.row["r_s"][sl] = m["r_s"]
+        P.row["maxAlpha"][sl] = q["maxAlpha"]
+        P.row["radius"][sl] = q["r"]
+        P.row["cos_gamma"][sl] = q["cos_gamma"]
+        P.row["theta0"][sl] = q["theta"][:, 0]
+        R_i = m["R"] / m["r_s"]
+        C_ = (1.0 / u - R_i)
+        C_ += np.log((1.0 / u - 1.0) / (R_i - 1.0))
+        C_ *= m["r_s"] / _C
+        P.row["lag_C"][sl] = C_
+        P.row["lag_scale"][sl] = m["f"] * _2PI
+        P.row_mesh[sl] = m_i
+        cs = slice(co, co + S * S)
+        A = q["area"]
+        P.cellArea[cs] = A.reshape(-1)
+        ph = q["phi"] - m["omit_azimuth"]
+        if m["antiphased"]:
+            ph = ph + math.pi
+        P.phi[cs] = ph.reshape(-1)
+        prm = np.ones((S, S, 2))
+        prm[..., :-1] *= m["logT"]
+        for j in range(S):
+            prm[:, j, -1] *= q["effGrav"]
+        P.params[cs] = prm.reshape(-1, 2)
+        P.radiates[cs] = np.greater(A, 0.0).astype(np.int32).reshape(-1)
+        spec = m["spec"]
+        P.meshes[m_i] = Mesh(S, S, ro, co, m["Omega"], m["inclination"],
+                             int(spec.image_order_limit or 0), int(spec.atm_ext),
+                             m_i * N_E * N_P)
+        P.d_sq[m_i] = m["d_sq"]
+        P.shifts[m["v"], m["h"]] = m["shift"]
+        ro += S
+        co += S * S
+    P.members = members
+    return P
+
+
+class BatchEvaluator:
+    """Device-resident model (tables, response, data) plus per-batch buffers."""
+
+    def __init__(self, model: Model, device=0):
+        import torch
+        self.torch = torch
+        self.model = model
+        self.dev = torch.device("cuda", device)
+        t = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt,
+                                                          device=self.dev)
+        self.energies = t(model.energies)
+        r0 = model.regions[0]
+        self.N_L = r0.num_leaves
+        self.N_R = r0.num_rays
+        self.leaves = t(np.linspace(0.0, _2PI, self.N_L))
+        self.phases = t(_2PI * np.linspace(0.0, 1.0, self.N_L))
+        self.comp_phases = t(np.linspace(0.0, 1.0, self.N_L))
+        self.log10E = t(np.log10(model.energies))
+        self.log10edges = t(np.log10(model.instrument.energy_edges))
+        self.matrix = t(model.instrument.matrix)
+        self.K, self.q = model.instrument.matrix.shape
+        d = model.data
+        self.counts = t(np.asarray(d.counts, dtype=np.float64))
+        self.phase_edges = t(d.phase_edges)
+        self.B = len(d.phase_edges) - 1
+        sup = d.support
+        if sup is None:
+            sup = -1.0 * np.ones((self.K, 2))
+            sup[:, 0] = 0.0
+        self.support = t(sup)
+        self.allow_negative = t(np.zeros(len(model.regions)), torch.int32)
+        self.precomp = torch.empty(self.K, dtype=torch.float64, device=self.dev)
+        from .likelihoods.default_background_marginalisation import precomputation
+        self.precomp.copy_(torch.as_tensor(precomputation(np.asarray(d.counts, np.int32))))
+        self.atmos = None
+        if model.atmosphere is not None:
+            self.atm_t = [t(a) for a in model.atmosphere]
+            a = self.atm_t
+            self.atmos = Atmos4D(a[0].data_ptr(), a[1].data_ptr(), a[2].data_ptr(),
+                                 a[3].data_ptr(), a[4].data_ptr(), a[0].numel(),
+                                 a[1].numel(), a[2].numel(), a[3].numel())
+
+    # ---------------------------------------------------------------- upload
+    def upload(self, P: Prepared, pinned=None):
+        """Copy a prepared batch to the device (non-blocking from pinned
+        memory when given) and allocate its work buffers."""
+        torch = self.torch
+        dev = self.dev
+        f64 = torch.float64
+
+        def put(a, dt=f64):
+            h = torch.from_numpy(np.ascontiguousarray(a))
+            if pinned is not None:
+                h = h.pin_memory()
+            return h.to(dev, non_blocking=True)
+        B = dict()
+        B["row"] = {k: put(v) for k, v in P.row.items()}
+        B["row_mesh"] = put(P.row_mesh)
+        B["cellArea"], B["phi"] = put(P.cellArea), put(P.phi)
+        B["params"], B["radiates"] = put(P.params), put(P.radiates)
+        B["d_sq"], B["shifts"] = put(P.d_sq), put(P.shifts)
+        self.alloc(P, B)
+        return B
+
+    def h2d_bytes(self, P: Prepared):
+        return int(sum(v.nbytes for v in P.row.values()) + P.row_mesh.nbytes
+                   + P.cellArea.nbytes + P.phi.nbytes + P.params.nbytes + P.radiates.nbytes
+                   + P.d_sq.nbytes + P.shifts.nbytes)
+
+    def alloc(self, P, B):
+        torch = self.torch
+        dev, f64 = self.dev, torch.float64
+        n_m = P.V * P.H
+        N_E, N_P = len(self.model.energies), self.N_L
+        tab = (P.n_rows, self.N_R)
+        B["defl"] = torch.empty(tab, dtype=f64, device=dev)
+        B["ca"] = torch.empty(tab, dtype=f64, device=dev)
+        B["lag"] = torch.empty(tab, dtype=f64, device=dev)
+        B["maxDefl"] = torch.empty(P.n_rows, dtype=f64, device=dev)
+        B["row_status"] = torch.empty(P.n_rows, dtype=torch.int32, device=dev)
+        B["maxAlpha"] = B["row"]["maxAlpha"]
+        B["flux"] = torch.empty((n_m, N_E, N_P), dtype=f64, device=dev)
+        B["mesh_status"] = torch.empty(n_m, dtype=torch.int32, device=dev)
+        B["off_in"] = torch.arange(n_m, dtype=torch.int64, device=dev) * (N_E * N_P)
+        B["off_out"] = torch.arange(n_m, dtype=torch.int64, device=dev) * (self.q * N_P)
+        B["integrated"] = torch.empty((n_m, self.q, N_P), dtype=f64, device=dev)
+        B["folded"] = torch.empty((n_m, self.K, N_P), dtype=f64, device=dev)
+        B["chan_ll"] = torch.empty((P.V, self.K), dtype=f64, device=dev)
+        B["chan_flag"] = torch.empty((P.V, self.K), dtype=torch.int32, device=dev)
+        B["loglike"] = torch.empty(P.V, dtype=f64, device=dev)
+        B["status"] = torch.empty(P.V, dtype=torch.int32, device=dev)
+        B["P"] = P
+
+    # ---------------------------------------------------------------- run
+    def run(self, B, stream=None, probe=None):
+        """Enqueue the five stages on `stream` (default: torch's current).
+        `probe` (optional dict) receives CUDA events around the integrator
+        launch and its algorithmic FLOP count (key "flops", a device tensor)."""
+        torch = self.torch
+        P = B["P"]
+        strm = stream or torch.cuda.current_stream(self.dev)
+        st = strm.cuda_stream
+        p = lambda x: x.data_ptr()
+        L = lib()
+        row = B["row"]
+        check(L.xgpu_rays_batch(P.n_rows, self.N_R, p(row["u"]), p(row["r_s"]),
+                                p(B["maxAlpha"]), p(B["defl"]), p(B["ca"]), p(B["lag"]),
+                                p(B["maxDefl"]), p(B["row_status"]), p(row["lag_C"]),
+                                p(row["lag_scale"]), st))
+        d = IntegrateBatchData()
+        d.row_mesh = p(B["row_mesh"])
+        d.radius, d.u, d.cos_gamma = p(row["radius"]), p(row["u"]), p(row["cos_gamma"])
+        d.theta0, d.maxDeflection = p(row["theta0"]), p(B["maxDefl"])
+        d.deflection, d.cos_alpha, d.lag = p(B["defl"]), p(B["ca"]), p(B["lag"])
+        d.cellArea, d.phi, d.params = p(B["cellArea"]), p(B["phi"]), p(B["params"])
+        d.n_params = 2
+        d.radiates = p(B["radiates"])
+        d.energies, d.leaves, d.phases = p(self.energies), p(self.leaves), p(self.phases)
+        if self.atmos is not None:
+            d.atmos = self.atmos
+        d.flux = p(B["flux"])
+        d.mesh_status = p(B["mesh_status"])
+        n_m = P.V * P.H
+        N_E, N_P = len(self.model.energies), self.N_L
+        if probe is not None:
+            d.flop_counter = p(probe["flops"])
+            probe["start"] = torch.cuda.Event(enable_timing=True)
+            probe["end"] = torch.cuda.Event(enable_timing=True)
+            probe["start"].record(strm)
+        check(L.xgpu_integrate_batch(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P,
+                                     C.byref(d), 0, st))
+        if probe is not None:
+            probe["end"].record(strm)
+        check(L.xgpu_energy_batch(n_m, N_E, N_P, self.log10edges.numel(), p(B["flux"]),
+                                  p(B["off_in"]), p(self.log10E), p(self.log10edges),
+                                  p(B["d_sq"]), p(B["integrated"]), p(B["off_out"]), 0, st))
+        check(L.xgpu_fold_batch(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
+                                p(B["integrated"]), p(B["folded"]), st))
+        m = self.model
+        ld = LikelihoodBatchData()
+        ld.n_vec, ld.K, ld.B, ld.H, ld.N_P = P.V, self.K, self.B, P.H, N_P
+        ld.exposure, ld.epsabs, ld.epsrel = m.data.exposure, 0.0, m.epsrel
+        ld.epsilon, ld.sigmas, ld.llzero, ld.slim = m.epsilon, m.sigmas, m.llzero, m.slim
+        ld.phase_edges, ld.comp_phases = p(self.phase_edges), p(self.comp_phases)
+        ld.counts, ld.precomp, ld.support = p(self.counts), p(self.precomp), p(self.support)
+        ld.background = None
+        ld.signals, ld.shifts = p(B["folded"]), p(B["shifts"])
+        ld.allow_negative = p(self.allow_negative)
+        ld.chan_ll, ld.chan_flag = p(B["chan_ll"]), p(B["chan_flag"])
+        ld.star = ld.mcl_bg = ld.mcl_bg_support = None
+        ld.loglike, ld.status = p(B["loglike"]), p(B["status"])
+        check(L.xgpu_likelihood_batch(C.byref(ld), st))
+
+    def statuses(self, B):
+        """Per-vector status word (ray, pulse, atmosphere, quadrature, slim)."""
+        torch = self.torch
+        P = B["P"]
+        st = B["status"].cpu().numpy().copy()
+        rs = B["row_status"].cpu().numpy()
+        ms = B["mesh_status"].cpu().numpy()
+        rm = B["row_mesh"].cpu().numpy()
+        vec_of_mesh = np.repeat(np.arange(P.V), P.H)
+        bad_rows = np.unique(rm[rs != 0])
+        for mi in bad_rows:
+            st[vec_of_mesh[mi]] = 1
+        for mi in np.nonzero(ms)[0]:
+            if st[vec_of_mesh[mi]] == 0:
+                st[vec_of_mesh[mi]] = 2
+        st[P.status != 0] = P.status[P.status != 0]
+        return st
+
+    def loglikelihood(self, params, n_threads=0):
+        """log L of every parameter vector (host in, host out) and statuses.
+        Vectors whose status is not 0 get a value near llzero, as
+        Likelihood.random_near_llzero does (Likelihood.py:268-271)."""
+        P = prepare(self.model, params, n_threads)
+        B = self.upload(P)
+        self.run(B)
+        ll = B["loglike"].cpu().numpy().copy()
+        st = self.statuses(B)
+        bad = st != 0
+        if bad.any():
+            rng = np.random.default_rng(12345)
+            ll[bad] = self.model.llzero * (0.1 + 0.9 * rng.random(int(bad.sum())))
+        return ll, st

@@ -47,6 +47,19 @@ int lib_stream(cudaStream_t *st) {
   return 0;
 }
 
+// keep freed stream-ordered memory in the device pool between calls
+void keep_pool(void) {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
+
 // stream-ordered device buffer
 struct Dev {
   void *p = nullptr;
@@ -59,6 +72,7 @@ struct Dev {
 };
 
 int dalloc(Dev &d, size_t bytes, cudaStream_t st) {
+  keep_pool();
   d.st = st;
   if (bytes == 0) bytes = 16;
   CK(cudaMallocAsync(&d.p, bytes, st));
@@ -226,6 +240,7 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.row_has_eval = sb; a.row_last_top = sb + n_rows; a.row_entry_top = sb + 2 * n_rows;
   a.member_status = d->mesh_status;
   a.flux = d->flux;
+  a.flop_counter = d->flop_counter;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
   return 0;
@@ -249,6 +264,12 @@ int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix, int ld
   xg::launch_fold_f64(a, static_cast<cudaStream_t>(stream));
   CK(cudaGetLastError());
   return 0;
+}
+
+double xgpu_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
+                       void *stream) {
+  return xg::launch_peak_probe(fp64, blocks, threads, iters, out,
+                               static_cast<cudaStream_t>(stream));
 }
 
 int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream) {

@@ -67,3 +67,47 @@ void launch_fold_f64(const FoldArgs &a, cudaStream_t st) {
 }
 
 }  // namespace xg
+
+namespace xg {
+namespace {
+// FP64 fused multiply-add throughput probe: 8 independent chains per thread
+__global__ void fp64_peak_kernel(int iters, double seed, double *out) {
+  double a[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) a[i] = seed + threadIdx.x * 1e-9 + i;
+  const double b = 0.999999999, c = 1e-9;
+  for (int k = 0; k < iters; k++) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) a[i] = fma(a[i], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) s += a[i];
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+__global__ void fp32_peak_kernel(int iters, float seed, float *out) {
+  float a[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) a[i] = seed + threadIdx.x * 1e-6f + i;
+  const float b = 0.9999999f, c = 1e-7f;
+  for (int k = 0; k < iters; k++) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) a[i] = fmaf(a[i], b, c);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; i++) s += a[i];
+  if (s == 12345.678f) out[0] = s;
+}
+}  // namespace
+
+// FLOPs issued by one launch: blocks * threads * iters * 8 FMAs * 2
+double launch_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
+                         cudaStream_t st) {
+  if (fp64)
+    fp64_peak_kernel<<<blocks, threads, 0, st>>>(iters, 1.0, static_cast<double *>(out));
+  else
+    fp32_peak_kernel<<<blocks, threads, 0, st>>>(iters, 1.0f, static_cast<float *>(out));
+  return 2.0 * 8.0 * (double)blocks * threads * iters;
+}
+}  // namespace xg

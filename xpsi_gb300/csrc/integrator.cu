@@ -477,6 +477,11 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
   const double mu_top3 = num4d ? a.atmos.mu[a.atmos.nmu - 3] : 0.0;
   const int groups = EC / kEPT;
   const int ntasks = N_P * groups;
+  // algorithmic FLOPs per (parallel, image), the cost model of the
+  // likelihood path: leaf work N_L (60 + N_E f_atm) and spline work
+  // N_E (30 N_L + C N_P 14), f_atm 12 (blackbody) or 1350 (4-D table)
+  double flops = 0.0;
+  const double f_atm = num4d ? 1350.0 : 12.0;
 
   for (int64_t row = r0; row < r1; row++) {
     const int i = (int)(row - M.row_off);
@@ -507,6 +512,12 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
         return;
       }
       if (invis) break;
+      if (threadIdx.x == 0 && a.flop_counter) {
+        int Cr = 0;
+        for (int j = 0; j < M.S1; j++) Cr += (rad[j] == 1);
+        flops += (double)N_L * (60.0 + N_E * f_atm) +
+                 (double)N_E * (30.0 * N_L + (double)Cr * N_P * 14.0);
+      }
 
       for (int e0 = 0; e0 < N_E; e0 += EC) {
         const int ne = min(EC, N_E - e0);
@@ -591,6 +602,7 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
       }
     }
   }
+  if (threadIdx.x == 0 && a.flop_counter && flops > 0.0) atomicAdd(a.flop_counter, flops);
 }
 
 // ordered reduction of the chunk partials and the 1/(E keV) factor (:605-612)

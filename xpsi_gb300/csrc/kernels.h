@@ -67,6 +67,7 @@ struct IntegrateArgs {
   uint8_t *row_has_eval, *row_last_top, *row_entry_top;  // [rows]
   int32_t *member_status;   // [n_members]
   double *flux;             // [..] at members[m].flux_off
+  double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
 };
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
 
@@ -96,6 +97,8 @@ struct FoldArgs {
   double *out;       // [batch][K][N]
 };
 void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
+double launch_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
+                         cudaStream_t st);
 
 // ---- K6 likelihood ----------------------------------------------------------
 struct LikeArgs {

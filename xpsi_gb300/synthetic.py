@@ -14,8 +14,11 @@ def num4d_table(shape=(35, 14, 67, 166), seed=2,
                 ranges=((5.0, 7.0), (13.4, 15.6), (0.0, 1.0), (-1.5, 2.7))):
     """A numerical 4-D hot atmosphere (logT, logg, mu, log10(E/kT)) filled with
     a limb-darkened modified blackbody plus 1e-3 seeded noise:
-    I = x^3/(e^x - 1) (0.42 + 0.58 mu) (1 + 0.05 (logg - 14.5)) (1 + 1e-3 N(0,1)),
-    x = 10^logE.  Returns the tuple X-PSI preloads: (logT, logg, mu, logE, I)."""
+    I = P x^3/(e^x - 1) (0.42 + 0.58 mu) (1 + 0.05 (logg - 14.5)) (1 + 1e-3 N(0,1)),
+    x = 10^logE, with P = 2 k^3 / (h^2 c^2) in cgs so that I T^3 is a specific
+    intensity per Hz (the units the Num4D evaluator expects,
+    hot_Num4D.pyx:437-461).  Returns the tuple X-PSI preloads:
+    (logT, logg, mu, logE, I)."""
     nT, ng, nmu, nE = shape
     logT = np.linspace(*ranges[0], nT)
     logg = np.linspace(*ranges[1], ng)
@@ -23,7 +26,8 @@ def num4d_table(shape=(35, 14, 67, 166), seed=2,
     logE = np.linspace(*ranges[3], nE)
     rng = np.random.default_rng(seed)
     x = 10.0 ** logE
-    planck = x ** 3 / np.expm1(x)
+    k_B, h, c = 1.380649e-16, 6.62607015e-27, 2.99792458e10
+    planck = (2.0 * k_B ** 3 / (h * h * c * c)) * x ** 3 / np.expm1(x)
     I = (planck[None, None, None, :] * (0.42 + 0.58 * mu)[None, None, :, None]
          * (1.0 + 0.05 * (logg - 14.5))[None, :, None, None]
          * np.ones((nT, 1, 1, 1)))
@@ -77,3 +81,95 @@ def poisson_data(registered, comp_phases, phase_edges, exposure, seed=20261203,
     bg = bg_fraction * src.sum(axis=1, keepdims=True) / B
     rng = np.random.default_rng(seed)
     return rng.poisson(src + bg).astype(np.int32)
+
+
+def _offset_point(colat, dist, chi):
+    """Point at angular distance `dist` from the spot centre (colat, azimuth 0)
+    in direction chi on the sphere; returns (colatitude, azimuth)."""
+    c = np.array([math.sin(colat), 0.0, math.cos(colat)])
+    e_t = np.array([math.cos(colat), 0.0, -math.sin(colat)])
+    e_p = np.array([0.0, 1.0, 0.0])
+    x = math.cos(dist) * c + math.sin(dist) * (math.cos(chi) * e_t + math.sin(chi) * e_p)
+    return math.acos(max(-1.0, min(1.0, x[2]))), math.atan2(x[1], x[0])
+
+
+def draw_spots(rng):
+    """Spot parameters of the full-size plain configuration: a circular spot
+    and a spot with an omitted crescent; colatitudes U(0, pi), radii
+    U(0.01, 0.5), log T U(5.8, 6.6), omit radius U(0.3, 0.9) x radius, omit
+    centre offset U(0.2, 0.8) x radius inside the spot, phase shifts U(0, 1)."""
+    out = []
+    for h in range(2):
+        colat = rng.uniform(0.0, math.pi)
+        rad = rng.uniform(0.01, 0.5)
+        logT = rng.uniform(5.8, 6.6)
+        shift = rng.uniform(0.0, 1.0)
+        out += [colat, rad, logT, shift]
+        if h == 1:
+            o_r = rng.uniform(0.3, 0.9) * rad
+            off = rng.uniform(0.2, 0.8) * rad
+            chi = rng.uniform(0.0, 2 * math.pi)
+            o_c, o_a = _offset_point(colat, off, chi)
+            out += [o_r, o_c, o_a]
+    return out
+
+
+def prior_vector(rng, fixed_star=None):
+    """One parameter vector of the batched configuration: M U(1, 3) Msun,
+    R U(3 r_g(M), 16 km), spin U(200, 600) Hz, cos i U(0, 1), D = 1 kpc,
+    spots as draw_spots."""
+    if fixed_star is not None:
+        star = list(fixed_star)
+    else:
+        M = rng.uniform(1.0, 3.0)
+        r_g_km = M * 0.5 * 2.95325024e3 / 1.0e3
+        R = rng.uniform(3.0 * r_g_km, 16.0)
+        star = [M, R, rng.uniform(200.0, 600.0), rng.uniform(0.0, 1.0), 1.0]
+    return star + draw_spots(rng)
+
+
+def config2_model(K=1500, q=128, num_energies=128, sqrt_num_cells=64, num_leaves=128,
+                  num_rays=1024, max_sqrt_num_cells=128, table_shape=(35, 14, 67, 166),
+                  data_seed=20261203):
+    """Model of the full-size plain configuration (two Num4D hot regions, one
+    with an omitted crescent) with synthetic instrument K x q; data are drawn
+    later by draw_data()."""
+    from .batch import Data, HotRegionSpec, Instrument, Model
+    M, in_edges, _ = gaussian_response(K, q)
+    regions = [HotRegionSpec(atm_ext=2, sqrt_num_cells=sqrt_num_cells, min_sqrt_num_cells=10,
+                             max_sqrt_num_cells=max_sqrt_num_cells, num_leaves=num_leaves,
+                             num_rays=num_rays),
+               HotRegionSpec(atm_ext=2, sqrt_num_cells=sqrt_num_cells, min_sqrt_num_cells=10,
+                             max_sqrt_num_cells=max_sqrt_num_cells, num_leaves=num_leaves,
+                             num_rays=num_rays, omit=True)]
+    data = Data(counts=np.zeros((K, 32), dtype=np.int32), phase_edges=np.linspace(0, 1, 33),
+                exposure=1.0e6)
+    return Model(regions=regions, instrument=Instrument(M, in_edges), data=data,
+                 num_energies=num_energies, atmosphere=num4d_table(table_shape, seed=2))
+
+
+def config2_vector(seed=1):
+    """The full-size configuration's parameter vector: the small configuration's
+    star (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc) and spots drawn with `seed`."""
+    rng = np.random.default_rng(seed)
+    return np.array(prior_vector(rng, fixed_star=[1.4, 12.0, 300.0, math.cos(1.0), 1.0]))
+
+
+def config3_vectors(V=4096, seed=3):
+    rng = np.random.default_rng(seed)
+    return np.array([prior_vector(rng) for _ in range(V)])
+
+
+def attach_data(model, registered_by_region, shifts, seed=20261203):
+    """Replace the model's counts by Poisson draws from the summed registered
+    signals of its hot regions (each [K, N_P], phase-shifted by `shifts`)."""
+    N_P = registered_by_region[0].shape[1]
+    ph = np.linspace(0.0, 1.0, N_P)
+    total = np.zeros_like(registered_by_region[0])
+    fine = np.linspace(0.0, 1.0, N_P)
+    for reg, s in zip(registered_by_region, shifts):
+        for c in range(reg.shape[0]):
+            total[c] += np.interp((fine - s) % 1.0, ph, reg[c])
+    model.data.counts = poisson_data(total, ph, model.data.phase_edges, model.data.exposure,
+                                     seed=seed)
+    return model
