@@ -693,6 +693,7 @@ int gsl_integration_qag(const gsl_function *f, double a, double b,
 }
 
 /* ---- stand-in for the doubly adaptive CQUAD routine ---- */
+static unsigned long long g_cquad_evals = 0, g_cquad_calls = 0;
 #define CQUAD_SUB_LIMIT 4000
 gsl_integration_cquad_workspace *gsl_integration_cquad_workspace_alloc(const size_t n) {
   if (n < 3) {
@@ -775,8 +776,18 @@ int gsl_integration_cquad(const gsl_function *f, double a, double b,
   *result = sign * r;
   *abserr = e;
   if (nevals) *nevals = nev;
+  g_cquad_evals += nev;
+  g_cquad_calls += 1;
   return GSL_SUCCESS;
 }
+
+/* test hook: integrand evaluations spent in the CQUAD stand-in so far */
+unsigned long long gslsub_cquad_evals(int reset) {
+  unsigned long long v = g_cquad_evals;
+  if (reset) { g_cquad_evals = 0; g_cquad_calls = 0; }
+  return v;
+}
+unsigned long long gslsub_cquad_calls(void) { return g_cquad_calls; }
 
 /* ------------------------------------------------------------------ */
 /* special functions                                                   */
