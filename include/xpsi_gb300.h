@@ -194,6 +194,23 @@ typedef struct {
 
 int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream);
 
+/* Allocation-free form of xgpu_likelihood_batch.  It has no counterpart in
+ * the reference: it exists for callers that cannot allocate device memory at
+ * call time -- a host whose framework owns all device memory through its own
+ * pool, or code held to a memory budget fixed in advance.  Inputs and outputs
+ * are the caller's device buffers exactly as for xgpu_likelihood_batch; the
+ * scratch arrays d->chan_ll and d->chan_flag are IGNORED and replaced by a
+ * fixed 4 MiB device array inside this library (12 bytes per evaluation and
+ * channel: n_vec * K <= 349525), which every GPU that loads the library
+ * holds until the process exits.  No device memory is allocated or freed.
+ * The first call on a device looks up that array's device address (once per
+ * device, with the device current); make that first call before any stream
+ * capture.  All calls share the one array, so calls that overlap on the GPU
+ * (other streams, other threads) race: serialise them on one stream.
+ * Returns 0, -2 for invalid sizes, -3 when n_vec * K exceeds the maximum,
+ * -4 when the array's address cannot be obtained, -5 when the launch fails. */
+int xgpu_likelihood_batch_static(const xgpu_likelihood_batch_data *d, void *stream);
+
 /* Measurement helper (no counterpart in the reference): launches an FMA
  * throughput probe (fp64 != 0: FP64, else FP32) and returns the FLOPs it
  * issues, so that kernel rates can be quoted against the device's own FP64 /

@@ -140,6 +140,7 @@ def _bind(L):
         "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
                                       P, P]),
         "xgpu_likelihood_batch": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
+        "xgpu_likelihood_batch_static": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
         "xgpu_allocate_cells": (C.c_int, [SZ, SZ, SZ, D, D, D, D, C.c_int, D, D, D, D, D, D,
                                           D, D, P]),
         "xgpu_cell_mesh": (C.c_int, [C.c_int, SZ, SZ, D, D, D, C.c_int, D, D, D, D, D, P, P,
@@ -158,7 +159,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_energy_integrator", "xgpu_response_fold", "xgpu_precomputation",
             "xgpu_eval_marginal_likelihood", "xgpu_rays_batch", "xgpu_integrate_batch",
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
-            "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe"]
+            "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
+            "xgpu_likelihood_batch_static"]
 
 
 def lib():

@@ -459,3 +459,74 @@ void launch_precomputation(int K, int B, const int32_t *counts, double *out, cud
   precomp_kernel<<<(K + 127) / 128, 128, 0, st>>>(K, B, counts, out);
 }
 }  // namespace xg
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the batched likelihood entry point.
+//
+// Some callers cannot allocate device memory when they call the likelihood:
+// a sampler or serving host whose framework owns all device memory through
+// its own pool (allocations from outside the pool fail or fragment it), and
+// code that must run in a fixed memory budget known in advance.  For them
+// xgpu_likelihood_batch_static takes device inputs and outputs from the
+// caller, as xgpu_likelihood_batch does, and keeps the per-(evaluation,
+// channel) scratch -- the channel's log-likelihood term and its early-exit
+// flag -- in the fixed array below, which every GPU that loads this library
+// holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#include "../../include/xpsi_gb300.h"
+
+namespace {
+
+// 4 MiB: 12 bytes per (evaluation, channel) -> at most 349525 of them
+constexpr size_t kLikeScratchBytes = size_t(4) << 20;
+constexpr size_t kLikeScratchPerChannel = sizeof(double) + sizeof(int32_t);
+static __device__ __align__(256) unsigned char g_like_scratch[kLikeScratchBytes];
+
+// device address of g_like_scratch per device, looked up once with that
+// device current (the host-side name of the array is not a device address)
+std::mutex g_like_scratch_mu;
+void *g_like_scratch_addr[64] = {};
+
+int like_scratch_address(void **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -4;
+  std::lock_guard<std::mutex> lk(g_like_scratch_mu);
+  if (!g_like_scratch_addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_like_scratch) != cudaSuccess || p == nullptr) return -4;
+    g_like_scratch_addr[dev] = p;
+  }
+  *out = g_like_scratch_addr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int xgpu_likelihood_batch_static(const xgpu_likelihood_batch_data *d,
+                                            void *stream) {
+  if (d == nullptr || d->n_vec < 0 || d->K <= 0) return -2;
+  if (d->B > 64 || d->N_P < 5) return -2;
+  const size_t n = (size_t)d->n_vec * (size_t)d->K;
+  if (n > kLikeScratchBytes / kLikeScratchPerChannel) return -3;
+  void *base = nullptr;
+  int rc = like_scratch_address(&base);
+  if (rc) return rc;
+  if (n == 0) return 0;
+  xg::LikeArgs a{};
+  a.n_vec = d->n_vec; a.K = d->K; a.B = d->B; a.H = d->H; a.N_P = d->N_P;
+  a.exposure = d->exposure; a.epsabs = d->epsabs; a.epsrel = d->epsrel;
+  a.epsilon = d->epsilon; a.sigmas = d->sigmas; a.llzero = d->llzero; a.slim = d->slim;
+  a.phase_edges = d->phase_edges; a.comp_phases = d->comp_phases; a.counts = d->counts;
+  a.precomp = d->precomp; a.support = d->support; a.background = d->background;
+  a.signals = d->signals; a.shifts = d->shifts; a.allow_negative = d->allow_negative;
+  // every (evaluation, channel) term and flag is written by the channel
+  // kernel before the finalize kernel reads it, so nothing needs clearing
+  a.chan_ll = static_cast<double *>(base);
+  a.chan_flag = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(base) + n * sizeof(double));
+  a.star = d->star; a.mcl_bg = d->mcl_bg; a.mcl_bg_s = d->mcl_bg_support;
+  a.loglike = d->loglike; a.status = d->status;
+  xg::launch_likelihood(a, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
