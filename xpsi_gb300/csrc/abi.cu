@@ -213,6 +213,10 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   if ((rc = dalloc(dpart, part_n * sizeof(double), st))) return rc;
   CK(cudaMemsetAsync(dpart.p, 0, part_n * sizeof(double), st));
   if ((rc = dalloc(dstate, (size_t)3 * n_rows + 16, st))) return rc;
+  Dev dslab;
+  if (d->atmos.intensity != nullptr &&
+      (rc = dalloc(dslab, (size_t)n_chunks * d->atmos.nmu * d->atmos.nE * sizeof(double), st)))
+    return rc;
   CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
 
   xg::IntegrateArgs a{};
@@ -241,6 +245,7 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.member_status = d->mesh_status;
   a.flux = d->flux;
   a.flop_counter = d->flop_counter;
+  a.slab = d->atmos.intensity != nullptr ? dslab.as<double>() : nullptr;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
   return 0;

@@ -315,67 +315,86 @@ __device__ __forceinline__ void lagrange4(const double *P, int b, double x, doub
   w[0] = d0 * s0; w[1] = d1 * s1; w[2] = d2 * s2; w[3] = d3 * s3;
 }
 
-// hot_Num4D.pyx:248-439 with the stencil the reference's cached walk lands on
-__device__ double eval_num4d(const Atmos4D &A, double E, double mu, bool clamp_mu,
-                             double vec0, double vec1) {
-  double v[4];
-  double E_eff = (kKB / kKeV) * pow(10.0, vec0);
-  v[0] = vec0;
-  v[1] = vec1;
-  v[2] = mu;
-  v[3] = log10(E / E_eff);
-  const double *g[4] = {A.logT, A.logg, A.mu, A.logE};
-  const int n[4] = {A.nT, A.ng, A.nmu, A.nE};
-  int b[4];
-  double w[4][4];
-#pragma unroll
-  for (int d = 0; d < 4; d++) {
-    double x = v[d];
-    if (d != 2) {  // in-table by construction; clamp as the walk would
-      if (x < g[d][0]) x = g[d][0];
-      if (x > g[d][n[d] - 1]) x = g[d][n[d] - 1];
-    } else {
-      if (x > g[2][n[2] - 1] && clamp_mu) x = g[2][n[2] - 1];
-    }
-    v[d] = x;
-    b[d] = stencil_base(g[d], n[d], x);
-    lagrange4(g[d], b[d], x, w[d]);
-  }
-  const int64_t S2 = A.nE, S1 = (int64_t)A.nmu * A.nE, S0 = (int64_t)A.ng * S1;
+struct AtmSmem {
+  double *gmu, *gE;      // grids of mu and log10(E/kT)
+  double *smu, *sE;      // inverse Lagrange denominators per stencil base, 4 each
+};
+
+// inverse denominators of the 4-point Lagrange basis on grid[b..b+3]
+// (hot_Num4D.pyx:177-188, computed in the reference's order)
+__device__ __forceinline__ void lagrange_space(const double *P, int b, double s[4]) {
+  double s0 = 1.0 / (P[b] - P[b + 1]); s0 /= P[b] - P[b + 2]; s0 /= P[b] - P[b + 3];
+  double s1 = 1.0 / (P[b + 1] - P[b]); s1 /= P[b + 1] - P[b + 2]; s1 /= P[b + 1] - P[b + 3];
+  double s2 = 1.0 / (P[b + 2] - P[b]); s2 /= P[b + 2] - P[b + 1]; s2 /= P[b + 2] - P[b + 3];
+  double s3 = 1.0 / (P[b + 3] - P[b]); s3 /= P[b + 3] - P[b + 1]; s3 /= P[b + 3] - P[b + 2];
+  s[0] = s0; s[1] = s1; s[2] = s2; s[3] = s3;
+}
+
+__device__ __forceinline__ void lagrange_w(const double *P, const double *S, int b, double x,
+                                           double w[4]) {
+  double d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
+  double d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
+  w[0] = d0 * S[4 * b]; w[1] = d1 * S[4 * b + 1]; w[2] = d2 * S[4 * b + 2];
+  w[3] = d3 * S[4 * b + 3];
+}
+
+// Num4D intensity for a parallel whose (log T, log g) stencil has been
+// contracted into `slab` [nmu][nE]: the remaining 4 x 4 (mu, energy) stencil
+// (hot_Num4D.pyx:248-439; the stencil bases are those the reference's cached
+// walk lands on, see the file header for the mu > 1 case)
+__device__ __forceinline__ double eval_num4d_slab(const Atmos4D &A, const AtmSmem &as,
+                                                  const double *slab, double E, double mu,
+                                                  bool clamp_mu, double E_eff, double p3) {
+  double v2 = mu;
+  const double mu_hi = as.gmu[A.nmu - 1];
+  if (v2 > mu_hi && clamp_mu) v2 = mu_hi;
+  if (v2 < as.gmu[0]) v2 = as.gmu[0];
+  double v3 = log10(E / E_eff);
+  if (v3 < as.gE[0]) v3 = as.gE[0];
+  if (v3 > as.gE[A.nE - 1]) v3 = as.gE[A.nE - 1];
+  const int b2 = stencil_base(as.gmu, A.nmu, v2);
+  const int b3 = stencil_base(as.gE, A.nE, v3);
+  double w2[4], w3[4];
+  lagrange_w(as.gmu, as.smu, b2, v2, w2);
+  lagrange_w(as.gE, as.sE, b3, v3, w3);
   double I = 0.0;
-  for (int i = 0; i < 4; i++)
-    for (int j = 0; j < 4; j++)
-      for (int k = 0; k < 4; k++) {
-        const double *row = A.I + (b[0] + i) * S0 + (b[1] + j) * S1 + (b[2] + k) * S2 + b[3];
 #pragma unroll
-        for (int l = 0; l < 4; l++) {
-          double t = w[0][i] * w[1][j] * w[2][k] * w[3][l];
-          I += t * __ldg(row + l);
-        }
-      }
+  for (int k = 0; k < 4; k++) {
+    const double *r = slab + (size_t)(b2 + k) * A.nE + b3;
+    double t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
+    I += w2[k] * t;
+  }
   if (I < 0.0) return 0.0;
-  return I * pow(10.0, 3.0 * v[0]);
+  return I * p3;
 }
 
 struct Layout {
-  int N_L, EC;
+  int N_L, EC, nmu, nE;
   size_t bytes;
 };
 
-__host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E) {
+// nmu, nE: Num4D grid sizes (0 when no mesh uses the numerical atmosphere)
+__host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu = 0,
+                                              int nE = 0) {
   Layout L;
   L.N_L = N_L;
+  L.nmu = nmu;
+  L.nE = nE;
   int ec = 8;
   while (ec < 32 && (long)N_P * (ec * 2 / kEPT) <= kThreads && ec * 2 <= N_E + kEPT) ec *= 2;
   while (ec > 8 && (size_t)ec * N_L * 32 > 96 * 1024) ec /= 2;
   L.EC = ec;
   L.bytes = (size_t)5 * N_L * sizeof(double)      // phase, leafphase, Z, ABB, GEOM
             + (size_t)ec * N_L * 4 * sizeof(double)  // coefficients
-            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 16;
+            + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
+            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 32;
   return L;
 }
 
-__device__ GeoSmem carve(char *base, int N_L, int EC, double **coef) {
+__device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0, int nE = 0,
+                         AtmSmem *atm = nullptr) {
   GeoSmem g;
   double *d = reinterpret_cast<double *>(base);
   g.phase = d; d += N_L;
@@ -385,6 +404,12 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef) {
   g.GEOM = d; d += N_L;
   d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(d) + 15) & ~uintptr_t(15));
   *coef = d; d += (size_t)EC * N_L * 4;
+  if (atm) {
+    atm->gmu = d; d += nmu;
+    atm->gE = d; d += nE;
+    atm->smu = d; d += (size_t)4 * nmu;
+    atm->sE = d; d += (size_t)4 * nE;
+  }
   int *ip = reinterpret_cast<int *>(d);
   g.src = ip; ip += N_L;
   g.calc = ip; ip += N_L;
@@ -464,13 +489,25 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
   const MemberDesc M = a.members[m];
   const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  const Layout L = make_layout(N_L, N_P, N_E);
+  const bool num4d = (M.atm == 2);
+  const int nmu = a.atmos.I ? a.atmos.nmu : 0, nEt = a.atmos.I ? a.atmos.nE : 0;
+  const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt);
   const int EC = L.EC;
   double *coef;
-  GeoSmem g = carve(smem, N_L, EC, &coef);
+  AtmSmem as{};
+  GeoSmem g = carve(smem, N_L, EC, &coef, nmu, nEt, &as);
   Piece *co4 = reinterpret_cast<Piece *>(coef);
   __shared__ int s_J, s_top, s_any;
-  const bool num4d = (M.atm == 2);
+  double *slab = nullptr;
+  if (num4d) {
+    for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.gmu[t] = a.atmos.mu[t];
+    for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.gE[t] = a.atmos.logE[t];
+    __syncthreads();
+    for (int b = threadIdx.x; b <= nmu - 4; b += blockDim.x) lagrange_space(as.gmu, b, as.smu + 4 * b);
+    for (int b = threadIdx.x; b <= nEt - 4; b += blockDim.x) lagrange_space(as.gE, b, as.sE + 4 * b);
+    slab = a.slab + (size_t)chunk * nmu * nEt;
+    __syncthreads();
+  }
   const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
   double *part = a.partial + (size_t)chunk * N_E * N_P;
   const double mu_max = num4d ? a.atmos.mu[a.atmos.nmu - 1] : 0.0;
@@ -492,6 +529,37 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
       s_any = 0;
     }
     __syncthreads();
+    double E_eff = 0.0, p3 = 0.0;
+    if (num4d) {
+      // contract the (log T, log g) stencil of this parallel once:
+      // slab[mu][logE] = sum_ij w_T[i] w_g[j] table[bT+i][bg+j][mu][logE]
+      double vT = c.vec0, vg = c.vec1;
+      if (vT < a.atmos.logT[0]) vT = a.atmos.logT[0];
+      if (vT > a.atmos.logT[a.atmos.nT - 1]) vT = a.atmos.logT[a.atmos.nT - 1];
+      if (vg < a.atmos.logg[0]) vg = a.atmos.logg[0];
+      if (vg > a.atmos.logg[a.atmos.ng - 1]) vg = a.atmos.logg[a.atmos.ng - 1];
+      const int bT = stencil_base(a.atmos.logT, a.atmos.nT, vT);
+      const int bg = stencil_base(a.atmos.logg, a.atmos.ng, vg);
+      double wT[4], wg[4];
+      lagrange4(a.atmos.logT, bT, vT, wT);
+      lagrange4(a.atmos.logg, bg, vg, wg);
+      const size_t S1t = (size_t)nmu * nEt, S0t = (size_t)a.atmos.ng * S1t;
+      const double *base = a.atmos.I + bT * S0t + bg * S1t;
+      for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
+        double r = 0.0;
+#pragma unroll
+        for (int ii = 0; ii < 4; ii++) {
+          const double *q = base + ii * S0t + t;
+          double u = wg[0] * __ldg(q) + wg[1] * __ldg(q + S1t) + wg[2] * __ldg(q + 2 * S1t) +
+                     wg[3] * __ldg(q + 3 * S1t);
+          r += wT[ii] * u;
+        }
+        slab[t] = r;
+      }
+      E_eff = (kKB / kKeV) * pow(10.0, c.vec0);
+      p3 = pow(10.0, 3.0 * vT);
+      __syncthreads();
+    }
     const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
     const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
     const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
@@ -531,7 +599,8 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
             const double Ep = a.energies[p] / g.Z[s];
             double I_E;
             if (num4d)
-              I_E = eval_num4d(a.atmos, Ep, g.ABB[s], p == 0 && g.clamp0[s], c.vec0, c.vec1);
+              I_E = eval_num4d_slab(a.atmos, as, slab, Ep, g.ABB[s], p == 0 && g.clamp0[s],
+                                    E_eff, p3);
             else
               I_E = eval_bb(Ep, c.vec0);
             y = (I_E * norm - 0.0) * g.GEOM[s];
@@ -623,7 +692,8 @@ __global__ void reduce_flux_kernel(IntegrateArgs a) {
 
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   if (a.n_members <= 0) return;
-  Layout L = make_layout(a.N_L, a.N_P, a.N_E);
+  Layout L = a.atmos.I ? make_layout(a.N_L, a.N_P, a.N_E, a.atmos.nmu, a.atmos.nE)
+                       : make_layout(a.N_L, a.N_P, a.N_E);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -68,6 +68,7 @@ struct IntegrateArgs {
   int32_t *member_status;   // [n_members]
   double *flux;             // [..] at members[m].flux_off
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
+  double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
 };
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
 

@@ -379,7 +379,17 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
         else A += a.llzero;
       }
       m.A = A;
-      double result = warp_marginal(m, w, lane, lower, upper, a.epsabs, a.epsrel);
+      double dsum = 0.0;
+      for (int j = 0; j < B; j++) dsum += w.data[j];
+      double result;
+      if (dsum == 0.0) {
+        // no counts in the channel: every term is -c_j, so the integrand is
+        // exp(-T (B - Bi)) exactly and its integral over the window is closed
+        // form (the reference's quadrature converges to this value)
+        result = exp(-T * (lower - Bi)) * (-expm1(-T * (upper - lower))) / T;
+      } else {
+        result = warp_marginal(m, w, lane, lower, upper, a.epsabs, a.epsrel);
+      }
       if (result > 0.0) term = log(result) + A + a.precomp[ch];
       else flag = 2;
     }
