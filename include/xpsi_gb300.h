@@ -163,6 +163,16 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows,
                          const xgpu_integrate_batch_data *d, int target_ctas,
                          void *stream);
 
+/* Mixed-precision form of xgpu_integrate_batch (same arguments): leaf
+ * geometry, visibility and phase knots in FP64; atmosphere interpolation,
+ * Akima pieces and the cell x phase sums in FP32; partial sums in FP64.
+ * Not bitwise the reference; its error against the FP64 path is reported
+ * per evaluation by the batched driver. */
+int xgpu_integrate_batch_mixed(int n_meshes, const xgpu_mesh *meshes,
+                               int64_t n_rows, int N_R, int N_E, int N_L,
+                               int N_P, const xgpu_integrate_batch_data *d,
+                               int target_ctas, void *stream);
+
 /* Energy integration of n_signals [N_E][N_P] signals at in_off[s] (device
  * int64 offsets) into [n_edges-1][N_P] at out_off[s]; d_sq[s] divides the
  * signal first (Likelihood.py:361-364); accumulate adds into out. */

@@ -135,6 +135,9 @@ def _bind(L):
         "xgpu_integrate_batch": (C.c_int, [C.c_int, C.POINTER(Mesh), I64, C.c_int,
                                            C.c_int, C.c_int, C.c_int,
                                            C.POINTER(IntegrateBatchData), C.c_int, P]),
+        "xgpu_integrate_batch_mixed": (C.c_int, [C.c_int, C.POINTER(Mesh), I64, C.c_int,
+                                                 C.c_int, C.c_int, C.c_int,
+                                                 C.POINTER(IntegrateBatchData), C.c_int, P]),
         "xgpu_energy_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P,
                                         P, P, P, C.c_int, P]),
         "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
@@ -160,7 +163,7 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_eval_marginal_likelihood", "xgpu_rays_batch", "xgpu_integrate_batch",
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
             "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
-            "xgpu_likelihood_batch_static"]
+            "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed"]
 
 
 def lib():

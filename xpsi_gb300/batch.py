@@ -242,10 +242,18 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
 
 
 class BatchEvaluator:
-    """Device-resident model (tables, response, data) plus per-batch buffers."""
+    """Device-resident model (tables, response, data) plus per-batch buffers.
 
-    def __init__(self, model: Model, device=0):
+    precision "plain": every stage in FP64 (the drop-in's numerics).
+    precision "mixed": the integrator's atmosphere interpolation, splines and
+    cell x phase sums in FP32 (xgpu_integrate_batch_mixed); rays, energy
+    integration, fold and the likelihood sum stay FP64."""
+
+    def __init__(self, model: Model, device=0, precision="plain"):
         import torch
+        if precision not in ("plain", "mixed"):
+            raise ValueError("precision is 'plain' or 'mixed'")
+        self.precision = precision
         self.torch = torch
         self.model = model
         self.dev = torch.device("cuda", device)
@@ -370,8 +378,9 @@ class BatchEvaluator:
             probe["start"] = torch.cuda.Event(enable_timing=True)
             probe["end"] = torch.cuda.Event(enable_timing=True)
             probe["start"].record(strm)
-        check(L.xgpu_integrate_batch(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P,
-                                     C.byref(d), 0, st))
+        integ = L.xgpu_integrate_batch_mixed if self.precision == "mixed" \
+            else L.xgpu_integrate_batch
+        check(integ(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P, C.byref(d), 0, st))
         if probe is not None:
             probe["end"].record(strm)
         check(L.xgpu_energy_batch(n_m, N_E, N_P, self.log10edges.numel(), p(B["flux"]),

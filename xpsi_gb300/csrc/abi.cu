@@ -177,9 +177,32 @@ int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u, const double *r_s,
   return 0;
 }
 
+namespace {
+int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
+                         int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
+                         int target_ctas, void *stream, int mixed);
+}
+
 int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
                          int target_ctas, void *stream) {
+  return integrate_batch_impl(n_meshes, meshes, n_rows, N_R, N_E, N_L, N_P, d, target_ctas,
+                              stream, 0);
+}
+
+int xgpu_integrate_batch_mixed(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
+                               int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
+                               int target_ctas, void *stream) {
+  return integrate_batch_impl(n_meshes, meshes, n_rows, N_R, N_E, N_L, N_P, d, target_ctas,
+                              stream, 1);
+}
+
+}  // extern "C"
+
+namespace {
+int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
+                         int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
+                         int target_ctas, void *stream, int mixed) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (n_meshes <= 0) return 0;
   if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
@@ -190,12 +213,18 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
     if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
   }
-  if (target_ctas <= 0) target_ctas = 4 * 152;
-  int64_t rpc = std::max<int64_t>(1, n_rows / target_ctas);
+  if (target_ctas <= 0) target_ctas = 8 * 152;
+  // chunks of consecutive parallels of one mesh, sized by estimated cost
+  // (cells per parallel) so that large meshes do not leave a long tail
+  double total_cost = 0.0;
+  for (int m = 0; m < n_meshes; m++) total_cost += (double)meshes[m].S0 * meshes[m].S1;
+  const double target_cost = std::max(1.0, total_cost / target_ctas);
   std::vector<int64_t> r0, r1;
   std::vector<int32_t> first(n_meshes + 1);
   for (int m = 0; m < n_meshes; m++) {
     first[m] = (int32_t)r0.size();
+    const int64_t rpc =
+        std::max<int64_t>(1, (int64_t)(target_cost / std::max(1, meshes[m].S1)));
     for (int64_t s = 0; s < meshes[m].S0; s += rpc) {
       r0.push_back(meshes[m].row_off + s);
       r1.push_back(meshes[m].row_off + std::min<int64_t>(meshes[m].S0, s + rpc));
@@ -246,10 +275,14 @@ int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.flux = d->flux;
   a.flop_counter = d->flop_counter;
   a.slab = d->atmos.intensity != nullptr ? dslab.as<double>() : nullptr;
+  a.mixed = mixed;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
   return 0;
 }
+}  // namespace
+
+extern "C" {
 
 int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges, const double *signal,
                       const int64_t *in_off, const double *log10_energies,

@@ -27,6 +27,8 @@
 // other energy extrapolates the last stencil.  The kernels reproduce the
 // reference's single-thread call order exactly: a geometry pre-pass and a
 // per-mesh scan hand each parallel the state its first evaluation sees.
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -36,12 +38,16 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kEPT = 8;  // energies per accumulation task
+constexpr int kMaxCellsF = 512;  // cells per parallel held as FP32 pairs (mixed form)
 
 // Akima piece of one energy row: value at the left knot and the three
-// polynomial coefficients; 32 bytes, read as two 16-byte shared loads.
-struct __align__(16) Piece {
-  double y, k1, k2, k3;
+// polynomial coefficients (FP64: 32 bytes, two 16-byte shared loads; FP32:
+// one 16-byte load).
+template <typename WT>
+struct __align__(16) PieceT {
+  WT y, k1, k2, k3;
 };
+using Piece = PieceT<double>;
 
 struct RowCtx {
   int S1, N_R, J, IO;
@@ -54,6 +60,7 @@ struct RowCtx {
 
 struct GeoSmem {
   double *phase, *leafphase, *Z, *ABB, *GEOM;
+  double *rD;  // the parallel's deflection table, staged for the binary searches
   int *src, *calc, *term, *clamp0;
   int *flags;  // [0] terminate, [1] invisible image, [2] any evaluation, [3] last_top
 };
@@ -259,11 +266,7 @@ __device__ bool load_row(const IntegrateArgs &a, const MemberDesc &M, int64_t ro
   c.D = a.deflection + row * a.N_R;
   c.CA = a.cos_alpha + row * a.N_R;
   c.LG = a.lag + row * a.N_R;
-  // first ray deflected beyond pi/2 (:301-303); the reference's loop is
-  // unbounded, here it stops at the row's last ray
-  int j = 0;
-  while (j < a.N_R - 1 && c.D[j] <= kHalfPi) j++;
-  c.jalt = j;
+  c.jalt = a.N_R - 1;  // set by stage_deflection()
   c.radius = a.radius[row];
   c.Grav_z = sqrt(1.0 - a.u[row]);
   c.cos_gamma = a.cos_gamma[row];
@@ -283,6 +286,23 @@ __device__ bool load_row(const IntegrateArgs &a, const MemberDesc &M, int64_t ro
   c.vec0 = vec[0];
   c.vec1 = vec[1];
   return true;
+}
+
+// Copy the parallel's deflection table to shared memory (the leaf searches
+// probe it ~10 times per lookup) and find the first ray deflected beyond
+// pi/2 (:301-303; the reference's scan is unbounded, here it stops at the
+// last ray).  All threads of the CTA call it.
+__device__ void stage_deflection(RowCtx &c, GeoSmem &g, int *s_jalt) {
+  const int N_R = c.N_R;
+  for (int t = threadIdx.x; t < N_R; t += blockDim.x) g.rD[t] = c.D[t];
+  if (threadIdx.x == 0) *s_jalt = N_R - 1;
+  __syncthreads();
+  for (int t = threadIdx.x; t < N_R - 1; t += blockDim.x)
+    if (g.rD[t] > kHalfPi) atomicMin(s_jalt, t);
+  __syncthreads();
+  c.jalt = *s_jalt;
+  c.D = g.rD;
+  __syncthreads();
 }
 
 __device__ __forceinline__ double eval_bb(double E, double vec0) {
@@ -318,6 +338,10 @@ __device__ __forceinline__ void lagrange4(const double *P, int b, double x, doub
 struct AtmSmem {
   double *gmu, *gE;      // grids of mu and log10(E/kT)
   double *smu, *sE;      // inverse Lagrange denominators per stencil base, 4 each
+  float *fgmu, *fgE, *fsmu, *fsE;  // FP32 copies for the mixed-precision form
+  float *fphase;         // FP32 copy of the phase knots
+  float *fphase_lo;      // phase knot minus its FP32 copy
+  float *fcphi, *fcphi_lo;  // cell azimuths of the parallel as float pairs (<= kMaxCellsF)
 };
 
 // inverse denominators of the 4-point Lagrange basis on grid[b..b+3]
@@ -370,6 +394,66 @@ __device__ __forceinline__ double eval_num4d_slab(const Atmos4D &A, const AtmSme
   return I * p3;
 }
 
+// FP32 forms for the mixed-precision integrator
+
+// Knuth's error-free sum: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ int stencil_base_f(const float *g, int n, float v) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (g[mid] > v) hi = mid; else lo = mid;
+  }
+  int b = lo - 1;
+  if (b < 0) b = 0;
+  if (b > n - 4) b = n - 4;
+  return b;
+}
+
+__device__ __forceinline__ void lagrange_wf(const float *P, const float *S, int b, float x,
+                                            float w[4]) {
+  float d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
+  float d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
+  float d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
+  float d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
+  w[0] = d0 * S[4 * b]; w[1] = d1 * S[4 * b + 1]; w[2] = d2 * S[4 * b + 2];
+  w[3] = d3 * S[4 * b + 3];
+}
+
+__device__ __forceinline__ float eval_num4d_slab_f(const Atmos4D &A, const AtmSmem &as,
+                                                   const float *slab, float E, float mu,
+                                                   bool clamp_mu, float E_eff, float p3) {
+  float v2 = mu;
+  const float mu_hi = as.fgmu[A.nmu - 1];
+  if (v2 > mu_hi && clamp_mu) v2 = mu_hi;
+  if (v2 < as.fgmu[0]) v2 = as.fgmu[0];
+  float v3 = log10f(E / E_eff);
+  if (v3 < as.fgE[0]) v3 = as.fgE[0];
+  if (v3 > as.fgE[A.nE - 1]) v3 = as.fgE[A.nE - 1];
+  const int b2 = stencil_base_f(as.fgmu, A.nmu, v2);
+  const int b3 = stencil_base_f(as.fgE, A.nE, v3);
+  float w2[4], w3[4];
+  lagrange_wf(as.fgmu, as.fsmu, b2, v2, w2);
+  lagrange_wf(as.fgE, as.fsE, b3, v3, w3);
+  float I = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float *r = slab + (size_t)(b2 + k) * A.nE + b3;
+    float t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
+    I += w2[k] * t;
+  }
+  if (I < 0.0f) return 0.0f;
+  return I * p3;
+}
+
+__device__ __forceinline__ float eval_bb_f(float E, float kT) {
+  return E * E * E / expm1f(E / kT);
+}
+
 struct Layout {
   int N_L, EC, nmu, nE;
   size_t bytes;
@@ -377,38 +461,52 @@ struct Layout {
 
 // nmu, nE: Num4D grid sizes (0 when no mesh uses the numerical atmosphere)
 __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu = 0,
-                                              int nE = 0) {
+                                              int nE = 0, int piece_bytes = 32, int N_R = 0) {
   Layout L;
   L.N_L = N_L;
   L.nmu = nmu;
   L.nE = nE;
   int ec = 8;
   while (ec < 32 && (long)N_P * (ec * 2 / kEPT) <= kThreads && ec * 2 <= N_E + kEPT) ec *= 2;
-  while (ec > 8 && (size_t)ec * N_L * 32 > 96 * 1024) ec /= 2;
+  while (ec > 8 && (size_t)ec * N_L * piece_bytes > 96 * 1024) ec /= 2;
   L.EC = ec;
   L.bytes = (size_t)5 * N_L * sizeof(double)      // phase, leafphase, Z, ABB, GEOM
-            + (size_t)ec * N_L * 4 * sizeof(double)  // coefficients
+            + (size_t)ec * N_L * piece_bytes       // coefficients
             + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
-            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 32;
+            + (size_t)(2 * N_L + nmu + nE) * 5 * sizeof(float)  // FP32 copies (mixed form)
+            + (size_t)2 * kMaxCellsF * sizeof(float)
+            + (size_t)N_R * sizeof(double)  // staged deflection table
+            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 64;
   return L;
 }
 
 __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0, int nE = 0,
-                         AtmSmem *atm = nullptr) {
+                         AtmSmem *atm = nullptr, int piece_bytes = 32, int N_R = 0) {
   GeoSmem g;
   double *d = reinterpret_cast<double *>(base);
+  g.rD = d; d += N_R;
   g.phase = d; d += N_L;
   g.leafphase = d; d += N_L;
   g.Z = d; d += N_L;
   g.ABB = d; d += N_L;
   g.GEOM = d; d += N_L;
   d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(d) + 15) & ~uintptr_t(15));
-  *coef = d; d += (size_t)EC * N_L * 4;
+  *coef = d; d += (size_t)EC * N_L * piece_bytes / 8;
   if (atm) {
     atm->gmu = d; d += nmu;
     atm->gE = d; d += nE;
     atm->smu = d; d += (size_t)4 * nmu;
     atm->sE = d; d += (size_t)4 * nE;
+    float *f = reinterpret_cast<float *>(d);
+    atm->fgmu = f; f += nmu;
+    atm->fgE = f; f += nE;
+    atm->fsmu = f; f += (size_t)4 * nmu;
+    atm->fsE = f; f += (size_t)4 * nE;
+    atm->fphase = f; f += N_L;
+    atm->fphase_lo = f; f += N_L;
+    atm->fcphi = f; f += kMaxCellsF;
+    atm->fcphi_lo = f; f += kMaxCellsF;
+    d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(f) + 15) & ~uintptr_t(15));
   }
   int *ip = reinterpret_cast<int *>(d);
   g.src = ip; ip += N_L;
@@ -433,14 +531,15 @@ __global__ void __launch_bounds__(128) num4d_prepass_kernel(IntegrateArgs a) {
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
   Layout L = make_layout(N_L, a.N_P, a.N_E);
   double *coef;
-  GeoSmem g = carve(smem, N_L, 0, &coef);
-  __shared__ int s_J, s_any, s_top;
+  GeoSmem g = carve(smem, N_L, 0, &coef, 0, 0, nullptr, 32, a.N_R);
+  __shared__ int s_J, s_any, s_top, s_jalt;
   RowCtx c;
   if (threadIdx.x == 0) { s_any = 0; s_top = 0; }
   if (!load_row(a, M, row, i, c, &s_J)) {
     if (threadIdx.x == 0) { a.row_has_eval[row] = 0; a.row_last_top[row] = 0; }
     return;
   }
+  stage_deflection(c, g, &s_jalt);
   (void)L;
   const double mu_max = a.atmos.mu[a.atmos.nmu - 1], mu_top3 = a.atmos.mu[a.atmos.nmu - 3];
   for (int I = 0; I < c.IO; I++) {
@@ -481,7 +580,12 @@ __global__ void num4d_scan_kernel(IntegrateArgs a) {
 // ---------------------------------------------------------------------------
 // main integrator kernel: one CTA per chunk of parallels of one mesh
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
+// WT = double: the plain FP64 drop-in.  WT = float: the mixed-precision form
+// (geometry, visibility and knots in FP64; atmosphere, Akima pieces and the
+// cell x phase sums in FP32; per-chunk partials in FP64).
+template <typename WT>
+__global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a) {
+  constexpr bool kMixed = std::is_same<WT, float>::value;
   extern __shared__ __align__(16) char smem[];
   const int chunk = blockIdx.x;
   const int64_t r0 = a.chunk_r0[chunk], r1 = a.chunk_r1[chunk];
@@ -491,21 +595,30 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
   const bool num4d = (M.atm == 2);
   const int nmu = a.atmos.I ? a.atmos.nmu : 0, nEt = a.atmos.I ? a.atmos.nE : 0;
-  const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt);
+  const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt, (int)sizeof(PieceT<WT>), a.N_R);
   const int EC = L.EC;
   double *coef;
   AtmSmem as{};
-  GeoSmem g = carve(smem, N_L, EC, &coef, nmu, nEt, &as);
-  Piece *co4 = reinterpret_cast<Piece *>(coef);
-  __shared__ int s_J, s_top, s_any;
+  GeoSmem g = carve(smem, N_L, EC, &coef, nmu, nEt, &as, (int)sizeof(PieceT<WT>), a.N_R);
+  PieceT<WT> *co4 = reinterpret_cast<PieceT<WT> *>(coef);
+  __shared__ int s_J, s_top, s_any, s_jalt;
   double *slab = nullptr;
+  float *slabf = nullptr;
   if (num4d) {
     for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.gmu[t] = a.atmos.mu[t];
     for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.gE[t] = a.atmos.logE[t];
     __syncthreads();
     for (int b = threadIdx.x; b <= nmu - 4; b += blockDim.x) lagrange_space(as.gmu, b, as.smu + 4 * b);
     for (int b = threadIdx.x; b <= nEt - 4; b += blockDim.x) lagrange_space(as.gE, b, as.sE + 4 * b);
+    __syncthreads();
+    if (kMixed) {
+      for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
+      for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
+      for (int t = threadIdx.x; t < 4 * nmu; t += blockDim.x) as.fsmu[t] = (float)as.smu[t];
+      for (int t = threadIdx.x; t < 4 * nEt; t += blockDim.x) as.fsE[t] = (float)as.sE[t];
+    }
     slab = a.slab + (size_t)chunk * nmu * nEt;
+    slabf = reinterpret_cast<float *>(slab);
     __syncthreads();
   }
   const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
@@ -524,6 +637,7 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
     const int i = (int)(row - M.row_off);
     RowCtx c;
     if (!load_row(a, M, row, i, c, &s_J)) continue;
+    stage_deflection(c, g, &s_jalt);
     if (threadIdx.x == 0) {
       s_top = num4d ? (int)a.row_entry_top[row] : 0;
       s_any = 0;
@@ -554,12 +668,14 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
                      wg[3] * __ldg(q + 3 * S1t);
           r += wT[ii] * u;
         }
-        slab[t] = r;
+        if (kMixed) slabf[t] = (float)r;
+        else slab[t] = r;
       }
       E_eff = (kKB / kKeV) * pow(10.0, c.vec0);
       p3 = pow(10.0, 3.0 * vT);
       __syncthreads();
     }
+    const float kT_f = (float)((kKB / kKeV) * pow(10.0, c.vec0));
     const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
     const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
     const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
@@ -580,6 +696,21 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
         return;
       }
       if (invis) break;
+      if (kMixed) {
+        for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+          const float hi = (float)g.phase[t];
+          as.fphase[t] = hi;
+          as.fphase_lo[t] = (float)(g.phase[t] - (double)hi);
+        }
+        if (M.S1 <= kMaxCellsF) {
+          for (int t = threadIdx.x; t < M.S1; t += blockDim.x) {
+            const float hi = (float)cellPhi[t];
+            as.fcphi[t] = hi;
+            as.fcphi_lo[t] = (float)(cellPhi[t] - (double)hi);
+          }
+        }
+        __syncthreads();
+      }
       if (threadIdx.x == 0 && a.flop_counter) {
         int Cr = 0;
         for (int j = 0; j < M.S1; j++) Cr += (rad[j] == 1);
@@ -594,16 +725,27 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
           const int pl = t / N_L, col = t - pl * N_L;
           const int p = e0 + pl;
           const int s = g.src[col];
-          double y = 0.0;
+          WT y = WT(0);
           if (s >= 0) {
-            const double Ep = a.energies[p] / g.Z[s];
-            double I_E;
-            if (num4d)
-              I_E = eval_num4d_slab(a.atmos, as, slab, Ep, g.ABB[s], p == 0 && g.clamp0[s],
-                                    E_eff, p3);
-            else
-              I_E = eval_bb(Ep, c.vec0);
-            y = (I_E * norm - 0.0) * g.GEOM[s];
+            if (kMixed) {
+              const float Ep = (float)(a.energies[p] / g.Z[s]);
+              float I_E;
+              if (num4d)
+                I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, (float)g.ABB[s],
+                                        p == 0 && g.clamp0[s], (float)E_eff, (float)p3);
+              else
+                I_E = eval_bb_f(Ep, kT_f);
+              y = (WT)((float)norm * I_E * (float)g.GEOM[s]);
+            } else {
+              const double Ep = a.energies[p] / g.Z[s];
+              double I_E;
+              if (num4d)
+                I_E = eval_num4d_slab(a.atmos, as, slab, Ep, g.ABB[s], p == 0 && g.clamp0[s],
+                                      E_eff, p3);
+              else
+                I_E = eval_bb(Ep, c.vec0);
+              y = (WT)((I_E * norm - 0.0) * g.GEOM[s]);
+            }
           }
           co4[pl * N_L + col].y = y;
         }
@@ -611,51 +753,106 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
         // Akima-periodic piece coefficients (:566-569)
         for (int t = threadIdx.x; t < ne * (N_L - 1); t += blockDim.x) {
           const int pl = t / (N_L - 1), iv = t - pl * (N_L - 1);
-          const Piece *yr = co4 + pl * N_L;
-          double mch[5];
+          const PieceT<WT> *yr = co4 + pl * N_L;
+          WT mch[5];
 #pragma unroll
           for (int d = 0; d < 5; d++) {
             int q = periodic_chord(iv - 2 + d, N_L);
-            mch[d] = (yr[q + 1].y - yr[q].y) / (g.phase[q + 1] - g.phase[q]);
+            // knot spacings from the FP64 knots: adjacent knots closer than
+            // an FP32 ulp stay distinct
+            mch[d] = (yr[q + 1].y - yr[q].y) / (WT)(g.phase[q + 1] - g.phase[q]);
           }
-          double k1, k2, k3;
-          akima_piece(mch[0], mch[1], mch[2], mch[3], mch[4], g.phase[iv + 1] - g.phase[iv], k1,
-                      k2, k3);
-          Piece *o = co4 + pl * N_L + iv;
+          WT k1, k2, k3;
+          const WT h = (WT)(g.phase[iv + 1] - g.phase[iv]);
+          akima_piece(mch[0], mch[1], mch[2], mch[3], mch[4], h, k1, k2, k3);
+          PieceT<WT> *o = co4 + pl * N_L + iv;
           o->k1 = k1;
           o->k2 = k2;
           o->k3 = k3;
         }
         __syncthreads();
         // cell x phase accumulation (:571-598)
-        const double x_lo = g.phase[0], x_hi = g.phase[N_L - 1];
         for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
           const int k = task % N_P, grp = task / N_P;
           const int pb = grp * kEPT;
           if (pb >= ne) continue;
-          double acc[kEPT];
+          WT acc[kEPT];
 #pragma unroll
-          for (int e = 0; e < kEPT; e++) acc[e] = 0.0;
-          const double ph = a.phases[k];
+          for (int e = 0; e < kEPT; e++) acc[e] = WT(0);
           int bad = 0;
-          for (int j = 0; j < M.S1; j++) {
-            if (rad[j] != 1) continue;
-            double x = ph + cellPhi[j];
-            if (x > x_hi) {
-              while (x > x_hi) x = x - kTwoPi;
-            } else if (x < x_lo) {
-              while (x < x_lo) x = x + kTwoPi;
-            }
-            if (x < x_lo || x > x_hi) { bad = 1; break; }
-            const int iv = locate(g.phase, N_L, x);
-            const double t = x - g.phase[iv];
-            const double A = cellA[j];
+          if (kMixed) {
+            // phases as unevaluated float pairs (hi + lo) with error-free
+            // sums, so the offset t into a piece keeps ~1e-14 rad absolute
+            // accuracy instead of one FP32 ulp of the phase (~5e-7 rad)
+            const float x_lo = as.fphase[0], x_hi = as.fphase[N_L - 1];
+            const double phd = a.phases[k];
+            const float ph = (float)phd, ph_lo = (float)(phd - (double)ph);
+            const float tp = (float)kTwoPi, tp_lo = (float)(kTwoPi - (double)tp);
+            const bool cached = M.S1 <= kMaxCellsF;
+            for (int j = 0; j < M.S1; j++) {
+              if (rad[j] != 1) continue;
+              float cp, cp_lo;
+              if (cached) {
+                cp = as.fcphi[j];
+                cp_lo = as.fcphi_lo[j];
+              } else {
+                const double cpd = cellPhi[j];
+                cp = (float)cpd;
+                cp_lo = (float)(cpd - (double)cp);
+              }
+              float x, lo;
+              two_sum(ph, cp, x, lo);
+              lo += ph_lo + cp_lo;
+              if (x > x_hi) {
+                while (x > x_hi) {
+                  float e;
+                  two_sum(x, -tp, x, e);
+                  lo += e - tp_lo;
+                }
+              } else if (x < x_lo) {
+                while (x < x_lo) {
+                  float e;
+                  two_sum(x, tp, x, e);
+                  lo += e + tp_lo;
+                }
+              }
+              if (x < x_lo || x > x_hi) { bad = 1; break; }
+              const int iv = locate(as.fphase, N_L, x);
+              float th, e3;
+              two_sum(x, -as.fphase[iv], th, e3);
+              const float t = th + (e3 + lo - as.fphase_lo[iv]);
+              const float A = (float)cellA[j];
 #pragma unroll
-            for (int e = 0; e < kEPT; e++) {
-              if (pb + e < ne) {
-                const Piece q = co4[(pb + e) * N_L + iv];
-                const double s = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
-                if (s > 0.0) acc[e] += A * s;
+              for (int e = 0; e < kEPT; e++) {
+                if (pb + e < ne) {
+                  const PieceT<WT> q = co4[(pb + e) * N_L + iv];
+                  const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
+                  if (sv > WT(0)) acc[e] += A * sv;
+                }
+              }
+            }
+          } else {
+            const double x_lo = g.phase[0], x_hi = g.phase[N_L - 1];
+            const double ph = a.phases[k];
+            for (int j = 0; j < M.S1; j++) {
+              if (rad[j] != 1) continue;
+              double x = ph + cellPhi[j];
+              if (x > x_hi) {
+                while (x > x_hi) x = x - kTwoPi;
+              } else if (x < x_lo) {
+                while (x < x_lo) x = x + kTwoPi;
+              }
+              if (x < x_lo || x > x_hi) { bad = 1; break; }
+              const int iv = locate(g.phase, N_L, x);
+              const double t = x - g.phase[iv];
+              const double A = cellA[j];
+#pragma unroll
+              for (int e = 0; e < kEPT; e++) {
+                if (pb + e < ne) {
+                  const PieceT<WT> q = co4[(pb + e) * N_L + iv];
+                  const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
+                  if (sv > WT(0)) acc[e] += A * sv;
+                }
               }
             }
           }
@@ -665,7 +862,7 @@ __global__ void __launch_bounds__(kThreads) integrate_kernel(IntegrateArgs a) {
           }
 #pragma unroll
           for (int e = 0; e < kEPT; e++)
-            if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += acc[e];
+            if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += (double)acc[e];
         }
         __syncthreads();
       }
@@ -692,22 +889,36 @@ __global__ void reduce_flux_kernel(IntegrateArgs a) {
 
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   if (a.n_members <= 0) return;
-  Layout L = a.atmos.I ? make_layout(a.N_L, a.N_P, a.N_E, a.atmos.nmu, a.atmos.nE)
-                       : make_layout(a.N_L, a.N_P, a.N_E);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    attr_set = true;
+  const int pb = a.mixed ? (int)sizeof(PieceT<float>) : (int)sizeof(PieceT<double>);
+  Layout L = a.atmos.I ? make_layout(a.N_L, a.N_P, a.N_E, a.atmos.nmu, a.atmos.nE, pb, a.N_R)
+                       : make_layout(a.N_L, a.N_P, a.N_E, 0, 0, pb, a.N_R);
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[a.mixed ? 1 : 0]) {
+    if (a.mixed)
+      cudaFuncSetAttribute(integrate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024);
+    else
+      cudaFuncSetAttribute(integrate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024);
+    attr_set[a.mixed ? 1 : 0] = true;
   }
   bool any_num4d = a.atmos.I != nullptr;
   if (any_num4d) {
     size_t pre_smem = (size_t)5 * a.N_L * sizeof(double) + (size_t)4 * a.N_L * sizeof(int) +
-                      8 * sizeof(int) + 16;
+                      8 * sizeof(int) + 16 + (size_t)a.N_R * sizeof(double);
+    static bool pre_attr = false;
+    if (!pre_attr) {
+      cudaFuncSetAttribute(num4d_prepass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024);
+      pre_attr = true;
+    }
     num4d_prepass_kernel<<<(unsigned)a.n_rows, 128, pre_smem, st>>>(a);
     num4d_scan_kernel<<<(a.n_members + 127) / 128, 128, 0, st>>>(a);
   }
-  integrate_kernel<<<a.n_chunks, kThreads, L.bytes, st>>>(a);
+  if (a.mixed)
+    integrate_kernel<float><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
+  else
+    integrate_kernel<double><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
   dim3 grid((a.N_E * a.N_P + 255) / 256, a.n_members);
   reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
 }

@@ -69,6 +69,7 @@ struct IntegrateArgs {
   double *flux;             // [..] at members[m].flux_off
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
   double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
+  int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
 };
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
 
