@@ -235,7 +235,14 @@ def run_gb300(args):
                        "peak_source": "measured FP64 FMA probe on this GPU (not in "
                        "MEASURED_PEAKS.json)", "hbm_peak_gbs": pk.get("hbm_gbs"),
                        "hbm_peak_source": pk_kind}
+    plain_ll = B["loglike"].cpu().numpy().copy()
     if rank == 0:
+        out["mixed"] = mixed_leg(model, P, plain_ll, st, args)
+        out["drop_in"] = drop_in_leg(model, P, min(V, args.drop_in_vectors))
+        out["batched_vs_drop_in"] = value / out["drop_in"]["value"]
+        out["mixed_vs_drop_in"] = out["mixed"]["value"] / out["drop_in"]["value"]
+        if args.serve_seconds > 0:
+            out["serving"] = serving_leg(args)
         out["cpu_baseline"] = cpu_baseline(args, model, params)
         print(json.dumps(out))
 
@@ -259,6 +266,176 @@ def fp64_peak(device):
         best = max(best, fl / (e0.elapsed_time(e1) / 1e3) / 1e12)
     return best
 
+
+
+def mixed_leg(model, P, plain_ll, plain_st, args):
+    """Batched mixed-precision form on the same vectors: throughput and
+    |Delta log L| against the FP64 path."""
+    import torch
+    from xpsi_gb300 import batch as BT
+    ev = BT.BatchEvaluator(model, precision="mixed")
+    B = ev.upload(P)
+    for _ in range(args.warmup):
+        ev.run(B)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        ev.run(B)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ll = B["loglike"].cpu().numpy()
+    st = ev.statuses(B)
+    ok = (st == 0) & (plain_st == 0)
+    d = np.abs(ll - plain_ll)[ok]
+    rel = d / np.abs(plain_ll[ok])
+    return {"value": P.V / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "precision": "FP32 atmosphere interpolation, Akima pieces and cell x phase sums; "
+                         "FP64 rays, knots, energy integration, fold and log L",
+            "dlogL_vs_fp64": {"median": float(np.median(d)) if d.size else None,
+                              "p99": float(np.percentile(d, 99)) if d.size else None,
+                              "max": float(d.max()) if d.size else None,
+                              "frac_within_1e-3": float((d <= 1e-3).mean()) if d.size else None,
+                              "median_relative": float(np.median(rel)) if d.size else None,
+                              "vectors": int(ok.sum())},
+            "status_equal": bool((st == plain_st).all())}
+
+
+def drop_in_leg(model, P, n_vec):
+    """The plain FP64 drop-in: one parameter vector at a time through the
+    module-level replacements of the reference callables (host arrays in and
+    out, as X-PSI's HotRegion/Signal would call them)."""
+    import math as _m
+    from xpsi_gb300.cellmesh import rays as R, integrator_for_azimuthal_invariance as I
+    from xpsi_gb300.tools import energy_integrator as EI
+    from xpsi_gb300.likelihoods import default_background_marginalisation as DBM
+    from xpsi_gb300 import instrument as INS
+    N_L = model.regions[0].num_leaves
+    N_R = model.regions[0].num_rays
+    leaves = np.linspace(0.0, 2 * _m.pi, N_L)
+    phases = 2 * _m.pi * np.linspace(0.0, 1.0, N_L)
+    cph = np.linspace(0.0, 1.0, N_L)
+    logE, logEd = np.log10(model.energies), np.log10(model.instrument.energy_edges)
+    counts = np.asarray(model.data.counts, np.float64)
+    K = counts.shape[0]
+    pre = DBM.precomputation(np.asarray(model.data.counts, np.int32))
+    sup = -np.ones((K, 2))
+    sup[:, 0] = 0.0
+    atm = model.atmosphere
+    t0 = time.perf_counter()
+    for v in range(n_vec):
+        regs = []
+        for h in range(P.H):
+            mi = v * P.H + h
+            mesh = P.meshes[mi]
+            S = mesh.S0
+            rs = slice(mesh.row_off, mesh.row_off + S)
+            cs = slice(mesh.cell_off, mesh.cell_off + S * S)
+            u = P.row["u"][rs].copy()
+            ma = P.row["maxAlpha"][rs].copy()
+            r_s = P.row["r_s"][mesh.row_off]
+            t, D, CA, L, MD = R.compute_rays(1, S, r_s, u, ma, N_R)
+            L -= P.row["lag_C"][rs][:, None]
+            L *= P.row["lag_scale"][mesh.row_off]
+            theta = np.repeat(P.row["theta0"][rs][:, None], S, axis=1)
+            spec = model.regions[h]
+            st, flux = I.integrate(1, 0.0, mesh.omega, r_s, mesh.inclination,
+                                   P.cellArea[cs].reshape(S, S), P.row["radius"][rs], u, theta,
+                                   P.phi[cs].reshape(S, S), P.params[cs].reshape(S, S, 2),
+                                   P.radiates[cs].reshape(S, S), None, N_R, D, CA, L, MD,
+                                   P.row["cos_gamma"][rs], model.energies, leaves, phases,
+                                   atm if spec.atm_ext == 2 else (), None, spec.atm_ext, None, 0)
+            if st != 0:
+                break
+            e = EI.energy_integrator(1, flux / P.d_sq[mi], logE, logEd)
+            regs.append(INS.fold(model.instrument.matrix, e))
+        if len(regs) == P.H:
+            DBM.eval_marginal_likelihood(model.data.exposure, model.data.phase_edges, counts,
+                                         regs, [cph] * P.H, P.shifts[v], pre, sup, 1000, 0.0,
+                                         model.epsrel, model.epsilon, model.sigmas,
+                                         model.llzero)
+    dt = time.perf_counter() - t0
+    return {"value": n_vec / dt, "unit": UNIT, "vectors": n_vec,
+            "what": "one vector per call through the drop-in module functions "
+                    "(host arrays, H2D/D2H per call), FP64"}
+
+
+def serving_leg(args):
+    """Poisson request stream through the serving loop: even blackbody /
+    Num4D mix, sqrt_num_cells in {32, 64, 96}, num_leaves in {64, 128},
+    mixed-precision form; p50/p99 latency and throughput."""
+    import torch
+    from xpsi_gb300 import batch as BT
+    from xpsi_gb300 import synthetic as SY
+    from xpsi_gb300.serving import Server, poisson_stream
+    models = {}
+    for kind in ("bb", "num4d"):
+        for sq in (32, 64, 96):
+            for nl in (64, 128):
+                if kind == "bb":
+                    w = SY.config1_workload()
+                    m = BT.Model(regions=[BT.HotRegionSpec(atm_ext=1, sqrt_num_cells=sq,
+                                                           min_sqrt_num_cells=10,
+                                                           max_sqrt_num_cells=128,
+                                                           num_leaves=nl, num_rays=512)],
+                                 instrument=BT.Instrument(w["matrix"], w["input_edges"]),
+                                 data=BT.Data(np.zeros((300, 32), np.int32), w["phase_edges"],
+                                              w["exposure"]), num_energies=64)
+                    ref = np.array([w["mass"], w["radius_km"], w["frequency"],
+                                    math.cos(w["inclination"]), 1.0, w["colatitude"],
+                                    w["spot_radius"], w["logT"], 0.0])
+                else:
+                    m = SY.config2_model(sqrt_num_cells=sq, num_leaves=nl)
+                    ref = SY.config2_vector(seed=1)
+                ev = BT.BatchEvaluator(m)
+                P0 = BT.prepare(m, ref[None, :])
+                B0 = ev.upload(P0)
+                ev.run(B0)
+                torch.cuda.synchronize()
+                f = B0["folded"].cpu().numpy()
+                SY.attach_data(m, [f[h] for h in range(P0.H)], P0.shifts[0])
+                models[f"{kind}_{sq}_{nl}"] = (m, ref)
+                del ev, B0
+    names = sorted(models)
+    stream = poisson_stream(args.serve_rate, args.serve_seconds, args.serve_max_batch, seed=5)
+    rng = np.random.default_rng(5)
+    reqs = []
+    for t, v in stream:
+        name = names[rng.integers(len(names))]
+        m, ref = models[name]
+        if name.startswith("bb"):
+            p = np.repeat(ref[None, :], v, axis=0)
+            p[:, 5] = rng.uniform(0.5, 2.5, v)
+            p[:, 6] = rng.uniform(0.03, 0.3, v)
+            p[:, 8] = rng.uniform(0.0, 1.0, v)
+        else:
+            p = SY.config3_vectors(v, seed=int(rng.integers(1 << 30)))
+        reqs.append((t, name, p))
+    srv = Server({k: v[0] for k, v in models.items()}, hbm_budget=120 << 30, slots=4,
+                 precision="mixed")
+    futs = []
+    t0 = time.perf_counter()
+    for t, name, p in reqs:
+        while time.perf_counter() - t0 < t:
+            time.sleep(0.0002)
+        futs.append(srv.submit(name, p))
+    for f in futs:
+        f.result(timeout=1800)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = srv.latency_percentiles()
+    nv = sum(p.shape[0] for _, _, p in reqs)
+    return {"p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"], "requests": len(reqs),
+            "vectors": nv, "throughput": nv / wall, "unit": UNIT, "wall_s": wall,
+            "arrivals": f"Poisson {args.serve_rate} req/s for {args.serve_seconds} s, "
+                        f"batch sizes log-uniform on [1, {args.serve_max_batch}]",
+            "launches": srv.stats.launches, "merged_requests": srv.stats.merged_requests,
+            "peak_concurrent_launches": srv.stats.peak_concurrency,
+            "peak_device_bytes_admitted": srv.stats.peak_bytes,
+            "models": len(names), "precision": "mixed"}
 
 # ------------------------------------------------------------------ CPU legs
 def oracle_evals(model, params, n_threads, budget_s):
@@ -333,6 +510,10 @@ def main():
     ap.add_argument("--vectors", type=int, default=256)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--drop-in-vectors", type=int, default=8)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-max-batch", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

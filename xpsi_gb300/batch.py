@@ -435,3 +435,42 @@ class BatchEvaluator:
             rng = np.random.default_rng(12345)
             ll[bad] = self.model.llzero * (0.1 + 0.9 * rng.random(int(bad.sum())))
         return ll, st
+
+
+def concat_prepared(parts, model: Model) -> Prepared:
+    """One packed batch from several prepared batches of the same model
+    (offsets re-based; no mesh is rebuilt)."""
+    if len(parts) == 1:
+        return parts[0]
+    N_E, N_P = len(model.energies), model.regions[0].num_leaves
+    P = Prepared()
+    P.H = parts[0].H
+    P.V = sum(p.V for p in parts)
+    P.n_rows = sum(p.n_rows for p in parts)
+    P.n_cells = sum(p.n_cells for p in parts)
+    P.status = np.concatenate([p.status for p in parts])
+    P.row = {k: np.concatenate([p.row[k] for p in parts]) for k in parts[0].row}
+    P.cellArea = np.concatenate([p.cellArea for p in parts])
+    P.phi = np.concatenate([p.phi for p in parts])
+    P.params = np.concatenate([p.params for p in parts])
+    P.radiates = np.concatenate([p.radiates for p in parts])
+    P.d_sq = np.concatenate([p.d_sq for p in parts])
+    P.shifts = np.concatenate([p.shifts for p in parts])
+    n_m = sum(len(p.meshes) for p in parts)
+    P.meshes = (Mesh * n_m)()
+    rm, members = [], []
+    ro = co = mo = 0
+    for p in parts:
+        for i in range(len(p.meshes)):
+            q = p.meshes[i]
+            P.meshes[mo + i] = Mesh(q.S0, q.S1, q.row_off + ro, q.cell_off + co, q.omega,
+                                    q.inclination, q.image_order_limit, q.atm_ext,
+                                    (mo + i) * N_E * N_P)
+        rm.append(p.row_mesh + mo)
+        members += p.members
+        ro += p.n_rows
+        co += p.n_cells
+        mo += len(p.meshes)
+    P.row_mesh = np.concatenate(rm).astype(np.int32)
+    P.members = members
+    return P
