@@ -423,7 +423,7 @@ def serving_leg(args):
             time.sleep(0.0002)
         futs.append(srv.submit(name, p))
     for f in futs:
-        f.result(timeout=1800)
+        f.result(timeout=600)
     wall = time.perf_counter() - t0
     srv.close()
     lat = srv.latency_percentiles()

@@ -24,6 +24,8 @@ def test_same_alone_and_in_the_mix():
         futs = [srv.submit("num4d", pn[i:i + 1]) for i in range(6)]
         futs += [srv.submit("bb", pb[i:i + 1]) for i in range(5)]
         futs.append(srv.submit("num4d", pn))
+        futs.append(srv.submit("num4d", pn[:3]))
+        futs.append(srv.submit("num4d", pn[3:5]))
         res = [f.result(timeout=300) for f in futs]
     finally:
         srv.close()
@@ -33,7 +35,7 @@ def test_same_alone_and_in_the_mix():
         assert st_a[0] == st_m[0]
         if st_a[0] == 0:
             assert abs(ll_a[0] - ll_m[0]) <= 1e-12 * abs(ll_a[0])
-        ll_all, st_all = res[-1]
+        ll_all, st_all = res[11]
         if st_all[i] == 0:
             assert abs(ll_all[i] - ll_a[0]) <= 1e-12 * abs(ll_a[0])
     ll_b, st_b = res[6]

@@ -32,7 +32,7 @@ import numpy as np
 from . import batch as BT
 
 
-@dataclass
+@dataclass(eq=False)
 class _Req:
     model: str
     params: np.ndarray
@@ -42,7 +42,7 @@ class _Req:
     t_ready: float = 0.0
 
 
-@dataclass
+@dataclass(eq=False)
 class _Launch:
     model: str
     reqs: list
@@ -100,6 +100,7 @@ class Server:
         self.ready = []
         self.ready_lock = threading.Lock()
         self.stats = ServerStats()
+        self.failed = None
         self._stop = threading.Event()
         self._prep = [threading.Thread(target=self._prep_loop, daemon=True)
                       for _ in range(prep_threads)]
@@ -112,6 +113,8 @@ class Server:
     def submit(self, model: str, params) -> Future:
         if model not in self.evals:
             raise KeyError("unknown model %r" % model)
+        if self.failed is not None:
+            raise RuntimeError("the serving loop stopped") from self.failed
         f = Future()
         self.incoming.put(_Req(model, np.atleast_2d(np.asarray(params, np.float64)), f,
                                time.perf_counter()))
@@ -152,6 +155,29 @@ class Server:
         return BT.concat_prepared([r.prepared for r in reqs], self.evals[reqs[0].model].model)
 
     def _dispatch_loop(self):
+        try:
+            self._dispatch()
+        except BaseException as e:  # noqa: BLE001 - delivered to every waiting caller
+            self._fail_all(e)
+
+    def _fail_all(self, e):
+        pending = [r for L in self.inflight for r in L.reqs]
+        with self.ready_lock:
+            pending += self.ready
+            self.ready = []
+        while True:
+            try:
+                r = self.incoming.get_nowait()
+            except queue.Empty:
+                break
+            if r is not None:
+                pending.append(r)
+        for r in pending:
+            if not r.future.done():
+                r.future.set_exception(e)
+        self.failed = e
+
+    def _dispatch(self):
         torch = self.torch
         torch.cuda.set_device(self.dev)
         while True:
@@ -208,8 +234,9 @@ class Server:
             need = estimate_bytes(ev, P)
             if self.in_use + need > self.budget and self.inflight:
                 break  # wait for memory to free up
+            taken = set(id(r) for r in group)
             with self.ready_lock:
-                self.ready = [r for r in self.ready if r not in group]
+                self.ready = [r for r in self.ready if id(r) not in taken]
             slot = self.free_slots.pop(0)
             s = self.streams[slot]
             torch = self.torch
