@@ -48,6 +48,9 @@ const char *xgpu_last_error(void);
 typedef struct {
   const double *logT, *logg, *mu, *logE, *intensity;
   size_t nT, ng, nmu, nE;
+  /* optional FP32 copy of the intensity table, read by the mixed-precision
+   * integrator only (NULL: it converts from the FP64 table) */
+  const float *intensity_f32;
 } xgpu_atmos4d;
 
 /* ---------------------------------------------------------------------- */

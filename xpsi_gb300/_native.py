@@ -81,7 +81,7 @@ I64 = C.c_int64
 
 class Atmos4D(C.Structure):
     _fields_ = [("logT", P), ("logg", P), ("mu", P), ("logE", P), ("intensity", P),
-                ("nT", SZ), ("ng", SZ), ("nmu", SZ), ("nE", SZ)]
+                ("nT", SZ), ("ng", SZ), ("nmu", SZ), ("nE", SZ), ("intensity_f32", P)]
 
 
 class Mesh(C.Structure):

@@ -245,9 +245,10 @@ class BatchEvaluator:
     """Device-resident model (tables, response, data) plus per-batch buffers.
 
     precision "plain": every stage in FP64 (the drop-in's numerics).
-    precision "mixed": the integrator's atmosphere interpolation, splines and
-    cell x phase sums in FP32 (xgpu_integrate_batch_mixed); rays, energy
-    integration, fold and the likelihood sum stay FP64."""
+    precision "mixed": the integrator's atmosphere interpolation (from an
+    FP32 copy of the table), splines and cell x phase sums in FP32
+    (xgpu_integrate_batch_mixed); rays, energy integration, fold and the
+    likelihood stay FP64."""
 
     def __init__(self, model: Model, device=0, precision="plain"):
         import torch
@@ -287,9 +288,11 @@ class BatchEvaluator:
         if model.atmosphere is not None:
             self.atm_t = [t(a) for a in model.atmosphere]
             a = self.atm_t
+            self.atm_f32 = a[4].to(torch.float32) if precision == "mixed" else None
             self.atmos = Atmos4D(a[0].data_ptr(), a[1].data_ptr(), a[2].data_ptr(),
                                  a[3].data_ptr(), a[4].data_ptr(), a[0].numel(),
-                                 a[1].numel(), a[2].numel(), a[3].numel())
+                                 a[1].numel(), a[2].numel(), a[3].numel(),
+                                 self.atm_f32.data_ptr() if self.atm_f32 is not None else None)
 
     # ---------------------------------------------------------------- upload
     def upload(self, P: Prepared, pinned=None):

@@ -54,7 +54,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
             raise ValueError("numerical atmosphere data were not preloaded")
         keep = tuple(f64(a) for a in hot_atmosphere[:5])
         atmos = Atmos4D(*(k.ctypes.data for k in keep), keep[0].size, keep[1].size,
-                        keep[2].size, keep[3].size)
+                        keep[2].size, keep[3].size, None)
     flux = np.empty((E.size, P.size))
     st = check(lib().xgpu_integrate(
         float(R), float(omega), float(r_s), float(inclination), S0, S1, ptr(A),

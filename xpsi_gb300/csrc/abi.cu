@@ -149,7 +149,7 @@ int atmos_device(const xgpu_atmos4d *A, cudaStream_t st, xg::Atmos4D *out) {
   g_atmos.sample = smp;
   g_atmos.dev = dev;
   g_atmos.view = xg::Atmos4D{pT, pg, pm, pE, pI, (int)A->nT, (int)A->ng, (int)A->nmu,
-                             (int)A->nE};
+                             (int)A->nE, nullptr};
   *out = g_atmos.view;
   return 0;
 }
@@ -263,7 +263,7 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.energies = d->energies; a.leaves = d->leaves; a.phases = d->phases;
   a.atmos = xg::Atmos4D{d->atmos.logT, d->atmos.logg, d->atmos.mu, d->atmos.logE,
                         d->atmos.intensity, (int)d->atmos.nT, (int)d->atmos.ng,
-                        (int)d->atmos.nmu, (int)d->atmos.nE};
+                        (int)d->atmos.nmu, (int)d->atmos.nE, d->atmos.intensity_f32};
   a.n_chunks = n_chunks;
   a.chunk_r0 = dr0.as<int64_t>();
   a.chunk_r1 = dr1.as<int64_t>();
@@ -408,7 +408,7 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   d.energies = dE.as<double>(); d.leaves = dLv.as<double>(); d.phases = dP.as<double>();
   if (atm_ext == 2) {
     d.atmos = xgpu_atmos4d{A.logT, A.logg, A.mu, A.logE, A.I, (size_t)A.nT, (size_t)A.ng,
-                           (size_t)A.nmu, (size_t)A.nE};
+                           (size_t)A.nmu, (size_t)A.nE, nullptr};
   }
   d.flux = dF.as<double>();
   d.mesh_status = dst.as<int32_t>();

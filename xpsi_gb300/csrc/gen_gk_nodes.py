@@ -109,7 +109,9 @@ def main():
         K = 2 * n + 1
         tag = f"{prefix}K{K}"
         lines.append(f"#define {tag}_HALF {half}")
-        fmt = lambda v: mp.nstr(v, 25, min_fixed=1, max_fixed=0)
+        # values below 1e-30 are round-off of exact zeros
+        fmt = lambda v: mp.nstr(v if abs(v) > mp.mpf(10) ** -30 else mp.mpf(0), 25,
+                                min_fixed=1, max_fixed=0)
         lines.append(f"GK_TABLE {tag}_X[{half}] = {{")
         lines += [f"    {fmt(v)}," for v in xk] + ["};"]
         lines.append(f"GK_TABLE {tag}_WK[{half}] = {{")

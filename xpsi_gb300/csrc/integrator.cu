@@ -39,6 +39,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kEPT = 8;  // energies per accumulation task
 constexpr int kMaxCellsF = 512;  // cells per parallel held as FP32 pairs (mixed form)
+constexpr int kMaxEnergiesF = 1024;  // energies held in FP32 (mixed form)
 
 // Akima piece of one energy row: value at the left knot and the three
 // polynomial coefficients (FP64: 32 bytes, two 16-byte shared loads; FP32:
@@ -342,6 +343,9 @@ struct AtmSmem {
   float *fphase;         // FP32 copy of the phase knots
   float *fphase_lo;      // phase knot minus its FP32 copy
   float *fcphi, *fcphi_lo;  // cell azimuths of the parallel as float pairs (<= kMaxCellsF)
+  float *fcarea;            // cell areas of the parallel (<= kMaxCellsF)
+  float *finvZ, *fabb, *fgeom;  // per profile column: 1/Z, mu eta, geometric factor
+  float *fE;                // energies
 };
 
 // inverse denominators of the 4-point Lagrange basis on grid[b..b+3]
@@ -474,7 +478,7 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
             + (size_t)ec * N_L * piece_bytes       // coefficients
             + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
             + (size_t)(2 * N_L + nmu + nE) * 5 * sizeof(float)  // FP32 copies (mixed form)
-            + (size_t)2 * kMaxCellsF * sizeof(float)
+            + (size_t)(3 * kMaxCellsF + 3 * N_L + kMaxEnergiesF) * sizeof(float)
             + (size_t)N_R * sizeof(double)  // staged deflection table
             + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 64;
   return L;
@@ -506,6 +510,11 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
     atm->fphase_lo = f; f += N_L;
     atm->fcphi = f; f += kMaxCellsF;
     atm->fcphi_lo = f; f += kMaxCellsF;
+    atm->fcarea = f; f += kMaxCellsF;
+    atm->finvZ = f; f += N_L;
+    atm->fabb = f; f += N_L;
+    atm->fgeom = f; f += N_L;
+    atm->fE = f; f += kMaxEnergiesF;
     d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(f) + 15) & ~uintptr_t(15));
   }
   int *ip = reinterpret_cast<int *>(d);
@@ -578,6 +587,135 @@ __global__ void num4d_scan_kernel(IntegrateArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Cell x phase sums (:571-598).  A task is one signal phase and kEPT energies
+// of the current chunk; it walks the radiating cells of the parallel in
+// azimuth order, so a cell's interval is found by stepping forward from the
+// previous cell's (one or two knot comparisons) rather than by bisection, and
+// each (cell, energy) costs the piece's Horner form plus one FMA.
+// ---------------------------------------------------------------------------
+constexpr int kWrapLimit = 1024;  // 2 pi shifts of a cell phase (a few suffice)
+
+// FP64 phase of cell j at signal phase ph, wrapped into the knot range
+// (:575-586).  Returns the interval, found by walking forward from `hint`
+// (the previous cell's interval) or by bisection, or -1 when the phase does
+// not land in the knot range.
+struct CellPhaseD {
+  const double *knot;
+  int N_L;
+  double x_lo, x_hi, ph;
+  const double *cphi;
+  __device__ __forceinline__ int operator()(int j, int hint, double &t) const {
+    double x = ph + cphi[j];
+    if (x > x_hi) {
+      for (int w = 0; x > x_hi && w < kWrapLimit; w++) x = x - kTwoPi;
+    } else if (x < x_lo) {
+      for (int w = 0; x < x_lo && w < kWrapLimit; w++) x = x + kTwoPi;
+    }
+    if (!(x >= x_lo && x <= x_hi)) return -1;
+    int iv = hint;
+    if (iv < 0 || knot[iv] > x) iv = locate(knot, N_L, x);
+    else
+      while (iv < N_L - 2 && knot[iv + 1] <= x) iv++;
+    t = x - knot[iv];
+    return iv;
+  }
+};
+
+// the same with phases as unevaluated float pairs (hi + lo) and error-free
+// sums, so the offset t keeps ~1e-14 rad absolute accuracy instead of one
+// FP32 ulp of the phase (~5e-7 rad)
+struct CellPhaseF {
+  const float *knot, *knot_lo;
+  int N_L;
+  float x_lo, x_hi, ph, ph_lo, tp, tp_lo;
+  const float *cphi, *cphi_lo;  // cached pairs, or null
+  const double *cphi_d;
+  __device__ __forceinline__ int operator()(int j, int hint, float &t) const {
+    float cp, cp_lo;
+    if (cphi) {
+      cp = cphi[j];
+      cp_lo = cphi_lo[j];
+    } else {
+      const double c = cphi_d[j];
+      cp = (float)c;
+      cp_lo = (float)(c - (double)cp);
+    }
+    float x, lo;
+    two_sum(ph, cp, x, lo);
+    lo += ph_lo + cp_lo;
+    if (x > x_hi) {
+      for (int w = 0; x > x_hi && w < kWrapLimit; w++) {
+        float e;
+        two_sum(x, -tp, x, e);
+        lo += e - tp_lo;
+      }
+    } else if (x < x_lo) {
+      for (int w = 0; x < x_lo && w < kWrapLimit; w++) {
+        float e;
+        two_sum(x, tp, x, e);
+        lo += e + tp_lo;
+      }
+    }
+    if (!(x >= x_lo && x <= x_hi)) return -1;
+    int iv = hint;
+    if (iv < 0 || knot[iv] > x) iv = locate(knot, N_L, x);
+    else
+      while (iv < N_L - 2 && knot[iv + 1] <= x) iv++;
+    float th, e3;
+    two_sum(x, -knot[iv], th, e3);
+    t = th + (e3 + lo - knot_lo[iv]);
+    return iv;
+  }
+};
+
+struct AreaD {
+  const double *A;
+  __device__ __forceinline__ double operator()(int j) const { return A[j]; }
+};
+struct AreaF {
+  const float *Af;  // cached, or null
+  const double *A;
+  __device__ __forceinline__ float operator()(int j) const { return Af ? Af[j] : (float)A[j]; }
+};
+
+// the reference adds an interpolant value when it is > 0 (:593-594).  FP64:
+// tested on the high word (integer pipe): positive normal numbers pass; NaN,
+// infinities and positive subnormals (< 2.3e-308, no measurable
+// contribution) do not.
+__device__ __forceinline__ bool positive(double v) {
+  const int hi = __double2hiint(v);
+  return hi >= 0x00100000 && hi < 0x7ff00000;
+}
+__device__ __forceinline__ bool positive(float v) { return v > 0.0f; }
+
+// sums over the radiating cells of one parallel at one signal phase for the
+// energies pb .. pb+kEPT-1 of the chunk; false when a cell phase cannot be
+// wrapped into the knot range (the reference's terminate)
+template <typename WT, typename CP, typename AR>
+__device__ __forceinline__ bool cell_phase_sums(const CP &cp, const AR &area, int S1,
+                                                const int32_t *rad, const PieceT<WT> *co4,
+                                                int N_L, int pb, int ne, WT (&acc)[kEPT]) {
+  int hint = -1;
+  for (int j = 0; j < S1; j++) {
+    if (rad[j] != 1) continue;
+    WT t;
+    const int iv = cp(j, hint, t);
+    if (iv < 0) return false;
+    hint = iv;
+    const WT A = area(j);
+#pragma unroll
+    for (int e = 0; e < kEPT; e++) {
+      if (pb + e < ne) {
+        const PieceT<WT> q = co4[(pb + e) * N_L + iv];
+        const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
+        if (positive(sv)) acc[e] += A * sv;
+      }
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // main integrator kernel: one CTA per chunk of parallels of one mesh
 // ---------------------------------------------------------------------------
 // WT = double: the plain FP64 drop-in.  WT = float: the mixed-precision form
@@ -613,12 +751,19 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     __syncthreads();
     if (kMixed) {
       for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
+      for (int t = threadIdx.x; t < min(N_E, kMaxEnergiesF); t += blockDim.x)
+        as.fE[t] = (float)a.energies[t];
       for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
       for (int t = threadIdx.x; t < 4 * nmu; t += blockDim.x) as.fsmu[t] = (float)as.smu[t];
       for (int t = threadIdx.x; t < 4 * nEt; t += blockDim.x) as.fsE[t] = (float)as.sE[t];
     }
     slab = a.slab + (size_t)chunk * nmu * nEt;
     slabf = reinterpret_cast<float *>(slab);
+    __syncthreads();
+  }
+  if (kMixed && !num4d) {
+    for (int t = threadIdx.x; t < min(N_E, kMaxEnergiesF); t += blockDim.x)
+      as.fE[t] = (float)a.energies[t];
     __syncthreads();
   }
   const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
@@ -658,18 +803,40 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
       lagrange4(a.atmos.logT, bT, vT, wT);
       lagrange4(a.atmos.logg, bg, vg, wg);
       const size_t S1t = (size_t)nmu * nEt, S0t = (size_t)a.atmos.ng * S1t;
-      const double *base = a.atmos.I + bT * S0t + bg * S1t;
-      for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
-        double r = 0.0;
+      if (kMixed && a.atmos.I32 != nullptr) {
+        // FP32 contraction from the FP32 copy of the table
+        const float *basef = a.atmos.I32 + bT * S0t + bg * S1t;
+        float wTf[4], wgf[4];
 #pragma unroll
         for (int ii = 0; ii < 4; ii++) {
-          const double *q = base + ii * S0t + t;
-          double u = wg[0] * __ldg(q) + wg[1] * __ldg(q + S1t) + wg[2] * __ldg(q + 2 * S1t) +
-                     wg[3] * __ldg(q + 3 * S1t);
-          r += wT[ii] * u;
+          wTf[ii] = (float)wT[ii];
+          wgf[ii] = (float)wg[ii];
         }
-        if (kMixed) slabf[t] = (float)r;
-        else slab[t] = r;
+        for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
+          float r = 0.0f;
+#pragma unroll
+          for (int ii = 0; ii < 4; ii++) {
+            const float *q = basef + ii * S0t + t;
+            float u = wgf[0] * __ldg(q) + wgf[1] * __ldg(q + S1t) + wgf[2] * __ldg(q + 2 * S1t) +
+                      wgf[3] * __ldg(q + 3 * S1t);
+            r += wTf[ii] * u;
+          }
+          slabf[t] = r;
+        }
+      } else {
+        const double *base = a.atmos.I + bT * S0t + bg * S1t;
+        for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
+          double r = 0.0;
+#pragma unroll
+          for (int ii = 0; ii < 4; ii++) {
+            const double *q = base + ii * S0t + t;
+            double u = wg[0] * __ldg(q) + wg[1] * __ldg(q + S1t) + wg[2] * __ldg(q + 2 * S1t) +
+                       wg[3] * __ldg(q + 3 * S1t);
+            r += wT[ii] * u;
+          }
+          if (kMixed) slabf[t] = (float)r;
+          else slab[t] = r;
+        }
       }
       E_eff = (kKB / kKeV) * pow(10.0, c.vec0);
       p3 = pow(10.0, 3.0 * vT);
@@ -707,6 +874,15 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             const float hi = (float)cellPhi[t];
             as.fcphi[t] = hi;
             as.fcphi_lo[t] = (float)(cellPhi[t] - (double)hi);
+            as.fcarea[t] = (float)cellA[t];
+          }
+        }
+        for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+          const int sidx = g.src[t];
+          if (sidx >= 0) {
+            as.finvZ[sidx] = (float)(1.0 / g.Z[sidx]);
+            as.fabb[sidx] = (float)g.ABB[sidx];
+            as.fgeom[sidx] = (float)g.GEOM[sidx];
           }
         }
         __syncthreads();
@@ -728,14 +904,15 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           WT y = WT(0);
           if (s >= 0) {
             if (kMixed) {
-              const float Ep = (float)(a.energies[p] / g.Z[s]);
+              const float Ef = p < kMaxEnergiesF ? as.fE[p] : (float)a.energies[p];
+              const float Ep = Ef * as.finvZ[s];
               float I_E;
               if (num4d)
-                I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, (float)g.ABB[s],
+                I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, as.fabb[s],
                                         p == 0 && g.clamp0[s], (float)E_eff, (float)p3);
               else
                 I_E = eval_bb_f(Ep, kT_f);
-              y = (WT)((float)norm * I_E * (float)g.GEOM[s]);
+              y = (WT)((float)norm * I_E * as.fgeom[s]);
             } else {
               const double Ep = a.energies[p] / g.Z[s];
               double I_E;
@@ -779,83 +956,23 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           WT acc[kEPT];
 #pragma unroll
           for (int e = 0; e < kEPT; e++) acc[e] = WT(0);
-          int bad = 0;
-          if (kMixed) {
-            // phases as unevaluated float pairs (hi + lo) with error-free
-            // sums, so the offset t into a piece keeps ~1e-14 rad absolute
-            // accuracy instead of one FP32 ulp of the phase (~5e-7 rad)
-            const float x_lo = as.fphase[0], x_hi = as.fphase[N_L - 1];
+          bool ok;
+          if constexpr (kMixed) {
             const double phd = a.phases[k];
-            const float ph = (float)phd, ph_lo = (float)(phd - (double)ph);
-            const float tp = (float)kTwoPi, tp_lo = (float)(kTwoPi - (double)tp);
+            const float ph = (float)phd;
+            const float tp = (float)kTwoPi;
             const bool cached = M.S1 <= kMaxCellsF;
-            for (int j = 0; j < M.S1; j++) {
-              if (rad[j] != 1) continue;
-              float cp, cp_lo;
-              if (cached) {
-                cp = as.fcphi[j];
-                cp_lo = as.fcphi_lo[j];
-              } else {
-                const double cpd = cellPhi[j];
-                cp = (float)cpd;
-                cp_lo = (float)(cpd - (double)cp);
-              }
-              float x, lo;
-              two_sum(ph, cp, x, lo);
-              lo += ph_lo + cp_lo;
-              if (x > x_hi) {
-                while (x > x_hi) {
-                  float e;
-                  two_sum(x, -tp, x, e);
-                  lo += e - tp_lo;
-                }
-              } else if (x < x_lo) {
-                while (x < x_lo) {
-                  float e;
-                  two_sum(x, tp, x, e);
-                  lo += e + tp_lo;
-                }
-              }
-              if (x < x_lo || x > x_hi) { bad = 1; break; }
-              const int iv = locate(as.fphase, N_L, x);
-              float th, e3;
-              two_sum(x, -as.fphase[iv], th, e3);
-              const float t = th + (e3 + lo - as.fphase_lo[iv]);
-              const float A = (float)cellA[j];
-#pragma unroll
-              for (int e = 0; e < kEPT; e++) {
-                if (pb + e < ne) {
-                  const PieceT<WT> q = co4[(pb + e) * N_L + iv];
-                  const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
-                  if (sv > WT(0)) acc[e] += A * sv;
-                }
-              }
-            }
+            CellPhaseF cp{as.fphase, as.fphase_lo, N_L, as.fphase[0], as.fphase[N_L - 1], ph,
+                          (float)(phd - (double)ph), tp, (float)(kTwoPi - (double)tp),
+                          cached ? as.fcphi : nullptr, cached ? as.fcphi_lo : nullptr, cellPhi};
+            AreaF ar{cached ? as.fcarea : nullptr, cellA};
+            ok = cell_phase_sums<WT>(cp, ar, M.S1, rad, co4, N_L, pb, ne, acc);
           } else {
-            const double x_lo = g.phase[0], x_hi = g.phase[N_L - 1];
-            const double ph = a.phases[k];
-            for (int j = 0; j < M.S1; j++) {
-              if (rad[j] != 1) continue;
-              double x = ph + cellPhi[j];
-              if (x > x_hi) {
-                while (x > x_hi) x = x - kTwoPi;
-              } else if (x < x_lo) {
-                while (x < x_lo) x = x + kTwoPi;
-              }
-              if (x < x_lo || x > x_hi) { bad = 1; break; }
-              const int iv = locate(g.phase, N_L, x);
-              const double t = x - g.phase[iv];
-              const double A = cellA[j];
-#pragma unroll
-              for (int e = 0; e < kEPT; e++) {
-                if (pb + e < ne) {
-                  const PieceT<WT> q = co4[(pb + e) * N_L + iv];
-                  const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
-                  if (sv > WT(0)) acc[e] += A * sv;
-                }
-              }
-            }
+            CellPhaseD cp{g.phase, N_L, g.phase[0], g.phase[N_L - 1], a.phases[k], cellPhi};
+            AreaD ar{cellA};
+            ok = cell_phase_sums<WT>(cp, ar, M.S1, rad, co4, N_L, pb, ne, acc);
           }
+          const int bad = !ok;
           if (bad) {
             atomicExch(&a.member_status[m], (int)kPulseFail);
             continue;

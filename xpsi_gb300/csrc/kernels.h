@@ -39,6 +39,7 @@ struct MemberDesc {
 struct Atmos4D {
   const double *logT, *logg, *mu, *logE, *I;
   int nT, ng, nmu, nE;
+  const float *I32;  // FP32 copy of the table for the mixed form (or null)
 };
 
 struct IntegrateArgs {

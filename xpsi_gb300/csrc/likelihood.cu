@@ -4,10 +4,11 @@
 //   xpsi/likelihoods/default_background_marginalisation.pyx:38-734.
 //
 // One warp per (likelihood evaluation, channel).  Lanes integrate the
-// Akima-periodic phase interpolant of each component over their phase bins;
-// the scalar Newton / window logic is replicated in every lane (all lanes see
-// identical values, so control flow stays warp-uniform) and the marginal
-// integral is a QUADPACK-style adaptive Gauss-Kronrod-21 quadrature run to
+// Akima-periodic phase interpolant of each component over their phase bins
+// and hold one phase bin each for the channel sums (Newton steps, Gaussian
+// width, the normalisation A), which are reduced with xor-butterfly shuffles
+// so every lane holds the same bits and control flow stays warp-uniform;
+// the marginal integral is a QUADPACK-style adaptive Gauss-Kronrod-21 quadrature run to
 // relative 1e-13 whose 21 node evaluations per panel are spread over the
 // lanes.  The reference's CQUAD call (:416-419) asks for relative 1e-8 on
 // this smooth integrand, so both converge to the same integral.  The channel
@@ -71,13 +72,26 @@ __device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
   return exp(x - m.A);
 }
 
-// :140-173 (returns the step; writes the Gaussian width)
-__device__ __forceinline__ double newton_delta(const Marg &m, double B, double &std) {
+// sum over the warp; the butterfly adds the same pairs in every lane, so all
+// lanes return identical bits
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// :140-173 (returns the step; writes the Gaussian width); lane-parallel over
+// the phase bins.  pow(s, 2.0) of the reference is s * s, as its C compiler
+// emits it.
+__device__ __forceinline__ double newton_delta(const Marg &m, double B, int lane, double &std) {
   double x = 0.0, y = 0.0;
-  for (int j = 0; j < m.n; j++) {
-    y += m.data[j] / (m.star[j] + B);
-    x += m.data[j] / pow(m.star[j] + B, 2.0);
+  for (int j = lane; j < m.n; j += 32) {
+    const double s = m.star[j] + B;
+    y += m.data[j] / s;
+    x += m.data[j] / (s * s);
   }
+  y = warp_sum(y);
+  x = warp_sum(x);
   y = 2.0 * m.T - 2.0 * y;
   x *= 2.0;
   std = sqrt(2.0 / x);
@@ -237,7 +251,8 @@ __device__ double warp_marginal(const Marg &m, WarpSmem &w, int lane, double a, 
   if (epsabs <= 0.0 && er < 50.0 * eps) er = 50.0 * eps;
   double r = warp_qag21_core(m, w, lane, a, b, epsabs, er);
   if (r == 0.0) {
-    double fa = marginal_integrand(m, a), fb = marginal_integrand(m, b);
+    double fa = marginal_integrand(m, a);
+    double fb = marginal_integrand(m, b);
     if (fa != 0.0 || fb != 0.0) {
       double mid = 0.5 * (a + b);
       double rl = (fa != 0.0) ? warp_dyadic(m, w, lane, a, mid, true, er)
@@ -294,10 +309,12 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   }
   __syncwarp();
   double av_STAR = 0.0, av_DATA = 0.0;
-  for (int j = 0; j < B; j++) {
+  for (int j = lane; j < B; j += 32) {
     av_STAR += w.star[j];
     av_DATA += w.data[j];
   }
+  av_STAR = warp_sum(av_STAR);
+  av_DATA = warp_sum(av_DATA);
   const size_t o = (size_t)v * a.K + ch;
   int flag = 0;
   double term = 0.0, Bout = 0.0;
@@ -340,7 +357,7 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
         }
       }
       double stdv;
-      double dB = newton_delta(m, Bv, stdv);
+      double dB = newton_delta(m, Bv, lane, stdv);
       int counter = 0, steps = 0;
       // the reference's Newton loop (:336-352) has no step limit; 10000 steps
       // bound it here (convergence takes a handful)
@@ -351,10 +368,14 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
           else counter = 2;
           Bv = B_min;
         }
-        dB = newton_delta(m, Bv, stdv);
+        dB = newton_delta(m, Bv, lane, stdv);
       }
       double std_est = 0.0;
-      for (int j = 0; j < B; j++) std_est += w.data[j] / pow(w.star[j] + Bv, 2.0);
+      for (int j = lane; j < B; j += 32) {
+        const double sb = w.star[j] + Bv;
+        std_est += w.data[j] / (sb * sb);
+      }
+      std_est = warp_sum(std_est);
       if (std_est > 0.0) std_est = sqrt(1.0 / std_est);
       else std_est = 1e90;
       double lower = Bv - a.sigmas * std_est, upper = Bv + a.sigmas * std_est;
@@ -371,16 +392,17 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
       }
       if (Bi < lower) Bi = lower;
       else if (Bi > upper) Bi = upper;
-      double A = 0.0;
-      for (int j = 0; j < B; j++) {
+      double A = 0.0, dsum = 0.0;
+      for (int j = lane; j < B; j += 32) {
         double c = SCALE * (w.star[j] + Bi);
         if (c > 0.0) A += w.data[j] * log(c) - c;
         else if (are_equal(c, 0.0) && are_equal(w.data[j], 0.0)) {}
         else A += a.llzero;
+        dsum += w.data[j];
       }
+      A = warp_sum(A);
+      dsum = warp_sum(dsum);
       m.A = A;
-      double dsum = 0.0;
-      for (int j = 0; j < B; j++) dsum += w.data[j];
       double result;
       if (dsum == 0.0) {
         // no counts in the channel: every term is -c_j, so the integrand is

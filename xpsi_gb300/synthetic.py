@@ -162,14 +162,17 @@ def config3_vectors(V=4096, seed=3):
 
 def attach_data(model, registered_by_region, shifts, seed=20261203):
     """Replace the model's counts by Poisson draws from the summed registered
-    signals of its hot regions (each [K, N_P], phase-shifted by `shifts`)."""
+    signals of its hot regions (each [K, N_P]).  The likelihood integrates a
+    region's signal over [edge + shift, edge' + shift]
+    (compute_expected_counts.pyx:146-152), so the count rate at data phase x
+    is signal(x + shift)."""
     N_P = registered_by_region[0].shape[1]
     ph = np.linspace(0.0, 1.0, N_P)
     total = np.zeros_like(registered_by_region[0])
     fine = np.linspace(0.0, 1.0, N_P)
     for reg, s in zip(registered_by_region, shifts):
         for c in range(reg.shape[0]):
-            total[c] += np.interp((fine - s) % 1.0, ph, reg[c])
+            total[c] += np.interp((fine + s) % 1.0, ph, reg[c])
     model.data.counts = poisson_data(total, ph, model.data.phase_edges, model.data.exposure,
                                      seed=seed)
     return model
