@@ -38,8 +38,9 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kEPT = 8;  // energies per accumulation task
-constexpr int kMaxCellsF = 512;  // cells per parallel held as FP32 pairs (mixed form)
-constexpr int kMaxEnergiesF = 1024;  // energies held in FP32 (mixed form)
+constexpr int kMaxCellsF = 256;  // cells per parallel held as FP32 pairs in shared memory
+constexpr int kMaxEnergiesF = 256;  // energies held in FP32 (mixed form)
+constexpr int kStrip = 8;  // Akima pieces per thread, built from a sliding window of chords
 
 // Akima piece of one energy row: value at the left knot and the three
 // polynomial coefficients (FP64: 32 bytes, two 16-byte shared loads; FP32:
@@ -64,6 +65,9 @@ struct GeoSmem {
   double *rD;  // the parallel's deflection table, staged for the binary searches
   int *src, *calc, *term, *clamp0;
   int *flags;  // [0] terminate, [1] invisible image, [2] any evaluation, [3] last_top
+  double *lgE;  // [EC] log10 of the chunk's energies (FP64 path, Num4D)
+  double *lzs;  // [N_L] log10(Z) + log10(E_eff) per leaf (FP64 path, Num4D)
+  int *sc_exp;  // [EC] binary exponent of the largest |profile value| per energy row
 };
 
 
@@ -306,9 +310,10 @@ __device__ void stage_deflection(RowCtx &c, GeoSmem &g, int *s_jalt) {
   __syncthreads();
 }
 
-__device__ __forceinline__ double eval_bb(double E, double vec0) {
-  double temp = (kKB / kKeV) * pow(10.0, vec0);
-  return E * E * E / (exp(E / temp) - 1.0);
+// hot_BB.pyx:54-82; kT = k_B 10^logT / keV is the same for every call of a
+// parallel and is computed once per parallel
+__device__ __forceinline__ double eval_bb(double E, double kT) {
+  return E * E * E / (exp(E / kT) - 1.0);
 }
 
 __device__ __forceinline__ int stencil_base(const double *g, int n, double v) {
@@ -343,7 +348,7 @@ struct AtmSmem {
   float *fphase;         // FP32 copy of the phase knots
   float *fphase_lo;      // phase knot minus its FP32 copy
   float *fcphi, *fcphi_lo;  // cell azimuths of the parallel as float pairs (<= kMaxCellsF)
-  float *fcarea;            // cell areas of the parallel (<= kMaxCellsF)
+  float *fcarea, *fcarea_lo;  // cell areas of the parallel as float pairs (<= kMaxCellsF)
   float *finvZ, *fabb, *fgeom;  // per profile column: 1/Z, mu eta, geometric factor
   float *fE;                // energies
 };
@@ -372,14 +377,15 @@ __device__ __forceinline__ void lagrange_w(const double *P, const double *S, int
 // contracted into `slab` [nmu][nE]: the remaining 4 x 4 (mu, energy) stencil
 // (hot_Num4D.pyx:248-439; the stencil bases are those the reference's cached
 // walk lands on, see the file header for the mu > 1 case)
+// (the caller passes v3 = log10(E / E_eff) as log10 E - log10 Z - log10 E_eff
+// from per-energy and per-leaf logarithms: one subtraction per evaluation)
 __device__ __forceinline__ double eval_num4d_slab(const Atmos4D &A, const AtmSmem &as,
-                                                  const double *slab, double E, double mu,
-                                                  bool clamp_mu, double E_eff, double p3) {
+                                                  const double *slab, double v3, double mu,
+                                                  bool clamp_mu, double p3) {
   double v2 = mu;
   const double mu_hi = as.gmu[A.nmu - 1];
   if (v2 > mu_hi && clamp_mu) v2 = mu_hi;
   if (v2 < as.gmu[0]) v2 = as.gmu[0];
-  double v3 = log10(E / E_eff);
   if (v3 < as.gE[0]) v3 = as.gE[0];
   if (v3 > as.gE[A.nE - 1]) v3 = as.gE[A.nE - 1];
   const int b2 = stencil_base(as.gmu, A.nmu, v2);
@@ -406,6 +412,45 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   float bb = __fsub_rn(s, a);
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
+
+// Double-float numbers: an unevaluated sum h + l of two floats, about 48
+// significant bits.  The FP64 path evaluates its cell x phase sums in this
+// form: an FP32 instruction issues at 64x the FP64 rate on this GPU and a
+// double-float multiply-add is ~15 FP32 instructions (Dekker's product
+// error through the FMA, Knuth's two-sum, a fast two-sum renormalisation), so
+// the sums keep FP64-class accuracy (~1e-14 relative) at a fraction of the
+// FP64 pipe's time.  The _rn intrinsics keep the compiler from contracting
+// or reassociating the error-free transformations.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_split(double v) {
+  const float h = (float)v;
+  return DF{h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double df_value(DF a) { return (double)a.h + (double)a.l; }
+// Dekker: s + e == a + b when |a| >= |b|
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// a * b + c (the a.l * b.l term, ~2^-48 relative, is dropped)
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  float s, f;
+  two_sum(p, c.h, s, f);
+  f = __fadd_rn(f, __fadd_rn(e, c.l));
+  return fast_two_sum(s, f);
+}
+
+// an Akima piece in double-float form, scaled by a power of two per energy
+// row (same 32 bytes as the FP64 piece it replaces in shared memory)
+struct __align__(16) PieceDF {
+  DF y, k1, k2, k3;
+};
 __device__ __forceinline__ int stencil_base_f(const float *g, int n, float v) {
   int lo = 0, hi = n - 1;
   while (hi > lo + 1) {
@@ -477,11 +522,19 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
   L.bytes = (size_t)5 * N_L * sizeof(double)      // phase, leafphase, Z, ABB, GEOM
             + (size_t)ec * N_L * piece_bytes       // coefficients
             + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
-            + (size_t)(2 * N_L + nmu + nE) * 5 * sizeof(float)  // FP32 copies (mixed form)
-            + (size_t)(3 * kMaxCellsF + 3 * N_L + kMaxEnergiesF) * sizeof(float)
+            + (size_t)(nmu + nE) * 5 * sizeof(float)   // their FP32 copies (mixed form)
+            + (size_t)(5 * N_L + 4 * kMaxCellsF + kMaxEnergiesF) * sizeof(float)
             + (size_t)N_R * sizeof(double)  // staged deflection table
-            + (size_t)4 * N_L * sizeof(int) + 8 * sizeof(int) + 64;
+            + (size_t)(ec + N_L) * sizeof(double)  // lgE, lzs
+            + (size_t)(4 * N_L + 8 + ec) * sizeof(int) + 64;
   return L;
+}
+
+// bytes carve() takes with no coefficients and no atmosphere arrays (the
+// Num4D pre-pass)
+inline size_t geometry_bytes(int N_L, int N_R) {
+  return (size_t)N_R * sizeof(double) + (size_t)6 * N_L * sizeof(double) + 16 /* alignment */ +
+         (size_t)(4 * N_L + 8) * sizeof(int) + 16;
 }
 
 __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0, int nE = 0,
@@ -494,6 +547,8 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
   g.Z = d; d += N_L;
   g.ABB = d; d += N_L;
   g.GEOM = d; d += N_L;
+  g.lzs = d; d += N_L;
+  g.lgE = d; d += EC;
   d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(d) + 15) & ~uintptr_t(15));
   *coef = d; d += (size_t)EC * N_L * piece_bytes / 8;
   if (atm) {
@@ -511,6 +566,7 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
     atm->fcphi = f; f += kMaxCellsF;
     atm->fcphi_lo = f; f += kMaxCellsF;
     atm->fcarea = f; f += kMaxCellsF;
+    atm->fcarea_lo = f; f += kMaxCellsF;
     atm->finvZ = f; f += N_L;
     atm->fabb = f; f += N_L;
     atm->fgeom = f; f += N_L;
@@ -522,7 +578,8 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
   g.calc = ip; ip += N_L;
   g.term = ip; ip += N_L;
   g.clamp0 = ip; ip += N_L;
-  g.flags = ip;
+  g.flags = ip; ip += 8;
+  g.sc_exp = ip;
   return g;
 }
 
@@ -538,7 +595,6 @@ __global__ void __launch_bounds__(128) num4d_prepass_kernel(IntegrateArgs a) {
   const int i = (int)(row - M.row_off);
   const int N_L = a.N_L;
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  Layout L = make_layout(N_L, a.N_P, a.N_E);
   double *coef;
   GeoSmem g = carve(smem, N_L, 0, &coef, 0, 0, nullptr, 32, a.N_R);
   __shared__ int s_J, s_any, s_top, s_jalt;
@@ -549,7 +605,6 @@ __global__ void __launch_bounds__(128) num4d_prepass_kernel(IntegrateArgs a) {
     return;
   }
   stage_deflection(c, g, &s_jalt);
-  (void)L;
   const double mu_max = a.atmos.mu[a.atmos.nmu - 1], mu_top3 = a.atmos.mu[a.atmos.nmu - 3];
   for (int I = 0; I < c.IO; I++) {
     for (int k = threadIdx.x; k < leaf_lim; k += blockDim.x)
@@ -595,33 +650,8 @@ __global__ void num4d_scan_kernel(IntegrateArgs a) {
 // ---------------------------------------------------------------------------
 constexpr int kWrapLimit = 1024;  // 2 pi shifts of a cell phase (a few suffice)
 
-// FP64 phase of cell j at signal phase ph, wrapped into the knot range
-// (:575-586).  Returns the interval, found by walking forward from `hint`
-// (the previous cell's interval) or by bisection, or -1 when the phase does
-// not land in the knot range.
-struct CellPhaseD {
-  const double *knot;
-  int N_L;
-  double x_lo, x_hi, ph;
-  const double *cphi;
-  __device__ __forceinline__ int operator()(int j, int hint, double &t) const {
-    double x = ph + cphi[j];
-    if (x > x_hi) {
-      for (int w = 0; x > x_hi && w < kWrapLimit; w++) x = x - kTwoPi;
-    } else if (x < x_lo) {
-      for (int w = 0; x < x_lo && w < kWrapLimit; w++) x = x + kTwoPi;
-    }
-    if (!(x >= x_lo && x <= x_hi)) return -1;
-    int iv = hint;
-    if (iv < 0 || knot[iv] > x) iv = locate(knot, N_L, x);
-    else
-      while (iv < N_L - 2 && knot[iv + 1] <= x) iv++;
-    t = x - knot[iv];
-    return iv;
-  }
-};
-
-// the same with phases as unevaluated float pairs (hi + lo) and error-free
+// the phase of cell j at a signal phase, wrapped into the knot range
+// (:575-586), with phases as unevaluated float pairs (hi + lo) and error-free
 // sums, so the offset t keeps ~1e-14 rad absolute accuracy instead of one
 // FP32 ulp of the phase (~5e-7 rad)
 struct CellPhaseF {
@@ -630,7 +660,8 @@ struct CellPhaseF {
   float x_lo, x_hi, ph, ph_lo, tp, tp_lo;
   const float *cphi, *cphi_lo;  // cached pairs, or null
   const double *cphi_d;
-  __device__ __forceinline__ int operator()(int j, int hint, float &t) const {
+  // interval and offset th + tl of cell j's phase
+  __device__ __forceinline__ int offset(int j, int hint, float &th, float &tl) const {
     float cp, cp_lo;
     if (cphi) {
       cp = cphi[j];
@@ -661,21 +692,36 @@ struct CellPhaseF {
     if (iv < 0 || knot[iv] > x) iv = locate(knot, N_L, x);
     else
       while (iv < N_L - 2 && knot[iv + 1] <= x) iv++;
-    float th, e3;
+    float e3;
     two_sum(x, -knot[iv], th, e3);
-    t = th + (e3 + lo - knot_lo[iv]);
+    tl = e3 + lo - knot_lo[iv];
+    return iv;
+  }
+  __device__ __forceinline__ int operator()(int j, int hint, float &t) const {
+    float th, tl;
+    const int iv = offset(j, hint, th, tl);
+    t = th + tl;
+    return iv;
+  }
+  __device__ __forceinline__ int operator()(int j, int hint, DF &t) const {
+    float th, tl;
+    const int iv = offset(j, hint, th, tl);
+    t = fast_two_sum(th, tl);
     return iv;
   }
 };
 
-struct AreaD {
-  const double *A;
-  __device__ __forceinline__ double operator()(int j) const { return A[j]; }
-};
 struct AreaF {
   const float *Af;  // cached, or null
   const double *A;
   __device__ __forceinline__ float operator()(int j) const { return Af ? Af[j] : (float)A[j]; }
+};
+struct AreaDF {
+  const float *Ah, *Al;  // cached pairs, or null
+  const double *A;
+  __device__ __forceinline__ DF operator()(int j) const {
+    return Ah ? DF{Ah[j], Al[j]} : df_split(A[j]);
+  }
 };
 
 // the reference adds an interpolant value when it is > 0 (:593-594).  FP64:
@@ -709,6 +755,32 @@ __device__ __forceinline__ bool cell_phase_sums(const CP &cp, const AR &area, in
         const PieceT<WT> q = co4[(pb + e) * N_L + iv];
         const WT sv = q.y + t * (q.k1 + t * (q.k2 + t * q.k3));
         if (positive(sv)) acc[e] += A * sv;
+      }
+    }
+  }
+  return true;
+}
+
+// the FP64 path's form of cell_phase_sums, in double-float arithmetic on
+// scaled pieces (the sign test is on the high part: h + l has the sign of h)
+template <typename CP, typename AR>
+__device__ __forceinline__ bool cell_phase_sums_df(const CP &cp, const AR &area, int S1,
+                                                   const int32_t *rad, const PieceDF *pc, int N_L,
+                                                   int pb, int ne, DF (&acc)[kEPT]) {
+  int hint = -1;
+  for (int j = 0; j < S1; j++) {
+    if (rad[j] != 1) continue;
+    DF t;
+    const int iv = cp(j, hint, t);
+    if (iv < 0) return false;
+    hint = iv;
+    const DF A = area(j);
+#pragma unroll
+    for (int e = 0; e < kEPT; e++) {
+      if (pb + e < ne) {
+        const PieceDF q = pc[(pb + e) * N_L + iv];
+        const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
+        if (sv.h > 0.0f) acc[e] = df_fma(A, sv, acc[e]);
       }
     }
   }
@@ -842,7 +914,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
       p3 = pow(10.0, 3.0 * vT);
       __syncthreads();
     }
-    const float kT_f = (float)((kKB / kKeV) * pow(10.0, c.vec0));
+    const double kT = (kKB / kKeV) * pow(10.0, c.vec0);
+    const float kT_f = (float)kT;
+    const double lg_Eeff = num4d ? log10(E_eff) : 0.0;
     const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
     const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
     const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
@@ -863,30 +937,36 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         return;
       }
       if (invis) break;
-      if (kMixed) {
-        for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
-          const float hi = (float)g.phase[t];
-          as.fphase[t] = hi;
-          as.fphase_lo[t] = (float)(g.phase[t] - (double)hi);
+      // phase knots, cell azimuths and areas as float pairs for the cell x
+      // phase sums (both forms)
+      for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+        const float hi = (float)g.phase[t];
+        as.fphase[t] = hi;
+        as.fphase_lo[t] = (float)(g.phase[t] - (double)hi);
+      }
+      if (M.S1 <= kMaxCellsF) {
+        for (int t = threadIdx.x; t < M.S1; t += blockDim.x) {
+          const float hi = (float)cellPhi[t];
+          as.fcphi[t] = hi;
+          as.fcphi_lo[t] = (float)(cellPhi[t] - (double)hi);
+          const float ah = (float)cellA[t];
+          as.fcarea[t] = ah;
+          as.fcarea_lo[t] = (float)(cellA[t] - (double)ah);
         }
-        if (M.S1 <= kMaxCellsF) {
-          for (int t = threadIdx.x; t < M.S1; t += blockDim.x) {
-            const float hi = (float)cellPhi[t];
-            as.fcphi[t] = hi;
-            as.fcphi_lo[t] = (float)(cellPhi[t] - (double)hi);
-            as.fcarea[t] = (float)cellA[t];
-          }
-        }
-        for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
-          const int sidx = g.src[t];
-          if (sidx >= 0) {
+      }
+      for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+        const int sidx = g.src[t];
+        if (sidx >= 0) {
+          if (kMixed) {
             as.finvZ[sidx] = (float)(1.0 / g.Z[sidx]);
             as.fabb[sidx] = (float)g.ABB[sidx];
             as.fgeom[sidx] = (float)g.GEOM[sidx];
+          } else if (num4d) {
+            g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
           }
         }
-        __syncthreads();
       }
+      __syncthreads();
       if (threadIdx.x == 0 && a.flop_counter) {
         int Cr = 0;
         for (int j = 0; j < M.S1; j++) Cr += (rad[j] == 1);
@@ -896,6 +976,10 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
 
       for (int e0 = 0; e0 < N_E; e0 += EC) {
         const int ne = min(EC, N_E - e0);
+        if (!kMixed && num4d) {
+          for (int t = threadIdx.x; t < ne; t += blockDim.x) g.lgE[t] = log10(a.energies[e0 + t]);
+          __syncthreads();
+        }
         // specific intensities of every profile column (:445-478)
         for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
           const int pl = t / N_L, col = t - pl * N_L;
@@ -914,72 +998,120 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                 I_E = eval_bb_f(Ep, kT_f);
               y = (WT)((float)norm * I_E * as.fgeom[s]);
             } else {
-              const double Ep = a.energies[p] / g.Z[s];
               double I_E;
               if (num4d)
-                I_E = eval_num4d_slab(a.atmos, as, slab, Ep, g.ABB[s], p == 0 && g.clamp0[s],
-                                      E_eff, p3);
+                I_E = eval_num4d_slab(a.atmos, as, slab, g.lgE[pl] - g.lzs[s], g.ABB[s],
+                                      p == 0 && g.clamp0[s], p3);
               else
-                I_E = eval_bb(Ep, c.vec0);
+                I_E = eval_bb(a.energies[p] / g.Z[s], kT);
               y = (WT)((I_E * norm - 0.0) * g.GEOM[s]);
             }
           }
           co4[pl * N_L + col].y = y;
         }
         __syncthreads();
-        // Akima-periodic piece coefficients (:566-569)
-        for (int t = threadIdx.x; t < ne * (N_L - 1); t += blockDim.x) {
-          const int pl = t / (N_L - 1), iv = t - pl * (N_L - 1);
-          const PieceT<WT> *yr = co4 + pl * N_L;
-          WT mch[5];
-#pragma unroll
-          for (int d = 0; d < 5; d++) {
-            int q = periodic_chord(iv - 2 + d, N_L);
-            // knot spacings from the FP64 knots: adjacent knots closer than
-            // an FP32 ulp stay distinct
-            mch[d] = (yr[q + 1].y - yr[q].y) / (WT)(g.phase[q + 1] - g.phase[q]);
+        // Akima-periodic piece coefficients (:566-569): a thread builds kStrip
+        // consecutive pieces of one energy row from a sliding window of the
+        // five chords each piece needs, so each chord is divided out once
+        // per strip instead of five times
+        {
+          const int n_iv = N_L - 1, strips = (n_iv + kStrip - 1) / kStrip;
+          for (int t = threadIdx.x; t < ne * strips; t += blockDim.x) {
+            const int pl = t / strips, i0 = (t - pl * strips) * kStrip;
+            const int i1 = min(i0 + kStrip, n_iv);
+            PieceT<WT> *yr = co4 + pl * N_L;
+            auto chord = [&](int j) -> WT {
+              const int q = periodic_chord(j, N_L);
+              // knot spacings from the FP64 knots: adjacent knots closer
+              // than an FP32 ulp stay distinct
+              return (yr[q + 1].y - yr[q].y) / (WT)(g.phase[q + 1] - g.phase[q]);
+            };
+            WT m0 = chord(i0 - 2), m1 = chord(i0 - 1), m2 = chord(i0), m3 = chord(i0 + 1),
+               m4 = chord(i0 + 2);
+            for (int iv = i0; iv < i1; iv++) {
+              if (iv > i0) {
+                m0 = m1; m1 = m2; m2 = m3; m3 = m4;
+                m4 = chord(iv + 2);
+              }
+              WT k1, k2, k3;
+              const WT h = (WT)(g.phase[iv + 1] - g.phase[iv]);
+              akima_piece(m0, m1, m2, m3, m4, h, k1, k2, k3);
+              PieceT<WT> *o = yr + iv;
+              o->k1 = k1;
+              o->k2 = k2;
+              o->k3 = k3;
+            }
           }
-          WT k1, k2, k3;
-          const WT h = (WT)(g.phase[iv + 1] - g.phase[iv]);
-          akima_piece(mch[0], mch[1], mch[2], mch[3], mch[4], h, k1, k2, k3);
-          PieceT<WT> *o = co4 + pl * N_L + iv;
-          o->k1 = k1;
-          o->k2 = k2;
-          o->k3 = k3;
         }
         __syncthreads();
+        if (!kMixed) {
+          // scale each energy row by a power of two (exact) so that its
+          // largest profile value lies in [0.5, 1): double-float pieces then
+          // keep the row's full relative precision whatever its magnitude
+          const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+          for (int pl = warp; pl < ne; pl += kThreads / 32) {
+            double mx = 0.0;
+            for (int col = lane; col < N_L; col += 32) mx = fmax(mx, fabs((double)co4[pl * N_L + col].y));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            int ex = 0;
+            if (mx > 0.0 && mx <= 1.7976931348623157e308) frexp(mx, &ex);
+            if (lane == 0) g.sc_exp[pl] = ex;
+          }
+          __syncthreads();
+          for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+            const int pl = t / N_L;
+            const double sc = ldexp(1.0, -g.sc_exp[pl]);
+            const PieceT<WT> q = co4[t];
+            PieceDF r;
+            r.y = df_split((double)q.y * sc);
+            r.k1 = df_split((double)q.k1 * sc);
+            r.k2 = df_split((double)q.k2 * sc);
+            r.k3 = df_split((double)q.k3 * sc);
+            reinterpret_cast<PieceDF *>(co4)[t] = r;
+          }
+          __syncthreads();
+        }
         // cell x phase accumulation (:571-598)
         for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
           const int k = task % N_P, grp = task / N_P;
           const int pb = grp * kEPT;
           if (pb >= ne) continue;
-          WT acc[kEPT];
-#pragma unroll
-          for (int e = 0; e < kEPT; e++) acc[e] = WT(0);
-          bool ok;
+          const double phd = a.phases[k];
+          const float ph = (float)phd;
+          const float tp = (float)kTwoPi;
+          const bool cached = M.S1 <= kMaxCellsF;
+          const CellPhaseF cp{as.fphase, as.fphase_lo, N_L, as.fphase[0], as.fphase[N_L - 1], ph,
+                              (float)(phd - (double)ph), tp, (float)(kTwoPi - (double)tp),
+                              cached ? as.fcphi : nullptr, cached ? as.fcphi_lo : nullptr,
+                              cellPhi};
           if constexpr (kMixed) {
-            const double phd = a.phases[k];
-            const float ph = (float)phd;
-            const float tp = (float)kTwoPi;
-            const bool cached = M.S1 <= kMaxCellsF;
-            CellPhaseF cp{as.fphase, as.fphase_lo, N_L, as.fphase[0], as.fphase[N_L - 1], ph,
-                          (float)(phd - (double)ph), tp, (float)(kTwoPi - (double)tp),
-                          cached ? as.fcphi : nullptr, cached ? as.fcphi_lo : nullptr, cellPhi};
-            AreaF ar{cached ? as.fcarea : nullptr, cellA};
-            ok = cell_phase_sums<WT>(cp, ar, M.S1, rad, co4, N_L, pb, ne, acc);
-          } else {
-            CellPhaseD cp{g.phase, N_L, g.phase[0], g.phase[N_L - 1], a.phases[k], cellPhi};
-            AreaD ar{cellA};
-            ok = cell_phase_sums<WT>(cp, ar, M.S1, rad, co4, N_L, pb, ne, acc);
-          }
-          const int bad = !ok;
-          if (bad) {
-            atomicExch(&a.member_status[m], (int)kPulseFail);
-            continue;
-          }
+            WT acc[kEPT];
 #pragma unroll
-          for (int e = 0; e < kEPT; e++)
-            if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += (double)acc[e];
+            for (int e = 0; e < kEPT; e++) acc[e] = WT(0);
+            const AreaF ar{cached ? as.fcarea : nullptr, cellA};
+            if (!cell_phase_sums<WT>(cp, ar, M.S1, rad, co4, N_L, pb, ne, acc)) {
+              atomicExch(&a.member_status[m], (int)kPulseFail);
+              continue;
+            }
+#pragma unroll
+            for (int e = 0; e < kEPT; e++)
+              if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += (double)acc[e];
+          } else {
+            DF acc[kEPT];
+#pragma unroll
+            for (int e = 0; e < kEPT; e++) acc[e] = DF{0.0f, 0.0f};
+            const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
+            if (!cell_phase_sums_df(cp, ar, M.S1, rad, reinterpret_cast<const PieceDF *>(co4), N_L,
+                                    pb, ne, acc)) {
+              atomicExch(&a.member_status[m], (int)kPulseFail);
+              continue;
+            }
+#pragma unroll
+            for (int e = 0; e < kEPT; e++)
+              if (pb + e < ne)
+                part[(size_t)(e0 + pb + e) * N_P + k] += ldexp(df_value(acc[e]), g.sc_exp[pb + e]);
+          }
         }
         __syncthreads();
       }
@@ -1021,8 +1153,7 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   }
   bool any_num4d = a.atmos.I != nullptr;
   if (any_num4d) {
-    size_t pre_smem = (size_t)5 * a.N_L * sizeof(double) + (size_t)4 * a.N_L * sizeof(int) +
-                      8 * sizeof(int) + 16 + (size_t)a.N_R * sizeof(double);
+    const size_t pre_smem = geometry_bytes(a.N_L, a.N_R);
     static bool pre_attr = false;
     if (!pre_attr) {
       cudaFuncSetAttribute(num4d_prepass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
