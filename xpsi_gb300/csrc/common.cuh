@@ -147,6 +147,97 @@ __device__ __forceinline__ int periodic_chord(int j, int n) {
   return j;
 }
 
+
+// ---------------------------------------------------------------------
+// Double-float numbers: an unevaluated sum h + l of two floats, about 48
+// significant bits (~4e-15 relative per operation).  On this GPU an FP32
+// instruction issues at 64x the FP64 rate, and a double-float operation is
+// 7-30 FP32 instructions, so FP64-path work whose values stay inside the
+// float exponent range runs in this form at FP64-class accuracy for a
+// fraction of the FP64 pipe's time.  Methods: Knuth's two-sum, Dekker's
+// fast two-sum and product (the product error taken with an FMA), one
+// correction step of long division for the quotient and of Newton's method
+// for the square root.  The _rn intrinsics keep the compiler from
+// contracting or reassociating the error-free transformations.
+// ---------------------------------------------------------------------
+struct DF {
+  float h, l;
+};
+
+// Knuth: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// Dekker: s + e == a + b when |a| >= |b|
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_split(double v) {
+  const float h = (float)v;
+  return DF{h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double df_value(DF a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return fast_two_sum(s, e);
+}
+__device__ __forceinline__ DF df_sub(DF a, DF b) { return df_add(a, df_neg(b)); }
+// a * b (the a.l * b.l term, ~2^-48 relative, is dropped)
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+// a * b + c
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  float s, f;
+  two_sum(p, c.h, s, f);
+  f = __fadd_rn(f, __fadd_rn(e, c.l));
+  return fast_two_sum(s, f);
+}
+// a / b: float quotient of the high parts, corrected by the remainder
+// a - q b (formed exactly through the FMA product error).  The quotients
+// may be the fast approximate ones (2 ulp): the correction absorbs the first
+// one's error and the second's is ~2^-23 of a ~2^-23 term.
+__device__ __forceinline__ DF df_div(DF a, DF b) {
+  const float q1 = __fdividef(a.h, b.h);
+  const float p = __fmul_rn(q1, b.h);
+  const float pe = __fmaf_rn(q1, b.h, -p);
+  float r = __fsub_rn(a.h, p);
+  r = __fsub_rn(r, pe);
+  r = __fadd_rn(r, a.l);
+  r = __fmaf_rn(-q1, b.l, r);
+  const float q2 = __fdividef(r, b.h);
+  return fast_two_sum(q1, q2);
+}
+// sqrt(a): an approximate float root s = a rsqrt(a) plus one Newton
+// correction (a - s^2) / (2 s) with the residual formed exactly; 0 for
+// a == 0, NaN for a < 0 (as sqrt)
+__device__ __forceinline__ DF df_sqrt(DF a) {
+  if (!(a.h > 0.0f)) return DF{__fsqrt_rn(a.h), 0.0f};
+  const float rs = rsqrtf(a.h);
+  const float s = __fmul_rn(a.h, rs);
+  const float p = __fmul_rn(s, s);
+  const float pe = __fmaf_rn(s, s, -p);
+  float r = __fsub_rn(a.h, p);
+  r = __fsub_rn(r, pe);
+  r = __fadd_rn(r, a.l);
+  const float c = __fmul_rn(r, __fmul_rn(0.5f, rs));
+  return fast_two_sum(s, c);
+}
+
 // ---------------------------------------------------------------------
 // QUADPACK QAG with a Gauss-Kronrod rule, one thread per integral.  The
 // interval list lives in the caller-provided arrays (local memory).
@@ -154,61 +245,15 @@ __device__ __forceinline__ int periodic_chord(int j, int n) {
 // 18 round-off, 21 singularity.  Result semantics match the reference's
 // GSL call (best estimate returned on every status).
 // ---------------------------------------------------------------------
-template <int HALF>
-struct GKRule {
-  const double *x, *wk, *wg;
-};
-
-template <int HALF, typename F>
-__device__ __forceinline__ void gk_panel(const F &f, const double *X, const double *WK,
-                                         const double *WG, double a, double b, double &res,
-                                         double &err, double &rabs, double &rasc) {
-  constexpr int NH = HALF - 1;
-  double c = 0.5 * (a + b), h = 0.5 * (b - a), ah = fabs(h);
-  double fv1[NH], fv2[NH];
-  double fc = f(c);
-  double rk = WK[NH] * fc;
-  double rg = WG[NH] * fc;
-  double ra = fabs(rk);
-#pragma unroll
-  for (int j = 0; j < NH; j++) {
-    double dx = h * X[j];
-    double f1 = f(c - dx), f2 = f(c + dx);
-    fv1[j] = f1;
-    fv2[j] = f2;
-    rk += WK[j] * (f1 + f2);
-    rg += WG[j] * (f1 + f2);
-    ra += WK[j] * (fabs(f1) + fabs(f2));
-  }
-  double mean = 0.5 * rk;
-  double rc = WK[NH] * fabs(fc - mean);
-#pragma unroll
-  for (int j = 0; j < NH; j++) rc += WK[j] * (fabs(fv1[j] - mean) + fabs(fv2[j] - mean));
-  res = rk * h;
-  ra *= ah;
-  rc *= ah;
-  double e = fabs((rk - rg) * h);
-  if (rc != 0.0 && e != 0.0) {
-    double sc = pow(200.0 * e / rc, 1.5);
-    e = sc < 1.0 ? rc * sc : rc;
-  }
-  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
-  if (ra > dmin / (50.0 * eps)) {
-    double fl = 50.0 * eps * ra;
-    if (fl > e) e = fl;
-  }
-  err = e;
-  rabs = ra;
-  rasc = rc;
-}
-
-template <int HALF, int LIMIT, typename F>
-__device__ int qag(const F &f, const double *X, const double *WK, const double *WG, double a,
-                   double b, double epsabs, double epsrel, double &result, double &abserr) {
+// the adaptive bisection, with panel(lo, hi, result, error, |f| integral,
+// |f - mean| integral) evaluating one Gauss-Kronrod panel
+template <int LIMIT, typename Panel>
+__device__ int qag_panels(const Panel &panel, double a, double b, double epsabs, double epsrel,
+                          double &result, double &abserr) {
   const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
   double al[LIMIT], bl[LIMIT], rl[LIMIT], el[LIMIT];
   double r0, e0, ra0, rc0;
-  gk_panel<HALF>(f, X, WK, WG, a, b, r0, e0, ra0, rc0);
+  panel(a, b, r0, e0, ra0, rc0);
   int size = 1;
   al[0] = a; bl[0] = b; rl[0] = r0; el[0] = e0;
   double tol = fmax(epsabs, epsrel * fabs(r0));
@@ -222,8 +267,8 @@ __device__ int qag(const F &f, const double *X, const double *WK, const double *
     double ai = al[k], bi = bl[k], ri = rl[k], ei = el[k];
     double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
     double r1, e1, ra1, rc1, r2, e2, ra2, rc2;
-    gk_panel<HALF>(f, X, WK, WG, a1, b1, r1, e1, ra1, rc1);
-    gk_panel<HALF>(f, X, WK, WG, a2, b2, r2, e2, ra2, rc2);
+    panel(a1, b1, r1, e1, ra1, rc1);
+    panel(a2, b2, r2, e2, ra2, rc2);
     double r12 = r1 + r2, e12 = e1 + e2;
     errsum += e12 - ei;
     area += r12 - ri;
@@ -260,6 +305,59 @@ __device__ int qag(const F &f, const double *X, const double *WK, const double *
   if (fail == 3) return 21;
   if (iter == LIMIT) return 11;
   return 5;
+}
+
+
+// One Gauss-Kronrod panel with the integrand evaluated and the Kronrod and
+// Gauss sums accumulated in double-float arithmetic (X2, WK2, WG2: the
+// rule's nodes and weights as float pairs); the |f| and |f - mean| sums,
+// which only scale the error estimate, in FP32; the panel's result and
+// error estimate in FP64 with QUADPACK's formulas (the (200 e / rc)^1.5
+// scaling and the 50 eps round-off floor).
+template <int HALF, typename F>
+__device__ __forceinline__ void gk_panel_df(const F &f, const float *X2, const float *WK2,
+                                            const float *WG2, double a, double b, double &res,
+                                            double &err, double &rabs, double &rasc) {
+  constexpr int NH = HALF - 1;
+  const double cd = 0.5 * (a + b), hd = 0.5 * (b - a);
+  const DF c = df_split(cd), h = df_split(hd);
+  float fv1[NH], fv2[NH];
+  const DF fc = f(c);
+  DF rk = df_mul(DF{WK2[2 * NH], WK2[2 * NH + 1]}, fc);
+  DF rg = df_mul(DF{WG2[2 * NH], WG2[2 * NH + 1]}, fc);
+  float ra = fabsf(rk.h);
+  // not unrolled: one inlined copy of the integrand, fv in local memory
+#pragma unroll 1
+  for (int j = 0; j < NH; j++) {
+    const DF dx = df_mul(h, DF{X2[2 * j], X2[2 * j + 1]});
+    const DF f1 = f(df_sub(c, dx)), f2 = f(df_add(c, dx));
+    fv1[j] = f1.h;
+    fv2[j] = f2.h;
+    const DF s2 = df_add(f1, f2);
+    rk = df_fma(DF{WK2[2 * j], WK2[2 * j + 1]}, s2, rk);
+    if (WG2[2 * j] != 0.0f) rg = df_fma(DF{WG2[2 * j], WG2[2 * j + 1]}, s2, rg);
+    ra += WK2[2 * j] * (fabsf(f1.h) + fabsf(f2.h));
+  }
+  const float mean = 0.5f * rk.h;
+  float rc = WK2[2 * NH] * fabsf(fc.h - mean);
+#pragma unroll 1
+  for (int j = 0; j < NH; j++) rc += WK2[2 * j] * (fabsf(fv1[j] - mean) + fabsf(fv2[j] - mean));
+  res = df_value(rk) * hd;
+  const double ah = fabs(hd);
+  const double rad = (double)ra * ah, rcd = (double)rc * ah;
+  double e = fabs(df_value(df_sub(rk, rg)) * hd);
+  if (rcd != 0.0 && e != 0.0) {
+    const double x = 200.0 * e / rcd, sc = x * sqrt(x);  // x^1.5
+    e = sc < 1.0 ? rcd * sc : rcd;
+  }
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  if (rad > dmin / (50.0 * eps)) {
+    const double fl = 50.0 * eps * rad;
+    if (fl > e) e = fl;
+  }
+  err = e;
+  rabs = rad;
+  rasc = rcd;
 }
 
 }  // namespace xg

@@ -15,6 +15,7 @@ Usage:  python gen_gk_nodes.py OUT.h PREFIX
 """
 import sys
 import mpmath as mp
+import numpy as np
 
 mp.mp.dps = 60
 
@@ -89,8 +90,10 @@ def main():
              "#pragma once",
              "#ifdef __CUDACC__",
              "#define GK_TABLE static __constant__ const double",
+             "#define GK_TABLE_F static __constant__ const float",
              "#else",
              "#define GK_TABLE static const double",
+             "#define GK_TABLE_F static const float",
              "#endif", ""]
     for n in (10, 30):
         nodes, kw, gx, gw = kronrod(n)
@@ -119,6 +122,17 @@ def main():
         lines.append(f"/* Gauss weight of the node, 0 where the node is Kronrod-only */")
         lines.append(f"GK_TABLE {tag}_WG[{half}] = {{")
         lines += [f"    {fmt(v)}," for v in wg] + ["};"]
+        # the same values as float pairs hi + lo (hi the nearest float, lo the
+        # nearest float to the remainder) for double-float arithmetic
+        lines.append(f"/* float pairs (hi, lo) of _X, _WK, _WG */")
+        for nm, vals in (("X", xk), ("WK", wk), ("WG", wg)):
+            lines.append(f"GK_TABLE_F {tag}_{nm}2[{2 * half}] = {{")
+            for v in vals:
+                v = v if abs(v) > mp.mpf(10) ** -30 else mp.mpf(0)
+                hi = float(np.float32(float(v)))
+                lo = float(np.float32(float(v - mp.mpf(hi))))
+                lines.append(f"    {hi!r}f, {lo!r}f,")
+            lines.append("};")
         lines.append("")
         # self-check: exactness of the Kronrod rule to degree 3n+1, Gauss to 2n-1
         for deg in range(0, 3 * n + 2):

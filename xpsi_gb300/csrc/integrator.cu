@@ -406,46 +406,6 @@ __device__ __forceinline__ double eval_num4d_slab(const Atmos4D &A, const AtmSme
 
 // FP32 forms for the mixed-precision integrator
 
-// Knuth's error-free sum: s + e == a + b exactly
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// Double-float numbers: an unevaluated sum h + l of two floats, about 48
-// significant bits.  The FP64 path evaluates its cell x phase sums in this
-// form: an FP32 instruction issues at 64x the FP64 rate on this GPU and a
-// double-float multiply-add is ~15 FP32 instructions (Dekker's product
-// error through the FMA, Knuth's two-sum, a fast two-sum renormalisation), so
-// the sums keep FP64-class accuracy (~1e-14 relative) at a fraction of the
-// FP64 pipe's time.  The _rn intrinsics keep the compiler from contracting
-// or reassociating the error-free transformations.
-struct DF {
-  float h, l;
-};
-__device__ __forceinline__ DF df_split(double v) {
-  const float h = (float)v;
-  return DF{h, (float)(v - (double)h)};
-}
-__device__ __forceinline__ double df_value(DF a) { return (double)a.h + (double)a.l; }
-// Dekker: s + e == a + b when |a| >= |b|
-__device__ __forceinline__ DF fast_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-// a * b + c (the a.l * b.l term, ~2^-48 relative, is dropped)
-__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  float s, f;
-  two_sum(p, c.h, s, f);
-  f = __fadd_rn(f, __fadd_rn(e, c.l));
-  return fast_two_sum(s, f);
-}
-
 // an Akima piece in double-float form, scaled by a power of two per energy
 // row (same 32 bytes as the FP64 piece it replaces in shared memory)
 struct __align__(16) PieceDF {

@@ -4,7 +4,9 @@
 //
 // Work decomposition: one CTA per mesh row ("parallel"), one thread per ray;
 // each thread runs its 2 or 4 QUADPACK-QAG / Gauss-Kronrod-61 integrals to
-// epsrel 1e-12 in FP64, exactly the reference's quadrature problem.  The
+// epsrel 1e-12, the reference's quadrature problem: interval bookkeeping and
+// error control in FP64, every panel's integrand evaluations and weighted
+// sums in double-float arithmetic (FP32 pipes, ~1e-14 relative).  The
 // row's NaN repair (:333-369) is a short sequential walk done by one thread
 // after the CTA barrier.  Optionally the lag is calibrated in the same pass
 // (HotRegion.py:880-901: lag -= C(r), lag *= 2 pi f_mode).
@@ -13,37 +15,53 @@
 
 namespace xg {
 
+// The integrands of rays.pyx:60-88 in double-float arithmetic (values of
+// order one on [0, 1], inside the float exponent range).  q is the
+// reciprocal of (Rr - 1) or (rc - 1), formed once per ray in FP64.
 struct OutDef {
-  double sas, Rr;
-  __device__ double operator()(double x) const {
-    return x / sqrt(1.0 - sas + x * x * sas * (2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (Rr - 1.0)));
+  DF oms, sas, q;  // 1 - sin^2 alpha, sin^2 alpha, 1 / (1/u - 1)
+  __device__ __forceinline__ DF root(DF x) const {
+    const DF x2 = df_mul(x, x);
+    const DF u = df_sub(DF{1.0f, 0.0f}, x2);
+    const DF w = df_sub(df_sub(DF{2.0f, 0.0f}, x2), df_mul(df_mul(u, u), q));
+    return df_sqrt(df_add(oms, df_mul(df_mul(x2, sas), w)));
   }
+  __device__ DF operator()(DF x) const { return df_div(x, root(x)); }
 };
 struct OutLag {
-  double sas, Rr;
-  __device__ double operator()(double x) const {
-    double f = sqrt(1.0 - sas + x * x * sas * (2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (Rr - 1.0)));
-    return x / (f + f * f);
+  OutDef d;
+  __device__ DF operator()(DF x) const {
+    const DF f = d.root(x);
+    return df_div(x, df_fma(f, f, f));
   }
 };
 struct InDef {
-  double rc;
-  __device__ double operator()(double x) const {
-    return 1.0 / sqrt(2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (rc - 1.0));
+  DF q;  // 1 / (rc - 1)
+  __device__ __forceinline__ DF value(DF x) const {
+    const DF x2 = df_mul(x, x);
+    const DF u = df_sub(DF{1.0f, 0.0f}, x2);
+    const DF w = df_sub(df_sub(DF{2.0f, 0.0f}, x2), df_mul(df_mul(u, u), q));
+    return df_div(DF{1.0f, 0.0f}, df_sqrt(w));
   }
+  __device__ DF operator()(DF x) const { return value(x); }
 };
 struct InLag {
-  double rc;
-  __device__ double operator()(double x) const {
-    double X = 1.0 / sqrt(2.0 - x * x - (1.0 - x * x) * (1.0 - x * x) / (rc - 1.0));
-    return X * X / (x + X);
+  InDef d;
+  __device__ DF operator()(DF x) const {
+    const DF X = d.value(x);
+    return df_div(df_mul(X, X), df_add(x, X));
   }
 };
 
+// QUADPACK QAG with the 61-point rule at relative 1e-12, limit 100
+// (rays.pyx:140-236), panels in double-float arithmetic
 template <typename F>
 __device__ __forceinline__ int q61(const F &f, double a, double b, double &r) {
   double e;
-  return qag<XG_K61_HALF, 100>(f, XG_K61_X, XG_K61_WK, XG_K61_WG, a, b, 0.0, 1.0e-12, r, e);
+  auto panel = [&](double lo, double hi, double &res, double &err, double &ra, double &rc) {
+    gk_panel_df<XG_K61_HALF>(f, XG_K61_X2, XG_K61_WK2, XG_K61_WG2, lo, hi, res, err, ra, rc);
+  };
+  return qag_panels<100>(panel, a, b, 0.0, 1.0e-12, r, e);
 }
 
 // rays.pyx:90-247; returns deflection in d, lag in seconds in l
@@ -57,8 +75,8 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
   d = 0.0;
   l = 0.0;
   if (b <= kBPhotonSphere) {
-    OutDef fd{sas, 1.0 / u};
-    OutLag fl{sas, 1.0 / u};
+    const OutDef fd{df_split(1.0 - sas), df_split(sas), df_split(1.0 / (1.0 / u - 1.0))};
+    const OutLag fl{fd};
     status = q61(fd, 0.0, 1.0, d);
     if (status == EFAILED) d = nan("");
     if (status != EFAILED) {
@@ -79,8 +97,8 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
       wR = sqrt(1.0 - rc * u);
     }
     if (isnan(wR)) wR = 0.0;
-    InDef fd{rc};
-    InLag fl{rc};
+    const InDef fd{df_split(1.0 / (rc - 1.0))};
+    const InLag fl{fd};
     status = q61(fd, wR, 1.0, d);
     if (status == EFAILED) d = nan("");
     if (status != EFAILED) {
@@ -95,8 +113,8 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
     double rc = 2.0 * b * cos((atan(sqrt(4.0 * b * b / 27.0 - 1.0)) - kPi) / 3.0) / sqrt(3.0);
     double wR = sqrt(1.0 - rc * u);
     if (isnan(wR)) wR = 0.0;
-    InDef fd{rc};
-    InLag fl{rc};
+    const InDef fd{df_split(1.0 / (rc - 1.0))};
+    const InLag fl{fd};
     double d1, d0, l1, l0;
     status = q61(fd, 0.0, 1.0, d1);
     if (status == EFAILED) d = nan("");
