@@ -68,6 +68,7 @@ struct GeoSmem {
   double *lgE;  // [EC] log10 of the chunk's energies (FP64 path, Num4D)
   double *lzs;  // [N_L] log10(Z) + log10(E_eff) per leaf (FP64 path, Num4D)
   int *sc_exp;  // [EC] binary exponent of the largest |profile value| per energy row
+  DF *ih, *ih2;  // [N_L] 1/h and 1/h^2 of the phase intervals (FP64 path)
 };
 
 
@@ -373,35 +374,93 @@ __device__ __forceinline__ void lagrange_w(const double *P, const double *S, int
   w[3] = d3 * S[4 * b + 3];
 }
 
+// stencil_base with the bisection run on the grid's FP32 copy (FP32 pipe)
+// and finished with FP64 comparisons.  Rounding to float is monotone, so the
+// float search never stops below the FP64 answer, and stepping down while
+// g[lo] > v lands on it exactly: the result equals stencil_base(g, n, v).
+__device__ __forceinline__ int stencil_base_guided(const double *g, const float *fg, int n,
+                                                   double v) {
+  const float vf = (float)v;
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (fg[mid] > vf) hi = mid; else lo = mid;
+  }
+  while (lo > 0 && g[lo] > v) lo--;
+  int b = lo - 1;
+  if (b < 0) b = 0;
+  if (b > n - 4) b = n - 4;
+  return b;
+}
+
 // Num4D intensity for a parallel whose (log T, log g) stencil has been
 // contracted into `slab` [nmu][nE]: the remaining 4 x 4 (mu, energy) stencil
 // (hot_Num4D.pyx:248-439; the stencil bases are those the reference's cached
-// walk lands on, see the file header for the mu > 1 case)
-// (the caller passes v3 = log10(E / E_eff) as log10 E - log10 Z - log10 E_eff
-// from per-energy and per-leaf logarithms: one subtraction per evaluation)
-__device__ __forceinline__ double eval_num4d_slab(const Atmos4D &A, const AtmSmem &as,
-                                                  const double *slab, double v3, double mu,
-                                                  bool clamp_mu, double p3) {
+// walk lands on, see the file header for the mu > 1 case).  It is split in
+// two: the mu stencil depends only on the profile column (its cos emission
+// angle), so a thread evaluating one column at several energies forms it
+// once.  The caller passes v3 = log10(E / E_eff) as log10 E - log10 Z -
+// log10 E_eff from per-energy and per-leaf logarithms.
+struct MuStencil {
+  int b2;
+  double w2[4];
+};
+__device__ __forceinline__ MuStencil mu_stencil(const Atmos4D &A, const AtmSmem &as, double mu,
+                                                bool clamp_mu) {
   double v2 = mu;
   const double mu_hi = as.gmu[A.nmu - 1];
   if (v2 > mu_hi && clamp_mu) v2 = mu_hi;
   if (v2 < as.gmu[0]) v2 = as.gmu[0];
+  MuStencil m;
+  m.b2 = stencil_base_guided(as.gmu, as.fgmu, A.nmu, v2);
+  lagrange_w(as.gmu, as.smu, m.b2, v2, m.w2);
+  return m;
+}
+__device__ __forceinline__ double eval_num4d_e(const Atmos4D &A, const AtmSmem &as,
+                                               const double *slab, const MuStencil &m,
+                                               double v3, double p3) {
   if (v3 < as.gE[0]) v3 = as.gE[0];
   if (v3 > as.gE[A.nE - 1]) v3 = as.gE[A.nE - 1];
-  const int b2 = stencil_base(as.gmu, A.nmu, v2);
-  const int b3 = stencil_base(as.gE, A.nE, v3);
-  double w2[4], w3[4];
-  lagrange_w(as.gmu, as.smu, b2, v2, w2);
+  const int b3 = stencil_base_guided(as.gE, as.fgE, A.nE, v3);
+  double w3[4];
   lagrange_w(as.gE, as.sE, b3, v3, w3);
   double I = 0.0;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const double *r = slab + (size_t)(b2 + k) * A.nE + b3;
-    double t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
-    I += w2[k] * t;
+    const double *r = slab + (size_t)(m.b2 + k) * A.nE + b3;
+    const double t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
+    I += m.w2[k] * t;
   }
   if (I < 0.0) return 0.0;
   return I * p3;
+}
+
+// Akima piece (common.cuh akima_piece) in double-float arithmetic, with the
+// divisions by h and h^2 taken as products with their reciprocals
+__device__ __forceinline__ DF df_abs(DF a) { return a.h < 0.0f ? df_neg(a) : a; }
+__device__ __forceinline__ void akima_piece_df(DF mm2, DF mm1, DF m0, DF mp1, DF mp2, DF ih,
+                                               DF ih2, DF &k1, DF &k2, DF &k3) {
+  const DF one{1.0f, 0.0f};
+  const DF wl = df_add(df_abs(df_sub(mp1, m0)), df_abs(df_sub(mm1, mm2)));
+  if (wl.h == 0.0f) {
+    k1 = m0;
+    k2 = k3 = DF{0.0f, 0.0f};
+    return;
+  }
+  const DF wr = df_add(df_abs(df_sub(mp2, mp1)), df_abs(df_sub(m0, mm1)));
+  const DF f = df_div(df_abs(df_sub(mm1, mm2)), wl);
+  const DF tl = df_fma(df_sub(one, f), mm1, df_mul(f, m0));
+  DF tr;
+  if (wr.h == 0.0f) {
+    tr = m0;
+  } else {
+    const DF gg = df_div(df_abs(df_sub(m0, mm1)), wr);
+    tr = df_fma(df_sub(one, gg), m0, df_mul(gg, mp1));
+  }
+  k1 = tl;
+  const DF m3 = df_add(df_add(m0, m0), m0);
+  k2 = df_mul(df_sub(df_sub(m3, df_add(tl, tl)), tr), ih);
+  k3 = df_mul(df_sub(df_add(tl, tr), df_add(m0, m0)), ih2);
 }
 
 // FP32 forms for the mixed-precision integrator
@@ -486,6 +545,7 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
             + (size_t)(5 * N_L + 4 * kMaxCellsF + kMaxEnergiesF) * sizeof(float)
             + (size_t)N_R * sizeof(double)  // staged deflection table
             + (size_t)(ec + N_L) * sizeof(double)  // lgE, lzs
+            + (size_t)2 * N_L * sizeof(DF)         // ih, ih2
             + (size_t)(4 * N_L + 8 + ec) * sizeof(int) + 64;
   return L;
 }
@@ -493,7 +553,7 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
 // bytes carve() takes with no coefficients and no atmosphere arrays (the
 // Num4D pre-pass)
 inline size_t geometry_bytes(int N_L, int N_R) {
-  return (size_t)N_R * sizeof(double) + (size_t)6 * N_L * sizeof(double) + 16 /* alignment */ +
+  return (size_t)N_R * sizeof(double) + (size_t)8 * N_L * sizeof(double) + 16 /* alignment */ +
          (size_t)(4 * N_L + 8) * sizeof(int) + 16;
 }
 
@@ -509,6 +569,8 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
   g.GEOM = d; d += N_L;
   g.lzs = d; d += N_L;
   g.lgE = d; d += EC;
+  g.ih = reinterpret_cast<DF *>(d); d += N_L;
+  g.ih2 = reinterpret_cast<DF *>(d); d += N_L;
   d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(d) + 15) & ~uintptr_t(15));
   *coef = d; d += (size_t)EC * N_L * piece_bytes / 8;
   if (atm) {
@@ -781,11 +843,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     for (int b = threadIdx.x; b <= nmu - 4; b += blockDim.x) lagrange_space(as.gmu, b, as.smu + 4 * b);
     for (int b = threadIdx.x; b <= nEt - 4; b += blockDim.x) lagrange_space(as.gE, b, as.sE + 4 * b);
     __syncthreads();
+    // FP32 grid copies: the guided stencil searches (both forms) and the
+    // mixed form's interpolation
+    for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
+    for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
     if (kMixed) {
-      for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
       for (int t = threadIdx.x; t < min(N_E, kMaxEnergiesF); t += blockDim.x)
         as.fE[t] = (float)a.energies[t];
-      for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
       for (int t = threadIdx.x; t < 4 * nmu; t += blockDim.x) as.fsmu[t] = (float)as.smu[t];
       for (int t = threadIdx.x; t < 4 * nEt; t += blockDim.x) as.fsE[t] = (float)as.sE[t];
     }
@@ -914,6 +978,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           as.fcarea_lo[t] = (float)(cellA[t] - (double)ah);
         }
       }
+      if (!kMixed) {
+        for (int t = threadIdx.x; t < N_L - 1; t += blockDim.x) {
+          const double h = g.phase[t + 1] - g.phase[t];
+          g.ih[t] = df_split(1.0 / h);
+          g.ih2[t] = df_split(1.0 / (h * h));
+        }
+      }
       for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
         const int sidx = g.src[t];
         if (sidx >= 0) {
@@ -940,42 +1011,58 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           for (int t = threadIdx.x; t < ne; t += blockDim.x) g.lgE[t] = log10(a.energies[e0 + t]);
           __syncthreads();
         }
-        // specific intensities of every profile column (:445-478)
-        for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
-          const int pl = t / N_L, col = t - pl * N_L;
-          const int p = e0 + pl;
-          const int s = g.src[col];
-          WT y = WT(0);
-          if (s >= 0) {
-            if (kMixed) {
-              const float Ef = p < kMaxEnergiesF ? as.fE[p] : (float)a.energies[p];
-              const float Ep = Ef * as.finvZ[s];
-              float I_E;
-              if (num4d)
-                I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, as.fabb[s],
-                                        p == 0 && g.clamp0[s], (float)E_eff, (float)p3);
-              else
-                I_E = eval_bb_f(Ep, kT_f);
-              y = (WT)((float)norm * I_E * as.fgeom[s]);
-            } else {
-              double I_E;
-              if (num4d)
-                I_E = eval_num4d_slab(a.atmos, as, slab, g.lgE[pl] - g.lzs[s], g.ABB[s],
-                                      p == 0 && g.clamp0[s], p3);
-              else
-                I_E = eval_bb(a.energies[p] / g.Z[s], kT);
-              y = (WT)((I_E * norm - 0.0) * g.GEOM[s]);
+        // specific intensities of every profile column (:445-478).  With
+        // N_L dividing the block size a thread keeps one column for all its
+        // energies, so its mu stencil (FP64 form) is formed once.
+        {
+          int mu_col = -1;
+          MuStencil ms{};
+          for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+            const int pl = t / N_L, col = t - pl * N_L;
+            const int p = e0 + pl;
+            const int s = g.src[col];
+            WT y = WT(0);
+            if (s >= 0) {
+              if constexpr (kMixed) {
+                const float Ef = p < kMaxEnergiesF ? as.fE[p] : (float)a.energies[p];
+                const float Ep = Ef * as.finvZ[s];
+                float I_E;
+                if (num4d)
+                  I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, as.fabb[s],
+                                          p == 0 && g.clamp0[s], (float)E_eff, (float)p3);
+                else
+                  I_E = eval_bb_f(Ep, kT_f);
+                y = (WT)((float)norm * I_E * as.fgeom[s]);
+              } else {
+                double I_E;
+                if (num4d) {
+                  const double v3 = g.lgE[pl] - g.lzs[s];
+                  if (p == 0 && g.clamp0[s]) {
+                    I_E = eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, g.ABB[s], true),
+                                       v3, p3);
+                  } else {
+                    if (s != mu_col) {
+                      ms = mu_stencil(a.atmos, as, g.ABB[s], false);
+                      mu_col = s;
+                    }
+                    I_E = eval_num4d_e(a.atmos, as, slab, ms, v3, p3);
+                  }
+                } else {
+                  I_E = eval_bb(a.energies[p] / g.Z[s], kT);
+                }
+                y = (WT)((I_E * norm - 0.0) * g.GEOM[s]);
+              }
             }
+            co4[pl * N_L + col].y = y;
           }
-          co4[pl * N_L + col].y = y;
         }
         __syncthreads();
         // Akima-periodic piece coefficients (:566-569): a thread builds kStrip
         // consecutive pieces of one energy row from a sliding window of the
-        // five chords each piece needs, so each chord is divided out once
-        // per strip instead of five times
-        {
-          const int n_iv = N_L - 1, strips = (n_iv + kStrip - 1) / kStrip;
+        // five chords each piece needs, so each chord is formed once per
+        // strip instead of five times
+        const int n_iv = N_L - 1, strips = (n_iv + kStrip - 1) / kStrip;
+        if constexpr (kMixed) {
           for (int t = threadIdx.x; t < ne * strips; t += blockDim.x) {
             const int pl = t / strips, i0 = (t - pl * strips) * kStrip;
             const int i1 = min(i0 + kStrip, n_iv);
@@ -1002,16 +1089,16 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               o->k3 = k3;
             }
           }
-        }
-        __syncthreads();
-        if (!kMixed) {
+          __syncthreads();
+        } else {
           // scale each energy row by a power of two (exact) so that its
-          // largest profile value lies in [0.5, 1): double-float pieces then
+          // largest profile value lies in [0.5, 1): double-float values then
           // keep the row's full relative precision whatever its magnitude
           const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
           for (int pl = warp; pl < ne; pl += kThreads / 32) {
             double mx = 0.0;
-            for (int col = lane; col < N_L; col += 32) mx = fmax(mx, fabs((double)co4[pl * N_L + col].y));
+            for (int col = lane; col < N_L; col += 32)
+              mx = fmax(mx, fabs((double)co4[pl * N_L + col].y));
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             int ex = 0;
@@ -1019,16 +1106,33 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             if (lane == 0) g.sc_exp[pl] = ex;
           }
           __syncthreads();
+          PieceDF *pc = reinterpret_cast<PieceDF *>(co4);
           for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
-            const int pl = t / N_L;
-            const double sc = ldexp(1.0, -g.sc_exp[pl]);
-            const PieceT<WT> q = co4[t];
-            PieceDF r;
-            r.y = df_split((double)q.y * sc);
-            r.k1 = df_split((double)q.k1 * sc);
-            r.k2 = df_split((double)q.k2 * sc);
-            r.k3 = df_split((double)q.k3 * sc);
-            reinterpret_cast<PieceDF *>(co4)[t] = r;
+            const double v = (double)co4[t].y;
+            pc[t].y = df_split(ldexp(v, -g.sc_exp[t / N_L]));
+          }
+          __syncthreads();
+          for (int t = threadIdx.x; t < ne * strips; t += blockDim.x) {
+            const int pl = t / strips, i0 = (t - pl * strips) * kStrip;
+            const int i1 = min(i0 + kStrip, n_iv);
+            PieceDF *yr = pc + pl * N_L;
+            auto chord = [&](int j) -> DF {
+              const int q = periodic_chord(j, N_L);
+              return df_mul(df_sub(yr[q + 1].y, yr[q].y), g.ih[q]);
+            };
+            DF m0 = chord(i0 - 2), m1 = chord(i0 - 1), m2 = chord(i0), m3 = chord(i0 + 1),
+               m4 = chord(i0 + 2);
+            for (int iv = i0; iv < i1; iv++) {
+              if (iv > i0) {
+                m0 = m1; m1 = m2; m2 = m3; m3 = m4;
+                m4 = chord(iv + 2);
+              }
+              DF k1, k2, k3;
+              akima_piece_df(m0, m1, m2, m3, m4, g.ih[iv], g.ih2[iv], k1, k2, k3);
+              yr[iv].k1 = k1;
+              yr[iv].k2 = k2;
+              yr[iv].k3 = k3;
+            }
           }
           __syncthreads();
         }
