@@ -238,6 +238,40 @@ __device__ __forceinline__ DF df_sqrt(DF a) {
   return fast_two_sum(s, c);
 }
 
+// Natural logarithm of a positive, normal double-float m.  With m = 2^e f,
+// f in [0.75, 1.5): log m = e ln 2 + 2 atanh(s), s = (f - 1) / (f + 1),
+// |s| <= 0.2, by the series atanh s = s (1 + s^2/3 + s^4/5 + ...) through
+// s^20/21 (truncation below 1e-17 relative).  The coefficients are 1/(2k+1)
+// and ln 2 as float pairs.
+__device__ __forceinline__ DF df_log(DF m) {
+  constexpr float kC[11][2] = {
+      {1.0f, 0.0f},
+      {0.3333333432674408f, -9.934107758624577e-09f},
+      {0.20000000298023224f, -2.9802322831784522e-09f},
+      {0.1428571492433548f, -6.38621200366174e-09f},
+      {0.1111111119389534f, -8.278422947149977e-10f},
+      {0.09090909361839294f, -2.709302115988521e-09f},
+      {0.07692307978868484f, -2.8656079731348427e-09f},
+      {0.06666667014360428f, -3.47693762670076e-09f},
+      {0.05882352963089943f, -2.1913472425527658e-10f},
+      {0.05263157933950424f, -3.9213582381236733e-10f},
+      {0.0476190485060215f, -8.869738832295582e-10f}};
+  const DF ln2{0.6931471824645996f, -1.9046542121259336e-09f};
+  // exponent e with m.h 2^-e in [0.75, 1.5), from the float's bits
+  const int bits = __float_as_int(m.h);
+  int e = ((bits >> 23) & 0xff) - 127;  // m.h = 1.x 2^e
+  if ((bits & 0x7fffff) >= 0x400000) e += 1;  // 1.x >= 1.5: use 0.75 2^(e+1)
+  const float sc = __int_as_float((127 - e) << 23);  // 2^-e, exact
+  const DF f{__fmul_rn(m.h, sc), __fmul_rn(m.l, sc)};
+  const DF one{1.0f, 0.0f};
+  const DF s = df_div(df_sub(f, one), df_add(f, one));
+  const DF s2 = df_mul(s, s);
+  DF p{kC[10][0], kC[10][1]};
+#pragma unroll
+  for (int k = 9; k >= 0; k--) p = df_fma(p, s2, DF{kC[k][0], kC[k][1]});
+  return df_fma(DF{(float)e, 0.0f}, ln2, df_mul(df_add(s, s), p));
+}
+
 // ---------------------------------------------------------------------
 // QUADPACK QAG with a Gauss-Kronrod rule, one thread per integral.  The
 // interval list lives in the caller-provided arrays (local memory).

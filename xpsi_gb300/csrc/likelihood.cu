@@ -28,6 +28,8 @@ constexpr int kQagLimit = 256; // interval list of the marginal quadrature
 struct WarpSmem {
   double star[kMaxB];
   double data[kMaxB];
+  DF q[kMaxB];        // SCALE / c_j(Bi): the relative form of the integrand
+  float dataf[kMaxB];  // counts (exact in float below 2^24)
   double fv[42];
   double al[kQagLimit], bl[kQagLimit], rl[kQagLimit], el[kQagLimit];
 };
@@ -58,10 +60,15 @@ struct Marg {
   int n;
   double SCALE, T, A;
   const double *data, *star;
+  // relative form (set when every c_j(Bi) > 0, so A = x(Bi))
+  int rel;
+  double Bi;
+  const DF *q;
+  const float *dataf;
 };
 
-// :84-138
-__device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
+// :84-138, as the reference writes it
+__device__ __forceinline__ double marginal_integrand_direct(const Marg &m, double B) {
   double x = 0.0;
   for (int j = 0; j < m.n; j++) {
     double c = m.SCALE * (m.star[j] + B);
@@ -70,6 +77,28 @@ __device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
     else return 0.0;
   }
   return exp(x - m.A);
+}
+
+// The same integrand in relative form.  With c_j(B) = SCALE (s_j + B) and
+// A = x(Bi),
+//   x(B) - A = sum_j d_j log(c_j(B) / c_j(Bi)) - n SCALE (B - Bi),
+// whose terms are O(d_j |B - Bi| / c_j) instead of O(d_j log c_j): no
+// cancellation against A.  The ratio 1 + (B - Bi) SCALE / c_j(Bi) and its
+// logarithm are taken in double-float arithmetic (FP32 pipes); a node where
+// some ratio is not positive (c_j(B) <= 0) takes the direct form, which
+// holds the reference's tests for that case.
+__device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
+  if (!m.rel) return marginal_integrand_direct(m, B);
+  const double dBd = B - m.Bi;
+  const DF dB = df_split(dBd);
+  const DF one{1.0f, 0.0f};
+  DF acc{0.0f, 0.0f};
+  for (int j = 0; j < m.n; j++) {
+    const DF r = df_fma(dB, m.q[j], one);
+    if (!(r.h > 0.0f)) return marginal_integrand_direct(m, B);
+    if (m.dataf[j] != 0.0f) acc = df_fma(DF{m.dataf[j], 0.0f}, df_log(r), acc);
+  }
+  return exp(df_value(acc) - (double)m.n * m.SCALE * dBd);
 }
 
 // sum over the warp; the butterfly adds the same pairs in every lane, so all
@@ -323,7 +352,7 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
     if (limit > 0.0) flag = 1;
   }
   const double *support = a.support + 2 * (size_t)ch;
-  Marg m{B, SCALE, T, 0.0, w.data, w.star};
+  Marg m{B, SCALE, T, 0.0, w.data, w.star, 0, 0.0, w.q, w.dataf};
   double Bfinal = 0.0;
   if (!flag) {
     av_STAR /= n;
@@ -403,6 +432,19 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
       A = warp_sum(A);
       dsum = warp_sum(dsum);
       m.A = A;
+      // relative form of the integrand when every c_j(Bi) > 0
+      bool pos = true;
+      for (int j = lane; j < B; j += 32) {
+        const double c = SCALE * (w.star[j] + Bi);
+        pos = pos && c > 0.0;
+        w.q[j] = c > 0.0 ? df_split(SCALE / c) : DF{0.0f, 0.0f};
+        w.dataf[j] = (float)w.data[j];
+      }
+      __syncwarp();
+      if (__all_sync(0xffffffffu, pos)) {
+        m.rel = 1;
+        m.Bi = Bi;
+      }
       double result;
       if (dsum == 0.0) {
         // no counts in the channel: every term is -c_j, so the integrand is
