@@ -234,16 +234,28 @@ def run_gb300(args):
                        "kernel_ms": int_ms, "flops_per_launch": int_flops,
                        "peak_source": "measured FP64 FMA probe on this GPU (not in "
                        "MEASURED_PEAKS.json)", "hbm_peak_gbs": pk.get("hbm_gbs"),
-                       "hbm_peak_source": pk_kind}
+                       "hbm_peak_source": pk_kind,
+                       "note": "achieved counts the reference algorithm's FP64 operations "
+                               "(cost model of the path); the kernel computes them at "
+                               "FP64-class accuracy as double-float arithmetic on the "
+                               "FP32 pipes (64x the FP64 issue rate), so frac can exceed "
+                               "1 against the FP64 pipe's peak; pipe utilisation of this "
+                               "kernel is in profiles/"}
     plain_ll = B["loglike"].cpu().numpy().copy()
     if rank == 0:
-        out["mixed"] = mixed_leg(model, P, plain_ll, st, args)
-        out["drop_in"] = drop_in_leg(model, P, min(V, args.drop_in_vectors))
-        out["batched_vs_drop_in"] = value / out["drop_in"]["value"]
-        out["mixed_vs_drop_in"] = out["mixed"]["value"] / out["drop_in"]["value"]
-        if args.serve_seconds > 0:
+        legs = set(args.legs.split(",")) if args.legs != "all" else \
+            {"mixed", "drop_in", "serving", "cpu"}
+        if "mixed" in legs:
+            out["mixed"] = mixed_leg(model, P, plain_ll, st, args)
+        if "drop_in" in legs:
+            out["drop_in"] = drop_in_leg(model, P, min(V, args.drop_in_vectors))
+            out["batched_vs_drop_in"] = value / out["drop_in"]["value"]
+            if "mixed" in out:
+                out["mixed_vs_drop_in"] = out["mixed"]["value"] / out["drop_in"]["value"]
+        if "serving" in legs and args.serve_seconds > 0:
             out["serving"] = serving_leg(args)
-        out["cpu_baseline"] = cpu_baseline(args, model, params)
+        if "cpu" in legs:
+            out["cpu_baseline"] = cpu_baseline(args, model, params)
         print(json.dumps(out))
 
 
@@ -415,7 +427,7 @@ def serving_leg(args):
             p = SY.config3_vectors(v, seed=int(rng.integers(1 << 30)))
         reqs.append((t, name, p))
     srv = Server({k: v[0] for k, v in models.items()}, hbm_budget=120 << 30, slots=4,
-                 precision="mixed")
+                 precision="mixed", prep_threads=8)
     futs = []
     t0 = time.perf_counter()
     for t, name, p in reqs:
@@ -509,9 +521,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--vectors", type=int, default=256)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    # comma-separated subset of mixed,drop_in,serving,cpu (or "all", "none"):
+    # the legs run after the timed plain-path steps
+    ap.add_argument("--legs", default="all")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--drop-in-vectors", type=int, default=8)
-    ap.add_argument("--serve-rate", type=float, default=200.0)
+    # the stream's shape (Poisson arrivals, log-uniform batch sizes, even
+    # model mix) at an offered load one GPU sustains; 200 req/s with batches
+    # up to 4096 offers ~1e5 vectors/s
+    ap.add_argument("--serve-rate", type=float, default=40.0)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-max-batch", type=int, default=16)
     args = ap.parse_args()
