@@ -185,6 +185,14 @@ int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges,
                       const double *d_sq, double *out, const int64_t *out_off,
                       int accumulate, void *stream);
 
+/* The fold of xgpu_fold_batch on the tensor cores for the mixed-precision form: every
+ * FP64 operand is split as hi + lo in TF32 and out = M_hi in_hi + M_hi in_lo
+ * + M_lo in_hi is accumulated in FP32 (tcgen05.mma, TMEM accumulator; FP32-
+ * class relative error ~1e-7).  Same arguments and layouts as
+ * xgpu_fold_batch; the operand splits use stream-ordered scratch memory. */
+int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int ld,
+                       const double *in, double *out, void *stream);
+
 /* out[b][K][N] = matrix[K][0:q] @ in[b][q][N] for b < batch (FP64). */
 int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix,
                     int ld, const double *in, double *out, void *stream);

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
-UNITS = ["rays", "integrator", "energy", "fold", "likelihood", "abi", "mesh"]
+UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -142,6 +142,8 @@ def _bind(L):
                                         P, P, P, C.c_int, P]),
         "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
                                       P, P]),
+        "xgpu_fold_batch_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
+                                         P, P]),
         "xgpu_likelihood_batch": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
         "xgpu_likelihood_batch_static": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
         "xgpu_allocate_cells": (C.c_int, [SZ, SZ, SZ, D, D, D, D, C.c_int, D, D, D, D, D, D,
@@ -163,7 +165,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_eval_marginal_likelihood", "xgpu_rays_batch", "xgpu_integrate_batch",
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
             "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
-            "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed"]
+            "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed",
+            "xgpu_fold_batch_tc"]
 
 
 def lib():

@@ -247,8 +247,9 @@ class BatchEvaluator:
     precision "plain": every stage in FP64 (the drop-in's numerics).
     precision "mixed": the integrator's atmosphere interpolation (from an
     FP32 copy of the table), splines and cell x phase sums in FP32
-    (xgpu_integrate_batch_mixed); rays, energy integration, fold and the
-    likelihood stay FP64."""
+    (xgpu_integrate_batch_mixed) and the response fold on the tensor cores
+    in 3xTF32 split products with FP32 accumulation (xgpu_fold_batch_tc);
+    rays, energy integration and the likelihood as in the plain form."""
 
     def __init__(self, model: Model, device=0, precision="plain"):
         import torch
@@ -389,7 +390,8 @@ class BatchEvaluator:
         check(L.xgpu_energy_batch(n_m, N_E, N_P, self.log10edges.numel(), p(B["flux"]),
                                   p(B["off_in"]), p(self.log10E), p(self.log10edges),
                                   p(B["d_sq"]), p(B["integrated"]), p(B["off_out"]), 0, st))
-        check(L.xgpu_fold_batch(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
+        fold = L.xgpu_fold_batch_tc if self.precision == "mixed" else L.xgpu_fold_batch
+        check(fold(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
                                 p(B["integrated"]), p(B["folded"]), st))
         m = self.model
         ld = LikelihoodBatchData()

@@ -304,6 +304,19 @@ int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix, int ld
   return 0;
 }
 
+int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int ld,
+                       const double *in, double *out, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  xg::FoldArgs a{batch, K, q, N, matrix, ld, in, out};
+  Dev scratch;
+  int rc = dalloc(scratch, xg::fold_tc_scratch_bytes(a), st);
+  if (rc) return rc;
+  rc = xg::launch_fold_tc(a, scratch.p, st);
+  if (rc) return fail_msg("tensor-map encoding failed for the tensor-core fold");
+  CK(cudaGetLastError());
+  return 0;
+}
+
 double xgpu_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
                        void *stream) {
   return xg::launch_peak_probe(fp64, blocks, threads, iters, out,

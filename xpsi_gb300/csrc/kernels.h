@@ -100,6 +100,11 @@ struct FoldArgs {
   double *out;       // [batch][K][N]
 };
 void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
+// tensor-core form (3xTF32 split products, FP32 accumulation in TMEM);
+// scratch: fold_tc_scratch_bytes(a) bytes of device memory, 16-byte aligned.
+// Returns 0, or < 0 when the tile maps cannot be encoded.
+size_t fold_tc_scratch_bytes(const FoldArgs &a);
+int launch_fold_tc(const FoldArgs &a, void *scratch, cudaStream_t st);
 double launch_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
                          cudaStream_t st);
 
