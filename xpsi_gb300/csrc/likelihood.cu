@@ -30,7 +30,6 @@ struct WarpSmem {
   double data[kMaxB];
   DF q[kMaxB];        // SCALE / c_j(Bi): the relative form of the integrand
   float dataf[kMaxB];  // counts (exact in float below 2^24)
-  double fv[42];
   double al[kQagLimit], bl[kQagLimit], rl[kQagLimit], el[kQagLimit];
 };
 
@@ -127,41 +126,18 @@ __device__ __forceinline__ double newton_delta(const Marg &m, double B, int lane
   return -1.0 * y / x;
 }
 
-// panel sums of the 21-point rule from the node values fv[0..20]:
-// nodes 0..9 at c - h X[j], 10 at c, 11..20 at c + h X[j]
-__device__ void gk21_sums(const double *fv, double a, double b, double &res, double &err,
-                          double &rabs, double &rasc) {
-  const int NH = XG_K21_HALF - 1;
-  double h = 0.5 * (b - a), ah = fabs(h);
-  double fc = fv[NH];
-  double rk = XG_K21_WK[NH] * fc, rg = XG_K21_WG[NH] * fc, ra = fabs(rk);
-  for (int j = 0; j < NH; j++) {
-    double f1 = fv[j], f2 = fv[NH + 1 + j];
-    rk += XG_K21_WK[j] * (f1 + f2);
-    rg += XG_K21_WG[j] * (f1 + f2);
-    ra += XG_K21_WK[j] * (fabs(f1) + fabs(f2));
-  }
-  double mean = 0.5 * rk;
-  double rc = XG_K21_WK[NH] * fabs(fc - mean);
-  for (int j = 0; j < NH; j++)
-    rc += XG_K21_WK[j] * (fabs(fv[j] - mean) + fabs(fv[NH + 1 + j] - mean));
-  res = rk * h;
-  ra *= ah;
-  rc *= ah;
-  double e = fabs((rk - rg) * h);
-  if (rc != 0.0 && e != 0.0) {
-    double sc = pow(200.0 * e / rc, 1.5);
-    e = sc < 1.0 ? rc * sc : rc;
-  }
-  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
-  if (ra > dmin / (50.0 * eps)) {
-    double fl = 50.0 * eps * ra;
-    if (fl > e) e = fl;
-  }
-  err = e;
-  rabs = ra;
-  rasc = rc;
-}
+// The 21-point Gauss-Kronrod panels of the marginal quadrature, evaluated by
+// the warp: lane l holds node l and node l + 32 of up to two panels (nodes
+// 0..20 the first, 21..41 the second; within a panel, nodes 0..9 at
+// c - h X[j], 10 at c, 11..20 at c + h X[j]).  The weighted sums of the
+// rule are lane-parallel xor-butterfly reductions (identical bits in every
+// lane); the error estimate follows QUADPACK (the (200 e / rc)^1.5 scaling,
+// the 50 eps round-off floor).
+struct Panel {
+  double res, err, rabs, rasc;
+};
+
+__device__ __forceinline__ int gk21_slot(int n) { return n < 10 ? n : (n == 10 ? 10 : n - 11); }
 
 __device__ __forceinline__ double gk21_node(double a, double b, int n) {
   const int NH = XG_K21_HALF - 1;
@@ -171,25 +147,100 @@ __device__ __forceinline__ double gk21_node(double a, double b, int n) {
   return c + h * XG_K21_X[n - NH - 1];
 }
 
-// two panels [a1,b1], [a2,b2] (the second optional) evaluated by the warp
-__device__ void warp_panels(const Marg &m, WarpSmem &w, int lane, double a1, double b1,
-                            double a2, double b2, bool two) {
-  const int total = two ? 42 : 21;
-  for (int t = lane; t < total; t += 32) {
-    double x = (t < 21) ? gk21_node(a1, b1, t) : gk21_node(a2, b2, t - 21);
-    w.fv[t] = marginal_integrand(m, x);
+__device__ __forceinline__ Panel gk21_finish(double rk, double rg, double ra, double rc, double a,
+                                             double b) {
+  const double h = 0.5 * (b - a), ah = fabs(h);
+  Panel P;
+  P.res = rk * h;
+  ra *= ah;
+  rc *= ah;
+  double e = fabs((rk - rg) * h);
+  if (rc != 0.0 && e != 0.0) {
+    const double x = 200.0 * e / rc, sc = x * sqrt(x);  // x^1.5
+    e = sc < 1.0 ? rc * sc : rc;
   }
-  __syncwarp();
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  if (ra > dmin / (50.0 * eps)) {
+    const double fl = 50.0 * eps * ra;
+    if (fl > e) e = fl;
+  }
+  P.err = e;
+  P.rabs = ra;
+  P.rasc = rc;
+  return P;
+}
+
+// one panel [a1, b1] (two: also [a2, b2]); returns the panels' sums
+__device__ void warp_panels(const Marg &m, int lane, double a1, double b1, double a2, double b2,
+                            bool two, Panel &P1, Panel &P2) {
+  const int total = two ? 42 : 21;
+  double f0 = 0.0, f1 = 0.0;
+  if (lane < total) f0 = marginal_integrand(m, lane < 21 ? gk21_node(a1, b1, lane)
+                                                         : gk21_node(a2, b2, lane - 21));
+  if (lane + 32 < total) f1 = marginal_integrand(m, gk21_node(a2, b2, lane + 32 - 21));
+  double rk1 = 0.0, rg1 = 0.0, ra1 = 0.0, rk2 = 0.0, rg2 = 0.0, ra2 = 0.0;
+  if (lane < total) {
+    if (lane < 21) {
+      const int s = gk21_slot(lane);
+      rk1 = XG_K21_WK[s] * f0; rg1 = XG_K21_WG[s] * f0; ra1 = XG_K21_WK[s] * fabs(f0);
+    } else {
+      const int s = gk21_slot(lane - 21);
+      rk2 = XG_K21_WK[s] * f0; rg2 = XG_K21_WG[s] * f0; ra2 = XG_K21_WK[s] * fabs(f0);
+    }
+  }
+  if (lane + 32 < total) {
+    const int s = gk21_slot(lane + 32 - 21);
+    rk2 += XG_K21_WK[s] * f1; rg2 += XG_K21_WG[s] * f1; ra2 += XG_K21_WK[s] * fabs(f1);
+  }
+  rk1 = warp_sum(rk1); rg1 = warp_sum(rg1); ra1 = warp_sum(ra1);
+  if (two) { rk2 = warp_sum(rk2); rg2 = warp_sum(rg2); ra2 = warp_sum(ra2); }
+  const double mean1 = 0.5 * rk1, mean2 = 0.5 * rk2;
+  double rc1 = 0.0, rc2 = 0.0;
+  if (lane < total) {
+    if (lane < 21) rc1 = XG_K21_WK[gk21_slot(lane)] * fabs(f0 - mean1);
+    else rc2 = XG_K21_WK[gk21_slot(lane - 21)] * fabs(f0 - mean2);
+  }
+  if (lane + 32 < total) rc2 += XG_K21_WK[gk21_slot(lane + 32 - 21)] * fabs(f1 - mean2);
+  rc1 = warp_sum(rc1);
+  P1 = gk21_finish(rk1, rg1, ra1, rc1, a1, b1);
+  if (two) {
+    rc2 = warp_sum(rc2);
+    P2 = gk21_finish(rk2, rg2, ra2, rc2, a2, b2);
+  }
+}
+
+// index of the first largest error among el[0..size) (QUADPACK's choice of
+// the interval to bisect), by a warp arg-max with ties to the lower index;
+// identical in every lane (a NaN error counts as -inf)
+__device__ __forceinline__ int warp_worst(const double *el, int size, int lane) {
+  double v = -INFINITY;
+  int k = 0x7fffffff;
+  for (int i = lane; i < size; i += 32) {
+    const double e = isnan(el[i]) ? -INFINITY : el[i];
+    if (k == 0x7fffffff || e > v) {
+      v = e;
+      k = i;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int k2 = __shfl_xor_sync(0xffffffffu, k, o);
+    if (v2 > v || (v2 == v && k2 < k)) {
+      v = v2;
+      k = k2;
+    }
+  }
+  return k;
 }
 
 // adaptive GK21 (same scheme as the rays' QAG), warp-cooperative; a < b
 __device__ double warp_qag21_core(const Marg &m, WarpSmem &w, int lane, double a, double b,
                                   double epsabs, double er) {
   const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
-  double r0, e0, ra0, rc0;
-  warp_panels(m, w, lane, a, b, 0, 0, false);
-  gk21_sums(w.fv, a, b, r0, e0, ra0, rc0);
-  __syncwarp();
+  Panel P0, Pu;
+  warp_panels(m, lane, a, b, 0.0, 0.0, false, P0, Pu);
+  const double r0 = P0.res, e0 = P0.err, ra0 = P0.rabs, rc0 = P0.rasc;
   double tol = fmax(epsabs, er * fabs(r0));
   double rfloor = 50.0 * eps * ra0;
   if ((e0 <= rfloor && e0 > tol) || (e0 <= tol && e0 != rc0) || e0 == 0.0) return r0;
@@ -200,11 +251,10 @@ __device__ double warp_qag21_core(const Marg &m, WarpSmem &w, int lane, double a
   do {
     double ai = w.al[k], bi = w.bl[k], ri = w.rl[k], ei = w.el[k];
     double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
-    warp_panels(m, w, lane, a1, b1, a2, b2, true);
-    double r1, e1, ra1, rc1, r2, e2, ra2, rc2;
-    gk21_sums(w.fv, a1, b1, r1, e1, ra1, rc1);
-    gk21_sums(w.fv + 21, a2, b2, r2, e2, ra2, rc2);
-    __syncwarp();
+    Panel P1, P2;
+    warp_panels(m, lane, a1, b1, a2, b2, true, P1, P2);
+    const double r1 = P1.res, e1 = P1.err, rc1 = P1.rasc;
+    const double r2 = P2.res, e2 = P2.err, rc2 = P2.rasc;
     double r12 = r1 + r2, e12 = e1 + e2;
     errsum += e12 - ei;
     area += r12 - ri;
@@ -220,6 +270,7 @@ __device__ double warp_qag21_core(const Marg &m, WarpSmem &w, int lane, double a
       if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
     }
     int nw = size++;
+    __syncwarp();
     if (lane == 0) {
       if (e2 > e1) {
         w.al[k] = a2; w.bl[k] = b2; w.rl[k] = r2; w.el[k] = e2;
@@ -230,13 +281,12 @@ __device__ double warp_qag21_core(const Marg &m, WarpSmem &w, int lane, double a
       }
     }
     __syncwarp();
-    k = 0;
-    for (int i = 1; i < size; i++)
-      if (w.el[i] > w.el[k]) k = i;
+    k = warp_worst(w.el, size, lane);
     iter++;
   } while (iter < kQagLimit && !fail && errsum > tol);
   double sum = 0.0;
-  for (int i = 0; i < size; i++) sum += w.rl[i];
+  for (int i = lane; i < size; i += 32) sum += w.rl[i];
+  sum = warp_sum(sum);
   __syncwarp();
   return sum;
 }
