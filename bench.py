@@ -34,6 +34,9 @@ sys.path.insert(0, HERE)
 
 METRIC = "likelihood evals/s at |ΔlogL|≤1e-3 vs FP64, batched vs plain GPU; p50/p99 latency"
 UNIT = "likelihood evals/s"
+WORKLOAD = ("batched prior vectors of the full-size plain model (2 Num4D hot regions, one "
+            "omitted crescent; 64/128 cells, 128 leaves, 1024 rays, 128 energies, 1500x128 "
+            "response, 32 bins)")
 
 
 def peaks():
@@ -210,9 +213,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded prior draws, "
         "Poisson counts from the model)",
-        "config": {"workload": "batched prior vectors of the full-size plain model "
-                   "(2 Num4D hot regions, one omitted crescent; 64/128 cells, 128 leaves, "
-                   "1024 rays, 128 energies, 1500x128 response, 32 bins)",
+        "config": {"workload": WORKLOAD,
                    "vectors_per_gpu": V, "precision": "plain FP64",
                    "l2": "inputs and ray tables larger than L2 (129 MB) every step",
                    "mesh_build_host_s": round(t_mesh, 3),
@@ -503,7 +504,7 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_tot / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded prior draws, Poisson counts from the model)",
-           "config": {"workload": "batched prior vectors of the full-size plain model",
+           "config": {"workload": WORKLOAD, "vectors_per_gpu": args.vectors,
                       "vectors_sampled": n_tot},
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
