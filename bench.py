@@ -130,9 +130,17 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def shard_vectors(V, rank, world, seed=3):
+    """This rank's V prior vectors: disjoint slices of one seeded draw of
+    V * world vectors (each replica evaluates its own vectors)."""
+    from xpsi_gb300 import synthetic as SY
+    return SY.config3_vectors(V * world, seed=seed)[rank * V:(rank + 1) * V]
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -156,7 +164,7 @@ def run_gb300(args):
     SY.attach_data(model, [folded[0], folded[1]], P0.shifts[0])
     ev = BT.BatchEvaluator(model, device=local)
     # each rank evaluates its own V vectors (independent parameter vectors)
-    params = SY.config3_vectors(V * world, seed=3)[rank * V:(rank + 1) * V]
+    params = shard_vectors(V, rank, world)
     t0 = time.time()
     P = BT.prepare(model, params)
     t_mesh = time.time() - t0
