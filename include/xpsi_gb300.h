@@ -280,6 +280,41 @@ typedef struct {
 /* Many meshes at once on n_threads host threads (0: all cores). */
 int xgpu_cell_mesh_many(int n, const xgpu_mesh_request *req, int n_threads);
 
+/* ---------------------------------------------------------------------- */
+/* The meshes of a batch built on the GPU and written straight into the     */
+/* packed arrays of xgpu_rays_batch / xgpu_integrate_batch (device          */
+/* pointers).  Member m's mesh (the request fields as in xgpu_mesh_request) */
+/* owns rows [row_off, row_off + S) and cells [cell_off, cell_off + S^2),   */
+/* packed in member order.  Per row: u = r_s / r, r_s, maxAlpha, radius,    */
+/* cos_gamma, theta0 (the row's colatitude), the lag calibration offset     */
+/* lag_C (HotRegion.py:880-901) and lag_scale, row_mesh = m.  Per cell:     */
+/* cellArea, phi (cell azimuth - omit_azimuth, + pi when antiphased),       */
+/* params = (logT, log10 effective gravity of the row), radiates =          */
+/* cellArea > 0.  Scratch comes from the stream-ordered allocator.          */
+/* Returns 0, -2 on inconsistent members, -5 on a CUDA error.               */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t polar;
+  size_t num_cells, S;
+  double R_eq, zeta, epsilon;
+  int32_t star_shape_ind;
+  double cede_radius, cede_colatitude, super_radius, super_colatitude,
+      super_azimuth;
+  int64_t row_off, cell_off;
+  double r_s, lag_scale, omit_azimuth, logT;
+  int32_t antiphased;
+} xgpu_mesh_member;
+
+typedef struct {
+  double *u, *r_s, *maxAlpha, *radius, *cos_gamma, *theta0, *lag_C, *lag_scale;
+  int32_t *row_mesh;
+  double *cellArea, *phi, *params;
+  int32_t *radiates;
+} xgpu_mesh_batch_out;
+
+int xgpu_mesh_batch(int n, const xgpu_mesh_member *members, int64_t n_rows,
+                    int64_t n_cells, const xgpu_mesh_batch_out *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

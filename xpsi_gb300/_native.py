@@ -16,7 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
-UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh"]
+UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh",
+         "mesh_gpu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -107,6 +108,20 @@ class MeshRequest(C.Structure):
                 ("maxAlpha", P), ("cos_gamma", P), ("effGrav", P)]
 
 
+class MeshMember(C.Structure):
+    _fields_ = [("polar", I32), ("num_cells", SZ), ("S", SZ), ("R_eq", D), ("zeta", D),
+                ("epsilon", D), ("star_shape_ind", I32), ("cede_radius", D),
+                ("cede_colatitude", D), ("super_radius", D), ("super_colatitude", D),
+                ("super_azimuth", D), ("row_off", I64), ("cell_off", I64), ("r_s", D),
+                ("lag_scale", D), ("omit_azimuth", D), ("logT", D), ("antiphased", I32)]
+
+
+class MeshBatchOut(C.Structure):
+    _fields_ = [("u", P), ("r_s", P), ("maxAlpha", P), ("radius", P), ("cos_gamma", P),
+                ("theta0", P), ("lag_C", P), ("lag_scale", P), ("row_mesh", P),
+                ("cellArea", P), ("phi", P), ("params", P), ("radiates", P)]
+
+
 class LikelihoodBatchData(C.Structure):
     _fields_ = [("n_vec", I32), ("K", I32), ("B", I32), ("H", I32), ("N_P", I32),
                 ("exposure", D), ("epsabs", D), ("epsrel", D), ("epsilon", D),
@@ -151,6 +166,8 @@ def _bind(L):
         "xgpu_cell_mesh": (C.c_int, [C.c_int, SZ, SZ, D, D, D, C.c_int, D, D, D, D, D, P, P,
                                      P, P, P, P, P]),
         "xgpu_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(MeshRequest), C.c_int]),
+        "xgpu_mesh_batch": (C.c_int, [C.c_int, C.POINTER(MeshMember), I64, I64,
+                                      C.POINTER(MeshBatchOut), P]),
         "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -166,7 +183,7 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
             "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
             "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed",
-            "xgpu_fold_batch_tc"]
+            "xgpu_fold_batch_tc", "xgpu_mesh_batch"]
 
 
 def lib():

@@ -24,7 +24,8 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._native import (Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh, check, lib)
+from ._native import (Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh, MeshBatchOut,
+                      MeshMember, check, lib)
 from .cellmesh import mesh as _mesh
 
 # xpsi/global_imports.py
@@ -127,9 +128,17 @@ class Prepared:
     """Host-packed inputs of one batch (numpy), ready to upload."""
 
 
-def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
+def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
+            meshes: str = "host") -> Prepared:
     """Derived quantities and meshes of every (vector, hot region) member,
-    packed into the flat arrays the kernels read."""
+    packed into the flat arrays the kernels read.
+
+    meshes="host": the meshes are built here on the host's cores (C++) and
+    packed in numpy.  meshes="gpu": only the cell budget of each member is
+    computed here; BatchEvaluator.upload builds the meshes on the GPU
+    (xgpu_mesh_batch) straight into the packed device arrays."""
+    if meshes not in ("host", "gpu"):
+        raise ValueError("meshes must be 'host' or 'gpu'")
     params = np.atleast_2d(np.asarray(params, dtype=np.float64))
     V = params.shape[0]
     H = len(model.regions)
@@ -181,12 +190,35 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
                              super_azimuth=o_a))
             members.append(dict(v=v, h=h, S=S, logT=logT, shift=shift, omit_azimuth=o_a,
                                 antiphased=r.is_antiphased, spec=r, **star))
-    _mesh.build_many(reqs, n_threads)
     n_rows = sum(m["S"] for m in members)
     n_cells = sum(m["S"] * m["S"] for m in members)
     P = Prepared()
     P.V, P.H, P.n_rows, P.n_cells = V, H, n_rows, n_cells
     P.status = status
+    N_E, N_P = len(model.energies), model.regions[0].num_leaves
+    P.meshes = (Mesh * len(members))()
+    P.d_sq = np.empty(len(members))
+    P.shifts = np.empty((V, H))
+    P.members = members
+    if meshes == "gpu":
+        P.mesh_members = (MeshMember * len(members))()
+        ro = co = 0
+        for m_i, (m, q) in enumerate(zip(members, reqs)):
+            S = m["S"]
+            P.mesh_members[m_i] = MeshMember(
+                int(q["polar"]), int(q["num_cells"]), S, float(q["R_eq"]), float(q["zeta"]),
+                float(q["epsilon"]), int(q["star_shape_ind"]), float(q["cede_radius"]),
+                float(q["cede_colatitude"]), float(q["super_radius"]),
+                float(q["super_colatitude"]), float(q["super_azimuth"]), ro, co,
+                float(m["r_s"]), float(m["f"] * _2PI), float(m["omit_azimuth"]),
+                float(m["logT"]), int(bool(m["antiphased"])))
+            _member_meta(P, m_i, m, ro, co, N_E, N_P)
+            ro += S
+            co += S * S
+        P.row = None
+        return P
+    P.mesh_members = None
+    _mesh.build_many(reqs, n_threads)
     P.row = {k: np.empty(n_rows) for k in ("u", "r_s", "maxAlpha", "radius", "cos_gamma",
                                            "theta0", "lag_C", "lag_scale")}
     P.row_mesh = np.empty(n_rows, dtype=np.int32)
@@ -194,10 +226,6 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
     P.phi = np.empty(n_cells)
     P.params = np.empty((n_cells, 2))
     P.radiates = np.empty(n_cells, dtype=np.int32)
-    P.meshes = (Mesh * len(members))()
-    P.d_sq = np.empty(len(members))
-    P.shifts = np.empty((V, H))
-    N_E, N_P = len(model.energies), model.regions[0].num_leaves
     ro = co = 0
     for m_i, (m, q) in enumerate(zip(members, reqs)):
         S = m["S"]
@@ -229,16 +257,18 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0) -> Prepared:
             prm[:, j, -1] *= q["effGrav"]
         P.params[cs] = prm.reshape(-1, 2)
         P.radiates[cs] = np.greater(A, 0.0).astype(np.int32).reshape(-1)
-        spec = m["spec"]
-        P.meshes[m_i] = Mesh(S, S, ro, co, m["Omega"], m["inclination"],
-                             int(spec.image_order_limit or 0), int(spec.atm_ext),
-                             m_i * N_E * N_P)
-        P.d_sq[m_i] = m["d_sq"]
-        P.shifts[m["v"], m["h"]] = m["shift"]
+        _member_meta(P, m_i, m, ro, co, N_E, N_P)
         ro += S
         co += S * S
-    P.members = members
     return P
+
+
+def _member_meta(P, m_i, m, ro, co, N_E, N_P):
+    S, spec = m["S"], m["spec"]
+    P.meshes[m_i] = Mesh(S, S, ro, co, m["Omega"], m["inclination"],
+                         int(spec.image_order_limit or 0), int(spec.atm_ext), m_i * N_E * N_P)
+    P.d_sq[m_i] = m["d_sq"]
+    P.shifts[m["v"], m["h"]] = m["shift"]
 
 
 class BatchEvaluator:
@@ -309,15 +339,43 @@ class BatchEvaluator:
                 h = h.pin_memory()
             return h.to(dev, non_blocking=True)
         B = dict()
-        B["row"] = {k: put(v) for k, v in P.row.items()}
-        B["row_mesh"] = put(P.row_mesh)
-        B["cellArea"], B["phi"] = put(P.cellArea), put(P.phi)
-        B["params"], B["radiates"] = put(P.params), put(P.radiates)
+        if P.mesh_members is not None:
+            self._gpu_meshes(P, B)
+        else:
+            B["row"] = {k: put(v) for k, v in P.row.items()}
+            B["row_mesh"] = put(P.row_mesh)
+            B["cellArea"], B["phi"] = put(P.cellArea), put(P.phi)
+            B["params"], B["radiates"] = put(P.params), put(P.radiates)
         B["d_sq"], B["shifts"] = put(P.d_sq), put(P.shifts)
         self.alloc(P, B)
         return B
 
+    def _gpu_meshes(self, P, B):
+        """Build the batch's meshes on the device (xgpu_mesh_batch) into the
+        packed row and cell arrays, on torch's current stream."""
+        torch = self.torch
+        dev, f64, i32 = self.dev, torch.float64, torch.int32
+        R, C_ = P.n_rows, P.n_cells
+        B["row"] = {k: torch.empty(R, dtype=f64, device=dev)
+                    for k in ("u", "r_s", "maxAlpha", "radius", "cos_gamma", "theta0",
+                              "lag_C", "lag_scale")}
+        B["row_mesh"] = torch.empty(R, dtype=i32, device=dev)
+        B["cellArea"] = torch.empty(C_, dtype=f64, device=dev)
+        B["phi"] = torch.empty(C_, dtype=f64, device=dev)
+        B["params"] = torch.empty((C_, 2), dtype=f64, device=dev)
+        B["radiates"] = torch.empty(C_, dtype=i32, device=dev)
+        p = lambda x: x.data_ptr()
+        row = B["row"]
+        o = MeshBatchOut(p(row["u"]), p(row["r_s"]), p(row["maxAlpha"]), p(row["radius"]),
+                         p(row["cos_gamma"]), p(row["theta0"]), p(row["lag_C"]),
+                         p(row["lag_scale"]), p(B["row_mesh"]), p(B["cellArea"]), p(B["phi"]),
+                         p(B["params"]), p(B["radiates"]))
+        st = torch.cuda.current_stream(dev).cuda_stream
+        check(lib().xgpu_mesh_batch(len(P.mesh_members), P.mesh_members, R, C_, C.byref(o), st))
+
     def h2d_bytes(self, P: Prepared):
+        if P.mesh_members is not None:
+            return int(C.sizeof(P.mesh_members) + P.d_sq.nbytes + P.shifts.nbytes)
         return int(sum(v.nbytes for v in P.row.values()) + P.row_mesh.nbytes
                    + P.cellArea.nbytes + P.phi.nbytes + P.params.nbytes + P.radiates.nbytes
                    + P.d_sq.nbytes + P.shifts.nbytes)
@@ -448,21 +506,28 @@ def concat_prepared(parts, model: Model) -> Prepared:
     if len(parts) == 1:
         return parts[0]
     N_E, N_P = len(model.energies), model.regions[0].num_leaves
+    gpu = parts[0].mesh_members is not None
+    if any((p.mesh_members is not None) != gpu for p in parts):
+        raise ValueError("cannot merge host-meshed and GPU-meshed batches")
     P = Prepared()
     P.H = parts[0].H
     P.V = sum(p.V for p in parts)
     P.n_rows = sum(p.n_rows for p in parts)
     P.n_cells = sum(p.n_cells for p in parts)
     P.status = np.concatenate([p.status for p in parts])
-    P.row = {k: np.concatenate([p.row[k] for p in parts]) for k in parts[0].row}
-    P.cellArea = np.concatenate([p.cellArea for p in parts])
-    P.phi = np.concatenate([p.phi for p in parts])
-    P.params = np.concatenate([p.params for p in parts])
-    P.radiates = np.concatenate([p.radiates for p in parts])
+    if gpu:
+        P.row = None
+    else:
+        P.row = {k: np.concatenate([p.row[k] for p in parts]) for k in parts[0].row}
+        P.cellArea = np.concatenate([p.cellArea for p in parts])
+        P.phi = np.concatenate([p.phi for p in parts])
+        P.params = np.concatenate([p.params for p in parts])
+        P.radiates = np.concatenate([p.radiates for p in parts])
     P.d_sq = np.concatenate([p.d_sq for p in parts])
     P.shifts = np.concatenate([p.shifts for p in parts])
     n_m = sum(len(p.meshes) for p in parts)
     P.meshes = (Mesh * n_m)()
+    P.mesh_members = (MeshMember * n_m)() if gpu else None
     rm, members = [], []
     ro = co = mo = 0
     for p in parts:
@@ -471,11 +536,19 @@ def concat_prepared(parts, model: Model) -> Prepared:
             P.meshes[mo + i] = Mesh(q.S0, q.S1, q.row_off + ro, q.cell_off + co, q.omega,
                                     q.inclination, q.image_order_limit, q.atm_ext,
                                     (mo + i) * N_E * N_P)
-        rm.append(p.row_mesh + mo)
+            if gpu:
+                mm = MeshMember()
+                C.memmove(C.byref(mm), C.byref(p.mesh_members[i]), C.sizeof(MeshMember))
+                mm.row_off += ro
+                mm.cell_off += co
+                P.mesh_members[mo + i] = mm
+        if not gpu:
+            rm.append(p.row_mesh + mo)
         members += p.members
         ro += p.n_rows
         co += p.n_cells
         mo += len(p.meshes)
-    P.row_mesh = np.concatenate(rm).astype(np.int32)
+    if not gpu:
+        P.row_mesh = np.concatenate(rm).astype(np.int32)
     P.members = members
     return P
