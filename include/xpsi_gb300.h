@@ -280,6 +280,19 @@ typedef struct {
 /* Many meshes at once on n_threads host threads (0: all cores). */
 int xgpu_cell_mesh_many(int n, const xgpu_mesh_request *req, int n_threads);
 
+/* Many cell budgets (xgpu_allocate_cells) at once on n_threads host threads
+ * (0: all cores); each request's result lands in its out[4]. */
+typedef struct {
+  size_t num_cells, min_sqrt, max_sqrt;
+  double R_eq, Omega, zeta, epsilon;
+  int32_t star_shape_ind;
+  double super_radius, cede_radius, super_colatitude, cede_colatitude,
+      super_azimuth, hole_colatitude, hole_radius, hole_azimuth;
+  double out[4];
+} xgpu_alloc_request;
+
+int xgpu_allocate_cells_many(int n, xgpu_alloc_request *req, int n_threads);
+
 /* ---------------------------------------------------------------------- */
 /* The meshes of a batch built on the GPU and written straight into the     */
 /* packed arrays of xgpu_rays_batch / xgpu_integrate_batch (device          */

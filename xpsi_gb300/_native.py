@@ -108,6 +108,14 @@ class MeshRequest(C.Structure):
                 ("maxAlpha", P), ("cos_gamma", P), ("effGrav", P)]
 
 
+class AllocRequest(C.Structure):
+    _fields_ = [("num_cells", SZ), ("min_sqrt", SZ), ("max_sqrt", SZ), ("R_eq", D),
+                ("Omega", D), ("zeta", D), ("epsilon", D), ("star_shape_ind", I32),
+                ("super_radius", D), ("cede_radius", D), ("super_colatitude", D),
+                ("cede_colatitude", D), ("super_azimuth", D), ("hole_colatitude", D),
+                ("hole_radius", D), ("hole_azimuth", D), ("out", D * 4)]
+
+
 class MeshMember(C.Structure):
     _fields_ = [("polar", I32), ("num_cells", SZ), ("S", SZ), ("R_eq", D), ("zeta", D),
                 ("epsilon", D), ("star_shape_ind", I32), ("cede_radius", D),
@@ -166,6 +174,7 @@ def _bind(L):
         "xgpu_cell_mesh": (C.c_int, [C.c_int, SZ, SZ, D, D, D, C.c_int, D, D, D, D, D, P, P,
                                      P, P, P, P, P]),
         "xgpu_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(MeshRequest), C.c_int]),
+        "xgpu_allocate_cells_many": (C.c_int, [C.c_int, C.POINTER(AllocRequest), C.c_int]),
         "xgpu_mesh_batch": (C.c_int, [C.c_int, C.POINTER(MeshMember), I64, I64,
                                       C.POINTER(MeshBatchOut), P]),
         "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
@@ -183,7 +192,7 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
             "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
             "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed",
-            "xgpu_fold_batch_tc", "xgpu_mesh_batch"]
+            "xgpu_fold_batch_tc", "xgpu_mesh_batch", "xgpu_allocate_cells_many"]
 
 
 def lib():

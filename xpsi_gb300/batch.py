@@ -24,8 +24,8 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._native import (Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh, MeshBatchOut,
-                      MeshMember, check, lib)
+from ._native import (AllocRequest, Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh,
+                      MeshBatchOut, MeshMember, check, lib)
 from .cellmesh import mesh as _mesh
 
 # xpsi/global_imports.py
@@ -146,7 +146,7 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
     if params.shape[1] != len(names):
         raise ValueError("expected %d parameters per vector: %s" % (len(names), names))
     col = {n: i for i, n in enumerate(names)}
-    reqs, members, status = [], [], np.zeros(V, dtype=np.int32)
+    reqs, members, pend, status = [], [], [], np.zeros(V, dtype=np.int32)
     atm = model.atmosphere
     for v in range(V):
         p = params[v]
@@ -179,17 +179,26 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
                 o_a = p[col[f"h{h}_omit_azimuth"]]
             else:
                 o_r = o_c = o_a = 0.0
-            a = _mesh.allocate_cells(r.sqrt_num_cells ** 2, r.min_sqrt_num_cells,
-                                     r.max_sqrt_num_cells, Mkg, r_s, R, Om, zeta, eps, 0, rad,
-                                     0.0, colat, colat, -0.0, o_c, o_r, o_a)
-            S = int(a[0])
-            polar = (colat - rad < 0.0) or (colat + rad > math.pi)
-            reqs.append(dict(polar=polar, num_cells=int(a[1]), S=S, R_eq=R, zeta=zeta,
-                             epsilon=eps, star_shape_ind=0, cede_radius=rad,
-                             cede_colatitude=colat, super_radius=o_r, super_colatitude=o_c,
-                             super_azimuth=o_a))
-            members.append(dict(v=v, h=h, S=S, logT=logT, shift=shift, omit_azimuth=o_a,
-                                antiphased=r.is_antiphased, spec=r, **star))
+            pend.append((AllocRequest(r.sqrt_num_cells ** 2, r.min_sqrt_num_cells,
+                                      r.max_sqrt_num_cells, R, Om, zeta, eps, 0, rad, 0.0,
+                                      colat, colat, -0.0, o_c, o_r, o_a),
+                         dict(colat=colat, rad=rad, o_r=o_r, o_c=o_c, o_a=o_a),
+                         dict(v=v, h=h, logT=logT, shift=shift, omit_azimuth=o_a,
+                              antiphased=r.is_antiphased, spec=r, **star)))
+    # cell budgets of all members at once (mesh_tools.pyx:892-1099), on the
+    # host's cores
+    alloc = (AllocRequest * len(pend))(*[q for q, _, _ in pend])
+    if pend:
+        check(lib().xgpu_allocate_cells_many(len(pend), alloc, int(n_threads)))
+    for k, (_, g, mem) in enumerate(pend):
+        S = int(alloc[k].out[0])
+        colat, rad = g["colat"], g["rad"]
+        polar = (colat - rad < 0.0) or (colat + rad > math.pi)
+        reqs.append(dict(polar=polar, num_cells=int(alloc[k].out[1]), S=S, R_eq=mem["R"],
+                         zeta=mem["zeta"], epsilon=mem["eps"], star_shape_ind=0,
+                         cede_radius=rad, cede_colatitude=colat, super_radius=g["o_r"],
+                         super_colatitude=g["o_c"], super_azimuth=g["o_a"]))
+        members.append(dict(S=S, **mem))
     n_rows = sum(m["S"] for m in members)
     n_cells = sum(m["S"] * m["S"] for m in members)
     P = Prepared()

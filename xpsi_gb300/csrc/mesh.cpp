@@ -162,6 +162,26 @@ int xgpu_cell_mesh(int polar, size_t num_cells, size_t S, double R_eq, double ze
                     super_colatitude, super_azimuth, o, *w);
 }
 
+int xgpu_allocate_cells_many(int n, xgpu_alloc_request *req, int n_threads) {
+  if (n <= 0) return 0;
+  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  n_threads = std::min(n_threads, n);
+  std::vector<std::thread> pool;
+  auto work = [&](int t) {
+    std::unique_ptr<Work> w(new Work);
+    for (int i = t; i < n; i += n_threads) {
+      xgpu_alloc_request &q = req[i];
+      Star s{q.R_eq, q.epsilon, q.zeta, q.Omega, q.star_shape_ind};
+      allocate(q.num_cells, q.min_sqrt, q.max_sqrt, s, q.super_radius, q.cede_radius,
+               q.super_colatitude, q.cede_colatitude, q.super_azimuth, q.hole_colatitude,
+               q.hole_radius, q.hole_azimuth, q.out, *w);
+    }
+  };
+  for (int t = 0; t < n_threads; t++) pool.emplace_back(work, t);
+  for (auto &th : pool) th.join();
+  return 0;
+}
+
 int xgpu_cell_mesh_many(int n, const xgpu_mesh_request *req, int n_threads) {
   if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
   std::vector<std::thread> pool;

@@ -11,11 +11,16 @@
 //   2. per mesh: the cell area and the S - 1 parallels (one thread, the
 //      reference's running sum), then one thread per parallel for its
 //      centre colatitude, radius, gravity, tilt and the packed row values;
-//   3. one thread per cell: the corner / centre membership tests and, for a
-//      cell cut by a region boundary, its area quadrature.
-// Each thread's quadrature keeps its interval list (128 intervals) in local
-// memory; the host builder's limit of 4000 gives bitwise the same meshes
-// (the boundary integrals converge in far fewer intervals).
+//   3. one thread per cell: the corner / centre membership tests; cells
+//      wholly inside or outside get their area at once, cells cut by a
+//      region boundary (~1 %) are queued;
+//   4. one warp per queued cell: its area quadrature, warp-cooperative (the
+//      21 or 42 Gauss-Kronrod nodes of a step over the lanes, the rule's
+//      sums reduced lane-parallel, the interval list in shared memory) --
+//      the same adaptive scheme the host builder runs serially.
+// The per-thread quadratures of steps 1-2 keep their interval list (128
+// intervals) in local memory; the host builder's limit of 4000 gives bitwise
+// the same meshes (these integrals converge in far fewer intervals).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,19 +105,218 @@ __global__ void __launch_bounds__(128) mesh_rows_kernel(const MeshJob *jobs, con
   }
 }
 
-// one thread per cell of the batch (cells of mesh m at [cell_off, cell_off + S^2))
-__global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, int n_mesh,
-                                                         int64_t n_cells, xgpu_mesh_batch_out o,
-                                                         const double *row_tmp,
-                                                         const double *mesh_tmp) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_cells) return;
+// ---------------------------------------------------------------------------
+// Warp-cooperative form of the quadrature of mesh_math.h (qag21, dyadic,
+// integrate): lane l evaluates node l and node l + 32 of the step's one or
+// two 21-point panels; sums are xor-butterfly reductions, identical in every
+// lane, so the control flow is warp-uniform.
+// ---------------------------------------------------------------------------
+constexpr int kWarpList = 128;
+struct WarpList {
+  double al[kWarpList], bl[kWarpList], rl[kWarpList], el[kWarpList];
+};
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct WPanel {
+  double res, err, rabs, rasc;
+};
+
+__device__ __forceinline__ int k21_slot(int n) { return n < 10 ? n : (n == 10 ? 10 : n - 11); }
+__device__ __forceinline__ double k21_node(double a, double b, int n) {
+  const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  if (n < 10) return c - h * XG_K21_X[n];
+  if (n == 10) return c;
+  return c + h * XG_K21_X[n - 11];
+}
+__device__ __forceinline__ WPanel k21_finish(double rk, double rg, double ra, double rc,
+                                             double a, double b) {
+  const double h = 0.5 * (b - a), ah = fabs(h);
+  WPanel P;
+  P.res = rk * h;
+  ra *= ah;
+  rc *= ah;
+  double e = fabs((rk - rg) * h);
+  if (rc != 0.0 && e != 0.0) {
+    const double sc = pow(200.0 * e / rc, 1.5);
+    e = sc < 1.0 ? rc * sc : rc;
+  }
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  if (ra > dmin / (50.0 * eps)) e = (e < 50.0 * eps * ra) ? 50.0 * eps * ra : e;
+  P.err = e;
+  P.rabs = ra;
+  P.rasc = rc;
+  return P;
+}
+
+template <typename F>
+__device__ void warp_k21(const F &f, int lane, double a1, double b1, double a2, double b2,
+                         bool two, WPanel &P1, WPanel &P2) {
+  const int total = two ? 42 : 21;
+  double f0 = 0.0, f1 = 0.0;
+  if (lane < total) f0 = f(lane < 21 ? k21_node(a1, b1, lane) : k21_node(a2, b2, lane - 21));
+  if (lane + 32 < total) f1 = f(k21_node(a2, b2, lane + 32 - 21));
+  double rk1 = 0.0, rg1 = 0.0, ra1 = 0.0, rk2 = 0.0, rg2 = 0.0, ra2 = 0.0;
+  if (lane < total) {
+    const int s = k21_slot(lane < 21 ? lane : lane - 21);
+    const double wk = XG_K21_WK[s], wg = XG_K21_WG[s];
+    if (lane < 21) { rk1 = wk * f0; rg1 = wg * f0; ra1 = wk * fabs(f0); }
+    else { rk2 = wk * f0; rg2 = wg * f0; ra2 = wk * fabs(f0); }
+  }
+  if (lane + 32 < total) {
+    const int s = k21_slot(lane + 32 - 21);
+    rk2 += XG_K21_WK[s] * f1; rg2 += XG_K21_WG[s] * f1; ra2 += XG_K21_WK[s] * fabs(f1);
+  }
+  rk1 = wsum(rk1); rg1 = wsum(rg1); ra1 = wsum(ra1);
+  if (two) { rk2 = wsum(rk2); rg2 = wsum(rg2); ra2 = wsum(ra2); }
+  const double mean1 = 0.5 * rk1, mean2 = 0.5 * rk2;
+  double rc1 = 0.0, rc2 = 0.0;
+  if (lane < total) {
+    if (lane < 21) rc1 = XG_K21_WK[k21_slot(lane)] * fabs(f0 - mean1);
+    else rc2 = XG_K21_WK[k21_slot(lane - 21)] * fabs(f0 - mean2);
+  }
+  if (lane + 32 < total) rc2 += XG_K21_WK[k21_slot(lane + 32 - 21)] * fabs(f1 - mean2);
+  P1 = k21_finish(rk1, rg1, ra1, wsum(rc1), a1, b1);
+  if (two) P2 = k21_finish(rk2, rg2, ra2, wsum(rc2), a2, b2);
+}
+
+template <typename F>
+__device__ double warp_qag21(const F &f, double a, double b, double epsabs, double er,
+                             WarpList &L, int lane) {
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  WPanel P0, Pu;
+  warp_k21(f, lane, a, b, 0.0, 0.0, false, P0, Pu);
+  const double r0 = P0.res, e0 = P0.err;
+  double tol = (epsabs < er * fabs(r0)) ? er * fabs(r0) : epsabs;
+  if ((e0 <= 50.0 * eps * P0.rabs && e0 > tol) || (e0 <= tol && e0 != P0.rasc) || e0 == 0.0)
+    return r0;
+  __syncwarp();
+  if (lane == 0) { L.al[0] = a; L.bl[0] = b; L.rl[0] = r0; L.el[0] = e0; }
+  __syncwarp();
+  int size = 1, iter = 1, k = 0, rnd1 = 0, rnd2 = 0, fail = 0;
+  double area = r0, errsum = e0;
+  do {
+    const double ai = L.al[k], bi = L.bl[k], ri = L.rl[k], ei = L.el[k];
+    const double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
+    WPanel P1, P2;
+    warp_k21(f, lane, a1, b1, a2, b2, true, P1, P2);
+    const double r1 = P1.res, e1 = P1.err, r2 = P2.res, e2 = P2.err;
+    const double r12 = r1 + r2, e12 = e1 + e2;
+    errsum += e12 - ei;
+    area += r12 - ri;
+    if (P1.rasc != e1 && P2.rasc != e2) {
+      if (fabs(ri - r12) <= 1.0e-5 * fabs(r12) && e12 >= 0.99 * ei) rnd1++;
+      if (iter >= 10 && e12 > ei) rnd2++;
+    }
+    tol = (epsabs < er * fabs(area)) ? er * fabs(area) : epsabs;
+    if (errsum > tol) {
+      if (rnd1 >= 6 || rnd2 >= 20) fail = 2;
+      const double edge = (1.0 + 100.0 * eps) * (fabs(a2) + 1000.0 * dmin);
+      if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
+    }
+    const int nw = size++;
+    __syncwarp();
+    if (lane == 0) {
+      if (e2 > e1) {
+        L.al[k] = a2; L.bl[k] = b2; L.rl[k] = r2; L.el[k] = e2;
+        L.al[nw] = a1; L.bl[nw] = b1; L.rl[nw] = r1; L.el[nw] = e1;
+      } else {
+        L.al[k] = a1; L.bl[k] = b1; L.rl[k] = r1; L.el[k] = e1;
+        L.al[nw] = a2; L.bl[nw] = b2; L.rl[nw] = r2; L.el[nw] = e2;
+      }
+    }
+    __syncwarp();
+    k = 0;
+    for (int i = 1; i < size; i++)
+      if (L.el[i] > L.el[k]) k = i;
+    iter++;
+  } while (iter < kWarpList && !fail && errsum > tol);
+  double sum = 0.0;
+  for (int i = 0; i < size; i++) sum += L.rl[i];
+  __syncwarp();
+  return sum;
+}
+
+template <typename F>
+__device__ double warp_dyadic(const F &f, double lo, double hi, bool toward_lo, double er,
+                              WarpList &L, int lane) {
+  const double Lw = hi - lo;
+  double sum = 0.0;
+  int seen = 0, quiet = 0;
+  for (int k = 0; k < 2100; k++) {
+    const double s1 = ldexp(Lw, -(k + 1)), s0 = ldexp(Lw, -k);
+    const double p0 = toward_lo ? lo + s1 : hi - s0;
+    const double p1 = toward_lo ? lo + s0 : hi - s1;
+    if (!(p0 < p1) || (toward_lo ? p0 <= lo : p1 >= hi)) break;
+    const double r = warp_qag21(f, p0, p1, 0.0, er, L, lane);
+    sum += r;
+    if (r != 0.0) seen = 1;
+    if (seen && fabs(r) <= 1.0e-17 * fabs(sum)) {
+      if (++quiet >= 4) break;
+    } else {
+      quiet = 0;
+    }
+  }
+  return sum;
+}
+
+template <typename F>
+__device__ double warp_integrate(const F &f, double a, double b, double epsabs, double epsrel,
+                                 WarpList &L, int lane) {
+  double sign = 1.0;
+  if (b < a) { const double t = a; a = b; b = t; sign = -1.0; }
+  if (a == b) return 0.0;
+  double er = (1.0e-13 < epsrel) ? 1.0e-13 : epsrel;
+  if (epsabs <= 0.0 && er < 50.0 * 2.220446049250313e-16) er = 50.0 * 2.220446049250313e-16;
+  double r = warp_qag21(f, a, b, epsabs, er, L, lane);
+  if (r == 0.0) {
+    const double fa = f(a), fb = f(b);
+    if (fa != 0.0 || fb != 0.0) {
+      const double m = 0.5 * (a + b);
+      const double rl = fa != 0.0 ? warp_dyadic(f, a, m, true, er, L, lane)
+                                  : warp_qag21(f, a, m, 0.0, er, L, lane);
+      const double rr = fb != 0.0 ? warp_dyadic(f, m, b, false, er, L, lane)
+                                  : warp_qag21(f, m, b, 0.0, er, L, lane);
+      r = rl + rr;
+    }
+  }
+  return sign * r;
+}
+
+__device__ __forceinline__ int mesh_of_cell(const MeshJob *jobs, int n_mesh, int64_t c) {
   int lo = 0, hi = n_mesh - 1;
   while (lo < hi) {  // last mesh whose cell_off <= c
     const int mid = (lo + hi + 1) >> 1;
     if (jobs[mid].cell_off <= c) lo = mid; else hi = mid - 1;
   }
-  const int m = lo;
+  return lo;
+}
+
+__device__ __forceinline__ void put_area(const MeshJob &J, xgpu_mesh_batch_out &o, int64_t c,
+                                         size_t i, size_t j, double A) {
+  const size_t S = J.pl.S;
+  o.cellArea[c] = A;
+  o.radiates[c] = A > 0.0 ? 1 : 0;
+  if (J.pl.sym) {
+    const int64_t cm = J.cell_off + (int64_t)(i * S + (S - 1 - j));
+    o.cellArea[cm] = A;
+    o.radiates[cm] = A > 0.0 ? 1 : 0;
+  }
+}
+
+// one thread per cell of the batch (cells of mesh m at [cell_off, cell_off + S^2))
+__global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, int n_mesh,
+                                                         int64_t n_cells, xgpu_mesh_batch_out o,
+                                                         const double *row_tmp,
+                                                         const double *mesh_tmp,
+                                                         int64_t *queue, unsigned *n_queue) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  const int m = mesh_of_cell(jobs, n_mesh, c);
   const MeshJob &J = jobs[m];
   const size_t S = J.pl.S;
   const int64_t k = c - J.cell_off;
@@ -127,20 +331,49 @@ __global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, in
   o.params[2 * c + 1] = row_tmp[4 * row + 3];
   const size_t j_max = J.pl.j_max;
   if (j < j_max) {
-    DWork w;
-    const double A = mesh_cell(J.pl, J.s, i, j, row_tmp[4 * row], row_tmp[4 * row + 1],
-                               row_tmp[4 * row + 2], mesh_tmp[2 * m], w);
-    o.cellArea[c] = A;
-    o.radiates[c] = A > 0.0 ? 1 : 0;
-    if (J.pl.sym) {
-      const int64_t cm = J.cell_off + (int64_t)(i * S + (S - 1 - j));
-      o.cellArea[cm] = A;
-      o.radiates[cm] = A > 0.0 ? 1 : 0;
-    }
+    double leftmost, rightmost;
+    const int kind = mesh_cell_kind(J.pl, i, j, row_tmp[4 * row], row_tmp[4 * row + 1],
+                                    row_tmp[4 * row + 2], leftmost, rightmost);
+    if (kind == 2) queue[atomicAdd(n_queue, 1u)] = c;
+    else put_area(J, o, c, i, j, kind == 1 ? mesh_tmp[2 * m] : 0.0);
   } else if (!J.pl.sym || j < S - j_max) {
     // columns no mirror reaches keep area 0
     o.cellArea[c] = 0.0;
     o.radiates[c] = 0;
+  }
+}
+
+// one warp per queued cell: the area quadrature of a cell cut by a boundary
+constexpr int kBoundaryWarps = 4;
+__global__ void __launch_bounds__(32 * kBoundaryWarps) mesh_boundary_kernel(
+    const MeshJob *jobs, int n_mesh, xgpu_mesh_batch_out o, const double *row_tmp,
+    const int64_t *queue, const unsigned *n_queue) {
+  __shared__ WarpList lists[kBoundaryWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpList &L = lists[wid];
+  const unsigned n = *n_queue;
+  const unsigned stride = gridDim.x * kBoundaryWarps;
+  for (unsigned q = blockIdx.x * kBoundaryWarps + wid; q < n; q += stride) {
+    const int64_t c = queue[q];
+    const int m = mesh_of_cell(jobs, n_mesh, c);
+    const MeshJob &J = jobs[m];
+    const size_t S = J.pl.S;
+    const int64_t k = c - J.cell_off;
+    const size_t i = (size_t)(k / (int64_t)S), j = (size_t)(k - (int64_t)i * (int64_t)S);
+    const int64_t row = J.row_off + (int64_t)i;
+    const double lower = row_tmp[4 * row], upper = row_tmp[4 * row + 1];
+    double pa, pb;
+    mesh_cell_kind(J.pl, i, j, lower, upper, row_tmp[4 * row + 2], pa, pb);
+    const Region g = mesh_region(J.pl);
+    const CellIntegrand f{J.s, g, pa, pb};
+    double integral = warp_integrate(f, lower, upper, 0.0, 1.0e-8, L, lane);
+    if (are_equal(integral, 0.0)) {
+      double tmin, tmax;
+      if (cell_fallback_interval(lower, upper, pa, pb, g, tmin, tmax))
+        integral = warp_integrate(f, tmin, tmax, 0.0, 1.0e-8, L, lane);
+    }
+    if (lane == 0) put_area(J, o, c, i, j, J.s.R_eq * J.s.R_eq * integral);
+    __syncwarp();
   }
 }
 
@@ -179,25 +412,34 @@ extern "C" int xgpu_mesh_batch(int n, const xgpu_mesh_member *members, int64_t n
   if (rows != n_rows || cells != n_cells) return -2;
   MeshJob *d_jobs = nullptr;
   double *tab = nullptr, *row_tmp = nullptr, *mesh_tmp = nullptr;
+  int64_t *queue = nullptr;
+  unsigned *n_queue = nullptr;
   if (cudaMallocAsync(&d_jobs, sizeof(MeshJob) * (size_t)n, st) != cudaSuccess) return -5;
   if (cudaMallocAsync(&tab, sizeof(double) * (size_t)n * kAreaTab, st) != cudaSuccess ||
       cudaMallocAsync(&row_tmp, sizeof(double) * 4 * (size_t)n_rows, st) != cudaSuccess ||
-      cudaMallocAsync(&mesh_tmp, sizeof(double) * 2 * (size_t)n, st) != cudaSuccess) {
+      cudaMallocAsync(&mesh_tmp, sizeof(double) * 2 * (size_t)n, st) != cudaSuccess ||
+      cudaMallocAsync(&queue, sizeof(int64_t) * (size_t)n_cells, st) != cudaSuccess ||
+      cudaMallocAsync(&n_queue, sizeof(unsigned), st) != cudaSuccess) {
     cudaFreeAsync(d_jobs, st);
     return -5;
   }
+  // (a copy from pageable memory has been staged when cudaMemcpyAsync
+  // returns, so the host jobs may go out of scope)
   cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(MeshJob) * (size_t)n, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(n_queue, 0, sizeof(unsigned), st);
   mesh_table_kernel<<<dim3((kAreaTab + 127) / 128, (unsigned)n), 128, 0, st>>>(d_jobs, tab);
   const size_t smem = sizeof(double) * (kAreaTab + S_max);
   mesh_rows_kernel<<<(unsigned)n, 128, smem, st>>>(d_jobs, tab, *out, row_tmp, mesh_tmp);
-  mesh_cells_kernel<<<(unsigned)((n_cells + 127) / 128), 128, 0, st>>>(d_jobs, n, n_cells, *out,
-                                                                         row_tmp, mesh_tmp);
-  // (a copy from pageable memory has been staged when cudaMemcpyAsync
-  // returns, so the host jobs may go out of scope)
+  mesh_cells_kernel<<<(unsigned)((n_cells + 127) / 128), 128, 0, st>>>(
+      d_jobs, n, n_cells, *out, row_tmp, mesh_tmp, queue, n_queue);
+  mesh_boundary_kernel<<<152 * 8, 32 * kBoundaryWarps, 0, st>>>(d_jobs, n, *out, row_tmp, queue,
+                                                                 n_queue);
   const cudaError_t e = cudaGetLastError();
   cudaFreeAsync(d_jobs, st);
   cudaFreeAsync(tab, st);
   cudaFreeAsync(row_tmp, st);
   cudaFreeAsync(mesh_tmp, st);
+  cudaFreeAsync(queue, st);
+  cudaFreeAsync(n_queue, st);
   return e == cudaSuccess ? 0 : -5;
 }

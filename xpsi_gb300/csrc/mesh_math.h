@@ -358,11 +358,13 @@ XG_HD inline double phi_edge(double theta, double phi_a, double phi_b, const Reg
   return v;
 }
 
-// mesh_tools.pyx:412-772
-template <typename W>
-XG_QD double integrateCell(double ta, double tb, double pa, double pb, const Star &s,
-                           const Region &g, W &w) {
-  auto f = [&](double theta) -> double {
+// mesh_tools.pyx:412-772: the integrand of a cell's area over colatitude
+// (the cell's share of the ring, times the surface element)
+struct CellIntegrand {
+  Star s;
+  Region g;
+  double pa, pb;
+  XG_HD double operator()(double theta) const {
     if (are_equal(theta, 0.0)) return 0.0;
     double mu = cos(theta);
     double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
@@ -371,35 +373,51 @@ XG_QD double integrateCell(double ta, double tb, double pa, double pb, const Sta
     double dphi = ring_extent(theta, g, true, pa, pb, zero);
     if (zero) return 0.0;
     return dphi * radius * radius * sqrt(1.0 + ft * ft) * sin(theta);
-  };
+  }
+};
+
+// when the integral over [ta, tb] vanishes, the reference integrates again
+// between the region boundary's crossings of the cell's edges
+XG_HD inline bool cell_fallback_interval(double ta, double tb, double pa, double pb,
+                                         const Region &g, double &tmin, double &tmax) {
+  const double interval[2] = {ta, tb};
+  double tl[2] = {theta_given_phi(pa, g.colat, g.cedeRadius, interval),
+                  theta_given_phi(pa - g.superAzi, g.superColat, g.superRadius, interval)};
+  double tr[2] = {theta_given_phi(pb, g.colat, g.cedeRadius, interval),
+                  theta_given_phi(pb - g.superAzi, g.superColat, g.superRadius, interval)};
+  double top[2] = {phi_edge(ta, pa, pb, g, false), phi_edge(ta, pa, pb, g, true)};
+  double bot[2] = {phi_edge(tb, pa, pb, g, false), phi_edge(tb, pa, pb, g, true)};
+  double inter[2][2];
+  for (int r = 0; r < 2; r++) {
+    for (int q = 0; q < 2; q++) {
+      if (tl[r] >= 0.0) { inter[r][q] = tl[r]; tl[r] = -1.0; }
+      else if (tr[r] >= 0.0) { inter[r][q] = tr[r]; tr[r] = -1.0; }
+      else if (top[r] >= 0.0) { inter[r][q] = ta; top[r] = -1.0; }
+      else if (bot[r] >= 0.0) { inter[r][q] = tb; bot[r] = -1.0; }
+      else inter[r][q] = -1.0;
+    }
+  }
+  tmin = tb;
+  tmax = ta;
+  double th[4] = {inter[0][0], inter[0][1], inter[1][0], inter[1][1]};
+  for (int i = 0; i < 4; i++) {
+    if (th[i] >= 0.0) {
+      if (th[i] < tmin) tmin = th[i];
+      if (th[i] > tmax) tmax = th[i];
+    }
+  }
+  return tmin < tmax;
+}
+
+template <typename W>
+XG_QD double integrateCell(double ta, double tb, double pa, double pb, const Star &s,
+                           const Region &g, W &w) {
+  const CellIntegrand f{s, g, pa, pb};
   double integral = integrate(f, ta, tb, 0.0, 1.0e-8, w);
   if (are_equal(integral, 0.0)) {
-    const double interval[2] = {ta, tb};
-    double tl[2] = {theta_given_phi(pa, g.colat, g.cedeRadius, interval),
-                    theta_given_phi(pa - g.superAzi, g.superColat, g.superRadius, interval)};
-    double tr[2] = {theta_given_phi(pb, g.colat, g.cedeRadius, interval),
-                    theta_given_phi(pb - g.superAzi, g.superColat, g.superRadius, interval)};
-    double top[2] = {phi_edge(ta, pa, pb, g, false), phi_edge(ta, pa, pb, g, true)};
-    double bot[2] = {phi_edge(tb, pa, pb, g, false), phi_edge(tb, pa, pb, g, true)};
-    double inter[2][2];
-    for (int r = 0; r < 2; r++) {
-      for (int q = 0; q < 2; q++) {
-        if (tl[r] >= 0.0) { inter[r][q] = tl[r]; tl[r] = -1.0; }
-        else if (tr[r] >= 0.0) { inter[r][q] = tr[r]; tr[r] = -1.0; }
-        else if (top[r] >= 0.0) { inter[r][q] = ta; top[r] = -1.0; }
-        else if (bot[r] >= 0.0) { inter[r][q] = tb; bot[r] = -1.0; }
-        else inter[r][q] = -1.0;
-      }
-    }
-    double tmin = tb, tmax = ta;
-    double th[4] = {inter[0][0], inter[0][1], inter[1][0], inter[1][1]};
-    for (int i = 0; i < 4; i++) {
-      if (th[i] >= 0.0) {
-        if (th[i] < tmin) tmin = th[i];
-        if (th[i] > tmax) tmax = th[i];
-      }
-    }
-    if (tmin < tmax) integral = integrate(f, tmin, tmax, 0.0, 1.0e-8, w);
+    double tmin, tmax;
+    if (cell_fallback_interval(ta, tb, pa, pb, g, tmin, tmax))
+      integral = integrate(f, tmin, tmax, 0.0, 1.0e-8, w);
   }
   return s.R_eq * s.R_eq * integral;
 }
@@ -586,14 +604,13 @@ XG_QD inline RowOut mesh_row(const Star &s, double lower, double upper, double e
   return o;
 }
 
-// area of cell (i, j) (mesh.pyx:170-400): corner / centre membership tests
-// against the ceding and superseding regions; a cell cut by a boundary is
-// integrated, a cell wholly inside gets the nominal cell area.  The cell's
-// left edge is replayed as the reference's running sum of cell widths.
-template <typename W>
-XG_QD inline double mesh_cell(const MeshPlan &pl, const Star &s, size_t i, size_t j,
-                              double lower, double upper, double colatC, double cellArea,
-                              W &w) {
+// cell (i, j) (mesh.pyx:170-400): corner / centre membership tests against
+// the ceding and superseding regions.  Returns 0 (area 0), 1 (the nominal
+// cell area) or 2 (a cell cut by a boundary: integrate it), and the cell's
+// azimuth edges, replayed as the reference's running sum of cell widths.
+XG_HD inline int mesh_cell_kind(const MeshPlan &pl, size_t i, size_t j, double lower,
+                                double upper, double colatC, double &leftmost,
+                                double &rightmost) {
   const bool polar = pl.polar;
   const double cedeColat = pl.cedeColat, cedeRadius = pl.cedeRadius;
   const double superRadius = pl.superRadius, superColat = pl.superColat;
@@ -604,7 +621,8 @@ XG_QD inline double mesh_cell(const MeshPlan &pl, const Star &s, size_t i, size_
     if (p1 == 1) { p1 = p1 * (superRadius <= superColat); p3 = p1; }
     else { p1 = p3 = 2; }
   }
-  double leftmost = polar ? -PI : -pl.boundary_phi, rightmost = leftmost + delta_phi;
+  leftmost = polar ? -PI : -pl.boundary_phi;
+  rightmost = leftmost + delta_phi;
   for (size_t k = 0; k < j; k++) {
     leftmost = rightmost;
     rightmost = leftmost + delta_phi;
@@ -632,22 +650,28 @@ XG_QD inline double mesh_cell(const MeshPlan &pl, const Star &s, size_t i, size_
     p5 = p5 * (superRadius <= eval_psi(colatC, leftmost + 0.5 * delta_phi - superAzi, superColat));
   else
     p5 = 2;
-  const Region g{cedeColat, cedeRadius, superRadius, superAzi, superColat};
-  double A = 0.0;
-  if (!(p1 == p2 && p2 == p3 && p3 == p4 && p4 == p5)) {
-    A = integrateCell(lower, upper, leftmost, rightmost, s, g, w);
-  } else if (superRadius > 0.0) {
-    auto in = [&](const double *q) {
-      return lower <= q[0] && q[0] <= upper && leftmost <= q[1] && q[1] <= rightmost;
-    };
-    if (in(pl.sp1) || in(pl.sp2) || in(pl.sp3) || in(pl.sp4))
-      A = integrateCell(lower, upper, leftmost, rightmost, s, g, w);
-    else if (p5 == 1)
-      A = cellArea;
-  } else if (p5 == 1) {
-    A = cellArea;
+  if (!(p1 == p2 && p2 == p3 && p3 == p4 && p4 == p5)) return 2;
+  if (superRadius > 0.0) {
+    const double l = leftmost, r = rightmost;
+    auto in = [&](const double *q) { return lower <= q[0] && q[0] <= upper && l <= q[1] && q[1] <= r; };
+    if (in(pl.sp1) || in(pl.sp2) || in(pl.sp3) || in(pl.sp4)) return 2;
   }
-  return A;
+  return p5 == 1 ? 1 : 0;
+}
+
+XG_HD inline Region mesh_region(const MeshPlan &pl) {
+  return Region{pl.cedeColat, pl.cedeRadius, pl.superRadius, pl.superAzi, pl.superColat};
+}
+
+// area of cell (i, j)
+template <typename W>
+XG_QD inline double mesh_cell(const MeshPlan &pl, const Star &s, size_t i, size_t j,
+                              double lower, double upper, double colatC, double cellArea,
+                              W &w) {
+  double leftmost, rightmost;
+  const int kind = mesh_cell_kind(pl, i, j, lower, upper, colatC, leftmost, rightmost);
+  if (kind == 2) return integrateCell(lower, upper, leftmost, rightmost, s, mesh_region(pl), w);
+  return kind == 1 ? cellArea : 0.0;
 }
 
 }  // namespace xgm

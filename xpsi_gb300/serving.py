@@ -7,7 +7,9 @@ resolutions, leaves, rays, energies) are registered once and their atmosphere
 table, response matrix, data and grids stay resident on the device.
 
 Pipeline:
-  submit -> host preparation thread(s): derived quantities and cell meshes
+  submit -> host preparation thread(s): derived quantities and cell budgets
+            (the meshes themselves are built on the GPU at admission, or on
+            the host with meshes="host")
          -> ready queue
          -> dispatcher: requests of one model that are ready together are
             merged into one launch (up to max_vectors); a launch is admitted
@@ -70,7 +72,11 @@ def estimate_bytes(ev: BT.BatchEvaluator, P) -> int:
     n_m = P.V * P.H
     N_E = len(ev.model.energies)
     N_P = ev.N_L
-    b = ev.h2d_bytes(P)
+    # packed rows (8 FP64 + mesh index) and cells (area, azimuth, 2 params,
+    # flag), whether uploaded or built on the device, plus the GPU mesh
+    # builder's scratch (area tables, per-row temporaries)
+    b = P.n_rows * (8 * 8 + 4) + P.n_cells * (4 * 8 + 4) + P.d_sq.nbytes + P.shifts.nbytes
+    b += len(P.meshes) * 1000 * 8 + P.n_rows * 4 * 8
     b += 3 * P.n_rows * ev.N_R * 8 + P.n_rows * 12
     b += n_m * (N_E * N_P + ev.q * N_P + ev.K * N_P) * 8
     b += P.V * ev.K * 12 + P.V * 12
@@ -82,7 +88,8 @@ def estimate_bytes(ev: BT.BatchEvaluator, P) -> int:
 
 class Server:
     def __init__(self, models: dict, device=0, hbm_budget=120 << 30, slots=4,
-                 max_vectors=4096, precision="plain", prep_threads=2, mesh_threads=0):
+                 max_vectors=4096, precision="plain", prep_threads=2, mesh_threads=0,
+                 meshes="gpu"):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
@@ -92,6 +99,7 @@ class Server:
         self.budget = int(hbm_budget)
         self.max_vectors = int(max_vectors)
         self.mesh_threads = mesh_threads
+        self.meshes = meshes
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(slots)]
         self.free_slots = list(range(slots))
         self.in_use = 0
@@ -143,7 +151,8 @@ class Server:
             if r is None:
                 return
             try:
-                r.prepared = BT.prepare(self.evals[r.model].model, r.params, self.mesh_threads)
+                r.prepared = BT.prepare(self.evals[r.model].model, r.params, self.mesh_threads,
+                                        meshes=self.meshes)
                 r.t_ready = time.perf_counter()
                 with self.ready_lock:
                     self.ready.append(r)
