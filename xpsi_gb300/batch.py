@@ -493,11 +493,12 @@ class BatchEvaluator:
         st[P.status != 0] = P.status[P.status != 0]
         return st
 
-    def loglikelihood(self, params, n_threads=0):
+    def loglikelihood(self, params, n_threads=0, meshes="gpu"):
         """log L of every parameter vector (host in, host out) and statuses.
         Vectors whose status is not 0 get a value near llzero, as
-        Likelihood.random_near_llzero does (Likelihood.py:268-271)."""
-        P = prepare(self.model, params, n_threads)
+        Likelihood.random_near_llzero does (Likelihood.py:268-271).  The
+        meshes are built on the GPU unless meshes="host"."""
+        P = prepare(self.model, params, n_threads, meshes=meshes)
         B = self.upload(P)
         self.run(B)
         ll = B["loglike"].cpu().numpy().copy()
