@@ -14,12 +14,12 @@
 // Kernel: one CTA (4 warps) per 128 x 128 tile of C.  Per 32-wide K block the
 // elected thread issues four TMA tile loads (A_hi, A_lo, B_hi, B_lo; 128 rows
 // x 128 bytes each, 128-byte swizzle) completing on an mbarrier, then the
-// twelve tcgen05.mma (4 K steps x 3 products, M = N = 128, K = 8) into one
-// FP32 accumulator of 128 TMEM columns, and a tcgen05.commit to a second
-// mbarrier before the buffers are refilled.  The epilogue: each warp reads
-// its 32 TMEM lanes (rows) with tcgen05.ld and stores FP64.  Every mbarrier
-// wait is bounded; on a timeout the tile is written as NaN and the kernel
-// still waits (bounded) for its copies and MMAs and frees its TMEM.
+// three tcgen05.mma per 8-wide K step (M = N = 128, K = 8) into an FP32
+// accumulator of 128 TMEM columns, committed to a second mbarrier; each
+// warp reads its 32 TMEM lanes (rows) with tcgen05.ld after every step and
+// sums the steps in registers, then stores FP64.  Every mbarrier wait is
+// bounded; on a timeout the tile is written as NaN and the kernel still
+// waits (bounded) for its copies and MMAs and frees its TMEM.
 #include <cuda.h>
 
 #include "common.cuh"
@@ -215,67 +215,77 @@ __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
-  if (threadIdx.x == 0) {
-    const int nkb = q_pad / kTK;
-    int pending = 0;  // on failure: 1 = a tile load, 2 = a commit still outstanding
-    uint32_t pending_par = 0;
-    for (int kb = 0; kb < nkb; kb++) {
-      const uint32_t par = (uint32_t)(kb & 1);
+  // Per K step (8 along K) the elected thread issues the three split
+  // products into the TMEM accumulator (fresh each step) and waits for them;
+  // every warp then reads its lanes' partial and adds it to FP32 registers
+  // (round to nearest).  The tensor core's accumulation then spans only 3
+  // products per step instead of all 3 x q / 8, which keeps its rounding
+  // bias at the FP32 level of one step's partial.
+  const int m = m0 + warp * 32 + lane;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  float acc[kTN];
+#pragma unroll
+  for (int c = 0; c < kTN; c++) acc[c] = 0.0f;
+  const int nkb = q_pad / kTK;
+  int step = 0;
+  for (int kb = 0; kb < nkb && !s_fail; kb++) {
+    if (threadIdx.x == 0) {
       mbar_expect_tx(&bar_full, kStageBytes);
       const int x = kb * kTK;
       tma_load_2d(sA_hi, &mapA, x, m0, &bar_full);
       tma_load_2d(sA_lo, &mapA, x, rows_a + m0, &bar_full);
       tma_load_2d(sB_hi, &mapB, x, (int)n0, &bar_full);
       tma_load_2d(sB_lo, &mapB, x, rows_b + (int)n0, &bar_full);
-      if (!mbar_wait(&bar_full, par)) {
+      if (!mbar_wait(&bar_full, (uint32_t)(kb & 1))) {
         s_fail = 1;
-        pending = 1;
-        pending_par = par;
-        break;
+        mbar_wait(&bar_full, (uint32_t)(kb & 1));  // let the copy land (bounded)
       }
-      tc_fence_after();
-#pragma unroll
-      for (int ks = 0; ks < kTK / 8; ks++) {
+    }
+    __syncthreads();
+    if (s_fail) break;
+    for (int ks = 0; ks < kTK / 8; ks++, step++) {
+      if (threadIdx.x == 0) {
+        tc_fence_after();
         const uint32_t off = (uint32_t)ks * 32;  // 8 TF32 = 32 bytes along K
         const uint64_t ah = smem_desc_sw128(smem_u32(sA_hi) + off);
         const uint64_t al = smem_desc_sw128(smem_u32(sA_lo) + off);
         const uint64_t bh = smem_desc_sw128(smem_u32(sB_hi) + off);
         const uint64_t bl = smem_desc_sw128(smem_u32(sB_lo) + off);
-        mma_tf32(tmem, ah, bh, kIdescTf32, (kb > 0 || ks > 0) ? 1u : 0u);
+        mma_tf32(tmem, ah, bh, kIdescTf32, 0u);
         mma_tf32(tmem, ah, bl, kIdescTf32, 1u);
         mma_tf32(tmem, al, bh, kIdescTf32, 1u);
+        mma_commit(&bar_mma);
+        if (!mbar_wait(&bar_mma, (uint32_t)(step & 1))) {
+          s_fail = 1;
+          mbar_wait(&bar_mma, (uint32_t)(step & 1));  // let the MMAs finish (bounded)
+        }
       }
-      mma_commit(&bar_mma);
-      if (!mbar_wait(&bar_mma, par)) {
-        s_fail = 1;
-        pending = 2;
-        pending_par = par;
-        break;
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (s_fail) break;
+#pragma unroll
+      for (int c = 0; c < kTN / 32; c++) {
+        uint32_t r[32];
+        tmem_ld32(lane_base + (uint32_t)(c * 32), r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 32; j++) acc[c * 32 + j] += __uint_as_float(r[j]);
       }
+      // the next step's MMA overwrites the accumulator: every read first
+      tc_fence_before();
+      __syncthreads();
     }
-    // after a timeout, let the copy or the MMAs still in flight land before
-    // the buffers and the accumulator are released (again bounded)
-    if (pending == 1) mbar_wait(&bar_full, pending_par);
-    if (pending == 2) mbar_wait(&bar_mma, pending_par);
   }
-  tc_fence_before();
-  __syncthreads();
   tc_fence_after();
   const bool fail = s_fail != 0;
-  // epilogue: warp w holds rows 32w .. 32w+31 of the tile in its TMEM lanes
-  const int m = m0 + warp * 32 + lane;
-  for (int c = 0; c < kTN / 32; c++) {
-    uint32_t r[32];
-    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
-    tmem_ld_wait();
-    if (m < K) {
+  if (m < K) {
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const long n = n0 + c * 32 + j;
-        if (n < cols) {
-          const long b = n / N, p = n - b * N;
-          out[((size_t)b * K + m) * N + p] = fail ? nan("") : (double)__uint_as_float(r[j]);
-        }
+    for (int c = 0; c < kTN; c++) {
+      const long n = n0 + c;
+      if (n < cols) {
+        const long b = n / N, p = n - b * N;
+        out[((size_t)b * K + m) * N + p] = fail ? nan("") : (double)acc[c];
       }
     }
   }
