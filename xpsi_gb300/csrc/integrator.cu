@@ -346,6 +346,7 @@ struct AtmSmem {
   double *gmu, *gE;      // grids of mu and log10(E/kT)
   double *smu, *sE;      // inverse Lagrange denominators per stencil base, 4 each
   float *fgmu, *fgE, *fsmu, *fsE;  // FP32 copies for the mixed-precision form
+  float *fgEo;           // [3 nE] offsets gE[b + i] - gE[b], i = 1..3 (mixed form)
   float *fphase;         // FP32 copy of the phase knots
   float *fphase_lo;      // phase knot minus its FP32 copy
   float *fcphi, *fcphi_lo;  // cell azimuths of the parallel as float pairs (<= kMaxCellsF)
@@ -492,27 +493,45 @@ __device__ __forceinline__ void lagrange_wf(const float *P, const float *S, int 
   w[3] = d3 * S[4 * b + 3];
 }
 
-__device__ __forceinline__ float eval_num4d_slab_f(const Atmos4D &A, const AtmSmem &as,
-                                                   const float *slab, float E, float mu,
-                                                   bool clamp_mu, float E_eff, float p3) {
+// Num4D intensity in the mixed form: the slab and the Lagrange weights in
+// FP32, the mu stencil formed once per profile column; the energy
+// coordinate v3 = log10 E - log10 Z - log10 E_eff and its offset from the
+// stencil base in FP64, so the weights see the FP32 rounding of an offset of
+// a few grid spacings (~1e-9 absolute) rather than that of the coordinate
+// (~3e-8, the same on every evaluation of a parallel: a systematic shift).
+struct MuStencilF {
+  int b2;
+  float w2[4];
+};
+__device__ __forceinline__ MuStencilF mu_stencil_f(const Atmos4D &A, const AtmSmem &as, float mu,
+                                                   bool clamp_mu) {
   float v2 = mu;
   const float mu_hi = as.fgmu[A.nmu - 1];
   if (v2 > mu_hi && clamp_mu) v2 = mu_hi;
   if (v2 < as.fgmu[0]) v2 = as.fgmu[0];
-  float v3 = log10f(E / E_eff);
-  if (v3 < as.fgE[0]) v3 = as.fgE[0];
-  if (v3 > as.fgE[A.nE - 1]) v3 = as.fgE[A.nE - 1];
-  const int b2 = stencil_base_f(as.fgmu, A.nmu, v2);
-  const int b3 = stencil_base_f(as.fgE, A.nE, v3);
-  float w2[4], w3[4];
-  lagrange_wf(as.fgmu, as.fsmu, b2, v2, w2);
-  lagrange_wf(as.fgE, as.fsE, b3, v3, w3);
+  MuStencilF m;
+  m.b2 = stencil_base_f(as.fgmu, A.nmu, v2);
+  lagrange_wf(as.fgmu, as.fsmu, m.b2, v2, m.w2);
+  return m;
+}
+__device__ __forceinline__ float eval_num4d_f(const Atmos4D &A, const AtmSmem &as,
+                                              const float *slab, const MuStencilF &m, double v3,
+                                              float p3) {
+  if (v3 < as.gE[0]) v3 = as.gE[0];
+  if (v3 > as.gE[A.nE - 1]) v3 = as.gE[A.nE - 1];
+  const int b3 = stencil_base_guided(as.gE, as.fgE, A.nE, v3);
+  const float u = (float)(v3 - as.gE[b3]);
+  const float *o = as.fgEo + 3 * b3;  // node offsets gE[b3 + i] - gE[b3], i = 1..3
+  const float d0 = u, d1 = u - o[0], d2 = u - o[1], d3 = u - o[2];
+  const float *S = as.fsE + 4 * b3;
+  const float w3[4] = {d1 * d2 * d3 * S[0], d0 * d2 * d3 * S[1], d0 * d1 * d3 * S[2],
+                       d0 * d1 * d2 * S[3]};
   float I = 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const float *r = slab + (size_t)(b2 + k) * A.nE + b3;
-    float t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
-    I += w2[k] * t;
+    const float *r = slab + (size_t)(m.b2 + k) * A.nE + b3;
+    const float t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
+    I += m.w2[k] * t;
   }
   if (I < 0.0f) return 0.0f;
   return I * p3;
@@ -542,6 +561,7 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
             + (size_t)ec * N_L * piece_bytes       // coefficients
             + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
             + (size_t)(nmu + nE) * 5 * sizeof(float)   // their FP32 copies (mixed form)
+            + (size_t)3 * nE * sizeof(float)           // energy-grid node offsets (mixed)
             + (size_t)(5 * N_L + 4 * kMaxCellsF + kMaxEnergiesF) * sizeof(float)
             + (size_t)N_R * sizeof(double)  // staged deflection table
             + (size_t)(ec + N_L) * sizeof(double)  // lgE, lzs
@@ -583,6 +603,7 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
     atm->fgE = f; f += nE;
     atm->fsmu = f; f += (size_t)4 * nmu;
     atm->fsE = f; f += (size_t)4 * nE;
+    atm->fgEo = f; f += (size_t)3 * nE;
     atm->fphase = f; f += N_L;
     atm->fphase_lo = f; f += N_L;
     atm->fcphi = f; f += kMaxCellsF;
@@ -852,6 +873,10 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         as.fE[t] = (float)a.energies[t];
       for (int t = threadIdx.x; t < 4 * nmu; t += blockDim.x) as.fsmu[t] = (float)as.smu[t];
       for (int t = threadIdx.x; t < 4 * nEt; t += blockDim.x) as.fsE[t] = (float)as.sE[t];
+      for (int t = threadIdx.x; t < 3 * nEt; t += blockDim.x) {
+        const int b = t / 3, i = t - 3 * b + 1;
+        as.fgEo[t] = b + i < nEt ? (float)(as.gE[b + i] - as.gE[b]) : 0.0f;
+      }
     }
     slab = a.slab + (size_t)chunk * nmu * nEt;
     slabf = reinterpret_cast<float *>(slab);
@@ -940,6 +965,11 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     }
     const double kT = (kKB / kKeV) * pow(10.0, c.vec0);
     const float kT_f = (float)kT;
+    // mixed form: the FP32 roundings of the constant factors norm and
+    // 10^(3 log T) are undone exactly on the parallel's FP64 partials
+    const float p3f = (float)p3;
+    const double fix = num4d ? (norm * p3) / ((double)(float)norm * (double)p3f)
+                             : norm / (double)(float)norm;
     const double lg_Eeff = num4d ? log10(E_eff) : 0.0;
     const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
     const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
@@ -992,9 +1022,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             as.finvZ[sidx] = (float)(1.0 / g.Z[sidx]);
             as.fabb[sidx] = (float)g.ABB[sidx];
             as.fgeom[sidx] = (float)g.GEOM[sidx];
-          } else if (num4d) {
-            g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
           }
+          if (num4d) g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
         }
       }
       __syncthreads();
@@ -1007,7 +1036,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
 
       for (int e0 = 0; e0 < N_E; e0 += EC) {
         const int ne = min(EC, N_E - e0);
-        if (!kMixed && num4d) {
+        if (num4d) {
           for (int t = threadIdx.x; t < ne; t += blockDim.x) g.lgE[t] = log10(a.energies[e0 + t]);
           __syncthreads();
         }
@@ -1017,6 +1046,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         {
           int mu_col = -1;
           MuStencil ms{};
+          MuStencilF msf{};
           for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
             const int pl = t / N_L, col = t - pl * N_L;
             const int p = e0 + pl;
@@ -1024,14 +1054,23 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             WT y = WT(0);
             if (s >= 0) {
               if constexpr (kMixed) {
-                const float Ef = p < kMaxEnergiesF ? as.fE[p] : (float)a.energies[p];
-                const float Ep = Ef * as.finvZ[s];
                 float I_E;
-                if (num4d)
-                  I_E = eval_num4d_slab_f(a.atmos, as, slabf, Ep, as.fabb[s],
-                                          p == 0 && g.clamp0[s], (float)E_eff, (float)p3);
-                else
-                  I_E = eval_bb_f(Ep, kT_f);
+                if (num4d) {
+                  const double v3 = g.lgE[pl] - g.lzs[s];
+                  if (p == 0 && g.clamp0[s]) {
+                    I_E = eval_num4d_f(a.atmos, as, slabf,
+                                       mu_stencil_f(a.atmos, as, as.fabb[s], true), v3, p3f);
+                  } else {
+                    if (s != mu_col) {
+                      msf = mu_stencil_f(a.atmos, as, as.fabb[s], false);
+                      mu_col = s;
+                    }
+                    I_E = eval_num4d_f(a.atmos, as, slabf, msf, v3, p3f);
+                  }
+                } else {
+                  const float Ef = p < kMaxEnergiesF ? as.fE[p] : (float)a.energies[p];
+                  I_E = eval_bb_f(Ef * as.finvZ[s], kT_f);
+                }
                 y = (WT)((float)norm * I_E * as.fgeom[s]);
               } else {
                 double I_E;
@@ -1160,7 +1199,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             }
 #pragma unroll
             for (int e = 0; e < kEPT; e++)
-              if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += (double)acc[e];
+              if (pb + e < ne) part[(size_t)(e0 + pb + e) * N_P + k] += (double)acc[e] * fix;
           } else {
             DF acc[kEPT];
 #pragma unroll
