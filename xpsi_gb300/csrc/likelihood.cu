@@ -530,28 +530,41 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   }
 }
 
-// channel-ordered sum and the reference's early exits
+// per-evaluation sum over channels and the reference's early exits: one
+// warp per evaluation; the first flagged channel (lowest index) decides the
+// early exit (:677-684, :423-429), otherwise the channel terms are summed by
+// lane partials in a fixed order (bitwise reproducible)
 __global__ void like_finalize_kernel(LikeArgs a) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (v >= a.n_vec) return;
   double LL = 0.0;
-  int st = kOk;
-  for (int ch = 0; ch < a.K; ch++) {
-    size_t o = (size_t)v * a.K + ch;
-    int f = a.chan_flag[o];
-    if (f != 0) {
-      // llzero * (0.1 + 0.9 U): U from a hash of (evaluation, channel)
-      uint32_t hsh = (uint32_t)v * 2654435761u ^ (uint32_t)ch * 40503u ^ 0x9e3779b9u;
-      hsh ^= hsh >> 16; hsh *= 0x7feb352du; hsh ^= hsh >> 15; hsh *= 0x846ca68bu; hsh ^= hsh >> 16;
-      double U = (double)(hsh >> 8) / 16777215.0;
-      LL = a.llzero * (0.1 + 0.9 * U);
-      st = (f == 1) ? kSlimCut : kQuadFail;
-      break;
+  int first = 0x7fffffff;
+  for (int ch = lane; ch < a.K; ch += 32) {
+    const size_t o = (size_t)v * a.K + ch;
+    if (a.chan_flag[o] != 0) {
+      if (ch < first) first = ch;
+    } else {
+      LL += a.chan_ll[o];
     }
-    LL += a.chan_ll[o];
   }
-  a.loglike[v] = LL;
-  a.status[v] = st;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+  LL = warp_sum(LL);
+  int st = kOk;
+  if (first != 0x7fffffff) {
+    const int f = a.chan_flag[(size_t)v * a.K + first];
+    // llzero * (0.1 + 0.9 U): U from a hash of (evaluation, channel)
+    uint32_t hsh = (uint32_t)v * 2654435761u ^ (uint32_t)first * 40503u ^ 0x9e3779b9u;
+    hsh ^= hsh >> 16; hsh *= 0x7feb352du; hsh ^= hsh >> 15; hsh *= 0x846ca68bu; hsh ^= hsh >> 16;
+    const double U = (double)(hsh >> 8) / 16777215.0;
+    LL = a.llzero * (0.1 + 0.9 * U);
+    st = (f == 1) ? kSlimCut : kQuadFail;
+  }
+  if (lane == 0) {
+    a.loglike[v] = LL;
+    a.status[v] = st;
+  }
 }
 
 }  // namespace
@@ -561,7 +574,7 @@ void launch_likelihood(const LikeArgs &a, cudaStream_t st) {
   if (warps <= 0) return;
   unsigned blocks = (unsigned)((warps + kWarps - 1) / kWarps);
   like_channel_kernel<<<blocks, 32 * kWarps, 0, st>>>(a);
-  like_finalize_kernel<<<(a.n_vec + 127) / 128, 128, 0, st>>>(a);
+  like_finalize_kernel<<<(a.n_vec + 3) / 4, 128, 0, st>>>(a);
 }
 
 }  // namespace xg
