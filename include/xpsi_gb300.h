@@ -328,6 +328,82 @@ typedef struct {
 int xgpu_mesh_batch(int n, const xgpu_mesh_member *members, int64_t n_rows,
                     int64_t n_cells, const xgpu_mesh_batch_out *out, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* The photosphere elsewhere: closed mesh and time-invariant integrator.    */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces xpsi.cellmesh.global_mesh.construct_closed_cellMesh
+ * (xpsi/cellmesh/global_mesh.pyx:21-137), host C++.  S = sqrt_numCell, even
+ * and >= 4.  Outputs theta[S][S], phi[S][S], r[S], *cellArea (the one area
+ * every cell has), maxAlpha[S], cos_gamma[S], effGrav[S].  Returns 0, or -1
+ * for an odd or too small S. */
+int xgpu_closed_cell_mesh(size_t S, size_t num_cells, double R_eq, double zeta,
+                          double epsilon, int star_shape_ind, double *theta,
+                          double *phi, double *r, double *cellArea,
+                          double *maxAlpha, double *cos_gamma, double *effGrav);
+
+/* Many closed meshes at once on n_threads host threads (0: all cores). */
+typedef struct {
+  size_t S, num_cells;
+  double R_eq, zeta, epsilon;
+  int32_t star_shape_ind;
+  double *theta, *phi, *r, *cellArea, *maxAlpha, *cos_gamma, *effGrav;
+} xgpu_closed_mesh_request;
+int xgpu_closed_cell_mesh_many(int n, const xgpu_closed_mesh_request *req,
+                               int n_threads);
+
+/* Replaces xpsi.cellmesh.integrator_for_time_invariance.integrate
+ * (xpsi/cellmesh/integrator_for_time_invariance.pyx:59-338).  Arguments in
+ * the reference's order: the closed mesh's S = sqrt_numPix parallels of S
+ * cells, its scalar cellArea, srcCellParams[S][S][n_params], ray tables
+ * [S][N_R]; atm_ext 1 (blackbody) or 2 (Num4D, `atmos`); image_order_limit
+ * 0 for the reference's None.  flux[N_E] receives the spectrum.  Returns 0,
+ * 1 where the reference returns (ERROR, None), < 0 on a usage or CUDA
+ * failure (including a parallel with more than 8 images). */
+int xgpu_integrate_time_invariant(double R, double omega, double r_s,
+                                  double inclination, size_t sqrt_numPix,
+                                  double cellArea,
+                                  const double *radialCoords_of_parallels,
+                                  const double *r_s_over_r, const double *theta,
+                                  const double *phi, const double *srcCellParams,
+                                  size_t n_params, size_t N_R,
+                                  const double *deflection,
+                                  const double *cos_alpha,
+                                  const double *maxDeflection,
+                                  const double *cos_gammaArray, size_t N_E,
+                                  const double *energies, int atm_ext,
+                                  const xgpu_atmos4d *atmos,
+                                  int image_order_limit, double *flux);
+
+/* Batched form over n_meshes packed closed meshes.  `meshes` is a HOST
+ * array; every other pointer is device memory.  Mesh m owns the packed
+ * parallels [row_off, row_off + S) and cells [cell_off, cell_off + S*S).
+ * flux receives [n_meshes][N_E]; mesh_status[m] gets XGPU_PULSE_FAIL where
+ * the reference would return (ERROR, None) and XGPU_BAD_INPUT for a parallel
+ * with more images than max_images (0: 8). */
+typedef struct {
+  int32_t S, row_off;
+  int64_t cell_off;
+  double omega, inclination, cellArea;
+  int32_t image_order_limit, atm_ext;
+} xgpu_elsewhere_mesh;
+
+typedef struct {
+  const int32_t *row_mesh;
+  const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;
+  const double *deflection, *cos_alpha;
+  const double *phi, *params;
+  int32_t n_params;
+  const double *energies;
+  xgpu_atmos4d atmos; /* device pointers; intensity NULL when no mesh is Num4D */
+  double *flux;
+  int32_t *mesh_status;
+} xgpu_elsewhere_batch_data;
+
+int xgpu_elsewhere_batch(int n_meshes, const xgpu_elsewhere_mesh *meshes,
+                         int64_t n_rows, int N_R, int N_E, int max_images,
+                         const xgpu_elsewhere_batch_data *d, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,7 @@ MODULES = [
     "cellmesh.common_functions", "cellmesh.mesh_tools", "cellmesh.mesh",
     "cellmesh.polar_mesh", "cellmesh.rays", "cellmesh.integrator",
     "cellmesh.integrator_for_azimuthal_invariance",
+    "cellmesh.global_mesh", "cellmesh.integrator_for_time_invariance",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
 ]

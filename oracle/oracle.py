@@ -62,6 +62,11 @@ def lib():
                 C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P,
                 C.c_size_t, P, P, P, P, P, C.c_size_t, P, C.c_size_t, P,
                 C.c_size_t, P, C.c_int, P, C.c_int, P]
+            L.xo_integrate_time_invariant.restype = C.c_int
+            L.xo_integrate_time_invariant.argtypes = [
+                C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                C.c_size_t, C.c_double, P, P, P, P, P, C.c_size_t, C.c_size_t,
+                P, P, P, P, C.c_size_t, P, C.c_int, P, C.c_int, P]
             L.xo_energy_integrator.restype = None
             L.xo_energy_integrator.argtypes = [C.c_int, C.c_size_t, C.c_size_t, P,
                                                P, C.c_size_t, P, P]
@@ -131,6 +136,35 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         _p(par), par.shape[2], _p(rad), int(numRays), _p(arrs[4]), _p(arrs[5]),
         _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
         P.size, _p(P), int(hot_atm_ext),
+        C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
+        int(image_order_limit or 0), _p(out))
+    del keep
+    if status != 0:
+        return (1, None)
+    return (0, out)
+
+
+def integrate_time_invariant(numThreads, R, omega, r_s, inclination, sqrt_numPix,
+                             cellArea, radialCoords_of_parallels, r_s_over_r, theta,
+                             phi, srcCellParams, numRays, deflection, cos_alpha,
+                             maxDeflection, cos_gammaArray, energies, atmosphere,
+                             atm_ext, image_order_limit=None, *args):
+    """integrator_for_time_invariance.integrate (:59-338): the photosphere
+    elsewhere, blackbody (atm_ext 1) or numerical 4-D (2)."""
+    if int(atm_ext) not in (1, 2):
+        raise NotImplementedError("oracle covers atm_ext 1 and 2")
+    S = int(sqrt_numPix)
+    par = _c(srcCellParams)
+    E = _c(energies)
+    out = np.zeros(E.size)
+    st, keep = _atmos_struct(atmosphere if int(atm_ext) == 2 else ())
+    arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
+            _c(deflection), _c(cos_alpha), _c(maxDeflection), _c(cos_gammaArray)]
+    status = lib().xo_integrate_time_invariant(
+        int(numThreads), float(R), float(omega), float(r_s), float(inclination), S,
+        float(cellArea), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]), _p(par),
+        par.shape[2], int(numRays), _p(arrs[4]), _p(arrs[5]), _p(arrs[6]), _p(arrs[7]),
+        E.size, _p(E), int(atm_ext),
         C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
         int(image_order_limit or 0), _p(out))
     del keep

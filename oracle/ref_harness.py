@@ -12,8 +12,9 @@ subset.  Only the pieces the likelihood path needs are loaded:
   are stubbed: they are not on the path;
 * numpy 2 removed `numpy.infty`, which the reference evaluates in two
   constructors; it is aliased to `numpy.inf`;
-* modules for Stokes and time-invariant integrators are stubbed, since the
-  model classes import them at construction but the path never calls them.
+* modules for Stokes integrators (and the closed mesh / time-invariant
+  integrator, when they were not built) are stubbed, since the model classes
+  import them at construction but the path never calls them.
 
 Available only where the reference checkout exists (not on the GPU host).
 """
@@ -21,6 +22,7 @@ import importlib
 import importlib.util
 import os
 import sys
+import sysconfig
 import types
 
 import numpy as np
@@ -121,10 +123,13 @@ def load():
     _package("xpsi.cellmesh", ("xpsi", "cellmesh"))
     _package("xpsi.likelihoods", ("xpsi", "likelihoods"))
 
+    suffix = sysconfig.get_config_var("EXT_SUFFIX")
     for name in ("integratorIQU_for_azimuthal_invariance", "integratorIQU",
                  "integrator_for_azimuthal_invariance_split",
                  "integratorIQU_for_azimuthal_invariance_split",
                  "global_mesh", "integrator_for_time_invariance"):
+        if os.path.exists(os.path.join(BUILT, "xpsi", "cellmesh", name + suffix)):
+            continue
         _stub("xpsi.cellmesh." + name, integrate=None,
               construct_closed_cellMesh=None)
     _stub("xpsi.shell_interpolator", Temp_Interpolator_shells=None)

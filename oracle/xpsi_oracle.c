@@ -14,6 +14,7 @@
  *   xo_compute_rays          cellmesh/rays.pyx:249-390 (+ rayIntegrator :90-247)
  *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665
  *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
+ *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
  *   xo_precomputation        likelihoods/default_background_marginalisation.pyx:38-68
  *   xo_eval_marginal_likelihood   same file :176-734 and
@@ -555,6 +556,152 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
       for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_E * N_P + p * N_P + k];
       flux[p * N_P + k] = s / (energies[p] * kKeV);
     }
+  free(priv); free(cos_defl); free(ca_alt);
+  return terminate_any ? 1 : 0;
+}
+
+/* ================================================================== */
+/* time-invariant integrator (the photosphere elsewhere):             */
+/* cellmesh/integrator_for_time_invariance.pyx:59-338                 */
+/* flux[N_E]; cellArea is the closed mesh's one cell area             */
+/* ================================================================== */
+int xo_integrate_time_invariant(int n_threads, double R, double omega,
+                                double r_s, double inclination, size_t S,
+                                double cellArea, const double *radius_arr,
+                                const double *u_arr, const double *theta,
+                                const double *phi, const double *srcCellParams,
+                                size_t n_params, size_t N_R,
+                                const double *deflection,
+                                const double *cos_alpha,
+                                const double *maxDeflection,
+                                const double *cos_gammaArray, size_t N_E,
+                                const double *energies, int atm_ext,
+                                const xo_atmos4d *atmos, int image_order_limit,
+                                double *flux) {
+  (void)R;
+  (void)r_s;
+  const double sin_i = sin(inclination), cos_i = cos(inclination);
+  /* elsewhere_wrapper.pyx:84-96 -> hot_BB.pyx:84-98, hot_Num4D.pyx:441-461 */
+  const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
+  int nt = n_threads > 0 ? n_threads : 1;
+  int terminate_any = 0;
+  double *priv = (double *)calloc((size_t)nt * N_E, sizeof(double));
+  /* :151-164 */
+  double *cos_defl = (double *)malloc(S * N_R * sizeof(double));
+  double *ca_alt = (double *)malloc(S * N_R * sizeof(double));
+  for (size_t i = 0; i < S; i++)
+    for (size_t j = 0; j < N_R; j++) {
+      cos_defl[i * N_R + j] = cos(deflection[i * N_R + N_R - j - 1]);
+      ca_alt[i * N_R + j] = cos_alpha[i * N_R + N_R - j - 1];
+    }
+  gsl_error_handler_t *prev = gsl_set_error_handler_off();
+
+#pragma omp parallel num_threads(nt) reduction(| : terminate_any)
+  {
+    int T = 0;
+#ifdef _OPENMP
+    T = omp_get_thread_num();
+#endif
+    double *pflux = priv + (size_t)T * N_E;
+    gsl_interp_accel *acc_a = gsl_interp_accel_alloc(), *acc_alt = gsl_interp_accel_alloc();
+    gsl_interp *ia = gsl_interp_alloc(gsl_interp_steffen, N_R);
+    num4d_state nst;
+    if (atm_ext == 2) num4d_reset(&nst, atmos);
+    int terminate = 0;
+#pragma omp for schedule(static, 1)
+    for (long ii = 0; ii < (long)S; ii++) {
+      size_t i = (size_t)ii, j;
+      if (terminate) continue;
+      const double *defl = deflection + i * N_R;
+      const double *ya = cos_alpha + i * N_R;
+      gsl_interp_accel_reset(acc_a);
+      j = 0;
+      while (defl[j] <= kHalfPi) j++;
+      const double *xalt = cos_defl + i * N_R + (N_R - j - 1);
+      const double *yalt = ca_alt + i * N_R + (N_R - j - 1);
+      gsl_interp *ialt = gsl_interp_alloc(gsl_interp_steffen, j + 1);
+      gsl_interp_init(ialt, xalt, yalt, j + 1);
+      gsl_interp_accel_reset(acc_alt);
+      gsl_interp_init(ia, defl, ya, N_R);
+
+      double radius = radius_arr[i];
+      double Grav_z = sqrt(1.0 - u_arr[i]);
+      double cos_gamma = cos_gammaArray[i];
+      double sin_gamma = sqrt(1.0 - cos_gamma * cos_gamma);
+      double cos_th = cos(theta[i * S]), sin_th = sin(theta[i * S]);
+      double th_over_pi = theta[i * S] / kPi;
+      double beta = radius * omega * sin_th / (kC * Grav_z);
+      double Lorentz = sqrt(1.0 - beta * beta);
+      for (j = 0; j < S && !terminate; j++) {
+        double ph = phi[i * S + j];
+        double c_psi0 = cos_i * cos_th + sin_i * sin_th * cos(ph);
+        double psi0 = acos(c_psi0);
+        int IO = image_order_limit > 0 ? image_order_limit
+                                       : (int)ceil(maxDeflection[i] / kPi);
+        for (int I = 0; I < IO; I++) {
+          double cos_psi = c_psi0;
+          double psi = image_deflection(I, psi0);
+          double sin_psi = sin(psi);
+          if (!are_equal(psi, 0.0) && are_equal(sin_psi, 0.0)) { /* :231-244 */
+            double _i = (cos_i >= 0.0) ? inclination + inclination * 1.0e-6
+                                       : inclination - inclination * 1.0e-6;
+            cos_psi = cos(_i) * cos_th + sin(_i) * sin_th * cos(ph);
+            psi = image_deflection(I, acos(cos_psi));
+            sin_psi = sin(psi);
+          }
+          if (psi > maxDeflection[i]) break; /* :246-247 */
+          if (psi < ia->xmin || psi > ia->xmax) { terminate = 1; break; }
+          int use_alt = (psi <= kHalfPi && cos_psi >= ialt->xmin);
+          double cos_a = use_alt ? gsl_interp_eval(ialt, xalt, yalt, cos_psi, acc_alt)
+                                 : gsl_interp_eval(ia, defl, ya, psi, acc_a);
+          double sin_alpha = sqrt(1.0 - cos_a * cos_a);
+          double mu = cos_a * cos_gamma;
+          if (!are_equal(psi, 0.0)) {
+            double cos_delta = (cos_i - cos_th * cos_psi) / (sin_th * sin_psi);
+            if (th_over_pi < 0.5) mu = mu + sin_alpha * sin_gamma * cos_delta;
+            else mu = mu - sin_alpha * sin_gamma * cos_delta;
+          }
+          if (!(mu > 0.0)) continue; /* :275 */
+          double superlum, eta;
+          if (!are_equal(sin_psi, 0.0)) {
+            double cos_xi = sin_alpha * sin_i * sin(ph) / sin_psi;
+            superlum = 1.0 + beta * cos_xi;
+            eta = Lorentz / superlum;
+          } else {
+            eta = Lorentz;
+          }
+          double deriv;
+          if (use_alt) {
+            deriv = gsl_interp_eval_deriv(ialt, xalt, yalt, cos_psi, acc_alt);
+          } else {
+            deriv = gsl_interp_eval_deriv(ia, defl, ya, psi, acc_a);
+            deriv = exp(log(fabs(deriv)) - log(fabs(sin_psi)));
+          }
+          double Z = eta * Grav_z;
+          double ABB = mu * eta;
+          double GEOM = mu * fabs(deriv) * Grav_z * eta * eta * eta;
+          const double *VEC = srcCellParams + (i * S + j) * n_params;
+          for (size_t e = 0; e < N_E; e++) {
+            double Ep = energies[e] / Z;
+            double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
+                                        : eval_bb(Ep, VEC);
+            pflux[e] += I_E * GEOM;
+          }
+        }
+      }
+      gsl_interp_free(ialt);
+    }
+    if (terminate) terminate_any = 1;
+    gsl_interp_free(ia);
+    gsl_interp_accel_free(acc_a); gsl_interp_accel_free(acc_alt);
+  }
+  gsl_set_error_handler(prev);
+  /* :318-323 */
+  for (size_t e = 0; e < N_E; e++) {
+    double s = 0.0;
+    for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_E + e];
+    flux[e] = s * (cellArea * norm / (energies[e] * kKeV));
+  }
   free(priv); free(cos_defl); free(ca_alt);
   return terminate_any ? 1 : 0;
 }

@@ -43,3 +43,41 @@ def row_rel(a, b):
 
 def atmos_of(f):
     return (f["atm_logT"], f["atm_logg"], f["atm_mu"], f["atm_logE"], f["atm_I"])
+
+
+def spectrum_rel(a, b):
+    """max |a-b| / |b| over the energies where b != 0 (where b == 0 the
+    value must be 0 too, else inf)."""
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    nz = b != 0
+    if np.any(a[~nz] != 0):
+        return float("inf")
+    return float(np.max(np.abs(a[nz] / b[nz] - 1.0))) if nz.any() else 0.0
+
+
+# the photosphere-elsewhere fixture's cases: (parameter key, atm_ext, table)
+ELSEWHERE_CASES = ("bb", "num4d", "num4d_mu09")
+
+
+def elsewhere_atmos(golden, case):
+    """The atmosphere argument of an elsewhere fixture case: () for the
+    blackbody, else the numerical table num4d_omit.npz stores (for
+    num4d_mu09 on a mu grid scaled to [0, 0.9])."""
+    if case == "bb":
+        return ()
+    t = atmos_of(golden("num4d_omit"))
+    if case == "num4d_mu09":
+        t = (t[0], t[1], np.ascontiguousarray(0.9 * t[2]), t[3], t[4])
+    return t
+
+
+def elsewhere_args(f, case, atmos, threads=1, image_order_limit=None, inclination=None,
+                   omega=None):
+    """Arguments of integrator_for_time_invariance.integrate for a fixture case."""
+    return (threads, float(f["R"]), float(f["Omega"] if omega is None else omega),
+            float(f["r_s"]), float(f["inclination"] if inclination is None else inclination),
+            int(f["S"]), float(f["cellArea"]), f["radius"], f["u"], f["theta"], f["phi"],
+            f[("num4d" if case != "bb" else "bb") + "_params"], int(f["N_R"]),
+            f["deflection"], f["cos_alpha"], f["maxDeflection"], f["cos_gamma"],
+            f["energies"], atmos, 1 if case == "bb" else 2, image_order_limit)

@@ -12,6 +12,9 @@ Cases
   num4d_omit     a spot with an omitted (crescent) region and a small seeded
                  numerical 4-D atmosphere; fast spin so that mu*eta > 1 and the
                  reference's history-dependent clamp is exercised.
+  elsewhere      the photosphere elsewhere: closed mesh, rays and the
+                 time-invariant integrator, blackbody and numerical 4-D, with
+                 1 and 4 threads.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -215,11 +218,74 @@ def config1(xpsi):
          support=support, logL=ml[0], star=ml[1], mcl_bg=ml[2], mcl_bg_s=ml[3])
 
 
+def closed_mesh(xpsi, *, M_sun, R_km, f_hz, sqrt_num_cells, N_R, star_shape_ind=0):
+    """Closed mesh and rays of the photosphere elsewhere via the reference's
+    own functions, with the glue Elsewhere applies (Elsewhere.py:254-303)."""
+    from xpsi.global_imports import _GM, _csq, _G, _km, _2pi
+    from xpsi.cellmesh.global_mesh import construct_closed_cellMesh
+    from xpsi.cellmesh.rays import compute_rays
+    r_g = M_sun * _GM
+    r_s = 2.0 * r_g
+    R = R_km * _km
+    Mkg = M_sun * _GM * _csq / _G
+    Omega = _2pi * f_hz
+    zeta = r_g / R
+    eps = Omega ** 2.0 * R ** 3.0 / (_G * Mkg)
+    S = int(sqrt_num_cells)
+    th, ph, r, cA, maxA, cg, g = construct_closed_cellMesh(1, S, S * S, Mkg, r_s, R, zeta, eps,
+                                                           star_shape_ind)
+    u = np.ascontiguousarray(r_s / r)
+    ma_in = np.array(maxA, copy=True)
+    ma = ma_in.copy()
+    t, D, CA, L, MD = compute_rays(1, S, r_s, u, ma, N_R)
+    assert t == 0
+    return dict(mass=Mkg, R=R, Omega=Omega, r_s=r_s, zeta=zeta, epsilon=eps,
+                star_shape_ind=star_shape_ind, S=S, theta=th, phi=ph, radius=r,
+                cellArea=cA, maxAlpha_in=ma_in, rays_maxAlpha_out=ma, cos_gamma=cg,
+                effGrav=g, u=u, deflection=D, cos_alpha=CA, maxDeflection=MD, N_R=N_R)
+
+
+def elsewhere(xpsi):
+    """The photosphere elsewhere: closed mesh, rays and the time-invariant
+    integrator (integrator_for_time_invariance.pyx:59-338) for a blackbody
+    and for the small numerical 4-D table, at 600 Hz so that mu * eta > 1
+    on the approaching limb (the Num4D clamp history)."""
+    from xpsi.cellmesh.integrator_for_time_invariance import integrate
+    m = closed_mesh(xpsi, M_sun=1.6, R_km=14.0, f_hz=600.0, sqrt_num_cells=24, N_R=256)
+    S = m["S"]
+    E = np.logspace(-1.0, 1.0, 48)
+    inclination = math.acos(0.55)
+    out = {}
+    # the numerical 4-D table num4d_omit.npz stores (not duplicated here)
+    ref = np.load(os.path.join(HERE, "num4d_omit.npz"))
+    atm = tuple(np.ascontiguousarray(ref[k]) for k in
+                ("atm_logT", "atm_logg", "atm_mu", "atm_logE", "atm_I"))
+    # the same table on a mu grid that tops out at 0.9, so that many queries
+    # lie above it and the evaluator's clamp history decides their value
+    atm09 = (atm[0], atm[1], np.ascontiguousarray(0.9 * atm[2]), atm[3], atm[4])
+    for tag, logT, ext, atmos in (("bb", 6.0, 1, ()), ("num4d", 6.1, 2, atm),
+                                  ("num4d_mu09", 6.1, 2, atm09)):
+        params = np.ones((S, S, 2))
+        params[..., :-1] *= logT
+        for j in range(S):
+            params[:, j, -1] *= m["effGrav"]
+        for nt in (1, 4):
+            st, flux = integrate(nt, m["R"], m["Omega"], m["r_s"], inclination, S,
+                                 m["cellArea"], m["radius"], m["u"], m["theta"], m["phi"],
+                                 params, m["N_R"], m["deflection"], m["cos_alpha"],
+                                 m["maxDeflection"], m["cos_gamma"], E, atmos, ext, None)
+            assert st == 0
+            out["%s_flux_threads%d" % (tag, nt)] = flux
+        out[tag + "_params"] = params
+    save("elsewhere", **m, inclination=inclination, energies=E, **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
     num4d_omit(xpsi)
     config1(xpsi)
+    elsewhere(xpsi)
 
 
 if __name__ == "__main__":

@@ -6,6 +6,8 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
 
     xpsi_gb300.cellmesh.rays.compute_rays
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
+    xpsi_gb300.cellmesh.global_mesh.construct_closed_cellMesh   (elsewhere)
+    xpsi_gb300.cellmesh.integrator_for_time_invariance.integrate (elsewhere)
     xpsi_gb300.tools.energy_integrator.energy_integrator
     xpsi_gb300.likelihoods.default_background_marginalisation.{precomputation,
                                                               eval_marginal_likelihood}
@@ -29,6 +31,7 @@ def install(xpsi_module):
     """
     import importlib
     from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
+    from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
     from .tools import energy_integrator as ei
     from .likelihoods import default_background_marginalisation as dbm
     done = []
@@ -40,6 +43,9 @@ def install(xpsi_module):
          dbm.eval_marginal_likelihood),
         ("xpsi.likelihoods.default_background_marginalisation", "precomputation",
          dbm.precomputation),
+        ("xpsi.cellmesh.global_mesh", "construct_closed_cellMesh",
+         global_mesh.construct_closed_cellMesh),
+        ("xpsi.cellmesh.integrator_for_time_invariance", "integrate", tinv.integrate),
     ]
     for modname, attr, fn in targets:
         try:
@@ -50,8 +56,15 @@ def install(xpsi_module):
         done.append(modname + "." + attr)
     # names bound at import time by the model classes
     for modname, attr, fn in (("xpsi.HotRegion", "_compute_rays", rays.compute_rays),
-                              ("xpsi.Signal", "energy_integrator", ei.energy_integrator)):
-        mod = importlib.import_module(modname)
+                              ("xpsi.Signal", "energy_integrator", ei.energy_integrator),
+                              ("xpsi.Elsewhere", "_compute_rays", rays.compute_rays),
+                              ("xpsi.Elsewhere", "_construct_closed_cellMesh",
+                               global_mesh.construct_closed_cellMesh),
+                              ("xpsi.Elsewhere", "_integrator", tinv.integrate)):
+        try:
+            mod = importlib.import_module(modname)
+        except ImportError:
+            continue
         setattr(mod, attr, fn)
         done.append(modname + "." + attr)
     HotRegion = importlib.import_module("xpsi.HotRegion").HotRegion

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
 UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh",
-         "mesh_gpu"]
+         "mesh_gpu", "elsewhere"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -130,6 +130,25 @@ class MeshBatchOut(C.Structure):
                 ("cellArea", P), ("phi", P), ("params", P), ("radiates", P)]
 
 
+class ClosedMeshRequest(C.Structure):
+    _fields_ = [("S", SZ), ("num_cells", SZ), ("R_eq", D), ("zeta", D), ("epsilon", D),
+                ("star_shape_ind", I32), ("theta", P), ("phi", P), ("r", P),
+                ("cellArea", P), ("maxAlpha", P), ("cos_gamma", P), ("effGrav", P)]
+
+
+class ElsewhereMesh(C.Structure):
+    _fields_ = [("S", I32), ("row_off", I32), ("cell_off", I64), ("omega", D),
+                ("inclination", D), ("cellArea", D), ("image_order_limit", I32),
+                ("atm_ext", I32)]
+
+
+class ElsewhereBatchData(C.Structure):
+    _fields_ = [("row_mesh", P), ("radius", P), ("u", P), ("cos_gamma", P),
+                ("theta0", P), ("maxDeflection", P), ("deflection", P), ("cos_alpha", P),
+                ("phi", P), ("params", P), ("n_params", I32), ("energies", P),
+                ("atmos", Atmos4D), ("flux", P), ("mesh_status", P)]
+
+
 class LikelihoodBatchData(C.Structure):
     _fields_ = [("n_vec", I32), ("K", I32), ("B", I32), ("H", I32), ("N_P", I32),
                 ("exposure", D), ("epsabs", D), ("epsrel", D), ("epsilon", D),
@@ -178,6 +197,15 @@ def _bind(L):
         "xgpu_mesh_batch": (C.c_int, [C.c_int, C.POINTER(MeshMember), I64, I64,
                                       C.POINTER(MeshBatchOut), P]),
         "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
+        "xgpu_closed_cell_mesh": (C.c_int, [SZ, SZ, D, D, D, C.c_int, P, P, P, P, P, P, P]),
+        "xgpu_closed_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(ClosedMeshRequest),
+                                                 C.c_int]),
+        "xgpu_integrate_time_invariant": (C.c_int, [D, D, D, D, SZ, D, P, P, P, P, P, SZ, SZ,
+                                                    P, P, P, P, SZ, P, C.c_int,
+                                                    C.POINTER(Atmos4D), C.c_int, P]),
+        "xgpu_elsewhere_batch": (C.c_int, [C.c_int, C.POINTER(ElsewhereMesh), I64, C.c_int,
+                                           C.c_int, C.c_int, C.POINTER(ElsewhereBatchData),
+                                           P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -192,7 +220,9 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_energy_batch", "xgpu_fold_batch", "xgpu_likelihood_batch",
             "xgpu_allocate_cells", "xgpu_cell_mesh", "xgpu_cell_mesh_many", "xgpu_peak_probe",
             "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed",
-            "xgpu_fold_batch_tc", "xgpu_mesh_batch", "xgpu_allocate_cells_many"]
+            "xgpu_fold_batch_tc", "xgpu_mesh_batch", "xgpu_allocate_cells_many",
+            "xgpu_closed_cell_mesh", "xgpu_closed_cell_mesh_many",
+            "xgpu_integrate_time_invariant", "xgpu_elsewhere_batch"]
 
 
 def lib():

@@ -563,4 +563,123 @@ int xgpu_eval_marginal_likelihood(double exposure_time, size_t B, const double *
   return status;
 }
 
+// ------------------------------------------------------------ elsewhere
+int xgpu_elsewhere_batch(int n_meshes, const xgpu_elsewhere_mesh *meshes, int64_t n_rows,
+                         int N_R, int N_E, int max_images, const xgpu_elsewhere_batch_data *d,
+                         void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_meshes <= 0) return 0;
+  if (N_R < 3) return fail_msg("num_rays must be at least 3");
+  if (N_E < 1) return fail_msg("at least one energy is needed");
+  if (max_images <= 0) max_images = 8;
+  int max_S = 0;
+  int64_t rows = 0;
+  for (int m = 0; m < n_meshes; m++) {
+    const xgpu_elsewhere_mesh &M = meshes[m];
+    if (M.atm_ext != 1 && M.atm_ext != 2) return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+    if (M.atm_ext == 2 && d->atmos.intensity == nullptr)
+      return fail_msg("a Num4D mesh needs the atmosphere table");
+    if (M.atm_ext == 2 && (d->atmos.nT < 4 || d->atmos.ng < 4 || d->atmos.nmu < 4 ||
+                           d->atmos.nE < 4))
+      return fail_msg("Num4D grids need at least 4 nodes per dimension");
+    if (M.atm_ext == 2 && d->n_params < 2)
+      return fail_msg("Num4D needs (log T, log g) per cell");
+    if (M.S < 1 || M.row_off < 0 || M.row_off + M.S > n_rows)
+      return fail_msg("closed mesh rows outside the packed parallels");
+    max_S = std::max(max_S, (int)M.S);
+    rows += M.S;
+  }
+  if (n_rows > INT32_MAX) return fail_msg("too many parallels in one launch");
+  if (xg::elsewhere_smem_bytes(N_R, max_S, max_images) > 227 * 1024)
+    return fail_msg("closed mesh too large for one CTA's shared memory");
+  Dev dm, drow;
+  int rc;
+  static_assert(sizeof(xgpu_elsewhere_mesh) == sizeof(xg::ElseMeshDesc), "elsewhere layout");
+  if ((rc = upload(dm, reinterpret_cast<const xg::ElseMeshDesc *>(meshes), n_meshes, st)))
+    return rc;
+  if ((rc = dalloc(drow, (size_t)n_rows * N_E * sizeof(double), st))) return rc;
+  CK(cudaMemsetAsync(drow.p, 0, (size_t)n_rows * N_E * sizeof(double), st));
+  CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
+  xg::ElsewhereArgs a{};
+  a.n_meshes = n_meshes;
+  a.n_rows = n_rows;
+  a.N_R = N_R;
+  a.N_E = N_E;
+  a.max_S = max_S;
+  a.max_images = max_images;
+  a.meshes = dm.as<xg::ElseMeshDesc>();
+  a.row_mesh = d->row_mesh;
+  a.radius = d->radius; a.u = d->u; a.cos_gamma = d->cos_gamma; a.theta0 = d->theta0;
+  a.maxDeflection = d->maxDeflection;
+  a.deflection = d->deflection; a.cos_alpha = d->cos_alpha;
+  a.phi = d->phi; a.params = d->params; a.n_params = d->n_params;
+  a.energies = d->energies;
+  a.atmos = xg::Atmos4D{d->atmos.logT, d->atmos.logg, d->atmos.mu, d->atmos.logE,
+                        d->atmos.intensity, (int)d->atmos.nT, (int)d->atmos.ng,
+                        (int)d->atmos.nmu, (int)d->atmos.nE, nullptr};
+  a.row_flux = drow.as<double>();
+  a.flux = d->flux;
+  a.status = d->mesh_status;
+  rc = xg::launch_elsewhere(a, st);
+  if (rc == -2) return fail_msg("closed mesh too large for one CTA's shared memory");
+  CK(cudaGetLastError());
+  return rc;
+}
+
+int xgpu_integrate_time_invariant(double R, double omega, double r_s, double inclination,
+                                  size_t S, double cellArea, const double *radius,
+                                  const double *r_s_over_r, const double *theta,
+                                  const double *phi, const double *srcCellParams,
+                                  size_t n_params, size_t N_R, const double *deflection,
+                                  const double *cos_alpha, const double *maxDeflection,
+                                  const double *cos_gamma, size_t N_E, const double *energies,
+                                  int atm_ext, const xgpu_atmos4d *atmos, int image_order_limit,
+                                  double *flux) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (S == 0 || N_E == 0) return 0;
+  if (n_params < 1) return fail_msg("srcCellParams needs at least 1 parameter per cell");
+  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
+  xg::Atmos4D A{};
+  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  const size_t cells = S * S;
+  std::vector<double> theta0(S);
+  for (size_t i = 0; i < S; i++) theta0[i] = theta[i * S];
+  std::vector<int32_t> row_mesh(S, 0);
+  Dev drad, du, dth0, dphi, dpar, dD, dCA, dMD, dcg, dE, dF, dst, drm;
+  if ((rc = upload(drad, radius, S, st)) || (rc = upload(du, r_s_over_r, S, st)) ||
+      (rc = upload(dth0, theta0.data(), S, st)) || (rc = upload(dphi, phi, cells, st)) ||
+      (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
+      (rc = upload(dD, deflection, S * N_R, st)) || (rc = upload(dCA, cos_alpha, S * N_R, st)) ||
+      (rc = upload(dMD, maxDeflection, S, st)) || (rc = upload(dcg, cos_gamma, S, st)) ||
+      (rc = upload(dE, energies, N_E, st)) || (rc = dalloc(dF, N_E * 8, st)) ||
+      (rc = dalloc(dst, 16, st)) || (rc = upload(drm, row_mesh.data(), S, st)))
+    return rc;
+  xgpu_elsewhere_mesh mesh{(int32_t)S, 0, 0, omega, inclination, cellArea, image_order_limit,
+                           atm_ext};
+  xgpu_elsewhere_batch_data d{};
+  d.row_mesh = drm.as<int32_t>();
+  d.radius = drad.as<double>(); d.u = du.as<double>(); d.cos_gamma = dcg.as<double>();
+  d.theta0 = dth0.as<double>(); d.maxDeflection = dMD.as<double>();
+  d.deflection = dD.as<double>(); d.cos_alpha = dCA.as<double>();
+  d.phi = dphi.as<double>(); d.params = dpar.as<double>(); d.n_params = (int32_t)n_params;
+  d.energies = dE.as<double>();
+  if (atm_ext == 2)
+    d.atmos = xgpu_atmos4d{A.logT, A.logg, A.mu, A.logE, A.I, (size_t)A.nT, (size_t)A.ng,
+                           (size_t)A.nmu, (size_t)A.nE, nullptr};
+  d.flux = dF.as<double>();
+  d.mesh_status = dst.as<int32_t>();
+  rc = xgpu_elsewhere_batch(1, &mesh, (int64_t)S, (int)N_R, (int)N_E, 0, &d, st);
+  if (rc) return rc;
+  int32_t status = 0;
+  CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux, dF.p, N_E * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (status == XGPU_BAD_INPUT) return fail_msg("a parallel has more than 8 images");
+  return status != 0 ? 1 : 0;
+}
+
 }  // extern "C"

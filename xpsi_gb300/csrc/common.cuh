@@ -105,6 +105,74 @@ __device__ __forceinline__ double cubic_deriv(const Cubic &c, double v) {
   return c.k1 + t * (2.0 * c.k2 + 3.0 * c.k3 * t);
 }
 
+// Views of one parallel's ray tables for the Steffen evaluations of the
+// integrators: the main table (deflection -> cos alpha or lag) and the
+// reversed table on cos(deflection) over the rays up to the first deflection
+// above pi/2 (integrator_for_azimuthal_invariance.pyx:209-227,
+// integrator_for_time_invariance.pyx:151-164,206-213).
+struct MainX { const double *D; __device__ double operator()(int j) const { return D[j]; } };
+struct ArrY { const double *Y; __device__ double operator()(int j) const { return Y[j]; } };
+struct AltX {
+  const double *D; int jalt;
+  __device__ double operator()(int t) const { return cos(D[jalt - t]); }
+};
+struct AltY {
+  const double *Y; int jalt;
+  __device__ double operator()(int t) const { return Y[jalt - t]; }
+};
+
+template <typename XF>
+__device__ __forceinline__ int locate_f(const XF &x, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (x(mid) > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+template <typename XF, typename YF>
+__device__ __forceinline__ void steffen_eval(const XF &x, const YF &y, int n, double v,
+                                             double *val, double *der) {
+  int i = locate_f(x, n, v);
+  Cubic c = steffen_piece(x, y, n, i);
+  if (val) *val = cubic_eval(c, v);
+  if (der) *der = cubic_deriv(c, v);
+}
+
+// hot_BB.pyx:54-82 with kT = k_B 10^logT / keV formed once by the caller
+__device__ __forceinline__ double eval_bb(double E, double kT) {
+  return E * E * E / (exp(E / kT) - 1.0);
+}
+
+// 4-point Lagrange stencils of the Num4D atmosphere (hot_Num4D.pyx:248-439):
+// the base node for a query inside the grid (the node the reference's cached
+// walk lands on) and the stencil weights in the reference's operation order.
+__device__ __forceinline__ int stencil_base(const double *g, int n, double v) {
+  // base node of the 4-point stencil around the interval holding v
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (g[mid] > v) hi = mid; else lo = mid;
+  }
+  int b = lo - 1;
+  if (b < 0) b = 0;
+  if (b > n - 4) b = n - 4;
+  return b;
+}
+
+__device__ __forceinline__ void lagrange4(const double *P, int b, double x, double w[4]) {
+  double d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
+  double d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
+  double d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
+  double s0 = 1.0 / (P[b] - P[b + 1]); s0 /= P[b] - P[b + 2]; s0 /= P[b] - P[b + 3];
+  double s1 = 1.0 / (P[b + 1] - P[b]); s1 /= P[b + 1] - P[b + 2]; s1 /= P[b + 1] - P[b + 3];
+  double s2 = 1.0 / (P[b + 2] - P[b]); s2 /= P[b + 2] - P[b + 1]; s2 /= P[b + 2] - P[b + 3];
+  double s3 = 1.0 / (P[b + 3] - P[b]); s3 /= P[b + 3] - P[b + 1]; s3 /= P[b + 3] - P[b + 2];
+  w[0] = d0 * s0; w[1] = d1 * s1; w[2] = d2 * s2; w[3] = d3 * s3;
+}
+
 // exact integral of a cubic piece over [x0 + u, x0 + w]
 __host__ __device__ __forceinline__ double piece_integral(double y0, double k1, double k2,
                                                           double k3, double u, double w) {

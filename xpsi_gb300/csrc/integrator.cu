@@ -72,36 +72,6 @@ struct GeoSmem {
 };
 
 
-struct MainX { const double *D; __device__ double operator()(int j) const { return D[j]; } };
-struct ArrY { const double *Y; __device__ double operator()(int j) const { return Y[j]; } };
-struct AltX {
-  const double *D; int jalt;
-  __device__ double operator()(int t) const { return cos(D[jalt - t]); }
-};
-struct AltY {
-  const double *Y; int jalt;
-  __device__ double operator()(int t) const { return Y[jalt - t]; }
-};
-
-template <typename XF>
-__device__ __forceinline__ int locate_f(const XF &x, int n, double v) {
-  int lo = 0, hi = n - 1;
-  while (hi > lo + 1) {
-    int mid = (lo + hi) >> 1;
-    if (x(mid) > v) hi = mid; else lo = mid;
-  }
-  return lo;
-}
-
-template <typename XF, typename YF>
-__device__ __forceinline__ void steffen_eval(const XF &x, const YF &y, int n, double v,
-                                             double *val, double *der) {
-  int i = locate_f(x, n, v);
-  Cubic c = steffen_piece(x, y, n, i);
-  if (val) *val = cubic_eval(c, v);
-  if (der) *der = cubic_deriv(c, v);
-}
-
 // per-leaf geometry, integrator_for_azimuthal_invariance.pyx:342-441
 __device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_lim,
                               const double *leaves, GeoSmem &g) {
@@ -311,36 +281,7 @@ __device__ void stage_deflection(RowCtx &c, GeoSmem &g, int *s_jalt) {
   __syncthreads();
 }
 
-// hot_BB.pyx:54-82; kT = k_B 10^logT / keV is the same for every call of a
-// parallel and is computed once per parallel
-__device__ __forceinline__ double eval_bb(double E, double kT) {
-  return E * E * E / (exp(E / kT) - 1.0);
-}
 
-__device__ __forceinline__ int stencil_base(const double *g, int n, double v) {
-  // base node of the 4-point stencil around the interval holding v
-  int lo = 0, hi = n - 1;
-  while (hi > lo + 1) {
-    int mid = (lo + hi) >> 1;
-    if (g[mid] > v) hi = mid; else lo = mid;
-  }
-  int b = lo - 1;
-  if (b < 0) b = 0;
-  if (b > n - 4) b = n - 4;
-  return b;
-}
-
-__device__ __forceinline__ void lagrange4(const double *P, int b, double x, double w[4]) {
-  double d0 = (x - P[b + 1]) * (x - P[b + 2]) * (x - P[b + 3]);
-  double d1 = (x - P[b]) * (x - P[b + 2]) * (x - P[b + 3]);
-  double d2 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 3]);
-  double d3 = (x - P[b]) * (x - P[b + 1]) * (x - P[b + 2]);
-  double s0 = 1.0 / (P[b] - P[b + 1]); s0 /= P[b] - P[b + 2]; s0 /= P[b] - P[b + 3];
-  double s1 = 1.0 / (P[b + 1] - P[b]); s1 /= P[b + 1] - P[b + 2]; s1 /= P[b + 1] - P[b + 3];
-  double s2 = 1.0 / (P[b + 2] - P[b]); s2 /= P[b + 2] - P[b + 1]; s2 /= P[b + 2] - P[b + 3];
-  double s3 = 1.0 / (P[b + 3] - P[b]); s3 /= P[b + 3] - P[b + 1]; s3 /= P[b + 3] - P[b + 2];
-  w[0] = d0 * s0; w[1] = d1 * s1; w[2] = d2 * s2; w[3] = d3 * s3;
-}
 
 struct AtmSmem {
   double *gmu, *gE;      // grids of mu and log10(E/kT)
@@ -767,14 +708,7 @@ struct AreaDF {
   }
 };
 
-// the reference adds an interpolant value when it is > 0 (:593-594).  FP64:
-// tested on the high word (integer pipe): positive normal numbers pass; NaN,
-// infinities and positive subnormals (< 2.3e-308, no measurable
-// contribution) do not.
-__device__ __forceinline__ bool positive(double v) {
-  const int hi = __double2hiint(v);
-  return hi >= 0x00100000 && hi < 0x7ff00000;
-}
+// the reference adds an interpolant value when it is > 0 (:593-594)
 __device__ __forceinline__ bool positive(float v) { return v > 0.0f; }
 
 // sums over the radiating cells of one parallel at one signal phase for the

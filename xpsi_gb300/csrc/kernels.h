@@ -133,4 +133,35 @@ struct LikeArgs {
 void launch_likelihood(const LikeArgs &a, cudaStream_t st);
 void launch_precomputation(int K, int B, const int32_t *counts, double *out, cudaStream_t st);
 
+// ---- the photosphere elsewhere (time-invariant integrator) --------------------
+struct ElseMeshDesc {
+  int32_t S;                  // parallels = cells per parallel (closed mesh)
+  int32_t row_off;            // first packed parallel
+  int64_t cell_off;           // first packed cell ([S][S] from here)
+  double omega, inclination, cellArea;
+  int32_t image_order_limit;  // 0: ceil(maxDeflection / pi) per parallel
+  int32_t atm_ext;            // 1 blackbody, 2 Num4D
+};
+struct ElsewhereArgs {
+  int n_meshes;
+  int64_t n_rows;
+  int N_R, N_E;
+  int max_S;                  // largest S of the launch
+  int max_images;             // images held per cell (parallels needing more report kBadInput)
+  const ElseMeshDesc *meshes;
+  const int32_t *row_mesh;    // [n_rows]
+  const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;  // [n_rows]
+  const double *deflection, *cos_alpha;                           // [n_rows][N_R]
+  const double *phi;          // [cells]
+  const double *params;       // [cells][n_params]
+  int n_params;
+  const double *energies;     // [N_E]
+  Atmos4D atmos;
+  double *row_flux;           // [n_rows][N_E] scratch
+  double *flux;               // [n_meshes][N_E]
+  int32_t *status;            // [n_meshes], zeroed by the caller
+};
+size_t elsewhere_smem_bytes(int N_R, int max_S, int max_images);
+int launch_elsewhere(const ElsewhereArgs &a, cudaStream_t st);
+
 }  // namespace xg

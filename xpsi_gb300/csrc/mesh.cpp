@@ -1,7 +1,9 @@
-// mesh.cpp -- host-side hot-region cell meshes: the cell budget
-// (xpsi/cellmesh/mesh_tools.pyx:892-1099, allocate_cells) and the spot /
-// polar-cap meshes (xpsi/cellmesh/mesh.pyx:23-417, polar_mesh.pyx:23-430),
-// built from the shared steps of mesh_math.h.  Meshes of many parameter
+// mesh.cpp -- host-side cell meshes: the cell budget
+// (xpsi/cellmesh/mesh_tools.pyx:892-1099, allocate_cells), the hot-region
+// spot / polar-cap meshes (xpsi/cellmesh/mesh.pyx:23-417,
+// polar_mesh.pyx:23-430) and the closed mesh of the photosphere elsewhere
+// (xpsi/cellmesh/global_mesh.pyx:21-137), built from the shared steps of
+// mesh_math.h.  Meshes of many parameter
 // vectors are built concurrently on the host's cores (one std::thread per
 // slice); mesh_gpu.cu builds the same meshes on the GPU.
 #include <algorithm>
@@ -60,6 +62,59 @@ int build_mesh(bool polar, size_t numCell, size_t S, const Star &s, double cedeR
       o.theta[i * S + j] = pl.invert ? PI - colatC[i] : colatC[i];
       o.phi[i * S + j] = mesh_phi(pl, j);
     }
+  return 0;
+}
+
+// global_mesh.pyx:21-137: the closed mesh of the whole star.  S rows of
+// equal area (the northern S/2 computed, the southern mirrored) by S cells of
+// equal azimuth width; every cell has the same area.
+int build_closed_mesh(size_t S, size_t numCell, const Star &s, double *theta, double *phi,
+                      double *r, double *cellArea_out, double *maxAlpha, double *cos_gamma,
+                      double *effGrav, Work &w) {
+  if (S < 4 || S % 2 != 0 || numCell == 0) return -1;
+  const size_t nc = S / 2;
+  double cellArea = TWO_PI * integrateArea(0.0, PI_2, s, 0, w) / (double)numCell;
+  cellArea *= 2.0;
+  const double eta = cellArea * (double)S / TWO_PI;
+  // np.linspace(pi/2, 0, 1000) and the area from each colatitude to the equator
+  std::vector<double> colat(kAreaTab), areaTab(kAreaTab), parallels(nc - 1), colatC(S);
+  const double step = (0.0 - PI_2) / (double)(kAreaTab - 1);
+  for (int i = 0; i < kAreaTab; i++) {
+    colat[i] = (i == kAreaTab - 1) ? 0.0 : PI_2 + (double)i * step;
+    areaTab[i] = integrateArea(colat[i], PI_2, s, 0, w);
+  }
+  double i_eta = (double)nc * eta;
+  for (size_t i = 0; i + 1 < nc; i++) {
+    i_eta -= eta;
+    parallels[i] = steffen_at(areaTab.data(), colat.data(), kAreaTab, i_eta);
+  }
+  for (size_t i = 0; i < nc; i++) {
+    const double lower = (i == 0) ? 0.0 : parallels[i - 1];
+    const double upper = (i == nc - 1) ? PI_2 : parallels[i];
+    const RowOut o = mesh_row(s, lower, upper, eta, w);
+    colatC[i] = o.colat;
+    r[i] = o.r;
+    effGrav[i] = o.effGrav;
+    cos_gamma[i] = o.cos_gamma;
+    maxAlpha[i] = o.maxAlpha;
+  }
+  for (size_t i = nc; i < S; i++) {
+    colatC[i] = PI - colatC[S - i - 1];
+    r[i] = r[S - i - 1];
+    cos_gamma[i] = cos_gamma[S - i - 1];
+    effGrav[i] = effGrav[S - i - 1];
+    maxAlpha[i] = maxAlpha[S - i - 1];
+  }
+  // np.linspace(-pi + d/2, pi - d/2, S) with d = 2 pi / S, as a meshgrid
+  const double d = TWO_PI / (double)S;
+  const double a = -PI + 0.5 * d, b = PI - 0.5 * d;
+  const double pstep = (b - a) / (double)(S - 1);
+  for (size_t i = 0; i < S; i++)
+    for (size_t j = 0; j < S; j++) {
+      theta[i * S + j] = colatC[i];
+      phi[i * S + j] = (j == S - 1) ? b : a + (double)j * pstep;
+    }
+  *cellArea_out = cellArea;
   return 0;
 }
 
@@ -160,6 +215,38 @@ int xgpu_cell_mesh(int polar, size_t num_cells, size_t S, double R_eq, double ze
   MeshOut o{theta, phi, r, area, maxAlpha, cos_gamma, effGrav};
   return build_mesh(polar != 0, num_cells, S, s, cede_radius, cede_colatitude, super_radius,
                     super_colatitude, super_azimuth, o, *w);
+}
+
+int xgpu_closed_cell_mesh(size_t S, size_t num_cells, double R_eq, double zeta,
+                          double epsilon, int star_shape_ind, double *theta, double *phi,
+                          double *r, double *cellArea, double *maxAlpha, double *cos_gamma,
+                          double *effGrav) {
+  Star s{R_eq, epsilon, zeta, 0.0, star_shape_ind};
+  std::unique_ptr<Work> w(new Work);
+  return build_closed_mesh(S, num_cells, s, theta, phi, r, cellArea, maxAlpha, cos_gamma,
+                           effGrav, *w);
+}
+
+int xgpu_closed_cell_mesh_many(int n, const xgpu_closed_mesh_request *req, int n_threads) {
+  if (n <= 0) return 0;
+  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  n_threads = std::min(n_threads, n);
+  std::vector<std::thread> pool;
+  std::vector<int> rc(n, 0);
+  auto work = [&](int t) {
+    std::unique_ptr<Work> wp(new Work);
+    for (int i = t; i < n; i += n_threads) {
+      const xgpu_closed_mesh_request &q = req[i];
+      Star s{q.R_eq, q.epsilon, q.zeta, 0.0, q.star_shape_ind};
+      rc[i] = build_closed_mesh(q.S, q.num_cells, s, q.theta, q.phi, q.r, q.cellArea,
+                                q.maxAlpha, q.cos_gamma, q.effGrav, *wp);
+    }
+  };
+  for (int t = 0; t < n_threads; t++) pool.emplace_back(work, t);
+  for (auto &th : pool) th.join();
+  for (int i = 0; i < n; i++)
+    if (rc[i]) return rc[i];
+  return 0;
 }
 
 int xgpu_allocate_cells_many(int n, xgpu_alloc_request *req, int n_threads) {
