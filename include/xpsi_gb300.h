@@ -67,23 +67,26 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R,
 
 /* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-98) for uniform
- * hot regions: no correction field, beam_opt 0, no disk (R_in >= 1e6).
- * atm_ext 1 = blackbody, 2 = Num4D (atmos required).  image_order_limit 0
- * means "infer" (the reference's None).  flux[N_E][N_P] is written on
- * success.  Returns 0 (SUCCESS) or 1 (ERROR, :657-665). */
+ * hot regions: beam_opt 0, no disk (R_in >= 1e6).  atm_ext 1 = blackbody,
+ * 2 = Num4D (atmos required).  correction_srcCellParams[S0][S1][n_correction]
+ * or NULL is the elsewhere correction (:257-261,469-478,593-594); the GPU
+ * path corrects for a blackbody elsewhere (else_atm_ext 1).
+ * image_order_limit 0 means "infer" (the reference's None).  flux[N_E][N_P]
+ * is written on success.  Returns 0 (SUCCESS) or 1 (ERROR, :657-665). */
 int xgpu_integrate(double R, double omega, double r_s, double inclination,
                    size_t S0, size_t S1, const double *cellArea,
                    const double *radialCoords_of_parallels,
                    const double *r_s_over_r, const double *theta,
                    const double *phi, const double *srcCellParams,
-                   size_t n_params, const int32_t *cell_radiates, size_t N_R,
-                   const double *deflection, const double *cos_alpha,
-                   const double *lag, const double *maxDeflection,
-                   const double *cos_gammaArray, size_t N_E,
-                   const double *energies, size_t N_L, const double *leaves,
-                   size_t N_P, const double *phases, int atm_ext,
-                   const xgpu_atmos4d *atmos, int image_order_limit,
-                   double *flux);
+                   size_t n_params, const int32_t *cell_radiates,
+                   const double *correction_srcCellParams, size_t n_correction,
+                   size_t N_R, const double *deflection,
+                   const double *cos_alpha, const double *lag,
+                   const double *maxDeflection, const double *cos_gammaArray,
+                   size_t N_E, const double *energies, size_t N_L,
+                   const double *leaves, size_t N_P, const double *phases,
+                   int atm_ext, const xgpu_atmos4d *atmos, int else_atm_ext,
+                   int image_order_limit, double *flux);
 
 /* Replaces xpsi.tools.energy_integrator.energy_integrator
  * (xpsi/tools/energy_integrator.pyx:27-31).  signal[N_E][N_P]; log10 energies
@@ -159,6 +162,10 @@ typedef struct {
   double *flux;
   int32_t *mesh_status;
   double *flop_counter; /* optional: algorithmic FLOPs of the launch are added */
+  /* optional elsewhere correction for every mesh of the launch (FP64 form):
+   * [cells][n_correction], log T of a blackbody elsewhere first; NULL: none */
+  const double *correction;
+  int32_t n_correction;
 } xgpu_integrate_batch_data;
 
 int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows,
@@ -380,7 +387,11 @@ int xgpu_integrate_time_invariant(double R, double omega, double r_s,
  * parallels [row_off, row_off + S) and cells [cell_off, cell_off + S*S).
  * flux receives [n_meshes][N_E]; mesh_status[m] gets XGPU_PULSE_FAIL where
  * the reference would return (ERROR, None) and XGPU_BAD_INPUT for a parallel
- * with more images than max_images (0: 8). */
+ * with more images than max_images (0: 8).  When `signal` is not NULL each
+ * successful mesh's spectrum is also added to every phase column of
+ * signal[m * signal_stride + e * signal_N_P + p] (the time-invariant
+ * component added to the first hot region's signal, Photosphere.py:588-592);
+ * the launch must follow the one that wrote the signal on the stream. */
 typedef struct {
   int32_t S, row_off;
   int64_t cell_off;
@@ -398,6 +409,9 @@ typedef struct {
   xgpu_atmos4d atmos; /* device pointers; intensity NULL when no mesh is Num4D */
   double *flux;
   int32_t *mesh_status;
+  double *signal;            /* optional, see above */
+  int64_t signal_stride;
+  int32_t signal_N_P;
 } xgpu_elsewhere_batch_data;
 
 int xgpu_elsewhere_batch(int n_meshes, const xgpu_elsewhere_mesh *meshes,

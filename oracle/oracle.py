@@ -59,7 +59,7 @@ def lib():
             L.xo_integrate.restype = C.c_int
             L.xo_integrate.argtypes = [
                 C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
-                C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P,
+                C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P, P, C.c_size_t,
                 C.c_size_t, P, P, P, P, P, C.c_size_t, P, C.c_size_t, P,
                 C.c_size_t, P, C.c_int, P, C.c_int, P]
             L.xo_integrate_time_invariant.restype = C.c_int
@@ -118,9 +118,16 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
               phases, hot_atmosphere, elsewhere_atmosphere, hot_atm_ext,
               else_atm_ext, beam_opt, image_order_limit=None, R_in=1e6):
     """integrator_for_azimuthal_invariance.integrate (:70-665) for the
-    uniform BB / Num4D hot regions the likelihood path uses."""
-    if correction_srcCellParams is not None or beam_opt != 0 or R_in < 1e6:
+    uniform BB / Num4D hot regions the likelihood path uses, with the
+    correction for a blackbody elsewhere (else_atm_ext 1) when
+    correction_srcCellParams is given."""
+    if beam_opt != 0 or R_in < 1e6:
         raise NotImplementedError("oracle covers the default hot-region path")
+    corr = None
+    if correction_srcCellParams is not None:
+        if int(else_atm_ext) != 1:
+            raise NotImplementedError("oracle corrects for a blackbody elsewhere only")
+        corr = _c(correction_srcCellParams)
     A = _c(cellArea); S0, S1 = A.shape
     par = _c(srcCellParams)
     rad = _c(CELL_RADIATES, np.int32)
@@ -133,7 +140,8 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     status = lib().xo_integrate(
         int(numThreads), float(R), float(omega), float(r_s), float(inclination),
         S0, S1, _p(A), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
-        _p(par), par.shape[2], _p(rad), int(numRays), _p(arrs[4]), _p(arrs[5]),
+        _p(par), par.shape[2], _p(rad), _p(corr) if corr is not None else None,
+        corr.shape[2] if corr is not None else 0, int(numRays), _p(arrs[4]), _p(arrs[5]),
         _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
         P.size, _p(P), int(hot_atm_ext),
         C.cast(C.pointer(st), C.c_void_p) if st is not None else None,

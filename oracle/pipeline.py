@@ -5,9 +5,12 @@ rays (rays.pyx) -> lag calibration (HotRegion.py:880-901) -> integrator
 (integrator_for_azimuthal_invariance.pyx) -> /d^2 and energy integration
 (Likelihood.py:361-364, energy_integrator.pyx) -> numpy dot fold
 (Instrument.py:192-197) -> background-marginalised likelihood
-(default_background_marginalisation.pyx).
+(default_background_marginalisation.pyx).  With an elsewhere: its rays, the
+time-invariant integrator (integrator_for_time_invariance.pyx), the hot
+regions' correction and the spectrum added to the first hot region's signal
+(Photosphere.py:588-592).
 
-The meshes come from the batched path's host mesh builder (an input here,
+The meshes come from the batched path's host mesh builders (an input here,
 like the data), so this checks every GPU stage."""
 import math
 
@@ -38,8 +41,15 @@ def loglike(model, P, n_threads=1, return_stages=False):
     out = np.zeros(V)
     status = np.zeros(V, dtype=np.int32)
     stages = []
+    else_V = getattr(P, "else_V", 0)
     for v in range(V):
         regs = []
+        spectrum = None
+        if else_V:
+            spectrum, est = _elsewhere(model, P, v, n_threads)
+            if est:
+                status[v] = est
+                continue
         for h in range(H):
             mi = v * H + h
             mesh = P.meshes[mi]
@@ -59,17 +69,20 @@ def loglike(model, P, n_threads=1, return_stages=False):
             L *= P.row["lag_scale"][r0]
             theta = np.repeat(P.row["theta0"][rs][:, None], S, axis=1)
             spec = model.regions[h]
+            corr = P.correction[cs].reshape(S, S, 2) if else_V else None
             st, flux = O.integrate(n_threads, 0.0, mesh.omega, r_s, mesh.inclination,
                                    P.cellArea[cs].reshape(S, S), P.row["radius"][rs], u,
                                    theta, P.phi[cs].reshape(S, S),
                                    P.params[cs].reshape(S, S, 2),
-                                   P.radiates[cs].reshape(S, S), None, N_R, D, CA, L, MD,
+                                   P.radiates[cs].reshape(S, S), corr, N_R, D, CA, L, MD,
                                    P.row["cos_gamma"][rs], model.energies, leaves, phases,
                                    atm if spec.atm_ext == 2 else (), None, spec.atm_ext,
-                                   None, 0, spec.image_order_limit)
+                                   1 if else_V else None, 0, spec.image_order_limit)
             if st:
                 status[v] = 2
                 break
+            if spectrum is not None and h == 0:
+                flux = flux + spectrum[:, None]
             ei = O.energy_integrator(n_threads, flux / P.d_sq[mi], logE, logEd)
             regs.append(np.dot(model.instrument.matrix, ei))
             if return_stages:
@@ -86,3 +99,29 @@ def loglike(model, P, n_threads=1, return_stages=False):
     if P.status is not None:
         status[P.status != 0] = P.status[P.status != 0]
     return (out, status, stages) if return_stages else (out, status)
+
+
+def _elsewhere(model, P, v, n_threads):
+    """The spectrum of vector v's elsewhere and a status (0, 1 ray failure,
+    7 integration failure)."""
+    spec = model.elsewhere
+    S = P.else_S
+    rs = slice(v * S, (v + 1) * S)
+    cs = slice(v * S * S, (v + 1) * S * S)
+    er = P.else_row
+    u = er["u"][rs].copy()
+    ma = er["maxAlpha"][rs].copy()
+    r_s = er["r_s"][v * S]
+    t, D, CA, L, MD = O.compute_rays(n_threads, S, r_s, u, ma, spec.num_rays)
+    if t:
+        return None, 1
+    m = P.else_meshes[v]
+    theta = np.repeat(er["theta0"][rs][:, None], S, axis=1)
+    st, spectrum = O.integrate_time_invariant(
+        n_threads, 0.0, m.omega, r_s, m.inclination, S, m.cellArea, er["radius"][rs], u,
+        theta, P.else_phi[cs].reshape(S, S), P.else_params[cs].reshape(S, S, 2),
+        spec.num_rays, D, CA, MD, er["cos_gamma"][rs], model.energies, (), spec.atm_ext,
+        spec.image_order_limit)
+    if st:
+        return None, 7
+    return spectrum, 0

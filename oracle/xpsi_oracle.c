@@ -335,7 +335,8 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                  const double *cellArea, const double *radius_arr,
                  const double *u_arr, const double *theta, const double *phi,
                  const double *srcCellParams, size_t n_params,
-                 const int *radiates, size_t N_R, const double *deflection,
+                 const int *radiates, const double *correction,
+                 size_t n_correction, size_t N_R, const double *deflection,
                  const double *cos_alpha, const double *lag,
                  const double *maxDeflection, const double *cos_gammaArray,
                  size_t N_E, const double *energies, size_t N_L,
@@ -343,6 +344,10 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                  int atm_ext, const xo_atmos4d *atmos, int image_order_limit,
                  double *flux) {
   (void)R;
+  /* the elsewhere correction (:257-261, :469-478): a blackbody elsewhere's
+   * intensity at correction[i, J] is subtracted from every profile value and
+   * every interpolated value is added, negative or not (:593-594) */
+  const int perform_correction = correction != NULL;
   const double sin_i = sin(inclination), cos_i = cos(inclination);
   const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
   const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
@@ -473,7 +478,11 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                   double Ep = energies[p] / Z;
                   double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
                                               : eval_bb(Ep, VEC);
-                  PROFILE[p * N_L + kdx] = (I_E * norm - 0.0) * GEOM;
+                  double corr = 0.0;
+                  if (perform_correction)
+                    corr = eval_bb(Ep, correction + (i * S1 + J) * n_correction) *
+                           (kErg * kPlanck);
+                  PROFILE[p * N_L + kdx] = (I_E * norm - corr) * GEOM;
                 }
               }
             }
@@ -534,7 +543,7 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
               }
               if (x < ip->xmin || x > ip->xmax) { terminate = 1; break; }
               double s = gsl_interp_eval(ip, PHASE, prof, x, acc_p);
-              if (s > 0.0) pflux[p * N_P + k] += A * s;
+              if (s > 0.0 || perform_correction) pflux[p * N_P + k] += A * s;
             }
           }
         }

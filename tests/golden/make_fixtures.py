@@ -15,6 +15,8 @@ Cases
   elsewhere      the photosphere elsewhere: closed mesh, rays and the
                  time-invariant integrator, blackbody and numerical 4-D, with
                  1 and 4 threads.
+  elsewhere_correction  the hot-region integrator with a blackbody
+                 elsewhere's correction, on config1's and num4d_omit's inputs.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -280,12 +282,46 @@ def elsewhere(xpsi):
     save("elsewhere", **m, inclination=inclination, energies=E, **out)
 
 
+def elsewhere_correction(xpsi):
+    """The hot-region integrator with the elsewhere correction
+    (integrator_for_azimuthal_invariance.pyx:257-261,469-478,593-594): a
+    blackbody elsewhere at log T 6.0 (config1's blackbody spot) and 6.2
+    (num4d_omit's numerical spot), correction vectors as Elsewhere and
+    HotRegion.embed build them (Elsewhere.py:305-330, HotRegion.py:1052-1067).
+    Inputs are the stored fixtures' own."""
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate
+    out = {}
+    for case, logT_else in (("config1", 6.0), ("num4d_omit", 6.2)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        corr = np.ones((S, S, 2))
+        corr[..., :-1] *= logT_else
+        for j in range(S):
+            corr[:, j, -1] *= f["effGrav"]
+        atm = ()
+        if int(f["atm_ext"]) == 2:
+            atm = tuple(np.ascontiguousarray(f[k]) for k in
+                        ("atm_logT", "atm_logg", "atm_mu", "atm_logE", "atm_I"))
+        st, flux = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                             float(f["inclination"]), f["cellArea"], f["radius"], f["u"],
+                             f["theta"], f["phi"], f["params"], f["radiates"], corr,
+                             int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+                             f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"],
+                             f["phases"], atm, (), int(f["atm_ext"]), 1, 0,
+                             int(f["image_order_limit"]) or None)
+        assert st == 0
+        out[case + "_correction"] = corr
+        out[case + "_flux"] = flux
+    save("elsewhere_correction", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
     num4d_omit(xpsi)
     config1(xpsi)
     elsewhere(xpsi)
+    elsewhere_correction(xpsi)
 
 
 if __name__ == "__main__":

@@ -64,3 +64,24 @@ def test_closed_mesh_rejects_odd_sizes(S):
     from xpsi_gb300.cellmesh.global_mesh import construct_closed_cellMesh
     with pytest.raises(ValueError):
         construct_closed_cellMesh(1, S, S * S, 1.0, 1.0, 1.2e4, 0.1, 0.1, 0)
+
+
+def _corrected_args(f, corr, atmos):
+    return (1, float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+            f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], f["params"],
+            f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+            f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"], f["phases"],
+            atmos, None, int(f["atm_ext"]), 1, 0, int(f["image_order_limit"]) or None)
+
+
+@pytest.mark.parametrize("case", ["config1", "num4d_omit"])
+def test_oracle_corrected_integrator_vs_reference(golden, case):
+    """The hot-region integrator with a blackbody elsewhere's correction
+    (integrator_for_azimuthal_invariance.pyx:257-261,469-478,593-594)."""
+    from conftest import atmos_of, row_rel
+    f = golden(case)
+    c = golden("elsewhere_correction")
+    atmos = atmos_of(f) if int(f["atm_ext"]) == 2 else ()
+    st, flux = O.integrate(*_corrected_args(f, c[case + "_correction"], atmos))
+    assert st == 0
+    assert row_rel(flux, c[case + "_flux"]) <= 1e-13

@@ -135,3 +135,71 @@ def test_elsewhere_batch_matches_single_calls(tinv, golden):
     out = flux.cpu().numpy()
     for m, s in enumerate(specs):
         np.testing.assert_array_equal(out[m], s["flux"])
+
+
+@pytest.mark.parametrize("case", ["config1", "num4d_omit"])
+def test_corrected_integrator_vs_reference(tinv, golden, case):
+    """The hot-region integrator with a blackbody elsewhere's correction
+    against the reference; 1e-9 relative to each energy row's largest value,
+    the bar of the uncorrected integrator."""
+    from conftest import atmos_of, row_rel
+    from test_elsewhere_host import _corrected_args
+    from xpsi_gb300.cellmesh import integrator_for_azimuthal_invariance as integ
+    f = golden(case)
+    c = golden("elsewhere_correction")
+    atmos = atmos_of(f) if int(f["atm_ext"]) == 2 else ()
+    st, flux = integ.integrate(*_corrected_args(f, c[case + "_correction"], atmos))
+    assert st == 0
+    assert row_rel(flux, c[case + "_flux"]) <= 1e-9
+    # the negative values the correction leaves are summed, not dropped
+    if case == "num4d_omit":
+        assert flux.min() < 0.0
+
+
+def test_corrected_integrator_rejects_num4d_elsewhere(tinv, golden):
+    from test_elsewhere_host import _corrected_args
+    from xpsi_gb300.cellmesh import integrator_for_azimuthal_invariance as integ
+    f = golden("config1")
+    c = golden("elsewhere_correction")
+    args = list(_corrected_args(f, c["config1_correction"], ()))
+    args[25] = 2
+    with pytest.raises(NotImplementedError):
+        integ.integrate(*args)
+
+
+@pytest.mark.parametrize("num4d", [False, True])
+@pytest.mark.parametrize("meshes", ["host", "gpu"])
+def test_batch_with_elsewhere_vs_oracle(tinv, num4d, meshes):
+    """The batched likelihood of a hot region plus a blackbody elsewhere
+    against the oracle pipeline on the same packed inputs: the corrected hot
+    signal with the spectrum added (1e-9 per energy row) and log L (1e-7)."""
+    import torch
+    from batch_cases import small_elsewhere
+    from conftest import row_rel
+    from oracle import pipeline as OP
+    from xpsi_gb300 import batch as BT
+    m, params = small_elsewhere(V=3, num4d=num4d)
+    P_host = BT.prepare(m, params)
+    ref, ref_st, stages = OP.loglike(m, P_host, return_stages=True)
+    ev = BT.BatchEvaluator(m)
+    P = BT.prepare(m, params, meshes=meshes)
+    B = ev.upload(P)
+    ev.run(B)
+    torch.cuda.synchronize()
+    st = ev.statuses(B)
+    np.testing.assert_array_equal(st, ref_st)
+    ok = st == 0
+    assert ok.all()
+    ll = B["loglike"].cpu().numpy()
+    assert np.max(np.abs(ll - ref)) <= 1e-7
+    flux = B["flux"].cpu().numpy()
+    for v in range(P.V):
+        assert row_rel(flux[v], stages[v]["flux"]) <= 1e-9
+
+
+def test_batch_with_elsewhere_rejects_mixed(tinv):
+    from batch_cases import small_elsewhere
+    from xpsi_gb300 import batch as BT
+    m, _ = small_elsewhere(V=1)
+    with pytest.raises(NotImplementedError):
+        BT.BatchEvaluator(m, precision="mixed")

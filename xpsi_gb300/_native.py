@@ -97,7 +97,8 @@ class IntegrateBatchData(C.Structure):
                 ("cos_alpha", P), ("lag", P), ("cellArea", P), ("phi", P),
                 ("params", P), ("n_params", I32), ("radiates", P), ("energies", P),
                 ("leaves", P), ("phases", P), ("atmos", Atmos4D), ("flux", P),
-                ("mesh_status", P), ("flop_counter", P)]
+                ("mesh_status", P), ("flop_counter", P), ("correction", P),
+                ("n_correction", I32)]
 
 
 class MeshRequest(C.Structure):
@@ -146,7 +147,8 @@ class ElsewhereBatchData(C.Structure):
     _fields_ = [("row_mesh", P), ("radius", P), ("u", P), ("cos_gamma", P),
                 ("theta0", P), ("maxDeflection", P), ("deflection", P), ("cos_alpha", P),
                 ("phi", P), ("params", P), ("n_params", I32), ("energies", P),
-                ("atmos", Atmos4D), ("flux", P), ("mesh_status", P)]
+                ("atmos", Atmos4D), ("flux", P), ("mesh_status", P), ("signal", P),
+                ("signal_stride", I64), ("signal_N_P", I32)]
 
 
 class LikelihoodBatchData(C.Structure):
@@ -164,9 +166,9 @@ def _bind(L):
         "xgpu_abi_version": (C.c_int, []),
         "xgpu_last_error": (C.c_char_p, []),
         "xgpu_compute_rays": (C.c_int, [SZ, D, P, P, SZ, P, P, P, P]),
-        "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, SZ,
+        "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ, SZ,
                                      P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
-                                     C.POINTER(Atmos4D), C.c_int, P]),
+                                     C.POINTER(Atmos4D), C.c_int, C.c_int, P]),
         "xgpu_energy_integrator": (C.c_int, [SZ, SZ, P, P, SZ, P, P]),
         "xgpu_response_fold": (C.c_int, [SZ, SZ, SZ, P, SZ, P, P]),
         "xgpu_precomputation": (C.c_int, [SZ, SZ, P, P]),

@@ -14,6 +14,12 @@ on the GPU:
            Likelihood.py:361-364) -> response fold (K5) -> background-
            marginalised log-likelihood of every vector (K6)
 
+With an Elsewhere (a blackbody photosphere outside the hot regions,
+Elsewhere.py) each vector also gets a closed mesh (host C++), its rays, the
+time-invariant integrator, the correction of the hot regions' intensities
+(integrator_for_azimuthal_invariance.pyx:469-478) and the spectrum added to
+the first hot region's signal (Photosphere.py:588-592).
+
 PyTorch supplies device buffers and the stream; the kernels are reached
 through the C ABI only.
 """
@@ -24,8 +30,10 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._native import (AllocRequest, Atmos4D, IntegrateBatchData, LikelihoodBatchData, Mesh,
-                      MeshBatchOut, MeshMember, check, lib)
+from ._native import (AllocRequest, Atmos4D, ElsewhereBatchData, ElsewhereMesh,
+                      IntegrateBatchData, LikelihoodBatchData, Mesh, MeshBatchOut, MeshMember,
+                      check, lib)
+from .cellmesh import global_mesh as _global_mesh
 from .cellmesh import mesh as _mesh
 
 # xpsi/global_imports.py
@@ -38,7 +46,7 @@ _KPC = 3.08567758e19
 _2PI = 2.0 * math.pi
 
 STATUS_NAMES = {0: "ok", 1: "RayError", 2: "PulseError", 3: "AtmosError", 4: "QuadFail",
-                5: "SlimCut", 6: "BadInput"}
+                5: "SlimCut", 6: "BadInput", 7: "IntegrationError"}
 
 
 @dataclass
@@ -53,6 +61,17 @@ class HotRegionSpec:
     image_order_limit: Optional[int] = None
     omit: bool = False
     is_antiphased: bool = False
+
+
+@dataclass
+class ElsewhereSpec:
+    """Resolution and kind of the photosphere elsewhere (Elsewhere.__init__
+    arguments).  Only the blackbody (atm_ext 1) is batched: the hot regions'
+    correction for a numerical elsewhere is not on the GPU path."""
+    atm_ext: int = 1
+    sqrt_num_cells: int = 64
+    num_rays: int = 1000
+    image_order_limit: Optional[int] = None
 
 
 @dataclass
@@ -82,8 +101,17 @@ class Model:
     sigmas: float = 10.0
     slim: float = 20.0
     energies: np.ndarray = field(default=None)
+    elsewhere: Optional[ElsewhereSpec] = None
 
     def __post_init__(self):
+        if self.elsewhere is not None:
+            e = self.elsewhere
+            if e.atm_ext != 1:
+                raise NotImplementedError("a batched elsewhere is a blackbody (atm_ext 1)")
+            if e.sqrt_num_cells < 10 or e.sqrt_num_cells % 2 != 0:
+                raise ValueError("elsewhere sqrt_num_cells must be an even integer >= 10")
+            if e.num_rays < 3:
+                raise ValueError("elsewhere num_rays must be at least 3")
         if self.energies is None:
             e = self.instrument.energy_edges
             # construct_energy_array for one waveband (Signal.py:1092-1197)
@@ -98,13 +126,16 @@ class Model:
 # parameter vector layout per vector:
 #   mass, radius_km, frequency, cos_inclination, distance_kpc,
 #   then per region: colatitude, angular radius, log10 T, phase shift,
-#   and for an omit region additionally omit radius, omit colatitude, omit azimuth
+#   and for an omit region additionally omit radius, omit colatitude, omit azimuth;
+#   last, with an elsewhere, its log10 T
 def param_names(model):
     names = ["mass", "radius", "frequency", "cos_inclination", "distance"]
     for h, r in enumerate(model.regions):
         names += [f"h{h}_colatitude", f"h{h}_radius", f"h{h}_temperature", f"h{h}_phase_shift"]
         if r.omit:
             names += [f"h{h}_omit_radius", f"h{h}_omit_colatitude", f"h{h}_omit_azimuth"]
+    if getattr(model, "elsewhere", None) is not None:
+        names.append("elsewhere_temperature")
     return names
 
 
@@ -147,6 +178,7 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
         raise ValueError("expected %d parameters per vector: %s" % (len(names), names))
     col = {n: i for i, n in enumerate(names)}
     reqs, members, pend, status = [], [], [], np.zeros(V, dtype=np.int32)
+    stars = []
     atm = model.atmosphere
     for v in range(V):
         p = params[v]
@@ -161,6 +193,7 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
         eps = Om ** 2.0 * R ** 3.0 / (_G * Mkg)
         star = dict(r_s=r_s, R=R, Omega=Om, zeta=zeta, eps=eps, inclination=math.acos(cosi),
                     d_sq=(Dkpc * _KPC) ** 2, f=f)
+        stars.append(star)
         if atm is not None and any(r.atm_ext == 2 for r in model.regions):
             # Photosphere.py:486-507
             gl = _effective_gravity_bounds(R, zeta, eps)
@@ -209,6 +242,9 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
     P.d_sq = np.empty(len(members))
     P.shifts = np.empty((V, H))
     P.members = members
+    P.else_V = 0
+    if model.elsewhere is not None:
+        _prepare_elsewhere(model, P, params, col, stars, n_threads)
     if meshes == "gpu":
         P.mesh_members = (MeshMember * len(members))()
         ro = co = 0
@@ -225,6 +261,7 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
             ro += S
             co += S * S
         P.row = None
+        P.correction = None  # formed on the device from the GPU-built params
         return P
     P.mesh_members = None
     _mesh.build_many(reqs, n_threads)
@@ -269,7 +306,51 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
         _member_meta(P, m_i, m, ro, co, N_E, N_P)
         ro += S
         co += S * S
+    if P.else_V:
+        # the hot regions' correction vectors: the elsewhere's log T with the
+        # hot mesh's effective gravity (Elsewhere.py:305-330, HotRegion.py:1052-1067)
+        P.correction = P.params.copy()
+        P.correction[:, 0] = np.repeat(P.else_logT[[m["v"] for m in members]],
+                                       [m["S"] * m["S"] for m in members])
     return P
+
+
+def _prepare_elsewhere(model, P, params, col, stars, n_threads):
+    """Closed meshes of every vector's elsewhere (host C++,
+    global_mesh.pyx:21-137) packed like the hot meshes: per parallel u, r_s,
+    maxAlpha, radius, cos_gamma, theta0; per cell phi and (log T, log10
+    effective gravity of the parallel) (Elsewhere.py:254-330)."""
+    spec = model.elsewhere
+    V = P.V
+    S = int(spec.sqrt_num_cells)
+    reqs = [dict(S=S, num_cells=S * S, R_eq=st["R"], zeta=st["zeta"], epsilon=st["eps"],
+                 star_shape_ind=0) for st in stars]
+    _global_mesh.build_many(reqs, n_threads)
+    P.else_V, P.else_S = V, S
+    P.else_logT = np.ascontiguousarray(params[:, col["elsewhere_temperature"]])
+    rows = V * S
+    P.else_row = {k: np.empty(rows) for k in ("u", "r_s", "maxAlpha", "radius", "cos_gamma",
+                                              "theta0")}
+    P.else_row_mesh = np.repeat(np.arange(V, dtype=np.int32), S)
+    P.else_phi = np.empty(V * S * S)
+    P.else_params = np.empty((V * S * S, 2))
+    P.else_meshes = (ElsewhereMesh * V)()
+    for v, (q, st) in enumerate(zip(reqs, stars)):
+        sl = slice(v * S, (v + 1) * S)
+        P.else_row["u"][sl] = st["r_s"] / q["r"]
+        P.else_row["r_s"][sl] = st["r_s"]
+        P.else_row["maxAlpha"][sl] = q["maxAlpha"]
+        P.else_row["radius"][sl] = q["r"]
+        P.else_row["cos_gamma"][sl] = q["cos_gamma"]
+        P.else_row["theta0"][sl] = q["theta"][:, 0]
+        cs = slice(v * S * S, (v + 1) * S * S)
+        P.else_phi[cs] = q["phi"].reshape(-1)
+        prm = P.else_params[cs].reshape(S, S, 2)
+        prm[..., 0] = P.else_logT[v]
+        prm[..., 1] = q["effGrav"][:, None]
+        P.else_meshes[v] = ElsewhereMesh(S, v * S, v * S * S, st["Omega"], st["inclination"],
+                                         q["cellArea"], int(spec.image_order_limit or 0),
+                                         int(spec.atm_ext))
 
 
 def _member_meta(P, m_i, m, ro, co, N_E, N_P):
@@ -294,6 +375,9 @@ class BatchEvaluator:
         import torch
         if precision not in ("plain", "mixed"):
             raise ValueError("precision is 'plain' or 'mixed'")
+        if precision == "mixed" and model.elsewhere is not None:
+            raise NotImplementedError("the elsewhere correction is computed by the FP64 "
+                                      "integrator only (precision 'plain')")
         self.precision = precision
         self.torch = torch
         self.model = model
@@ -356,6 +440,21 @@ class BatchEvaluator:
             B["cellArea"], B["phi"] = put(P.cellArea), put(P.phi)
             B["params"], B["radiates"] = put(P.params), put(P.radiates)
         B["d_sq"], B["shifts"] = put(P.d_sq), put(P.shifts)
+        if P.else_V:
+            B["else_row"] = {k: put(v) for k, v in P.else_row.items()}
+            B["else_row_mesh"] = put(P.else_row_mesh)
+            B["else_phi"], B["else_params"] = put(P.else_phi), put(P.else_params)
+            if P.correction is not None:
+                B["correction"] = put(P.correction)
+            else:
+                # the elsewhere's log T over each hot member's cells, with the
+                # hot mesh's effective gravity
+                torch = self.torch
+                corr = B["params"].clone()
+                per = torch.from_numpy(P.else_logT[[m["v"] for m in P.members]])
+                counts = torch.tensor([m["S"] * m["S"] for m in P.members])
+                corr[:, 0] = torch.repeat_interleave(per, counts).to(self.dev)
+                B["correction"] = corr
         self.alloc(P, B)
         return B
 
@@ -383,9 +482,17 @@ class BatchEvaluator:
         check(lib().xgpu_mesh_batch(len(P.mesh_members), P.mesh_members, R, C_, C.byref(o), st))
 
     def h2d_bytes(self, P: Prepared):
+        n = 0
+        if P.else_V:
+            n += (sum(v.nbytes for v in P.else_row.values()) + P.else_row_mesh.nbytes
+                  + P.else_phi.nbytes + P.else_params.nbytes)
+            if P.correction is not None:
+                n += P.correction.nbytes
+            else:
+                n += 8 * len(P.members)
         if P.mesh_members is not None:
-            return int(C.sizeof(P.mesh_members) + P.d_sq.nbytes + P.shifts.nbytes)
-        return int(sum(v.nbytes for v in P.row.values()) + P.row_mesh.nbytes
+            return int(n + C.sizeof(P.mesh_members) + P.d_sq.nbytes + P.shifts.nbytes)
+        return int(n + sum(v.nbytes for v in P.row.values()) + P.row_mesh.nbytes
                    + P.cellArea.nbytes + P.phi.nbytes + P.params.nbytes + P.radiates.nbytes
                    + P.d_sq.nbytes + P.shifts.nbytes)
 
@@ -411,6 +518,15 @@ class BatchEvaluator:
         B["chan_flag"] = torch.empty((P.V, self.K), dtype=torch.int32, device=dev)
         B["loglike"] = torch.empty(P.V, dtype=f64, device=dev)
         B["status"] = torch.empty(P.V, dtype=torch.int32, device=dev)
+        if P.else_V:
+            n_er = P.else_V * P.else_S
+            etab = (n_er, self.model.elsewhere.num_rays)
+            for k in ("else_defl", "else_ca", "else_lag"):
+                B[k] = torch.empty(etab, dtype=f64, device=dev)
+            B["else_maxDefl"] = torch.empty(n_er, dtype=f64, device=dev)
+            B["else_row_status"] = torch.empty(n_er, dtype=torch.int32, device=dev)
+            B["else_flux"] = torch.empty((P.else_V, N_E), dtype=f64, device=dev)
+            B["else_status"] = torch.empty(P.else_V, dtype=torch.int32, device=dev)
         B["P"] = P
 
     # ---------------------------------------------------------------- run
@@ -444,6 +560,15 @@ class BatchEvaluator:
         d.mesh_status = p(B["mesh_status"])
         n_m = P.V * P.H
         N_E, N_P = len(self.model.energies), self.N_L
+        if P.else_V:
+            er = B["else_row"]
+            N_Re = self.model.elsewhere.num_rays
+            check(L.xgpu_rays_batch(P.else_V * P.else_S, N_Re, p(er["u"]), p(er["r_s"]),
+                                    p(er["maxAlpha"]), p(B["else_defl"]), p(B["else_ca"]),
+                                    p(B["else_lag"]), p(B["else_maxDefl"]),
+                                    p(B["else_row_status"]), None, None, st))
+            d.correction = p(B["correction"])
+            d.n_correction = 2
         if probe is not None:
             d.flop_counter = p(probe["flops"])
             probe["start"] = torch.cuda.Event(enable_timing=True)
@@ -454,6 +579,22 @@ class BatchEvaluator:
         check(integ(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P, C.byref(d), 0, st))
         if probe is not None:
             probe["end"].record(strm)
+        if P.else_V:
+            # the time-invariant spectrum of every vector, added to its first
+            # hot region's signal (integrator_for_time_invariance.pyx:59-338,
+            # Photosphere.py:588-592)
+            ed = ElsewhereBatchData()
+            ed.row_mesh = p(B["else_row_mesh"])
+            ed.radius, ed.u = p(er["radius"]), p(er["u"])
+            ed.cos_gamma, ed.theta0 = p(er["cos_gamma"]), p(er["theta0"])
+            ed.maxDeflection = p(B["else_maxDefl"])
+            ed.deflection, ed.cos_alpha = p(B["else_defl"]), p(B["else_ca"])
+            ed.phi, ed.params, ed.n_params = p(B["else_phi"]), p(B["else_params"]), 2
+            ed.energies = p(self.energies)
+            ed.flux, ed.mesh_status = p(B["else_flux"]), p(B["else_status"])
+            ed.signal, ed.signal_stride, ed.signal_N_P = p(B["flux"]), P.H * N_E * N_P, N_P
+            check(L.xgpu_elsewhere_batch(P.else_V, P.else_meshes, P.else_V * P.else_S, N_Re,
+                                         N_E, 0, C.byref(ed), st))
         check(L.xgpu_energy_batch(n_m, N_E, N_P, self.log10edges.numel(), p(B["flux"]),
                                   p(B["off_in"]), p(self.log10E), p(self.log10edges),
                                   p(B["d_sq"]), p(B["integrated"]), p(B["off_out"]), 0, st))
@@ -490,6 +631,15 @@ class BatchEvaluator:
         for mi in np.nonzero(ms)[0]:
             if st[vec_of_mesh[mi]] == 0:
                 st[vec_of_mesh[mi]] = 2
+        if P.else_V:
+            ers = B["else_row_status"].cpu().numpy()
+            erm = B["else_row_mesh"].cpu().numpy()
+            est = B["else_status"].cpu().numpy()
+            for v in np.unique(erm[ers != 0]):
+                st[v] = 1
+            for v in np.nonzero(est)[0]:
+                if st[v] == 0:
+                    st[v] = 7
         st[P.status != 0] = P.status[P.status != 0]
         return st
 
@@ -539,7 +689,7 @@ def concat_prepared(parts, model: Model) -> Prepared:
     P.meshes = (Mesh * n_m)()
     P.mesh_members = (MeshMember * n_m)() if gpu else None
     rm, members = [], []
-    ro = co = mo = 0
+    ro = co = mo = vb = 0
     for p in parts:
         for i in range(len(p.meshes)):
             q = p.meshes[i]
@@ -554,11 +704,38 @@ def concat_prepared(parts, model: Model) -> Prepared:
                 P.mesh_members[mo + i] = mm
         if not gpu:
             rm.append(p.row_mesh + mo)
-        members += p.members
+        members += [dict(m, v=m["v"] + vb) for m in p.members]
+        vb += p.V
         ro += p.n_rows
         co += p.n_cells
         mo += len(p.meshes)
     if not gpu:
         P.row_mesh = np.concatenate(rm).astype(np.int32)
     P.members = members
+    P.else_V = sum(p.else_V for p in parts)
+    if P.else_V:
+        _concat_elsewhere(P, parts)
     return P
+
+
+def _concat_elsewhere(P, parts):
+    S = parts[0].else_S
+    P.else_S = S
+    P.else_logT = np.concatenate([p.else_logT for p in parts])
+    P.else_row = {k: np.concatenate([p.else_row[k] for p in parts]) for k in parts[0].else_row}
+    P.else_row_mesh = np.repeat(np.arange(P.else_V, dtype=np.int32), S)
+    P.else_phi = np.concatenate([p.else_phi for p in parts])
+    P.else_params = np.concatenate([p.else_params for p in parts])
+    P.else_meshes = (ElsewhereMesh * P.else_V)()
+    v0 = 0
+    for p in parts:
+        for i in range(p.else_V):
+            q = p.else_meshes[i]
+            P.else_meshes[v0 + i] = ElsewhereMesh(q.S, (v0 + i) * S, (v0 + i) * S * S, q.omega,
+                                                  q.inclination, q.cellArea,
+                                                  q.image_order_limit, q.atm_ext)
+        v0 += p.else_V
+    if all(p.correction is not None for p in parts):
+        P.correction = np.concatenate([p.correction for p in parts])
+    else:
+        P.correction = None

@@ -21,12 +21,18 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
 
     Returns (0, flux[N_E, N_P]) or (1, None) exactly as the reference does.
     Supported: blackbody (hot_atm_ext 1) and numerical 4-D (2) hot
-    atmospheres with beam_opt 0, no elsewhere correction and no disk
-    (R_in >= 1e6) -- the hot-region likelihood path.  Other options raise
-    NotImplementedError rather than silently computing something else.
+    atmospheres with beam_opt 0 and no disk (R_in >= 1e6), with or without
+    the correction for a blackbody elsewhere (else_atm_ext 1) -- the
+    hot-region likelihood path.  Other options raise NotImplementedError
+    rather than silently computing something else.
     """
+    corr = None
     if correction_srcCellParams is not None:
-        raise NotImplementedError("elsewhere correction fields are not on the GPU path")
+        if int(else_atm_ext) != 1:
+            raise NotImplementedError("the GPU path corrects for a blackbody elsewhere only")
+        corr = f64(correction_srcCellParams)
+        if corr.ndim != 3 or corr.shape[:2] != f64(cellArea).shape:
+            raise ValueError("correction_srcCellParams must be [rows, cells, n_params]")
     if int(beam_opt) != 0:
         raise NotImplementedError("beaming options 1-3 are not on the GPU path")
     if R_in < 1e6:
@@ -59,9 +65,10 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     st = check(lib().xgpu_integrate(
         float(R), float(omega), float(r_s), float(inclination), S0, S1, ptr(A),
         ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]), ptr(arrs[3]), ptr(par), par.shape[2],
-        ptr(rad), N_R, ptr(arrs[4]), ptr(arrs[5]), ptr(arrs[6]), ptr(arrs[7]),
-        ptr(arrs[8]), E.size, ptr(E), Lv.size, ptr(Lv), P.size, ptr(P), atm,
-        C.byref(atmos) if atmos is not None else None,
+        ptr(rad), ptr(corr), corr.shape[2] if corr is not None else 0, N_R, ptr(arrs[4]),
+        ptr(arrs[5]), ptr(arrs[6]), ptr(arrs[7]), ptr(arrs[8]), E.size, ptr(E), Lv.size,
+        ptr(Lv), P.size, ptr(P), atm, C.byref(atmos) if atmos is not None else None,
+        int(else_atm_ext) if corr is not None else 0,
         int(image_order_limit) if image_order_limit is not None else 0, ptr(flux)))
     del keep
     if st != 0:

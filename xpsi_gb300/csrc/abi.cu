@@ -213,6 +213,10 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
     if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
   }
+  if (d->correction != nullptr && mixed)
+    return fail_msg("the elsewhere correction is computed by the FP64 integrator only");
+  if (d->correction != nullptr && d->n_correction < 1)
+    return fail_msg("correction vectors need at least 1 parameter per cell");
   if (target_ctas <= 0) target_ctas = 8 * 152;
   // chunks of consecutive parallels of one mesh, sized by estimated cost
   // (cells per parallel) so that large meshes do not leave a long tail
@@ -259,6 +263,8 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.N_R = N_R;
   a.cellArea = d->cellArea; a.phi = d->phi; a.params = d->params; a.n_params = d->n_params;
   a.radiates = d->radiates;
+  a.correction = d->correction;
+  a.n_correction = d->n_correction;
   a.N_E = N_E; a.N_L = N_L; a.N_P = N_P;
   a.energies = d->energies; a.leaves = d->leaves; a.phases = d->phases;
   a.atmos = xg::Atmos4D{d->atmos.logT, d->atmos.logg, d->atmos.mu, d->atmos.logE,
@@ -380,11 +386,12 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
                    size_t S1, const double *cellArea, const double *radius,
                    const double *r_s_over_r, const double *theta, const double *phi,
                    const double *srcCellParams, size_t n_params, const int32_t *radiates,
-                   size_t N_R, const double *deflection, const double *cos_alpha,
-                   const double *lag, const double *maxDeflection, const double *cos_gamma,
-                   size_t N_E, const double *energies, size_t N_L, const double *leaves,
-                   size_t N_P, const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
-                   int image_order_limit, double *flux) {
+                   const double *correction, size_t n_correction, size_t N_R,
+                   const double *deflection, const double *cos_alpha, const double *lag,
+                   const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                   const double *energies, size_t N_L, const double *leaves, size_t N_P,
+                   const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
+                   int else_atm_ext, int image_order_limit, double *flux) {
   (void)R;
   (void)r_s;
   cudaStream_t st;
@@ -392,9 +399,15 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   if ((rc = lib_stream(&st))) return rc;
   if (n_params < 2) return fail_msg("srcCellParams needs at least 2 parameters per cell");
   if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
+  if (correction && else_atm_ext != 1)
+    return fail_msg("the GPU integrator corrects for a blackbody elsewhere only");
+  if (correction && n_correction < 1)
+    return fail_msg("correction vectors need at least 1 parameter per cell");
   xg::Atmos4D A{};
   if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
   const size_t cells = S0 * S1;
+  Dev dcorr;
+  if (correction && (rc = upload(dcorr, correction, cells * n_correction, st))) return rc;
   std::vector<double> theta0(S0);
   for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
   std::vector<int32_t> row_mesh(S0, 0);
@@ -425,6 +438,8 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   }
   d.flux = dF.as<double>();
   d.mesh_status = dst.as<int32_t>();
+  d.correction = correction ? dcorr.as<double>() : nullptr;
+  d.n_correction = (int32_t)n_correction;
   rc = xgpu_integrate_batch(1, &mesh, (int64_t)S0, (int)N_R, (int)N_E, (int)N_L, (int)N_P, &d,
                             0, st);
   if (rc) return rc;
@@ -620,6 +635,9 @@ int xgpu_elsewhere_batch(int n_meshes, const xgpu_elsewhere_mesh *meshes, int64_
   a.row_flux = drow.as<double>();
   a.flux = d->flux;
   a.status = d->mesh_status;
+  a.signal = d->signal;
+  a.signal_stride = d->signal_stride;
+  a.signal_N_P = d->signal_N_P;
   rc = xg::launch_elsewhere(a, st);
   if (rc == -2) return fail_msg("closed mesh too large for one CTA's shared memory");
   CK(cudaGetLastError());

@@ -309,7 +309,9 @@ __global__ void __launch_bounds__(kElseThreads) elsewhere_row_kernel(ElsewhereAr
   }
 }
 
-// :312-323: the parallels in order, times cellArea x norm / (E keV)
+// :312-323: the parallels in order, times cellArea x norm / (E keV); with a
+// signal given, the spectrum is also added to every phase column of that
+// mesh's signal [N_E][signal_N_P] (Photosphere.py:588-592)
 __global__ void elsewhere_finish_kernel(ElsewhereArgs a) {
   const int m = blockIdx.x;
   const ElseMeshDesc M = a.meshes[m];
@@ -317,7 +319,12 @@ __global__ void elsewhere_finish_kernel(ElsewhereArgs a) {
   for (int e = threadIdx.x; e < a.N_E; e += blockDim.x) {
     double s = 0.0;
     for (int i = 0; i < M.S; i++) s += a.row_flux[(int64_t)(M.row_off + i) * a.N_E + e];
-    a.flux[(int64_t)m * a.N_E + e] = s * (M.cellArea * norm / (a.energies[e] * kKeV));
+    const double f = s * (M.cellArea * norm / (a.energies[e] * kKeV));
+    a.flux[(int64_t)m * a.N_E + e] = f;
+    if (a.signal != nullptr && a.status[m] == 0) {
+      double *row = a.signal + (int64_t)m * a.signal_stride + (int64_t)e * a.signal_N_P;
+      for (int p = 0; p < a.signal_N_P; p++) row[p] += f;
+    }
   }
 }
 

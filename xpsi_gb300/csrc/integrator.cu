@@ -739,11 +739,13 @@ __device__ __forceinline__ bool cell_phase_sums(const CP &cp, const AR &area, in
 }
 
 // the FP64 path's form of cell_phase_sums, in double-float arithmetic on
-// scaled pieces (the sign test is on the high part: h + l has the sign of h)
+// scaled pieces (the sign test is on the high part: h + l has the sign of h;
+// with the elsewhere correction every value is added, :593-594)
 template <typename CP, typename AR>
 __device__ __forceinline__ bool cell_phase_sums_df(const CP &cp, const AR &area, int S1,
                                                    const int32_t *rad, const PieceDF *pc, int N_L,
-                                                   int pb, int ne, DF (&acc)[kEPT]) {
+                                                   int pb, int ne, bool add_all,
+                                                   DF (&acc)[kEPT]) {
   int hint = -1;
   for (int j = 0; j < S1; j++) {
     if (rad[j] != 1) continue;
@@ -757,7 +759,7 @@ __device__ __forceinline__ bool cell_phase_sums_df(const CP &cp, const AR &area,
       if (pb + e < ne) {
         const PieceDF q = pc[(pb + e) * N_L + iv];
         const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
-        if (sv.h > 0.0f) acc[e] = df_fma(A, sv, acc[e]);
+        if (sv.h > 0.0f || add_all) acc[e] = df_fma(A, sv, acc[e]);
       }
     }
   }
@@ -905,6 +907,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     const double fix = num4d ? (norm * p3) / ((double)(float)norm * (double)p3f)
                              : norm / (double)(float)norm;
     const double lg_Eeff = num4d ? log10(E_eff) : 0.0;
+    // the elsewhere correction's blackbody temperature at the parallel's
+    // first radiating cell (:469-476)
+    const bool corr = !kMixed && a.correction != nullptr;
+    const double kT_c =
+        corr ? (kKB / kKeV) *
+                   pow(10.0, a.correction[(M.cell_off + (int64_t)i * M.S1 + c.J) * a.n_correction])
+             : 0.0;
     const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
     const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
     const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
@@ -1023,7 +1032,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                 } else {
                   I_E = eval_bb(a.energies[p] / g.Z[s], kT);
                 }
-                y = (WT)((I_E * norm - 0.0) * g.GEOM[s]);
+                const double I_c =
+                    corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
+                y = (WT)((I_E * norm - I_c) * g.GEOM[s]);
               }
             }
             co4[pl * N_L + col].y = y;
@@ -1140,7 +1151,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             for (int e = 0; e < kEPT; e++) acc[e] = DF{0.0f, 0.0f};
             const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
             if (!cell_phase_sums_df(cp, ar, M.S1, rad, reinterpret_cast<const PieceDF *>(co4), N_L,
-                                    pb, ne, acc)) {
+                                    pb, ne, corr, acc)) {
               atomicExch(&a.member_status[m], (int)kPulseFail);
               continue;
             }

@@ -55,6 +55,11 @@ struct IntegrateArgs {
   const double *cellArea, *phi, *params;  // params [cells][n_params]
   int n_params;
   const int32_t *radiates;
+  // elsewhere correction (FP64 form only): a blackbody elsewhere whose
+  // intensity at correction[cell of the parallel's first radiating cell][0]
+  // (log T) is subtracted from every profile value; null: none
+  const double *correction;   // [cells][n_correction]
+  int n_correction;
   // shared grids
   int N_E, N_L, N_P;
   const double *energies, *leaves, *phases;
@@ -160,6 +165,9 @@ struct ElsewhereArgs {
   double *row_flux;           // [n_rows][N_E] scratch
   double *flux;               // [n_meshes][N_E]
   int32_t *status;            // [n_meshes], zeroed by the caller
+  double *signal;             // or null: mesh m's spectrum is added to every phase
+  int64_t signal_stride;      //   column of signal[m * signal_stride + e * signal_N_P + p]
+  int signal_N_P;
 };
 size_t elsewhere_smem_bytes(int N_R, int max_S, int max_images);
 int launch_elsewhere(const ElsewhereArgs &a, cudaStream_t st);

@@ -83,6 +83,14 @@ def estimate_bytes(ev: BT.BatchEvaluator, P) -> int:
     b += 8 * 152 * (N_E * N_P * 8)           # chunk partials (bounded)
     if ev.atmos is not None:
         b += 8 * 152 * ev.atmos.nmu * ev.atmos.nE * 8
+    if getattr(P, "else_V", 0):
+        # elsewhere: packed parallels and cells, ray tables, per-parallel
+        # spectra, the spectra, and the hot regions' correction vectors
+        er = P.else_V * P.else_S
+        b += er * (6 * 8 + 4) + er * P.else_S * 3 * 8
+        b += 3 * er * ev.model.elsewhere.num_rays * 8 + er * 12
+        b += er * N_E * 8 + P.else_V * (N_E * 8 + 4)
+        b += P.n_cells * 2 * 8
     return int(b)
 
 
