@@ -88,6 +88,30 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination,
                    int atm_ext, const xgpu_atmos4d *atmos, int else_atm_ext,
                    int image_order_limit, double *flux);
 
+/* Replaces xpsi.cellmesh.integrator.integrate (xpsi/cellmesh/integrator.pyx:
+ * 48-667), the general integrator of HotRegion(symmetry=False) for source
+ * parameters that vary from cell to cell.  Same arguments as xgpu_integrate
+ * (the phase interpolant of the geometric factor is Akima periodic, the
+ * reference's default).  Returns 0 (SUCCESS) or 1 (ERROR, :657-665), < 0 on a
+ * usage or CUDA failure. */
+int xgpu_integrate_general(double R, double omega, double r_s,
+                           double inclination, size_t S0, size_t S1,
+                           const double *cellArea,
+                           const double *radialCoords_of_parallels,
+                           const double *r_s_over_r, const double *theta,
+                           const double *phi, const double *srcCellParams,
+                           size_t n_params, const int32_t *cell_radiates,
+                           const double *correction_srcCellParams,
+                           size_t n_correction, size_t N_R,
+                           const double *deflection, const double *cos_alpha,
+                           const double *lag, const double *maxDeflection,
+                           const double *cos_gammaArray, size_t N_E,
+                           const double *energies, size_t N_L,
+                           const double *leaves, size_t N_P,
+                           const double *phases, int atm_ext,
+                           const xgpu_atmos4d *atmos, int else_atm_ext,
+                           int image_order_limit, double *flux);
+
 /* Replaces xpsi.tools.energy_integrator.energy_integrator
  * (xpsi/tools/energy_integrator.pyx:27-31).  signal[N_E][N_P]; log10 energies
  * and log10 interval edges; out[n_edges-1][N_P] (the reference's return,

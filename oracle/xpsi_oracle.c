@@ -14,6 +14,7 @@
  *   xo_compute_rays          cellmesh/rays.pyx:249-390 (+ rayIntegrator :90-247)
  *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665
  *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
+ *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
  *   xo_precomputation        likelihoods/default_background_marginalisation.pyx:38-68
@@ -563,6 +564,286 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
     for (size_t k = 0; k < N_P; k++) {
       double s = 0.0;
       for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_E * N_P + p * N_P + k];
+      flux[p * N_P + k] = s / (energies[p] * kKeV);
+    }
+  free(priv); free(cos_defl); free(ca_alt);
+  return terminate_any ? 1 : 0;
+}
+
+/* ================================================================== */
+/* general integrator (HotRegion symmetry=False):                     */
+/* cellmesh/integrator.pyx:48-667                                     */
+/* per cell: the leaf profiles of Z, mu eta and the geometric factor  */
+/* are splined in phase (Steffen, Steffen, Akima periodic) and the    */
+/* atmosphere is evaluated at every (cell, phase, energy)             */
+/* ================================================================== */
+int xo_integrate_general(int n_threads, double R, double omega, double r_s,
+                         double inclination, size_t S0, size_t S1,
+                         const double *cellArea, const double *radius_arr,
+                         const double *u_arr, const double *theta,
+                         const double *phi, const double *srcCellParams,
+                         size_t n_params, const int *radiates,
+                         const double *correction, size_t n_correction,
+                         size_t N_R, const double *deflection,
+                         const double *cos_alpha, const double *lag,
+                         const double *maxDeflection,
+                         const double *cos_gammaArray, size_t N_E,
+                         const double *energies, size_t N_L,
+                         const double *leaves, size_t N_P, const double *phases,
+                         int atm_ext, const xo_atmos4d *atmos,
+                         int image_order_limit, double *flux) {
+  (void)R;
+  (void)r_s;
+  const double sin_i = sin(inclination), cos_i = cos(inclination);
+  const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
+  const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
+  const int perform_correction = correction != NULL;
+  int nt = n_threads > 0 ? n_threads : 1;
+  int terminate_any = 0;
+  double *priv = (double *)calloc((size_t)nt * N_P * N_E, sizeof(double));
+  /* :255-270 */
+  double *cos_defl = (double *)malloc(S0 * N_R * sizeof(double));
+  double *ca_alt = (double *)malloc(S0 * N_R * sizeof(double));
+  for (size_t i = 0; i < S0; i++)
+    for (size_t j = 0; j < N_R; j++) {
+      cos_defl[i * N_R + j] = cos(deflection[i * N_R + N_R - j - 1]);
+      ca_alt[i * N_R + j] = cos_alpha[i * N_R + N_R - j - 1];
+    }
+  gsl_error_handler_t *prev = gsl_set_error_handler_off();
+
+#pragma omp parallel num_threads(nt) reduction(| : terminate_any)
+  {
+    int T = 0;
+#ifdef _OPENMP
+    T = omp_get_thread_num();
+#endif
+    double *pflux = priv + (size_t)T * N_P * N_E; /* [N_P][N_E] as :120 */
+    gsl_interp_accel *acc_a = gsl_interp_accel_alloc(), *acc_alt = gsl_interp_accel_alloc();
+    gsl_interp_accel *acc_l = gsl_interp_accel_alloc();
+    gsl_interp_accel *acc_g = gsl_interp_accel_alloc(), *acc_z = gsl_interp_accel_alloc();
+    gsl_interp_accel *acc_b = gsl_interp_accel_alloc();
+    gsl_interp *ia = gsl_interp_alloc(gsl_interp_steffen, N_R);
+    gsl_interp *il = gsl_interp_alloc(gsl_interp_steffen, N_R);
+    gsl_interp *iz = gsl_interp_alloc(gsl_interp_steffen, N_L);
+    gsl_interp *ib = gsl_interp_alloc(gsl_interp_steffen, N_L);
+    gsl_interp *ig = gsl_interp_alloc(gsl_interp_akima_periodic, N_L);
+    double *PH = (double *)malloc(N_L * sizeof(double));
+    double *ZZ = (double *)malloc(N_L * sizeof(double));
+    double *AB = (double *)malloc(N_L * sizeof(double));
+    double *GE = (double *)malloc(N_L * sizeof(double));
+    num4d_state nst;
+    if (atm_ext == 2) num4d_reset(&nst, atmos);
+    int terminate = 0;
+#pragma omp for schedule(static, 1)
+    for (long ii = 0; ii < (long)S0; ii++) {
+      size_t i = (size_t)ii, j;
+      if (terminate) continue;
+      for (j = 0; j < S1; j++)
+        if (radiates[i * S1 + j] == 1) break;
+      if (j == S1) continue;
+      const double *defl = deflection + i * N_R;
+      gsl_interp_accel_reset(acc_a);
+      gsl_interp_accel_reset(acc_l);
+      j = 0;
+      while (defl[j] <= kHalfPi) j++;
+      const double *xalt = cos_defl + i * N_R + (N_R - j - 1);
+      const double *yalt = ca_alt + i * N_R + (N_R - j - 1);
+      gsl_interp *ialt = gsl_interp_alloc(gsl_interp_steffen, j + 1);
+      gsl_interp_init(ialt, xalt, yalt, j + 1);
+      gsl_interp_accel_reset(acc_alt);
+      gsl_interp_init(ia, defl, cos_alpha + i * N_R, N_R);
+      gsl_interp_init(il, defl, lag + i * N_R, N_R);
+      const double *ya = cos_alpha + i * N_R, *yl = lag + i * N_R;
+
+      double radius = radius_arr[i];
+      double Grav_z = sqrt(1.0 - u_arr[i]);
+      double cos_gamma = cos_gammaArray[i];
+      double sin_gamma = sqrt(1.0 - cos_gamma * cos_gamma);
+      double cos_th = cos(theta[i * S1]), sin_th = sin(theta[i * S1]);
+      double th_over_pi = theta[i * S1] / kPi;
+      double beta = radius * omega * sin_th / (kC * Grav_z);
+      double Lorentz = sqrt(1.0 - beta * beta);
+      double cos_a = -1.0, deriv = -1.0;
+      int IO = image_order_limit > 0 ? image_order_limit
+                                     : (int)ceil(maxDeflection[i] / kPi);
+      for (int I = 0; I < IO; I++) {
+        int InvisFlag = 2;
+        size_t InvisPhase = 0;
+        double InvisStep, Zs, As;
+        for (size_t k = 0; k < N_L; k++) { /* :321-505 (all leaves) */
+          double cos_psi = cos_i * cos_th + sin_i * sin_th * cos(leaves[k]);
+          double psi = image_deflection(I, acos(cos_psi));
+          double sin_psi = sin(psi);
+          if (!are_equal(psi, 0.0) && are_equal(sin_psi, 0.0)) {
+            double _i = (cos_i >= 0.0) ? inclination + inclination * 1.0e-6
+                                       : inclination - inclination * 1.0e-6;
+            cos_psi = cos(_i) * cos_th + sin(_i) * sin_th * cos(leaves[k]);
+            psi = image_deflection(I, acos(cos_psi));
+            sin_psi = sin(psi);
+          }
+          int visible = 0;
+          double sin_alpha = 0.0, mu = 0.0;
+          if (psi <= maxDeflection[i]) {
+            if (psi < ia->xmin || psi > ia->xmax) { terminate = 1; break; }
+            if (psi <= kHalfPi && cos_psi >= ialt->xmin)
+              cos_a = gsl_interp_eval(ialt, xalt, yalt, cos_psi, acc_alt);
+            else
+              cos_a = gsl_interp_eval(ia, defl, ya, psi, acc_a);
+            sin_alpha = sqrt(1.0 - cos_a * cos_a);
+            mu = cos_a * cos_gamma;
+            if (!are_equal(psi, 0.0)) {
+              double cos_delta = (cos_i - cos_th * cos_psi) / (sin_th * sin_psi);
+              if (th_over_pi < 0.5) mu = mu + sin_alpha * sin_gamma * cos_delta;
+              else mu = mu - sin_alpha * sin_gamma * cos_delta;
+            }
+            visible = mu > 0.0;
+          }
+          if (visible) {
+            if (psi <= kHalfPi && cos_psi >= ialt->xmin) {
+              deriv = gsl_interp_eval_deriv(ialt, xalt, yalt, cos_psi, acc_alt);
+            } else {
+              deriv = gsl_interp_eval_deriv(ia, defl, ya, psi, acc_a);
+              deriv = exp(log(fabs(deriv)) - log(fabs(sin_psi)));
+            }
+            if (psi < il->xmin || psi > il->xmax) { terminate = 1; break; }
+            double plag = gsl_interp_eval(il, defl, yl, psi, acc_l);
+            for (int ks = 0; ks < 2; ks++) {
+              if ((0 < k && k < leaf_lim - 1) || (k == 0 && ks == 0) ||
+                  (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
+                  (k == leaf_lim - 1 && N_L % 2 == 0)) {
+                size_t kdx = (ks == 0) ? k : N_L - 1 - k;
+                double superlum, eta;
+                if (!are_equal(psi, 0.0)) {
+                  double cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
+                  superlum = 1.0 + beta * cos_xi;
+                  eta = Lorentz / superlum;
+                } else {
+                  superlum = 1.0;
+                  eta = Lorentz;
+                }
+                ZZ[kdx] = eta * Grav_z;
+                AB[kdx] = mu * eta;
+                GE[kdx] = mu * fabs(deriv) * Grav_z * eta * eta * eta / superlum;
+                PH[kdx] = leaves[kdx] + plag;
+              }
+            }
+            if (k == 0) { /* :422-427 */
+              PH[N_L - 1] = PH[0] + kTwoPi;
+              ZZ[N_L - 1] = ZZ[0];
+              AB[N_L - 1] = AB[0];
+              GE[N_L - 1] = GE[0];
+            } else if (k > 0 && InvisFlag == 2) { /* :428-460 */
+              InvisStep = leaves[k] / (double)k;
+              Zs = (ZZ[k] - ZZ[N_L - k - 1]) / (2.0 * (double)k);
+              As = (AB[k] - AB[N_L - k - 1]) / (2.0 * (double)k);
+              for (size_t m = N_L - k; m < N_L; m++) {
+                PH[m] = PH[m - 1] + InvisStep;
+                ZZ[m] = ZZ[m - 1] + Zs;
+                AB[m] = AB[m - 1] + As;
+                GE[m] = 0.0;
+              }
+              PH[0] = PH[N_L - 1] - kTwoPi;
+              ZZ[0] = ZZ[N_L - 1];
+              AB[0] = AB[N_L - 1];
+              GE[0] = GE[N_L - 1];
+              for (size_t m = 1; m < k; m++) {
+                PH[m] = PH[m - 1] + InvisStep;
+                ZZ[m] = ZZ[m - 1] + Zs;
+                AB[m] = AB[m - 1] + As;
+                GE[m] = 0.0;
+              }
+            } else if (InvisFlag == 1) { /* :461-488 */
+              InvisStep = (PH[k] - PH[InvisPhase - 1]) / (double)(k - InvisPhase + 1);
+              Zs = (ZZ[k] - ZZ[InvisPhase - 1]) / (double)(k - InvisPhase + 1);
+              As = (AB[k] - AB[InvisPhase - 1]) / (double)(k - InvisPhase + 1);
+              for (size_t m = InvisPhase; m < k; m++) {
+                PH[m] = PH[m - 1] + InvisStep;
+                ZZ[m] = ZZ[m - 1] + Zs;
+                AB[m] = AB[m - 1] + As;
+              }
+              InvisStep = (PH[N_L - InvisPhase] - PH[N_L - 1 - k]) / (double)(k - InvisPhase + 1);
+              Zs = (ZZ[N_L - InvisPhase] - ZZ[N_L - 1 - k]) / (double)(k - InvisPhase + 1);
+              As = (AB[N_L - InvisPhase] - AB[N_L - 1 - k]) / (double)(k - InvisPhase + 1);
+              for (size_t m = N_L - k; m < N_L - InvisPhase; m++) {
+                PH[m] = PH[m - 1] + InvisStep;
+                ZZ[m] = ZZ[m - 1] + Zs;
+                AB[m] = AB[m - 1] + As;
+              }
+            }
+            InvisFlag = 0;
+          } else if (InvisFlag == 0) { /* :491-505, :507-525 */
+            InvisStep = (PH[N_L - k] - PH[k - 1]) / (double)(N_L - 2 * k + 1);
+            Zs = (ZZ[N_L - k] - ZZ[k - 1]) / (double)(N_L - 2 * k + 1);
+            As = (AB[N_L - k] - AB[k - 1]) / (double)(N_L - 2 * k + 1);
+            for (size_t m = k; m < N_L - k; m++) {
+              PH[m] = PH[m - 1] + InvisStep;
+              ZZ[m] = ZZ[m - 1] + Zs;
+              AB[m] = AB[m - 1] + As;
+              GE[m] = 0.0;
+            }
+            InvisFlag = 1;
+            InvisPhase = k;
+          }
+        }
+        if (terminate) break;
+        if (InvisFlag == 2) break;
+        for (size_t m = 1; m < N_L; m++)
+          if (PH[m] <= PH[m - 1]) { terminate = 1; break; }
+        if (terminate) break;
+        gsl_interp_accel_reset(acc_z);
+        gsl_interp_init(iz, PH, ZZ, N_L);
+        gsl_interp_accel_reset(acc_b);
+        gsl_interp_init(ib, PH, AB, N_L);
+        gsl_interp_accel_reset(acc_g);
+        gsl_interp_init(ig, PH, GE, N_L);
+        for (j = 0; j < S1 && !terminate; j++) { /* :549-594 */
+          if (radiates[i * S1 + j] != 1) continue;
+          const double shift = phi[i * S1 + j];
+          const double A = cellArea[i * S1 + j];
+          const double *VEC = srcCellParams + (i * S1 + j) * n_params;
+          for (size_t k = 0; k < N_P; k++) {
+            double x = phases[k] + shift;
+            if (x > PH[N_L - 1]) {
+              while (x > PH[N_L - 1]) x = x - kTwoPi;
+            } else if (x < PH[0]) {
+              while (x < PH[0]) x = x + kTwoPi;
+            }
+            if (x < ig->xmin || x > ig->xmax) { terminate = 1; break; }
+            double G = gsl_interp_eval(ig, PH, GE, x, acc_g);
+            if (G > 0.0) {
+              double Z = gsl_interp_eval(iz, PH, ZZ, x, acc_z);
+              double ABB = gsl_interp_eval(ib, PH, AB, x, acc_b);
+              for (size_t p = 0; p < N_E; p++) {
+                double Ep = energies[p] / Z;
+                double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
+                                            : eval_bb(Ep, VEC);
+                I_E = I_E * norm;
+                double corr = 0.0;
+                if (perform_correction)
+                  corr = eval_bb(Ep, correction + (i * S1 + j) * n_correction) *
+                         (kErg * kPlanck);
+                pflux[k * N_E + p] += A * (I_E - corr) * G;
+              }
+            }
+          }
+        }
+        if (terminate) break;
+      }
+      gsl_interp_free(ialt);
+    }
+    if (terminate) terminate_any = 1;
+    gsl_interp_free(ia); gsl_interp_free(il); gsl_interp_free(iz); gsl_interp_free(ib);
+    gsl_interp_free(ig);
+    gsl_interp_accel_free(acc_a); gsl_interp_accel_free(acc_alt); gsl_interp_accel_free(acc_l);
+    gsl_interp_accel_free(acc_g); gsl_interp_accel_free(acc_z); gsl_interp_accel_free(acc_b);
+    free(PH); free(ZZ); free(AB); free(GE);
+  }
+  gsl_set_error_handler(prev);
+  /* :603-610 */
+  for (size_t p = 0; p < N_E; p++)
+    for (size_t k = 0; k < N_P; k++) {
+      double s = 0.0;
+      for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_P * N_E + k * N_E + p];
       flux[p * N_P + k] = s / (energies[p] * kKeV);
     }
   free(priv); free(cos_defl); free(ca_alt);

@@ -81,3 +81,46 @@ def elsewhere_args(f, case, atmos, threads=1, image_order_limit=None, inclinatio
             f[("num4d" if case != "bb" else "bb") + "_params"], int(f["N_R"]),
             f["deflection"], f["cos_alpha"], f["maxDeflection"], f["cos_gamma"],
             f["energies"], atmos, 1 if case == "bb" else 2, image_order_limit)
+
+
+def general_args(golden, case, threads=1, corrected=False, mu09=False, image_order_limit=None):
+    """Arguments of integrator.integrate (the general integrator) for a
+    general_integrator.npz case on its base fixture's mesh and rays."""
+    f = golden(case)
+    g = golden("general_integrator")
+    atmos = ()
+    if int(f["atm_ext"]) == 2:
+        atmos = atmos_of(f)
+        if mu09:
+            atmos = (atmos[0], atmos[1], np.ascontiguousarray(0.9 * atmos[2]), atmos[3],
+                     atmos[4])
+    corr = g[case + "_corrected_correction"] if corrected else None
+    iol = image_order_limit if image_order_limit is not None else (
+        int(f["image_order_limit"]) or None)
+    return (threads, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+            float(f["inclination"]), f["cellArea"], f["radius"], f["u"], f["theta"],
+            f["phi"], g[case + "_params"], f["radiates"], corr, int(f["N_R"]),
+            f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"], f["cos_gamma"],
+            f["energies"], f["leaves"], f["phases"], atmos, None, int(f["atm_ext"]),
+            1 if corrected else None, 0, iol)
+
+
+# the general-integrator fixture's cases: (base fixture, corrected, mu09, key)
+GENERAL_CASES = (("config1", False, False, "config1_flux_threads1"),
+                 ("config1", True, False, "config1_corrected_flux_threads1"),
+                 ("num4d_omit", False, False, "num4d_omit_flux_threads1"),
+                 ("num4d_omit", False, True, "num4d_omit_mu09_flux_threads1"))
+
+
+def row_rel_floor(a, b, floor=1e-15):
+    """row_rel with each energy row's scale floored at `floor` times the
+    spectrum's largest value: rows many orders of magnitude below the peak
+    (the 4-point Lagrange stencil cancelling in the Num4D table's exponential
+    tail, where the reference's own value is rounding residue) are held
+    against that floor instead of their own maximum."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    peak = np.max(np.abs(b))
+    scale = np.maximum(np.max(np.abs(b), axis=1, keepdims=True), floor * peak)
+    scale = np.where(scale > 0, scale, 1e300)
+    return float(np.max(np.abs(a - b) / scale))

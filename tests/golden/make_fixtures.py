@@ -17,6 +17,9 @@ Cases
                  1 and 4 threads.
   elsewhere_correction  the hot-region integrator with a blackbody
                  elsewhere's correction, on config1's and num4d_omit's inputs.
+  general_integrator  the general integrator (HotRegion symmetry=False) with a
+                 temperature varying across the mesh, on config1's and
+                 num4d_omit's inputs.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -315,6 +318,63 @@ def elsewhere_correction(xpsi):
     save("elsewhere_correction", **out)
 
 
+def general_integrator(xpsi):
+    """The general integrator of HotRegion(symmetry=False)
+    (cellmesh/integrator.pyx:48-667) on stored fixtures' meshes and rays,
+    with a temperature that varies from cell to cell (the non-uniform hot
+    region it exists for): config1's blackbody spot (with and without a
+    blackbody elsewhere's correction) and num4d_omit's numerical spot at
+    600 Hz (1 and 4 threads)."""
+    from xpsi.cellmesh.integrator import integrate
+    out = {}
+    for case in ("config1", "num4d_omit"):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        params = np.array(f["params"], copy=True)
+        # log T rising by 0.1 dex across the mesh's azimuth and colatitude
+        jj, ii = np.meshgrid(np.arange(S), np.arange(S))
+        params[..., 0] += 0.1 * (jj / max(S - 1, 1)) - 0.05 * (ii / max(S - 1, 1))
+        atm = ()
+        if int(f["atm_ext"]) == 2:
+            atm = tuple(np.ascontiguousarray(f[k]) for k in
+                        ("atm_logT", "atm_logg", "atm_mu", "atm_logE", "atm_I"))
+        corr_cases = [("", None)]
+        if case == "config1":
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = 6.0
+            corr[..., 1] = f["effGrav"][:, None]
+            corr_cases.append(("_corrected", corr))
+        for tag, corr in corr_cases:
+            for nt in ((1, 4) if case == "num4d_omit" else (1,)):
+                st, flux = integrate(nt, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                                     float(f["inclination"]), f["cellArea"], f["radius"],
+                                     f["u"], f["theta"], f["phi"], params, f["radiates"], corr,
+                                     int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+                                     f["maxDeflection"], f["cos_gamma"], f["energies"],
+                                     f["leaves"], f["phases"], atm, (), int(f["atm_ext"]),
+                                     1 if corr is not None else None, 0,
+                                     int(f["image_order_limit"]) or None)
+                assert st == 0
+                out["%s%s_flux_threads%d" % (case, tag, nt)] = flux
+            if corr is not None:
+                out[case + tag + "_correction"] = corr
+        out[case + "_params"] = params
+        if case == "num4d_omit":
+            # the same table on a mu grid topped at 0.9: many evaluations lie
+            # above it and the evaluator's clamp history decides their value
+            atm09 = (atm[0], atm[1], np.ascontiguousarray(0.9 * atm[2]), atm[3], atm[4])
+            st, flux = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                                 float(f["inclination"]), f["cellArea"], f["radius"], f["u"],
+                                 f["theta"], f["phi"], params, f["radiates"], None,
+                                 int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+                                 f["maxDeflection"], f["cos_gamma"], f["energies"],
+                                 f["leaves"], f["phases"], atm09, (), 2, None, 0,
+                                 int(f["image_order_limit"]) or None)
+            assert st == 0
+            out["num4d_omit_mu09_flux_threads1"] = flux
+    save("general_integrator", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -322,6 +382,7 @@ def main():
     config1(xpsi)
     elsewhere(xpsi)
     elsewhere_correction(xpsi)
+    general_integrator(xpsi)
 
 
 if __name__ == "__main__":

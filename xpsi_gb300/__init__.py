@@ -6,6 +6,7 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
 
     xpsi_gb300.cellmesh.rays.compute_rays
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
+    xpsi_gb300.cellmesh.integrator.integrate          (HotRegion symmetry=False)
     xpsi_gb300.cellmesh.global_mesh.construct_closed_cellMesh   (elsewhere)
     xpsi_gb300.cellmesh.integrator_for_time_invariance.integrate (elsewhere)
     xpsi_gb300.tools.energy_integrator.energy_integrator
@@ -32,6 +33,7 @@ def install(xpsi_module):
     import importlib
     from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
+    from .cellmesh import integrator as general
     from .tools import energy_integrator as ei
     from .likelihoods import default_background_marginalisation as dbm
     done = []
@@ -46,6 +48,7 @@ def install(xpsi_module):
         ("xpsi.cellmesh.global_mesh", "construct_closed_cellMesh",
          global_mesh.construct_closed_cellMesh),
         ("xpsi.cellmesh.integrator_for_time_invariance", "integrate", tinv.integrate),
+        ("xpsi.cellmesh.integrator", "integrate", general.integrate),
     ]
     for modname, attr, fn in targets:
         try:
@@ -72,8 +75,8 @@ def install(xpsi_module):
 
     def _symmetry(self, declaration, _orig=orig):
         _orig(self, declaration)
-        if declaration and not getattr(self, "_split", False):
-            self._integrator = integ.integrate
+        if not getattr(self, "_split", False):
+            self._integrator = integ.integrate if declaration else general.integrate
     HotRegion.symmetry = property(HotRegion.symmetry.fget, _symmetry)
     done.append("xpsi.HotRegion.HotRegion.symmetry")
     return done

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
 UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh",
-         "mesh_gpu", "elsewhere"]
+         "mesh_gpu", "elsewhere", "general"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -199,6 +199,10 @@ def _bind(L):
         "xgpu_mesh_batch": (C.c_int, [C.c_int, C.POINTER(MeshMember), I64, I64,
                                       C.POINTER(MeshBatchOut), P]),
         "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
+        "xgpu_integrate_general": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P,
+                                             SZ, SZ, P, P, P, P, P, SZ, P, SZ, P, SZ, P,
+                                             C.c_int, C.POINTER(Atmos4D), C.c_int, C.c_int,
+                                             P]),
         "xgpu_closed_cell_mesh": (C.c_int, [SZ, SZ, D, D, D, C.c_int, P, P, P, P, P, P, P]),
         "xgpu_closed_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(ClosedMeshRequest),
                                                  C.c_int]),
@@ -224,7 +228,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_likelihood_batch_static", "xgpu_integrate_batch_mixed",
             "xgpu_fold_batch_tc", "xgpu_mesh_batch", "xgpu_allocate_cells_many",
             "xgpu_closed_cell_mesh", "xgpu_closed_cell_mesh_many",
-            "xgpu_integrate_time_invariant", "xgpu_elsewhere_batch"]
+            "xgpu_integrate_time_invariant", "xgpu_elsewhere_batch",
+            "xgpu_integrate_general"]
 
 
 def lib():

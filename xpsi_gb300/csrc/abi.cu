@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -447,6 +448,102 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(flux, dF.p, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return status != 0 ? 1 : 0;
+}
+
+int xgpu_integrate_general(double R, double omega, double r_s, double inclination, size_t S0,
+                           size_t S1, const double *cellArea, const double *radius,
+                           const double *r_s_over_r, const double *theta, const double *phi,
+                           const double *srcCellParams, size_t n_params,
+                           const int32_t *radiates, const double *correction,
+                           size_t n_correction, size_t N_R, const double *deflection,
+                           const double *cos_alpha, const double *lag,
+                           const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                           const double *energies, size_t N_L, const double *leaves,
+                           size_t N_P, const double *phases, int atm_ext,
+                           const xgpu_atmos4d *atmos, int else_atm_ext, int image_order_limit,
+                           double *flux) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (S0 == 0 || S1 == 0 || N_E == 0 || N_P == 0) return 0;
+  if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
+  if (N_R < 3) return fail_msg("num_rays must be at least 3");
+  if (atm_ext != 1 && atm_ext != 2) return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
+  if (atm_ext == 2 && n_params < 2)
+    return fail_msg("srcCellParams needs (log T, log g) per cell for Num4D");
+  if (n_params < 1) return fail_msg("srcCellParams needs at least 1 parameter per cell");
+  if (correction && else_atm_ext != 1)
+    return fail_msg("the GPU integrator corrects for a blackbody elsewhere only");
+  if (correction && n_correction < 1)
+    return fail_msg("correction vectors need at least 1 parameter per cell");
+  if (xg::general_geometry_smem_bytes((int)N_R, (int)N_L) > 227 * 1024)
+    return fail_msg("num_rays and num_leaves too large for one CTA's shared memory");
+  // images per parallel: the reference's image order of the rows it evaluates
+  int IOmax = 1;
+  for (size_t i = 0; i < S0; i++) {
+    bool any = false;
+    for (size_t j = 0; j < S1 && !any; j++) any = radiates[i * S1 + j] == 1;
+    if (!any) continue;
+    const double io = image_order_limit > 0 ? (double)image_order_limit
+                                            : std::ceil(maxDeflection[i] / 3.14159265358979323846);
+    if (io > 64.0) return fail_msg("a parallel has more than 64 images");
+    IOmax = std::max(IOmax, (int)io);
+  }
+  xg::Atmos4D A{};
+  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  const size_t cells = S0 * S1;
+  std::vector<double> theta0(S0);
+  for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
+  const size_t n_ent = cells * (size_t)IOmax * N_P;
+  Dev dA, drad, du, dth0, dphi, dpar, dR, dD, dCA, dL, dMD, dcg, dE, dLv, dP, dF, dst, dcorr;
+  Dev deG, deZ, deA, dimg, dpart;
+  if ((rc = upload(dA, cellArea, cells, st)) || (rc = upload(drad, radius, S0, st)) ||
+      (rc = upload(du, r_s_over_r, S0, st)) || (rc = upload(dth0, theta0.data(), S0, st)) ||
+      (rc = upload(dphi, phi, cells, st)) || (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
+      (rc = upload(dR, radiates, cells, st)) || (rc = upload(dD, deflection, S0 * N_R, st)) ||
+      (rc = upload(dCA, cos_alpha, S0 * N_R, st)) || (rc = upload(dL, lag, S0 * N_R, st)) ||
+      (rc = upload(dMD, maxDeflection, S0, st)) || (rc = upload(dcg, cos_gamma, S0, st)) ||
+      (rc = upload(dE, energies, N_E, st)) || (rc = upload(dLv, leaves, N_L, st)) ||
+      (rc = upload(dP, phases, N_P, st)) || (rc = dalloc(dF, N_E * N_P * 8, st)) ||
+      (rc = dalloc(dst, 16, st)) || (rc = dalloc(deG, n_ent * 8, st)) ||
+      (rc = dalloc(deZ, n_ent * 8, st)) || (rc = dalloc(deA, n_ent * 8, st)) ||
+      (rc = dalloc(dimg, S0 * 4, st)) ||
+      (rc = dalloc(dpart, S0 * (size_t)IOmax * N_E * N_P * 8, st)))
+    return rc;
+  if (correction && (rc = upload(dcorr, correction, cells * n_correction, st))) return rc;
+  CK(cudaMemsetAsync(dst.p, 0, 16, st));
+  xg::GeneralArgs a{};
+  a.S0 = (int)S0; a.S1 = (int)S1; a.N_R = (int)N_R; a.N_L = (int)N_L; a.N_P = (int)N_P;
+  a.N_E = (int)N_E; a.IOmax = IOmax;
+  a.omega = omega; a.inclination = inclination; a.image_order_limit = image_order_limit;
+  a.atm_ext = atm_ext;
+  a.radiates = dR.as<int32_t>();
+  a.cellArea = dA.as<double>(); a.phi = dphi.as<double>(); a.params = dpar.as<double>();
+  a.n_params = (int)n_params;
+  a.correction = correction ? dcorr.as<double>() : nullptr;
+  a.n_correction = (int)n_correction;
+  a.radius = drad.as<double>(); a.u = du.as<double>(); a.cos_gamma = dcg.as<double>();
+  a.theta0 = dth0.as<double>(); a.maxDeflection = dMD.as<double>();
+  a.deflection = dD.as<double>(); a.cos_alpha = dCA.as<double>(); a.lag = dL.as<double>();
+  a.energies = dE.as<double>(); a.leaves = dLv.as<double>(); a.phases = dP.as<double>();
+  a.atmos = A;
+  a.eG = deG.as<double>(); a.eZ = deZ.as<double>(); a.eA = deA.as<double>();
+  a.n_img = dimg.as<int32_t>();
+  a.partial = dpart.as<double>();
+  a.flux = dF.as<double>();
+  a.status = dst.as<int32_t>();
+  rc = xg::launch_general(a, st);
+  if (rc == -2) return fail_msg("integrator shared memory too large");
+  CK(cudaGetLastError());
+  int32_t status = 0;
+  CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux, dF.p, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (status == XGPU_BAD_INPUT) return fail_msg("a parallel has more images than held");
   return status != 0 ? 1 : 0;
 }
 

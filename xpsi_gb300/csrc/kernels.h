@@ -170,6 +170,31 @@ struct ElsewhereArgs {
   int signal_N_P;
 };
 size_t elsewhere_smem_bytes(int N_R, int max_S, int max_images);
+
+// ---- the general integrator (HotRegion symmetry=False) -------------------------
+struct GeneralArgs {
+  int S0, S1, N_R, N_L, N_P, N_E;
+  int IOmax;                  // images held per parallel in the entry scratch
+  double omega, inclination;
+  int image_order_limit;      // 0: ceil(maxDeflection / pi) per parallel
+  int atm_ext;                // 1 blackbody, 2 Num4D
+  const int32_t *radiates;    // [S0][S1]
+  const double *cellArea, *phi, *params;  // [S0][S1], [S0][S1], [S0][S1][n_params]
+  int n_params;
+  const double *correction;   // [S0][S1][n_correction] or null (blackbody elsewhere)
+  int n_correction;
+  const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;  // [S0]
+  const double *deflection, *cos_alpha, *lag;                     // [S0][N_R]
+  const double *energies, *leaves, *phases;
+  Atmos4D atmos;
+  double *eG, *eZ, *eA;       // [S0][IOmax][S1][N_P] entry scratch
+  int32_t *n_img;             // [S0] images evaluated per parallel
+  double *partial;            // [S0][IOmax][N_E][N_P]
+  double *flux;               // [N_E][N_P]
+  int32_t *status;            // [1], zeroed by the caller
+};
+size_t general_geometry_smem_bytes(int N_R, int N_L);
+int launch_general(const GeneralArgs &a, cudaStream_t st);
 int launch_elsewhere(const ElsewhereArgs &a, cudaStream_t st);
 
 }  // namespace xg
