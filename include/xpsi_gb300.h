@@ -442,6 +442,63 @@ int xgpu_elsewhere_batch(int n_meshes, const xgpu_elsewhere_mesh *meshes,
                          int64_t n_rows, int N_R, int N_E, int max_images,
                          const xgpu_elsewhere_batch_data *d, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* Synthesis: expected counts, phase integration, Poisson realisations.     */
+/* ---------------------------------------------------------------------- */
+
+/* One component signal (count rates [K][ld], phases [n] in cycles on [0, 1],
+ * phase shift in cycles). */
+typedef struct {
+  const double *signal;
+  const double *phases;
+  int64_t ld;
+  int32_t n;
+  double shift;
+} xgpu_component;
+
+/* Replaces compute_expected_counts (xpsi/tools/compute_expected_counts.pyx:
+ * 200-276), the core of synthesise_exposure and
+ * synthesise_given_total_count_number (xpsi/tools/synthesise.pyx).  HOST
+ * arrays: H components over the phase-bin edges phases[B + 1]; background
+ * count rates [K][B] or NULL; allow_negative[H].  out[K][B] = exposure x
+ * (sum of the components' bin-integrated rates, clamped at zero, + the
+ * background rate).  Returns 0, < 0 on a usage or CUDA failure. */
+int xgpu_compute_expected_counts(double exposure_time, size_t B,
+                                 const double *phases, size_t K, size_t H,
+                                 const xgpu_component *components,
+                                 const double *background,
+                                 const int32_t *allow_negative, double *out);
+
+/* Replaces xpsi.tools.phase_integrator.phase_integrator
+ * (xpsi/tools/phase_integrator.pyx:23-121): signal[rows][n_phases] (HOST)
+ * integrated over the phase-shifted bins of phases[n_edges], times the
+ * exposure; out[rows][n_edges - 1]. */
+int xgpu_phase_integrator(double exposure_time, size_t n_edges,
+                          const double *phases, size_t rows, size_t n_phases,
+                          const double *signal, const double *signal_phases,
+                          double phase_shift, int allow_negative, double *out);
+
+/* Poisson realisations of mean[n] (HOST): out[i] ~ Poisson(mean[i]) drawn
+ * from Philox4x32-10 keyed by `seed` at element offset + i (so a draw
+ * depends only on the seed and its element number).  The law is GSL's
+ * gsl_ran_poisson's (synthesise.pyx:130-140); the stream is not GSL's.
+ * Returns 0, 1 if a draw hit the rejection loop's bound, < 0 on failure. */
+int xgpu_poisson(size_t n, const double *mean, uint64_t seed, uint64_t offset,
+                 double *out);
+
+/* Batched forms (device pointers; `components` is a HOST array of
+ * n_sets x H descriptors whose pointers are device memory). */
+int xgpu_expected_counts_batch(int n_sets, int K, int B, int H,
+                               double exposure, const double *phase_edges,
+                               const xgpu_component *components,
+                               const int32_t *allow_negative,
+                               const double *background, double *out,
+                               void *stream);
+/* fail (device int32, may be NULL) is set to 1 if a draw hit the bound. */
+int xgpu_poisson_batch(int64_t n, const double *mean, double *out,
+                       uint64_t seed, uint64_t offset, int32_t *fail,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

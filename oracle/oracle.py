@@ -79,6 +79,12 @@ def lib():
                 C.c_double, C.c_size_t, P, C.c_size_t, P, C.c_size_t, P, P, P, P,
                 P, P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                 P, C.c_double, P, C.c_uint, P, P, P, P]
+            L.xo_expected_counts.restype = None
+            L.xo_expected_counts.argtypes = [C.c_double, C.c_size_t, P, C.c_size_t, C.c_size_t,
+                                             P, P, P, P, P, P, P]
+            L.xo_phase_integrator.restype = None
+            L.xo_phase_integrator.argtypes = [C.c_double, C.c_size_t, P, C.c_size_t, C.c_size_t,
+                                              P, P, C.c_double, C.c_int, P]
             L.xo_lnfact.restype = C.c_double
             L.xo_lnfact.argtypes = [C.c_uint]
             _lib = L
@@ -280,3 +286,40 @@ def eval_marginal_likelihood(exposure_time, phases, counts, components,
         _p(STAR), _p(mb), _p(mbs))
     res = (ll.value, STAR, mb, mbs)
     return (res, st) if return_status else res
+
+
+def compute_expected_counts(exposure_time, phases, components, component_phases, phase_shifts,
+                            background=None, allow_negative=False):
+    """compute_expected_counts (compute_expected_counts.pyx:200-276): [K, B]
+    expected counts; background is a count-rate array [K, B] or None."""
+    ph = _c(phases)
+    comps = [_c(c) for c in components]
+    cph = [_c(c) for c in component_phases]
+    H = len(comps)
+    K = comps[0].shape[0]
+    B = ph.size - 1
+    if isinstance(allow_negative, bool):
+        an = np.full(H, int(allow_negative), dtype=np.int32)
+    else:
+        an = _c([int(x) for x in allow_negative], np.int32)
+    ptrs = (C.c_void_p * H)(*[_p(c).value for c in comps])
+    pptrs = (C.c_void_p * H)(*[_p(c).value for c in cph])
+    nph = np.array([c.shape[1] for c in comps], dtype=np.uint64)
+    sh = _c(phase_shifts)
+    bg = _c(background) if background is not None else None
+    out = np.zeros((K, B))
+    lib().xo_expected_counts(float(exposure_time), B, _p(ph), K, H, C.cast(ptrs, C.c_void_p),
+                             _p(nph), C.cast(pptrs, C.c_void_p), _p(sh),
+                             _p(bg) if bg is not None else None, _p(an), _p(out))
+    return out
+
+
+def phase_integrator(exposure_time, phases, signal, signal_phases, phase_shift,
+                     allow_negative=False):
+    """tools.phase_integrator.phase_integrator (phase_integrator.pyx:23-121)."""
+    ph = _c(phases); S = _c(signal); sp = _c(signal_phases)
+    out = np.zeros((S.shape[0], ph.size - 1))
+    lib().xo_phase_integrator(float(exposure_time), ph.size, _p(ph), S.shape[0], S.shape[1],
+                              _p(S), _p(sp), float(phase_shift), int(bool(allow_negative)),
+                              _p(out))
+    return out

@@ -17,6 +17,8 @@
  *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
+ *   xo_expected_counts       tools/compute_expected_counts.pyx:200-276
+ *   xo_phase_integrator      tools/phase_integrator.pyx:23-121
  *   xo_precomputation        likelihoods/default_background_marginalisation.pyx:38-68
  *   xo_eval_marginal_likelihood   same file :176-734 and
  *                            tools/compute_expected_counts.pyx:66-197
@@ -1204,6 +1206,73 @@ static void star_rate_channel(size_t B, const double *phase_edges, size_t H,
   }
   for (size_t j = 0; j < B; j++)
     if (STAR[j] < 0.0) STAR[j] = 0.0;
+}
+
+/* tools/compute_expected_counts.pyx:200-276: out[K][B] = exposure x (the
+ * components' bin-integrated rates, clamped at zero, + background rate) */
+void xo_expected_counts(double exposure_time, size_t B, const double *phase_edges,
+                        size_t K, size_t H, const double *const *components,
+                        const size_t *n_phase, const double *const *component_phases,
+                        const double *shifts, const double *background,
+                        const int *allow_negative, double *out) {
+  gsl_interp **ip = (gsl_interp **)calloc(H, sizeof(gsl_interp *));
+  gsl_interp_accel **acc = (gsl_interp_accel **)calloc(H, sizeof(gsl_interp_accel *));
+  for (size_t p = 0; p < H; p++) {
+    if (n_phase[p] > 1) {
+      ip[p] = gsl_interp_alloc(gsl_interp_akima_periodic, n_phase[p]);
+      acc[p] = gsl_interp_accel_alloc();
+    }
+  }
+  for (size_t i = 0; i < K; i++) {
+    double *STAR = out + i * B;
+    for (size_t j = 0; j < B; j++) STAR[j] = 0.0;
+    star_rate_channel(B, phase_edges, H, components, n_phase, component_phases, shifts, ip,
+                      acc, STAR, i, allow_negative);
+    for (size_t j = 0; j < B; j++) {
+      STAR[j] += background ? background[i * B + j] : 0.0;
+      STAR[j] *= exposure_time;
+    }
+  }
+  for (size_t p = 0; p < H; p++) {
+    if (ip[p]) gsl_interp_free(ip[p]);
+    if (acc[p]) gsl_interp_accel_free(acc[p]);
+  }
+  free(ip);
+  free(acc);
+}
+
+/* tools/phase_integrator.pyx:23-121 */
+void xo_phase_integrator(double exposure_time, size_t n_edges, const double *phases,
+                         size_t rows, size_t n_phases, const double *signal,
+                         const double *signal_phases, double phase_shift, int allow_negative,
+                         double *out) {
+  gsl_interp *ip = gsl_interp_alloc(gsl_interp_akima_periodic, n_phases);
+  gsl_interp_accel *acc = gsl_interp_accel_alloc();
+  const size_t B = n_edges - 1;
+  for (size_t i = 0; i < rows; i++) {
+    gsl_interp_accel_reset(acc);
+    const double *y = signal + i * n_phases;
+    gsl_interp_init(ip, signal_phases, y, n_phases);
+    for (size_t j = 0; j < B; j++) {
+      double a = phases[j] + phase_shift, b = phases[j + 1] + phase_shift, v;
+      double *o = out + i * B + j;
+      *o = 0.0;
+      if (b - a == 1.0) { a = 0.0; b = 1.0; }
+      else { a -= floor(a); b -= floor(b); }
+      if (a < b) {
+        v = gsl_interp_eval_integ(ip, signal_phases, y, a, b, acc);
+        if (v > 0.0 || allow_negative) *o = v;
+      } else {
+        v = gsl_interp_eval_integ(ip, signal_phases, y, a, 1.0, acc);
+        if (v > 0.0 || allow_negative) *o = v;
+        v = gsl_interp_eval_integ(ip, signal_phases, y, 0.0, b, acc);
+        if (v > 0.0 || allow_negative) *o += v;
+      }
+      *o *= exposure_time;
+    }
+  }
+  gsl_interp_free(ip);
+  gsl_interp_accel_free(acc);
 }
 
 /* default_background_marginalisation.pyx:450-734.  Returns 0 normally,

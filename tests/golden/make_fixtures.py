@@ -20,6 +20,8 @@ Cases
   general_integrator  the general integrator (HotRegion symmetry=False) with a
                  temperature varying across the mesh, on config1's and
                  num4d_omit's inputs.
+  synthesis      expected counts of the reference's synthesis routines and
+                 its phase integrator on config1's folded signal.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -375,6 +377,41 @@ def general_integrator(xpsi):
     save("general_integrator", **out)
 
 
+def synthesis(xpsi):
+    """Expected counts of the reference's synthesis routines
+    (tools/synthesise.pyx: synthesise_exposure and
+    synthesise_given_total_count_number, both through
+    compute_expected_counts.pyx:200-276) and tools/phase_integrator.pyx on
+    config1's folded signal: two components on different phase grids (the
+    second a shifted copy sampled on a coarser grid), negative parts allowed for the
+    second, a phase-dependent background.  The realisations (SYNTHETIC) come
+    from the random stream of the build and are not stored."""
+    from xpsi.tools.synthesise import synthesise_exposure, synthesise_given_total_count_number
+    from xpsi.tools.phase_integrator import phase_integrator
+    f = np.load(os.path.join(HERE, "config1.npz"))
+    c1 = np.ascontiguousarray(f["folded"])
+    p1 = np.ascontiguousarray(f["comp_phases"])
+    p2 = np.linspace(0.0, 1.0, 33)
+    c2 = np.ascontiguousarray(
+        [0.3 * np.interp((p2 + 0.11) % 1.0, p1, row) for row in c1])
+    edges = np.ascontiguousarray(f["phase_edges"])
+    K, B = c1.shape[0], edges.size - 1
+    rng = np.random.default_rng(5)
+    bkg = np.ascontiguousarray(rng.uniform(0.5, 1.5, (K, B)) * c1.mean(axis=1)[:, None])
+    shifts = np.array([0.1, -0.3])
+    ex = synthesise_exposure(2.0e5, edges, (c1, c2), (p1, p2), shifts, 3.0e4, bkg,
+                             allow_negative=[False, True], gsl_seed=7)
+    tc = synthesise_given_total_count_number(edges, 1.0e6, (c1, c2), (p1, p2), shifts, 2.0e5,
+                                             bkg, allow_negative=[False, True], gsl_seed=7)
+    pi = phase_integrator(1.0e5, edges, c1, p1, 0.25)
+    pi_neg = phase_integrator(1.0e5, edges, c2, p2, -0.7, True)
+    # c1, p1 and the bin edges are config1.npz's folded, comp_phases, phase_edges
+    save("synthesis", c2=c2, p2=p2, bkg=bkg, shifts=shifts,
+         exposure_expec=ex[0], exposure_scale_background=ex[2], total_expec=tc[0],
+         total_scale_star=tc[2], total_scale_ratio=tc[3], phase_integrated=pi,
+         phase_integrated_neg=pi_neg)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -383,6 +420,7 @@ def main():
     elsewhere(xpsi)
     elsewhere_correction(xpsi)
     general_integrator(xpsi)
+    synthesis(xpsi)
 
 
 if __name__ == "__main__":

@@ -10,6 +10,9 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
     xpsi_gb300.cellmesh.global_mesh.construct_closed_cellMesh   (elsewhere)
     xpsi_gb300.cellmesh.integrator_for_time_invariance.integrate (elsewhere)
     xpsi_gb300.tools.energy_integrator.energy_integrator
+    xpsi_gb300.tools.phase_integrator.phase_integrator
+    xpsi_gb300.tools.synthesise.{synthesise_exposure,
+                                 synthesise_given_total_count_number}
     xpsi_gb300.likelihoods.default_background_marginalisation.{precomputation,
                                                               eval_marginal_likelihood}
     xpsi_gb300.instrument.fold        (Instrument.__call__'s matrix product)
@@ -35,6 +38,7 @@ def install(xpsi_module):
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
     from .cellmesh import integrator as general
     from .tools import energy_integrator as ei
+    from .tools import phase_integrator as pint, synthesise as syn
     from .likelihoods import default_background_marginalisation as dbm
     done = []
     targets = [
@@ -49,6 +53,10 @@ def install(xpsi_module):
          global_mesh.construct_closed_cellMesh),
         ("xpsi.cellmesh.integrator_for_time_invariance", "integrate", tinv.integrate),
         ("xpsi.cellmesh.integrator", "integrate", general.integrate),
+        ("xpsi.tools.phase_integrator", "phase_integrator", pint.phase_integrator),
+        ("xpsi.tools.synthesise", "synthesise_exposure", syn.synthesise_exposure),
+        ("xpsi.tools.synthesise", "synthesise_given_total_count_number",
+         syn.synthesise_given_total_count_number),
     ]
     for modname, attr, fn in targets:
         try:
@@ -60,6 +68,10 @@ def install(xpsi_module):
     # names bound at import time by the model classes
     for modname, attr, fn in (("xpsi.HotRegion", "_compute_rays", rays.compute_rays),
                               ("xpsi.Signal", "energy_integrator", ei.energy_integrator),
+                              ("xpsi.Signal", "phase_integrator", pint.phase_integrator),
+                              ("xpsi.Signal", "_synthesise_expo", syn.synthesise_exposure),
+                              ("xpsi.Signal", "_synthesise_given_total_count_number",
+                               syn.synthesise_given_total_count_number),
                               ("xpsi.Elsewhere", "_compute_rays", rays.compute_rays),
                               ("xpsi.Elsewhere", "_construct_closed_cellMesh",
                                global_mesh.construct_closed_cellMesh),

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxpsi_gb300.so")
 UNITS = ["rays", "integrator", "energy", "fold", "fold_tc", "likelihood", "abi", "mesh",
-         "mesh_gpu", "elsewhere", "general"]
+         "mesh_gpu", "elsewhere", "general", "synth"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
@@ -151,6 +151,10 @@ class ElsewhereBatchData(C.Structure):
                 ("signal_stride", I64), ("signal_N_P", I32)]
 
 
+class Component(C.Structure):
+    _fields_ = [("signal", P), ("phases", P), ("ld", I64), ("n", I32), ("shift", D)]
+
+
 class LikelihoodBatchData(C.Structure):
     _fields_ = [("n_vec", I32), ("K", I32), ("B", I32), ("H", I32), ("N_P", I32),
                 ("exposure", D), ("epsabs", D), ("epsrel", D), ("epsilon", D),
@@ -203,6 +207,13 @@ def _bind(L):
                                              SZ, SZ, P, P, P, P, P, SZ, P, SZ, P, SZ, P,
                                              C.c_int, C.POINTER(Atmos4D), C.c_int, C.c_int,
                                              P]),
+        "xgpu_compute_expected_counts": (C.c_int, [D, SZ, P, SZ, SZ, C.POINTER(Component), P, P,
+                                                   P]),
+        "xgpu_phase_integrator": (C.c_int, [D, SZ, P, SZ, SZ, P, P, D, C.c_int, P]),
+        "xgpu_poisson": (C.c_int, [SZ, P, C.c_uint64, C.c_uint64, P]),
+        "xgpu_expected_counts_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, D, P,
+                                                 C.POINTER(Component), P, P, P, P]),
+        "xgpu_poisson_batch": (C.c_int, [I64, P, P, C.c_uint64, C.c_uint64, P, P]),
         "xgpu_closed_cell_mesh": (C.c_int, [SZ, SZ, D, D, D, C.c_int, P, P, P, P, P, P, P]),
         "xgpu_closed_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(ClosedMeshRequest),
                                                  C.c_int]),
@@ -229,7 +240,9 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_fold_batch_tc", "xgpu_mesh_batch", "xgpu_allocate_cells_many",
             "xgpu_closed_cell_mesh", "xgpu_closed_cell_mesh_many",
             "xgpu_integrate_time_invariant", "xgpu_elsewhere_batch",
-            "xgpu_integrate_general"]
+            "xgpu_integrate_general", "xgpu_compute_expected_counts",
+            "xgpu_phase_integrator", "xgpu_poisson", "xgpu_expected_counts_batch",
+            "xgpu_poisson_batch"]
 
 
 def lib():

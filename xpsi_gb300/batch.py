@@ -30,7 +30,7 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._native import (AllocRequest, Atmos4D, ElsewhereBatchData, ElsewhereMesh,
+from ._native import (AllocRequest, Atmos4D, Component, ElsewhereBatchData, ElsewhereMesh,
                       IntegrateBatchData, LikelihoodBatchData, Mesh, MeshBatchOut, MeshMember,
                       check, lib)
 from .cellmesh import global_mesh as _global_mesh
@@ -530,10 +530,11 @@ class BatchEvaluator:
         B["P"] = P
 
     # ---------------------------------------------------------------- run
-    def run(self, B, stream=None, probe=None):
+    def run(self, B, stream=None, probe=None, likelihood=True):
         """Enqueue the five stages on `stream` (default: torch's current).
         `probe` (optional dict) receives CUDA events around the integrator
-        launch and its algorithmic FLOP count (key "flops", a device tensor)."""
+        launch and its algorithmic FLOP count (key "flops", a device tensor).
+        likelihood=False stops after the response fold (B["folded"])."""
         torch = self.torch
         P = B["P"]
         strm = stream or torch.cuda.current_stream(self.dev)
@@ -601,6 +602,8 @@ class BatchEvaluator:
         fold = L.xgpu_fold_batch_tc if self.precision == "mixed" else L.xgpu_fold_batch
         check(fold(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
                                 p(B["integrated"]), p(B["folded"]), st))
+        if not likelihood:
+            return
         m = self.model
         ld = LikelihoodBatchData()
         ld.n_vec, ld.K, ld.B, ld.H, ld.N_P = P.V, self.K, self.B, P.H, N_P
@@ -615,6 +618,58 @@ class BatchEvaluator:
         ld.star = ld.mcl_bg = ld.mcl_bg_support = None
         ld.loglike, ld.status = p(B["loglike"]), p(B["status"])
         check(L.xgpu_likelihood_batch(C.byref(ld), st))
+
+    def synthesise(self, params, exposure_time, background=None, seed=0, n_threads=0,
+                   meshes="gpu"):
+        """Synthetic data sets for many parameter vectors in one pass, as
+        Signal.synthesise does for one (Signal.py:725-855 with an exposure
+        time, tools/synthesise.pyx:35-140): the signal of every vector, its
+        expected counts per (channel, phase bin) =
+        exposure x (the hot regions' bin-integrated count rates, clamped at
+        zero, + `background` count rates [K, B]), and a Poisson realisation
+        of each, drawn on the GPU from Philox4x32-10 keyed by `seed` at the
+        element's index in the batch.  Returns host arrays (expected
+        [V, K, B], counts [V, K, B], status [V]); vectors with a non-zero
+        status (ray or integration failure, atmosphere bounds) carry no data
+        set."""
+        torch = self.torch
+        P = prepare(self.model, params, n_threads, meshes=meshes)
+        B = self.upload(P)
+        self.run(B, likelihood=False)
+        p = lambda x: x.data_ptr()
+        N_P = self.N_L
+        n_m = P.V * P.H
+        comps = (Component * n_m)()
+        base = p(B["folded"])
+        for i in range(n_m):
+            comps[i] = Component(base + 8 * i * self.K * N_P, p(self.comp_phases), N_P, N_P,
+                                 float(P.shifts[i // P.H, i % P.H]))
+        bg = None
+        if background is not None:
+            bg = torch.as_tensor(np.ascontiguousarray(background, dtype=np.float64),
+                                 device=self.dev)
+            if tuple(bg.shape) != (self.K, self.B):
+                raise ValueError("background must be [channels, phase bins]")
+        expec = torch.empty((P.V, self.K, self.B), dtype=torch.float64, device=self.dev)
+        counts = torch.empty_like(expec)
+        fail = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        L = lib()
+        check(L.xgpu_expected_counts_batch(P.V, self.K, self.B, P.H, float(exposure_time),
+                                           p(self.phase_edges), comps, p(self.allow_negative),
+                                           p(bg) if bg is not None else None, p(expec), st))
+        check(L.xgpu_poisson_batch(expec.numel(), p(expec), p(counts),
+                                   int(seed) & (2 ** 64 - 1), 0, p(fail), st))
+        status = self.statuses_no_likelihood(B)
+        if int(fail.item()):
+            raise RuntimeError("a Poisson draw hit the rejection loop's bound")
+        return expec.cpu().numpy(), counts.cpu().numpy(), status
+
+    def statuses_no_likelihood(self, B):
+        """Per-vector status of a run stopped after the fold (ray, pulse,
+        atmosphere and elsewhere failures)."""
+        B["status"].zero_()
+        return self.statuses(B)
 
     def statuses(self, B):
         """Per-vector status word (ray, pulse, atmosphere, quadrature, slim)."""

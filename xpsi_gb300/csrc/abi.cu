@@ -797,4 +797,121 @@ int xgpu_integrate_time_invariant(double R, double omega, double r_s, double inc
   return status != 0 ? 1 : 0;
 }
 
+// ------------------------------------------------------------- synthesis
+int xgpu_expected_counts_batch(int n_sets, int K, int B, int H, double exposure,
+                               const double *phase_edges, const xgpu_component *components,
+                               const int32_t *allow_negative, const double *background,
+                               double *out, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_sets <= 0 || K <= 0 || B <= 0) return 0;
+  if (H <= 0) return fail_msg("at least one component is needed");
+  static_assert(sizeof(xgpu_component) == sizeof(xg::CompDesc), "component layout");
+  for (int64_t c = 0; c < (int64_t)n_sets * H; c++)
+    if (components[c].n < 1 || (components[c].n > 1 && components[c].n < 5))
+      return fail_msg("a component needs one phase or at least five (Akima spline)");
+  Dev dc;
+  int rc;
+  if ((rc = upload(dc, reinterpret_cast<const xg::CompDesc *>(components),
+                   (size_t)n_sets * H, st)))
+    return rc;
+  xg::ExpectedArgs a{n_sets, K, B, H, exposure, phase_edges, dc.as<xg::CompDesc>(),
+                     allow_negative, background, out};
+  xg::launch_expected_counts(a, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_poisson_batch(int64_t n, const double *mean, double *out, uint64_t seed,
+                       uint64_t offset, int32_t *fail_flag, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n <= 0) return 0;
+  Dev df;
+  int rc;
+  if (!fail_flag) {
+    if ((rc = dalloc(df, 16, st))) return rc;
+    fail_flag = df.as<int32_t>();
+    CK(cudaMemsetAsync(fail_flag, 0, 4, st));
+  }
+  xg::launch_poisson(n, mean, out, seed, offset, fail_flag, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_compute_expected_counts(double exposure_time, size_t B, const double *phases, size_t K,
+                                 size_t H, const xgpu_component *components,
+                                 const double *background, const int32_t *allow_negative,
+                                 double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (K == 0 || B == 0) return 0;
+  if (H == 0) return fail_msg("at least one component is needed");
+  std::vector<Dev> keep(2 * H);
+  std::vector<xgpu_component> dcomp(H);
+  for (size_t h = 0; h < H; h++) {
+    const xgpu_component &c = components[h];
+    if (c.n < 1 || c.ld < c.n) return fail_msg("component shape is invalid");
+    if ((rc = upload(keep[2 * h], c.signal, K * (size_t)c.ld, st)) ||
+        (rc = upload(keep[2 * h + 1], c.phases, (size_t)c.n, st)))
+      return rc;
+    dcomp[h] = xgpu_component{keep[2 * h].as<double>(), keep[2 * h + 1].as<double>(), c.ld, c.n,
+                              c.shift};
+  }
+  Dev de, dneg, dbg, dout;
+  if ((rc = upload(de, phases, B + 1, st)) || (rc = upload(dneg, allow_negative, H, st)) ||
+      (background && (rc = upload(dbg, background, K * B, st))) ||
+      (rc = dalloc(dout, K * B * 8, st)))
+    return rc;
+  rc = xgpu_expected_counts_batch(1, (int)K, (int)B, (int)H, exposure_time, de.as<double>(),
+                                  dcomp.data(), dneg.as<int32_t>(),
+                                  background ? dbg.as<double>() : nullptr, dout.as<double>(), st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, dout.p, K * B * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_phase_integrator(double exposure_time, size_t n_edges, const double *phases, size_t rows,
+                          size_t n_phases, const double *signal, const double *signal_phases,
+                          double phase_shift, int allow_negative, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (rows == 0 || n_edges < 2) return 0;
+  if (n_phases < 5) return fail_msg("the signal needs at least five phases (Akima spline)");
+  const size_t B = n_edges - 1;
+  Dev de, ds, dp, dout;
+  if ((rc = upload(de, phases, n_edges, st)) || (rc = upload(ds, signal, rows * n_phases, st)) ||
+      (rc = upload(dp, signal_phases, n_phases, st)) || (rc = dalloc(dout, rows * B * 8, st)))
+    return rc;
+  xg::PhaseIntArgs a{(int64_t)rows, (int)n_phases, (int)B, exposure_time, phase_shift,
+                     allow_negative ? 1 : 0, de.as<double>(), ds.as<double>(), dp.as<double>(),
+                     dout.as<double>()};
+  xg::launch_phase_integrator(a, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout.p, rows * B * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_poisson(size_t n, const double *mean, uint64_t seed, uint64_t offset, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (n == 0) return 0;
+  Dev dm, dout, df;
+  if ((rc = upload(dm, mean, n, st)) || (rc = dalloc(dout, n * 8, st)) ||
+      (rc = dalloc(df, 16, st)))
+    return rc;
+  CK(cudaMemsetAsync(df.p, 0, 4, st));
+  if ((rc = xgpu_poisson_batch((int64_t)n, dm.as<double>(), dout.as<double>(), seed, offset,
+                               df.as<int32_t>(), st)))
+    return rc;
+  int32_t hit_bound = 0;
+  CK(cudaMemcpyAsync(out, dout.p, n * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&hit_bound, df.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return hit_bound ? 1 : 0;
+}
+
 }  // extern "C"

@@ -216,6 +216,29 @@ __device__ __forceinline__ int periodic_chord(int j, int n) {
 }
 
 
+// integral of the Akima-periodic interpolant through (x[i], y[i]) over [lo, hi]
+__device__ inline double akima_periodic_integral(const double *x, const double *y, int n, double lo,
+                                          double hi) {
+  if (lo > hi || lo < x[0] || hi > x[n - 1]) return nan("");
+  if (lo == hi) return 0.0;
+  auto chord = [&](int j) -> double {
+    int q = periodic_chord(j, n);
+    return (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
+  };
+  int ia = locate(x, n, lo), ib = locate(x, n, hi);
+  double acc = 0.0;
+  for (int i = ia; i <= ib; i++) {
+    double h = x[i + 1] - x[i];
+    double k1, k2, k3;
+    akima_piece(chord(i - 2), chord(i - 1), chord(i), chord(i + 1), chord(i + 2), h, k1, k2, k3);
+    double u = (i == ia) ? lo - x[i] : 0.0;
+    double w = (i == ib) ? hi - x[i] : h;
+    acc += piece_integral(y[i], k1, k2, k3, u, w);
+  }
+  return acc;
+}
+
+
 // ---------------------------------------------------------------------
 // Double-float numbers: an unevaluated sum h + l of two floats, about 48
 // significant bits (~4e-15 relative per operation).  On this GPU an FP32

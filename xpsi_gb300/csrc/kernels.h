@@ -195,6 +195,38 @@ struct GeneralArgs {
 };
 size_t general_geometry_smem_bytes(int N_R, int N_L);
 int launch_general(const GeneralArgs &a, cudaStream_t st);
+
+// ---- synthesis: expected counts, phase integration, Poisson draws ----------
+struct CompDesc {             // one component signal of one set
+  const double *signal;       // [K][ld] count rates
+  const double *phases;       // [n] phases in cycles on [0, 1]
+  int64_t ld;
+  int n;
+  double shift;               // phase shift in cycles
+};
+struct ExpectedArgs {
+  int n_sets, K, B, H;
+  double exposure;
+  const double *phase_edges;  // [B + 1]
+  const CompDesc *comps;      // [n_sets][H]
+  const int32_t *allow_negative;  // [H]
+  const double *background;   // [K][B] count rates, or null
+  double *out;                // [n_sets][K][B]
+};
+void launch_expected_counts(const ExpectedArgs &a, cudaStream_t st);
+struct PhaseIntArgs {
+  int64_t rows;
+  int n_phases, B;
+  double exposure, shift;
+  int allow_negative;
+  const double *phase_edges;    // [B + 1]
+  const double *signal;         // [rows][n_phases]
+  const double *signal_phases;  // [n_phases]
+  double *out;                  // [rows][B]
+};
+void launch_phase_integrator(const PhaseIntArgs &a, cudaStream_t st);
+void launch_poisson(int64_t n, const double *mean, double *out, uint64_t seed, uint64_t offset,
+                    int32_t *fail, cudaStream_t st);
 int launch_elsewhere(const ElsewhereArgs &a, cudaStream_t st);
 
 }  // namespace xg

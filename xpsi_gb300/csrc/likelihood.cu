@@ -33,28 +33,6 @@ struct WarpSmem {
   double al[kQagLimit], bl[kQagLimit], rl[kQagLimit], el[kQagLimit];
 };
 
-// integral of the Akima-periodic interpolant through (x[i], y[i]) over [lo, hi]
-__device__ double akima_periodic_integral(const double *x, const double *y, int n, double lo,
-                                          double hi) {
-  if (lo > hi || lo < x[0] || hi > x[n - 1]) return nan("");
-  if (lo == hi) return 0.0;
-  auto chord = [&](int j) -> double {
-    int q = periodic_chord(j, n);
-    return (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
-  };
-  int ia = locate(x, n, lo), ib = locate(x, n, hi);
-  double acc = 0.0;
-  for (int i = ia; i <= ib; i++) {
-    double h = x[i + 1] - x[i];
-    double k1, k2, k3;
-    akima_piece(chord(i - 2), chord(i - 1), chord(i), chord(i + 1), chord(i + 2), h, k1, k2, k3);
-    double u = (i == ia) ? lo - x[i] : 0.0;
-    double w = (i == ib) ? hi - x[i] : h;
-    acc += piece_integral(y[i], k1, k2, k3, u, w);
-  }
-  return acc;
-}
-
 struct Marg {
   int n;
   double SCALE, T, A;

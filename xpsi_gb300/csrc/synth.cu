@@ -1,0 +1,213 @@
+// synth.cu -- data synthesis on the GPU: expected counts per (channel, phase
+// bin) and their Poisson realisations, replacing
+//   xpsi/tools/compute_expected_counts.pyx:66-197 (compute_expected_counts),
+//   xpsi/tools/phase_integrator.pyx:23-121 (phase_integrator) and the draws of
+//   xpsi/tools/synthesise.pyx:35-276 (synthesise_exposure,
+//   synthesise_given_total_count_number).
+//
+// Phase-bin integrals: one warp per (signal, channel) row, lanes over the
+// bins, each bin the exact integral of the Akima-periodic interpolant of the
+// row over the phase-shifted bin (wrapped into [0, 1)), with the reference's
+// positive-part rules.
+//
+// Poisson draws: element i of a launch with key `seed` draws from the
+// counter-based generator Philox4x32-10 (Salmon, Moraes, Dror and Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11) at counter
+// (offset + i, attempt), so a draw depends only on (seed, offset + i) and not
+// on how elements are batched.  Means below 10 are inverted by sequential
+// search of the cumulative distribution; larger means use the transformed
+// rejection with squeeze of Hormann ("The transformed rejection method for
+// generating Poisson random variables", Insurance: Mathematics and Economics
+// 12, 1993), PTRS.  Every loop is bounded.  The realisations follow the
+// Poisson law as GSL's gsl_ran_poisson does; they are not GSL's stream.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int kSynWarps = 4;
+
+// ---------------------------------------------------------------- Philox
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox_round(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+  const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+  return U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+}
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    c = philox_round(c, k0, k1);
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// uniform doubles in [0, 1) with 53 random bits, two per generator call
+struct UniformStream {
+  uint64_t elem;
+  uint32_t k0, k1, n;
+  double spare;
+  bool have;
+  __device__ double next() {
+    if (have) {
+      have = false;
+      return spare;
+    }
+    const U4 r = philox4x32_10(U4{(uint32_t)elem, (uint32_t)(elem >> 32), n, 0x5eed5eedu}, k0, k1);
+    n++;
+    const double s = 1.0 / 9007199254740992.0;  // 2^-53
+    const double a = (double)(((uint64_t)(r.x >> 5) << 26) | (r.y >> 6)) * s;
+    spare = (double)(((uint64_t)(r.z >> 5) << 26) | (r.w >> 6)) * s;
+    have = true;
+    return a;
+  }
+};
+
+__device__ double poisson_draw(double mu, UniformStream &u, int *fail) {
+  if (!(mu > 0.0)) return (mu == 0.0) ? 0.0 : nan("");
+  if (mu < 10.0) {
+    // inversion: the smallest k with F(k) >= U
+    const double U = u.next();
+    double p = exp(-mu), F = p;
+    int k = 0;
+    while (U > F && k < 1000) {
+      k++;
+      p *= mu / (double)k;
+      F += p;
+    }
+    return (double)k;
+  }
+  // PTRS (Hormann 1993): transformed rejection with squeeze
+  const double slam = sqrt(mu), loglam = log(mu);
+  const double b = 0.931 + 2.53 * slam;
+  const double a = -0.059 + 0.02483 * b;
+  const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int attempt = 0; attempt < 10000; attempt++) {
+    const double U = u.next() - 0.5;
+    const double V = u.next();
+    const double us = 0.5 - fabs(U);
+    const double k = floor((2.0 * a / us + b) * U + mu + 0.43);
+    if (us >= 0.07 && V <= vr) return k;
+    if (k < 0.0 || (us < 0.013 && V > us)) continue;
+    if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -mu + k * loglam - lgamma(k + 1.0))
+      return k;
+  }
+  *fail = 1;
+  return floor(mu + 0.5);
+}
+
+__global__ void poisson_kernel(int64_t n, const double *mean, double *out, uint64_t seed,
+                               uint64_t offset, int32_t *fail) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    UniformStream u{offset + (uint64_t)i, (uint32_t)seed, (uint32_t)(seed >> 32), 0u, 0.0, false};
+    int f = 0;
+    out[i] = poisson_draw(mean[i], u, &f);
+    if (f) atomicExch(fail, 1);
+  }
+}
+
+// ------------------------------------------------- phase-bin integrals
+// one bin of one component (compute_expected_counts.pyx:127-162 with
+// `exact_cycle` false; phase_integrator.pyx:93-115 with it true, where a full
+// cycle is recognised by exact equality and the first branch assigns)
+__device__ __forceinline__ double bin_integral(const double *ph, const double *y, int n, double a,
+                                               double b, bool neg, bool exact_cycle) {
+  const bool full = exact_cycle ? (b - a == 1.0) : are_equal(b - a, 1.0);
+  if (full) {
+    a = 0.0;
+    b = 1.0;
+  } else {
+    a -= floor(a);
+    b -= floor(b);
+  }
+  double s = 0.0;
+  if (a < b) {
+    const double v = akima_periodic_integral(ph, y, n, a, b);
+    if (v > 0.0 || neg) s += v;
+  } else {
+    double v = akima_periodic_integral(ph, y, n, a, 1.0);
+    if (v > 0.0 || neg) s += v;
+    v = akima_periodic_integral(ph, y, n, 0.0, b);
+    if (v > 0.0 || neg) s += v;
+  }
+  return s;
+}
+
+// expected counts of one (set, channel) row: exposure x (sum over components
+// of the star rate, clamped at zero, + background rate)
+__global__ void __launch_bounds__(32 * kSynWarps) expected_counts_kernel(ExpectedArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * kSynWarps + (threadIdx.x >> 5);
+  if (gw >= (int64_t)a.n_sets * a.K) return;
+  const int s = (int)(gw / a.K), ch = (int)(gw - (int64_t)s * a.K);
+  for (int j = lane; j < a.B; j += 32) {
+    double st = 0.0;
+    for (int h = 0; h < a.H; h++) {
+      const CompDesc c = a.comps[(int64_t)s * a.H + h];
+      const double *row = c.signal + (int64_t)ch * c.ld;
+      if (c.n > 1) {
+        st += bin_integral(c.phases, row, c.n, a.phase_edges[j] + c.shift,
+                           a.phase_edges[j + 1] + c.shift, a.allow_negative[h] == 1, false);
+      } else if (j == 0) {
+        st = row[0];  // :161-162
+      }
+    }
+    if (st < 0.0) st = 0.0;  // :164-166
+    const double bg = a.background ? a.background[(int64_t)ch * a.B + j] : 0.0;
+    double e = st + bg;
+    e *= a.exposure;
+    a.out[((int64_t)s * a.K + ch) * a.B + j] = e;
+  }
+}
+
+// phase_integrator.pyx:23-121 for rows of one signal
+__global__ void __launch_bounds__(32 * kSynWarps) phase_integrator_kernel(PhaseIntArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * kSynWarps + (threadIdx.x >> 5);
+  if (row >= a.rows) return;
+  const double *y = a.signal + row * a.n_phases;
+  for (int j = lane; j < a.B; j += 32) {
+    double v = bin_integral(a.signal_phases, y, a.n_phases, a.phase_edges[j] + a.shift,
+                            a.phase_edges[j + 1] + a.shift, a.allow_negative, true);
+    v *= a.exposure;
+    a.out[row * a.B + j] = v;
+  }
+}
+
+}  // namespace
+
+void launch_expected_counts(const ExpectedArgs &a, cudaStream_t st) {
+  const int64_t warps = (int64_t)a.n_sets * a.K;
+  if (warps <= 0) return;
+  expected_counts_kernel<<<(unsigned)((warps + kSynWarps - 1) / kSynWarps), 32 * kSynWarps, 0,
+                           st>>>(a);
+}
+
+void launch_phase_integrator(const PhaseIntArgs &a, cudaStream_t st) {
+  if (a.rows <= 0) return;
+  phase_integrator_kernel<<<(unsigned)((a.rows + kSynWarps - 1) / kSynWarps), 32 * kSynWarps, 0,
+                            st>>>(a);
+}
+
+void launch_poisson(int64_t n, const double *mean, double *out, uint64_t seed, uint64_t offset,
+                    int32_t *fail, cudaStream_t st) {
+  if (n <= 0) return;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+  poisson_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, mean, out, seed, offset, fail);
+}
+
+}  // namespace xg
