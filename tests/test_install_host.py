@@ -1,0 +1,37 @@
+"""xpsi_gb300.install rebinds the native callables inside the reference
+package (imported from its checkout through oracle/ref_harness.py; skipped
+where the checkout is absent).  CPU only: no compute call is made."""
+import pytest
+
+from oracle import ref_harness as H
+
+pytestmark = pytest.mark.skipif(not H.available(), reason="reference checkout not present")
+
+
+def test_install_rebinds_path_callables():
+    import importlib
+    xpsi = H.load()
+    import xpsi_gb300
+    from xpsi_gb300.cellmesh import (global_mesh, integrator, integrator_for_azimuthal_invariance,
+                                     integrator_for_time_invariance, rays)
+    from xpsi_gb300.tools import energy_integrator, phase_integrator, synthesise
+    done = xpsi_gb300.install(xpsi)
+    assert "xpsi.Elsewhere._integrator" in done
+    E = importlib.import_module("xpsi.Elsewhere")
+    assert E._integrator is integrator_for_time_invariance.integrate
+    assert E._construct_closed_cellMesh is global_mesh.construct_closed_cellMesh
+    assert E._compute_rays is rays.compute_rays
+    S = importlib.import_module("xpsi.Signal")
+    assert S.energy_integrator is energy_integrator.energy_integrator
+    assert S.phase_integrator is phase_integrator.phase_integrator
+    assert S._synthesise_expo is synthesise.synthesise_exposure
+    assert S._synthesise_given_total_count_number is synthesise.synthesise_given_total_count_number
+    assert importlib.import_module("xpsi.HotRegion")._compute_rays is rays.compute_rays
+    # the symmetry setter picks the GPU integrators
+    HR = importlib.import_module("xpsi.HotRegion").HotRegion
+    hr = object.__new__(HR)
+    hr._split = False
+    hr.symmetry = True
+    assert hr._integrator is integrator_for_azimuthal_invariance.integrate
+    hr.symmetry = False
+    assert hr._integrator is integrator.integrate
