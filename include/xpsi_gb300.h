@@ -88,6 +88,28 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination,
                    int atm_ext, const xgpu_atmos4d *atmos, int else_atm_ext,
                    int image_order_limit, double *flux);
 
+/* Replaces xpsi.cellmesh.integratorIQU_for_azimuthal_invariance.integrate
+ * (xpsi/cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743), the
+ * Stokes integrator of HotRegion.integrate_stokes: arguments as
+ * xgpu_integrate, atm_ext 1 (blackbody, Q = U = 0) or 3 (burst blackbody,
+ * hot_BB_burst.pyx); outputs flux_I, flux_Q, flux_U [N_E][N_P].  Returns 0
+ * (SUCCESS) or 1 (ERROR), < 0 on a usage or CUDA failure. */
+int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination,
+                          size_t S0, size_t S1, const double *cellArea,
+                          const double *radialCoords_of_parallels,
+                          const double *r_s_over_r, const double *theta,
+                          const double *phi, const double *srcCellParams,
+                          size_t n_params, const int32_t *cell_radiates,
+                          const double *correction_srcCellParams,
+                          size_t n_correction, size_t N_R,
+                          const double *deflection, const double *cos_alpha,
+                          const double *lag, const double *maxDeflection,
+                          const double *cos_gammaArray, size_t N_E,
+                          const double *energies, size_t N_L,
+                          const double *leaves, size_t N_P, const double *phases,
+                          int atm_ext, int else_atm_ext, int image_order_limit,
+                          double *flux_I, double *flux_Q, double *flux_U);
+
 /* Replaces xpsi.cellmesh.integrator.integrate (xpsi/cellmesh/integrator.pyx:
  * 48-667), the general integrator of HotRegion(symmetry=False) for source
  * parameters that vary from cell to cell.  Same arguments as xgpu_integrate

@@ -39,6 +39,7 @@ MODULES = [
     "cellmesh.polar_mesh", "cellmesh.rays", "cellmesh.integrator",
     "cellmesh.integrator_for_azimuthal_invariance",
     "cellmesh.global_mesh", "cellmesh.integrator_for_time_invariance",
+    "cellmesh.integratorIQU_for_azimuthal_invariance",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
 ]

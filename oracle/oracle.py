@@ -61,9 +61,9 @@ def lib():
                 C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                 C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P, P, C.c_size_t,
                 C.c_size_t, P, P, P, P, P, C.c_size_t, P, C.c_size_t, P,
-                C.c_size_t, P, C.c_int, P, C.c_int, P]
+                C.c_size_t, P, C.c_int, P, C.c_int, P, P, P]
             L.xo_integrate_general.restype = C.c_int
-            L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)
+            L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)[:-2]
             L.xo_integrate_time_invariant.restype = C.c_int
             L.xo_integrate_time_invariant.argtypes = [
                 C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -153,11 +153,53 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
         P.size, _p(P), int(hot_atm_ext),
         C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
-        int(image_order_limit or 0), _p(out))
+        int(image_order_limit or 0), _p(out), None, None)
     del keep
     if status != 0:
         return (1, None)
     return (0, out)
+
+
+def integrate_iqu(numThreads, R, omega, r_s, inclination, cellArea,
+                  radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                  CELL_RADIATES, correction_srcCellParams, numRays, deflection, cos_alpha, lag,
+                  maxDeflection, cos_gammaArray, energies, leaves, phases, hot_atmosphere_I,
+                  hot_atmosphere_Q, elsewhere_atmosphere, hot_atm_ext, else_atm_ext, beam_opt,
+                  image_order_limit=None, R_in=1e6):
+    """integratorIQU_for_azimuthal_invariance.integrate (:68-743):
+    (0, flux_I, flux_Q, flux_U) or (1, None) for the blackbody (1), Num4D (2)
+    and burst blackbody (3) atmospheres."""
+    if beam_opt != 0 or R_in < 1e6:
+        raise NotImplementedError("oracle covers beam_opt 0 without a disk")
+    if int(hot_atm_ext) not in (1, 2, 3):
+        raise NotImplementedError("oracle covers atmospheres 1, 2 and 3")
+    corr = None
+    if correction_srcCellParams is not None:
+        if int(else_atm_ext) != 1:
+            raise NotImplementedError("oracle corrects for a blackbody elsewhere only")
+        corr = _c(correction_srcCellParams)
+    A = _c(cellArea); S0, S1 = A.shape
+    par = _c(srcCellParams)
+    rad = _c(CELL_RADIATES, np.int32)
+    E = _c(energies); Lv = _c(leaves); P = _c(phases)
+    out = [np.zeros((E.size, P.size)) for _ in range(3)]
+    st, keep = _atmos_struct(hot_atmosphere_I if int(hot_atm_ext) == 2 else ())
+    arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
+            _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
+            _c(cos_gammaArray)]
+    status = lib().xo_integrate(
+        int(numThreads), float(R), float(omega), float(r_s), float(inclination),
+        S0, S1, _p(A), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
+        _p(par), par.shape[2], _p(rad), _p(corr) if corr is not None else None,
+        corr.shape[2] if corr is not None else 0, int(numRays), _p(arrs[4]), _p(arrs[5]),
+        _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
+        P.size, _p(P), int(hot_atm_ext),
+        C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
+        int(image_order_limit or 0), _p(out[0]), _p(out[1]), _p(out[2]))
+    del keep
+    if status != 0:
+        return (1, None)
+    return (0, out[0], out[1], out[2])
 
 
 def integrate_general(numThreads, R, omega, r_s, inclination, cellArea,

@@ -12,7 +12,10 @@
  *
  * Stages:
  *   xo_compute_rays          cellmesh/rays.pyx:249-390 (+ rayIntegrator :90-247)
- *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665
+ *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665,
+ *                            with Stokes Q and U as
+ *                            cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743
+ *                            (atmospheres 1, 2, 3 = hot_BB_burst.pyx)
  *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
  *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
@@ -330,6 +333,29 @@ static double eval_num4d(const xo_atmos4d *A, num4d_state *st, double E,
   return I * pow(10.0, 3.0 * v[0]);
 }
 
+/* cellmesh/common_functions.pyx:7-66: the polarisation angle in the oblate
+ * Schwarzschild approximation (Loktev et al. 2020) */
+static double pol_angle(double leaf, double sin_psi, double cos_psi, double sin_alpha,
+                        double cos_alpha, double sin_th, double cos_th, double sin_i,
+                        double cos_i, double sin_gamma, double cos_gamma, double Grav_z,
+                        double mu, double eta, double beta, double Lorentz, double cos_xi) {
+  double sin_chi_0 = -sin_th * sin(leaf);
+  double cos_chi_0 = sin_i * cos_th - sin_th * cos_i * cos(leaf);
+  double chi_0 = atan2(sin_chi_0, cos_chi_0);
+  double sa_over_sp = !are_equal(sin_psi, 0.0) ? sin_alpha / sin_psi : Grav_z;
+  double sin_chi_1 = sin_gamma * sin_i * sin(leaf) * sa_over_sp;
+  double cos_chi_1 = cos_gamma - cos_alpha * mu;
+  double chi_1 = atan2(sin_chi_1, cos_chi_1);
+  double sin_lambda = sin_th * cos_gamma - sin_gamma * cos_th;
+  double cos_lambda = cos_th * cos_gamma + sin_th * sin_gamma;
+  double cos_eps = sa_over_sp * (cos_i * sin_lambda - sin_i * cos_lambda * cos(leaf) +
+                                 cos_psi * sin_gamma) - cos_alpha * sin_gamma;
+  double sin_chi_p = cos_eps * eta * mu * beta / Lorentz;
+  double cos_chi_p = (1. - pow(mu, 2.0) / (1. + beta * cos_xi));
+  double chi_p = atan2(sin_chi_p, cos_chi_p);
+  return chi_0 + chi_1 + chi_p;
+}
+
 /* ================================================================== */
 /* cell-mesh integrator, azimuthal invariance                         */
 /* ================================================================== */
@@ -345,18 +371,22 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                  size_t N_E, const double *energies, size_t N_L,
                  const double *leaves, size_t N_P, const double *phases,
                  int atm_ext, const xo_atmos4d *atmos, int image_order_limit,
-                 double *flux) {
+                 double *flux, double *flux_Q, double *flux_U) {
   (void)R;
   /* the elsewhere correction (:257-261, :469-478): a blackbody elsewhere's
    * intensity at correction[i, J] is subtracted from every profile value and
    * every interpolated value is added, negative or not (:593-594) */
   const int perform_correction = correction != NULL;
+  /* Stokes Q and U (integratorIQU_for_azimuthal_invariance.pyx:68-743) when
+   * flux_Q and flux_U are given: profiles Q cos 2chi and Q sin 2chi beside I,
+   * added wherever I is (:646-650) */
+  const int ns = (flux_Q != NULL && flux_U != NULL) ? 3 : 1;
   const double sin_i = sin(inclination), cos_i = cos(inclination);
   const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
   const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
   int nt = n_threads > 0 ? n_threads : 1;
   int terminate_any = 0;
-  double *priv = (double *)calloc((size_t)nt * N_E * N_P, sizeof(double));
+  double *priv = (double *)calloc((size_t)nt * ns * N_E * N_P, sizeof(double));
   /* integrator_for_azimuthal_invariance.pyx:213-226 */
   double *cos_defl = (double *)malloc(S0 * N_R * sizeof(double));
   double *ca_alt = (double *)malloc(S0 * N_R * sizeof(double));
@@ -373,14 +403,19 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
 #ifdef _OPENMP
     T = omp_get_thread_num();
 #endif
-    double *pflux = priv + (size_t)T * N_E * N_P;
+    double *pflux = priv + (size_t)T * ns * N_E * N_P;
     gsl_interp_accel *acc_a = gsl_interp_accel_alloc(), *acc_alt = gsl_interp_accel_alloc();
     gsl_interp_accel *acc_l = gsl_interp_accel_alloc(), *acc_p = gsl_interp_accel_alloc();
+    gsl_interp_accel *acc_q = gsl_interp_accel_alloc(), *acc_u = gsl_interp_accel_alloc();
     gsl_interp *ia = gsl_interp_alloc(gsl_interp_steffen, N_R);
     gsl_interp *il = gsl_interp_alloc(gsl_interp_steffen, N_R);
     gsl_interp *ip = gsl_interp_alloc(gsl_interp_akima_periodic, N_L);
+    gsl_interp *iq = gsl_interp_alloc(gsl_interp_akima_periodic, N_L);
+    gsl_interp *iu = gsl_interp_alloc(gsl_interp_akima_periodic, N_L);
     double *PHASE = (double *)malloc(N_L * sizeof(double));
-    double *PROFILE = (double *)malloc(N_E * N_L * sizeof(double));
+    /* ns blocks of [N_E][N_L]: I, then Q and U */
+    double *PROFILE = (double *)malloc((size_t)ns * N_E * N_L * sizeof(double));
+    const size_t NR = (size_t)ns * N_E;
     num4d_state nst;
     if (atm_ext == 2) num4d_reset(&nst, atmos);
     int terminate = 0;
@@ -477,29 +512,50 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                 double ABB = mu * eta;
                 double GEOM = mu * fabs(deriv) * Grav_z * eta * eta * eta / superlum;
                 PHASE[kdx] = leaves[kdx] + plag;
+                double c2chi = 0.0, s2chi = 0.0;
+                if (ns == 3) {
+                  double cos_xi = are_equal(psi, 0.0) ? 0.0
+                                                      : sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
+                  double chi = pol_angle(leaves[kdx], sin_psi, cos_psi, sin_alpha, cos_a, sin_th,
+                                         cos_th, sin_i, cos_i, sin_gamma, cos_gamma, Grav_z, mu,
+                                         eta, beta, Lorentz, cos_xi);
+                  c2chi = cos(2 * chi);
+                  s2chi = sin(2 * chi);
+                }
                 for (size_t p = 0; p < N_E; p++) {
                   double Ep = energies[p] / Z;
-                  double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
-                                              : eval_bb(Ep, VEC);
+                  double I_E, Q_E = 0.0;
+                  if (atm_ext == 2) {
+                    I_E = eval_num4d(atmos, &nst, Ep, ABB, VEC);
+                  } else if (atm_ext == 3) { /* hot_BB_burst.pyx: I and Q */
+                    I_E = eval_bb(Ep, VEC) * (0.421 + 0.868 * ABB);
+                    Q_E = (0.1171 * (ABB - 1.) / (1. + 3.582 * ABB)) * I_E;
+                  } else {
+                    I_E = eval_bb(Ep, VEC);
+                  }
                   double corr = 0.0;
                   if (perform_correction)
                     corr = eval_bb(Ep, correction + (i * S1 + J) * n_correction) *
                            (kErg * kPlanck);
                   PROFILE[p * N_L + kdx] = (I_E * norm - corr) * GEOM;
+                  if (ns == 3) {
+                    PROFILE[(N_E + p) * N_L + kdx] = ((Q_E * c2chi) * norm) * GEOM;
+                    PROFILE[(2 * N_E + p) * N_L + kdx] = ((Q_E * s2chi) * norm) * GEOM;
+                  }
                 }
               }
             }
             if (k == 0) {
               PHASE[N_L - 1] = PHASE[0] + kTwoPi;
-              for (size_t p = 0; p < N_E; p++) PROFILE[p * N_L + N_L - 1] = PROFILE[p * N_L];
+              for (size_t p = 0; p < NR; p++) PROFILE[p * N_L + N_L - 1] = PROFILE[p * N_L];
             } else if (k > 0 && InvisFlag == 2) {
               InvisStep = leaves[k] / (double)k;
               for (size_t m = N_L - k; m < N_L; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
-              for (size_t p = 0; p < N_E; p++)
+              for (size_t p = 0; p < NR; p++)
                 for (size_t m = N_L - k; m < N_L; m++) PROFILE[p * N_L + m] = 0.0;
               PHASE[0] = PHASE[N_L - 1] - kTwoPi;
               for (size_t m = 1; m < k; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
-              for (size_t p = 0; p < N_E; p++) {
+              for (size_t p = 0; p < NR; p++) {
                 PROFILE[p * N_L] = 0.0;
                 for (size_t m = 1; m < k; m++) PROFILE[p * N_L + m] = 0.0;
               }
@@ -517,7 +573,7 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
               InvisStep = PHASE[N_L - k] - PHASE[k - 1];
               InvisStep = InvisStep / (double)(N_L - 2 * k + 1);
               for (size_t m = k; m < N_L - k; m++) PHASE[m] = PHASE[m - 1] + InvisStep;
-              for (size_t p = 0; p < N_E; p++)
+              for (size_t p = 0; p < NR; p++)
                 for (size_t m = k; m < N_L - k; m++) PROFILE[p * N_L + m] = 0.0;
               InvisFlag = 1;
               InvisPhase = k;
@@ -531,8 +587,15 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
         if (terminate) break;
         for (size_t p = 0; p < N_E && !terminate; p++) {
           const double *prof = PROFILE + p * N_L;
+          const double *profq = PROFILE + (N_E + p) * N_L, *profu = PROFILE + (2 * N_E + p) * N_L;
           gsl_interp_accel_reset(acc_p);
           gsl_interp_init(ip, PHASE, prof, N_L);
+          if (ns == 3) {
+            gsl_interp_accel_reset(acc_q);
+            gsl_interp_init(iq, PHASE, profq, N_L);
+            gsl_interp_accel_reset(acc_u);
+            gsl_interp_init(iu, PHASE, profu, N_L);
+          }
           for (j = 0; j < S1 && !terminate; j++) {
             if (radiates[i * S1 + j] != 1) continue;
             double shift = phi[i * S1 + j];
@@ -546,7 +609,13 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
               }
               if (x < ip->xmin || x > ip->xmax) { terminate = 1; break; }
               double s = gsl_interp_eval(ip, PHASE, prof, x, acc_p);
-              if (s > 0.0 || perform_correction) pflux[p * N_P + k] += A * s;
+              if (s > 0.0 || perform_correction) {
+                pflux[p * N_P + k] += A * s;
+                if (ns == 3) {
+                  pflux[(N_E + p) * N_P + k] += A * gsl_interp_eval(iq, PHASE, profq, x, acc_q);
+                  pflux[(2 * N_E + p) * N_P + k] += A * gsl_interp_eval(iu, PHASE, profu, x, acc_u);
+                }
+              }
             }
           }
         }
@@ -556,18 +625,23 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
     }
     if (terminate) terminate_any = 1;
     gsl_interp_free(ia); gsl_interp_free(il); gsl_interp_free(ip);
+    gsl_interp_free(iq); gsl_interp_free(iu);
     gsl_interp_accel_free(acc_a); gsl_interp_accel_free(acc_alt);
     gsl_interp_accel_free(acc_l); gsl_interp_accel_free(acc_p);
+    gsl_interp_accel_free(acc_q); gsl_interp_accel_free(acc_u);
     free(PHASE); free(PROFILE);
   }
   gsl_set_error_handler(prev);
-  /* :605-612 */
-  for (size_t p = 0; p < N_E; p++)
-    for (size_t k = 0; k < N_P; k++) {
-      double s = 0.0;
-      for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_E * N_P + p * N_P + k];
-      flux[p * N_P + k] = s / (energies[p] * kKeV);
-    }
+  /* :605-612 (IQU: :715-725) */
+  double *outs[3] = {flux, flux_Q, flux_U};
+  for (int c = 0; c < ns; c++)
+    for (size_t p = 0; p < N_E; p++)
+      for (size_t k = 0; k < N_P; k++) {
+        double s = 0.0;
+        for (int T = 0; T < nt; T++)
+          s += priv[(size_t)T * ns * N_E * N_P + ((size_t)c * N_E + p) * N_P + k];
+        outs[c][p * N_P + k] = s / (energies[p] * kKeV);
+      }
   free(priv); free(cos_defl); free(ca_alt);
   return terminate_any ? 1 : 0;
 }

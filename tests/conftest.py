@@ -124,3 +124,23 @@ def row_rel_floor(a, b, floor=1e-15):
     scale = np.maximum(np.max(np.abs(b), axis=1, keepdims=True), floor * peak)
     scale = np.where(scale > 0, scale, 1e300)
     return float(np.max(np.abs(a - b) / scale))
+
+
+# the Stokes fixture's cases: (base fixture, atm_ext, corrected)
+STOKES_CASES = (("config1", 3, False), ("num4d_omit", 3, False), ("config1", 1, True))
+
+
+def stokes_args(golden, case, ext, corrected, image_order_limit=None):
+    """Arguments of integratorIQU_for_azimuthal_invariance.integrate for a
+    stokes.npz case on its base fixture's mesh and rays."""
+    f = golden(case)
+    z = golden("stokes")
+    tag = "%s_ext%d%s" % (case, ext, "_corrected" if corrected else "")
+    corr = z[tag + "_correction"] if corrected else None
+    iol = image_order_limit if image_order_limit is not None else (
+        int(f["image_order_limit"]) or None)
+    return tag, (1, float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+                 f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], f["params"],
+                 f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+                 f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"], f["phases"],
+                 (), (), (), ext, 1 if corrected else None, 0, iol)

@@ -22,6 +22,8 @@ Cases
                  num4d_omit's inputs.
   synthesis      expected counts of the reference's synthesis routines and
                  its phase integrator on config1's folded signal.
+  stokes         the Stokes I/Q/U integrator for the burst blackbody and the
+                 plain blackbody with a correction.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -412,6 +414,38 @@ def synthesis(xpsi):
          phase_integrated_neg=pi_neg)
 
 
+def stokes(xpsi):
+    """The Stokes integrator (integratorIQU_for_azimuthal_invariance.pyx:
+    68-743) on config1's mesh and rays: the burst blackbody (atm_ext 3,
+    hot_BB_burst.pyx: limb-darkened, polarised), also at 600 Hz on
+    num4d_omit's mesh (a fast, oblate star), and the plain blackbody
+    (Q = U = 0) with a blackbody elsewhere's correction."""
+    from xpsi.cellmesh.integratorIQU_for_azimuthal_invariance import integrate
+    out = {}
+    for case, ext, corr_T in (("config1", 3, None), ("num4d_omit", 3, None),
+                              ("config1", 1, 6.0)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        params = np.array(f["params"], copy=True)
+        corr = None
+        if corr_T is not None:
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = corr_T
+            corr[..., 1] = f["effGrav"][:, None]
+        res = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                        float(f["inclination"]), f["cellArea"], f["radius"], f["u"], f["theta"],
+                        f["phi"], params, f["radiates"], corr, int(f["N_R"]), f["deflection"],
+                        f["cos_alpha"], f["lag"], f["maxDeflection"], f["cos_gamma"],
+                        f["energies"], f["leaves"], f["phases"], (), (), (), ext,
+                        1 if corr is not None else None, 0, int(f["image_order_limit"]) or None)
+        assert res[0] == 0
+        tag = "%s_ext%d%s" % (case, ext, "_corrected" if corr is not None else "")
+        out[tag + "_I"], out[tag + "_Q"], out[tag + "_U"] = res[1], res[2], res[3]
+        if corr is not None:
+            out[tag + "_correction"] = corr
+    save("stokes", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -421,6 +455,7 @@ def main():
     elsewhere_correction(xpsi)
     general_integrator(xpsi)
     synthesis(xpsi)
+    stokes(xpsi)
 
 
 if __name__ == "__main__":

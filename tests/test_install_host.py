@@ -13,7 +13,8 @@ def test_install_rebinds_path_callables():
     xpsi = H.load()
     import xpsi_gb300
     from xpsi_gb300.cellmesh import (global_mesh, integrator, integrator_for_azimuthal_invariance,
-                                     integrator_for_time_invariance, rays)
+                                     integrator_for_time_invariance,
+                                     integratorIQU_for_azimuthal_invariance, rays)
     from xpsi_gb300.tools import energy_integrator, phase_integrator, synthesise
     done = xpsi_gb300.install(xpsi)
     assert "xpsi.Elsewhere._integrator" in done
@@ -33,5 +34,6 @@ def test_install_rebinds_path_callables():
     hr._split = False
     hr.symmetry = True
     assert hr._integrator is integrator_for_azimuthal_invariance.integrate
+    assert hr._integratorIQU is integratorIQU_for_azimuthal_invariance.integrate
     hr.symmetry = False
     assert hr._integrator is integrator.integrate

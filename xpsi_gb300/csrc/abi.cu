@@ -451,6 +451,90 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   return status != 0 ? 1 : 0;
 }
 
+int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination, size_t S0,
+                          size_t S1, const double *cellArea, const double *radius,
+                          const double *r_s_over_r, const double *theta, const double *phi,
+                          const double *srcCellParams, size_t n_params, const int32_t *radiates,
+                          const double *correction, size_t n_correction, size_t N_R,
+                          const double *deflection, const double *cos_alpha, const double *lag,
+                          const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                          const double *energies, size_t N_L, const double *leaves, size_t N_P,
+                          const double *phases, int atm_ext, int else_atm_ext,
+                          int image_order_limit, double *flux_I, double *flux_Q,
+                          double *flux_U) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (S0 == 0 || S1 == 0 || N_E == 0 || N_P == 0) return 0;
+  if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
+  if (N_R < 3) return fail_msg("num_rays must be at least 3");
+  if (atm_ext != 1 && atm_ext != 3)
+    return fail_msg("the Stokes integrator takes atm_ext 1 (BB) or 3 (burst BB)");
+  if (n_params < 1) return fail_msg("srcCellParams needs at least 1 parameter per cell");
+  if (correction && else_atm_ext != 1)
+    return fail_msg("the GPU integrator corrects for a blackbody elsewhere only");
+  if (correction && n_correction < 1)
+    return fail_msg("correction vectors need at least 1 parameter per cell");
+  if (xg::stokes_smem_bytes((int)N_L, (int)N_P, (int)N_E, (int)N_R) > 227 * 1024)
+    return fail_msg("num_leaves and num_rays too large for one CTA's shared memory");
+  const size_t cells = S0 * S1;
+  std::vector<double> theta0(S0);
+  for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
+  std::vector<int32_t> row_mesh(S0, 0);
+  Dev dA, drad, du, dth0, dphi, dpar, dR, dD, dCA, dL, dMD, dcg, dE, dLv, dP, dF, dst, drm;
+  Dev dcorr, dmem, dpart;
+  if ((rc = upload(dA, cellArea, cells, st)) || (rc = upload(drad, radius, S0, st)) ||
+      (rc = upload(du, r_s_over_r, S0, st)) || (rc = upload(dth0, theta0.data(), S0, st)) ||
+      (rc = upload(dphi, phi, cells, st)) || (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
+      (rc = upload(dR, radiates, cells, st)) || (rc = upload(dD, deflection, S0 * N_R, st)) ||
+      (rc = upload(dCA, cos_alpha, S0 * N_R, st)) || (rc = upload(dL, lag, S0 * N_R, st)) ||
+      (rc = upload(dMD, maxDeflection, S0, st)) || (rc = upload(dcg, cos_gamma, S0, st)) ||
+      (rc = upload(dE, energies, N_E, st)) || (rc = upload(dLv, leaves, N_L, st)) ||
+      (rc = upload(dP, phases, N_P, st)) || (rc = dalloc(dF, 3 * N_E * N_P * 8, st)) ||
+      (rc = dalloc(dst, 16, st)) || (rc = upload(drm, row_mesh.data(), S0, st)))
+    return rc;
+  if (correction && (rc = upload(dcorr, correction, cells * n_correction, st))) return rc;
+  xg::MemberDesc mesh{(int32_t)S0, (int32_t)S1, 0, 0, omega, inclination, image_order_limit,
+                      atm_ext, 0};
+  if ((rc = upload(dmem, &mesh, 1, st))) return rc;
+  xg::IntegrateArgs a{};
+  a.n_members = 1;
+  a.n_rows = (int64_t)S0;
+  a.members = dmem.as<xg::MemberDesc>();
+  a.row_member = drm.as<int32_t>();
+  a.radius = drad.as<double>(); a.u = du.as<double>(); a.cos_gamma = dcg.as<double>();
+  a.theta0 = dth0.as<double>(); a.maxDeflection = dMD.as<double>();
+  a.deflection = dD.as<double>(); a.cos_alpha = dCA.as<double>(); a.lag = dL.as<double>();
+  a.N_R = (int)N_R;
+  a.cellArea = dA.as<double>(); a.phi = dphi.as<double>(); a.params = dpar.as<double>();
+  a.n_params = (int)n_params; a.radiates = dR.as<int32_t>();
+  a.correction = correction ? dcorr.as<double>() : nullptr;
+  a.n_correction = (int)n_correction;
+  a.N_E = (int)N_E; a.N_L = (int)N_L; a.N_P = (int)N_P;
+  a.energies = dE.as<double>(); a.leaves = dLv.as<double>(); a.phases = dP.as<double>();
+  a.member_status = dst.as<int32_t>();
+  a.flux = dF.as<double>();
+  a.flux_q = a.flux + N_E * N_P;
+  a.flux_u = a.flux_q + N_E * N_P;
+  const size_t np = xg::stokes_partial_doubles(a);
+  if ((rc = dalloc(dpart, np * 8, st))) return rc;
+  CK(cudaMemsetAsync(dpart.p, 0, np * 8, st));
+  CK(cudaMemsetAsync(dst.p, 0, 16, st));
+  a.partial = dpart.as<double>();
+  rc = xg::launch_stokes(a, st);
+  if (rc == -2) return fail_msg("integrator shared memory too large");
+  CK(cudaGetLastError());
+  int32_t status = 0;
+  CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux_I, a.flux, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux_Q, a.flux_q, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(flux_U, a.flux_u, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return status != 0 ? 1 : 0;
+}
+
 int xgpu_integrate_general(double R, double omega, double r_s, double inclination, size_t S0,
                            size_t S1, const double *cellArea, const double *radius,
                            const double *r_s_over_r, const double *theta, const double *phi,

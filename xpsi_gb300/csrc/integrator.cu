@@ -69,8 +69,29 @@ struct GeoSmem {
   double *lzs;  // [N_L] log10(Z) + log10(E_eff) per leaf (FP64 path, Num4D)
   int *sc_exp;  // [EC] binary exponent of the largest |profile value| per energy row
   DF *ih, *ih2;  // [N_L] 1/h and 1/h^2 of the phase intervals (FP64 path)
+  double *c2chi = nullptr, *s2chi = nullptr;  // [N_L] cos, sin of twice the polarisation
+                                              // angle (Stokes kernel only)
 };
 
+
+// the polarisation angle in the oblate Schwarzschild approximation (Loktev
+// et al. 2020), cellmesh/common_functions.pyx:7-66
+__device__ double pol_angle(double leaf, double sin_psi, double cos_psi, double sin_alpha,
+                            double cos_alpha, double sin_th, double cos_th, double sin_i,
+                            double cos_i, double sin_gamma, double cos_gamma, double Grav_z,
+                            double mu, double eta, double beta, double Lorentz, double cos_xi) {
+  const double chi_0 = atan2(-sin_th * sin(leaf), sin_i * cos_th - sin_th * cos_i * cos(leaf));
+  const double sa_over_sp = !are_equal(sin_psi, 0.0) ? sin_alpha / sin_psi : Grav_z;
+  const double chi_1 = atan2(sin_gamma * sin_i * sin(leaf) * sa_over_sp,
+                             cos_gamma - cos_alpha * mu);
+  const double sin_lambda = sin_th * cos_gamma - sin_gamma * cos_th;
+  const double cos_lambda = cos_th * cos_gamma + sin_th * sin_gamma;
+  const double cos_eps = sa_over_sp * (cos_i * sin_lambda - sin_i * cos_lambda * cos(leaf) +
+                                       cos_psi * sin_gamma) - cos_alpha * sin_gamma;
+  const double chi_p = atan2(cos_eps * eta * mu * beta / Lorentz,
+                             (1. - mu * mu / (1. + beta * cos_xi)));
+  return chi_0 + chi_1 + chi_p;
+}
 
 // per-leaf geometry, integrator_for_azimuthal_invariance.pyx:342-441
 __device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_lim,
@@ -125,9 +146,9 @@ __device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_l
           (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
           (k == leaf_lim - 1 && N_L % 2 == 0)) {
         int kdx = (ks == 0) ? k : N_L - 1 - k;
-        double superlum, eta;
+        double superlum, eta, cos_xi = 0.0;
         if (!are_equal(psi, 0.0)) {
-          double cos_xi = sin_alpha * c.sin_i * sin(leaves[kdx]) / sin_psi;
+          cos_xi = sin_alpha * c.sin_i * sin(leaves[kdx]) / sin_psi;
           superlum = 1.0 + c.beta * cos_xi;
           eta = c.Lorentz / superlum;
         } else {
@@ -138,6 +159,13 @@ __device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_l
         g.ABB[kdx] = mu * eta;
         g.GEOM[kdx] = mu * fabs(deriv) * c.Grav_z * eta * eta * eta / superlum;
         g.leafphase[kdx] = leaves[kdx] + plag;
+        if (g.c2chi) {  // integratorIQU_for_azimuthal_invariance.pyx:463-466
+          const double chi = pol_angle(leaves[kdx], sin_psi, cos_psi, sin_alpha, cos_a, c.sin_th,
+                                       c.cos_th, c.sin_i, c.cos_i, c.sin_gamma, c.cos_gamma,
+                                       c.Grav_z, mu, eta, c.beta, c.Lorentz, cos_xi);
+          g.c2chi[kdx] = cos(2 * chi);
+          g.s2chi[kdx] = sin(2 * chi);
+        }
       }
     }
   }
@@ -1168,6 +1196,252 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   if (threadIdx.x == 0 && a.flop_counter && flops > 0.0) atomicAdd(a.flop_counter, flops);
 }
 
+// ---------------------------------------------------------------------------
+// Stokes I, Q, U (integratorIQU_for_azimuthal_invariance.pyx:68-743) for the
+// blackbody (Q = 0) and burst blackbody (hot_BB_burst.pyx) atmospheres: one
+// CTA per parallel.  Per chunk of energies the I, Q and U profiles of the
+// leaves are scaled, splined (Akima periodic) and summed over cells x phases
+// in double-float exactly as the FP64 integrator does for I; Q and U are
+// added wherever I is (:646-650).
+// ---------------------------------------------------------------------------
+constexpr int kStokesPiece = 3 * (int)sizeof(PieceDF);
+
+template <typename CP, typename AR>
+__device__ __forceinline__ bool cell_phase_sums_stokes(const CP &cp, const AR &area, int S1,
+                                                       const int32_t *rad, const PieceDF *pI,
+                                                       const PieceDF *pQ, const PieceDF *pU,
+                                                       int N_L, int pb, int ne, bool add_all,
+                                                       DF (&aI)[kEPT], DF (&aQ)[kEPT],
+                                                       DF (&aU)[kEPT]) {
+  int hint = -1;
+  for (int j = 0; j < S1; j++) {
+    if (rad[j] != 1) continue;
+    DF t;
+    const int iv = cp(j, hint, t);
+    if (iv < 0) return false;
+    hint = iv;
+    const DF A = area(j);
+#pragma unroll
+    for (int e = 0; e < kEPT; e++) {
+      if (pb + e < ne) {
+        const int o = (pb + e) * N_L + iv;
+        const PieceDF q = pI[o];
+        const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
+        if (sv.h > 0.0f || add_all) {
+          aI[e] = df_fma(A, sv, aI[e]);
+          const PieceDF qq = pQ[o], qu = pU[o];
+          aQ[e] = df_fma(A, df_fma(t, df_fma(t, df_fma(t, qq.k3, qq.k2), qq.k1), qq.y), aQ[e]);
+          aU[e] = df_fma(A, df_fma(t, df_fma(t, df_fma(t, qu.k3, qu.k2), qu.k1), qu.y), aU[e]);
+        }
+      }
+    }
+  }
+  return true;
+}
+
+size_t stokes_smem(int N_L, int N_P, int N_E, int N_R) {
+  const Layout L = make_layout(N_L, N_P, N_E, 0, 0, kStokesPiece, N_R);
+  return L.bytes + (size_t)2 * N_L * sizeof(double) + (size_t)2 * L.EC * sizeof(int) + 64;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
+  extern __shared__ __align__(16) char smem[];
+  const int64_t row = blockIdx.x;
+  const int m = a.row_member[row];
+  const MemberDesc M = a.members[m];
+  const int i = (int)(row - M.row_off);
+  const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
+  const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
+  const Layout L = make_layout(N_L, N_P, N_E, 0, 0, kStokesPiece, a.N_R);
+  const int EC = L.EC;
+  double *coef;
+  AtmSmem as{};
+  GeoSmem g = carve(smem, N_L, EC, &coef, 0, 0, &as, kStokesPiece, a.N_R);
+  double *xd = reinterpret_cast<double *>(
+      (reinterpret_cast<uintptr_t>(g.sc_exp + EC) + 15) & ~uintptr_t(15));
+  g.c2chi = xd;
+  g.s2chi = xd + N_L;
+  int *scQ = reinterpret_cast<int *>(xd + 2 * N_L), *scU = scQ + EC;
+  Piece *coI = reinterpret_cast<Piece *>(coef);
+  Piece *coQ = coI + (size_t)EC * N_L, *coU = coQ + (size_t)EC * N_L;
+  __shared__ int s_J, s_jalt;
+  double *part = a.partial + (size_t)row * 3 * N_E * N_P;
+  RowCtx c;
+  if (!load_row(a, M, row, i, c, &s_J)) return;
+  stage_deflection(c, g, &s_jalt);
+  const bool burst = (M.atm == 3);
+  const double norm = kErg * kPlanck;
+  const double kT = (kKB / kKeV) * pow(10.0, c.vec0);
+  const bool corr = a.correction != nullptr;
+  const double kT_c =
+      corr ? (kKB / kKeV) *
+                 pow(10.0, a.correction[(M.cell_off + (int64_t)i * M.S1 + c.J) * a.n_correction])
+           : 0.0;
+  const double *cellA = a.cellArea + M.cell_off + (int64_t)i * M.S1;
+  const double *cellPhi = a.phi + M.cell_off + (int64_t)i * M.S1;
+  const int32_t *rad = a.radiates + M.cell_off + (int64_t)i * M.S1;
+  const int n_iv = N_L - 1, strips = (n_iv + kStrip - 1) / kStrip;
+  for (int I = 0; I < c.IO; I++) {
+    for (int k = threadIdx.x; k < leaf_lim; k += blockDim.x)
+      leaf_geometry(c, I, k, N_L, leaf_lim, a.leaves, g);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int top = 0, any = 0;
+      state_machine(N_L, leaf_lim, a.leaves, g, false, 0.0, 0.0, top, any);
+    }
+    __syncthreads();
+    if (g.flags[0]) {
+      if (threadIdx.x == 0) atomicExch(&a.member_status[m], (int)kPulseFail);
+      return;
+    }
+    if (g.flags[1]) break;
+    for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+      const float hi = (float)g.phase[t];
+      as.fphase[t] = hi;
+      as.fphase_lo[t] = (float)(g.phase[t] - (double)hi);
+    }
+    if (M.S1 <= kMaxCellsF) {
+      for (int t = threadIdx.x; t < M.S1; t += blockDim.x) {
+        const float hi = (float)cellPhi[t];
+        as.fcphi[t] = hi;
+        as.fcphi_lo[t] = (float)(cellPhi[t] - (double)hi);
+        const float ah = (float)cellA[t];
+        as.fcarea[t] = ah;
+        as.fcarea_lo[t] = (float)(cellA[t] - (double)ah);
+      }
+    }
+    for (int t = threadIdx.x; t < N_L - 1; t += blockDim.x) {
+      const double h = g.phase[t + 1] - g.phase[t];
+      g.ih[t] = df_split(1.0 / h);
+      g.ih2[t] = df_split(1.0 / (h * h));
+    }
+    __syncthreads();
+    for (int e0 = 0; e0 < N_E; e0 += EC) {
+      const int ne = min(EC, N_E - e0);
+      // I, Q cos 2chi and Q sin 2chi of every profile column (:468-497)
+      for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+        const int pl = t / N_L, col = t - pl * N_L;
+        const int p = e0 + pl;
+        const int s = g.src[col];
+        double yI = 0.0, yQ = 0.0, yU = 0.0;
+        if (s >= 0) {
+          const double Ep = a.energies[p] / g.Z[s];
+          const double abb = g.ABB[s];
+          double I_E = eval_bb(Ep, kT), Q_E = 0.0;
+          if (burst) {
+            I_E = I_E * (0.421 + 0.868 * abb);
+            Q_E = (0.1171 * (abb - 1.) / (1. + 3.582 * abb)) * I_E;
+          }
+          const double I_c = corr ? eval_bb(Ep, kT_c) * norm : 0.0;
+          yI = (I_E * norm - I_c) * g.GEOM[s];
+          yQ = ((Q_E * g.c2chi[s]) * norm) * g.GEOM[s];
+          yU = ((Q_E * g.s2chi[s]) * norm) * g.GEOM[s];
+        }
+        coI[pl * N_L + col].y = yI;
+        coQ[pl * N_L + col].y = yQ;
+        coU[pl * N_L + col].y = yU;
+      }
+      __syncthreads();
+      // an exact power-of-two scale per (component, energy row)
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int r = warp; r < 3 * ne; r += kThreads / 32) {
+        const int comp = r / ne, pl = r - comp * ne;
+        const Piece *co = comp == 0 ? coI : (comp == 1 ? coQ : coU);
+        double mx = 0.0;
+        for (int col = lane; col < N_L; col += 32) mx = fmax(mx, fabs(co[pl * N_L + col].y));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        int ex = 0;
+        if (mx > 0.0 && mx <= 1.7976931348623157e308) frexp(mx, &ex);
+        if (lane == 0) (comp == 0 ? g.sc_exp : (comp == 1 ? scQ : scU))[pl] = ex;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < 3 * ne * N_L; t += blockDim.x) {
+        const int comp = t / (ne * N_L), u = t - comp * ne * N_L;
+        Piece *co = comp == 0 ? coI : (comp == 1 ? coQ : coU);
+        const int *sc = comp == 0 ? g.sc_exp : (comp == 1 ? scQ : scU);
+        const double v = co[u].y;
+        reinterpret_cast<PieceDF *>(co)[u].y = df_split(ldexp(v, -sc[u / N_L]));
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < 3 * ne * strips; t += blockDim.x) {
+        const int comp = t / (ne * strips), u = t - comp * ne * strips;
+        const int pl = u / strips, i0 = (u - pl * strips) * kStrip;
+        const int i1 = min(i0 + kStrip, n_iv);
+        PieceDF *yr = reinterpret_cast<PieceDF *>(comp == 0 ? coI : (comp == 1 ? coQ : coU)) +
+                      pl * N_L;
+        auto chord = [&](int j) -> DF {
+          const int q = periodic_chord(j, N_L);
+          return df_mul(df_sub(yr[q + 1].y, yr[q].y), g.ih[q]);
+        };
+        DF m0 = chord(i0 - 2), m1 = chord(i0 - 1), m2 = chord(i0), m3 = chord(i0 + 1),
+           m4 = chord(i0 + 2);
+        for (int iv = i0; iv < i1; iv++) {
+          if (iv > i0) {
+            m0 = m1; m1 = m2; m2 = m3; m3 = m4;
+            m4 = chord(iv + 2);
+          }
+          DF k1, k2, k3;
+          akima_piece_df(m0, m1, m2, m3, m4, g.ih[iv], g.ih2[iv], k1, k2, k3);
+          yr[iv].k1 = k1;
+          yr[iv].k2 = k2;
+          yr[iv].k3 = k3;
+        }
+      }
+      __syncthreads();
+      // cell x phase accumulation (:612-650)
+      const int ntasks = N_P * ((ne + kEPT - 1) / kEPT);
+      for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
+        const int k = task % N_P, pb = (task / N_P) * kEPT;
+        const double phd = a.phases[k];
+        const float ph = (float)phd;
+        const float tp = (float)kTwoPi;
+        const bool cached = M.S1 <= kMaxCellsF;
+        const CellPhaseF cp{as.fphase, as.fphase_lo, N_L, as.fphase[0], as.fphase[N_L - 1], ph,
+                            (float)(phd - (double)ph), tp, (float)(kTwoPi - (double)tp),
+                            cached ? as.fcphi : nullptr, cached ? as.fcphi_lo : nullptr,
+                            cellPhi};
+        const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
+        DF aI[kEPT], aQ[kEPT], aU[kEPT];
+#pragma unroll
+        for (int e = 0; e < kEPT; e++) aI[e] = aQ[e] = aU[e] = DF{0.0f, 0.0f};
+        if (!cell_phase_sums_stokes(cp, ar, M.S1, rad, reinterpret_cast<const PieceDF *>(coI),
+                                    reinterpret_cast<const PieceDF *>(coQ),
+                                    reinterpret_cast<const PieceDF *>(coU), N_L, pb, ne, corr, aI,
+                                    aQ, aU)) {
+          atomicExch(&a.member_status[m], (int)kPulseFail);
+          continue;
+        }
+#pragma unroll
+        for (int e = 0; e < kEPT; e++) {
+          if (pb + e < ne) {
+            const int p = e0 + pb + e;
+            part[(size_t)p * N_P + k] += ldexp(df_value(aI[e]), g.sc_exp[pb + e]);
+            part[(size_t)(N_E + p) * N_P + k] += ldexp(df_value(aQ[e]), scQ[pb + e]);
+            part[(size_t)(2 * N_E + p) * N_P + k] += ldexp(df_value(aU[e]), scU[pb + e]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// the parallels' Stokes partials of each member in order, / (E keV) (:715-725)
+__global__ void reduce_stokes_kernel(IntegrateArgs a) {
+  const int m = blockIdx.y, comp = blockIdx.z;
+  const MemberDesc M = a.members[m];
+  const int n = a.N_E * a.N_P;
+  double *out = comp == 0 ? a.flux : (comp == 1 ? a.flux_q : a.flux_u);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < M.S0; r++)
+      s += a.partial[((size_t)(M.row_off + r) * 3 + comp) * n + t];
+    const int p = t / a.N_P;
+    out[M.flux_off + t] = s / (a.energies[p] * kKeV);
+  }
+}
+
 // ordered reduction of the chunk partials and the 1/(E keV) factor (:605-612)
 __global__ void reduce_flux_kernel(IntegrateArgs a) {
   const int m = blockIdx.y;
@@ -1217,6 +1491,29 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
     integrate_kernel<double><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
   dim3 grid((a.N_E * a.N_P + 255) / 256, a.n_members);
   reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
+}
+
+
+size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R) {
+  return stokes_smem(N_L, N_P, N_E, N_R);
+}
+
+size_t stokes_partial_doubles(const IntegrateArgs &a) {
+  return (size_t)a.n_rows * 3 * a.N_E * a.N_P;
+}
+
+int launch_stokes(const IntegrateArgs &a, cudaStream_t st) {
+  if (a.n_members <= 0) return 0;
+  const size_t smem = stokes_smem(a.N_L, a.N_P, a.N_E, a.N_R);
+  if (smem > 227 * 1024) return -2;
+  if (cudaFuncSetAttribute(stokes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -5;
+  stokes_kernel<<<(unsigned)a.n_rows, kThreads, smem, st>>>(a);
+  const int n = a.N_E * a.N_P;
+  dim3 grid((n + 255) / 256, a.n_members, 3);
+  reduce_stokes_kernel<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
 }  // namespace xg

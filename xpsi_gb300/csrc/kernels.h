@@ -76,8 +76,14 @@ struct IntegrateArgs {
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
   double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
   int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
+  double *flux_q = nullptr, *flux_u = nullptr;  // Stokes Q, U (launch_stokes only)
 };
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
+// Stokes I (a.flux), Q, U for blackbody (1) and burst blackbody (3) members;
+// a.partial: stokes_partial_doubles(a) doubles, zeroed; a.chunk_* unused
+size_t stokes_partial_doubles(const IntegrateArgs &a);
+size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R);
+int launch_stokes(const IntegrateArgs &a, cudaStream_t st);
 
 // ---- K4 energy integrator ------------------------------------------------
 struct EnergyArgs {
