@@ -521,6 +521,23 @@ int xgpu_poisson_batch(int64_t n, const double *mean, double *out,
                        uint64_t seed, uint64_t offset, int32_t *fail,
                        void *stream);
 
+/* Gaussian log-likelihoods of polarimetry (HOST arrays):
+ * -sum_ij (model_ij - data_ij)^2 / (2 errors_ij^2) + log(2 pi errors_ij^2)/2
+ * over data[rows][cols]; model row i starts at model + i * model_row_stride
+ * (0: one model row for every data row, as _gaussian_likelihood_QnUn.pyx:
+ * 31-36 does; cols: the expected counts of
+ * _gaussian_likelihood_given_background_IQU.pyx:70-78). */
+int xgpu_gaussian_loglike(size_t rows, size_t cols, const double *model,
+                          size_t model_row_stride, const double *data,
+                          const double *errors, double *loglike);
+/* Batched form (device pointers): n_sets models at model_set_stride against
+ * one data set; loglike[n_sets]. */
+int xgpu_gaussian_loglike_batch(int n_sets, int rows, int cols,
+                                const double *model, int64_t model_set_stride,
+                                int64_t model_row_stride, const double *data,
+                                const double *errors, double *loglike,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif

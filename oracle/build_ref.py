@@ -42,6 +42,8 @@ MODULES = [
     "cellmesh.integratorIQU_for_azimuthal_invariance",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
+    "likelihoods._gaussian_likelihood_QnUn",
+    "likelihoods._gaussian_likelihood_given_background_IQU",
 ]
 
 

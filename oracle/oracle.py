@@ -365,3 +365,21 @@ def phase_integrator(exposure_time, phases, signal, signal_phases, phase_shift,
                               _p(S), _p(sp), float(phase_shift), int(bool(allow_negative)),
                               _p(out))
     return out
+
+
+def gaussian_loglike(model, counts, errors):
+    """The Gaussian log-likelihood of _gaussian_likelihood_given_background_IQU
+    .pyx:70-78 and _gaussian_likelihood_QnUn.pyx:31-36, summed in the
+    reference's order; `model` is [rows, cols] or one row [cols]."""
+    import math
+    d = _c(counts)
+    e = _c(errors)
+    m = _c(model)
+    L = 0.0
+    for i in range(d.shape[0]):
+        row = m[i] if m.ndim == 2 else m
+        for j in range(d.shape[1]):
+            s2 = math.pow(e[i, j], 2.0)
+            norm = 0.5 * math.log(2.0 * math.pi * s2)
+            L -= (row[j] - d[i, j]) ** 2 / (2.0 * s2) + norm
+    return L

@@ -24,6 +24,7 @@ Cases
                  its phase integrator on config1's folded signal.
   stokes         the Stokes I/Q/U integrator for the burst blackbody and the
                  plain blackbody with a correction.
+  gaussian       the Gaussian likelihoods of polarimetry.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -446,6 +447,34 @@ def stokes(xpsi):
     save("stokes", **out)
 
 
+def gaussian(xpsi):
+    """The Gaussian likelihoods of polarimetry
+    (likelihoods/_gaussian_likelihood_given_background_IQU.pyx,
+    likelihoods/_gaussian_likelihood_QnUn.pyx) on config1's folded signal
+    with seeded counts and errors."""
+    from xpsi.likelihoods._gaussian_likelihood_given_background_IQU import (
+        gaussian_likelihood_given_background)
+    from xpsi.likelihoods._gaussian_likelihood_QnUn import gaussian_likelihood_QnUn
+    f = np.load(os.path.join(HERE, "config1.npz"))
+    c1 = np.ascontiguousarray(f["folded"][:40])
+    p1 = np.ascontiguousarray(f["comp_phases"])
+    edges = np.ascontiguousarray(f["phase_edges"])
+    K, B = c1.shape[0], edges.size - 1
+    rng = np.random.default_rng(8)
+    bkg = np.ascontiguousarray(rng.uniform(0.5, 1.5, (K, B)) * c1.mean(axis=1)[:, None])
+    T = 1.0e4
+    counts = np.ascontiguousarray(rng.uniform(0.5, 2.0, (K, B)) * c1.mean(axis=1)[:, None] * T)
+    errors = np.ascontiguousarray(np.sqrt(counts) * rng.uniform(0.8, 1.2, (K, B)))
+    ll, expec = gaussian_likelihood_given_background(T, edges, counts, errors, (c1,), (p1,),
+                                                     np.array([0.2]), bkg)
+    qn = np.ascontiguousarray(rng.normal(0.0, 0.05, (3, B)))
+    qn_err = np.ascontiguousarray(rng.uniform(0.02, 0.08, (3, B)))
+    star = np.ascontiguousarray(rng.normal(0.0, 0.05, B))
+    ll_qn, _ = gaussian_likelihood_QnUn(edges, qn, qn_err, star)
+    save("gaussian", bkg=bkg, counts=counts, errors=errors, exposure=T, loglike=ll,
+         expec=expec, qn=qn, qn_err=qn_err, star=star, loglike_qn=ll_qn)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -456,6 +485,7 @@ def main():
     general_integrator(xpsi)
     synthesis(xpsi)
     stokes(xpsi)
+    gaussian(xpsi)
 
 
 if __name__ == "__main__":

@@ -42,6 +42,8 @@ def install(xpsi_module):
     from .tools import energy_integrator as ei
     from .tools import phase_integrator as pint, synthesise as syn
     from .likelihoods import default_background_marginalisation as dbm
+    from .likelihoods import _gaussian_likelihood_given_background_IQU as gbg
+    from .likelihoods import _gaussian_likelihood_QnUn as gqu
     done = []
     targets = [
         ("xpsi.cellmesh.rays", "compute_rays", rays.compute_rays),
@@ -57,6 +59,10 @@ def install(xpsi_module):
         ("xpsi.cellmesh.integrator", "integrate", general.integrate),
         ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance", "integrate", iqu.integrate),
         ("xpsi.tools.phase_integrator", "phase_integrator", pint.phase_integrator),
+        ("xpsi.likelihoods._gaussian_likelihood_given_background_IQU",
+         "gaussian_likelihood_given_background", gbg.gaussian_likelihood_given_background),
+        ("xpsi.likelihoods._gaussian_likelihood_QnUn", "gaussian_likelihood_QnUn",
+         gqu.gaussian_likelihood_QnUn),
         ("xpsi.tools.synthesise", "synthesise_exposure", syn.synthesise_exposure),
         ("xpsi.tools.synthesise", "synthesise_given_total_count_number",
          syn.synthesise_given_total_count_number),

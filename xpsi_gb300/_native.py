@@ -203,6 +203,9 @@ def _bind(L):
         "xgpu_mesh_batch": (C.c_int, [C.c_int, C.POINTER(MeshMember), I64, I64,
                                       C.POINTER(MeshBatchOut), P]),
         "xgpu_peak_probe": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
+        "xgpu_gaussian_loglike": (C.c_int, [SZ, SZ, P, SZ, P, P, P]),
+        "xgpu_gaussian_loglike_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, P, I64, I64, P, P,
+                                                  P, P]),
         "xgpu_integrate_stokes": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ,
                                             SZ, P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
                                             C.c_int, C.c_int, P, P, P]),
@@ -245,7 +248,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_integrate_time_invariant", "xgpu_elsewhere_batch",
             "xgpu_integrate_general", "xgpu_compute_expected_counts",
             "xgpu_phase_integrator", "xgpu_poisson", "xgpu_expected_counts_batch",
-            "xgpu_poisson_batch", "xgpu_integrate_stokes"]
+            "xgpu_poisson_batch", "xgpu_integrate_stokes", "xgpu_gaussian_loglike",
+            "xgpu_gaussian_loglike_batch"]
 
 
 def lib():

@@ -998,4 +998,40 @@ int xgpu_poisson(size_t n, const double *mean, uint64_t seed, uint64_t offset, d
   return hit_bound ? 1 : 0;
 }
 
+int xgpu_gaussian_loglike_batch(int n_sets, int rows, int cols, const double *model,
+                                int64_t model_set_stride, int64_t model_row_stride,
+                                const double *data, const double *errors, double *loglike,
+                                void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_sets <= 0) return 0;
+  xg::launch_gaussian(n_sets, rows, cols, model, model_set_stride, model_row_stride, data,
+                      errors, loglike, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_gaussian_loglike(size_t rows, size_t cols, const double *model,
+                          size_t model_row_stride, const double *data, const double *errors,
+                          double *loglike) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (rows == 0 || cols == 0) {
+    *loglike = 0.0;
+    return 0;
+  }
+  const size_t model_n = model_row_stride ? (rows - 1) * model_row_stride + cols : cols;
+  Dev dm, dd, de, dl;
+  if ((rc = upload(dm, model, model_n, st)) || (rc = upload(dd, data, rows * cols, st)) ||
+      (rc = upload(de, errors, rows * cols, st)) || (rc = dalloc(dl, 8, st)))
+    return rc;
+  if ((rc = xgpu_gaussian_loglike_batch(1, (int)rows, (int)cols, dm.as<double>(), 0,
+                                        (int64_t)model_row_stride, dd.as<double>(),
+                                        de.as<double>(), dl.as<double>(), st)))
+    return rc;
+  CK(cudaMemcpyAsync(loglike, dl.p, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
 }  // extern "C"

@@ -233,6 +233,9 @@ struct PhaseIntArgs {
 void launch_phase_integrator(const PhaseIntArgs &a, cudaStream_t st);
 void launch_poisson(int64_t n, const double *mean, double *out, uint64_t seed, uint64_t offset,
                     int32_t *fail, cudaStream_t st);
+void launch_gaussian(int n_sets, int rows, int cols, const double *model,
+                     int64_t model_set_stride, int64_t model_row_stride, const double *data,
+                     const double *errors, double *loglike, cudaStream_t st);
 int launch_elsewhere(const ElsewhereArgs &a, cudaStream_t st);
 
 }  // namespace xg

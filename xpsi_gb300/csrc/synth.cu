@@ -3,12 +3,17 @@
 //   xpsi/tools/compute_expected_counts.pyx:66-197 (compute_expected_counts),
 //   xpsi/tools/phase_integrator.pyx:23-121 (phase_integrator) and the draws of
 //   xpsi/tools/synthesise.pyx:35-276 (synthesise_exposure,
-//   synthesise_given_total_count_number).
+//   synthesise_given_total_count_number), and the Gaussian likelihoods of
+//   xpsi/likelihoods/_gaussian_likelihood_given_background_IQU.pyx and
+//   _gaussian_likelihood_QnUn.pyx.
 //
 // Phase-bin integrals: one warp per (signal, channel) row, lanes over the
 // bins, each bin the exact integral of the Akima-periodic interpolant of the
 // row over the phase-shifted bin (wrapped into [0, 1)), with the reference's
 // positive-part rules.
+//
+// Gaussian likelihoods of polarimetry: one warp per data set, the terms
+// summed row by row in column order.
 //
 // Poisson draws: element i of a launch with key `seed` draws from the
 // counter-based generator Philox4x32-10 (Salmon, Moraes, Dror and Shaw,
@@ -188,7 +193,60 @@ __global__ void __launch_bounds__(32 * kSynWarps) phase_integrator_kernel(PhaseI
   }
 }
 
+// Gaussian log-likelihood of one data set (the polarimetry likelihoods,
+// _gaussian_likelihood_given_background_IQU.pyx:70-78 and
+// _gaussian_likelihood_QnUn.pyx:31-36): -sum over (row, column) of
+// (model - data)^2 / (2 sigma^2) + log(2 pi sigma^2) / 2.  One warp per data
+// set: lane r sums rows r, r+32, ... in column order, the lanes' sums are
+// added in row order by lane 0.
+__global__ void gaussian_kernel(int n_sets, int rows, int cols, const double *model,
+                                int64_t model_set_stride, int64_t model_row_stride,
+                                const double *data, const double *errors, double *loglike) {
+  const int lane = threadIdx.x & 31;
+  const int set = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (set >= n_sets) return;
+  const double *mdl = model + set * model_set_stride;
+  double rowsum[8];
+  double part = 0.0;
+  int nr = 0;
+  for (int i = lane; i < rows; i += 32) {
+    double s = 0.0;
+    for (int j = 0; j < cols; j++) {
+      const double sig2 = pow(errors[(int64_t)i * cols + j], 2.0);
+      const double norm = 0.5 * log(2.0 * kPi * sig2);
+      const double d = mdl[(int64_t)i * model_row_stride + j] - data[(int64_t)i * cols + j];
+      s += d * d / (2.0 * sig2) + norm;
+    }
+    if (nr < 8) rowsum[nr] = s;
+    else part += s;
+    nr++;
+  }
+  // rows in order: row i lives in lane i % 32, slot i / 32
+  __shared__ double red[8][32 * 8];
+  const int w = threadIdx.x >> 5;
+  for (int k = 0; k < 8; k++) red[w][k * 32 + lane] = (k < nr && k < 8) ? rowsum[k] : 0.0;
+  __syncwarp();
+  const double extra = part;
+  double tot_extra = extra;
+  for (int o = 16; o > 0; o >>= 1) tot_extra += __shfl_xor_sync(0xffffffffu, tot_extra, o);
+  if (lane == 0) {
+    double L = 0.0;
+    const int first = min(rows, 8 * 32);
+    for (int i = 0; i < first; i++) L -= red[w][(i / 32) * 32 + (i % 32)];
+    L -= tot_extra;
+    loglike[set] = L;
+  }
+}
+
 }  // namespace
+
+void launch_gaussian(int n_sets, int rows, int cols, const double *model,
+                     int64_t model_set_stride, int64_t model_row_stride, const double *data,
+                     const double *errors, double *loglike, cudaStream_t st) {
+  if (n_sets <= 0) return;
+  gaussian_kernel<<<(n_sets + 3) / 4, 128, 0, st>>>(n_sets, rows, cols, model, model_set_stride,
+                                                     model_row_stride, data, errors, loglike);
+}
 
 void launch_expected_counts(const ExpectedArgs &a, cudaStream_t st) {
   const int64_t warps = (int64_t)a.n_sets * a.K;
