@@ -169,11 +169,15 @@ def run_gb300(args):
     P = BT.prepare(model, params)
     t_mesh = time.time() - t0
     B = ev.upload(P)
+    # two batches in flight on two streams, the steps alternating between
+    # them: one batch's FP64-bound stages run beside the other's FP32-bound
+    # integrator sums
+    Bs = [B, ev.upload(P)]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
     flops = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     # warm-up
-    for _ in range(args.warmup):
-        ev.run(B)
+    pipelined_steps(ev, Bs, streams, args.warmup)
     torch.cuda.synchronize()
     # integrator time (CUDA events on the launching stream) and its
     # algorithmic FLOPs for one step
@@ -187,15 +191,8 @@ def run_gb300(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     with clocks:
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            ev.run(B)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        ms = pipelined_steps(ev, Bs, streams, args.steps)
     barrier(world)
-    ms = e0.elapsed_time(e1) / args.steps
     ms = max_over_ranks(ms, world)
     st = ev.statuses(B)
     value = V * world / (ms / 1e3)
@@ -207,16 +204,12 @@ def run_gb300(args):
     Pg = BT.prepare(model, params, meshes="gpu")
     h2d = ev.h2d_bytes(Pg)
     d2h = V * (8 + 4)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(4, args.steps)
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        Pg = BT.prepare(model, params, meshes="gpu")
-        Bx = ev.upload(Pg, pinned=True)
-        ev.run(Bx)
-        ll = Bx["loglike"].cpu()
-        stx = Bx["status"].cpu()
+    for ll, stx in ev.loglikelihood_pipelined([params] * e2e_steps, depth=2):
+        pass
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_s = max_over_ranks(e2e_s, world)
@@ -241,6 +234,8 @@ def run_gb300(args):
         "config": {"workload": WORKLOAD,
                    "vectors_per_gpu": V, "precision": "plain FP64",
                    "l2": "inputs and ray tables larger than L2 (129 MB) every step",
+                   "streams": "two batches resident, steps alternating over two CUDA streams "
+                              "(events bracket all steps of both)",
                    "mesh_build_host_s": round(t_mesh, 3),
                    "mesh_build_gpu_ms": round(mesh_gpu_ms, 2),
                    "prepare_for_gpu_meshes_s": round(t_prep, 3),
@@ -248,8 +243,9 @@ def run_gb300(args):
                                      zip(*np.unique(st, return_counts=True))}},
         "e2e": {"value": V * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "from host parameter vectors: host cell budgets, GPU meshes, the five "
-                        "stages, log L and statuses back to the host"},
+                "what": "from host parameter vectors: host cell budgets, pinned copies, GPU "
+                        "meshes, the five stages, log L and statuses back to the host; "
+                        "BatchEvaluator.loglikelihood_pipelined, two batches in flight"},
         "gpu_launches": None,
         "clocks": clocks.summary(),
     }
@@ -271,6 +267,7 @@ def run_gb300(args):
                                "FP32 pipes (64x the FP64 issue rate), so frac can exceed "
                                "1 against the FP64 pipe's peak; pipe utilisation of this "
                                "kernel is in profiles/"}
+    torch.cuda.synchronize()
     plain_ll = B["loglike"].cpu().numpy().copy()
     if rank == 0:
         legs = set(args.legs.split(",")) if args.legs != "all" else \
@@ -310,6 +307,31 @@ def fp64_peak(device):
 
 
 
+def pipelined_steps(ev, Bs, streams, steps):
+    """Run `steps` evaluations of the resident batches Bs, step k on
+    streams[k % len] with Bs[k % len]; returns ms per step from CUDA events
+    recorded before the first and after the last step of every stream."""
+    import torch
+    cur = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(cur)
+    for s in streams:
+        s.wait_event(e0)
+    for k in range(steps):
+        s = streams[k % len(streams)]
+        with torch.cuda.stream(s):
+            ev.run(Bs[k % len(Bs)], stream=s)
+    for s in streams:
+        done = torch.cuda.Event()
+        done.record(s)
+        cur.wait_event(done)
+    e1.record(cur)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / max(1, steps)
+
+
 def mixed_leg(model, P, plain_ll, plain_st, args):
     """Batched mixed-precision form on the same vectors: throughput and
     |Delta log L| against the FP64 path."""
@@ -317,18 +339,10 @@ def mixed_leg(model, P, plain_ll, plain_st, args):
     from xpsi_gb300 import batch as BT
     ev = BT.BatchEvaluator(model, precision="mixed")
     B = ev.upload(P)
-    for _ in range(args.warmup):
-        ev.run(B)
-    torch.cuda.synchronize()
-    s = torch.cuda.current_stream()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(args.steps):
-        ev.run(B)
-    e1.record(s)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    Bs = [B, ev.upload(P)]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    pipelined_steps(ev, Bs, streams, args.warmup)
+    ms = pipelined_steps(ev, Bs, streams, args.steps)
     ll = B["loglike"].cpu().numpy()
     st = ev.statuses(B)
     ok = (st == 0) & (plain_st == 0)

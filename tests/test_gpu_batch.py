@@ -53,3 +53,17 @@ def test_batch_vector_independence(cuda):
     ll_all, _ = ev.loglikelihood(params)
     ll_one, _ = ev.loglikelihood(params[2:3])
     assert abs(ll_all[2] - ll_one[0]) <= 1e-12 * abs(ll_one[0])
+
+
+def test_pipelined_equals_sequential(cuda):
+    """Batches evaluated two at a time on separate streams give exactly the
+    sequential results, in order."""
+    m, params = small_num4d(V=4)
+    ev = BT.BatchEvaluator(m)
+    batches = [params[:2], params[2:], params[1:3]]
+    seq = [ev.loglikelihood(b) for b in batches]
+    pipe = list(ev.loglikelihood_pipelined(batches, depth=2))
+    assert len(pipe) == len(seq)
+    for (a, sa), (b, sb) in zip(seq, pipe):
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(sa, sb)

@@ -698,6 +698,41 @@ class BatchEvaluator:
         st[P.status != 0] = P.status[P.status != 0]
         return st
 
+    def loglikelihood_pipelined(self, batches, n_threads=0, meshes="gpu", depth=2):
+        """log L and statuses of a sequence of parameter batches, yielded in
+        order, with up to `depth` batches in flight on separate CUDA streams:
+        batch i+1's host preparation, copies and GPU mesh build overlap batch
+        i's stages.  Each yielded pair is as loglikelihood() returns."""
+        from collections import deque
+        torch = self.torch
+        streams = [torch.cuda.Stream(device=self.dev) for _ in range(max(1, int(depth)))]
+        inflight = deque()
+        for i, params in enumerate(batches):
+            s = streams[i % len(streams)]
+            P = prepare(self.model, params, n_threads, meshes=meshes)
+            with torch.cuda.stream(s):
+                B = self.upload(P, pinned=True)
+                self.run(B, stream=s)
+                ll = torch.empty(P.V, dtype=torch.float64, pin_memory=True)
+                ll.copy_(B["loglike"], non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(s)
+            inflight.append((done, B, ll))
+            if len(inflight) >= len(streams):
+                yield self._finish(*inflight.popleft())
+        while inflight:
+            yield self._finish(*inflight.popleft())
+
+    def _finish(self, done, B, ll):
+        done.synchronize()
+        ll = ll.numpy().copy()
+        st = self.statuses(B)
+        bad = st != 0
+        if bad.any():
+            rng = np.random.default_rng(12345)
+            ll[bad] = self.model.llzero * (0.1 + 0.9 * rng.random(int(bad.sum())))
+        return ll, st
+
     def loglikelihood(self, params, n_threads=0, meshes="gpu"):
         """log L of every parameter vector (host in, host out) and statuses.
         Vectors whose status is not 0 get a value near llzero, as

@@ -85,8 +85,14 @@ class BatchedLikelihood:
     def __call__(self, points) -> np.ndarray:
         full = self.full_vectors(points)
         ll = np.empty(full.shape[0])
-        for s in range(0, full.shape[0], self.max_batch):
-            part, st = self.ev.loglikelihood(full[s:s + self.max_batch])
+        starts = list(range(0, full.shape[0], self.max_batch))
+        chunks = [full[s:s + self.max_batch] for s in starts]
+        if len(chunks) > 1 and hasattr(self.ev, "loglikelihood_pipelined"):
+            # several batches: two in flight on separate streams
+            results = self.ev.loglikelihood_pipelined(chunks)
+        else:
+            results = (self.ev.loglikelihood(c) for c in chunks)
+        for s, (part, st) in zip(starts, results):
             if self.exit_value == "-inf":
                 part = np.where(st != 0, -np.inf, part)
             ll[s:s + self.max_batch] = part
