@@ -169,11 +169,11 @@ def run_gb300(args):
     P = BT.prepare(model, params)
     t_mesh = time.time() - t0
     B = ev.upload(P)
-    # two batches in flight on two streams, the steps alternating between
-    # them: one batch's FP64-bound stages run beside the other's FP32-bound
+    # three batches in flight on three streams, the steps rotating between
+    # them: one batch's FP64-bound stages run beside another's FP32-bound
     # integrator sums
-    Bs = [B, ev.upload(P)]
-    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    Bs = [B, ev.upload(P), ev.upload(P)]
+    streams = [torch.cuda.Stream() for _ in Bs]
     flops = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     # warm-up
@@ -204,11 +204,11 @@ def run_gb300(args):
     Pg = BT.prepare(model, params, meshes="gpu")
     h2d = ev.h2d_bytes(Pg)
     d2h = V * (8 + 4)
-    e2e_steps = max(4, args.steps)
+    e2e_steps = max(6, args.steps)
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for ll, stx in ev.loglikelihood_pipelined([params] * e2e_steps, depth=2):
+    for ll, stx in ev.loglikelihood_pipelined([params] * e2e_steps, depth=3):
         pass
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
@@ -234,8 +234,8 @@ def run_gb300(args):
         "config": {"workload": WORKLOAD,
                    "vectors_per_gpu": V, "precision": "plain FP64",
                    "l2": "inputs and ray tables larger than L2 (129 MB) every step",
-                   "streams": "two batches resident, steps alternating over two CUDA streams "
-                              "(events bracket all steps of both)",
+                   "streams": "three batches resident, steps rotating over three CUDA streams "
+                              "(events bracket all steps of all three)",
                    "mesh_build_host_s": round(t_mesh, 3),
                    "mesh_build_gpu_ms": round(mesh_gpu_ms, 2),
                    "prepare_for_gpu_meshes_s": round(t_prep, 3),
@@ -245,7 +245,7 @@ def run_gb300(args):
                 "d2h_bytes_per_step": d2h,
                 "what": "from host parameter vectors: host cell budgets, pinned copies, GPU "
                         "meshes, the five stages, log L and statuses back to the host; "
-                        "BatchEvaluator.loglikelihood_pipelined, two batches in flight"},
+                        "BatchEvaluator.loglikelihood_pipelined, three batches in flight"},
         "gpu_launches": None,
         "clocks": clocks.summary(),
     }
@@ -339,8 +339,8 @@ def mixed_leg(model, P, plain_ll, plain_st, args):
     from xpsi_gb300 import batch as BT
     ev = BT.BatchEvaluator(model, precision="mixed")
     B = ev.upload(P)
-    Bs = [B, ev.upload(P)]
-    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    Bs = [B, ev.upload(P), ev.upload(P)]
+    streams = [torch.cuda.Stream() for _ in Bs]
     pipelined_steps(ev, Bs, streams, args.warmup)
     ms = pipelined_steps(ev, Bs, streams, args.steps)
     ll = B["loglike"].cpu().numpy()

@@ -698,7 +698,7 @@ class BatchEvaluator:
         st[P.status != 0] = P.status[P.status != 0]
         return st
 
-    def loglikelihood_pipelined(self, batches, n_threads=0, meshes="gpu", depth=2):
+    def loglikelihood_pipelined(self, batches, n_threads=0, meshes="gpu", depth=3):
         """log L and statuses of a sequence of parameter batches, yielded in
         order, with up to `depth` batches in flight on separate CUDA streams:
         batch i+1's host preparation, copies and GPU mesh build overlap batch
