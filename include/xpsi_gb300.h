@@ -25,7 +25,10 @@
 extern "C" {
 #endif
 
-#define XGPU_ABI_VERSION 1
+/* 2: xgpu_integrate takes the elsewhere correction (correction_srcCellParams,
+ * n_correction, else_atm_ext); the elsewhere, general, Stokes, synthesis and
+ * Gaussian-likelihood entry points were added. */
+#define XGPU_ABI_VERSION 2
 
 /* Status words of the batched layer (per parameter vector). */
 enum {

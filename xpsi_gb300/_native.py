@@ -252,6 +252,9 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_gaussian_loglike_batch"]
 
 
+ABI_VERSION = 2  # XGPU_ABI_VERSION of include/xpsi_gb300.h
+
+
 def lib():
     """The loaded C ABI (built on first use if the sources are newer)."""
     global _lib
@@ -259,7 +262,12 @@ def lib():
         if _lib is None:
             if not os.path.exists(LIB) or os.path.getmtime(LIB) < _sources_mtime():
                 build()
-            _lib = _bind(C.CDLL(LIB))
+            L = _bind(C.CDLL(LIB))
+            if L.xgpu_abi_version() != ABI_VERSION:
+                raise RuntimeError("%s has C ABI version %d, these bindings expect %d: rebuild "
+                                   "with xpsi_gb300.build(force=True)"
+                                   % (LIB, L.xgpu_abi_version(), ABI_VERSION))
+            _lib = L
     return _lib
 
 
