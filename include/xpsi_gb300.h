@@ -27,8 +27,9 @@ extern "C" {
 
 /* 2: xgpu_integrate takes the elsewhere correction (correction_srcCellParams,
  * n_correction, else_atm_ext); the elsewhere, general, Stokes, synthesis and
- * Gaussian-likelihood entry points were added. */
-#define XGPU_ABI_VERSION 2
+ * Gaussian-likelihood entry points were added.
+ * 3: xgpu_atmos5d and xgpu_integrate_split (split atmospheres). */
+#define XGPU_ABI_VERSION 3
 
 /* Status words of the batched layer (per parameter vector). */
 enum {
@@ -90,6 +91,37 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination,
                    const double *leaves, size_t N_P, const double *phases,
                    int atm_ext, const xgpu_atmos4d *atmos, int else_atm_ext,
                    int image_order_limit, double *flux);
+
+/* A split atmosphere (hot_Num5D_split.pyx:77-220): grids of t_e, t_bb,
+ * tau, mu and E (electron rest energies), intensity [n0][n1][n2][n3][n4]. */
+typedef struct {
+  const double *grid[5];
+  size_t n[5];
+  const double *intensity;
+} xgpu_atmos5d;
+
+/* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance_split.integrate
+ * (xpsi/cellmesh/integrator_for_azimuthal_invariance_split.pyx:74-103), the
+ * integrator of a uniform hot region with a split atmosphere: the 5-D table
+ * is reduced to (mu, E) at the first cell's (t_e, t_bb, tau) (:270-275) and
+ * evaluated per leaf and energy at E / Z in electron rest energies
+ * (:457-471).  Other arguments and the return value as xgpu_integrate
+ * (beam_opt 0, no disk). */
+int xgpu_integrate_split(double R, double omega, double r_s, double inclination,
+                         size_t S0, size_t S1, const double *cellArea,
+                         const double *radialCoords_of_parallels,
+                         const double *r_s_over_r, const double *theta,
+                         const double *phi, const double *srcCellParams,
+                         size_t n_params, const int32_t *CELL_RADIATES,
+                         const double *correction_srcCellParams,
+                         size_t n_correction, size_t N_R,
+                         const double *deflection, const double *cos_alpha,
+                         const double *lag, const double *maxDeflection,
+                         const double *cos_gammaArray, size_t N_E,
+                         const double *energies, size_t N_L,
+                         const double *leaves, size_t N_P,
+                         const double *phases, const xgpu_atmos5d *atmos,
+                         int else_atm_ext, int image_order_limit, double *flux);
 
 /* Replaces xpsi.cellmesh.integratorIQU_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743), the

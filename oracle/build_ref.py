@@ -40,6 +40,8 @@ MODULES = [
     "cellmesh.integrator_for_azimuthal_invariance",
     "cellmesh.global_mesh", "cellmesh.integrator_for_time_invariance",
     "cellmesh.integratorIQU_for_azimuthal_invariance",
+    "surface_radiation_field.hot_Num2D_split",
+    "cellmesh.integrator_for_azimuthal_invariance_split",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
     "likelihoods._gaussian_likelihood_QnUn",

@@ -62,6 +62,8 @@ def lib():
                 C.c_size_t, C.c_size_t, P, P, P, P, P, P, C.c_size_t, P, P, C.c_size_t,
                 C.c_size_t, P, P, P, P, P, C.c_size_t, P, C.c_size_t, P,
                 C.c_size_t, P, C.c_int, P, C.c_int, P, P, P]
+            L.xo_integrate_split.restype = C.c_int
+            L.xo_integrate_split.argtypes = list(L.xo_integrate.argtypes)[:-6] + [P, C.c_int, P]
             L.xo_integrate_general.restype = C.c_int
             L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)[:-2]
             L.xo_integrate_time_invariant.restype = C.c_int
@@ -383,3 +385,47 @@ def gaussian_loglike(model, counts, errors):
             norm = 0.5 * math.log(2.0 * math.pi * s2)
             L -= (row[j] - d[i, j]) ** 2 / (2.0 * s2) + norm
     return L
+
+
+class Atmos5D(C.Structure):
+    _fields_ = [("grid", C.c_void_p * 5), ("n", C.c_size_t * 5), ("I", C.c_void_p)]
+
+
+def integrate_split(numThreads, R, omega, r_s, inclination, cellArea,
+                    radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                    CELL_RADIATES, correction_srcCellParams, numRays, deflection, cos_alpha,
+                    lag, maxDeflection, cos_gammaArray, energies, leaves, phases,
+                    hot_atmosphere, elsewhere_atmosphere, hot_atm_ext, else_atm_ext, beam_opt,
+                    image_order_limit=None, R_in=1e6):
+    """integrator_for_azimuthal_invariance_split.integrate: the 5-D split
+    atmosphere hot_atmosphere = (t_e, t_bb, tau, mu, E grids, intensity)."""
+    if beam_opt != 0 or R_in < 1e6:
+        raise NotImplementedError("oracle covers beam_opt 0 without a disk")
+    corr = None
+    if correction_srcCellParams is not None:
+        if int(else_atm_ext) != 1:
+            raise NotImplementedError("oracle corrects for a blackbody elsewhere only")
+        corr = _c(correction_srcCellParams)
+    A = _c(cellArea); S0, S1 = A.shape
+    par = _c(srcCellParams)
+    rad = _c(CELL_RADIATES, np.int32)
+    E = _c(energies); Lv = _c(leaves); P_ = _c(phases)
+    out = np.zeros((E.size, P_.size))
+    keep = tuple(_c(a) for a in hot_atmosphere)
+    a5 = Atmos5D((C.c_void_p * 5)(*[_p(k).value for k in keep[:5]]),
+                 (C.c_size_t * 5)(*[k.size for k in keep[:5]]), _p(keep[5]).value)
+    arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
+            _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
+            _c(cos_gammaArray)]
+    status = lib().xo_integrate_split(
+        int(numThreads), float(R), float(omega), float(r_s), float(inclination),
+        S0, S1, _p(A), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
+        _p(par), par.shape[2], _p(rad), _p(corr) if corr is not None else None,
+        corr.shape[2] if corr is not None else 0, int(numRays), _p(arrs[4]), _p(arrs[5]),
+        _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
+        P_.size, _p(P_), C.cast(C.pointer(a5), C.c_void_p), int(image_order_limit or 0),
+        _p(out))
+    del keep
+    if status != 0:
+        return (1, None)
+    return (0, out)

@@ -17,6 +17,8 @@
  *                            cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743
  *                            (atmospheres 1, 2, 3 = hot_BB_burst.pyx)
  *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
+ *   xo_integrate_split       cellmesh/integrator_for_azimuthal_invariance_split.pyx
+ *                            (hot_Num5D_split.pyx, hot_Num2D_split.pyx)
  *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
@@ -356,6 +358,81 @@ static double pol_angle(double leaf, double sin_psi, double cos_psi, double sin_
   return chi_0 + chi_1 + chi_p;
 }
 
+/* The reference's cached 4-point stencil walk in nd <= 5 dimensions, as
+ * hot_Num5D_split.pyx:267-481 and hot_Num2D_split.pyx:200-347 run it: the
+ * base node of a dimension moves only when the query leaves the central
+ * interval, and a query beyond the grid is clamped only by the move that
+ * reaches the grid end.  Weights are formed as the reference forms them
+ * (products of the numerators, then of the inverse denominators). */
+typedef struct {
+  size_t BN[5];
+  double node[10];
+} walk_state;
+
+static void walk_reset(walk_state *st, const double *const *g, int nd) {
+  for (int d = 0; d < nd; d++) {
+    st->BN[d] = 0;
+    st->node[2 * d] = g[d][1];
+    st->node[2 * d + 1] = g[d][2];
+  }
+}
+
+static double walk_eval(const double *const *g, const size_t *n, int nd, const double *table,
+                        walk_state *st, const double *vin) {
+  double v[5], DIFF[5][4], SPACE[5][4];
+  size_t *BN = st->BN;
+  for (int i = 0; i < nd; i++) {
+    const double *P = g[i];
+    v[i] = vin[i];
+    if (v[i] < st->node[2 * i] && BN[i] != 0) {
+      while (v[i] < P[BN[i] + 1]) {
+        if (BN[i] > 0) BN[i] -= 1;
+        else if (v[i] <= P[0]) { v[i] = P[0]; break; }
+        else break;
+      }
+      st->node[2 * i] = P[BN[i] + 1];
+      st->node[2 * i + 1] = P[BN[i] + 2];
+    } else if (v[i] > st->node[2 * i + 1] && BN[i] != n[i] - 4) {
+      while (v[i] > P[BN[i] + 2]) {
+        if (BN[i] < n[i] - 4) BN[i] += 1;
+        else if (v[i] >= P[n[i] - 1]) { v[i] = P[n[i] - 1]; break; }
+        else break;
+      }
+      st->node[2 * i] = P[BN[i] + 1];
+      st->node[2 * i + 1] = P[BN[i] + 2];
+    }
+    const size_t b = BN[i];
+    const double x = v[i];
+    DIFF[i][0] = x - P[b + 1]; DIFF[i][0] *= x - P[b + 2]; DIFF[i][0] *= x - P[b + 3];
+    DIFF[i][1] = x - P[b]; DIFF[i][1] *= x - P[b + 2]; DIFF[i][1] *= x - P[b + 3];
+    DIFF[i][2] = x - P[b]; DIFF[i][2] *= x - P[b + 1]; DIFF[i][2] *= x - P[b + 3];
+    DIFF[i][3] = x - P[b]; DIFF[i][3] *= x - P[b + 1]; DIFF[i][3] *= x - P[b + 2];
+    SPACE[i][0] = 1.0 / (P[b] - P[b + 1]); SPACE[i][0] /= P[b] - P[b + 2]; SPACE[i][0] /= P[b] - P[b + 3];
+    SPACE[i][1] = 1.0 / (P[b + 1] - P[b]); SPACE[i][1] /= P[b + 1] - P[b + 2]; SPACE[i][1] /= P[b + 1] - P[b + 3];
+    SPACE[i][2] = 1.0 / (P[b + 2] - P[b]); SPACE[i][2] /= P[b + 2] - P[b + 1]; SPACE[i][2] /= P[b + 2] - P[b + 3];
+    SPACE[i][3] = 1.0 / (P[b + 3] - P[b]); SPACE[i][3] /= P[b + 3] - P[b + 1]; SPACE[i][3] /= P[b + 3] - P[b + 2];
+  }
+  size_t stride[5];
+  stride[nd - 1] = 1;
+  for (int d = nd - 2; d >= 0; d--) stride[d] = stride[d + 1] * n[d + 1];
+  double I = 0.0;
+  const size_t total = (size_t)1 << (2 * nd);
+  for (size_t c = 0; c < total; c++) {
+    size_t idx[5], rem = c, off = 0;
+    for (int d = nd - 1; d >= 0; d--) { idx[d] = rem & 3; rem >>= 2; }
+    double dp = 1.0, sp = 1.0;
+    for (int d = 0; d < nd; d++) {
+      dp *= DIFF[d][idx[d]];
+      sp *= SPACE[d][idx[d]];
+      off += (BN[d] + idx[d]) * stride[d];
+    }
+    double temp = dp;
+    temp *= sp;
+    I += temp * table[off];
+  }
+  return I;
+}
+
 /* ================================================================== */
 /* cell-mesh integrator, azimuthal invariance                         */
 /* ================================================================== */
@@ -383,7 +460,9 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
   const int ns = (flux_Q != NULL && flux_U != NULL) ? 3 : 1;
   const double sin_i = sin(inclination), cos_i = cos(inclination);
   const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
+  /* hot_Num4D.pyx:441-461, hot_Num5D_split.pyx:538-563 (atm_ext 6: the split
+   * atmosphere reduced to (mu, E) by xo_integrate_split), hot_BB.pyx:84-98 */
+  const double norm = (atm_ext == 2 || atm_ext == 6) ? kErg / kHKeV : kErg * kPlanck;
   int nt = n_threads > 0 ? n_threads : 1;
   int terminate_any = 0;
   double *priv = (double *)calloc((size_t)nt * ns * N_E * N_P, sizeof(double));
@@ -418,6 +497,10 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
     const size_t NR = (size_t)ns * N_E;
     num4d_state nst;
     if (atm_ext == 2) num4d_reset(&nst, atmos);
+    walk_state wst;
+    const double *g2[2] = {atmos ? atmos->mu : NULL, atmos ? atmos->logE : NULL};
+    const size_t n2[2] = {atmos ? atmos->nmu : 0, atmos ? atmos->nE : 0};
+    if (atm_ext == 6) walk_reset(&wst, g2, 2);
     int terminate = 0;
 #pragma omp for schedule(static, 1)
     for (long ii = 0; ii < (long)S0; ii++) {
@@ -527,6 +610,11 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                   double I_E, Q_E = 0.0;
                   if (atm_ext == 2) {
                     I_E = eval_num4d(atmos, &nst, Ep, ABB, VEC);
+                  } else if (atm_ext == 6) {
+                    /* integrator_for_azimuthal_invariance_split.pyx:457-460 */
+                    double q[2] = {ABB, Ep * 0.001956951};
+                    I_E = walk_eval(g2, n2, 2, atmos->I, &wst, q);
+                    if (I_E < 0.0) I_E = 0.0;
                   } else if (atm_ext == 3) { /* hot_BB_burst.pyx: I and Q */
                     I_E = eval_bb(Ep, VEC) * (0.421 + 0.868 * ABB);
                     Q_E = (0.1171 * (ABB - 1.) / (1. + 3.582 * ABB)) * I_E;
@@ -644,6 +732,50 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
       }
   free(priv); free(cos_defl); free(ca_alt);
   return terminate_any ? 1 : 0;
+}
+
+/* ================================================================== */
+/* split integrator: cellmesh/integrator_for_azimuthal_invariance_split.pyx */
+/* the 5-D split atmosphere (t_e, t_bb, tau, mu, E) is reduced once to  */
+/* (mu, E) at the first cell's parameters (hot_Num5D_split.pyx:566-640, */
+/* produce_2D_data and make_atmosphere_2D), then integrated as above    */
+/* ================================================================== */
+typedef struct {
+  const double *grid[5];
+  size_t n[5];
+  const double *I;
+} xo_atmos5d;
+
+int xo_integrate_split(int n_threads, double R, double omega, double r_s,
+                       double inclination, size_t S0, size_t S1,
+                       const double *cellArea, const double *radius_arr,
+                       const double *u_arr, const double *theta, const double *phi,
+                       const double *srcCellParams, size_t n_params,
+                       const int *radiates, const double *correction,
+                       size_t n_correction, size_t N_R, const double *deflection,
+                       const double *cos_alpha, const double *lag,
+                       const double *maxDeflection, const double *cos_gammaArray,
+                       size_t N_E, const double *energies, size_t N_L,
+                       const double *leaves, size_t N_P, const double *phases,
+                       const xo_atmos5d *atm5, int image_order_limit, double *flux) {
+  const size_t nmu = atm5->n[3], nE = atm5->n[4];
+  double *I2 = (double *)malloc(nmu * nE * sizeof(double));
+  walk_state st;
+  walk_reset(&st, atm5->grid, 5);
+  for (size_t i = 0; i < nmu; i++)
+    for (size_t j = 0; j < nE; j++) {
+      const double v[5] = {srcCellParams[0], srcCellParams[1], srcCellParams[2],
+                           atm5->grid[3][i], atm5->grid[4][j]};
+      I2[i * nE + j] = walk_eval(atm5->grid, atm5->n, 5, atm5->I, &st, v);
+    }
+  xo_atmos4d a2 = {NULL, NULL, atm5->grid[3], atm5->grid[4], I2, 0, 0, nmu, nE};
+  int rc = xo_integrate(n_threads, R, omega, r_s, inclination, S0, S1, cellArea, radius_arr,
+                        u_arr, theta, phi, srcCellParams, n_params, radiates, correction,
+                        n_correction, N_R, deflection, cos_alpha, lag, maxDeflection,
+                        cos_gammaArray, N_E, energies, N_L, leaves, N_P, phases, 6, &a2,
+                        image_order_limit, flux, NULL, NULL);
+  free(I2);
+  return rc;
 }
 
 /* ================================================================== */

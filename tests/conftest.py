@@ -144,3 +144,27 @@ def stokes_args(golden, case, ext, corrected, image_order_limit=None):
                  f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
                  f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"], f["phases"],
                  (), (), (), ext, 1 if corrected else None, 0, iol)
+
+
+# the split fixture's cases: (tag, base fixture)
+SPLIT_CASES = (("config1", "config1"), ("num4d_omit", "num4d_omit"),
+               ("config1_corrected", "config1"), ("config1_outside", "config1"))
+
+
+def split_args(golden, tag, case, image_order_limit=None):
+    """Arguments of integrator_for_azimuthal_invariance_split.integrate for a
+    split.npz case on its base fixture's mesh and rays (uniform (t_e, t_bb,
+    tau) over the cells, the table of synthetic.split_table)."""
+    from xpsi_gb300 import synthetic
+    f = golden(case)
+    z = golden("split")
+    S = int(f["S"])
+    params = np.ones((S, S, 3)) * z[tag + "_vec"]
+    corr = z.get(tag + "_correction")
+    iol = image_order_limit if image_order_limit is not None else (
+        int(f["image_order_limit"]) or None)
+    return (1, float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+            f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], params, f["radiates"],
+            corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"],
+            f["cos_gamma"], f["energies"], f["leaves"], f["phases"], synthetic.split_table(),
+            (), None, 1 if corr is not None else None, 0, iol)

@@ -25,6 +25,7 @@ Cases
   stokes         the Stokes I/Q/U integrator for the burst blackbody and the
                  plain blackbody with a correction.
   gaussian       the Gaussian likelihoods of polarimetry.
+  split          the split integrator with a synthetic 5-D split atmosphere.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -475,6 +476,44 @@ def gaussian(xpsi):
          expec=expec, qn=qn, qn_err=qn_err, star=star, loglike_qn=ll_qn)
 
 
+def split(xpsi):
+    """The split integrator (integrator_for_azimuthal_invariance_split.pyx):
+    the 5-D split atmosphere of synthetic.split_table reduced to (mu, E) at
+    the first cell's (t_e, t_bb, tau) (hot_Num5D_split.pyx:566-640) and
+    interpolated per leaf and energy (hot_Num2D_split.pyx:200-384), on
+    config1's mesh (300 Hz) and num4d_omit's (600 Hz), with a blackbody
+    elsewhere's correction, and with (t_e, t_bb, tau) outside the table
+    (above, above, below: the cached walk clamps the first query only)."""
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance_split import integrate
+    atm = synthetic.split_table()
+    out = {}
+    for tag, case, vec, corr_T in (("config1", "config1", (0.7, 0.004, 1.5), None),
+                                   ("num4d_omit", "num4d_omit", (0.45, 0.0035, 2.2), None),
+                                   ("config1_corrected", "config1", (0.7, 0.004, 1.5), 5.9),
+                                   ("config1_outside", "config1", (1.35, 0.0063, 0.4), None)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        params = np.ones((S, S, 3)) * np.array(vec)
+        corr = None
+        if corr_T is not None:
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = corr_T
+            corr[..., 1] = f["effGrav"][:, None]
+        st, flux = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                             float(f["inclination"]), f["cellArea"], f["radius"], f["u"],
+                             f["theta"], f["phi"], params, f["radiates"], corr, int(f["N_R"]),
+                             f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"],
+                             f["cos_gamma"], f["energies"], f["leaves"], f["phases"], atm, (),
+                             None, 1 if corr is not None else None, 0,
+                             int(f["image_order_limit"]) or None)
+        assert st == 0
+        out[tag + "_flux"] = flux
+        out[tag + "_vec"] = np.array(vec)
+        if corr is not None:
+            out[tag + "_correction"] = corr
+    save("split", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -486,6 +525,7 @@ def main():
     synthesis(xpsi)
     stokes(xpsi)
     gaussian(xpsi)
+    split(xpsi)
 
 
 if __name__ == "__main__":

@@ -37,3 +37,19 @@ def test_install_rebinds_path_callables():
     assert hr._integratorIQU is integratorIQU_for_azimuthal_invariance.integrate
     hr.symmetry = False
     assert hr._integrator is integrator.integrate
+
+
+def test_install_binds_split_integrator():
+    import importlib
+    xpsi = H.load()
+    import xpsi_gb300
+    from xpsi_gb300.cellmesh import integrator_for_azimuthal_invariance_split as split
+    done = xpsi_gb300.install(xpsi)
+    HR = importlib.import_module("xpsi.HotRegion").HotRegion
+    hr = object.__new__(HR)
+    hr._split = True
+    hr.symmetry = True
+    assert hr._integrator is split.integrate
+    if "xpsi.cellmesh.integrator_for_azimuthal_invariance_split.integrate" in done:
+        mod = importlib.import_module("xpsi.cellmesh.integrator_for_azimuthal_invariance_split")
+        assert mod.integrate is split.integrate

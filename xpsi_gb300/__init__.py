@@ -7,6 +7,8 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
     xpsi_gb300.cellmesh.rays.compute_rays
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
     xpsi_gb300.cellmesh.integrator.integrate          (HotRegion symmetry=False)
+    xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance_split.integrate
+                                                      (HotRegion split=True)
     xpsi_gb300.cellmesh.integratorIQU_for_azimuthal_invariance.integrate (Stokes)
     xpsi_gb300.cellmesh.global_mesh.construct_closed_cellMesh   (elsewhere)
     xpsi_gb300.cellmesh.integrator_for_time_invariance.integrate (elsewhere)
@@ -38,6 +40,7 @@ def install(xpsi_module):
     from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
     from .cellmesh import integrator as general
+    from .cellmesh import integrator_for_azimuthal_invariance_split as split
     from .cellmesh import integratorIQU_for_azimuthal_invariance as iqu
     from .tools import energy_integrator as ei
     from .tools import phase_integrator as pint, synthesise as syn
@@ -57,6 +60,8 @@ def install(xpsi_module):
          global_mesh.construct_closed_cellMesh),
         ("xpsi.cellmesh.integrator_for_time_invariance", "integrate", tinv.integrate),
         ("xpsi.cellmesh.integrator", "integrate", general.integrate),
+        ("xpsi.cellmesh.integrator_for_azimuthal_invariance_split", "integrate",
+         split.integrate),
         ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance", "integrate", iqu.integrate),
         ("xpsi.tools.phase_integrator", "phase_integrator", pint.phase_integrator),
         ("xpsi.likelihoods._gaussian_likelihood_given_background_IQU",
@@ -100,6 +105,9 @@ def install(xpsi_module):
             self._integrator = integ.integrate if declaration else general.integrate
             if declaration:
                 self._integratorIQU = iqu.integrate
+        elif declaration:
+            # split=True and symmetry=False raise in the original setter
+            self._integrator = split.integrate
     HotRegion.symmetry = property(HotRegion.symmetry.fget, _symmetry)
     done.append("xpsi.HotRegion.HotRegion.symmetry")
     return done

@@ -85,6 +85,11 @@ class Atmos4D(C.Structure):
                 ("nT", SZ), ("ng", SZ), ("nmu", SZ), ("nE", SZ), ("intensity_f32", P)]
 
 
+class Atmos5D(C.Structure):
+    """xgpu_atmos5d: a split atmosphere's 5 grids and intensity table."""
+    _fields_ = [("grid", P * 5), ("n", SZ * 5), ("intensity", P)]
+
+
 class Mesh(C.Structure):
     _fields_ = [("S0", I32), ("S1", I32), ("row_off", I64), ("cell_off", I64),
                 ("omega", D), ("inclination", D), ("image_order_limit", I32),
@@ -173,6 +178,9 @@ def _bind(L):
         "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ, SZ,
                                      P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
                                      C.POINTER(Atmos4D), C.c_int, C.c_int, P]),
+        "xgpu_integrate_split": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ,
+                                           SZ, P, P, P, P, P, SZ, P, SZ, P, SZ, P,
+                                           C.POINTER(Atmos5D), C.c_int, C.c_int, P]),
         "xgpu_energy_integrator": (C.c_int, [SZ, SZ, P, P, SZ, P, P]),
         "xgpu_response_fold": (C.c_int, [SZ, SZ, SZ, P, SZ, P, P]),
         "xgpu_precomputation": (C.c_int, [SZ, SZ, P, P]),
@@ -249,10 +257,10 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_integrate_general", "xgpu_compute_expected_counts",
             "xgpu_phase_integrator", "xgpu_poisson", "xgpu_expected_counts_batch",
             "xgpu_poisson_batch", "xgpu_integrate_stokes", "xgpu_gaussian_loglike",
-            "xgpu_gaussian_loglike_batch"]
+            "xgpu_gaussian_loglike_batch", "xgpu_integrate_split"]
 
 
-ABI_VERSION = 2  # XGPU_ABI_VERSION of include/xpsi_gb300.h
+ABI_VERSION = 3  # XGPU_ABI_VERSION of include/xpsi_gb300.h
 
 
 def lib():

@@ -181,7 +181,8 @@ int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u, const double *r_s,
 namespace {
 int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
-                         int target_ctas, void *stream, int mixed);
+                         int target_ctas, void *stream, int mixed,
+                         const double *split_slab = nullptr);
 }
 
 int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
@@ -203,7 +204,7 @@ int xgpu_integrate_batch_mixed(int n_meshes, const xgpu_mesh *meshes, int64_t n_
 namespace {
 int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
-                         int target_ctas, void *stream, int mixed) {
+                         int target_ctas, void *stream, int mixed, const double *split_slab) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (n_meshes <= 0) return 0;
   if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
@@ -211,7 +212,9 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   for (int m = 0; m < n_meshes; m++) {
     if (meshes[m].atm_ext == 2 && d->atmos.intensity == nullptr)
       return fail_msg("a Num4D mesh needs the atmosphere table");
-    if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2)
+    if (meshes[m].atm_ext == 6 && (split_slab == nullptr || mixed))
+      return fail_msg("atm_ext 6 (split) is reached through xgpu_integrate_split only");
+    if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2 && meshes[m].atm_ext != 6)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
   }
   if (d->correction != nullptr && mixed)
@@ -248,7 +251,7 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   CK(cudaMemsetAsync(dpart.p, 0, part_n * sizeof(double), st));
   if ((rc = dalloc(dstate, (size_t)3 * n_rows + 16, st))) return rc;
   Dev dslab;
-  if (d->atmos.intensity != nullptr &&
+  if (d->atmos.intensity != nullptr && split_slab == nullptr &&
       (rc = dalloc(dslab, (size_t)n_chunks * d->atmos.nmu * d->atmos.nE * sizeof(double), st)))
     return rc;
   CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
@@ -281,7 +284,8 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.member_status = d->mesh_status;
   a.flux = d->flux;
   a.flop_counter = d->flop_counter;
-  a.slab = d->atmos.intensity != nullptr ? dslab.as<double>() : nullptr;
+  a.slab = d->atmos.intensity != nullptr && split_slab == nullptr ? dslab.as<double>() : nullptr;
+  a.split_slab = split_slab;
   a.mixed = mixed;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
@@ -383,7 +387,12 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R, double *
   return 0;
 }
 
-int xgpu_integrate(double R, double omega, double r_s, double inclination, size_t S0,
+}  // extern "C"
+
+namespace {
+// the drop-in integrators' common host path: upload, one batched launch on
+// the library stream, copy back
+int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
                    size_t S1, const double *cellArea, const double *radius,
                    const double *r_s_over_r, const double *theta, const double *phi,
                    const double *srcCellParams, size_t n_params, const int32_t *radiates,
@@ -391,21 +400,15 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
                    const double *deflection, const double *cos_alpha, const double *lag,
                    const double *maxDeflection, const double *cos_gamma, size_t N_E,
                    const double *energies, size_t N_L, const double *leaves, size_t N_P,
-                   const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
-                   int else_atm_ext, int image_order_limit, double *flux) {
-  (void)R;
-  (void)r_s;
-  cudaStream_t st;
+                   const double *phases, int atm_ext, const xg::Atmos4D &A,
+                   const double *split_slab, int else_atm_ext, int image_order_limit,
+                   double *flux) {
   int rc;
-  if ((rc = lib_stream(&st))) return rc;
   if (n_params < 2) return fail_msg("srcCellParams needs at least 2 parameters per cell");
-  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
   if (correction && else_atm_ext != 1)
     return fail_msg("the GPU integrator corrects for a blackbody elsewhere only");
   if (correction && n_correction < 1)
     return fail_msg("correction vectors need at least 1 parameter per cell");
-  xg::Atmos4D A{};
-  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
   const size_t cells = S0 * S1;
   Dev dcorr;
   if (correction && (rc = upload(dcorr, correction, cells * n_correction, st))) return rc;
@@ -433,7 +436,7 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   d.cellArea = dA.as<double>(); d.phi = dphi.as<double>(); d.params = dpar.as<double>();
   d.n_params = (int32_t)n_params; d.radiates = dR.as<int32_t>();
   d.energies = dE.as<double>(); d.leaves = dLv.as<double>(); d.phases = dP.as<double>();
-  if (atm_ext == 2) {
+  if (atm_ext == 2 || atm_ext == 6) {
     d.atmos = xgpu_atmos4d{A.logT, A.logg, A.mu, A.logE, A.I, (size_t)A.nT, (size_t)A.ng,
                            (size_t)A.nmu, (size_t)A.nE, nullptr};
   }
@@ -441,14 +444,100 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   d.mesh_status = dst.as<int32_t>();
   d.correction = correction ? dcorr.as<double>() : nullptr;
   d.n_correction = (int32_t)n_correction;
-  rc = xgpu_integrate_batch(1, &mesh, (int64_t)S0, (int)N_R, (int)N_E, (int)N_L, (int)N_P, &d,
-                            0, st);
+  rc = integrate_batch_impl(1, &mesh, (int64_t)S0, (int)N_R, (int)N_E, (int)N_L, (int)N_P, &d,
+                            0, st, 0, split_slab);
   if (rc) return rc;
   int32_t status = 0;
   CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(flux, dF.p, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return status != 0 ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xgpu_integrate(double R, double omega, double r_s, double inclination, size_t S0,
+                   size_t S1, const double *cellArea, const double *radius,
+                   const double *r_s_over_r, const double *theta, const double *phi,
+                   const double *srcCellParams, size_t n_params, const int32_t *radiates,
+                   const double *correction, size_t n_correction, size_t N_R,
+                   const double *deflection, const double *cos_alpha, const double *lag,
+                   const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                   const double *energies, size_t N_L, const double *leaves, size_t N_P,
+                   const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
+                   int else_atm_ext, int image_order_limit, double *flux) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
+  if (atm_ext != 1 && atm_ext != 2) return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+  xg::Atmos4D A{};
+  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  return integrate_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta,
+                        phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                        deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
+                        N_L, leaves, N_P, phases, atm_ext, A, nullptr, else_atm_ext,
+                        image_order_limit, flux);
+}
+
+int xgpu_integrate_split(double R, double omega, double r_s, double inclination, size_t S0,
+                         size_t S1, const double *cellArea, const double *radius,
+                         const double *r_s_over_r, const double *theta, const double *phi,
+                         const double *srcCellParams, size_t n_params,
+                         const int32_t *radiates, const double *correction,
+                         size_t n_correction, size_t N_R, const double *deflection,
+                         const double *cos_alpha, const double *lag,
+                         const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                         const double *energies, size_t N_L, const double *leaves,
+                         size_t N_P, const double *phases, const xgpu_atmos5d *atmos,
+                         int else_atm_ext, int image_order_limit, double *flux) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (!atmos || !atmos->intensity) return fail_msg("the split integrator needs the 5-D atmosphere");
+  if (n_params < 3) return fail_msg("the split atmosphere needs 3 parameters per cell");
+  if (S0 * S1 == 0) return fail_msg("empty cell mesh");
+  size_t nI = 1, ng = 0;
+  for (int d = 0; d < 5; d++) {
+    if (atmos->n[d] < 4) return fail_msg("split grids need at least 4 nodes per dimension");
+    nI *= atmos->n[d];
+    ng += atmos->n[d];
+  }
+  const size_t nmu = atmos->n[3], nE = atmos->n[4];
+  Dev dg, dI, dslab;
+  if ((rc = dalloc(dg, ng * 8, st)) || (rc = upload(dI, atmos->intensity, nI, st)) ||
+      (rc = dalloc(dslab, nmu * nE * 8, st)))
+    return rc;
+  xg::SplitArgs sa{};
+  double *gp = dg.as<double>();
+  for (int d = 0; d < 5; d++) {
+    CK(cudaMemcpyAsync(gp, atmos->grid[d], atmos->n[d] * 8, cudaMemcpyHostToDevice, st));
+    sa.grid[d] = gp;
+    sa.n[d] = (int)atmos->n[d];
+    gp += atmos->n[d];
+  }
+  sa.I = dI.as<double>();
+  // produce_2D_data at the first cell's parameter vector
+  // (integrator_for_azimuthal_invariance_split.pyx:270)
+  for (int d = 0; d < 3; d++) sa.vec[d] = srcCellParams[d];
+  sa.out = dslab.as<double>();
+  xg::launch_split_reduce(sa, st);
+  CK(cudaGetLastError());
+  xg::Atmos4D A{};
+  A.mu = sa.grid[3];
+  A.logE = sa.grid[4];
+  A.I = dslab.as<double>();
+  A.nmu = (int)nmu;
+  A.nE = (int)nE;
+  return integrate_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta,
+                        phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                        deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
+                        N_L, leaves, N_P, phases, 6, A, dslab.as<double>(), else_atm_ext,
+                        image_order_limit, flux);
 }
 
 int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination, size_t S0,

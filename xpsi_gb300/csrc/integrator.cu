@@ -644,7 +644,7 @@ __global__ void num4d_scan_kernel(IntegrateArgs a) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= a.n_members) return;
   const MemberDesc M = a.members[m];
-  if (M.atm != 2) return;
+  if (M.atm != 2 && M.atm != 6) return;
   uint8_t carry = 0;
   for (int i = 0; i < M.S0; i++) {
     int64_t row = M.row_off + i;
@@ -810,7 +810,11 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   const MemberDesc M = a.members[m];
   const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  const bool num4d = (M.atm == 2);
+  // split (atm 6): the (mu, E) table of a split atmosphere, reduced once per
+  // call, with the energy in electron rest energies and no 10^(3 log T)
+  // (integrator_for_azimuthal_invariance_split.pyx:270-275,457-476)
+  const bool split = (M.atm == 6) && !kMixed;
+  const bool num4d = (M.atm == 2) || split;
   const int nmu = a.atmos.I ? a.atmos.nmu : 0, nEt = a.atmos.I ? a.atmos.nE : 0;
   const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt, (int)sizeof(PieceT<WT>), a.N_R);
   const int EC = L.EC;
@@ -842,7 +846,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         as.fgEo[t] = b + i < nEt ? (float)(as.gE[b + i] - as.gE[b]) : 0.0f;
       }
     }
-    slab = a.slab + (size_t)chunk * nmu * nEt;
+    slab = split ? const_cast<double *>(a.split_slab) : a.slab + (size_t)chunk * nmu * nEt;
     slabf = reinterpret_cast<float *>(slab);
     __syncthreads();
   }
@@ -874,7 +878,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     }
     __syncthreads();
     double E_eff = 0.0, p3 = 0.0;
-    if (num4d) {
+    if (split) {
+      p3 = 1.0;
+    } else if (num4d) {
       // contract the (log T, log g) stencil of this parallel once:
       // slab[mu][logE] = sum_ij w_T[i] w_g[j] table[bT+i][bg+j][mu][logE]
       double vT = c.vec0, vg = c.vec1;
@@ -934,7 +940,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     const float p3f = (float)p3;
     const double fix = num4d ? (norm * p3) / ((double)(float)norm * (double)p3f)
                              : norm / (double)(float)norm;
-    const double lg_Eeff = num4d ? log10(E_eff) : 0.0;
+    const double lg_Eeff = (num4d && !split) ? log10(E_eff) : 0.0;
     // the elsewhere correction's blackbody temperature at the parallel's
     // first radiating cell (:469-476)
     const bool corr = !kMixed && a.correction != nullptr;
@@ -994,7 +1000,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             as.fabb[sidx] = (float)g.ABB[sidx];
             as.fgeom[sidx] = (float)g.GEOM[sidx];
           }
-          if (num4d) g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
+          if (split) g.lzs[sidx] = g.Z[sidx];
+          else if (num4d) g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
         }
       }
       __syncthreads();
@@ -1008,7 +1015,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
       for (int e0 = 0; e0 < N_E; e0 += EC) {
         const int ne = min(EC, N_E - e0);
         if (num4d) {
-          for (int t = threadIdx.x; t < ne; t += blockDim.x) g.lgE[t] = log10(a.energies[e0 + t]);
+          for (int t = threadIdx.x; t < ne; t += blockDim.x)
+            g.lgE[t] = split ? a.energies[e0 + t] : log10(a.energies[e0 + t]);
           __syncthreads();
         }
         // specific intensities of every profile column (:445-478).  With
@@ -1027,7 +1035,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               if constexpr (kMixed) {
                 float I_E;
                 if (num4d) {
-                  const double v3 = g.lgE[pl] - g.lzs[s];
+                  // split: E' = E / Z in electron rest energies (:457-458)
+                  const double v3 = split ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
+                                          : g.lgE[pl] - g.lzs[s];
                   if (p == 0 && g.clamp0[s]) {
                     I_E = eval_num4d_f(a.atmos, as, slabf,
                                        mu_stencil_f(a.atmos, as, as.fabb[s], true), v3, p3f);
@@ -1046,7 +1056,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               } else {
                 double I_E;
                 if (num4d) {
-                  const double v3 = g.lgE[pl] - g.lzs[s];
+                  // split: E' = E / Z in electron rest energies (:457-458)
+                  const double v3 = split ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
+                                          : g.lgE[pl] - g.lzs[s];
                   if (p == 0 && g.clamp0[s]) {
                     I_E = eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, g.ABB[s], true),
                                        v3, p3);
@@ -1442,6 +1454,87 @@ __global__ void reduce_stokes_kernel(IntegrateArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// The split atmosphere's (mu, E) table at the first cell's (t_e, t_bb, tau)
+// (integrator_for_azimuthal_invariance_split.pyx:270-275 calls
+// hot_Num5D_split.pyx:267-481 once per (mu, E) node, mu outer, from a fresh
+// evaluator).  The cached walk's state at each call is known in closed form:
+// on t_e, t_bb, tau the first call moves the base node from 0 (clamping a
+// query beyond the top of the grid on that call only) and later calls leave
+// it; a query on the node mu_k or E_k has base node min(max(k - 2, 0), n - 4).
+// On those two dimensions only the weight of the node itself is nonzero, so
+// the 64 remaining terms are summed in the reference's order with its
+// products (numerators, then inverse denominators, multiplied dimension by
+// dimension) and without contraction, which reproduces its rounding.  One
+// thread per (mu, E) node.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void walk_factors(const double *P, int b, double x, double D[4],
+                                             double S[4]) {
+  D[0] = x - P[b + 1]; D[0] *= x - P[b + 2]; D[0] *= x - P[b + 3];
+  D[1] = x - P[b];     D[1] *= x - P[b + 2]; D[1] *= x - P[b + 3];
+  D[2] = x - P[b];     D[2] *= x - P[b + 1]; D[2] *= x - P[b + 3];
+  D[3] = x - P[b];     D[3] *= x - P[b + 1]; D[3] *= x - P[b + 2];
+  S[0] = 1.0 / (P[b] - P[b + 1]);     S[0] /= P[b] - P[b + 2];     S[0] /= P[b] - P[b + 3];
+  S[1] = 1.0 / (P[b + 1] - P[b]);     S[1] /= P[b + 1] - P[b + 2]; S[1] /= P[b + 1] - P[b + 3];
+  S[2] = 1.0 / (P[b + 2] - P[b]);     S[2] /= P[b + 2] - P[b + 1]; S[2] /= P[b + 2] - P[b + 3];
+  S[3] = 1.0 / (P[b + 3] - P[b]);     S[3] /= P[b + 3] - P[b + 1]; S[3] /= P[b + 3] - P[b + 2];
+}
+
+__global__ void split_reduce_kernel(SplitArgs a) {
+  const int n3 = a.n[3], n4 = a.n[4];
+  // the first call's walk on t_e, t_bb, tau from base node 0
+  __shared__ int b[3];
+  __shared__ double vfirst[3];
+  if (threadIdx.x < 3) {
+    const int d = threadIdx.x, n = a.n[d];
+    const double *P = a.grid[d];
+    double v = a.vec[d];
+    int bn = 0;
+    if (v > P[2] && n != 4) {
+      for (int it = 0; it < n && v > P[bn + 2]; it++) {
+        if (bn < n - 4) {
+          bn++;
+        } else {
+          if (v >= P[n - 1]) v = P[n - 1];
+          break;
+        }
+      }
+    }
+    b[d] = bn;
+    vfirst[d] = v;
+  }
+  __syncthreads();
+  const size_t s3 = (size_t)n4, s2 = (size_t)n3 * n4, s1 = (size_t)a.n[2] * s2,
+               s0 = (size_t)a.n[1] * s1;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n3 * n4; t += gridDim.x * blockDim.x) {
+    const int i = t / n4, j = t - i * n4;
+    double D[3][4], S[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++) walk_factors(a.grid[d], b[d], t == 0 ? vfirst[d] : a.vec[d], D[d], S[d]);
+    const int b3 = min(max(i - 2, 0), n3 - 4), b4 = min(max(j - 2, 0), n4 - 4);
+    double D3[4], S3[4], D4[4], S4[4];
+    walk_factors(a.grid[3], b3, a.grid[3][i], D3, S3);
+    walk_factors(a.grid[4], b4, a.grid[4][j], D4, S4);
+    const double d3 = D3[i - b3], sp3 = S3[i - b3], d4 = D4[j - b4], sp4 = S4[j - b4];
+    const double *T = a.I + (size_t)i * s3 + j;
+    double I = 0.0;
+    for (int k0 = 0; k0 < 4; k0++)
+      for (int k1 = 0; k1 < 4; k1++)
+        for (int k2 = 0; k2 < 4; k2++) {
+          double dp = D[0][k0];
+          dp = __dmul_rn(dp, D[1][k1]); dp = __dmul_rn(dp, D[2][k2]);
+          dp = __dmul_rn(dp, d3); dp = __dmul_rn(dp, d4);
+          double sp = S[0][k0];
+          sp = __dmul_rn(sp, S[1][k1]); sp = __dmul_rn(sp, S[2][k2]);
+          sp = __dmul_rn(sp, sp3); sp = __dmul_rn(sp, sp4);
+          const double v = T[(size_t)(b[0] + k0) * s0 + (size_t)(b[1] + k1) * s1 +
+                             (size_t)(b[2] + k2) * s2];
+          I = __dadd_rn(I, __dmul_rn(__dmul_rn(dp, sp), v));
+        }
+    a.out[t] = I;
+  }
+}
+
 // ordered reduction of the chunk partials and the 1/(E keV) factor (:605-612)
 __global__ void reduce_flux_kernel(IntegrateArgs a) {
   const int m = blockIdx.y;
@@ -1493,6 +1586,11 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
 }
 
+
+void launch_split_reduce(const SplitArgs &a, cudaStream_t st) {
+  const int n = a.n[3] * a.n[4];
+  split_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
+}
 
 size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R) {
   return stokes_smem(N_L, N_P, N_E, N_R);

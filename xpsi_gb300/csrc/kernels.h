@@ -77,7 +77,19 @@ struct IntegrateArgs {
   double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
   int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
   double *flux_q = nullptr, *flux_u = nullptr;  // Stokes Q, U (launch_stokes only)
+  // split atmosphere (members with atm 6): the reduced (mu, E) table
+  // [nmu][nE] on the grids atmos.mu, atmos.logE (E in electron rest energies)
+  const double *split_slab = nullptr;
 };
+// the 5-D split atmosphere's reduction to (mu, E) at one parameter vector
+struct SplitArgs {
+  const double *grid[5];
+  int n[5];
+  const double *I;      // [n0][n1][n2][n3][n4]
+  double vec[3];        // t_e, t_bb, tau
+  double *out;          // [n3][n4]
+};
+void launch_split_reduce(const SplitArgs &a, cudaStream_t st);
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
 // Stokes I (a.flux), Q, U for blackbody (1) and burst blackbody (3) members;
 // a.partial: stokes_partial_doubles(a) doubles, zeroed; a.chunk_* unused

@@ -35,6 +35,21 @@ def num4d_table(shape=(35, 14, 67, 166), seed=2,
     return (logT, logg, mu, logE, np.ascontiguousarray(I.reshape(-1)))
 
 
+def split_table(shape=(6, 5, 5, 12, 64), seed=4,
+                ranges=((0.2, 1.2), (0.002, 0.006), (0.5, 3.0), (0.0, 1.0), (5e-5, 0.03))):
+    """A 5-D split atmosphere (t_e, t_bb, tau, mu, E in electron rest energies)
+    for the split integrator: a Comptonised-blackbody-like shape
+    x^2 exp(-E / t_bb') (1 + tau (0.3 + 0.7 mu)) (1 + 0.1 t_e) with
+    t_bb' = t_bb (1 + 0.2 tau), times 1 + 1e-3 seeded noise; positive
+    everywhere.  Returns the tuple X-PSI preloads (5 grids, intensity)."""
+    g = [np.linspace(lo, hi, n) for (lo, hi), n in zip(ranges, shape)]
+    te, tbb, tau, mu, E = np.meshgrid(*g, indexing="ij")
+    tb = tbb * (1.0 + 0.2 * tau)
+    I = (E / tb) ** 2 * np.exp(-E / tb) * (1.0 + tau * (0.3 + 0.7 * mu)) * (1.0 + 0.1 * te)
+    I = I * (1.0 + 1.0e-3 * np.random.default_rng(seed).standard_normal(I.shape))
+    return tuple(np.ascontiguousarray(x) for x in g) + (np.ascontiguousarray(I.reshape(-1)),)
+
+
 def gaussian_response(n_channels, n_inputs, e_lo=0.1, e_hi=10.0, width=0.1):
     """Synthetic response matrix [channels, inputs]: Gaussian redistribution
     (sigma = width * E) times a smooth effective area of 100-1000 cm^2,
