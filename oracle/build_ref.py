@@ -42,6 +42,7 @@ MODULES = [
     "cellmesh.integratorIQU_for_azimuthal_invariance",
     "surface_radiation_field.hot_Num2D_split",
     "cellmesh.integrator_for_azimuthal_invariance_split",
+    "cellmesh.integratorIQU_for_azimuthal_invariance_split",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
     "likelihoods._gaussian_likelihood_QnUn",

@@ -43,7 +43,7 @@ class Atmos4D(C.Structure):
     _fields_ = [("logT", C.c_void_p), ("logg", C.c_void_p), ("mu", C.c_void_p),
                 ("logE", C.c_void_p), ("I", C.c_void_p),
                 ("nT", C.c_size_t), ("ng", C.c_size_t), ("nmu", C.c_size_t),
-                ("nE", C.c_size_t)]
+                ("nE", C.c_size_t), ("Q", C.c_void_p)]
 
 
 def lib():
@@ -64,6 +64,9 @@ def lib():
                 C.c_size_t, P, C.c_int, P, C.c_int, P, P, P]
             L.xo_integrate_split.restype = C.c_int
             L.xo_integrate_split.argtypes = list(L.xo_integrate.argtypes)[:-6] + [P, C.c_int, P]
+            L.xo_integrate_split_iqu.restype = C.c_int
+            L.xo_integrate_split_iqu.argtypes = (list(L.xo_integrate.argtypes)[:-6] +
+                                                 [P, P, C.c_int, P, P, P])
             L.xo_integrate_general.restype = C.c_int
             L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)[:-2]
             L.xo_integrate_time_invariant.restype = C.c_int
@@ -112,12 +115,26 @@ def compute_rays(N_T, N_u, r_s, r_s_over_R, maxAlpha, N_R):
     return t, D, CA, L, MD
 
 
-def _atmos_struct(hot_atmosphere):
+def _atmos_struct(hot_atmosphere, atm_ext=2, hot_atmosphere_Q=None):
+    """The C struct of a preloaded atmosphere: the 4-D table (logT, logg, mu,
+    logE, I), or for atm_ext 4 (Pol_Num2D) the 2-D table (mu, logE, I) with
+    the Q table of hot_atmosphere_Q on the same grids."""
     if not hot_atmosphere:
         return None, ()
     keep = tuple(_c(a) for a in hot_atmosphere)
-    s = Atmos4D(*(_p(a).value for a in keep), keep[0].size, keep[1].size,
-                keep[2].size, keep[3].size)
+    if int(atm_ext) == 4:
+        q = None
+        if hot_atmosphere_Q:
+            qk = tuple(_c(a) for a in hot_atmosphere_Q)
+            if not (np.array_equal(qk[0], keep[0]) and np.array_equal(qk[1], keep[1])):
+                raise NotImplementedError("I and Q tables on different grids")
+            keep = keep + (qk[2],)
+            q = _p(qk[2]).value
+        s = Atmos4D(None, None, _p(keep[0]).value, _p(keep[1]).value, _p(keep[2]).value,
+                    0, 0, keep[0].size, keep[1].size, q)
+        return s, keep
+    s = Atmos4D(*(_p(a).value for a in keep[:5]), keep[0].size, keep[1].size,
+                keep[2].size, keep[3].size, None)
     return s, keep
 
 
@@ -128,7 +145,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
               phases, hot_atmosphere, elsewhere_atmosphere, hot_atm_ext,
               else_atm_ext, beam_opt, image_order_limit=None, R_in=1e6):
     """integrator_for_azimuthal_invariance.integrate (:70-665) for the
-    uniform BB / Num4D hot regions the likelihood path uses, with the
+    uniform BB / Num4D / Pol_Num2D (I) hot regions, with the
     correction for a blackbody elsewhere (else_atm_ext 1) when
     correction_srcCellParams is given."""
     if beam_opt != 0 or R_in < 1e6:
@@ -143,7 +160,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     rad = _c(CELL_RADIATES, np.int32)
     E = _c(energies); Lv = _c(leaves); P = _c(phases)
     out = np.zeros((E.size, P.size))
-    st, keep = _atmos_struct(hot_atmosphere)
+    st, keep = _atmos_struct(hot_atmosphere, hot_atm_ext)
     arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
             _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
             _c(cos_gammaArray)]
@@ -169,12 +186,12 @@ def integrate_iqu(numThreads, R, omega, r_s, inclination, cellArea,
                   hot_atmosphere_Q, elsewhere_atmosphere, hot_atm_ext, else_atm_ext, beam_opt,
                   image_order_limit=None, R_in=1e6):
     """integratorIQU_for_azimuthal_invariance.integrate (:68-743):
-    (0, flux_I, flux_Q, flux_U) or (1, None) for the blackbody (1), Num4D (2)
-    and burst blackbody (3) atmospheres."""
+    (0, flux_I, flux_Q, flux_U) or (1, None) for the blackbody (1), Num4D (2),
+    burst blackbody (3) and Pol_Num2D (4) atmospheres."""
     if beam_opt != 0 or R_in < 1e6:
         raise NotImplementedError("oracle covers beam_opt 0 without a disk")
-    if int(hot_atm_ext) not in (1, 2, 3):
-        raise NotImplementedError("oracle covers atmospheres 1, 2 and 3")
+    if int(hot_atm_ext) not in (1, 2, 3, 4):
+        raise NotImplementedError("oracle covers atmospheres 1 to 4")
     corr = None
     if correction_srcCellParams is not None:
         if int(else_atm_ext) != 1:
@@ -185,7 +202,8 @@ def integrate_iqu(numThreads, R, omega, r_s, inclination, cellArea,
     rad = _c(CELL_RADIATES, np.int32)
     E = _c(energies); Lv = _c(leaves); P = _c(phases)
     out = [np.zeros((E.size, P.size)) for _ in range(3)]
-    st, keep = _atmos_struct(hot_atmosphere_I if int(hot_atm_ext) == 2 else ())
+    st, keep = _atmos_struct(hot_atmosphere_I if int(hot_atm_ext) in (2, 4) else (),
+                             hot_atm_ext, hot_atmosphere_Q)
     arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
             _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
             _c(cos_gammaArray)]
@@ -429,3 +447,50 @@ def integrate_split(numThreads, R, omega, r_s, inclination, cellArea,
     if status != 0:
         return (1, None)
     return (0, out)
+
+
+def integrate_split_iqu(numThreads, R, omega, r_s, inclination, cellArea,
+                        radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                        CELL_RADIATES, correction_srcCellParams, numRays, deflection,
+                        cos_alpha, lag, maxDeflection, cos_gammaArray, energies, leaves,
+                        phases, hot_atmosphere_I, hot_atmosphere_Q, elsewhere_atmosphere,
+                        hot_atm_ext, else_atm_ext, beam_opt, image_order_limit=None,
+                        R_in=1e6):
+    """integratorIQU_for_azimuthal_invariance_split.integrate (:75-758):
+    (0, flux_I, flux_Q, flux_U) or (1, None) for split I and Q tables
+    (t_e, t_bb, tau, mu, E grids, values)."""
+    if beam_opt != 0 or R_in < 1e6:
+        raise NotImplementedError("oracle covers beam_opt 0 without a disk")
+    corr = None
+    if correction_srcCellParams is not None:
+        if int(else_atm_ext) != 1:
+            raise NotImplementedError("oracle corrects for a blackbody elsewhere only")
+        corr = _c(correction_srcCellParams)
+    A = _c(cellArea); S0, S1 = A.shape
+    par = _c(srcCellParams)
+    rad = _c(CELL_RADIATES, np.int32)
+    E = _c(energies); Lv = _c(leaves); P_ = _c(phases)
+    out = [np.zeros((E.size, P_.size)) for _ in range(3)]
+    kI = tuple(_c(a) for a in hot_atmosphere_I)
+    kQ = tuple(_c(a) for a in hot_atmosphere_Q)
+    aI = Atmos5D((C.c_void_p * 5)(*[_p(k).value for k in kI[:5]]),
+                 (C.c_size_t * 5)(*[k.size for k in kI[:5]]), _p(kI[5]).value)
+    aQ = Atmos5D((C.c_void_p * 5)(*[_p(k).value for k in kQ[:5]]),
+                 (C.c_size_t * 5)(*[k.size for k in kQ[:5]]), _p(kQ[5]).value)
+    arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
+            _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
+            _c(cos_gammaArray)]
+    status = lib().xo_integrate_split_iqu(
+        int(numThreads), float(R), float(omega), float(r_s), float(inclination),
+        S0, S1, _p(A), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
+        _p(par), par.shape[2], _p(rad), _p(corr) if corr is not None else None,
+        corr.shape[2] if corr is not None else 0, int(numRays), _p(arrs[4]), _p(arrs[5]),
+        _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
+        P_.size, _p(P_), C.cast(C.pointer(aI), C.c_void_p), C.cast(C.pointer(aQ), C.c_void_p),
+        int(image_order_limit or 0), _p(out[0]), _p(out[1]), _p(out[2]))
+    del kI, kQ
+    if status < 0:
+        raise NotImplementedError("I and Q split tables on different (mu, E) grids")
+    if status != 0:
+        return (1, None)
+    return (0, out[0], out[1], out[2])

@@ -15,10 +15,12 @@
  *   xo_integrate             cellmesh/integrator_for_azimuthal_invariance.pyx:70-665,
  *                            with Stokes Q and U as
  *                            cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743
- *                            (atmospheres 1, 2, 3 = hot_BB_burst.pyx)
+ *                            (atmospheres 1, 2, 3 = hot_BB_burst.pyx,
+ *                            4 = hot_Num2D.pyx)
  *                            atmospheres: hot_BB.pyx:54-98, hot_Num4D.pyx:248-461
  *   xo_integrate_split       cellmesh/integrator_for_azimuthal_invariance_split.pyx
  *                            (hot_Num5D_split.pyx, hot_Num2D_split.pyx)
+ *   xo_integrate_split_iqu   cellmesh/integratorIQU_for_azimuthal_invariance_split.pyx
  *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
@@ -241,9 +243,13 @@ int xo_compute_rays(int n_threads, size_t N_u, double r_s,
 /* atmospheres                                                        */
 /* ================================================================== */
 typedef struct {
-  /* numerical 4-D table, dims (logT, logg, mu, log10(E/kT)), row major */
+  /* numerical 4-D table, dims (logT, logg, mu, log10(E/kT)), row major;
+   * for the 2-D tables (atm_ext 4: Pol_Num2D, dims (mu, log10 E);
+   * atm_ext 6: a split atmosphere reduced to (mu, E)) only mu, logE, I and,
+   * for Stokes Q, the Q table on the same grids */
   const double *logT, *logg, *mu, *logE, *I;
   size_t nT, ng, nmu, nE;
+  const double *Q;
 } xo_atmos4d;
 
 /* hot_BB.pyx:54-82 (times the norm :84-98 applied by the caller) */
@@ -460,9 +466,11 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
   const int ns = (flux_Q != NULL && flux_U != NULL) ? 3 : 1;
   const double sin_i = sin(inclination), cos_i = cos(inclination);
   const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  /* hot_Num4D.pyx:441-461, hot_Num5D_split.pyx:538-563 (atm_ext 6: the split
-   * atmosphere reduced to (mu, E) by xo_integrate_split), hot_BB.pyx:84-98 */
-  const double norm = (atm_ext == 2 || atm_ext == 6) ? kErg / kHKeV : kErg * kPlanck;
+  /* hot_Num4D.pyx:441-461, hot_Num2D.pyx:359-367 (atm_ext 4),
+   * hot_Num5D_split.pyx:538-563 (atm_ext 6: the split atmosphere reduced to
+   * (mu, E) by xo_integrate_split), hot_BB.pyx:84-98 */
+  const double norm =
+      (atm_ext == 2 || atm_ext == 4 || atm_ext == 6) ? kErg / kHKeV : kErg * kPlanck;
   int nt = n_threads > 0 ? n_threads : 1;
   int terminate_any = 0;
   double *priv = (double *)calloc((size_t)nt * ns * N_E * N_P, sizeof(double));
@@ -497,10 +505,15 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
     const size_t NR = (size_t)ns * N_E;
     num4d_state nst;
     if (atm_ext == 2) num4d_reset(&nst, atmos);
-    walk_state wst;
+    /* the 2-D tables' evaluators, I and Q each with its own cached walk
+     * (hot_Num2D.pyx:56-146, hot_Num2D_split.pyx; one per thread) */
+    walk_state wst, wstq;
     const double *g2[2] = {atmos ? atmos->mu : NULL, atmos ? atmos->logE : NULL};
     const size_t n2[2] = {atmos ? atmos->nmu : 0, atmos ? atmos->nE : 0};
-    if (atm_ext == 6) walk_reset(&wst, g2, 2);
+    if (atm_ext == 4 || atm_ext == 6) {
+      walk_reset(&wst, g2, 2);
+      walk_reset(&wstq, g2, 2);
+    }
     int terminate = 0;
 #pragma omp for schedule(static, 1)
     for (long ii = 0; ii < (long)S0; ii++) {
@@ -610,11 +623,16 @@ int xo_integrate(int n_threads, double R, double omega, double r_s,
                   double I_E, Q_E = 0.0;
                   if (atm_ext == 2) {
                     I_E = eval_num4d(atmos, &nst, Ep, ABB, VEC);
-                  } else if (atm_ext == 6) {
-                    /* integrator_for_azimuthal_invariance_split.pyx:457-460 */
-                    double q[2] = {ABB, Ep * 0.001956951};
+                  } else if (atm_ext == 4 || atm_ext == 6) {
+                    /* Pol_Num2D at (mu, log10 E') (hot_Num2D.pyx:187-232,
+                     * 369-400), or the reduced split table at E' in electron
+                     * rest energies (integrator_for_azimuthal_invariance_split.pyx:457-460,
+                     * integratorIQU_for_azimuthal_invariance_split.pyx:515-520);
+                     * I clipped at 0, Q not */
+                    double q[2] = {ABB, atm_ext == 4 ? log10(Ep) : Ep * 0.001956951};
                     I_E = walk_eval(g2, n2, 2, atmos->I, &wst, q);
                     if (I_E < 0.0) I_E = 0.0;
+                    if (ns == 3 && atmos->Q) Q_E = walk_eval(g2, n2, 2, atmos->Q, &wstq, q);
                   } else if (atm_ext == 3) { /* hot_BB_burst.pyx: I and Q */
                     I_E = eval_bb(Ep, VEC) * (0.421 + 0.868 * ABB);
                     Q_E = (0.1171 * (ABB - 1.) / (1. + 3.582 * ABB)) * I_E;
@@ -746,6 +764,19 @@ typedef struct {
   const double *I;
 } xo_atmos5d;
 
+static double *split_reduce(const xo_atmos5d *atm5, const double *vec) {
+  const size_t nmu = atm5->n[3], nE = atm5->n[4];
+  double *I2 = (double *)malloc(nmu * nE * sizeof(double));
+  walk_state st;
+  walk_reset(&st, atm5->grid, 5);
+  for (size_t i = 0; i < nmu; i++)
+    for (size_t j = 0; j < nE; j++) {
+      const double v[5] = {vec[0], vec[1], vec[2], atm5->grid[3][i], atm5->grid[4][j]};
+      I2[i * nE + j] = walk_eval(atm5->grid, atm5->n, 5, atm5->I, &st, v);
+    }
+  return I2;
+}
+
 int xo_integrate_split(int n_threads, double R, double omega, double r_s,
                        double inclination, size_t S0, size_t S1,
                        const double *cellArea, const double *radius_arr,
@@ -758,23 +789,52 @@ int xo_integrate_split(int n_threads, double R, double omega, double r_s,
                        size_t N_E, const double *energies, size_t N_L,
                        const double *leaves, size_t N_P, const double *phases,
                        const xo_atmos5d *atm5, int image_order_limit, double *flux) {
-  const size_t nmu = atm5->n[3], nE = atm5->n[4];
-  double *I2 = (double *)malloc(nmu * nE * sizeof(double));
-  walk_state st;
-  walk_reset(&st, atm5->grid, 5);
-  for (size_t i = 0; i < nmu; i++)
-    for (size_t j = 0; j < nE; j++) {
-      const double v[5] = {srcCellParams[0], srcCellParams[1], srcCellParams[2],
-                           atm5->grid[3][i], atm5->grid[4][j]};
-      I2[i * nE + j] = walk_eval(atm5->grid, atm5->n, 5, atm5->I, &st, v);
-    }
-  xo_atmos4d a2 = {NULL, NULL, atm5->grid[3], atm5->grid[4], I2, 0, 0, nmu, nE};
+  double *I2 = split_reduce(atm5, srcCellParams);
+  xo_atmos4d a2 = {NULL, NULL, atm5->grid[3], atm5->grid[4], I2, 0, 0, atm5->n[3],
+                   atm5->n[4], NULL};
   int rc = xo_integrate(n_threads, R, omega, r_s, inclination, S0, S1, cellArea, radius_arr,
                         u_arr, theta, phi, srcCellParams, n_params, radiates, correction,
                         n_correction, N_R, deflection, cos_alpha, lag, maxDeflection,
                         cos_gammaArray, N_E, energies, N_L, leaves, N_P, phases, 6, &a2,
                         image_order_limit, flux, NULL, NULL);
   free(I2);
+  return rc;
+}
+
+/* integratorIQU_for_azimuthal_invariance_split.pyx:75-758: the I and Q
+ * split tables each reduced to (mu, E) at the first cell's vector by its own
+ * fresh evaluator (:310-322), then I, Q cos 2chi, Q sin 2chi per leaf and
+ * energy (:515-530) */
+int xo_integrate_split_iqu(int n_threads, double R, double omega, double r_s,
+                           double inclination, size_t S0, size_t S1,
+                           const double *cellArea, const double *radius_arr,
+                           const double *u_arr, const double *theta, const double *phi,
+                           const double *srcCellParams, size_t n_params,
+                           const int *radiates, const double *correction,
+                           size_t n_correction, size_t N_R, const double *deflection,
+                           const double *cos_alpha, const double *lag,
+                           const double *maxDeflection, const double *cos_gammaArray,
+                           size_t N_E, const double *energies, size_t N_L,
+                           const double *leaves, size_t N_P, const double *phases,
+                           const xo_atmos5d *atm5_I, const xo_atmos5d *atm5_Q,
+                           int image_order_limit, double *flux, double *flux_Q,
+                           double *flux_U) {
+  for (int d = 3; d < 5; d++) {
+    if (atm5_I->n[d] != atm5_Q->n[d]) return -1;
+    for (size_t k = 0; k < atm5_I->n[d]; k++)
+      if (atm5_I->grid[d][k] != atm5_Q->grid[d][k]) return -1;
+  }
+  double *I2 = split_reduce(atm5_I, srcCellParams);
+  double *Q2 = split_reduce(atm5_Q, srcCellParams);
+  xo_atmos4d a2 = {NULL, NULL, atm5_I->grid[3], atm5_I->grid[4], I2, 0, 0,
+                   atm5_I->n[3], atm5_I->n[4], Q2};
+  int rc = xo_integrate(n_threads, R, omega, r_s, inclination, S0, S1, cellArea, radius_arr,
+                        u_arr, theta, phi, srcCellParams, n_params, radiates, correction,
+                        n_correction, N_R, deflection, cos_alpha, lag, maxDeflection,
+                        cos_gammaArray, N_E, energies, N_L, leaves, N_P, phases, 6, &a2,
+                        image_order_limit, flux, flux_Q, flux_U);
+  free(I2);
+  free(Q2);
   return rc;
 }
 

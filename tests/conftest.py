@@ -168,3 +168,39 @@ def split_args(golden, tag, case, image_order_limit=None):
             corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"],
             f["cos_gamma"], f["energies"], f["leaves"], f["phases"], synthetic.split_table(),
             (), None, 1 if corr is not None else None, 0, iol)
+
+
+# the Pol_Num2D fixture's cases: (tag, base fixture)
+POL2D_CASES = (("config1", "config1"), ("num4d_omit", "num4d_omit"),
+               ("config1_corrected", "config1"), ("config1_mu09", "config1"))
+
+
+def pol2d_args(golden, tag, case, stokes, image_order_limit=None):
+    """Arguments of the plain (stokes False) or Stokes integrator for a
+    pol_num2d.npz case: atm_ext 4 with synthetic.pol2d_tables on the base
+    fixture's mesh and rays."""
+    from xpsi_gb300 import synthetic
+    f = golden(case)
+    z = golden("pol_num2d")
+    atm_I, atm_Q = synthetic.pol2d_tables(mu_top=float(z[tag + "_mu_top"]))
+    corr = z.get(tag + "_correction")
+    iol = image_order_limit if image_order_limit is not None else (
+        int(f["image_order_limit"]) or None)
+    common = (1, float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+              f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], f["params"],
+              f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+              f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"], f["phases"])
+    atm = (atm_I, atm_Q) if stokes else (atm_I,)
+    return common + atm + ((), 4, 1 if corr is not None else None, 0, iol)
+
+
+def split_iqu_args(golden, tag, case, image_order_limit=None):
+    """Arguments of integratorIQU_for_azimuthal_invariance_split.integrate for
+    a split_iqu.npz case (synthetic.split_table and split_table_q)."""
+    from xpsi_gb300 import synthetic
+    a = list(split_args(golden, tag, case, image_order_limit))
+    z = golden("split_iqu")
+    a[10] = np.ones_like(a[10]) * z[tag + "_vec"]
+    a[12] = z.get(tag + "_correction")
+    a[25] = 1 if a[12] is not None else None
+    return tuple(a[:23]) + (synthetic.split_table_q(),) + tuple(a[23:])

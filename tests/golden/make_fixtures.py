@@ -514,6 +514,84 @@ def split(xpsi):
     save("split", **out)
 
 
+def pol_num2d(xpsi):
+    """The numerical polarised 2-D atmosphere (atm_ext 4, "Pol_Num2D",
+    hot_Num2D.pyx) of synthetic.pol2d_tables: the plain integrator
+    (integrator_for_azimuthal_invariance.pyx, I only) and the Stokes
+    integrator (integratorIQU_for_azimuthal_invariance.pyx, I and Q tables)
+    on config1's mesh (300 Hz) and num4d_omit's (600 Hz), with a blackbody
+    elsewhere's correction, and on a mu grid topped at 0.9 (queries above
+    the table: the cached walk's clamp history)."""
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate as plain
+    from xpsi.cellmesh.integratorIQU_for_azimuthal_invariance import integrate as iqu
+    out = {}
+    for tag, case, corr_T, mu_top in (("config1", "config1", None, 1.0),
+                                      ("num4d_omit", "num4d_omit", None, 1.0),
+                                      ("config1_corrected", "config1", 6.0, 1.0),
+                                      ("config1_mu09", "config1", None, 0.9)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        atm_I, atm_Q = synthetic.pol2d_tables(mu_top=mu_top)
+        corr = None
+        if corr_T is not None:
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = corr_T
+            corr[..., 1] = f["effGrav"][:, None]
+        common = (float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+                  f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"],
+                  np.array(f["params"], copy=True), f["radiates"], corr, int(f["N_R"]),
+                  f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"], f["cos_gamma"],
+                  f["energies"], f["leaves"], f["phases"])
+        iol = int(f["image_order_limit"]) or None
+        st, flux = plain(1, *common, atm_I, (), 4, 1 if corr is not None else None, 0, iol)
+        assert st == 0
+        res = iqu(1, *common, atm_I, atm_Q, (), 4, 1 if corr is not None else None, 0, iol)
+        assert res[0] == 0
+        out[tag + "_plain"] = flux
+        out[tag + "_I"], out[tag + "_Q"], out[tag + "_U"] = res[1], res[2], res[3]
+        out[tag + "_mu_top"] = np.array(mu_top)
+        if corr is not None:
+            out[tag + "_correction"] = corr
+    save("pol_num2d", **out)
+
+
+def split_iqu(xpsi):
+    """The split Stokes integrator
+    (integratorIQU_for_azimuthal_invariance_split.pyx): I and Q split tables
+    (synthetic.split_table, split_table_q), each reduced to (mu, E) at the
+    first cell's (t_e, t_bb, tau), on config1's and num4d_omit's meshes,
+    with a blackbody elsewhere's correction, and outside the table."""
+    from xpsi.cellmesh.integratorIQU_for_azimuthal_invariance_split import integrate
+    atm_I = synthetic.split_table()
+    atm_Q = synthetic.split_table_q()
+    out = {}
+    for tag, case, vec, corr_T in (("config1", "config1", (0.7, 0.004, 1.5), None),
+                                   ("num4d_omit", "num4d_omit", (0.45, 0.0035, 2.2), None),
+                                   ("config1_corrected", "config1", (0.7, 0.004, 1.5), 5.9),
+                                   ("config1_outside", "config1", (1.35, 0.0063, 0.4), None)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        params = np.ones((S, S, 3)) * np.array(vec)
+        corr = None
+        if corr_T is not None:
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = corr_T
+            corr[..., 1] = f["effGrav"][:, None]
+        res = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                        float(f["inclination"]), f["cellArea"], f["radius"], f["u"],
+                        f["theta"], f["phi"], params, f["radiates"], corr, int(f["N_R"]),
+                        f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"],
+                        f["cos_gamma"], f["energies"], f["leaves"], f["phases"], atm_I, atm_Q,
+                        (), None, 1 if corr is not None else None, 0,
+                        int(f["image_order_limit"]) or None)
+        assert res[0] == 0
+        out[tag + "_I"], out[tag + "_Q"], out[tag + "_U"] = res[1], res[2], res[3]
+        out[tag + "_vec"] = np.array(vec)
+        if corr is not None:
+            out[tag + "_correction"] = corr
+    save("split_iqu", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -526,6 +604,8 @@ def main():
     stokes(xpsi)
     gaussian(xpsi)
     split(xpsi)
+    pol_num2d(xpsi)
+    split_iqu(xpsi)
 
 
 if __name__ == "__main__":

@@ -50,6 +50,40 @@ def split_table(shape=(6, 5, 5, 12, 64), seed=4,
     return tuple(np.ascontiguousarray(x) for x in g) + (np.ascontiguousarray(I.reshape(-1)),)
 
 
+def split_table_q(shape=(6, 5, 5, 12, 64), seed=9, **kw):
+    """Stokes Q of a split atmosphere on split_table's grids: the intensity
+    times -(0.05 + 0.1 (1 - mu)) (polarisation across the surface normal,
+    strongest at the limb), times 1 + 1e-3 seeded noise.  Returns the tuple
+    (5 grids, Q)."""
+    g = split_table(shape=shape, **kw)
+    I = g[5].reshape(shape)
+    mu = g[3][None, None, None, :, None]
+    Q = -(0.05 + 0.1 * (1.0 - mu)) * I
+    Q = Q * (1.0 + 1.0e-3 * np.random.default_rng(seed).standard_normal(Q.shape))
+    return g[:5] + (np.ascontiguousarray(Q.reshape(-1)),)
+
+
+def pol2d_tables(shape=(12, 80), seed=6, kT=0.6, mu_top=1.0, logE_range=(-1.3, 1.3)):
+    """A numerical polarised 2-D atmosphere (HotRegion atm_ext "Pol_Num2D",
+    hot_Num2D.pyx): I and Q on a (mu, log10 E/keV) grid.  I = E^3 /
+    (exp(E/kT) - 1) (0.421 + 0.868 mu), Q = 0.1171 (mu - 1) / (1 + 3.582 mu)
+    (1 + 0.2 log10 E) I (the burst approximation with an energy trend), each
+    times 1 + 1e-3 seeded noise; the mu grid runs over [0, mu_top].  Returns
+    ((mu, logE, I), (mu, logE, Q)) as X-PSI preloads them."""
+    mu = np.linspace(0.0, mu_top, shape[0])
+    lgE = np.linspace(logE_range[0], logE_range[1], shape[1])
+    M, L = np.meshgrid(mu, lgE, indexing="ij")
+    E = 10.0 ** L
+    I = E ** 3 / np.expm1(E / kT) * (0.421 + 0.868 * M)
+    Q = 0.1171 * (M - 1.0) / (1.0 + 3.582 * M) * (1.0 + 0.2 * L) * I
+    rng = np.random.default_rng(seed)
+    I = I * (1.0 + 1.0e-3 * rng.standard_normal(I.shape))
+    Q = Q * (1.0 + 1.0e-3 * rng.standard_normal(Q.shape))
+    mu, lgE = np.ascontiguousarray(mu), np.ascontiguousarray(lgE)
+    return ((mu, lgE, np.ascontiguousarray(I.reshape(-1))),
+            (mu.copy(), lgE.copy(), np.ascontiguousarray(Q.reshape(-1))))
+
+
 def gaussian_response(n_channels, n_inputs, e_lo=0.1, e_hi=10.0, width=0.1):
     """Synthetic response matrix [channels, inputs]: Gaussian redistribution
     (sigma = width * E) times a smooth effective area of 100-1000 cm^2,
