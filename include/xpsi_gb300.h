@@ -28,7 +28,9 @@ extern "C" {
 /* 2: xgpu_integrate takes the elsewhere correction (correction_srcCellParams,
  * n_correction, else_atm_ext); the elsewhere, general, Stokes, synthesis and
  * Gaussian-likelihood entry points were added.
- * 3: xgpu_atmos5d and xgpu_integrate_split (split atmospheres). */
+ * 3: xgpu_atmos5d, xgpu_integrate_split and xgpu_integrate_split_stokes (split
+ * atmospheres); xgpu_integrate_stokes takes the I and Q tables of atm_ext 4
+ * (Pol_Num2D), which xgpu_integrate also takes. */
 #define XGPU_ABI_VERSION 3
 
 /* Status words of the batched layer (per parameter vector). */
@@ -72,7 +74,9 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R,
 /* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-98) for uniform
  * hot regions: beam_opt 0, no disk (R_in >= 1e6).  atm_ext 1 = blackbody,
- * 2 = Num4D (atmos required).  correction_srcCellParams[S0][S1][n_correction]
+ * 2 = Num4D (atmos required), 4 = Pol_Num2D's intensity (hot_Num2D.pyx:
+ * atmos->mu, logE and intensity [nmu][nE] on (mu, log10 E/keV); the other
+ * fields unused).  correction_srcCellParams[S0][S1][n_correction]
  * or NULL is the elsewhere correction (:257-261,469-478,593-594); the GPU
  * path corrects for a blackbody elsewhere (else_atm_ext 1).
  * image_order_limit 0 means "infer" (the reference's None).  flux[N_E][N_P]
@@ -126,9 +130,12 @@ int xgpu_integrate_split(double R, double omega, double r_s, double inclination,
 /* Replaces xpsi.cellmesh.integratorIQU_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integratorIQU_for_azimuthal_invariance.pyx:68-743), the
  * Stokes integrator of HotRegion.integrate_stokes: arguments as
- * xgpu_integrate, atm_ext 1 (blackbody, Q = U = 0) or 3 (burst blackbody,
- * hot_BB_burst.pyx); outputs flux_I, flux_Q, flux_U [N_E][N_P].  Returns 0
- * (SUCCESS) or 1 (ERROR), < 0 on a usage or CUDA failure. */
+ * xgpu_integrate, atm_ext 1 (blackbody, Q = U = 0), 3 (burst blackbody,
+ * hot_BB_burst.pyx) or 4 (Pol_Num2D, hot_Num2D.pyx: atmos_I and atmos_Q
+ * hold the I and Q tables [nmu][nE] on the same (mu, log10 E/keV) grids in
+ * mu, logE and intensity; other fields unused; NULL otherwise); outputs
+ * flux_I, flux_Q, flux_U [N_E][N_P].  Returns 0 (SUCCESS) or 1 (ERROR),
+ * < 0 on a usage or CUDA failure. */
 int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination,
                           size_t S0, size_t S1, const double *cellArea,
                           const double *radialCoords_of_parallels,
@@ -142,8 +149,36 @@ int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination
                           const double *cos_gammaArray, size_t N_E,
                           const double *energies, size_t N_L,
                           const double *leaves, size_t N_P, const double *phases,
-                          int atm_ext, int else_atm_ext, int image_order_limit,
-                          double *flux_I, double *flux_Q, double *flux_U);
+                          int atm_ext, const xgpu_atmos4d *atmos_I,
+                          const xgpu_atmos4d *atmos_Q, int else_atm_ext,
+                          int image_order_limit, double *flux_I, double *flux_Q,
+                          double *flux_U);
+
+/* Replaces xpsi.cellmesh.integratorIQU_for_azimuthal_invariance_split.integrate
+ * (xpsi/cellmesh/integratorIQU_for_azimuthal_invariance_split.pyx:75-758),
+ * the Stokes integrator of a split hot region: the I and Q split tables
+ * (same mu and E grids) are each reduced to (mu, E) at the first cell's
+ * (t_e, t_bb, tau) (:310-322), then I, Q cos 2chi and Q sin 2chi are
+ * integrated as xgpu_integrate_split does I (:515-530).  Returns as
+ * xgpu_integrate_stokes. */
+int xgpu_integrate_split_stokes(double R, double omega, double r_s,
+                                double inclination, size_t S0, size_t S1,
+                                const double *cellArea,
+                                const double *radialCoords_of_parallels,
+                                const double *r_s_over_r, const double *theta,
+                                const double *phi, const double *srcCellParams,
+                                size_t n_params, const int32_t *CELL_RADIATES,
+                                const double *correction_srcCellParams,
+                                size_t n_correction, size_t N_R,
+                                const double *deflection, const double *cos_alpha,
+                                const double *lag, const double *maxDeflection,
+                                const double *cos_gammaArray, size_t N_E,
+                                const double *energies, size_t N_L,
+                                const double *leaves, size_t N_P,
+                                const double *phases, const xgpu_atmos5d *atmos_I,
+                                const xgpu_atmos5d *atmos_Q, int else_atm_ext,
+                                int image_order_limit, double *flux_I,
+                                double *flux_Q, double *flux_U);
 
 /* Replaces xpsi.cellmesh.integrator.integrate (xpsi/cellmesh/integrator.pyx:
  * 48-667), the general integrator of HotRegion(symmetry=False) for source

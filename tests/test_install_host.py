@@ -44,12 +44,14 @@ def test_install_binds_split_integrator():
     xpsi = H.load()
     import xpsi_gb300
     from xpsi_gb300.cellmesh import integrator_for_azimuthal_invariance_split as split
+    from xpsi_gb300.cellmesh import integratorIQU_for_azimuthal_invariance_split as iqu_split
     done = xpsi_gb300.install(xpsi)
     HR = importlib.import_module("xpsi.HotRegion").HotRegion
     hr = object.__new__(HR)
     hr._split = True
     hr.symmetry = True
     assert hr._integrator is split.integrate
+    assert hr._integratorIQU is iqu_split.integrate
     if "xpsi.cellmesh.integrator_for_azimuthal_invariance_split.integrate" in done:
         mod = importlib.import_module("xpsi.cellmesh.integrator_for_azimuthal_invariance_split")
         assert mod.integrate is split.integrate

@@ -8,6 +8,7 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
     xpsi_gb300.cellmesh.integrator.integrate          (HotRegion symmetry=False)
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance_split.integrate
+    xpsi_gb300.cellmesh.integratorIQU_for_azimuthal_invariance_split.integrate
                                                       (HotRegion split=True)
     xpsi_gb300.cellmesh.integratorIQU_for_azimuthal_invariance.integrate (Stokes)
     xpsi_gb300.cellmesh.global_mesh.construct_closed_cellMesh   (elsewhere)
@@ -41,6 +42,7 @@ def install(xpsi_module):
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
     from .cellmesh import integrator as general
     from .cellmesh import integrator_for_azimuthal_invariance_split as split
+    from .cellmesh import integratorIQU_for_azimuthal_invariance_split as iqu_split
     from .cellmesh import integratorIQU_for_azimuthal_invariance as iqu
     from .tools import energy_integrator as ei
     from .tools import phase_integrator as pint, synthesise as syn
@@ -62,6 +64,8 @@ def install(xpsi_module):
         ("xpsi.cellmesh.integrator", "integrate", general.integrate),
         ("xpsi.cellmesh.integrator_for_azimuthal_invariance_split", "integrate",
          split.integrate),
+        ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance_split", "integrate",
+         iqu_split.integrate),
         ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance", "integrate", iqu.integrate),
         ("xpsi.tools.phase_integrator", "phase_integrator", pint.phase_integrator),
         ("xpsi.likelihoods._gaussian_likelihood_given_background_IQU",
@@ -108,6 +112,7 @@ def install(xpsi_module):
         elif declaration:
             # split=True and symmetry=False raise in the original setter
             self._integrator = split.integrate
+            self._integratorIQU = iqu_split.integrate
     HotRegion.symmetry = property(HotRegion.symmetry.fget, _symmetry)
     done.append("xpsi.HotRegion.HotRegion.symmetry")
     return done

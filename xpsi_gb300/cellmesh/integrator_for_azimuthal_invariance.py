@@ -6,6 +6,7 @@ import numpy as np
 
 from .._arr import f64, i32, ptr
 from .._native import Atmos4D, check, lib
+from ._tables import table2d
 
 SUCCESS = 0
 ERROR = 1
@@ -20,10 +21,10 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     """Integrate over the image of a star on a distant observer's sky (GPU).
 
     Returns (0, flux[N_E, N_P]) or (1, None) exactly as the reference does.
-    Supported: blackbody (hot_atm_ext 1) and numerical 4-D (2) hot
-    atmospheres with beam_opt 0 and no disk (R_in >= 1e6), with or without
-    the correction for a blackbody elsewhere (else_atm_ext 1) -- the
-    hot-region likelihood path.  Other options raise NotImplementedError
+    Supported: blackbody (hot_atm_ext 1), numerical 4-D (2) and Pol_Num2D's
+    intensity table (4, hot_atmosphere = (mu, log10 E, I)) hot atmospheres
+    with beam_opt 0 and no disk (R_in >= 1e6), with or without the
+    correction for a blackbody elsewhere (else_atm_ext 1).  Other options raise NotImplementedError
     rather than silently computing something else.
     """
     corr = None
@@ -38,7 +39,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     if R_in < 1e6:
         raise NotImplementedError("disk occultation is not on the GPU path")
     atm = int(hot_atm_ext)
-    if atm not in (1, 2):
+    if atm not in (1, 2, 4):
         raise NotImplementedError("hot atmosphere extension %d is not on the GPU path" % atm)
     A = f64(cellArea)
     S0, S1 = A.shape
@@ -55,6 +56,8 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         raise ValueError("ray tables must be [rows, numRays]")
     atmos = None
     keep = ()
+    if atm == 4:
+        atmos, keep = table2d(hot_atmosphere)
     if atm == 2:
         if not hot_atmosphere:
             raise ValueError("numerical atmosphere data were not preloaded")

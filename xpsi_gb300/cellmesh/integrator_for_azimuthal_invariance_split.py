@@ -7,7 +7,8 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
-from .._native import Atmos5D, check, lib
+from .._native import check, lib
+from ._tables import table5d
 
 SUCCESS = 0
 ERROR = 1
@@ -41,8 +42,6 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         raise NotImplementedError("beaming options 1-3 are not on the GPU path")
     if R_in < 1e6:
         raise NotImplementedError("disk occultation is not on the GPU path")
-    if not hot_atmosphere or len(hot_atmosphere) < 6:
-        raise ValueError("split atmosphere data (5 grids and the intensity) were not preloaded")
     A = f64(cellArea)
     S0, S1 = A.shape
     par = f64(srcCellParams)
@@ -58,14 +57,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     N_R = int(numRays)
     if arrs[4].shape != (S0, N_R):
         raise ValueError("ray tables must be [rows, numRays]")
-    grids = tuple(f64(g) for g in hot_atmosphere[:5])
-    table = f64(hot_atmosphere[5])
-    n = [g.size for g in grids]
-    if table.size != int(np.prod(n)):
-        raise ValueError("split intensity table has %d values, grids give %d"
-                         % (table.size, int(np.prod(n))))
-    atmos = Atmos5D((C.c_void_p * 5)(*(g.ctypes.data for g in grids)), (C.c_size_t * 5)(*n),
-                    table.ctypes.data)
+    atmos, keep = table5d(hot_atmosphere)
     flux = np.empty((E.size, P.size))
     st = check(lib().xgpu_integrate_split(
         float(R), float(omega), float(r_s), float(inclination), S0, S1, ptr(A),
@@ -75,7 +67,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         ptr(Lv), P.size, ptr(P), C.byref(atmos),
         int(else_atm_ext) if corr is not None else 0,
         int(image_order_limit) if image_order_limit is not None else 0, ptr(flux)))
-    del grids, table
+    del keep
     if st != 0:
         return (ERROR, None)
     return (SUCCESS, flux)

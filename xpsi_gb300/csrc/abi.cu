@@ -181,8 +181,7 @@ int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u, const double *r_s,
 namespace {
 int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
-                         int target_ctas, void *stream, int mixed,
-                         const double *split_slab = nullptr);
+                         int target_ctas, void *stream, int mixed, int table2d = 0);
 }
 
 int xgpu_integrate_batch(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
@@ -204,7 +203,7 @@ int xgpu_integrate_batch_mixed(int n_meshes, const xgpu_mesh *meshes, int64_t n_
 namespace {
 int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
-                         int target_ctas, void *stream, int mixed, const double *split_slab) {
+                         int target_ctas, void *stream, int mixed, int table2d) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (n_meshes <= 0) return 0;
   if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
@@ -212,9 +211,13 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   for (int m = 0; m < n_meshes; m++) {
     if (meshes[m].atm_ext == 2 && d->atmos.intensity == nullptr)
       return fail_msg("a Num4D mesh needs the atmosphere table");
-    if (meshes[m].atm_ext == 6 && (split_slab == nullptr || mixed))
-      return fail_msg("atm_ext 6 (split) is reached through xgpu_integrate_split only");
-    if (meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2 && meshes[m].atm_ext != 6)
+    const int ext = meshes[m].atm_ext;
+    if ((ext == 4 || ext == 6) && (!table2d || mixed))
+      return fail_msg("2-D table atmospheres (atm_ext 4, 6) are reached through the drop-in "
+                      "integrators only");
+    if (table2d && ext != 4 && ext != 6)
+      return fail_msg("a 2-D table call takes atm_ext 4 or 6 only");
+    if (ext != 1 && ext != 2 && ext != 4 && ext != 6)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
   }
   if (d->correction != nullptr && mixed)
@@ -251,7 +254,7 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   CK(cudaMemsetAsync(dpart.p, 0, part_n * sizeof(double), st));
   if ((rc = dalloc(dstate, (size_t)3 * n_rows + 16, st))) return rc;
   Dev dslab;
-  if (d->atmos.intensity != nullptr && split_slab == nullptr &&
+  if (d->atmos.intensity != nullptr && !table2d &&
       (rc = dalloc(dslab, (size_t)n_chunks * d->atmos.nmu * d->atmos.nE * sizeof(double), st)))
     return rc;
   CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
@@ -284,8 +287,7 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.member_status = d->mesh_status;
   a.flux = d->flux;
   a.flop_counter = d->flop_counter;
-  a.slab = d->atmos.intensity != nullptr && split_slab == nullptr ? dslab.as<double>() : nullptr;
-  a.split_slab = split_slab;
+  a.slab = d->atmos.intensity != nullptr && !table2d ? dslab.as<double>() : nullptr;
   a.mixed = mixed;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
@@ -390,6 +392,83 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R, double *
 }  // extern "C"
 
 namespace {
+// a 2-D table atmosphere on the device: grids (mu, E coordinate) and the
+// I table [nmu][nE] of `I`, and the Q table of `Q` (on the same grids) when Q
+// is given; one allocation held by `buf`
+int table2d_device(cudaStream_t st, const xgpu_atmos4d *I, const xgpu_atmos4d *Q, Dev &buf,
+                   xg::Atmos4D *out, const double **q_out) {
+  if (!I->mu || !I->logE || !I->intensity) return fail_msg("the 2-D table is incomplete");
+  if (I->nmu < 4 || I->nE < 4) return fail_msg("2-D table grids need at least 4 nodes");
+  if (Q) {
+    if (!Q->intensity) return fail_msg("the Q table is missing");
+    if (Q->nmu != I->nmu || Q->nE != I->nE) return fail_msg("I and Q tables on different grids");
+    for (size_t k = 0; k < I->nmu; k++)
+      if (Q->mu[k] != I->mu[k]) return fail_msg("I and Q tables on different grids");
+    for (size_t k = 0; k < I->nE; k++)
+      if (Q->logE[k] != I->logE[k]) return fail_msg("I and Q tables on different grids");
+  }
+  const size_t nt = I->nmu * I->nE;
+  int rc;
+  if ((rc = dalloc(buf, (I->nmu + I->nE + (Q ? 2 : 1) * nt) * 8, st))) return rc;
+  double *b = buf.as<double>();
+  CK(cudaMemcpyAsync(b, I->mu, I->nmu * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(b + I->nmu, I->logE, I->nE * 8, cudaMemcpyHostToDevice, st));
+  double *tI = b + I->nmu + I->nE;
+  CK(cudaMemcpyAsync(tI, I->intensity, nt * 8, cudaMemcpyHostToDevice, st));
+  if (Q) CK(cudaMemcpyAsync(tI + nt, Q->intensity, nt * 8, cudaMemcpyHostToDevice, st));
+  *out = xg::Atmos4D{};
+  out->mu = b;
+  out->logE = b + I->nmu;
+  out->I = tI;
+  out->nmu = (int)I->nmu;
+  out->nE = (int)I->nE;
+  if (q_out) *q_out = Q ? tI + nt : nullptr;
+  return 0;
+}
+
+// a split atmosphere uploaded and reduced on the device to its (mu, E)
+// table at vec (the first cell's t_e, t_bb, tau): grids in `dg`, the 5-D
+// table in `dI`, the 2-D table in `dslab`
+int split_device(cudaStream_t st, const xgpu_atmos5d *atmos, const double *vec, Dev &dg,
+                 Dev &dI, Dev &dslab, xg::Atmos4D *out) {
+  if (!atmos || !atmos->intensity) return fail_msg("the split integrator needs the 5-D atmosphere");
+  size_t nI = 1, ng = 0;
+  for (int d = 0; d < 5; d++) {
+    if (atmos->n[d] < 4) return fail_msg("split grids need at least 4 nodes per dimension");
+    nI *= atmos->n[d];
+    ng += atmos->n[d];
+  }
+  const size_t nmu = atmos->n[3], nE = atmos->n[4];
+  int rc;
+  if ((rc = dalloc(dg, ng * 8, st)) || (rc = upload(dI, atmos->intensity, nI, st)) ||
+      (rc = dalloc(dslab, nmu * nE * 8, st)))
+    return rc;
+  xg::SplitArgs sa{};
+  double *gp = dg.as<double>();
+  for (int d = 0; d < 5; d++) {
+    CK(cudaMemcpyAsync(gp, atmos->grid[d], atmos->n[d] * 8, cudaMemcpyHostToDevice, st));
+    sa.grid[d] = gp;
+    sa.n[d] = (int)atmos->n[d];
+    gp += atmos->n[d];
+  }
+  sa.I = dI.as<double>();
+  // produce_2D_data at the first cell's parameter vector
+  // (integrator_for_azimuthal_invariance_split.pyx:270)
+  for (int d = 0; d < 3; d++) sa.vec[d] = vec[d];
+  sa.out = dslab.as<double>();
+  xg::launch_split_reduce(sa, st);
+  CK(cudaGetLastError());
+  *out = xg::Atmos4D{};
+  out->mu = sa.grid[3];
+  out->logE = sa.grid[4];
+  out->I = dslab.as<double>();
+  out->nmu = (int)nmu;
+  out->nE = (int)nE;
+  return 0;
+}
+}  // namespace
+
+namespace {
 // the drop-in integrators' common host path: upload, one batched launch on
 // the library stream, copy back
 int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
@@ -401,8 +480,7 @@ int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
                    const double *maxDeflection, const double *cos_gamma, size_t N_E,
                    const double *energies, size_t N_L, const double *leaves, size_t N_P,
                    const double *phases, int atm_ext, const xg::Atmos4D &A,
-                   const double *split_slab, int else_atm_ext, int image_order_limit,
-                   double *flux) {
+                   int else_atm_ext, int image_order_limit, double *flux) {
   int rc;
   if (n_params < 2) return fail_msg("srcCellParams needs at least 2 parameters per cell");
   if (correction && else_atm_ext != 1)
@@ -436,7 +514,7 @@ int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
   d.cellArea = dA.as<double>(); d.phi = dphi.as<double>(); d.params = dpar.as<double>();
   d.n_params = (int32_t)n_params; d.radiates = dR.as<int32_t>();
   d.energies = dE.as<double>(); d.leaves = dLv.as<double>(); d.phases = dP.as<double>();
-  if (atm_ext == 2 || atm_ext == 6) {
+  if (atm_ext == 2 || atm_ext == 4 || atm_ext == 6) {
     d.atmos = xgpu_atmos4d{A.logT, A.logg, A.mu, A.logE, A.I, (size_t)A.nT, (size_t)A.ng,
                            (size_t)A.nmu, (size_t)A.nE, nullptr};
   }
@@ -445,7 +523,7 @@ int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
   d.correction = correction ? dcorr.as<double>() : nullptr;
   d.n_correction = (int32_t)n_correction;
   rc = integrate_batch_impl(1, &mesh, (int64_t)S0, (int)N_R, (int)N_E, (int)N_L, (int)N_P, &d,
-                            0, st, 0, split_slab);
+                            0, st, 0, (atm_ext == 4 || atm_ext == 6) ? 1 : 0);
   if (rc) return rc;
   int32_t status = 0;
   CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
@@ -471,15 +549,19 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   cudaStream_t st;
   int rc;
   if ((rc = lib_stream(&st))) return rc;
-  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
-  if (atm_ext != 1 && atm_ext != 2) return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+  if ((atm_ext == 2 || atm_ext == 4) && !atmos)
+    return fail_msg("numerical atmospheres (atm_ext 2, 4) need the table");
+  if (atm_ext != 1 && atm_ext != 2 && atm_ext != 4)
+    return fail_msg("atm_ext must be 1 (BB), 2 (Num4D) or 4 (Pol_Num2D)");
   xg::Atmos4D A{};
+  Dev dt;
   if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  if (atm_ext == 4 && (rc = table2d_device(st, atmos, nullptr, dt, &A, nullptr))) return rc;
   return integrate_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta,
                         phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
                         deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
-                        N_L, leaves, N_P, phases, atm_ext, A, nullptr, else_atm_ext,
-                        image_order_limit, flux);
+                        N_L, leaves, N_P, phases, atm_ext, A, else_atm_ext, image_order_limit,
+                        flux);
 }
 
 int xgpu_integrate_split(double R, double omega, double r_s, double inclination, size_t S0,
@@ -498,49 +580,23 @@ int xgpu_integrate_split(double R, double omega, double r_s, double inclination,
   cudaStream_t st;
   int rc;
   if ((rc = lib_stream(&st))) return rc;
-  if (!atmos || !atmos->intensity) return fail_msg("the split integrator needs the 5-D atmosphere");
   if (n_params < 3) return fail_msg("the split atmosphere needs 3 parameters per cell");
   if (S0 * S1 == 0) return fail_msg("empty cell mesh");
-  size_t nI = 1, ng = 0;
-  for (int d = 0; d < 5; d++) {
-    if (atmos->n[d] < 4) return fail_msg("split grids need at least 4 nodes per dimension");
-    nI *= atmos->n[d];
-    ng += atmos->n[d];
-  }
-  const size_t nmu = atmos->n[3], nE = atmos->n[4];
   Dev dg, dI, dslab;
-  if ((rc = dalloc(dg, ng * 8, st)) || (rc = upload(dI, atmos->intensity, nI, st)) ||
-      (rc = dalloc(dslab, nmu * nE * 8, st)))
-    return rc;
-  xg::SplitArgs sa{};
-  double *gp = dg.as<double>();
-  for (int d = 0; d < 5; d++) {
-    CK(cudaMemcpyAsync(gp, atmos->grid[d], atmos->n[d] * 8, cudaMemcpyHostToDevice, st));
-    sa.grid[d] = gp;
-    sa.n[d] = (int)atmos->n[d];
-    gp += atmos->n[d];
-  }
-  sa.I = dI.as<double>();
-  // produce_2D_data at the first cell's parameter vector
-  // (integrator_for_azimuthal_invariance_split.pyx:270)
-  for (int d = 0; d < 3; d++) sa.vec[d] = srcCellParams[d];
-  sa.out = dslab.as<double>();
-  xg::launch_split_reduce(sa, st);
-  CK(cudaGetLastError());
   xg::Atmos4D A{};
-  A.mu = sa.grid[3];
-  A.logE = sa.grid[4];
-  A.I = dslab.as<double>();
-  A.nmu = (int)nmu;
-  A.nE = (int)nE;
+  if ((rc = split_device(st, atmos, srcCellParams, dg, dI, dslab, &A))) return rc;
   return integrate_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta,
                         phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
                         deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
-                        N_L, leaves, N_P, phases, 6, A, dslab.as<double>(), else_atm_ext,
-                        image_order_limit, flux);
+                        N_L, leaves, N_P, phases, 6, A, else_atm_ext, image_order_limit, flux);
 }
 
-int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination, size_t S0,
+}  // extern "C"
+
+namespace {
+// the Stokes drop-ins' common host path: upload, the Stokes kernel on the
+// library stream, copy back
+int stokes_host(cudaStream_t st, double omega, double inclination, size_t S0,
                           size_t S1, const double *cellArea, const double *radius,
                           const double *r_s_over_r, const double *theta, const double *phi,
                           const double *srcCellParams, size_t n_params, const int32_t *radiates,
@@ -548,32 +604,27 @@ int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination
                           const double *deflection, const double *cos_alpha, const double *lag,
                           const double *maxDeflection, const double *cos_gamma, size_t N_E,
                           const double *energies, size_t N_L, const double *leaves, size_t N_P,
-                          const double *phases, int atm_ext, int else_atm_ext,
-                          int image_order_limit, double *flux_I, double *flux_Q,
-                          double *flux_U) {
-  (void)R;
-  (void)r_s;
-  cudaStream_t st;
+                          const double *phases, int atm_ext, const xg::Atmos4D &A,
+                          const double *dQ, int else_atm_ext, int image_order_limit,
+                          double *flux_I, double *flux_Q, double *flux_U) {
   int rc;
-  if ((rc = lib_stream(&st))) return rc;
   if (S0 == 0 || S1 == 0 || N_E == 0 || N_P == 0) return 0;
   if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
   if (N_R < 3) return fail_msg("num_rays must be at least 3");
-  if (atm_ext != 1 && atm_ext != 3)
-    return fail_msg("the Stokes integrator takes atm_ext 1 (BB) or 3 (burst BB)");
   if (n_params < 1) return fail_msg("srcCellParams needs at least 1 parameter per cell");
   if (correction && else_atm_ext != 1)
     return fail_msg("the GPU integrator corrects for a blackbody elsewhere only");
   if (correction && n_correction < 1)
     return fail_msg("correction vectors need at least 1 parameter per cell");
-  if (xg::stokes_smem_bytes((int)N_L, (int)N_P, (int)N_E, (int)N_R) > 227 * 1024)
+  if (xg::stokes_smem_bytes((int)N_L, (int)N_P, (int)N_E, (int)N_R, A.I ? A.nmu : 0,
+                            A.I ? A.nE : 0) > 227 * 1024)
     return fail_msg("num_leaves and num_rays too large for one CTA's shared memory");
   const size_t cells = S0 * S1;
   std::vector<double> theta0(S0);
   for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
   std::vector<int32_t> row_mesh(S0, 0);
   Dev dA, drad, du, dth0, dphi, dpar, dR, dD, dCA, dL, dMD, dcg, dE, dLv, dP, dF, dst, drm;
-  Dev dcorr, dmem, dpart;
+  Dev dcorr, dmem, dpart, dstate;
   if ((rc = upload(dA, cellArea, cells, st)) || (rc = upload(drad, radius, S0, st)) ||
       (rc = upload(du, r_s_over_r, S0, st)) || (rc = upload(dth0, theta0.data(), S0, st)) ||
       (rc = upload(dphi, phi, cells, st)) || (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
@@ -604,6 +655,13 @@ int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination
   a.N_E = (int)N_E; a.N_L = (int)N_L; a.N_P = (int)N_P;
   a.energies = dE.as<double>(); a.leaves = dLv.as<double>(); a.phases = dP.as<double>();
   a.member_status = dst.as<int32_t>();
+  if (A.I) {
+    a.atmos = A;
+    a.table_q = dQ;
+    if ((rc = dalloc(dstate, 3 * S0 + 16, st))) return rc;
+    uint8_t *sb = dstate.as<uint8_t>();
+    a.row_has_eval = sb; a.row_last_top = sb + S0; a.row_entry_top = sb + 2 * S0;
+  }
   a.flux = dF.as<double>();
   a.flux_q = a.flux + N_E * N_P;
   a.flux_u = a.flux_q + N_E * N_P;
@@ -622,6 +680,83 @@ int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination
   CK(cudaMemcpyAsync(flux_U, a.flux_u, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return status != 0 ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xgpu_integrate_stokes(double R, double omega, double r_s, double inclination, size_t S0,
+                          size_t S1, const double *cellArea, const double *radius,
+                          const double *r_s_over_r, const double *theta, const double *phi,
+                          const double *srcCellParams, size_t n_params, const int32_t *radiates,
+                          const double *correction, size_t n_correction, size_t N_R,
+                          const double *deflection, const double *cos_alpha, const double *lag,
+                          const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                          const double *energies, size_t N_L, const double *leaves, size_t N_P,
+                          const double *phases, int atm_ext, const xgpu_atmos4d *atmos_I,
+                          const xgpu_atmos4d *atmos_Q, int else_atm_ext, int image_order_limit,
+                          double *flux_I, double *flux_Q, double *flux_U) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (atm_ext != 1 && atm_ext != 3 && atm_ext != 4)
+    return fail_msg("the Stokes integrator takes atm_ext 1 (BB), 3 (burst BB) or 4 (Pol_Num2D)");
+  xg::Atmos4D A{};
+  const double *dQ = nullptr;
+  Dev dt;
+  if (atm_ext == 4) {
+    if (!atmos_I || !atmos_Q) return fail_msg("atm_ext 4 (Pol_Num2D) needs the I and Q tables");
+    if ((rc = table2d_device(st, atmos_I, atmos_Q, dt, &A, &dQ))) return rc;
+  }
+  return stokes_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta, phi,
+                     srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                     deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies, N_L,
+                     leaves, N_P, phases, atm_ext, A, dQ, else_atm_ext, image_order_limit,
+                     flux_I, flux_Q, flux_U);
+}
+
+int xgpu_integrate_split_stokes(double R, double omega, double r_s, double inclination,
+                                size_t S0, size_t S1, const double *cellArea,
+                                const double *radius, const double *r_s_over_r,
+                                const double *theta, const double *phi,
+                                const double *srcCellParams, size_t n_params,
+                                const int32_t *radiates, const double *correction,
+                                size_t n_correction, size_t N_R, const double *deflection,
+                                const double *cos_alpha, const double *lag,
+                                const double *maxDeflection, const double *cos_gamma,
+                                size_t N_E, const double *energies, size_t N_L,
+                                const double *leaves, size_t N_P, const double *phases,
+                                const xgpu_atmos5d *atmos_I, const xgpu_atmos5d *atmos_Q,
+                                int else_atm_ext, int image_order_limit, double *flux_I,
+                                double *flux_Q, double *flux_U) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (n_params < 3) return fail_msg("the split atmosphere needs 3 parameters per cell");
+  if (S0 * S1 == 0) return fail_msg("empty cell mesh");
+  if (!atmos_I || !atmos_Q) return fail_msg("the split Stokes integrator needs I and Q tables");
+  for (int d = 3; d < 5; d++) {
+    if (atmos_I->n[d] != atmos_Q->n[d]) return fail_msg("I and Q tables on different grids");
+    for (size_t k = 0; k < atmos_I->n[d]; k++)
+      if (atmos_I->grid[d][k] != atmos_Q->grid[d][k])
+        return fail_msg("I and Q tables on different grids");
+  }
+  // each table reduced by its own evaluator (:310-322)
+  Dev gI, tI, sI, gQ, tQ, sQ;
+  xg::Atmos4D A{}, AQ{};
+  if ((rc = split_device(st, atmos_I, srcCellParams, gI, tI, sI, &A)) ||
+      (rc = split_device(st, atmos_Q, srcCellParams, gQ, tQ, sQ, &AQ)))
+    return rc;
+  return stokes_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta, phi,
+                     srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                     deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies, N_L,
+                     leaves, N_P, phases, 6, A, AQ.I, else_atm_ext, image_order_limit, flux_I,
+                     flux_Q, flux_U);
 }
 
 int xgpu_integrate_general(double R, double omega, double r_s, double inclination, size_t S0,

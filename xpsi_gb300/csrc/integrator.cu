@@ -344,6 +344,21 @@ __device__ __forceinline__ void lagrange_w(const double *P, const double *S, int
   w[3] = d3 * S[4 * b + 3];
 }
 
+// the table grids of a numerical atmosphere in shared memory: mu and E
+// nodes, the inverse Lagrange denominators of every stencil base, and the
+// FP32 copies the guided stencil searches use; ends with a block barrier
+__device__ __forceinline__ void stage_table_grids(const Atmos4D &A, AtmSmem &as, int nmu,
+                                                  int nEt) {
+  for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.gmu[t] = A.mu[t];
+  for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.gE[t] = A.logE[t];
+  __syncthreads();
+  for (int b = threadIdx.x; b <= nmu - 4; b += blockDim.x) lagrange_space(as.gmu, b, as.smu + 4 * b);
+  for (int b = threadIdx.x; b <= nEt - 4; b += blockDim.x) lagrange_space(as.gE, b, as.sE + 4 * b);
+  for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
+  for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
+  __syncthreads();
+}
+
 // stencil_base with the bisection run on the grid's FP32 copy (FP32 pipe)
 // and finished with FP64 comparisons.  Rounding to float is monotone, so the
 // float search never stops below the FP64 answer, and stepping down while
@@ -385,6 +400,24 @@ __device__ __forceinline__ MuStencil mu_stencil(const Atmos4D &A, const AtmSmem 
   m.b2 = stencil_base_guided(as.gmu, as.fgmu, A.nmu, v2);
   lagrange_w(as.gmu, as.smu, m.b2, v2, m.w2);
   return m;
+}
+// the stencil sum itself (a Stokes Q table: no positive part, no factor)
+__device__ __forceinline__ double eval_table_raw(const Atmos4D &A, const AtmSmem &as,
+                                                 const double *slab, const MuStencil &m,
+                                                 double v3) {
+  if (v3 < as.gE[0]) v3 = as.gE[0];
+  if (v3 > as.gE[A.nE - 1]) v3 = as.gE[A.nE - 1];
+  const int b3 = stencil_base_guided(as.gE, as.fgE, A.nE, v3);
+  double w3[4];
+  lagrange_w(as.gE, as.sE, b3, v3, w3);
+  double I = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double *r = slab + (size_t)(m.b2 + k) * A.nE + b3;
+    const double t = w3[0] * r[0] + w3[1] * r[1] + w3[2] * r[2] + w3[3] * r[3];
+    I += m.w2[k] * t;
+  }
+  return I;
 }
 __device__ __forceinline__ double eval_num4d_e(const Atmos4D &A, const AtmSmem &as,
                                                const double *slab, const MuStencil &m,
@@ -644,7 +677,7 @@ __global__ void num4d_scan_kernel(IntegrateArgs a) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= a.n_members) return;
   const MemberDesc M = a.members[m];
-  if (M.atm != 2 && M.atm != 6) return;
+  if (M.atm != 2 && M.atm != 4 && M.atm != 6) return;
   uint8_t carry = 0;
   for (int i = 0; i < M.S0; i++) {
     int64_t row = M.row_off + i;
@@ -810,11 +843,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   const MemberDesc M = a.members[m];
   const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  // split (atm 6): the (mu, E) table of a split atmosphere, reduced once per
-  // call, with the energy in electron rest energies and no 10^(3 log T)
+  // 2-D tables (atmos.I is [nmu][nE], no 10^(3 log T)): atm 4, Pol_Num2D's
+  // I on (mu, log10 E') (hot_Num2D.pyx:187-400); atm 6, a split atmosphere
+  // reduced once per call to (mu, E) with E' in electron rest energies
   // (integrator_for_azimuthal_invariance_split.pyx:270-275,457-476)
-  const bool split = (M.atm == 6) && !kMixed;
-  const bool num4d = (M.atm == 2) || split;
+  const bool tab2 = (M.atm == 4 || M.atm == 6) && !kMixed;
+  const bool erest = (M.atm == 6);
+  const bool num4d = (M.atm == 2) || tab2;
   const int nmu = a.atmos.I ? a.atmos.nmu : 0, nEt = a.atmos.I ? a.atmos.nE : 0;
   const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt, (int)sizeof(PieceT<WT>), a.N_R);
   const int EC = L.EC;
@@ -826,16 +861,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   double *slab = nullptr;
   float *slabf = nullptr;
   if (num4d) {
-    for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.gmu[t] = a.atmos.mu[t];
-    for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.gE[t] = a.atmos.logE[t];
-    __syncthreads();
-    for (int b = threadIdx.x; b <= nmu - 4; b += blockDim.x) lagrange_space(as.gmu, b, as.smu + 4 * b);
-    for (int b = threadIdx.x; b <= nEt - 4; b += blockDim.x) lagrange_space(as.gE, b, as.sE + 4 * b);
-    __syncthreads();
-    // FP32 grid copies: the guided stencil searches (both forms) and the
-    // mixed form's interpolation
-    for (int t = threadIdx.x; t < nmu; t += blockDim.x) as.fgmu[t] = (float)as.gmu[t];
-    for (int t = threadIdx.x; t < nEt; t += blockDim.x) as.fgE[t] = (float)as.gE[t];
+    stage_table_grids(a.atmos, as, nmu, nEt);
+    // the mixed form's FP32 interpolation data
     if (kMixed) {
       for (int t = threadIdx.x; t < min(N_E, kMaxEnergiesF); t += blockDim.x)
         as.fE[t] = (float)a.energies[t];
@@ -846,7 +873,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         as.fgEo[t] = b + i < nEt ? (float)(as.gE[b + i] - as.gE[b]) : 0.0f;
       }
     }
-    slab = split ? const_cast<double *>(a.split_slab) : a.slab + (size_t)chunk * nmu * nEt;
+    slab = tab2 ? const_cast<double *>(a.atmos.I) : a.slab + (size_t)chunk * nmu * nEt;
     slabf = reinterpret_cast<float *>(slab);
     __syncthreads();
   }
@@ -878,7 +905,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     }
     __syncthreads();
     double E_eff = 0.0, p3 = 0.0;
-    if (split) {
+    if (tab2) {
       p3 = 1.0;
     } else if (num4d) {
       // contract the (log T, log g) stencil of this parallel once:
@@ -940,7 +967,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     const float p3f = (float)p3;
     const double fix = num4d ? (norm * p3) / ((double)(float)norm * (double)p3f)
                              : norm / (double)(float)norm;
-    const double lg_Eeff = (num4d && !split) ? log10(E_eff) : 0.0;
+    const double lg_Eeff = (num4d && !tab2) ? log10(E_eff) : 0.0;
     // the elsewhere correction's blackbody temperature at the parallel's
     // first radiating cell (:469-476)
     const bool corr = !kMixed && a.correction != nullptr;
@@ -1000,7 +1027,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             as.fabb[sidx] = (float)g.ABB[sidx];
             as.fgeom[sidx] = (float)g.GEOM[sidx];
           }
-          if (split) g.lzs[sidx] = g.Z[sidx];
+          if (erest) g.lzs[sidx] = g.Z[sidx];
           else if (num4d) g.lzs[sidx] = log10(g.Z[sidx]) + lg_Eeff;
         }
       }
@@ -1016,7 +1043,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         const int ne = min(EC, N_E - e0);
         if (num4d) {
           for (int t = threadIdx.x; t < ne; t += blockDim.x)
-            g.lgE[t] = split ? a.energies[e0 + t] : log10(a.energies[e0 + t]);
+            g.lgE[t] = erest ? a.energies[e0 + t] : log10(a.energies[e0 + t]);
           __syncthreads();
         }
         // specific intensities of every profile column (:445-478).  With
@@ -1035,8 +1062,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               if constexpr (kMixed) {
                 float I_E;
                 if (num4d) {
-                  // split: E' = E / Z in electron rest energies (:457-458)
-                  const double v3 = split ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
+                  // atm 6: E' = E / Z in electron rest energies (:457-458)
+                  const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
                                           : g.lgE[pl] - g.lzs[s];
                   if (p == 0 && g.clamp0[s]) {
                     I_E = eval_num4d_f(a.atmos, as, slabf,
@@ -1056,8 +1083,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               } else {
                 double I_E;
                 if (num4d) {
-                  // split: E' = E / Z in electron rest energies (:457-458)
-                  const double v3 = split ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
+                  // atm 6: E' = E / Z in electron rest energies (:457-458)
+                  const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
                                           : g.lgE[pl] - g.lzs[s];
                   if (p == 0 && g.clamp0[s]) {
                     I_E = eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, g.ABB[s], true),
@@ -1251,8 +1278,8 @@ __device__ __forceinline__ bool cell_phase_sums_stokes(const CP &cp, const AR &a
   return true;
 }
 
-size_t stokes_smem(int N_L, int N_P, int N_E, int N_R) {
-  const Layout L = make_layout(N_L, N_P, N_E, 0, 0, kStokesPiece, N_R);
+size_t stokes_smem(int N_L, int N_P, int N_E, int N_R, int nmu, int nE) {
+  const Layout L = make_layout(N_L, N_P, N_E, nmu, nE, kStokesPiece, N_R);
   return L.bytes + (size_t)2 * N_L * sizeof(double) + (size_t)2 * L.EC * sizeof(int) + 64;
 }
 
@@ -1264,11 +1291,18 @@ __global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
   const int i = (int)(row - M.row_off);
   const int N_L = a.N_L, N_E = a.N_E, N_P = a.N_P;
   const int leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  const Layout L = make_layout(N_L, N_P, N_E, 0, 0, kStokesPiece, a.N_R);
+  // 2-D table atmospheres: atm 4 (Pol_Num2D, I and Q on (mu, log10 E'),
+  // hot_Num2D.pyx:187-400) and atm 6 (split I and Q reduced to (mu, E), E'
+  // in electron rest energies,
+  // integratorIQU_for_azimuthal_invariance_split.pyx:310-322,515-530)
+  const bool tab2 = (M.atm == 4 || M.atm == 6);
+  const bool erest = (M.atm == 6);
+  const int nmu = a.atmos.I ? a.atmos.nmu : 0, nEt = a.atmos.I ? a.atmos.nE : 0;
+  const Layout L = make_layout(N_L, N_P, N_E, nmu, nEt, kStokesPiece, a.N_R);
   const int EC = L.EC;
   double *coef;
   AtmSmem as{};
-  GeoSmem g = carve(smem, N_L, EC, &coef, 0, 0, &as, kStokesPiece, a.N_R);
+  GeoSmem g = carve(smem, N_L, EC, &coef, nmu, nEt, &as, kStokesPiece, a.N_R);
   double *xd = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(g.sc_exp + EC) + 15) & ~uintptr_t(15));
   g.c2chi = xd;
@@ -1276,13 +1310,22 @@ __global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
   int *scQ = reinterpret_cast<int *>(xd + 2 * N_L), *scU = scQ + EC;
   Piece *coI = reinterpret_cast<Piece *>(coef);
   Piece *coQ = coI + (size_t)EC * N_L, *coU = coQ + (size_t)EC * N_L;
-  __shared__ int s_J, s_jalt;
+  __shared__ int s_J, s_jalt, s_top, s_any;
   double *part = a.partial + (size_t)row * 3 * N_E * N_P;
   RowCtx c;
   if (!load_row(a, M, row, i, c, &s_J)) return;
   stage_deflection(c, g, &s_jalt);
+  if (tab2) stage_table_grids(a.atmos, as, nmu, nEt);
+  if (threadIdx.x == 0) {
+    s_top = tab2 ? (int)a.row_entry_top[row] : 0;
+    s_any = 0;
+  }
+  __syncthreads();
+  const double mu_max = tab2 ? a.atmos.mu[nmu - 1] : 0.0;
+  const double mu_top3 = tab2 ? a.atmos.mu[nmu - 3] : 0.0;
   const bool burst = (M.atm == 3);
-  const double norm = kErg * kPlanck;
+  // hot_BB_burst.pyx, hot_Num2D.pyx:359-367, hot_Num5D_split.pyx:538-563
+  const double norm = tab2 ? kErg / kHKeV : kErg * kPlanck;
   const double kT = (kKB / kKeV) * pow(10.0, c.vec0);
   const bool corr = a.correction != nullptr;
   const double kT_c =
@@ -1298,8 +1341,10 @@ __global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
       leaf_geometry(c, I, k, N_L, leaf_lim, a.leaves, g);
     __syncthreads();
     if (threadIdx.x == 0) {
-      int top = 0, any = 0;
-      state_machine(N_L, leaf_lim, a.leaves, g, false, 0.0, 0.0, top, any);
+      int top = s_top, any = s_any;
+      state_machine(N_L, leaf_lim, a.leaves, g, tab2, mu_top3, mu_max, top, any);
+      s_top = top;
+      s_any = any;
     }
     __syncthreads();
     if (g.flags[0]) {
@@ -1327,10 +1372,23 @@ __global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
       g.ih[t] = df_split(1.0 / h);
       g.ih2[t] = df_split(1.0 / (h * h));
     }
+    if (tab2) {
+      for (int t = threadIdx.x; t < N_L; t += blockDim.x) {
+        const int sidx = g.src[t];
+        if (sidx >= 0) g.lzs[sidx] = erest ? g.Z[sidx] : log10(g.Z[sidx]);
+      }
+    }
     __syncthreads();
     for (int e0 = 0; e0 < N_E; e0 += EC) {
       const int ne = min(EC, N_E - e0);
+      if (tab2) {
+        for (int t = threadIdx.x; t < ne; t += blockDim.x)
+          g.lgE[t] = erest ? a.energies[e0 + t] : log10(a.energies[e0 + t]);
+        __syncthreads();
+      }
       // I, Q cos 2chi and Q sin 2chi of every profile column (:468-497)
+      int mu_col = -1;
+      MuStencil ms{};
       for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
         const int pl = t / N_L, col = t - pl * N_L;
         const int p = e0 + pl;
@@ -1339,12 +1397,31 @@ __global__ void __launch_bounds__(kThreads, 1) stokes_kernel(IntegrateArgs a) {
         if (s >= 0) {
           const double Ep = a.energies[p] / g.Z[s];
           const double abb = g.ABB[s];
-          double I_E = eval_bb(Ep, kT), Q_E = 0.0;
-          if (burst) {
-            I_E = I_E * (0.421 + 0.868 * abb);
-            Q_E = (0.1171 * (abb - 1.) / (1. + 3.582 * abb)) * I_E;
+          double I_E, Q_E = 0.0;
+          if (tab2) {
+            // the walk's mu clamp applies to a leaf's first energy only
+            const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
+                                    : g.lgE[pl] - g.lzs[s];
+            MuStencil m1;
+            if (p == 0 && g.clamp0[s]) {
+              m1 = mu_stencil(a.atmos, as, abb, true);
+            } else {
+              if (s != mu_col) {
+                ms = mu_stencil(a.atmos, as, abb, false);
+                mu_col = s;
+              }
+              m1 = ms;
+            }
+            I_E = eval_num4d_e(a.atmos, as, a.atmos.I, m1, v3, 1.0);
+            if (a.table_q) Q_E = eval_table_raw(a.atmos, as, a.table_q, m1, v3);
+          } else {
+            I_E = eval_bb(Ep, kT);
+            if (burst) {
+              I_E = I_E * (0.421 + 0.868 * abb);
+              Q_E = (0.1171 * (abb - 1.) / (1. + 3.582 * abb)) * I_E;
+            }
           }
-          const double I_c = corr ? eval_bb(Ep, kT_c) * norm : 0.0;
+          const double I_c = corr ? eval_bb(Ep, kT_c) * (kErg * kPlanck) : 0.0;
           yI = (I_E * norm - I_c) * g.GEOM[s];
           yQ = ((Q_E * g.c2chi[s]) * norm) * g.GEOM[s];
           yU = ((Q_E * g.s2chi[s]) * norm) * g.GEOM[s];
@@ -1551,6 +1628,20 @@ __global__ void reduce_flux_kernel(IntegrateArgs a) {
 
 }  // namespace
 
+// each parallel's entry state of a table atmosphere's mu walk: the
+// geometry pre-pass, then the per-mesh scan in call order
+static void launch_table_state(const IntegrateArgs &a, cudaStream_t st) {
+  const size_t pre_smem = geometry_bytes(a.N_L, a.N_R);
+  static bool pre_attr = false;
+  if (!pre_attr) {
+    cudaFuncSetAttribute(num4d_prepass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+    pre_attr = true;
+  }
+  num4d_prepass_kernel<<<(unsigned)a.n_rows, 128, pre_smem, st>>>(a);
+  num4d_scan_kernel<<<(a.n_members + 127) / 128, 128, 0, st>>>(a);
+}
+
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   if (a.n_members <= 0) return;
   const int pb = a.mixed ? (int)sizeof(PieceT<float>) : (int)sizeof(PieceT<double>);
@@ -1566,18 +1657,7 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
                            200 * 1024);
     attr_set[a.mixed ? 1 : 0] = true;
   }
-  bool any_num4d = a.atmos.I != nullptr;
-  if (any_num4d) {
-    const size_t pre_smem = geometry_bytes(a.N_L, a.N_R);
-    static bool pre_attr = false;
-    if (!pre_attr) {
-      cudaFuncSetAttribute(num4d_prepass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024);
-      pre_attr = true;
-    }
-    num4d_prepass_kernel<<<(unsigned)a.n_rows, 128, pre_smem, st>>>(a);
-    num4d_scan_kernel<<<(a.n_members + 127) / 128, 128, 0, st>>>(a);
-  }
+  if (a.atmos.I != nullptr) launch_table_state(a, st);
   if (a.mixed)
     integrate_kernel<float><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
   else
@@ -1592,8 +1672,8 @@ void launch_split_reduce(const SplitArgs &a, cudaStream_t st) {
   split_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
 }
 
-size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R) {
-  return stokes_smem(N_L, N_P, N_E, N_R);
+size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R, int nmu, int nE) {
+  return stokes_smem(N_L, N_P, N_E, N_R, nmu, nE);
 }
 
 size_t stokes_partial_doubles(const IntegrateArgs &a) {
@@ -1602,8 +1682,10 @@ size_t stokes_partial_doubles(const IntegrateArgs &a) {
 
 int launch_stokes(const IntegrateArgs &a, cudaStream_t st) {
   if (a.n_members <= 0) return 0;
-  const size_t smem = stokes_smem(a.N_L, a.N_P, a.N_E, a.N_R);
+  const int nmu = a.atmos.I ? a.atmos.nmu : 0, nE = a.atmos.I ? a.atmos.nE : 0;
+  const size_t smem = stokes_smem(a.N_L, a.N_P, a.N_E, a.N_R, nmu, nE);
   if (smem > 227 * 1024) return -2;
+  if (a.atmos.I != nullptr) launch_table_state(a, st);
   if (cudaFuncSetAttribute(stokes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -5;

@@ -77,9 +77,9 @@ struct IntegrateArgs {
   double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
   int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
   double *flux_q = nullptr, *flux_u = nullptr;  // Stokes Q, U (launch_stokes only)
-  // split atmosphere (members with atm 6): the reduced (mu, E) table
-  // [nmu][nE] on the grids atmos.mu, atmos.logE (E in electron rest energies)
-  const double *split_slab = nullptr;
+  // Stokes Q of a 2-D table atmosphere (atm 4, 6; launch_stokes only):
+  // [nmu][nE] on the grids of atmos (whose I is the intensity table)
+  const double *table_q = nullptr;
 };
 // the 5-D split atmosphere's reduction to (mu, E) at one parameter vector
 struct SplitArgs {
@@ -94,7 +94,7 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
 // Stokes I (a.flux), Q, U for blackbody (1) and burst blackbody (3) members;
 // a.partial: stokes_partial_doubles(a) doubles, zeroed; a.chunk_* unused
 size_t stokes_partial_doubles(const IntegrateArgs &a);
-size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R);
+size_t stokes_smem_bytes(int N_L, int N_P, int N_E, int N_R, int nmu = 0, int nE = 0);
 int launch_stokes(const IntegrateArgs &a, cudaStream_t st);
 
 // ---- K4 energy integrator ------------------------------------------------
