@@ -43,6 +43,7 @@ MODULES = [
     "surface_radiation_field.hot_Num2D_split",
     "cellmesh.integrator_for_azimuthal_invariance_split",
     "cellmesh.integratorIQU_for_azimuthal_invariance_split",
+    "cellmesh.integratorIQU",
     "likelihoods.default_background_marginalisation",
     "likelihoods._poisson_likelihood_given_background",
     "likelihoods._gaussian_likelihood_QnUn",

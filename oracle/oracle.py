@@ -68,7 +68,7 @@ def lib():
             L.xo_integrate_split_iqu.argtypes = (list(L.xo_integrate.argtypes)[:-6] +
                                                  [P, P, C.c_int, P, P, P])
             L.xo_integrate_general.restype = C.c_int
-            L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)[:-2]
+            L.xo_integrate_general.argtypes = list(L.xo_integrate.argtypes)
             L.xo_integrate_time_invariant.restype = C.c_int
             L.xo_integrate_time_invariant.argtypes = [
                 C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -222,17 +222,15 @@ def integrate_iqu(numThreads, R, omega, r_s, inclination, cellArea,
     return (0, out[0], out[1], out[2])
 
 
-def integrate_general(numThreads, R, omega, r_s, inclination, cellArea,
-                      radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
-                      CELL_RADIATES, correction_srcCellParams, numRays, deflection,
-                      cos_alpha, lag, maxDeflection, cos_gammaArray, energies, leaves,
-                      phases, hot_atmosphere, elsewhere_atmosphere, hot_atm_ext,
-                      else_atm_ext, beam_opt, image_order_limit=None, R_in=1e6):
-    """integrator.integrate (integrator.pyx:48-667), the general integrator
-    of HotRegion(symmetry=False), with the blackbody elsewhere correction
-    when correction_srcCellParams is given."""
+def _general(numThreads, R, omega, r_s, inclination, cellArea, radialCoords_of_parallels,
+             r_s_over_r, theta, phi, srcCellParams, CELL_RADIATES, correction_srcCellParams,
+             numRays, deflection, cos_alpha, lag, maxDeflection, cos_gammaArray, energies,
+             leaves, phases, hot_atmosphere, hot_atmosphere_Q, hot_atm_ext, else_atm_ext,
+             beam_opt, image_order_limit, R_in, stokes):
     if beam_opt != 0 or R_in < 1e6:
         raise NotImplementedError("oracle covers beam_opt 0 without a disk")
+    if int(hot_atm_ext) not in (1, 2, 3, 4):
+        raise NotImplementedError("oracle covers atmospheres 1 to 4")
     corr = None
     if correction_srcCellParams is not None:
         if int(else_atm_ext) != 1:
@@ -242,8 +240,9 @@ def integrate_general(numThreads, R, omega, r_s, inclination, cellArea,
     par = _c(srcCellParams)
     rad = _c(CELL_RADIATES, np.int32)
     E = _c(energies); Lv = _c(leaves); P = _c(phases)
-    out = np.zeros((E.size, P.size))
-    st, keep = _atmos_struct(hot_atmosphere)
+    out = [np.zeros((E.size, P.size)) for _ in range(3 if stokes else 1)]
+    st, keep = _atmos_struct(hot_atmosphere if int(hot_atm_ext) in (2, 4) else (),
+                             hot_atm_ext, hot_atmosphere_Q)
     arrs = [_c(radialCoords_of_parallels), _c(r_s_over_r), _c(theta), _c(phi),
             _c(deflection), _c(cos_alpha), _c(lag), _c(maxDeflection),
             _c(cos_gammaArray)]
@@ -255,11 +254,46 @@ def integrate_general(numThreads, R, omega, r_s, inclination, cellArea,
         _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), E.size, _p(E), Lv.size, _p(Lv),
         P.size, _p(P), int(hot_atm_ext),
         C.cast(C.pointer(st), C.c_void_p) if st is not None else None,
-        int(image_order_limit or 0), _p(out))
+        int(image_order_limit or 0), _p(out[0]), _p(out[1]) if stokes else None,
+        _p(out[2]) if stokes else None)
     del keep
     if status != 0:
         return (1, None)
-    return (0, out)
+    return (0,) + tuple(out)
+
+
+def integrate_general(numThreads, R, omega, r_s, inclination, cellArea,
+                      radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                      CELL_RADIATES, correction_srcCellParams, numRays, deflection,
+                      cos_alpha, lag, maxDeflection, cos_gammaArray, energies, leaves,
+                      phases, hot_atmosphere, elsewhere_atmosphere, hot_atm_ext,
+                      else_atm_ext, beam_opt, image_order_limit=None, R_in=1e6):
+    """integrator.integrate (integrator.pyx:48-667), the general integrator
+    of HotRegion(symmetry=False), with the blackbody elsewhere correction
+    when correction_srcCellParams is given; atmospheres 1 to 4."""
+    return _general(numThreads, R, omega, r_s, inclination, cellArea,
+                    radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                    CELL_RADIATES, correction_srcCellParams, numRays, deflection, cos_alpha,
+                    lag, maxDeflection, cos_gammaArray, energies, leaves, phases,
+                    hot_atmosphere, None, hot_atm_ext, else_atm_ext, beam_opt,
+                    image_order_limit, R_in, False)
+
+
+def integrate_general_iqu(numThreads, R, omega, r_s, inclination, cellArea,
+                          radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                          CELL_RADIATES, correction_srcCellParams, numRays, deflection,
+                          cos_alpha, lag, maxDeflection, cos_gammaArray, energies, leaves,
+                          phases, hot_atmosphere_I, hot_atmosphere_Q, elsewhere_atmosphere,
+                          hot_atm_ext, else_atm_ext, beam_opt, image_order_limit=None,
+                          R_in=1e6):
+    """integratorIQU.integrate (integratorIQU.pyx:76-717), the general Stokes
+    integrator: (0, flux_I, flux_Q, flux_U) or (1, None)."""
+    return _general(numThreads, R, omega, r_s, inclination, cellArea,
+                    radialCoords_of_parallels, r_s_over_r, theta, phi, srcCellParams,
+                    CELL_RADIATES, correction_srcCellParams, numRays, deflection, cos_alpha,
+                    lag, maxDeflection, cos_gammaArray, energies, leaves, phases,
+                    hot_atmosphere_I, hot_atmosphere_Q, hot_atm_ext, else_atm_ext, beam_opt,
+                    image_order_limit, R_in, True)
 
 
 def integrate_time_invariant(numThreads, R, omega, r_s, inclination, sqrt_numPix,

@@ -21,7 +21,8 @@
  *   xo_integrate_split       cellmesh/integrator_for_azimuthal_invariance_split.pyx
  *                            (hot_Num5D_split.pyx, hot_Num2D_split.pyx)
  *   xo_integrate_split_iqu   cellmesh/integratorIQU_for_azimuthal_invariance_split.pyx
- *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False)
+ *   xo_integrate_general     cellmesh/integrator.pyx:48-667 (symmetry=False),
+ *                            with Stokes Q and U as cellmesh/integratorIQU.pyx
  *   xo_integrate_time_invariant  cellmesh/integrator_for_time_invariance.pyx:59-338
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
  *   xo_expected_counts       tools/compute_expected_counts.pyx:200-276
@@ -859,16 +860,21 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
                          const double *energies, size_t N_L,
                          const double *leaves, size_t N_P, const double *phases,
                          int atm_ext, const xo_atmos4d *atmos,
-                         int image_order_limit, double *flux) {
+                         int image_order_limit, double *flux, double *flux_Q,
+                         double *flux_U) {
   (void)R;
   (void)r_s;
   const double sin_i = sin(inclination), cos_i = cos(inclination);
   const size_t leaf_lim = (N_L % 2 == 0) ? N_L / 2 : (N_L + 1) / 2;
-  const double norm = (atm_ext == 2) ? kErg / kHKeV : kErg * kPlanck;
+  /* hot_Num4D.pyx:441-461, hot_Num2D.pyx:359-367, hot_BB(_burst).pyx */
+  const double norm = (atm_ext == 2 || atm_ext == 4) ? kErg / kHKeV : kErg * kPlanck;
   const int perform_correction = correction != NULL;
+  /* Stokes Q and U (integratorIQU.pyx:76-717) when flux_Q and flux_U are
+   * given */
+  const int ns = (flux_Q != NULL && flux_U != NULL) ? 3 : 1;
   int nt = n_threads > 0 ? n_threads : 1;
   int terminate_any = 0;
-  double *priv = (double *)calloc((size_t)nt * N_P * N_E, sizeof(double));
+  double *priv = (double *)calloc((size_t)nt * ns * N_P * N_E, sizeof(double));
   /* :255-270 */
   double *cos_defl = (double *)malloc(S0 * N_R * sizeof(double));
   double *ca_alt = (double *)malloc(S0 * N_R * sizeof(double));
@@ -885,7 +891,7 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
 #ifdef _OPENMP
     T = omp_get_thread_num();
 #endif
-    double *pflux = priv + (size_t)T * N_P * N_E; /* [N_P][N_E] as :120 */
+    double *pflux = priv + (size_t)T * ns * N_P * N_E; /* ns x [N_P][N_E] as :120 */
     gsl_interp_accel *acc_a = gsl_interp_accel_alloc(), *acc_alt = gsl_interp_accel_alloc();
     gsl_interp_accel *acc_l = gsl_interp_accel_alloc();
     gsl_interp_accel *acc_g = gsl_interp_accel_alloc(), *acc_z = gsl_interp_accel_alloc();
@@ -901,6 +907,24 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
     double *GE = (double *)malloc(N_L * sizeof(double));
     num4d_state nst;
     if (atm_ext == 2) num4d_reset(&nst, atmos);
+    /* Pol_Num2D's I and Q evaluators (hot_Num2D.pyx:56-146), one per thread */
+    walk_state wst, wstq;
+    const double *g2[2] = {atmos ? atmos->mu : NULL, atmos ? atmos->logE : NULL};
+    const size_t n2[2] = {atmos ? atmos->nmu : 0, atmos ? atmos->nE : 0};
+    if (atm_ext == 4) {
+      walk_reset(&wst, g2, 2);
+      walk_reset(&wstq, g2, 2);
+    }
+    /* the polarisation angle's inputs as the reference leaves them after a
+     * leaf loop (integratorIQU.pyx:593-596 reads the loop's last values:
+     * cos psi and sin psi of the last leaf, cos alpha, sin alpha and mu of
+     * the last leaf within the maximum deflection, eta, cos xi and the leaf
+     * index of the last (leaf, mirror) assignment); thread-private and
+     * carried from parallel to parallel as Cython's first/lastprivate
+     * variables are */
+    double x_cpsi = NAN, x_spsi = NAN, x_ca = NAN, x_sa = NAN, x_mu = NAN, x_eta = NAN,
+           x_cxi = NAN;
+    size_t x_kdx = 0;
     int terminate = 0;
 #pragma omp for schedule(static, 1)
     for (long ii = 0; ii < (long)S0; ii++) {
@@ -932,6 +956,7 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
       double beta = radius * omega * sin_th / (kC * Grav_z);
       double Lorentz = sqrt(1.0 - beta * beta);
       double cos_a = -1.0, deriv = -1.0;
+      x_ca = -1.0; /* :326 */
       int IO = image_order_limit > 0 ? image_order_limit
                                      : (int)ceil(maxDeflection[i] / kPi);
       for (int I = 0; I < IO; I++) {
@@ -951,6 +976,8 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
           }
           int visible = 0;
           double sin_alpha = 0.0, mu = 0.0;
+          x_cpsi = cos_psi;
+          x_spsi = sin_psi;
           if (psi <= maxDeflection[i]) {
             if (psi < ia->xmin || psi > ia->xmax) { terminate = 1; break; }
             if (psi <= kHalfPi && cos_psi >= ialt->xmin)
@@ -965,6 +992,9 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
               else mu = mu - sin_alpha * sin_gamma * cos_delta;
             }
             visible = mu > 0.0;
+            x_ca = cos_a;
+            x_sa = sin_alpha;
+            x_mu = mu;
           }
           if (visible) {
             if (psi <= kHalfPi && cos_psi >= ialt->xmin) {
@@ -980,15 +1010,19 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
                   (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
                   (k == leaf_lim - 1 && N_L % 2 == 0)) {
                 size_t kdx = (ks == 0) ? k : N_L - 1 - k;
-                double superlum, eta;
+                double superlum, eta, cos_xi;
                 if (!are_equal(psi, 0.0)) {
-                  double cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
+                  cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
                   superlum = 1.0 + beta * cos_xi;
                   eta = Lorentz / superlum;
                 } else {
+                  cos_xi = 0.0;
                   superlum = 1.0;
                   eta = Lorentz;
                 }
+                x_kdx = kdx;
+                x_eta = eta;
+                x_cxi = cos_xi;
                 ZZ[kdx] = eta * Grav_z;
                 AB[kdx] = mu * eta;
                 GE[kdx] = mu * fabs(deriv) * Grav_z * eta * eta * eta / superlum;
@@ -1064,6 +1098,14 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
         gsl_interp_init(ib, PH, AB, N_L);
         gsl_interp_accel_reset(acc_g);
         gsl_interp_init(ig, PH, GE, N_L);
+        double c2chi = 0.0, s2chi = 0.0;
+        if (ns == 3) { /* integratorIQU.pyx:593-596, the same for every entry */
+          double chi = pol_angle(leaves[x_kdx], x_spsi, x_cpsi, x_sa, x_ca, sin_th, cos_th,
+                                 sin_i, cos_i, sin_gamma, cos_gamma, Grav_z, x_mu, x_eta, beta,
+                                 Lorentz, x_cxi);
+          c2chi = cos(2 * chi);
+          s2chi = sin(2 * chi);
+        }
         for (j = 0; j < S1 && !terminate; j++) { /* :549-594 */
           if (radiates[i * S1 + j] != 1) continue;
           const double shift = phi[i * S1 + j];
@@ -1083,14 +1125,32 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
               double ABB = gsl_interp_eval(ib, PH, AB, x, acc_b);
               for (size_t p = 0; p < N_E; p++) {
                 double Ep = energies[p] / Z;
-                double I_E = (atm_ext == 2) ? eval_num4d(atmos, &nst, Ep, ABB, VEC)
-                                            : eval_bb(Ep, VEC);
+                double I_E, Q_E = 0.0;
+                if (atm_ext == 2) {
+                  I_E = eval_num4d(atmos, &nst, Ep, ABB, VEC);
+                } else if (atm_ext == 3) { /* hot_BB_burst.pyx */
+                  I_E = eval_bb(Ep, VEC) * (0.421 + 0.868 * ABB);
+                  Q_E = (0.1171 * (ABB - 1.) / (1. + 3.582 * ABB)) * I_E;
+                } else if (atm_ext == 4) { /* hot_Num2D.pyx:187-400 */
+                  double q[2] = {ABB, log10(Ep)};
+                  I_E = walk_eval(g2, n2, 2, atmos->I, &wst, q);
+                  if (I_E < 0.0) I_E = 0.0;
+                  if (ns == 3 && atmos->Q) Q_E = walk_eval(g2, n2, 2, atmos->Q, &wstq, q);
+                } else {
+                  I_E = eval_bb(Ep, VEC);
+                }
                 I_E = I_E * norm;
                 double corr = 0.0;
                 if (perform_correction)
                   corr = eval_bb(Ep, correction + (i * S1 + j) * n_correction) *
                          (kErg * kPlanck);
                 pflux[k * N_E + p] += A * (I_E - corr) * G;
+                if (ns == 3) { /* integratorIQU.pyx:606-633 */
+                  Q_E = Q_E * norm;
+                  double Q_obs = Q_E * c2chi, U_obs = Q_E * s2chi;
+                  pflux[(N_P + k) * N_E + p] += A * Q_obs * G;
+                  pflux[(2 * N_P + k) * N_E + p] += A * U_obs * G;
+                }
               }
             }
           }
@@ -1108,12 +1168,15 @@ int xo_integrate_general(int n_threads, double R, double omega, double r_s,
   }
   gsl_set_error_handler(prev);
   /* :603-610 */
-  for (size_t p = 0; p < N_E; p++)
-    for (size_t k = 0; k < N_P; k++) {
-      double s = 0.0;
-      for (int T = 0; T < nt; T++) s += priv[(size_t)T * N_P * N_E + k * N_E + p];
-      flux[p * N_P + k] = s / (energies[p] * kKeV);
-    }
+  double *outs[3] = {flux, flux_Q, flux_U};
+  for (int c = 0; c < ns; c++)
+    for (size_t p = 0; p < N_E; p++)
+      for (size_t k = 0; k < N_P; k++) {
+        double s = 0.0;
+        for (int T = 0; T < nt; T++)
+          s += priv[(size_t)T * ns * N_P * N_E + ((size_t)c * N_P + k) * N_E + p];
+        outs[c][p * N_P + k] = s / (energies[p] * kKeV);
+      }
   free(priv); free(cos_defl); free(ca_alt);
   return terminate_any ? 1 : 0;
 }

@@ -204,3 +204,30 @@ def split_iqu_args(golden, tag, case, image_order_limit=None):
     a[12] = z.get(tag + "_correction")
     a[25] = 1 if a[12] is not None else None
     return tuple(a[:23]) + (synthetic.split_table_q(),) + tuple(a[23:])
+
+
+# the general Stokes fixture's cases: (tag, base fixture, atm_ext)
+GENERAL_IQU_CASES = (("config1_ext3", "config1", 3), ("num4d_omit_ext3", "num4d_omit", 3),
+                     ("config1_ext1_corrected", "config1", 1), ("config1_ext4", "config1", 4),
+                     ("num4d_omit_ext4_mu09", "num4d_omit", 4))
+
+
+def general_iqu_args(golden, tag, case, ext, stokes=True, image_order_limit=None):
+    """Arguments of the general Stokes (stokes True) or intensity integrator
+    for a general_iqu.npz case on the general integrator's cell-varying
+    temperatures."""
+    from xpsi_gb300 import synthetic
+    f = golden(case)
+    z = golden("general_iqu")
+    g = golden("general_integrator")
+    corr = z.get(tag + "_correction")
+    atm_I, atm_Q = (synthetic.pol2d_tables(mu_top=float(z[tag + "_mu_top"])) if ext == 4
+                    else ((), ()))
+    iol = image_order_limit if image_order_limit is not None else (
+        int(f["image_order_limit"]) or None)
+    common = (1, float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+              f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], g[case + "_params"],
+              f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"], f["lag"],
+              f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"], f["phases"])
+    atm = (atm_I, atm_Q) if stokes else (atm_I,)
+    return common + atm + ((), ext, 1 if corr is not None else None, 0, iol)

@@ -592,6 +592,49 @@ def split_iqu(xpsi):
     save("split_iqu", **out)
 
 
+def general_iqu(xpsi):
+    """The general Stokes integrator of HotRegion(symmetry=False)
+    (cellmesh/integratorIQU.pyx) and, for the same atmospheres, the general
+    intensity integrator (cellmesh/integrator.pyx), on the general
+    integrator's cell-varying temperatures: the burst blackbody (atm_ext 3)
+    at 300 and 600 Hz, the blackbody with a blackbody elsewhere's
+    correction, and Pol_Num2D (atm_ext 4) on full and 0.9-topped mu grids."""
+    from xpsi.cellmesh.integrator import integrate as plain
+    from xpsi.cellmesh.integratorIQU import integrate as iqu
+    g = np.load(os.path.join(HERE, "general_integrator.npz"))
+    out = {}
+    for tag, case, ext, corr_T, mu_top in (("config1_ext3", "config1", 3, None, 1.0),
+                                           ("num4d_omit_ext3", "num4d_omit", 3, None, 1.0),
+                                           ("config1_ext1_corrected", "config1", 1, 6.0, 1.0),
+                                           ("config1_ext4", "config1", 4, None, 1.0),
+                                           ("num4d_omit_ext4_mu09", "num4d_omit", 4, None, 0.9)):
+        f = np.load(os.path.join(HERE, case + ".npz"))
+        S = int(f["S"])
+        params = np.ascontiguousarray(g[case + "_params"])
+        corr = None
+        if corr_T is not None:
+            corr = np.ones((S, S, 2))
+            corr[..., 0] = corr_T
+            corr[..., 1] = f["effGrav"][:, None]
+        atm_I, atm_Q = synthetic.pol2d_tables(mu_top=mu_top) if ext == 4 else ((), ())
+        common = (float(f["R"]), float(f["Omega"]), float(f["r_s"]), float(f["inclination"]),
+                  f["cellArea"], f["radius"], f["u"], f["theta"], f["phi"], params,
+                  f["radiates"], corr, int(f["N_R"]), f["deflection"], f["cos_alpha"],
+                  f["lag"], f["maxDeflection"], f["cos_gamma"], f["energies"], f["leaves"],
+                  f["phases"])
+        iol = int(f["image_order_limit"]) or None
+        res = iqu(1, *common, atm_I, atm_Q, (), ext, 1 if corr is not None else None, 0, iol)
+        assert res[0] == 0
+        st, flux = plain(1, *common, atm_I, (), ext, 1 if corr is not None else None, 0, iol)
+        assert st == 0
+        out[tag + "_I"], out[tag + "_Q"], out[tag + "_U"] = res[1], res[2], res[3]
+        out[tag + "_plain"] = flux
+        out[tag + "_mu_top"] = np.array(mu_top)
+        if corr is not None:
+            out[tag + "_correction"] = corr
+    save("general_iqu", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -606,6 +649,7 @@ def main():
     split(xpsi)
     pol_num2d(xpsi)
     split_iqu(xpsi)
+    general_iqu(xpsi)
 
 
 if __name__ == "__main__":

@@ -5,7 +5,8 @@ integrator (integratorIQU_for_azimuthal_invariance_split.pyx,
 tests/golden/split_iqu.npz).  CPU only."""
 import pytest
 
-from conftest import POL2D_CASES, SPLIT_CASES, pol2d_args, row_rel, split_iqu_args
+from conftest import (GENERAL_IQU_CASES, POL2D_CASES, SPLIT_CASES, general_iqu_args, pol2d_args,
+                      row_rel, split_iqu_args)
 from oracle import oracle as O
 
 
@@ -38,3 +39,18 @@ def test_split_iqu_rejects_tables_on_different_grids(golden):
     a[23] = tuple(q)
     with pytest.raises(NotImplementedError):
         O.integrate_split_iqu(*a)
+
+
+@pytest.mark.parametrize("tag,case,ext", GENERAL_IQU_CASES)
+def test_oracle_general_iqu_vs_reference(golden, tag, case, ext):
+    """The general Stokes integrator (integratorIQU.pyx), whose polarisation
+    angle reads the leaf loop's last values, and the general intensity
+    integrator with the same atmospheres."""
+    z = golden("general_iqu")
+    res = O.integrate_general_iqu(*general_iqu_args(golden, tag, case, ext))
+    assert res[0] == 0
+    for k, s in enumerate("IQU"):
+        assert row_rel(res[k + 1], z[tag + "_" + s]) <= 1e-13, s
+    st, flux = O.integrate_general(*general_iqu_args(golden, tag, case, ext, stokes=False))
+    assert st == 0
+    assert row_rel(flux, z[tag + "_plain"]) <= 1e-13
