@@ -30,7 +30,8 @@ extern "C" {
  * Gaussian-likelihood entry points were added.
  * 3: xgpu_atmos5d, xgpu_integrate_split and xgpu_integrate_split_stokes (split
  * atmospheres); xgpu_integrate_stokes takes the I and Q tables of atm_ext 4
- * (Pol_Num2D), which xgpu_integrate also takes. */
+ * (Pol_Num2D), which xgpu_integrate and xgpu_integrate_general also take;
+ * xgpu_integrate_general_stokes. */
 #define XGPU_ABI_VERSION 3
 
 /* Status words of the batched layer (per parameter vector). */
@@ -182,9 +183,10 @@ int xgpu_integrate_split_stokes(double R, double omega, double r_s,
 
 /* Replaces xpsi.cellmesh.integrator.integrate (xpsi/cellmesh/integrator.pyx:
  * 48-667), the general integrator of HotRegion(symmetry=False) for source
- * parameters that vary from cell to cell.  Same arguments as xgpu_integrate
- * (the phase interpolant of the geometric factor is Akima periodic, the
- * reference's default).  Returns 0 (SUCCESS) or 1 (ERROR, :657-665), < 0 on a
+ * parameters that vary from cell to cell.  Same arguments as xgpu_integrate,
+ * with atm_ext 3 (burst blackbody's intensity) also taken (the phase
+ * interpolant of the geometric factor is Akima periodic, the reference's
+ * default).  Returns 0 (SUCCESS) or 1 (ERROR, :657-665), < 0 on a
  * usage or CUDA failure. */
 int xgpu_integrate_general(double R, double omega, double r_s,
                            double inclination, size_t S0, size_t S1,
@@ -203,6 +205,33 @@ int xgpu_integrate_general(double R, double omega, double r_s,
                            const double *phases, int atm_ext,
                            const xgpu_atmos4d *atmos, int else_atm_ext,
                            int image_order_limit, double *flux);
+
+/* Replaces xpsi.cellmesh.integratorIQU.integrate
+ * (xpsi/cellmesh/integratorIQU.pyx:76-717), the Stokes integrator of
+ * HotRegion(symmetry=False): arguments as xgpu_integrate_general, with
+ * atmos_I and atmos_Q as xgpu_integrate_stokes takes them (atm_ext 1, 2 with
+ * Q = 0, 3, 4).  The polarisation angle of each (parallel, image) is the
+ * reference's: computed from the leaf loop's last values (:593-596).
+ * Outputs flux_I, flux_Q, flux_U [N_E][N_P]. */
+int xgpu_integrate_general_stokes(double R, double omega, double r_s,
+                                  double inclination, size_t S0, size_t S1,
+                                  const double *cellArea,
+                                  const double *radialCoords_of_parallels,
+                                  const double *r_s_over_r, const double *theta,
+                                  const double *phi, const double *srcCellParams,
+                                  size_t n_params, const int32_t *cell_radiates,
+                                  const double *correction_srcCellParams,
+                                  size_t n_correction, size_t N_R,
+                                  const double *deflection, const double *cos_alpha,
+                                  const double *lag, const double *maxDeflection,
+                                  const double *cos_gammaArray, size_t N_E,
+                                  const double *energies, size_t N_L,
+                                  const double *leaves, size_t N_P,
+                                  const double *phases, int atm_ext,
+                                  const xgpu_atmos4d *atmos_I,
+                                  const xgpu_atmos4d *atmos_Q, int else_atm_ext,
+                                  int image_order_limit, double *flux_I,
+                                  double *flux_Q, double *flux_U);
 
 /* Replaces xpsi.tools.energy_integrator.energy_integrator
  * (xpsi/tools/energy_integrator.pyx:27-31).  signal[N_E][N_P]; log10 energies

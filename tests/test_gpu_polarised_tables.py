@@ -5,7 +5,8 @@ integrator (tests/golden/split_iqu.npz).  Every energy row of I, Q and U to
 1e-9 of its largest value, the integrator's bar."""
 import pytest
 
-from conftest import POL2D_CASES, SPLIT_CASES, pol2d_args, row_rel, split_iqu_args
+from conftest import (GENERAL_IQU_CASES, POL2D_CASES, SPLIT_CASES, general_iqu_args, pol2d_args,
+                      row_rel, row_rel_floor, split_iqu_args)
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -70,3 +71,21 @@ def test_split_stokes_intensity_is_the_split_integrators(mods, golden):
     st, flux = split.integrate(*split_args(golden, "num4d_omit", "num4d_omit"))
     assert res[0] == st == 0
     assert row_rel(res[1], flux) <= 1e-12
+
+
+@pytest.mark.parametrize("tag,case,ext", GENERAL_IQU_CASES)
+def test_general_stokes_vs_reference(golden, tag, case, ext):
+    """The general Stokes integrator (integratorIQU.pyx) and the general
+    intensity integrator with the same atmospheres, on the GPU."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from xpsi_gb300.cellmesh import integrator, integratorIQU
+    z = golden("general_iqu")
+    res = integratorIQU.integrate(*general_iqu_args(golden, tag, case, ext))
+    assert res[0] == 0
+    for k, s in enumerate("IQU"):
+        assert row_rel_floor(res[k + 1], z[tag + "_" + s]) <= RTOL, s
+    st, flux = integrator.integrate(*general_iqu_args(golden, tag, case, ext, stokes=False))
+    assert st == 0
+    assert row_rel_floor(flux, z[tag + "_plain"]) <= RTOL

@@ -37,6 +37,8 @@ def test_install_rebinds_path_callables():
     assert hr._integratorIQU is integratorIQU_for_azimuthal_invariance.integrate
     hr.symmetry = False
     assert hr._integrator is integrator.integrate
+    from xpsi_gb300.cellmesh import integratorIQU
+    assert hr._integratorIQU is integratorIQU.integrate
 
 
 def test_install_binds_split_integrator():

@@ -7,6 +7,7 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
     xpsi_gb300.cellmesh.rays.compute_rays
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
     xpsi_gb300.cellmesh.integrator.integrate          (HotRegion symmetry=False)
+    xpsi_gb300.cellmesh.integratorIQU.integrate       (the same, Stokes)
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance_split.integrate
     xpsi_gb300.cellmesh.integratorIQU_for_azimuthal_invariance_split.integrate
                                                       (HotRegion split=True)
@@ -41,6 +42,7 @@ def install(xpsi_module):
     from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
     from .cellmesh import integrator as general
+    from .cellmesh import integratorIQU as general_iqu
     from .cellmesh import integrator_for_azimuthal_invariance_split as split
     from .cellmesh import integratorIQU_for_azimuthal_invariance_split as iqu_split
     from .cellmesh import integratorIQU_for_azimuthal_invariance as iqu
@@ -62,6 +64,7 @@ def install(xpsi_module):
          global_mesh.construct_closed_cellMesh),
         ("xpsi.cellmesh.integrator_for_time_invariance", "integrate", tinv.integrate),
         ("xpsi.cellmesh.integrator", "integrate", general.integrate),
+        ("xpsi.cellmesh.integratorIQU", "integrate", general_iqu.integrate),
         ("xpsi.cellmesh.integrator_for_azimuthal_invariance_split", "integrate",
          split.integrate),
         ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance_split", "integrate",
@@ -107,8 +110,7 @@ def install(xpsi_module):
         _orig(self, declaration)
         if not getattr(self, "_split", False):
             self._integrator = integ.integrate if declaration else general.integrate
-            if declaration:
-                self._integratorIQU = iqu.integrate
+            self._integratorIQU = iqu.integrate if declaration else general_iqu.integrate
         elif declaration:
             # split=True and symmetry=False raise in the original setter
             self._integrator = split.integrate

@@ -8,6 +8,7 @@ import numpy as np
 
 from .._arr import f64, i32, ptr
 from .._native import Atmos4D, check, lib
+from ._tables import table2d
 
 SUCCESS = 0
 ERROR = 1
@@ -22,7 +23,8 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     """Integrate over the image of a star on a distant observer's sky (GPU).
 
     Returns (0, flux[N_E, N_P]) or (1, None) exactly as the reference does.
-    Supported: blackbody (hot_atm_ext 1) and numerical 4-D (2) hot
+    Supported: blackbody (hot_atm_ext 1), numerical 4-D (2), burst
+    blackbody (3, its intensity) and Pol_Num2D (4, its intensity table) hot
     atmospheres with beam_opt 0 and no disk (R_in >= 1e6), with or without
     the correction for a blackbody elsewhere (else_atm_ext 1); the geometric
     factor is splined in phase with the Akima periodic interpolant (the
@@ -42,7 +44,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     if R_in < 1e6:
         raise NotImplementedError("disk occultation is not on the GPU path")
     atm = int(hot_atm_ext)
-    if atm not in (1, 2):
+    if atm not in (1, 2, 3, 4):
         raise NotImplementedError("hot atmosphere extension %d is not on the GPU path" % atm)
     par = f64(srcCellParams)
     rad = i32(CELL_RADIATES)
@@ -57,6 +59,8 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         raise ValueError("ray tables must be [rows, numRays]")
     atmos = None
     keep = ()
+    if atm == 4:
+        atmos, keep = table2d(hot_atmosphere)
     if atm == 2:
         if not hot_atmosphere:
             raise ValueError("numerical atmosphere data were not preloaded")

@@ -759,7 +759,11 @@ int xgpu_integrate_split_stokes(double R, double omega, double r_s, double incli
                      flux_Q, flux_U);
 }
 
-int xgpu_integrate_general(double R, double omega, double r_s, double inclination, size_t S0,
+}  // extern "C"
+
+namespace {
+// the general integrators' common host path (I, or I, Q and U)
+int general_host(cudaStream_t st, double omega, double inclination, size_t S0,
                            size_t S1, const double *cellArea, const double *radius,
                            const double *r_s_over_r, const double *theta, const double *phi,
                            const double *srcCellParams, size_t n_params,
@@ -769,18 +773,15 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
                            const double *maxDeflection, const double *cos_gamma, size_t N_E,
                            const double *energies, size_t N_L, const double *leaves,
                            size_t N_P, const double *phases, int atm_ext,
-                           const xgpu_atmos4d *atmos, int else_atm_ext, int image_order_limit,
-                           double *flux) {
-  (void)R;
-  (void)r_s;
-  cudaStream_t st;
+                           const xg::Atmos4D &A, const double *dQ, int else_atm_ext,
+                           int image_order_limit, double *flux, double *flux_Q,
+                           double *flux_U) {
   int rc;
-  if ((rc = lib_stream(&st))) return rc;
+  const int stokes = (flux_Q != nullptr && flux_U != nullptr) ? 1 : 0;
+  const int ns = stokes ? 3 : 1;
   if (S0 == 0 || S1 == 0 || N_E == 0 || N_P == 0) return 0;
   if (N_L < 5) return fail_msg("num_leaves must be at least 5 (Akima spline)");
   if (N_R < 3) return fail_msg("num_rays must be at least 3");
-  if (atm_ext != 1 && atm_ext != 2) return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
-  if (atm_ext == 2 && !atmos) return fail_msg("atm_ext 2 (Num4D) needs the atmosphere");
   if (atm_ext == 2 && n_params < 2)
     return fail_msg("srcCellParams needs (log T, log g) per cell for Num4D");
   if (n_params < 1) return fail_msg("srcCellParams needs at least 1 parameter per cell");
@@ -801,14 +802,12 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
     if (io > 64.0) return fail_msg("a parallel has more than 64 images");
     IOmax = std::max(IOmax, (int)io);
   }
-  xg::Atmos4D A{};
-  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
   const size_t cells = S0 * S1;
   std::vector<double> theta0(S0);
   for (size_t i = 0; i < S0; i++) theta0[i] = theta[i * S1];
   const size_t n_ent = cells * (size_t)IOmax * N_P;
   Dev dA, drad, du, dth0, dphi, dpar, dR, dD, dCA, dL, dMD, dcg, dE, dLv, dP, dF, dst, dcorr;
-  Dev deG, deZ, deA, dimg, dpart;
+  Dev deG, deZ, deA, dimg, dpart, dchi, dFq;
   if ((rc = upload(dA, cellArea, cells, st)) || (rc = upload(drad, radius, S0, st)) ||
       (rc = upload(du, r_s_over_r, S0, st)) || (rc = upload(dth0, theta0.data(), S0, st)) ||
       (rc = upload(dphi, phi, cells, st)) || (rc = upload(dpar, srcCellParams, cells * n_params, st)) ||
@@ -820,8 +819,10 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
       (rc = dalloc(dst, 16, st)) || (rc = dalloc(deG, n_ent * 8, st)) ||
       (rc = dalloc(deZ, n_ent * 8, st)) || (rc = dalloc(deA, n_ent * 8, st)) ||
       (rc = dalloc(dimg, S0 * 4, st)) ||
-      (rc = dalloc(dpart, S0 * (size_t)IOmax * N_E * N_P * 8, st)))
+      (rc = dalloc(dpart, S0 * (size_t)IOmax * ns * N_E * N_P * 8, st)) ||
+      (rc = dalloc(dchi, S0 * (size_t)IOmax * 2 * 8, st)))
     return rc;
+  if (stokes && (rc = dalloc(dFq, 2 * N_E * N_P * 8, st))) return rc;
   if (correction && (rc = upload(dcorr, correction, cells * n_correction, st))) return rc;
   CK(cudaMemsetAsync(dst.p, 0, 16, st));
   xg::GeneralArgs a{};
@@ -829,6 +830,7 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
   a.N_E = (int)N_E; a.IOmax = IOmax;
   a.omega = omega; a.inclination = inclination; a.image_order_limit = image_order_limit;
   a.atm_ext = atm_ext;
+  a.stokes = stokes;
   a.radiates = dR.as<int32_t>();
   a.cellArea = dA.as<double>(); a.phi = dphi.as<double>(); a.params = dpar.as<double>();
   a.n_params = (int)n_params;
@@ -839,10 +841,14 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
   a.deflection = dD.as<double>(); a.cos_alpha = dCA.as<double>(); a.lag = dL.as<double>();
   a.energies = dE.as<double>(); a.leaves = dLv.as<double>(); a.phases = dP.as<double>();
   a.atmos = A;
+  a.table_q = dQ;
+  a.chi2 = dchi.as<double>();
   a.eG = deG.as<double>(); a.eZ = deZ.as<double>(); a.eA = deA.as<double>();
   a.n_img = dimg.as<int32_t>();
   a.partial = dpart.as<double>();
   a.flux = dF.as<double>();
+  a.flux_q = stokes ? dFq.as<double>() : nullptr;
+  a.flux_u = stokes ? dFq.as<double>() + N_E * N_P : nullptr;
   a.status = dst.as<int32_t>();
   rc = xg::launch_general(a, st);
   if (rc == -2) return fail_msg("integrator shared memory too large");
@@ -850,9 +856,85 @@ int xgpu_integrate_general(double R, double omega, double r_s, double inclinatio
   int32_t status = 0;
   CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(flux, dF.p, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  if (stokes) {
+    CK(cudaMemcpyAsync(flux_Q, a.flux_q, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(flux_U, a.flux_u, N_E * N_P * 8, cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaStreamSynchronize(st));
   if (status == XGPU_BAD_INPUT) return fail_msg("a parallel has more images than held");
   return status != 0 ? 1 : 0;
+}
+}  // namespace
+
+extern "C" {
+
+int xgpu_integrate_general(double R, double omega, double r_s, double inclination, size_t S0,
+                           size_t S1, const double *cellArea, const double *radius,
+                           const double *r_s_over_r, const double *theta, const double *phi,
+                           const double *srcCellParams, size_t n_params,
+                           const int32_t *radiates, const double *correction,
+                           size_t n_correction, size_t N_R, const double *deflection,
+                           const double *cos_alpha, const double *lag,
+                           const double *maxDeflection, const double *cos_gamma, size_t N_E,
+                           const double *energies, size_t N_L, const double *leaves,
+                           size_t N_P, const double *phases, int atm_ext,
+                           const xgpu_atmos4d *atmos, int else_atm_ext, int image_order_limit,
+                           double *flux) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (atm_ext < 1 || atm_ext > 4)
+    return fail_msg("atm_ext must be 1 (BB), 2 (Num4D), 3 (burst BB) or 4 (Pol_Num2D)");
+  if ((atm_ext == 2 || atm_ext == 4) && !atmos)
+    return fail_msg("numerical atmospheres (atm_ext 2, 4) need the table");
+  xg::Atmos4D A{};
+  Dev dt;
+  if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
+  if (atm_ext == 4 && (rc = table2d_device(st, atmos, nullptr, dt, &A, nullptr))) return rc;
+  return general_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta, phi,
+                      srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                      deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies, N_L,
+                      leaves, N_P, phases, atm_ext, A, nullptr, else_atm_ext,
+                      image_order_limit, flux, nullptr, nullptr);
+}
+
+int xgpu_integrate_general_stokes(double R, double omega, double r_s, double inclination,
+                                  size_t S0, size_t S1, const double *cellArea,
+                                  const double *radius, const double *r_s_over_r,
+                                  const double *theta, const double *phi,
+                                  const double *srcCellParams, size_t n_params,
+                                  const int32_t *radiates, const double *correction,
+                                  size_t n_correction, size_t N_R, const double *deflection,
+                                  const double *cos_alpha, const double *lag,
+                                  const double *maxDeflection, const double *cos_gamma,
+                                  size_t N_E, const double *energies, size_t N_L,
+                                  const double *leaves, size_t N_P, const double *phases,
+                                  int atm_ext, const xgpu_atmos4d *atmos_I,
+                                  const xgpu_atmos4d *atmos_Q, int else_atm_ext,
+                                  int image_order_limit, double *flux_I, double *flux_Q,
+                                  double *flux_U) {
+  (void)R;
+  (void)r_s;
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (atm_ext < 1 || atm_ext > 4)
+    return fail_msg("atm_ext must be 1 (BB), 2 (Num4D), 3 (burst BB) or 4 (Pol_Num2D)");
+  if (atm_ext == 2 && !atmos_I) return fail_msg("atm_ext 2 (Num4D) needs the I table");
+  if (atm_ext == 4 && (!atmos_I || !atmos_Q))
+    return fail_msg("atm_ext 4 (Pol_Num2D) needs the I and Q tables");
+  xg::Atmos4D A{};
+  const double *dQ = nullptr;
+  Dev dt;
+  if (atm_ext == 2 && (rc = atmos_device(atmos_I, st, &A))) return rc;
+  if (atm_ext == 4 && (rc = table2d_device(st, atmos_I, atmos_Q, dt, &A, &dQ))) return rc;
+  return general_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta, phi,
+                      srcCellParams, n_params, radiates, correction, n_correction, N_R,
+                      deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies, N_L,
+                      leaves, N_P, phases, atm_ext, A, dQ, else_atm_ext, image_order_limit,
+                      flux_I, flux_Q, flux_U);
 }
 
 int xgpu_energy_integrator(size_t N_E, size_t N_P, const double *signal,

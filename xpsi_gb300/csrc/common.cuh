@@ -485,4 +485,23 @@ __device__ __forceinline__ void gk_panel_df(const F &f, const float *X2, const f
   rasc = rcd;
 }
 
+// the polarisation angle in the oblate Schwarzschild approximation (Loktev
+// et al. 2020), cellmesh/common_functions.pyx:7-66
+__device__ inline double pol_angle(double leaf, double sin_psi, double cos_psi, double sin_alpha,
+                            double cos_alpha, double sin_th, double cos_th, double sin_i,
+                            double cos_i, double sin_gamma, double cos_gamma, double Grav_z,
+                            double mu, double eta, double beta, double Lorentz, double cos_xi) {
+  const double chi_0 = atan2(-sin_th * sin(leaf), sin_i * cos_th - sin_th * cos_i * cos(leaf));
+  const double sa_over_sp = !are_equal(sin_psi, 0.0) ? sin_alpha / sin_psi : Grav_z;
+  const double chi_1 = atan2(sin_gamma * sin_i * sin(leaf) * sa_over_sp,
+                             cos_gamma - cos_alpha * mu);
+  const double sin_lambda = sin_th * cos_gamma - sin_gamma * cos_th;
+  const double cos_lambda = cos_th * cos_gamma + sin_th * sin_gamma;
+  const double cos_eps = sa_over_sp * (cos_i * sin_lambda - sin_i * cos_lambda * cos(leaf) +
+                                       cos_psi * sin_gamma) - cos_alpha * sin_gamma;
+  const double chi_p = atan2(cos_eps * eta * mu * beta / Lorentz,
+                             (1. - mu * mu / (1. + beta * cos_xi)));
+  return chi_0 + chi_1 + chi_p;
+}
+
 }  // namespace xg

@@ -1,8 +1,16 @@
 // general.cu -- the general cell-mesh integrator (HotRegion with
 // symmetry=False: source parameters that vary from cell to cell), replacing
-// xpsi/cellmesh/integrator.pyx:48-667 with the blackbody (hot_BB.pyx:54-98)
-// and numerical 4-D (hot_Num4D.pyx:248-461) atmospheres and the correction
-// for a blackbody elsewhere (:577-592).
+// xpsi/cellmesh/integrator.pyx:48-667 with the blackbody (hot_BB.pyx:54-98),
+// numerical 4-D (hot_Num4D.pyx:248-461), burst blackbody (hot_BB_burst.pyx)
+// and Pol_Num2D (hot_Num2D.pyx:187-400) atmospheres and the correction for a
+// blackbody elsewhere (:577-592); with `stokes`, also Q and U as
+// xpsi/cellmesh/integratorIQU.pyx:76-717 does.
+//
+// The Stokes integrator's polarisation angle (integratorIQU.pyx:593-596) is
+// computed from the variables as the leaf loop leaves them: cos psi and
+// sin psi of the last leaf, cos alpha, sin alpha and mu of the last leaf
+// within the maximum deflection, and eta, cos xi and the leaf index of the
+// last (leaf, mirror) assignment -- one angle per (parallel, image).
 //
 // Unlike the azimuthally invariant integrator, the atmosphere is evaluated
 // per cell at every signal phase: per parallel and image, the leaf profiles
@@ -51,6 +59,10 @@ struct GenRow {
 
 struct GenSmem {
   double *rD;                      // [N_R] staged deflections
+  // per leaf, the polarisation angle's inputs as the leaf loop assigns them
+  double *xcpsi, *xspsi, *xca, *xsa, *xmu, *xeta, *xcxi;  // [N_L]
+  int *xvis, *xks;                 // [N_L] within max deflection; last mirror pass
+                                   // (0 none, 1 the leaf, 2 its mirror)
   double *lPH, *lZ, *lAB, *lGE;    // [N_L] leaf values written by the geometry
   double *PH, *ZZ, *AB, *GE;       // [N_L] the state machine's knots and values
   double *pZ, *pA, *pG;            // [4 (N_L - 1)] spline pieces (y, k1, k2, k3)
@@ -72,9 +84,18 @@ __device__ GenSmem gen_carve(double *sm, int N_R, int N_L) {
   g.pZ = g.GE + N_L;
   g.pA = g.pZ + 4 * N_L;
   g.pG = g.pA + 4 * N_L;
-  g.calc = reinterpret_cast<int *>(g.pG + 4 * N_L);
+  g.xcpsi = g.pG + 4 * N_L;
+  g.xspsi = g.xcpsi + N_L;
+  g.xca = g.xspsi + N_L;
+  g.xsa = g.xca + N_L;
+  g.xmu = g.xsa + N_L;
+  g.xeta = g.xmu + N_L;
+  g.xcxi = g.xeta + N_L;
+  g.calc = reinterpret_cast<int *>(g.xcxi + N_L);
   g.term = g.calc + N_L;
-  g.flags = g.term + N_L;
+  g.xvis = g.term + N_L;
+  g.xks = g.xvis + N_L;
+  g.flags = g.xks + N_L;
   return g;
 }
 
@@ -95,12 +116,13 @@ __device__ void gen_leaf(const GenRow &r, double cos_i, double sin_i, double inc
   AltX ax{r.D, r.jalt};
   AltY ay{r.CA, r.jalt};
   const double alt_xmin = cos(r.D[r.jalt]);
-  int calc = 0, term = 0;
-  double sin_alpha = 0.0, mu = 0.0, cos_a;
+  int calc = 0, term = 0, vis = 0, ks_last = 0;
+  double sin_alpha = 0.0, mu = 0.0, cos_a = 0.0, eta_last = 0.0, cxi_last = 0.0;
   if (psi <= r.maxDefl) {
     if (psi < r.D[0] || psi > r.D[r.N_R - 1]) {
       term = 1;
     } else {
+      vis = 1;
       if (psi <= kHalfPi && cos_psi >= alt_xmin)
         steffen_eval(ax, ay, r.jalt + 1, cos_psi, &cos_a, nullptr);
       else
@@ -130,15 +152,19 @@ __device__ void gen_leaf(const GenRow &r, double cos_i, double sin_i, double inc
           (k == leaf_lim - 1 && N_L % 2 == 1 && ks == 0) ||
           (k == leaf_lim - 1 && N_L % 2 == 0)) {
         const int kdx = (ks == 0) ? k : N_L - 1 - k;
-        double superlum, eta;
+        double superlum, eta, cos_xi;
         if (!are_equal(psi, 0.0)) {
-          const double cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
+          cos_xi = sin_alpha * sin_i * sin(leaves[kdx]) / sin_psi;
           superlum = 1.0 + r.beta * cos_xi;
           eta = r.Lorentz / superlum;
         } else {
+          cos_xi = 0.0;
           superlum = 1.0;
           eta = r.Lorentz;
         }
+        ks_last = ks + 1;
+        eta_last = eta;
+        cxi_last = cos_xi;
         g.lZ[kdx] = eta * r.Grav_z;
         g.lAB[kdx] = mu * eta;
         g.lGE[kdx] = mu * fabs(deriv) * r.Grav_z * eta * eta * eta / superlum;
@@ -148,6 +174,15 @@ __device__ void gen_leaf(const GenRow &r, double cos_i, double sin_i, double inc
   }
   g.calc[k] = calc;
   g.term[k] = term;
+  g.xcpsi[k] = cos_psi;
+  g.xspsi[k] = sin_psi;
+  g.xvis[k] = vis;
+  g.xca[k] = cos_a;
+  g.xsa[k] = sin_alpha;
+  g.xmu[k] = mu;
+  g.xks[k] = ks_last;
+  g.xeta[k] = eta_last;
+  g.xcxi[k] = cxi_last;
 }
 
 // :421-535, one thread, in the reference's leaf order: a visible leaf's
@@ -294,6 +329,12 @@ __global__ void __launch_bounds__(kGenThreads) general_geometry_kernel(GeneralAr
   r.maxDefl = a.maxDeflection[i];
   const int IO = a.image_order_limit > 0 ? a.image_order_limit : (int)ceil(r.maxDefl / kPi);
   const double cos_i = cos(a.inclination), sin_i = sin(a.inclination);
+  // the polarisation angle's inputs carried over images (thread 0); at the
+  // parallel's start cos alpha is -1 (integratorIQU.pyx:326) and the others
+  // are not yet assigned
+  double x_cpsi = NAN, x_spsi = NAN, x_ca = -1.0, x_sa = NAN, x_mu = NAN, x_eta = NAN,
+         x_cxi = NAN;
+  int x_kdx = 0;
   int done = 0;
   for (int I = 0; I < IO; I++) {
     if (I >= a.IOmax) {  // more images than the scratch holds
@@ -310,6 +351,28 @@ __global__ void __launch_bounds__(kGenThreads) general_geometry_kernel(GeneralAr
       break;
     }
     if (g.flags[1]) break;
+    if (a.stokes && threadIdx.x == 0) {
+      for (int k = 0; k < N_L; k++) {
+        x_cpsi = g.xcpsi[k];
+        x_spsi = g.xspsi[k];
+        if (g.xvis[k]) {
+          x_ca = g.xca[k];
+          x_sa = g.xsa[k];
+          x_mu = g.xmu[k];
+        }
+        if (g.xks[k]) {
+          x_kdx = g.xks[k] == 1 ? k : N_L - 1 - k;
+          x_eta = g.xeta[k];
+          x_cxi = g.xcxi[k];
+        }
+      }
+      const double chi = pol_angle(a.leaves[x_kdx], x_spsi, x_cpsi, x_sa, x_ca, r.sin_th,
+                                   r.cos_th, sin_i, cos_i, r.sin_gamma, r.cos_gamma, r.Grav_z,
+                                   x_mu, x_eta, r.beta, r.Lorentz, x_cxi);
+      double *c2 = a.chi2 + ((int64_t)i * a.IOmax + I) * 2;
+      c2[0] = cos(2 * chi);
+      c2[1] = sin(2 * chi);
+    }
     // spline pieces: Steffen for Z and mu eta, Akima periodic for the
     // geometric factor (the reference's default phase interpolant)
     for (int t = threadIdx.x; t < N_L - 1; t += blockDim.x) {
@@ -373,7 +436,8 @@ __global__ void __launch_bounds__(kGenThreads) general_geometry_kernel(GeneralAr
 
 // the coordinates of the call before entry t's first energy: the last entry
 // before t (in call order) with a positive geometric factor, at the last
-// energy; -inf (a fresh walk) when there is none
+// energy; -inf (a fresh walk) when there is none.  Num4D: (log T, log g, mu,
+// log10(E/E_eff)); Pol_Num2D: (mu, log10 E) in vp[0..1]
 __device__ void gen_prev_coords(const GeneralArgs &a, int64_t t, double vp[4]) {
   const int64_t per_img = (int64_t)a.S1 * a.N_P;
   int64_t u = t - 1;
@@ -394,6 +458,12 @@ __device__ void gen_prev_coords(const GeneralArgs &a, int64_t t, double vp[4]) {
   const int64_t rj = u / per_img;
   const int row = (int)(rj / a.IOmax);
   const int j = (int)((u - rj * per_img) / a.N_P);
+  if (a.atm_ext == 4) {
+    vp[0] = a.eA[u];
+    vp[1] = log10(a.energies[a.N_E - 1] / a.eZ[u]);
+    vp[2] = vp[3] = 0.0;
+    return;
+  }
   const double *vec = a.params + ((int64_t)row * a.S1 + j) * a.n_params;
   const double E_eff = (kKB / kKeV) * pow(10.0, vec[0]);
   vp[0] = vec[0];
@@ -402,14 +472,39 @@ __device__ void gen_prev_coords(const GeneralArgs &a, int64_t t, double vp[4]) {
   vp[3] = log10((a.energies[a.N_E - 1] / a.eZ[u]) / E_eff);
 }
 
+// Pol_Num2D (hot_Num2D.pyx:187-347): the cached walk on (mu, log10 E) after
+// a call at vp[2]; the stencil sum without the positive part
+__device__ double num2d_walk(const Atmos4D &A, const double *table, const double vp[2],
+                             double v0, double v1) {
+  double v[2] = {v0, v1};
+  const double *g[2] = {A.mu, A.logE};
+  const int n[2] = {A.nmu, A.nE};
+  int b[2];
+  double w[2][4];
+#pragma unroll
+  for (int d = 0; d < 2; d++) {
+    b[d] = walk_base(g[d], n[d], vp[d], v[d]);
+    lagrange4(g[d], b[d], v[d], w[d]);
+  }
+  double I = 0.0;
+  for (int i = 0; i < 4; i++) {
+    const double *r = table + (size_t)(b[0] + i) * A.nE + b[1];
+    I += w[0][i] * (w[1][0] * __ldg(r) + w[1][1] * __ldg(r + 1) + w[1][2] * __ldg(r + 2) +
+                    w[1][3] * __ldg(r + 3));
+  }
+  return I;
+}
+
 __global__ void __launch_bounds__(kGenAccThreads) general_accumulate_kernel(GeneralArgs a) {
   const int64_t ri = blockIdx.x;
   const int i = (int)(ri / a.IOmax), I = (int)(ri - (int64_t)i * a.IOmax);
   if (I >= a.n_img[i]) return;
   const int S1 = a.S1, N_P = a.N_P, N_E = a.N_E;
-  const bool num4d = a.atm_ext == 2;
+  const bool num4d = a.atm_ext == 2, burst = a.atm_ext == 3, num2d = a.atm_ext == 4;
+  const bool stokes = a.stokes != 0;
   const bool corr = a.correction != nullptr;
-  const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
+  const double norm = (num4d || num2d) ? kErg / kHKeV : kErg * kPlanck;
+  const double c2chi = stokes ? a.chi2[ri * 2] : 0.0, s2chi = stokes ? a.chi2[ri * 2 + 1] : 0.0;
   extern __shared__ double sm[];
   double *cT = sm, *cC = sm + S1;  // per cell: kT or E_eff; the correction's kT
   for (int j = threadIdx.x; j < S1; j += blockDim.x) {
@@ -426,9 +521,9 @@ __global__ void __launch_bounds__(kGenAccThreads) general_accumulate_kernel(Gene
   for (int task = threadIdx.x; task < N_P * groups; task += blockDim.x) {
     const int k = task % N_P, grp = task / N_P;
     const int p0 = grp * kGenEPT;
-    double acc[kGenEPT];
+    double acc[kGenEPT], accQ[kGenEPT], accU[kGenEPT];
 #pragma unroll
-    for (int e = 0; e < kGenEPT; e++) acc[e] = 0.0;
+    for (int e = 0; e < kGenEPT; e++) acc[e] = accQ[e] = accU[e] = 0.0;
     for (int j = 0; j < S1; j++) {
       if (rad[j] != 1) continue;
       const int64_t t = base + (int64_t)j * N_P + k;
@@ -441,8 +536,24 @@ __global__ void __launch_bounds__(kGenAccThreads) general_accumulate_kernel(Gene
         const int p = p0 + e;
         if (p >= N_E) break;
         const double Ep = a.energies[p] / Z;
-        double I_E;
-        if (num4d) {
+        double I_E, Q_E = 0.0;
+        if (num2d) {
+          const double v1 = log10(Ep);
+          double vp[4];
+          if (p > 0) {
+            vp[0] = AB;
+            vp[1] = log10(a.energies[p - 1] / Z);
+          } else {
+            const Atmos4D &T = a.atmos;
+            const bool inside = AB >= T.mu[0] && AB <= T.mu[T.nmu - 1] && v1 >= T.logE[0] &&
+                                v1 <= T.logE[T.nE - 1];
+            if (inside) vp[0] = vp[1] = 0.0;  // not read inside the table
+            else gen_prev_coords(a, t, vp);
+          }
+          I_E = num2d_walk(a.atmos, a.atmos.I, vp, AB, v1);
+          if (I_E < 0.0) I_E = 0.0;
+          if (stokes && a.table_q) Q_E = num2d_walk(a.atmos, a.table_q, vp, AB, v1);
+        } else if (num4d) {
           const double v3 = log10(Ep / cT[j]);
           double vp[4];
           if (p > 0) {
@@ -460,19 +571,33 @@ __global__ void __launch_bounds__(kGenAccThreads) general_accumulate_kernel(Gene
             else gen_prev_coords(a, t, vp);
           }
           I_E = num4d_walk(a.atmos, vp, vec[0], vec[1], AB, v3);
+        } else if (burst) {  // hot_BB_burst.pyx
+          I_E = eval_bb(Ep, cT[j]) * (0.421 + 0.868 * AB);
+          Q_E = (0.1171 * (AB - 1.) / (1. + 3.582 * AB)) * I_E;
         } else {
           I_E = eval_bb(Ep, cT[j]);
         }
         I_E = I_E * norm;
         const double c = corr ? eval_bb(Ep, cC[j]) * (kErg * kPlanck) : 0.0;
         acc[e] += A * (I_E - c) * G;
+        if (stokes) {  // integratorIQU.pyx:615-633
+          Q_E = Q_E * norm;
+          accQ[e] += A * (Q_E * c2chi) * G;
+          accU[e] += A * (Q_E * s2chi) * G;
+        }
       }
     }
-    double *part = a.partial + ri * (int64_t)N_E * N_P;
+    double *part = a.partial + ri * (int64_t)(stokes ? 3 : 1) * N_E * N_P;
 #pragma unroll
     for (int e = 0; e < kGenEPT; e++) {
       const int p = p0 + e;
-      if (p < N_E) part[(int64_t)p * N_P + k] = acc[e];
+      if (p < N_E) {
+        part[(int64_t)p * N_P + k] = acc[e];
+        if (stokes) {
+          part[(int64_t)(N_E + p) * N_P + k] = accQ[e];
+          part[(int64_t)(2 * N_E + p) * N_P + k] = accU[e];
+        }
+      }
     }
   }
 }
@@ -480,22 +605,26 @@ __global__ void __launch_bounds__(kGenAccThreads) general_accumulate_kernel(Gene
 // :600-610: the (parallel, image) partials in order, divided by E keV
 __global__ void general_reduce_kernel(GeneralArgs a) {
   const int n = a.N_E * a.N_P;
+  const int ns = a.stokes ? 3 : 1;
+  const int c = blockIdx.y;  // I, Q, U
   const int64_t n_ri = (int64_t)a.S0 * a.IOmax;
+  double *out = c == 0 ? a.flux : (c == 1 ? a.flux_q : a.flux_u);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int64_t ri = 0; ri < n_ri; ri++) {
       const int row = (int)(ri / a.IOmax), I = (int)(ri - (int64_t)row * a.IOmax);
-      if (I < a.n_img[row]) s += a.partial[ri * n + t];
+      if (I < a.n_img[row]) s += a.partial[(ri * ns + c) * n + t];
     }
     const int p = t / a.N_P;
-    a.flux[t] = s / (a.energies[p] * kKeV);
+    out[t] = s / (a.energies[p] * kKeV);
   }
 }
 
 }  // namespace
 
 size_t general_geometry_smem_bytes(int N_R, int N_L) {
-  return (size_t)(N_R + 8 * N_L + 12 * N_L) * sizeof(double) + (size_t)(2 * N_L + 4) * sizeof(int);
+  return (size_t)(N_R + 8 * N_L + 12 * N_L + 7 * N_L) * sizeof(double) +
+         (size_t)(4 * N_L + 4) * sizeof(int);
 }
 
 int launch_general(const GeneralArgs &a, cudaStream_t st) {
@@ -510,7 +639,7 @@ int launch_general(const GeneralArgs &a, cudaStream_t st) {
   general_accumulate_kernel<<<(unsigned)((int64_t)a.S0 * a.IOmax), kGenAccThreads, smem_acc,
                               st>>>(a);
   const int n = a.N_E * a.N_P;
-  general_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
+  general_reduce_kernel<<<dim3((n + 255) / 256, a.stokes ? 3 : 1), 256, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 

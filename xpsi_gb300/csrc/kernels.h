@@ -195,7 +195,8 @@ struct GeneralArgs {
   int IOmax;                  // images held per parallel in the entry scratch
   double omega, inclination;
   int image_order_limit;      // 0: ceil(maxDeflection / pi) per parallel
-  int atm_ext;                // 1 blackbody, 2 Num4D
+  int atm_ext;                // 1 blackbody, 2 Num4D, 3 burst blackbody, 4 Pol_Num2D
+  int stokes;                 // 1: also Q and U (integratorIQU.pyx)
   const int32_t *radiates;    // [S0][S1]
   const double *cellArea, *phi, *params;  // [S0][S1], [S0][S1], [S0][S1][n_params]
   int n_params;
@@ -204,11 +205,14 @@ struct GeneralArgs {
   const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;  // [S0]
   const double *deflection, *cos_alpha, *lag;                     // [S0][N_R]
   const double *energies, *leaves, *phases;
-  Atmos4D atmos;
+  Atmos4D atmos;              // Num4D table, or Pol_Num2D's I table (mu, logE, I)
+  const double *table_q;      // Pol_Num2D's Q table on the same grids (Stokes)
+  double *chi2;               // [S0][IOmax][2] cos, sin of twice the polarisation angle
   double *eG, *eZ, *eA;       // [S0][IOmax][S1][N_P] entry scratch
   int32_t *n_img;             // [S0] images evaluated per parallel
-  double *partial;            // [S0][IOmax][N_E][N_P]
+  double *partial;            // [S0][IOmax][1 or 3][N_E][N_P]
   double *flux;               // [N_E][N_P]
+  double *flux_q, *flux_u;    // [N_E][N_P] (Stokes)
   int32_t *status;            // [1], zeroed by the caller
 };
 size_t general_geometry_smem_bytes(int N_R, int N_L);
