@@ -143,7 +143,7 @@ void allocate(size_t num_cells, size_t mn, size_t mx, const Star &s, double supe
   }
   (void)super_bphi;
   super_cellArea *= integrateArea(super_lims[0], super_lims[1], s, 0, w);
-  Region gs{superColat, superRadius, holeRadius, holeAzi, holeColat};
+  Region gs = make_region(superColat, superRadius, holeRadius, holeAzi, holeColat);
   double super_area = integrateSpot(super_lims[0], super_lims[1], s, gs, w);
   auto clamp_even = [&](double v) {
     if (v < (double)mn) v = (double)mn;
@@ -177,7 +177,7 @@ void allocate(size_t num_cells, size_t mn, size_t mx, const Star &s, double supe
     cede_cellArea = 2.0 * std::asin(std::sin(cedeRadius) / std::sin(cedeColat));
   }
   cede_cellArea *= integrateArea(cede_lims[0], cede_lims[1], s, 0, w);
-  Region gc{cedeColat, cedeRadius, superRadius, superAzi, superColat};
+  Region gc = make_region(cedeColat, cedeRadius, superRadius, superAzi, superColat);
   double cede_area = integrateSpot(cede_lims[0], cede_lims[1], s, gc, w);
   if (are_equal(super_area, 0.0)) super_area = super_cellArea / 1000.0;
   if (are_equal(cede_area, 0.0)) cede_area = cede_cellArea / 1000.0;

@@ -244,15 +244,42 @@ XG_HD inline double get_interval(double a, double b, double LB, double UB) {
 
 struct Region {
   double colat, cedeRadius, superRadius, superAzi, superColat;
+  // cosines and sines of the region's angles, formed once (the ring extent
+  // at every quadrature node needs them)
+  double cos_colat, sin_colat, cos_cede, cos_sc, sin_sc, cos_sr;
 };
+XG_HD inline Region make_region(double colat, double cedeRadius, double superRadius,
+                                double superAzi, double superColat) {
+  Region g;
+  g.colat = colat;
+  g.cedeRadius = cedeRadius;
+  g.superRadius = superRadius;
+  g.superAzi = superAzi;
+  g.superColat = superColat;
+  g.cos_colat = cos(colat);
+  g.sin_colat = sin(colat);
+  g.cos_cede = cos(cedeRadius);
+  g.cos_sc = cos(superColat);
+  g.sin_sc = sin(superColat);
+  g.cos_sr = cos(superRadius);
+  return g;
+}
+// eval_phi with the trigonometric values given (the same operations)
+XG_HD inline double eval_phi_cs(double cos_theta, double sin_theta, double cos_THETA,
+                                double sin_THETA, double cos_psi) {
+  double cos_phi = cos_psi - cos_THETA * cos_theta;
+  cos_phi /= sin_THETA * sin_theta;
+  if (!(-1.0 <= cos_phi && cos_phi <= 1.0)) return -1.0;
+  return acos(cos_phi);
+}
 
 // azimuthal extent of the ceding annulus at colatitude theta restricted to
 // [phi_a, phi_b] (cell) or unrestricted (spot): mesh_tools.pyx:302-370, 775-830
-XG_HD inline double ring_extent(double theta, const Region &g, bool cell, double phi_a, double phi_b,
-                   bool &zero) {
+XG_HD inline double ring_extent(double theta, double cos_theta, double sin_theta, const Region &g,
+                                bool cell, double phi_a, double phi_b, bool &zero) {
   zero = false;
   double aLB, aUB, cLB, cUB;
-  aUB = eval_phi(theta, g.colat, g.cedeRadius);
+  aUB = eval_phi_cs(cos_theta, sin_theta, g.cos_colat, g.sin_colat, g.cos_cede);
   if (are_equal(aUB, -1.0)) {
     if (theta + g.colat < g.cedeRadius) {
       aUB = PI;
@@ -267,7 +294,7 @@ XG_HD inline double ring_extent(double theta, const Region &g, bool cell, double
   if (fabs(theta - g.superColat) > g.superRadius) {
     cLB = cUB = 0.0;
   } else {
-    cUB = eval_phi(theta, g.superColat, g.superRadius);
+    cUB = eval_phi_cs(cos_theta, sin_theta, g.cos_sc, g.sin_sc, g.cos_sr);
     if (are_equal(cUB, -1.0)) {
       zero = true;
       return 0.0;
@@ -366,13 +393,13 @@ struct CellIntegrand {
   double pa, pb;
   XG_HD double operator()(double theta) const {
     if (are_equal(theta, 0.0)) return 0.0;
-    double mu = cos(theta);
+    double mu = cos(theta), st = sin(theta);
     double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
     double ft = f_theta(mu, radius, s.epsilon, s.zeta, s.shape);
     bool zero;
-    double dphi = ring_extent(theta, g, true, pa, pb, zero);
+    double dphi = ring_extent(theta, mu, st, g, true, pa, pb, zero);
     if (zero) return 0.0;
-    return dphi * radius * radius * sqrt(1.0 + ft * ft) * sin(theta);
+    return dphi * radius * radius * sqrt(1.0 + ft * ft) * st;
   }
 };
 
@@ -427,13 +454,13 @@ template <typename W>
 XG_QD double integrateSpot(double ta, double tb, const Star &s, const Region &g, W &w) {
   auto f = [&](double theta) -> double {
     if (are_equal(theta, 0.0)) return 0.0;
-    double mu = cos(theta);
+    double mu = cos(theta), st = sin(theta);
     double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
     double ft = f_theta(mu, radius, s.epsilon, s.zeta, s.shape);
     bool zero;
-    double dphi = ring_extent(theta, g, false, 0.0, 0.0, zero);
+    double dphi = ring_extent(theta, mu, st, g, false, 0.0, 0.0, zero);
     if (zero) return 0.0;
-    return dphi * radius * radius * sqrt(1.0 + ft * ft) * sin(theta);
+    return dphi * radius * radius * sqrt(1.0 + ft * ft) * st;
   };
   return s.R_eq * s.R_eq * integrate(f, ta, tb, 0.0, 1.0e-8, w);
 }
@@ -660,7 +687,7 @@ XG_HD inline int mesh_cell_kind(const MeshPlan &pl, size_t i, size_t j, double l
 }
 
 XG_HD inline Region mesh_region(const MeshPlan &pl) {
-  return Region{pl.cedeColat, pl.cedeRadius, pl.superRadius, pl.superAzi, pl.superColat};
+  return make_region(pl.cedeColat, pl.cedeRadius, pl.superRadius, pl.superAzi, pl.superColat);
 }
 
 // area of cell (i, j)
