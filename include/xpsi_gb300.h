@@ -31,7 +31,7 @@ extern "C" {
  * 3: xgpu_atmos5d, xgpu_integrate_split and xgpu_integrate_split_stokes (split
  * atmospheres); xgpu_integrate_stokes takes the I and Q tables of atm_ext 4
  * (Pol_Num2D), which xgpu_integrate and xgpu_integrate_general also take;
- * xgpu_integrate_general_stokes. */
+ * xgpu_integrate_general_stokes; xgpu_phase_interpolator, xgpu_energy_interpolator. */
 #define XGPU_ABI_VERSION 3
 
 /* Status words of the batched layer (per parameter vector). */
@@ -75,7 +75,8 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R,
 /* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-98) for uniform
  * hot regions: beam_opt 0, no disk (R_in >= 1e6).  atm_ext 1 = blackbody,
- * 2 = Num4D (atmos required), 4 = Pol_Num2D's intensity (hot_Num2D.pyx:
+ * 2 = Num4D (atmos required), 3 = the burst blackbody's intensity
+ * (hot_BB_burst.pyx), 4 = Pol_Num2D's intensity (hot_Num2D.pyx:
  * atmos->mu, logE and intensity [nmu][nE] on (mu, log10 E/keV); the other
  * fields unused).  correction_srcCellParams[S0][S1][n_correction]
  * or NULL is the elsewhere correction (:257-261,469-478,593-594); the GPU
@@ -232,6 +233,25 @@ int xgpu_integrate_general_stokes(double R, double omega, double r_s,
                                   const xgpu_atmos4d *atmos_Q, int else_atm_ext,
                                   int image_order_limit, double *flux_I,
                                   double *flux_Q, double *flux_U);
+
+/* Replaces xpsi.tools.phase_interpolator.phase_interpolator
+ * (xpsi/tools/phase_interpolator.pyx:25-95, the default Akima-periodic
+ * interpolant): signal[rows][n_phases] on phases (cycles, [0, 1]) evaluated
+ * at new_phases + phase_shift wrapped into [0, 1); values <= 0 become 0
+ * unless allow_negative.  out[rows][n_new]. */
+int xgpu_phase_interpolator(size_t n_new, const double *new_phases, size_t n_phases,
+                            const double *phases, size_t rows, const double *signal,
+                            double phase_shift, int allow_negative, double *out);
+
+/* Replaces xpsi.tools.energy_interpolator.energy_interpolator
+ * (xpsi/tools/energy_interpolator.pyx:27-125, the default Steffen
+ * interpolant): each column of signal[N_E][n_cols] splined in log10 E (in
+ * log10 of the signal when the column is positive throughout) at
+ * log10_new_energies; 0 above the last energy.  out[n_new][n_cols], the
+ * reference's return. */
+int xgpu_energy_interpolator(size_t N_E, size_t n_cols, const double *signal,
+                             const double *log10_energies, size_t n_new,
+                             const double *log10_new_energies, double *out);
 
 /* Replaces xpsi.tools.energy_integrator.energy_integrator
  * (xpsi/tools/energy_integrator.pyx:27-31).  signal[N_E][N_P]; log10 energies

@@ -64,6 +64,11 @@ def lib():
                 C.c_size_t, P, C.c_int, P, C.c_int, P, P, P]
             L.xo_integrate_split.restype = C.c_int
             L.xo_integrate_split.argtypes = list(L.xo_integrate.argtypes)[:-6] + [P, C.c_int, P]
+            L.xo_phase_interpolator.restype = None
+            L.xo_phase_interpolator.argtypes = [C.c_size_t, P, C.c_size_t, P, C.c_size_t, P,
+                                                C.c_double, C.c_int, P]
+            L.xo_energy_interpolator.restype = None
+            L.xo_energy_interpolator.argtypes = [C.c_size_t, C.c_size_t, P, P, C.c_size_t, P, P]
             L.xo_integrate_split_iqu.restype = C.c_int
             L.xo_integrate_split_iqu.argtypes = (list(L.xo_integrate.argtypes)[:-6] +
                                                  [P, P, C.c_int, P, P, P])
@@ -528,3 +533,22 @@ def integrate_split_iqu(numThreads, R, omega, r_s, inclination, cellArea,
     if status != 0:
         return (1, None)
     return (0, out[0], out[1], out[2])
+
+
+def phase_interpolator(new_phases, phases, signal, phase_shift, allow_negative=0):
+    """tools/phase_interpolator.pyx:25-95 (Akima periodic)."""
+    nf = _c(new_phases); ph = _c(phases); sig = _c(signal)
+    out = np.zeros((sig.shape[0], nf.size))
+    lib().xo_phase_interpolator(nf.size, _p(nf), ph.size, _p(ph), sig.shape[0], _p(sig),
+                                float(phase_shift), int(bool(allow_negative)), _p(out))
+    return out
+
+
+def energy_interpolator(N_Ts, signal, energies, new_energies):
+    """tools/energy_interpolator.pyx:27-113 (Steffen); energies and
+    new_energies are log10 of the energies."""
+    sig = _c(signal); E = _c(energies); nE = _c(new_energies)
+    out = np.zeros((sig.shape[1], nE.size))
+    lib().xo_energy_interpolator(E.size, sig.shape[1], _p(sig), _p(E), nE.size, _p(nE),
+                                 _p(out))
+    return np.ascontiguousarray(out.T)  # :125, [new energies][columns]

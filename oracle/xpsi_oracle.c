@@ -27,6 +27,8 @@
  *   xo_energy_integrator     tools/energy_integrator.pyx:27-114
  *   xo_expected_counts       tools/compute_expected_counts.pyx:200-276
  *   xo_phase_integrator      tools/phase_integrator.pyx:23-121
+ *   xo_phase_interpolator    tools/phase_interpolator.pyx:25-95
+ *   xo_energy_interpolator   tools/energy_interpolator.pyx:27-113
  *   xo_precomputation        likelihoods/default_background_marginalisation.pyx:38-68
  *   xo_eval_marginal_likelihood   same file :176-734 and
  *                            tools/compute_expected_counts.pyx:66-197
@@ -1677,3 +1679,63 @@ int xo_eval_marginal_likelihood(
 
 /* ---- oracle-side exposure of the quadrature subset for tests ---- */
 double xo_lnfact(unsigned n) { return gsl_sf_lnfact(n); }
+
+/* ================================================================== */
+/* tools/phase_interpolator.pyx:25-95: each signal row's Akima-periodic */
+/* interpolant at new_phases + phase_shift (wrapped into [0, 1)), kept   */
+/* when positive unless allow_negative; out[rows][n_new]                 */
+/* ================================================================== */
+void xo_phase_interpolator(size_t n_new, const double *new_phases, size_t n_phases,
+                           const double *phases, size_t rows, const double *signal,
+                           double phase_shift, int allow_negative, double *out) {
+  gsl_interp *ip = gsl_interp_alloc(gsl_interp_akima_periodic, n_phases);
+  gsl_interp_accel *acc = gsl_interp_accel_alloc();
+  for (size_t i = 0; i < rows; i++) {
+    gsl_interp_accel_reset(acc);
+    const double *y = signal + i * n_phases;
+    gsl_interp_init(ip, phases, y, n_phases);
+    for (size_t j = 0; j < n_new; j++) {
+      double PHASE = new_phases[j] + phase_shift;
+      PHASE -= floor(PHASE);
+      const double v = gsl_interp_eval(ip, phases, y, PHASE, acc);
+      out[i * n_new + j] = (v > 0.0 || allow_negative) ? v : 0.0;
+    }
+  }
+  gsl_interp_accel_free(acc);
+  gsl_interp_free(ip);
+}
+
+/* ================================================================== */
+/* tools/energy_interpolator.pyx:27-113: each column of signal[N_E][n]  */
+/* splined (Steffen) in log10 E, in log10 of the signal when the column */
+/* is positive throughout; zero above the last energy;                  */
+/* out[n][n_new] (the reference returns its transpose, :125)           */
+/* ================================================================== */
+void xo_energy_interpolator(size_t N_E, size_t n_cols, const double *signal,
+                            const double *energies, size_t n_new, const double *new_energies,
+                            double *out) {
+  gsl_interp *ip = gsl_interp_alloc(gsl_interp_steffen, N_E);
+  gsl_interp_accel *acc = gsl_interp_accel_alloc();
+  double *cpy = (double *)malloc(N_E * sizeof(double));
+  const double max_energy = energies[N_E - 1];
+  for (size_t i = 0; i < n_cols; i++) {
+    int mode = 1;
+    for (size_t j = 0; j < N_E; j++)
+      if (signal[j * n_cols + i] <= 0.0) mode = 0;
+    for (size_t j = 0; j < N_E; j++)
+      cpy[j] = mode ? log10(signal[j * n_cols + i]) : signal[j * n_cols + i];
+    gsl_interp_accel_reset(acc);
+    gsl_interp_init(ip, energies, cpy, N_E);
+    for (size_t j = 0; j < n_new; j++) {
+      double v = 0.0;
+      if (!(new_energies[j] > max_energy)) {
+        v = gsl_interp_eval(ip, energies, cpy, new_energies[j], acc);
+        if (mode) v = pow(10.0, v);
+      }
+      out[i * n_new + j] = v;
+    }
+  }
+  free(cpy);
+  gsl_interp_accel_free(acc);
+  gsl_interp_free(ip);
+}

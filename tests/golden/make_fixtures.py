@@ -635,6 +635,38 @@ def general_iqu(xpsi):
     save("general_iqu", **out)
 
 
+def interpolators(xpsi):
+    """The phase and energy interpolators (tools/phase_interpolator.pyx,
+    tools/energy_interpolator.pyx, with the default Akima-periodic and
+    Steffen interpolants) on config1's folded signal (phases in cycles,
+    shifted; negative parts dropped or kept) and its photon flux (log10
+    energies, new energies inside and above the grid; one column made
+    non-positive so that it is splined without the logarithm)."""
+    from xpsi.tools.phase_interpolator import phase_interpolator
+    from xpsi.tools.energy_interpolator import energy_interpolator
+    f = np.load(os.path.join(HERE, "config1.npz"))
+    folded = np.ascontiguousarray(f["folded"][:60])
+    ph = np.ascontiguousarray(f["comp_phases"])
+    rng = np.random.default_rng(11)
+    new_ph = np.ascontiguousarray(np.sort(rng.uniform(-0.3, 1.3, 97)))
+    # a row with an oscillation, so that the interpolant dips below zero
+    osc = np.ascontiguousarray(np.vstack([folded, np.sin(2 * np.pi * 3 * ph[None, :]) * 0.1]))
+    out = {"phase_signal": osc, "phase_phases": ph, "phase_new": new_ph}
+    for tag, shift, neg in (("shift", 0.23, 0), ("neg", -0.41, 1)):
+        out["phase_" + tag] = phase_interpolator(new_ph, ph, osc, shift, neg)
+        out["phase_%s_shift" % tag] = np.array(shift)
+    flux = np.array(f["flux"], copy=True)
+    flux[:, 5] = flux[:, 5] - flux[:, 5].max() * 0.5  # a column with non-positive entries
+    flux = np.ascontiguousarray(flux)
+    lgE = np.ascontiguousarray(f["log10_energies"])
+    new_lgE = np.ascontiguousarray(np.linspace(lgE[0], lgE[-1] + 0.1, 150))
+    out["energy_signal"] = flux
+    out["energy_log10"] = lgE
+    out["energy_new"] = new_lgE
+    out["energy_out"] = energy_interpolator(1, flux, lgE, new_lgE)
+    save("interpolators", **out)
+
+
 def main():
     xpsi = H.load()
     examples_fast(xpsi)
@@ -650,6 +682,7 @@ def main():
     pol_num2d(xpsi)
     split_iqu(xpsi)
     general_iqu(xpsi)
+    interpolators(xpsi)
 
 
 if __name__ == "__main__":

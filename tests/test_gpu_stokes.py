@@ -65,3 +65,17 @@ def test_stokes_bitwise_reproducible(iqu, golden):
     b = iqu.integrate(*args)
     for k in range(1, 4):
         np.testing.assert_array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("case", ["config1", "num4d_omit"])
+def test_plain_integrator_burst_intensity(iqu, golden, case):
+    """The azimuthal intensity integrator with the burst blackbody (atm_ext 3)
+    against the reference Stokes integrator's I and the oracle."""
+    from xpsi_gb300.cellmesh import integrator_for_azimuthal_invariance as az
+    tag, args = stokes_args(golden, case, 3, False)
+    plain = args[:22] + (args[22],) + args[24:]
+    st, flux = az.integrate(*plain)
+    assert st == 0
+    assert row_rel(flux, golden("stokes")[tag + "_I"]) <= RTOL
+    ref = O.integrate(*plain)
+    assert ref[0] == 0 and row_rel(flux, ref[1]) <= RTOL

@@ -15,3 +15,13 @@ def test_oracle_stokes_vs_reference(golden, case, ext, corrected):
     z = golden("stokes")
     for k, s in enumerate("IQU"):
         assert row_rel(out[k + 1], z[tag + "_" + s]) <= 1e-13
+
+
+@pytest.mark.parametrize("case", ["config1", "num4d_omit"])
+def test_oracle_plain_burst_intensity_is_the_reference_stokes_i(golden, case):
+    """The azimuthal intensity integrator with the burst blackbody (atm_ext
+    3) gives the reference Stokes integrator's I."""
+    tag, args = stokes_args(golden, case, 3, False)
+    st, flux = O.integrate(*(args[:22] + (args[22],) + args[24:]))
+    assert st == 0
+    assert row_rel(flux, golden("stokes")[tag + "_I"]) <= 1e-13

@@ -16,6 +16,7 @@ hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
     xpsi_gb300.cellmesh.integrator_for_time_invariance.integrate (elsewhere)
     xpsi_gb300.tools.energy_integrator.energy_integrator
     xpsi_gb300.tools.phase_integrator.phase_integrator
+    xpsi_gb300.tools.{phase_interpolator,energy_interpolator}
     xpsi_gb300.tools.synthesise.{synthesise_exposure,
                                  synthesise_given_total_count_number}
     xpsi_gb300.likelihoods.default_background_marginalisation.{precomputation,
@@ -48,6 +49,7 @@ def install(xpsi_module):
     from .cellmesh import integratorIQU_for_azimuthal_invariance as iqu
     from .tools import energy_integrator as ei
     from .tools import phase_integrator as pint, synthesise as syn
+    from .tools import phase_interpolator as pinterp, energy_interpolator as einterp
     from .likelihoods import default_background_marginalisation as dbm
     from .likelihoods import _gaussian_likelihood_given_background_IQU as gbg
     from .likelihoods import _gaussian_likelihood_QnUn as gqu
@@ -71,6 +73,9 @@ def install(xpsi_module):
          iqu_split.integrate),
         ("xpsi.cellmesh.integratorIQU_for_azimuthal_invariance", "integrate", iqu.integrate),
         ("xpsi.tools.phase_integrator", "phase_integrator", pint.phase_integrator),
+        ("xpsi.tools.phase_interpolator", "phase_interpolator", pinterp.phase_interpolator),
+        ("xpsi.tools.energy_interpolator", "energy_interpolator",
+         einterp.energy_interpolator),
         ("xpsi.likelihoods._gaussian_likelihood_given_background_IQU",
          "gaussian_likelihood_given_background", gbg.gaussian_likelihood_given_background),
         ("xpsi.likelihoods._gaussian_likelihood_QnUn", "gaussian_likelihood_QnUn",
@@ -96,7 +101,13 @@ def install(xpsi_module):
                               ("xpsi.Elsewhere", "_compute_rays", rays.compute_rays),
                               ("xpsi.Elsewhere", "_construct_closed_cellMesh",
                                global_mesh.construct_closed_cellMesh),
-                              ("xpsi.Elsewhere", "_integrator", tinv.integrate)):
+                              ("xpsi.Elsewhere", "_integrator", tinv.integrate),
+                              ("xpsi.PostProcessing._pulse", "interp",
+                               pinterp.phase_interpolator),
+                              ("xpsi.PostProcessing._spectrum", "interp",
+                               pinterp.phase_interpolator),
+                              ("xpsi.PostProcessing._spectrum", "energy_interpolator",
+                               einterp.energy_interpolator)):
         try:
             mod = importlib.import_module(modname)
         except ImportError:

@@ -223,6 +223,8 @@ def _bind(L):
                                                     SZ, P, C.c_int, C.POINTER(Atmos4D),
                                                     C.POINTER(Atmos4D), C.c_int, C.c_int, P, P,
                                                     P]),
+        "xgpu_phase_interpolator": (C.c_int, [SZ, P, SZ, P, SZ, P, D, C.c_int, P]),
+        "xgpu_energy_interpolator": (C.c_int, [SZ, SZ, P, P, SZ, P, P]),
         "xgpu_integrate_split_stokes": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P,
                                                   P, SZ, SZ, P, P, P, P, P, SZ, P, SZ, P, SZ,
                                                   P, C.POINTER(Atmos5D), C.POINTER(Atmos5D),
@@ -268,7 +270,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_phase_integrator", "xgpu_poisson", "xgpu_expected_counts_batch",
             "xgpu_poisson_batch", "xgpu_integrate_stokes", "xgpu_gaussian_loglike",
             "xgpu_gaussian_loglike_batch", "xgpu_integrate_split",
-            "xgpu_integrate_split_stokes", "xgpu_integrate_general_stokes"]
+            "xgpu_integrate_split_stokes", "xgpu_integrate_general_stokes",
+            "xgpu_phase_interpolator", "xgpu_energy_interpolator"]
 
 
 ABI_VERSION = 3  # XGPU_ABI_VERSION of include/xpsi_gb300.h

@@ -21,8 +21,9 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     """Integrate over the image of a star on a distant observer's sky (GPU).
 
     Returns (0, flux[N_E, N_P]) or (1, None) exactly as the reference does.
-    Supported: blackbody (hot_atm_ext 1), numerical 4-D (2) and Pol_Num2D's
-    intensity table (4, hot_atmosphere = (mu, log10 E, I)) hot atmospheres
+    Supported: blackbody (hot_atm_ext 1), numerical 4-D (2), the burst
+    blackbody's intensity (3) and Pol_Num2D's intensity table (4,
+    hot_atmosphere = (mu, log10 E, I)) hot atmospheres
     with beam_opt 0 and no disk (R_in >= 1e6), with or without the
     correction for a blackbody elsewhere (else_atm_ext 1).  Other options raise NotImplementedError
     rather than silently computing something else.
@@ -39,7 +40,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     if R_in < 1e6:
         raise NotImplementedError("disk occultation is not on the GPU path")
     atm = int(hot_atm_ext)
-    if atm not in (1, 2, 4):
+    if atm not in (1, 2, 3, 4):
         raise NotImplementedError("hot atmosphere extension %d is not on the GPU path" % atm)
     A = f64(cellArea)
     S0, S1 = A.shape

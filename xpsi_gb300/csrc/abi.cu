@@ -217,7 +217,8 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
                       "integrators only");
     if (table2d && ext != 4 && ext != 6)
       return fail_msg("a 2-D table call takes atm_ext 4 or 6 only");
-    if (ext != 1 && ext != 2 && ext != 4 && ext != 6)
+    if (ext == 3 && mixed) return fail_msg("the mixed integrator takes atm_ext 1 or 2");
+    if (ext != 1 && ext != 2 && ext != 3 && ext != 4 && ext != 6)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
   }
   if (d->correction != nullptr && mixed)
@@ -551,8 +552,8 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
   if ((rc = lib_stream(&st))) return rc;
   if ((atm_ext == 2 || atm_ext == 4) && !atmos)
     return fail_msg("numerical atmospheres (atm_ext 2, 4) need the table");
-  if (atm_ext != 1 && atm_ext != 2 && atm_ext != 4)
-    return fail_msg("atm_ext must be 1 (BB), 2 (Num4D) or 4 (Pol_Num2D)");
+  if (atm_ext < 1 || atm_ext > 4)
+    return fail_msg("atm_ext must be 1 (BB), 2 (Num4D), 3 (burst BB) or 4 (Pol_Num2D)");
   xg::Atmos4D A{};
   Dev dt;
   if (atm_ext == 2 && (rc = atmos_device(atmos, st, &A))) return rc;
@@ -1280,6 +1281,49 @@ int xgpu_phase_integrator(double exposure_time, size_t n_edges, const double *ph
   xg::launch_phase_integrator(a, st);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, dout.p, rows * B * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_phase_interpolator(size_t n_new, const double *new_phases, size_t n_phases,
+                            const double *phases, size_t rows, const double *signal,
+                            double phase_shift, int allow_negative, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (rows == 0 || n_new == 0) return 0;
+  if (n_phases < 5) return fail_msg("the signal needs at least five phases (Akima spline)");
+  Dev dn, dp, ds, dout;
+  if ((rc = upload(dn, new_phases, n_new, st)) || (rc = upload(dp, phases, n_phases, st)) ||
+      (rc = upload(ds, signal, rows * n_phases, st)) || (rc = dalloc(dout, rows * n_new * 8, st)))
+    return rc;
+  xg::InterpArgs a{(int64_t)rows, (int)n_phases, (int)n_new, dp.as<double>(), dn.as<double>(),
+                   ds.as<double>(), phase_shift, allow_negative ? 1 : 0, dout.as<double>()};
+  xg::launch_phase_interpolator(a, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout.p, rows * n_new * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_energy_interpolator(size_t N_E, size_t n_cols, const double *signal,
+                             const double *log10_energies, size_t n_new,
+                             const double *log10_new_energies, double *out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (n_cols == 0 || n_new == 0) return 0;
+  if (N_E < 3) return fail_msg("at least three energies are needed (Steffen spline)");
+  Dev dE, dn, ds, dout;
+  if ((rc = upload(dE, log10_energies, N_E, st)) ||
+      (rc = upload(dn, log10_new_energies, n_new, st)) ||
+      (rc = upload(ds, signal, N_E * n_cols, st)) || (rc = dalloc(dout, n_new * n_cols * 8, st)))
+    return rc;
+  xg::InterpArgs a{(int64_t)n_cols, (int)N_E, (int)n_new, dE.as<double>(), dn.as<double>(),
+                   ds.as<double>(), 0.0, 0, dout.as<double>()};
+  xg::launch_energy_interpolator(a, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout.p, n_new * n_cols * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return 0;
 }

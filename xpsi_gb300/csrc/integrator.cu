@@ -1079,6 +1079,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                   }
                 } else {
                   I_E = eval_bb(a.energies[p] / g.Z[s], kT);
+                  // the burst blackbody's limb darkening (hot_BB_burst.pyx)
+                  if (M.atm == 3) I_E = I_E * (0.421 + 0.868 * g.ABB[s]);
                 }
                 const double I_c =
                     corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;

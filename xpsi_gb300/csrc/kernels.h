@@ -246,6 +246,20 @@ struct PhaseIntArgs {
   const double *signal_phases;  // [n_phases]
   double *out;                  // [rows][B]
 };
+// the phase (Akima periodic) and energy (Steffen) interpolators
+struct InterpArgs {
+  int64_t rows;          // signal rows (phase) or columns (energy)
+  int n;                 // grid nodes
+  int n_new;             // new abscissae
+  const double *grid;    // [n] phases in cycles, or log10 energies
+  const double *new_x;   // [n_new]
+  const double *signal;  // [rows][n] (phase) or [n][rows] (energy)
+  double shift;          // phase shift in cycles (phase)
+  int allow_negative;    // (phase)
+  double *out;           // [rows][n_new] (phase) or [n_new][rows] (energy)
+};
+void launch_phase_interpolator(const InterpArgs &a, cudaStream_t st);
+void launch_energy_interpolator(const InterpArgs &a, cudaStream_t st);
 void launch_phase_integrator(const PhaseIntArgs &a, cudaStream_t st);
 void launch_poisson(int64_t n, const double *mean, double *out, uint64_t seed, uint64_t offset,
                     int32_t *fail, cudaStream_t st);

@@ -261,6 +261,91 @@ void launch_phase_integrator(const PhaseIntArgs &a, cudaStream_t st) {
                             st>>>(a);
 }
 
+// phase_interpolator.pyx:25-95: the Akima-periodic interpolant of each row
+// at new_phases + shift wrapped into [0, 1), kept when positive unless
+// allow_negative; a warp per row, lanes over the new phases
+__global__ void __launch_bounds__(32 * kSynWarps) phase_interp_kernel(InterpArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * kSynWarps + (threadIdx.x >> 5);
+  if (row >= a.rows) return;
+  const int n = a.n;
+  const double *x = a.grid, *y = a.signal + row * n;
+  for (int j = lane; j < a.n_new; j += 32) {
+    double p = a.new_x[j] + a.shift;
+    p -= floor(p);
+    double v;
+    if (p < x[0] || p > x[n - 1]) {
+      v = nan("");  // outside the interpolant's domain
+    } else {
+      const int i = locate(x, n, p);
+      auto chord = [&](int k) -> double {
+        const int q = periodic_chord(k, n);
+        return (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
+      };
+      double k1, k2, k3;
+      akima_piece(chord(i - 2), chord(i - 1), chord(i), chord(i + 1), chord(i + 2),
+                  x[i + 1] - x[i], k1, k2, k3);
+      const double u = p - x[i];
+      v = y[i] + u * (k1 + u * (k2 + u * k3));
+    }
+    a.out[row * a.n_new + j] = (v > 0.0 || a.allow_negative) ? v : 0.0;
+  }
+}
+
+struct ColumnY {
+  const double *s;
+  int64_t stride;
+  bool lg;
+  __device__ double operator()(int k) const {
+    const double v = s[(int64_t)k * stride];
+    return lg ? log10(v) : v;
+  }
+};
+
+// energy_interpolator.pyx:27-113: each column of signal[N_E][n_cols]
+// splined (Steffen) in log10 E -- in log10 of the signal when the column is
+// positive throughout -- at the new energies, zero above the last energy;
+// out[n_new][n_cols] as the reference returns it (:125).  A warp per column.
+__global__ void __launch_bounds__(32 * kSynWarps) energy_interp_kernel(InterpArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t col = (int64_t)blockIdx.x * kSynWarps + (threadIdx.x >> 5);
+  if (col >= a.rows) return;
+  const int n = a.n;
+  const double *x = a.grid;
+  bool pos = true;
+  for (int k = lane; k < n; k += 32) pos = pos && (a.signal[(int64_t)k * a.rows + col] > 0.0);
+  const bool lg = __all_sync(0xffffffffu, pos);
+  const ColumnY Y{a.signal + col, a.rows, lg};
+  const double x_max = x[n - 1];
+  for (int j = lane; j < a.n_new; j += 32) {
+    const double e = a.new_x[j];
+    double v = 0.0;
+    if (!(e > x_max)) {
+      if (e < x[0]) {
+        v = nan("");  // below the grid: outside the interpolant's domain
+      } else {
+        const int i = locate(x, n, e);
+        const Cubic c = steffen_piece(ArrY{x}, Y, n, i);
+        v = cubic_eval(c, e);
+        if (lg) v = pow(10.0, v);
+      }
+    }
+    a.out[(int64_t)j * a.rows + col] = v;
+  }
+}
+
+void launch_phase_interpolator(const InterpArgs &a, cudaStream_t st) {
+  if (a.rows <= 0 || a.n_new <= 0) return;
+  phase_interp_kernel<<<(unsigned)((a.rows + kSynWarps - 1) / kSynWarps), 32 * kSynWarps, 0,
+                        st>>>(a);
+}
+
+void launch_energy_interpolator(const InterpArgs &a, cudaStream_t st) {
+  if (a.rows <= 0 || a.n_new <= 0) return;
+  energy_interp_kernel<<<(unsigned)((a.rows + kSynWarps - 1) / kSynWarps), 32 * kSynWarps, 0,
+                         st>>>(a);
+}
+
 void launch_poisson(int64_t n, const double *mean, double *out, uint64_t seed, uint64_t offset,
                     int32_t *fail, cudaStream_t st) {
   if (n <= 0) return;
