@@ -67,3 +67,21 @@ def test_mesh_builder_vs_reference_fixtures():
     np.testing.assert_allclose(r, f["radius"], rtol=1e-14)
     np.testing.assert_allclose(cg, f["cos_gamma"], rtol=1e-14)
     np.testing.assert_allclose(ma, f["maxAlpha_in"], rtol=1e-14)
+
+
+def test_allocate_cells_drop_in_matches_reference_types():
+    """The drop-in cell budget returns the reference's values and types."""
+    from oracle import ref_harness as H
+    if not H.available():
+        import pytest
+        pytest.skip("reference checkout not present")
+    H.load()
+    import xpsi.cellmesh.mesh_tools as MT
+    from xpsi_gb300.cellmesh import mesh as M
+    for cede in (0.0, 0.35):
+        args = (400, 10, 40, 2.8e30, 4136.0, 12000.0, 2 * 3.14159 * 300, 0.2, 0.05, 0, 0.3,
+                cede, 1.2, 1.25, 0.0, 0.0, 0.0, 0.0)
+        ref = MT.allocate_cells(*args)
+        ours = M.allocate_cells(*args)
+        assert ours == ref
+        assert [type(x) for x in ours] == [type(x) for x in ref]

@@ -28,6 +28,11 @@ def test_install_rebinds_path_callables():
     assert S._synthesise_expo is synthesise.synthesise_exposure
     assert S._synthesise_given_total_count_number is synthesise.synthesise_given_total_count_number
     assert importlib.import_module("xpsi.HotRegion")._compute_rays is rays.compute_rays
+    from xpsi_gb300.cellmesh import mesh as hot_mesh
+    HRm = importlib.import_module("xpsi.HotRegion")
+    assert HRm._allocate_cells is hot_mesh.allocate_cells
+    assert HRm._construct_spot_cellMesh is hot_mesh.construct_spot_cellMesh
+    assert HRm._construct_polar_cellMesh is hot_mesh.construct_polar_cellMesh
     # the symmetry setter picks the GPU integrators
     HR = importlib.import_module("xpsi.HotRegion").HotRegion
     hr = object.__new__(HR)

@@ -5,6 +5,8 @@ Drop-in replacements for the native callables on X-PSI's likelihood path
 hand-written sm_103a CUDA kernels behind the C ABI in include/xpsi_gb300.h:
 
     xpsi_gb300.cellmesh.rays.compute_rays
+    xpsi_gb300.cellmesh.mesh.{construct_spot_cellMesh, construct_polar_cellMesh,
+                              allocate_cells}         (host C++, threaded)
     xpsi_gb300.cellmesh.integrator_for_azimuthal_invariance.integrate
     xpsi_gb300.cellmesh.integrator.integrate          (HotRegion symmetry=False)
     xpsi_gb300.cellmesh.integratorIQU.integrate       (the same, Stokes)
@@ -42,6 +44,7 @@ def install(xpsi_module):
     import importlib
     from .cellmesh import rays, integrator_for_azimuthal_invariance as integ
     from .cellmesh import global_mesh, integrator_for_time_invariance as tinv
+    from .cellmesh import mesh as hot_mesh
     from .cellmesh import integrator as general
     from .cellmesh import integratorIQU as general_iqu
     from .cellmesh import integrator_for_azimuthal_invariance_split as split
@@ -56,6 +59,10 @@ def install(xpsi_module):
     done = []
     targets = [
         ("xpsi.cellmesh.rays", "compute_rays", rays.compute_rays),
+        ("xpsi.cellmesh.mesh_tools", "allocate_cells", hot_mesh.allocate_cells),
+        ("xpsi.cellmesh.mesh", "construct_spot_cellMesh", hot_mesh.construct_spot_cellMesh),
+        ("xpsi.cellmesh.polar_mesh", "construct_polar_cellMesh",
+         hot_mesh.construct_polar_cellMesh),
         ("xpsi.cellmesh.integrator_for_azimuthal_invariance", "integrate", integ.integrate),
         ("xpsi.tools.energy_integrator", "energy_integrator", ei.energy_integrator),
         ("xpsi.likelihoods.default_background_marginalisation", "eval_marginal_likelihood",
@@ -93,6 +100,11 @@ def install(xpsi_module):
         done.append(modname + "." + attr)
     # names bound at import time by the model classes
     for modname, attr, fn in (("xpsi.HotRegion", "_compute_rays", rays.compute_rays),
+                              ("xpsi.HotRegion", "_allocate_cells", hot_mesh.allocate_cells),
+                              ("xpsi.HotRegion", "_construct_spot_cellMesh",
+                               hot_mesh.construct_spot_cellMesh),
+                              ("xpsi.HotRegion", "_construct_polar_cellMesh",
+                               hot_mesh.construct_polar_cellMesh),
                               ("xpsi.Signal", "energy_integrator", ei.energy_integrator),
                               ("xpsi.Signal", "phase_integrator", pint.phase_integrator),
                               ("xpsi.Signal", "_synthesise_expo", syn.synthesise_exposure),

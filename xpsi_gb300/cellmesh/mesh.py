@@ -13,7 +13,9 @@ from .._native import MeshRequest, check, lib
 def allocate_cells(num_cells, min_sqrt_num_cells, max_sqrt_num_cells, mass, r_s, R_eq, Omega,
                    zeta, epsilon, star_shape_ind, superRadius, cedeRadius, superColatitude,
                    cedeColatitude, superAzimuth, holeColatitude, holeRadius, holeAzimuth):
-    """Cell budget per member: (super_sqrt, super_num, cede_sqrt, cede_num)."""
+    """Cell budget per member: (super_sqrt, super_num, cede_sqrt, cede_num), with
+    the reference's types (floats; integer zeros for the ceding region when
+    there is none, mesh_tools.pyx:985-1004)."""
     out = np.zeros(4)
     check(lib().xgpu_allocate_cells(int(num_cells), int(min_sqrt_num_cells),
                                     int(max_sqrt_num_cells), float(R_eq), float(Omega),
@@ -22,7 +24,9 @@ def allocate_cells(num_cells, min_sqrt_num_cells, max_sqrt_num_cells, mass, r_s,
                                     float(superColatitude), float(cedeColatitude),
                                     float(superAzimuth), float(holeColatitude),
                                     float(holeRadius), float(holeAzimuth), ptr(out)))
-    return (out[0], out[1], out[2], out[3])
+    if abs(float(cedeRadius)) < 1.0e-12:
+        return (float(out[0]), float(out[1]), 0, 0)
+    return (float(out[0]), float(out[1]), float(out[2]), float(out[3]))
 
 
 def _mesh(polar, numThreads, numCell, sqrt_numCell, mass, r_s, R_eq, zeta, epsilon,
