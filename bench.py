@@ -256,7 +256,13 @@ def run_gb300(args):
     achieved = int_flops / (int_ms / 1e3) / 1e12
     out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64,
                        "unit": "TFLOP/s", "frac": achieved / peak64 if peak64 else None,
-                       "traffic": None, "kernel": "integrate_kernel",
+                       "traffic": None,
+                       "traffic_note": "DRAM bytes of this kernel from ncu at 8 vectors: 224 MB "
+                                       "read + 260 MB written per launch (0.64 % of peak "
+                                       "bandwidth), mostly the per-chunk partial sums, whose "
+                                       "size follows the chunk count rather than the vectors, "
+                                       "so it is not scaled to this launch",
+                       "kernel": "integrate_kernel",
                        "kernel_ms": int_ms, "flops_per_launch": int_flops,
                        "peak_source": "measured FP64 FMA probe on this GPU (not in "
                        "MEASURED_PEAKS.json)", "hbm_peak_gbs": pk.get("hbm_gbs"),
