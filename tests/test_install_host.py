@@ -62,3 +62,25 @@ def test_install_binds_split_integrator():
     if "xpsi.cellmesh.integrator_for_azimuthal_invariance_split.integrate" in done:
         mod = importlib.import_module("xpsi.cellmesh.integrator_for_azimuthal_invariance_split")
         assert mod.integrate is split.integrate
+
+
+def test_drop_ins_refuse_other_interpolants():
+    """X-PSI's global interpolant settings (tools/core.pyx) other than the
+    defaults are refused, not silently replaced by the defaults."""
+    import numpy as np
+    H.load()
+    import xpsi.tools.core as core
+    from xpsi_gb300.tools import energy_interpolator, phase_interpolator
+    try:
+        core.set_phase_interpolant("Steffen")
+        with pytest.raises(NotImplementedError):
+            phase_interpolator.phase_interpolator(np.zeros(3), np.linspace(0, 1, 8),
+                                                  np.zeros((2, 8)), 0.0)
+        core.set_phase_interpolant("Akima")
+        core.set_energy_interpolant("Cubic")
+        with pytest.raises(NotImplementedError):
+            energy_interpolator.energy_interpolator(1, np.ones((5, 3)), np.arange(5.0),
+                                                    np.arange(2.0))
+    finally:
+        core.set_phase_interpolant("Akima")
+        core.set_energy_interpolant("Steffen")

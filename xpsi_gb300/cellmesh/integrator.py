@@ -7,6 +7,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import Atmos4D, check, lib
 from ._tables import table2d
 
@@ -30,6 +31,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     factor is splined in phase with the Akima periodic interpolant (the
     reference's default).  Other options raise NotImplementedError.
     """
+    require_default_interpolants(phase=True, energy=False)
     corr = None
     A = f64(cellArea)
     S0, S1 = A.shape

@@ -7,6 +7,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import Atmos4D, check, lib
 from ._tables import same_grids, table2d
 
@@ -29,6 +30,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     image), from the leaf loop's last values (:593-596).  beam_opt 0, no
     disk, and the correction for a blackbody elsewhere; other options raise
     NotImplementedError."""
+    require_default_interpolants(phase=True, energy=False)
     ext = int(hot_atm_ext)
     if int(beam_opt) != 0:
         raise NotImplementedError("beaming options 1-3 are not on the GPU path")

@@ -6,6 +6,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 from . import integrator_for_azimuthal_invariance as _az
 from ._tables import same_grids, table2d
@@ -28,6 +29,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     table (2), for which the reference's Q is zero and I is the azimuthal
     integrator's.  beam_opt 0, no disk, and the correction for a blackbody
     elsewhere; other options raise NotImplementedError."""
+    require_default_interpolants(phase=True, energy=False)
     ext = int(hot_atm_ext)
     if int(beam_opt) != 0:
         raise NotImplementedError("beaming options 1-3 are not on the GPU path")

@@ -5,6 +5,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import Atmos4D, check, lib
 from ._tables import table2d
 
@@ -28,6 +29,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     correction for a blackbody elsewhere (else_atm_ext 1).  Other options raise NotImplementedError
     rather than silently computing something else.
     """
+    require_default_interpolants(phase=True, energy=False)
     corr = None
     if correction_srcCellParams is not None:
         if int(else_atm_ext) != 1:

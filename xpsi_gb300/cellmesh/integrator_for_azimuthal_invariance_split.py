@@ -7,6 +7,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 from ._tables import table5d
 
@@ -31,6 +32,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     correction for a blackbody elsewhere (else_atm_ext 1); other options
     raise NotImplementedError.
     """
+    require_default_interpolants(phase=True, energy=False)
     corr = None
     if correction_srcCellParams is not None:
         if int(else_atm_ext) != 1:

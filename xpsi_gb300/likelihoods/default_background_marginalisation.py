@@ -5,6 +5,7 @@ import ctypes as C
 import numpy as np
 
 from .._arr import f64, i32, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 
 XGPU_SLIM_CUT = 5
@@ -31,6 +32,7 @@ def eval_marginal_likelihood(exposure_time, phases, counts, components, componen
     (slim cut, vanished integral) so does this, drawn from a hash of the
     channel index instead of numpy's global generator.
     """
+    require_default_interpolants(phase=True, energy=False)
     ph = f64(phases)
     cnt = f64(counts)
     comps = [f64(c) for c in components]

@@ -2,6 +2,7 @@
 import numpy as np
 
 from .._arr import f64, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 
 
@@ -11,6 +12,7 @@ def energy_integrator(N_Ts, signal, energies, energy_edges):
     signal[N_E, N_P] (energy increases with row), log10 energies and log10
     interval edges; returns [len(edges)-1, N_P] like the reference.
     """
+    require_default_interpolants(phase=True, energy=False)
     S = f64(signal)
     E = f64(energies)
     ed = f64(energy_edges)

@@ -3,6 +3,7 @@
 import numpy as np
 
 from .._arr import f64, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 
 
@@ -11,6 +12,7 @@ def energy_interpolator(N_Ts, signal, energies, new_energies):
     columns] splined (Steffen) in log10 E -- in log10 of the signal when the
     column is positive throughout -- at `new_energies` (log10); zero above
     the last energy.  N_Ts (the reference's thread count) is not used."""
+    require_default_interpolants(phase=False, energy=True)
     S = f64(signal)
     E = f64(energies)
     nE = f64(new_energies)

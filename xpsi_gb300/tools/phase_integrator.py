@@ -3,6 +3,7 @@
 import numpy as np
 
 from .._arr import f64, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 
 
@@ -10,6 +11,7 @@ def phase_integrator(exposure_time, phases, signal, signal_phases, phase_shift,
                      allow_negative=0):
     """[rows, len(phases) - 1]: each row of `signal` integrated over the
     phase-shifted intervals (Akima periodic), times the exposure time."""
+    require_default_interpolants(phase=True, energy=False)
     ph = f64(phases)
     S = f64(signal)
     sp = f64(signal_phases)

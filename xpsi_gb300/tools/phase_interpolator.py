@@ -3,6 +3,7 @@
 import numpy as np
 
 from .._arr import f64, ptr
+from .._interp import require_default_interpolants
 from .._native import check, lib
 
 
@@ -10,6 +11,7 @@ def phase_interpolator(new_phases, phases, signal, phase_shift, allow_negative=0
     """[rows, len(new_phases)]: each row of `signal` (Akima periodic on
     `phases`, cycles in [0, 1]) at new_phases + phase_shift wrapped into
     [0, 1); values <= 0 are 0 unless allow_negative."""
+    require_default_interpolants(phase=True, energy=False)
     nf = f64(new_phases)
     ph = f64(phases)
     S = f64(signal)

@@ -10,6 +10,7 @@ import time
 import numpy as np
 
 from .._arr import f64, ptr
+from .._interp import require_default_interpolants
 from .._native import Component, check, lib
 
 
@@ -26,6 +27,7 @@ def compute_expected_counts(exposure_time, phases, components, component_phases,
                             phase_shifts, background, allow_negative=False):
     """[K, B] expected counts: exposure x (the components' bin-integrated
     count rates, clamped at zero, + the background count rates [K, B])."""
+    require_default_interpolants(phase=True, energy=False)
     ph = f64(phases)
     comps = [f64(c) for c in components]
     cph = [f64(c) for c in component_phases]
