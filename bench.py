@@ -262,6 +262,9 @@ def run_gb300(args):
                                        "bandwidth), mostly the per-chunk partial sums, whose "
                                        "size follows the chunk count rather than the vectors, "
                                        "so it is not scaled to this launch",
+                       "pipes_ncu": {"fp64_pipe_active": 0.620, "fma_pipe_active": 0.273,
+                                     "issue_active": 0.407, "source": "ncu --set full of this "
+                                     "kernel at 8 vectors (profiles/)"},
                        "kernel": "integrate_kernel",
                        "kernel_ms": int_ms, "flops_per_launch": int_flops,
                        "peak_source": "measured FP64 FMA probe on this GPU (not in "
