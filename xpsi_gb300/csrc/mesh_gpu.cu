@@ -106,19 +106,28 @@ __global__ void __launch_bounds__(128) mesh_rows_kernel(const MeshJob *jobs, con
 }
 
 // ---------------------------------------------------------------------------
-// Warp-cooperative form of the quadrature of mesh_math.h (qag21, dyadic,
-// integrate): lane l evaluates node l and node l + 32 of the step's one or
-// two 21-point panels; sums are xor-butterfly reductions, identical in every
-// lane, so the control flow is warp-uniform.
+// Group-cooperative form of the quadrature of mesh_math.h (qag21, dyadic,
+// integrate): a group of kGrp = 16 lanes (half a warp) integrates one cell.
+// Lane l of the group evaluates nodes l, l + 16 and l + 32 of the step's one
+// or two 21-point panels, so the 42 nodes of a bisection step take three
+// passes (88 % of the lane slots; one cell per warp took two passes of 32,
+// 66 %).  Sums are xor-butterfly reductions within the group, identical in
+// each of its lanes, so the control flow is group-uniform; the two groups of
+// a warp run independently (group masks on every shuffle and sync).
 // ---------------------------------------------------------------------------
+constexpr int kGrp = 16;
 constexpr int kWarpList = 128;
 struct WarpList {
   double al[kWarpList], bl[kWarpList], rl[kWarpList], el[kWarpList];
 };
+struct Grp {
+  int l;          // lane within the group
+  unsigned mask;  // the group's lanes
+};
 
-__device__ __forceinline__ double wsum(double v) {
+__device__ __forceinline__ double gsum(const Grp &g, double v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = kGrp / 2; o > 0; o >>= 1) v += __shfl_xor_sync(g.mask, v, o);
   return v;
 }
 
@@ -154,56 +163,62 @@ __device__ __forceinline__ WPanel k21_finish(double rk, double rg, double ra, do
 }
 
 template <typename F>
-__device__ void warp_k21(const F &f, int lane, double a1, double b1, double a2, double b2,
-                         bool two, WPanel &P1, WPanel &P2) {
+__device__ void grp_k21(const F &f, const Grp &g, double a1, double b1, double a2, double b2,
+                        bool two, WPanel &P1, WPanel &P2) {
   const int total = two ? 42 : 21;
-  double f0 = 0.0, f1 = 0.0;
-  if (lane < total) f0 = f(lane < 21 ? k21_node(a1, b1, lane) : k21_node(a2, b2, lane - 21));
-  if (lane + 32 < total) f1 = f(k21_node(a2, b2, lane + 32 - 21));
+  double fv[3];
   double rk1 = 0.0, rg1 = 0.0, ra1 = 0.0, rk2 = 0.0, rg2 = 0.0, ra2 = 0.0;
-  if (lane < total) {
-    const int s = k21_slot(lane < 21 ? lane : lane - 21);
-    const double wk = XG_K21_WK[s], wg = XG_K21_WG[s];
-    if (lane < 21) { rk1 = wk * f0; rg1 = wg * f0; ra1 = wk * fabs(f0); }
-    else { rk2 = wk * f0; rg2 = wg * f0; ra2 = wk * fabs(f0); }
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const int n = g.l + p * kGrp;
+    fv[p] = 0.0;
+    if (n < total) {
+      const bool first = n < 21;
+      const int m = first ? n : n - 21;
+      const double v = f(first ? k21_node(a1, b1, m) : k21_node(a2, b2, m));
+      fv[p] = v;
+      const int s = k21_slot(m);
+      const double wk = XG_K21_WK[s], wg = XG_K21_WG[s];
+      if (first) { rk1 += wk * v; rg1 += wg * v; ra1 += wk * fabs(v); }
+      else { rk2 += wk * v; rg2 += wg * v; ra2 += wk * fabs(v); }
+    }
   }
-  if (lane + 32 < total) {
-    const int s = k21_slot(lane + 32 - 21);
-    rk2 += XG_K21_WK[s] * f1; rg2 += XG_K21_WG[s] * f1; ra2 += XG_K21_WK[s] * fabs(f1);
-  }
-  rk1 = wsum(rk1); rg1 = wsum(rg1); ra1 = wsum(ra1);
-  if (two) { rk2 = wsum(rk2); rg2 = wsum(rg2); ra2 = wsum(ra2); }
+  rk1 = gsum(g, rk1); rg1 = gsum(g, rg1); ra1 = gsum(g, ra1);
+  if (two) { rk2 = gsum(g, rk2); rg2 = gsum(g, rg2); ra2 = gsum(g, ra2); }
   const double mean1 = 0.5 * rk1, mean2 = 0.5 * rk2;
   double rc1 = 0.0, rc2 = 0.0;
-  if (lane < total) {
-    if (lane < 21) rc1 = XG_K21_WK[k21_slot(lane)] * fabs(f0 - mean1);
-    else rc2 = XG_K21_WK[k21_slot(lane - 21)] * fabs(f0 - mean2);
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const int n = g.l + p * kGrp;
+    if (n < total) {
+      if (n < 21) rc1 += XG_K21_WK[k21_slot(n)] * fabs(fv[p] - mean1);
+      else rc2 += XG_K21_WK[k21_slot(n - 21)] * fabs(fv[p] - mean2);
+    }
   }
-  if (lane + 32 < total) rc2 += XG_K21_WK[k21_slot(lane + 32 - 21)] * fabs(f1 - mean2);
-  P1 = k21_finish(rk1, rg1, ra1, wsum(rc1), a1, b1);
-  if (two) P2 = k21_finish(rk2, rg2, ra2, wsum(rc2), a2, b2);
+  P1 = k21_finish(rk1, rg1, ra1, gsum(g, rc1), a1, b1);
+  if (two) P2 = k21_finish(rk2, rg2, ra2, gsum(g, rc2), a2, b2);
 }
 
 template <typename F>
-__device__ double warp_qag21(const F &f, double a, double b, double epsabs, double er,
-                             WarpList &L, int lane) {
+__device__ double grp_qag21(const F &f, double a, double b, double epsabs, double er,
+                            WarpList &L, const Grp &g) {
   const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
   WPanel P0, Pu;
-  warp_k21(f, lane, a, b, 0.0, 0.0, false, P0, Pu);
+  grp_k21(f, g, a, b, 0.0, 0.0, false, P0, Pu);
   const double r0 = P0.res, e0 = P0.err;
   double tol = (epsabs < er * fabs(r0)) ? er * fabs(r0) : epsabs;
   if ((e0 <= 50.0 * eps * P0.rabs && e0 > tol) || (e0 <= tol && e0 != P0.rasc) || e0 == 0.0)
     return r0;
-  __syncwarp();
-  if (lane == 0) { L.al[0] = a; L.bl[0] = b; L.rl[0] = r0; L.el[0] = e0; }
-  __syncwarp();
+  __syncwarp(g.mask);
+  if (g.l == 0) { L.al[0] = a; L.bl[0] = b; L.rl[0] = r0; L.el[0] = e0; }
+  __syncwarp(g.mask);
   int size = 1, iter = 1, k = 0, rnd1 = 0, rnd2 = 0, fail = 0;
   double area = r0, errsum = e0;
   do {
     const double ai = L.al[k], bi = L.bl[k], ri = L.rl[k], ei = L.el[k];
     const double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
     WPanel P1, P2;
-    warp_k21(f, lane, a1, b1, a2, b2, true, P1, P2);
+    grp_k21(f, g, a1, b1, a2, b2, true, P1, P2);
     const double r1 = P1.res, e1 = P1.err, r2 = P2.res, e2 = P2.err;
     const double r12 = r1 + r2, e12 = e1 + e2;
     errsum += e12 - ei;
@@ -219,8 +234,8 @@ __device__ double warp_qag21(const F &f, double a, double b, double epsabs, doub
       if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
     }
     const int nw = size++;
-    __syncwarp();
-    if (lane == 0) {
+    __syncwarp(g.mask);
+    if (g.l == 0) {
       if (e2 > e1) {
         L.al[k] = a2; L.bl[k] = b2; L.rl[k] = r2; L.el[k] = e2;
         L.al[nw] = a1; L.bl[nw] = b1; L.rl[nw] = r1; L.el[nw] = e1;
@@ -229,7 +244,7 @@ __device__ double warp_qag21(const F &f, double a, double b, double epsabs, doub
         L.al[nw] = a2; L.bl[nw] = b2; L.rl[nw] = r2; L.el[nw] = e2;
       }
     }
-    __syncwarp();
+    __syncwarp(g.mask);
     k = 0;
     for (int i = 1; i < size; i++)
       if (L.el[i] > L.el[k]) k = i;
@@ -237,13 +252,13 @@ __device__ double warp_qag21(const F &f, double a, double b, double epsabs, doub
   } while (iter < kWarpList && !fail && errsum > tol);
   double sum = 0.0;
   for (int i = 0; i < size; i++) sum += L.rl[i];
-  __syncwarp();
+  __syncwarp(g.mask);
   return sum;
 }
 
 template <typename F>
-__device__ double warp_dyadic(const F &f, double lo, double hi, bool toward_lo, double er,
-                              WarpList &L, int lane) {
+__device__ double grp_dyadic(const F &f, double lo, double hi, bool toward_lo, double er,
+                             WarpList &L, const Grp &g) {
   const double Lw = hi - lo;
   double sum = 0.0;
   int seen = 0, quiet = 0;
@@ -252,7 +267,7 @@ __device__ double warp_dyadic(const F &f, double lo, double hi, bool toward_lo, 
     const double p0 = toward_lo ? lo + s1 : hi - s0;
     const double p1 = toward_lo ? lo + s0 : hi - s1;
     if (!(p0 < p1) || (toward_lo ? p0 <= lo : p1 >= hi)) break;
-    const double r = warp_qag21(f, p0, p1, 0.0, er, L, lane);
+    const double r = grp_qag21(f, p0, p1, 0.0, er, L, g);
     sum += r;
     if (r != 0.0) seen = 1;
     if (seen && fabs(r) <= 1.0e-17 * fabs(sum)) {
@@ -265,22 +280,22 @@ __device__ double warp_dyadic(const F &f, double lo, double hi, bool toward_lo, 
 }
 
 template <typename F>
-__device__ double warp_integrate(const F &f, double a, double b, double epsabs, double epsrel,
-                                 WarpList &L, int lane) {
+__device__ double grp_integrate(const F &f, double a, double b, double epsabs, double epsrel,
+                                WarpList &L, const Grp &g) {
   double sign = 1.0;
   if (b < a) { const double t = a; a = b; b = t; sign = -1.0; }
   if (a == b) return 0.0;
   double er = (1.0e-13 < epsrel) ? 1.0e-13 : epsrel;
   if (epsabs <= 0.0 && er < 50.0 * 2.220446049250313e-16) er = 50.0 * 2.220446049250313e-16;
-  double r = warp_qag21(f, a, b, epsabs, er, L, lane);
+  double r = grp_qag21(f, a, b, epsabs, er, L, g);
   if (r == 0.0) {
     const double fa = f(a), fb = f(b);
     if (fa != 0.0 || fb != 0.0) {
       const double m = 0.5 * (a + b);
-      const double rl = fa != 0.0 ? warp_dyadic(f, a, m, true, er, L, lane)
-                                  : warp_qag21(f, a, m, 0.0, er, L, lane);
-      const double rr = fb != 0.0 ? warp_dyadic(f, m, b, false, er, L, lane)
-                                  : warp_qag21(f, m, b, 0.0, er, L, lane);
+      const double rl = fa != 0.0 ? grp_dyadic(f, a, m, true, er, L, g)
+                                  : grp_qag21(f, a, m, 0.0, er, L, g);
+      const double rr = fb != 0.0 ? grp_dyadic(f, m, b, false, er, L, g)
+                                  : grp_qag21(f, m, b, 0.0, er, L, g);
       r = rl + rr;
     }
   }
@@ -343,17 +358,20 @@ __global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, in
   }
 }
 
-// one warp per queued cell: the area quadrature of a cell cut by a boundary
+// one group of 16 lanes per queued cell: the area quadrature of a cell cut
+// by a boundary
 constexpr int kBoundaryWarps = 4;
 __global__ void __launch_bounds__(32 * kBoundaryWarps) mesh_boundary_kernel(
     const MeshJob *jobs, int n_mesh, xgpu_mesh_batch_out o, const double *row_tmp,
     const int64_t *queue, const unsigned *n_queue) {
-  __shared__ WarpList lists[kBoundaryWarps];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  WarpList &L = lists[wid];
+  __shared__ WarpList lists[2 * kBoundaryWarps];
+  const int lane = threadIdx.x & 31, half = lane / kGrp;
+  const int grp = (threadIdx.x >> 5) * 2 + half;
+  const Grp gp{lane - half * kGrp, 0xFFFFu << (kGrp * half)};
+  WarpList &L = lists[grp];
   const unsigned n = *n_queue;
-  const unsigned stride = gridDim.x * kBoundaryWarps;
-  for (unsigned q = blockIdx.x * kBoundaryWarps + wid; q < n; q += stride) {
+  const unsigned stride = gridDim.x * kBoundaryWarps * 2;
+  for (unsigned q = blockIdx.x * kBoundaryWarps * 2 + grp; q < n; q += stride) {
     const int64_t c = queue[q];
     const int m = mesh_of_cell(jobs, n_mesh, c);
     const MeshJob &J = jobs[m];
@@ -366,14 +384,14 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps) mesh_boundary_kernel(
     mesh_cell_kind(J.pl, i, j, lower, upper, row_tmp[4 * row + 2], pa, pb);
     const Region g = mesh_region(J.pl);
     const CellIntegrand f{J.s, g, pa, pb};
-    double integral = warp_integrate(f, lower, upper, 0.0, 1.0e-8, L, lane);
+    double integral = grp_integrate(f, lower, upper, 0.0, 1.0e-8, L, gp);
     if (are_equal(integral, 0.0)) {
       double tmin, tmax;
       if (cell_fallback_interval(lower, upper, pa, pb, g, tmin, tmax))
-        integral = warp_integrate(f, tmin, tmax, 0.0, 1.0e-8, L, lane);
+        integral = grp_integrate(f, tmin, tmax, 0.0, 1.0e-8, L, gp);
     }
-    if (lane == 0) put_area(J, o, c, i, j, J.s.R_eq * J.s.R_eq * integral);
-    __syncwarp();
+    if (gp.l == 0) put_area(J, o, c, i, j, J.s.R_eq * J.s.R_eq * integral);
+    __syncwarp(gp.mask);
   }
 }
 
