@@ -64,6 +64,8 @@ def lib():
                 C.c_size_t, P, C.c_int, P, C.c_int, P, P, P]
             L.xo_integrate_split.restype = C.c_int
             L.xo_integrate_split.argtypes = list(L.xo_integrate.argtypes)[:-6] + [P, C.c_int, P]
+            L.xo_pol_angle.restype = C.c_double
+            L.xo_pol_angle.argtypes = [C.c_double] * 17
             L.xo_phase_interpolator.restype = None
             L.xo_phase_interpolator.argtypes = [C.c_size_t, P, C.c_size_t, P, C.c_size_t, P,
                                                 C.c_double, C.c_int, P]
@@ -552,3 +554,8 @@ def energy_interpolator(N_Ts, signal, energies, new_energies):
     lib().xo_energy_interpolator(E.size, sig.shape[1], _p(sig), _p(E), nE.size, _p(nE),
                                  _p(out))
     return np.ascontiguousarray(out.T)  # :125, [new energies][columns]
+
+
+def pol_angle(*args):
+    """cellmesh/common_functions.pyx:7-66, compute_pol_ang (17 arguments)."""
+    return lib().xo_pol_angle(*[float(a) for a in args])

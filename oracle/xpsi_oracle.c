@@ -1739,3 +1739,13 @@ void xo_energy_interpolator(size_t N_E, size_t n_cols, const double *signal,
   gsl_interp_accel_free(acc);
   gsl_interp_free(ip);
 }
+
+/* cellmesh/common_functions.pyx:7-66 (compute_pol_ang), exported for the
+ * unit tests that mirror xpsi/tests/test_cellmesh.py */
+double xo_pol_angle(double leaf, double sin_psi, double cos_psi, double sin_alpha,
+                    double cos_alpha, double sin_th, double cos_th, double sin_i, double cos_i,
+                    double sin_gamma, double cos_gamma, double Grav_z, double mu, double eta,
+                    double beta, double Lorentz, double cos_xi) {
+  return pol_angle(leaf, sin_psi, cos_psi, sin_alpha, cos_alpha, sin_th, cos_th, sin_i, cos_i,
+                   sin_gamma, cos_gamma, Grav_z, mu, eta, beta, Lorentz, cos_xi);
+}
