@@ -208,7 +208,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for ll, stx in ev.loglikelihood_pipelined([params] * e2e_steps, depth=3):
+    for ll, stx in ev.loglikelihood_pipelined([params] * e2e_steps, depth=args.e2e_depth):
         pass
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
@@ -579,6 +579,8 @@ def main():
     # comma-separated subset of mixed,drop_in,serving,cpu (or "all", "none"):
     # the legs run after the timed plain-path steps
     ap.add_argument("--legs", default="all")
+    ap.add_argument("--e2e-depth", type=int, default=3,
+                    help="batches in flight in the end-to-end leg")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--drop-in-vectors", type=int, default=8)
     # the stream's shape (Poisson arrivals, log-uniform batch sizes, even
