@@ -295,24 +295,32 @@ def run_gb300(args):
         print(json.dumps(out))
 
 
-def fp64_peak(device):
+def pipe_peak(fp64):
+    """FMA throughput of the FP64 (fp64=1) or FP32 (fp64=0) pipe on this GPU:
+    8 independent FMA chains per thread, 8 CTAs of 256 threads per SM, best
+    of three timed launches (CUDA events), TFLOP/s."""
     import torch
     from xpsi_gb300._native import lib
     buf = torch.zeros(1, dtype=torch.float64, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
     L = lib()
-    L.xgpu_peak_probe(1, 152 * 8, 256, 64, buf.data_ptr(), st)
+    iters = 4096 if fp64 else 65536
+    L.xgpu_peak_probe(fp64, 152 * 8, 256, 64, buf.data_ptr(), st)
     torch.cuda.synchronize()
     best = 0.0
     for _ in range(3):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        fl = L.xgpu_peak_probe(1, 152 * 8, 256, 4096, buf.data_ptr(), st)
+        fl = L.xgpu_peak_probe(fp64, 152 * 8, 256, iters, buf.data_ptr(), st)
         e1.record()
         torch.cuda.synchronize()
         best = max(best, fl / (e0.elapsed_time(e1) / 1e3) / 1e12)
     return best
+
+
+def fp64_peak(device):
+    return pipe_peak(1)
 
 
 

@@ -31,8 +31,9 @@ extern "C" {
  * 3: xgpu_atmos5d, xgpu_integrate_split and xgpu_integrate_split_stokes (split
  * atmospheres); xgpu_integrate_stokes takes the I and Q tables of atm_ext 4
  * (Pol_Num2D), which xgpu_integrate and xgpu_integrate_general also take;
- * xgpu_integrate_general_stokes; xgpu_phase_interpolator, xgpu_energy_interpolator. */
-#define XGPU_ABI_VERSION 3
+ * xgpu_integrate_general_stokes; xgpu_phase_interpolator, xgpu_energy_interpolator.
+ * 4: xgpu_atmos_cache_invalidate. */
+#define XGPU_ABI_VERSION 4
 
 /* Status words of the batched layer (per parameter vector). */
 enum {
@@ -59,6 +60,15 @@ typedef struct {
    * integrator only (NULL: it converts from the FP64 table) */
   const float *intensity_f32;
 } xgpu_atmos4d;
+
+/* The drop-in entry points keep one device copy of the last Num4D table per
+ * device, keyed by the host pointers, the sizes and a strided sample of the
+ * table (the reference preloads a table once and never edits it).  A caller
+ * that edits a table in place, or frees one and allocates another at the
+ * same address, calls this before its next call on the calling thread's
+ * current device; it waits for the device and frees the copy.  No counterpart
+ * in the reference (which reads the host table directly). */
+int xgpu_atmos_cache_invalidate(void);
 
 /* ---------------------------------------------------------------------- */
 /* 1. drop-in entry points (host arrays)                                  */
@@ -396,9 +406,9 @@ int xgpu_likelihood_batch(const xgpu_likelihood_batch_data *d, void *stream);
  * fixed 4 MiB device array inside this library (12 bytes per evaluation and
  * channel: n_vec * K <= 349525), which every GPU that loads the library
  * holds until the process exits.  No device memory is allocated or freed.
- * The first call on a device looks up that array's device address (once per
- * device, with the device current); make that first call before any stream
- * capture.  All calls share the one array, so calls that overlap on the GPU
+ * The first call on a device looks up that array's device address (with the
+ * device current), and so does the first call after the device's context was
+ * re-created (cudaDeviceReset); make such a call before any stream capture.  All calls share the one array, so calls that overlap on the GPU
  * (other streams, other threads) race: serialise them on one stream.
  * Returns 0, -2 for invalid sizes, -3 when n_vec * K exceeds the maximum,
  * -4 when the array's address cannot be obtained, -5 when the launch fails. */

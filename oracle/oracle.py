@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SOURCES = [os.path.join(HERE, "xpsi_oracle.c"),
+           os.path.join(HERE, "xpsi_oracle_mesh.c"),
            os.path.join(HERE, "gslsub", "gslsub.c")]
 
 _lock = threading.Lock()
@@ -99,6 +100,16 @@ def lib():
                                               P, P, C.c_double, C.c_int, P]
             L.xo_lnfact.restype = C.c_double
             L.xo_lnfact.argtypes = [C.c_uint]
+            D_ = C.c_double
+            L.xo_allocate_cells.restype = None
+            L.xo_allocate_cells.argtypes = [C.c_size_t, C.c_size_t, C.c_size_t, D_, D_, D_, D_,
+                                            C.c_int] + [D_] * 8 + [P]
+            L.xo_cell_mesh.restype = C.c_int
+            L.xo_cell_mesh.argtypes = [C.c_int, C.c_size_t, C.c_size_t, D_, D_, D_, C.c_int,
+                                       D_, D_, D_, D_, D_, C.c_int] + [P] * 7
+            L.xo_closed_cell_mesh.restype = C.c_int
+            L.xo_closed_cell_mesh.argtypes = [C.c_size_t, C.c_size_t, D_, D_, D_, C.c_int,
+                                              C.c_int] + [P] * 7
             _lib = L
     return _lib
 
@@ -109,6 +120,69 @@ def _c(a, dtype=np.float64):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def allocate_cells(num_cells, min_sqrt_num_cells, max_sqrt_num_cells, mass, r_s, R_eq,
+                   Omega, zeta, epsilon, star_shape_ind, superRadius, cedeRadius,
+                   superColatitude, cedeColatitude, superAzimuth, holeColatitude,
+                   holeRadius, holeAzimuth):
+    """mesh_tools.allocate_cells (mesh_tools.pyx:892-1099): (super_sqrt,
+    super_num, cede_sqrt, cede_num), integer zeros for the ceding region when
+    there is none, as the reference returns."""
+    out = np.zeros(4)
+    lib().xo_allocate_cells(int(num_cells), int(min_sqrt_num_cells), int(max_sqrt_num_cells),
+                            float(R_eq), float(Omega), float(zeta), float(epsilon),
+                            int(star_shape_ind), float(superRadius), float(cedeRadius),
+                            float(superColatitude), float(cedeColatitude), float(superAzimuth),
+                            float(holeColatitude), float(holeRadius), float(holeAzimuth),
+                            _p(out))
+    if abs(float(cedeRadius)) < 1.0e-12:
+        return (float(out[0]), float(out[1]), 0, 0)
+    return tuple(float(x) for x in out)
+
+
+def _cell_mesh(polar, numThreads, numCell, sqrt_numCell, mass, r_s, R_eq, zeta, epsilon,
+               star_shape_ind, cedeRadius, cedeColatitude, superRadius, superColatitude,
+               superAzimuth):
+    S = int(sqrt_numCell)
+    th, ph, r, ma, cg, g = (np.empty(S) for _ in range(6))
+    A = np.empty((S, S))
+    rc = lib().xo_cell_mesh(int(polar), int(numCell), S, float(R_eq), float(zeta),
+                            float(epsilon), int(star_shape_ind), float(cedeRadius),
+                            float(cedeColatitude), float(superRadius), float(superColatitude),
+                            float(superAzimuth), int(numThreads), _p(th), _p(ph), _p(r), _p(A),
+                            _p(ma), _p(cg), _p(g))
+    if rc:
+        raise ValueError("mesh needs at least 2 cells per side")
+    phi, theta = np.meshgrid(ph, th)
+    return theta, phi, r, A, ma, cg, g
+
+
+def construct_spot_cellMesh(*args):
+    """mesh.construct_spot_cellMesh (mesh.pyx:23-417): (theta, phi, r,
+    cellArea, maxEmissionAngle, cos_gamma, effGrav)."""
+    return _cell_mesh(0, *args)
+
+
+def construct_polar_cellMesh(*args):
+    """polar_mesh.construct_polar_cellMesh (polar_mesh.pyx:23-430)."""
+    return _cell_mesh(1, *args)
+
+
+def construct_closed_cellMesh(numThreads, sqrt_numCell, numCell, mass, r_s, R_eq, zeta,
+                              epsilon, star_shape_ind):
+    """global_mesh.construct_closed_cellMesh (global_mesh.pyx:21-137):
+    (theta, phi, r, cellArea (scalar), maxEmissionAngle, cos_gamma, effGrav)."""
+    S = int(sqrt_numCell)
+    th, ph, r, ma, cg, g = (np.empty(S) for _ in range(6))
+    area = np.zeros(1)
+    rc = lib().xo_closed_cell_mesh(S, int(numCell), float(R_eq), float(zeta), float(epsilon),
+                                   int(star_shape_ind), int(numThreads), _p(th), _p(ph), _p(r),
+                                   _p(area), _p(ma), _p(cg), _p(g))
+    if rc:
+        raise ValueError("closed mesh needs at least 4 cells per side")
+    phi, theta = np.meshgrid(ph, th)
+    return theta, phi, r, float(area[0]), ma, cg, g
 
 
 def compute_rays(N_T, N_u, r_s, r_s_over_R, maxAlpha, N_R):

@@ -10,8 +10,10 @@ time-invariant integrator (integrator_for_time_invariance.pyx), the hot
 regions' correction and the spectrum added to the first hot region's signal
 (Photosphere.py:588-592).
 
-The meshes come from the batched path's host mesh builders (an input here,
-like the data), so this checks every GPU stage."""
+P is a prepared batch: oracle/prepare.py builds one with the oracle's own
+meshes (so nothing of the GPU library runs), and the batched path's
+preparation gives the same fields (to check the GPU stages on identical
+inputs)."""
 import math
 
 import numpy as np
@@ -86,7 +88,8 @@ def loglike(model, P, n_threads=1, return_stages=False):
             ei = O.energy_integrator(n_threads, flux / P.d_sq[mi], logE, logEd)
             regs.append(np.dot(model.instrument.matrix, ei))
             if return_stages:
-                stages.append(dict(flux=flux, energy=ei, folded=regs[-1], deflection=D, lag=L))
+                stages.append(dict(v=v, h=h, flux=flux, energy=ei, folded=regs[-1],
+                                   deflection=D, lag=L))
         if status[v]:
             continue
         (ll, star, mb, mbs), st = O.eval_marginal_likelihood(

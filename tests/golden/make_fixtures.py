@@ -7,6 +7,10 @@ oracle/build_ref.py, Python model classes imported from the checkout), so
 the GPU tests compare against the reference, not against a restatement.
 
 Cases
+  meshes         the reference's cell budgets and spot / polar-cap meshes at the
+                 full-size resolution for the prior vectors of the full-size
+                 parity test (polar caps on either member, omitted crescents)
+                 and three hand-set members.
   examples_fast  the model of xpsi/tests/test_likelihood.py (blackbody spot,
                  golden log L -47881.27817666349); all stage inputs/outputs.
   num4d_omit     a spot with an omitted (crescent) region and a small seeded
@@ -32,7 +36,7 @@ Cases
                  32 phase bins, 1e6 s, seeded Poisson data) with a reduced
                  phase/energy grid only where noted.
 
-Usage:  python tests/golden/make_fixtures.py
+Usage:  python tests/golden/make_fixtures.py [case ...]   (all cases by default)
 """
 import math
 import os
@@ -163,6 +167,75 @@ def mesh_member(xpsi, *, M_sun, R_km, f_hz, cos_i, colat, radius, logT, omit=Non
                 radiates=radiates, maxAlpha_in=ma_in, rays_maxAlpha_out=ma,
                 deflection=D, cos_alpha=CA, raw_lag=raw_lag, lag=L, maxDeflection=MD,
                 cos_gamma=cg, effGrav=g, N_R=N_R)
+
+
+# prior vectors of the batched configuration (config3_vectors(64, seed=3))
+# used by the full-size parity test: 4, 5, 18 carry a polar-cap mesh on the
+# member with an omitted crescent, 17 and 26 on the circular member, 20 on
+# both; 0, 1, 2 are ordinary spots
+FULL_SIZE_VECTORS = (0, 1, 2, 4, 5, 17, 18, 20, 26)
+
+
+def meshes(xpsi):
+    """Reference meshes at the full-size resolution (sqrt_num_cells 64,
+    min 10, max 128): the cell budget (mesh_tools.allocate_cells) and the
+    spot or polar-cap mesh (mesh.construct_spot_cellMesh,
+    polar_mesh.construct_polar_cellMesh), chosen and called as
+    HotRegion.__construct_cellMesh does (HotRegion.py:774-836), for every
+    hot-region member of the parameter vectors FULL_SIZE_VECTORS, plus three
+    hand-set members: a south polar cap with an omitted region over the
+    pole, a north polar cap at a fast spin, and a spot of the smallest
+    prior radius."""
+    from xpsi.global_imports import _GM, _csq, _G, _km, _2pi
+    from xpsi.cellmesh.mesh_tools import allocate_cells
+    from xpsi.cellmesh.mesh import construct_spot_cellMesh
+    from xpsi.cellmesh.polar_mesh import construct_polar_cellMesh
+    from xpsi_gb300 import batch as BT
+    model = synthetic.config2_model()
+    names = BT.param_names(model)
+    col = {n: i for i, n in enumerate(names)}
+    params = synthetic.config3_vectors(64, seed=3)[list(FULL_SIZE_VECTORS)]
+    members = []
+    for v in range(params.shape[0]):
+        p = params[v]
+        for h, r in enumerate(model.regions):
+            om = (p[col[f"h{h}_omit_radius"]], p[col[f"h{h}_omit_colatitude"]],
+                  p[col[f"h{h}_omit_azimuth"]]) if r.omit else (0.0, 0.0, 0.0)
+            members.append((p[0], p[1], p[2], p[col[f"h{h}_colatitude"]],
+                            p[col[f"h{h}_radius"]]) + om)
+    members += [(1.8, 13.0, 450.0, 2.9, 0.45, 0.2, 3.05, 0.4),
+                (1.2, 15.5, 600.0, 0.3, 0.48, 0.0, 0.0, 0.0),
+                (2.6, 12.5, 250.0, 1.4, 0.01, 0.0, 0.0, 0.0)]
+    out = dict(params=params, vector_index=np.array(FULL_SIZE_VECTORS),
+               members=np.array(members), sqrt_num_cells=64, min_sqrt_num_cells=10,
+               max_sqrt_num_cells=128)
+    for k, (M_sun, R_km, f_hz, colat, rad, o_r, o_c, o_a) in enumerate(members):
+        r_g = M_sun * _GM
+        r_s = 2.0 * r_g
+        R = R_km * _km
+        Mkg = M_sun * _GM * _csq / _G
+        Omega = _2pi * f_hz
+        zeta = r_g / R
+        eps = Omega ** 2.0 * R ** 3.0 / (_G * Mkg)
+        S, N, _, _ = allocate_cells(64 ** 2, 10, 128, Mkg, r_s, R, Omega, zeta, eps, 0, rad,
+                                    0.0, colat, colat, -0.0, o_c, o_r, o_a)
+        polar = colat - rad < 0.0 or colat + rad > math.pi
+        fn = construct_polar_cellMesh if polar else construct_spot_cellMesh
+        th, ph, r, A, maxA, cg, g = fn(1, int(N), int(S), Mkg, r_s, R, zeta, eps, 0, rad, colat,
+                                       o_r, o_c, o_a)
+        assert np.all(th == th[:, :1]) and np.all(ph == ph[:1, :])
+        out[f"m{k}_S"] = int(S)
+        out[f"m{k}_num_cells"] = int(N)
+        out[f"m{k}_polar"] = int(polar)
+        out[f"m{k}_theta"] = th[:, 0]
+        out[f"m{k}_phi"] = ph[0, :]
+        out[f"m{k}_cellArea"] = A
+        out[f"m{k}_radius"] = r
+        out[f"m{k}_maxAlpha"] = maxA
+        out[f"m{k}_cos_gamma"] = cg
+        out[f"m{k}_effGrav"] = g
+    out["n_members"] = len(members)
+    save("meshes", **out)
 
 
 def num4d_omit(xpsi):
@@ -669,6 +742,11 @@ def interpolators(xpsi):
 
 def main():
     xpsi = H.load()
+    if len(sys.argv) > 1:
+        for name in sys.argv[1:]:
+            globals()[name](xpsi)
+        return
+    meshes(xpsi)
     examples_fast(xpsi)
     num4d_omit(xpsi)
     config1(xpsi)

@@ -27,4 +27,4 @@ def test_library_exports_header_symbols():
     for n in names:
         getattr(lib, n)
     assert set(names) == set(_native.EXPORTED)
-    assert lib.xgpu_abi_version() == 3
+    assert lib.xgpu_abi_version() == _native.ABI_VERSION == 4

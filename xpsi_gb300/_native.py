@@ -174,6 +174,7 @@ def _bind(L):
     sig = {
         "xgpu_abi_version": (C.c_int, []),
         "xgpu_last_error": (C.c_char_p, []),
+        "xgpu_atmos_cache_invalidate": (C.c_int, []),
         "xgpu_compute_rays": (C.c_int, [SZ, D, P, P, SZ, P, P, P, P]),
         "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ, SZ,
                                      P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
@@ -271,10 +272,11 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_poisson_batch", "xgpu_integrate_stokes", "xgpu_gaussian_loglike",
             "xgpu_gaussian_loglike_batch", "xgpu_integrate_split",
             "xgpu_integrate_split_stokes", "xgpu_integrate_general_stokes",
-            "xgpu_phase_interpolator", "xgpu_energy_interpolator"]
+            "xgpu_phase_interpolator", "xgpu_energy_interpolator",
+            "xgpu_atmos_cache_invalidate"]
 
 
-ABI_VERSION = 3  # XGPU_ABI_VERSION of include/xpsi_gb300.h
+ABI_VERSION = 4  # XGPU_ABI_VERSION of include/xpsi_gb300.h
 
 
 def lib():

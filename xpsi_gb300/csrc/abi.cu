@@ -88,16 +88,19 @@ int upload(Dev &d, const T *h, size_t n, cudaStream_t st) {
   return 0;
 }
 
-// device copy of the most recent Num4D table passed to the drop-in layer,
-// keyed by its host pointers, sizes and a strided content sample
+// Device copy of the most recent Num4D table passed to the drop-in layer, one
+// per device, keyed by the table's host pointers, sizes and a strided sample
+// of its contents.  The key cannot see every in-place edit of the host table
+// or a new table allocated at a freed one's address with the same sample:
+// callers that change a table in place call xgpu_atmos_cache_invalidate().
 struct AtmosCache {
   const double *host_I = nullptr;
   size_t nT = 0, ng = 0, nmu = 0, nE = 0;
   uint64_t sample = 0;
-  int dev = -1;
   void *buf = nullptr;
   xg::Atmos4D view{};
-} g_atmos;
+};
+AtmosCache g_atmos[64];
 
 uint64_t sample_table(const xgpu_atmos4d *A) {
   size_t n = A->nT * A->ng * A->nmu * A->nE;
@@ -117,41 +120,50 @@ uint64_t sample_table(const xgpu_atmos4d *A) {
   return h;
 }
 
+// frees device `dev`'s cached table; the caller holds g_mu and has made
+// `dev` current.  Every stream of the device may still read the buffer (the
+// drop-in stream, or a caller's), so the whole device is synchronised first.
+int atmos_release(int dev) {
+  AtmosCache &c = g_atmos[dev];
+  if (!c.buf) return 0;
+  CK(cudaDeviceSynchronize());
+  CK(cudaFree(c.buf));
+  c = AtmosCache{};
+  return 0;
+}
+
 int atmos_device(const xgpu_atmos4d *A, cudaStream_t st, xg::Atmos4D *out) {
   if (A->nT < 4 || A->ng < 4 || A->nmu < 4 || A->nE < 4)
     return fail_msg("Num4D grids need at least 4 nodes per dimension");
   int dev = 0;
   CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail_msg("device index out of range");
   uint64_t smp = sample_table(A);
   std::lock_guard<std::mutex> lk(g_mu);
-  if (g_atmos.buf && g_atmos.dev == dev && g_atmos.host_I == A->intensity &&
-      g_atmos.nT == A->nT && g_atmos.ng == A->ng && g_atmos.nmu == A->nmu &&
-      g_atmos.nE == A->nE && g_atmos.sample == smp) {
-    *out = g_atmos.view;
+  AtmosCache &c = g_atmos[dev];
+  if (c.buf && c.host_I == A->intensity && c.nT == A->nT && c.ng == A->ng &&
+      c.nmu == A->nmu && c.nE == A->nE && c.sample == smp) {
+    *out = c.view;
     return 0;
   }
-  if (g_atmos.buf) {
-    CK(cudaStreamSynchronize(st));
-    cudaFree(g_atmos.buf);
-    g_atmos.buf = nullptr;
-  }
+  int rc = atmos_release(dev);
+  if (rc) return rc;
   size_t nI = A->nT * A->ng * A->nmu * A->nE;
   size_t tot = A->nT + A->ng + A->nmu + A->nE + nI;
-  CK(cudaMalloc(&g_atmos.buf, tot * sizeof(double)));
-  double *b = static_cast<double *>(g_atmos.buf);
+  CK(cudaMalloc(&c.buf, tot * sizeof(double)));
+  double *b = static_cast<double *>(c.buf);
   double *pT = b, *pg = pT + A->nT, *pm = pg + A->ng, *pE = pm + A->nmu, *pI = pE + A->nE;
   CK(cudaMemcpyAsync(pT, A->logT, A->nT * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(pg, A->logg, A->ng * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(pm, A->mu, A->nmu * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(pE, A->logE, A->nE * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(pI, A->intensity, nI * 8, cudaMemcpyHostToDevice, st));
-  g_atmos.host_I = A->intensity;
-  g_atmos.nT = A->nT; g_atmos.ng = A->ng; g_atmos.nmu = A->nmu; g_atmos.nE = A->nE;
-  g_atmos.sample = smp;
-  g_atmos.dev = dev;
-  g_atmos.view = xg::Atmos4D{pT, pg, pm, pE, pI, (int)A->nT, (int)A->ng, (int)A->nmu,
-                             (int)A->nE, nullptr};
-  *out = g_atmos.view;
+  c.host_I = A->intensity;
+  c.nT = A->nT; c.ng = A->ng; c.nmu = A->nmu; c.nE = A->nE;
+  c.sample = smp;
+  c.view = xg::Atmos4D{pT, pg, pm, pE, pI, (int)A->nT, (int)A->ng, (int)A->nmu,
+                       (int)A->nE, nullptr};
+  *out = c.view;
   return 0;
 }
 
@@ -163,6 +175,14 @@ extern "C" {
 
 int xgpu_abi_version(void) { return XGPU_ABI_VERSION; }
 const char *xgpu_last_error(void) { return g_err.c_str(); }
+
+int xgpu_atmos_cache_invalidate(void) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail_msg("device index out of range");
+  std::lock_guard<std::mutex> lk(g_mu);
+  return atmos_release(dev);
+}
 
 // ------------------------------------------------------------------ batched
 int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u, const double *r_s,
@@ -326,6 +346,7 @@ int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int
   int rc = dalloc(scratch, xg::fold_tc_scratch_bytes(a), st);
   if (rc) return rc;
   rc = xg::launch_fold_tc(a, scratch.p, st);
+  if (rc == -5) return fail_msg("could not set the tensor-core fold's shared-memory size");
   if (rc) return fail_msg("tensor-map encoding failed for the tensor-core fold");
   CK(cudaGetLastError());
   return 0;

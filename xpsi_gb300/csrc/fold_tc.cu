@@ -228,7 +228,9 @@ __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
   for (int c = 0; c < kTN; c++) acc[c] = 0.0f;
   const int nkb = q_pad / kTK;
   int step = 0;
-  for (int kb = 0; kb < nkb && !s_fail; kb++) {
+  // s_fail is written by thread 0 only and read by every thread only after
+  // the barrier that follows the write, so all threads leave together
+  for (int kb = 0; kb < nkb; kb++) {
     if (threadIdx.x == 0) {
       mbar_expect_tx(&bar_full, kStageBytes);
       const int x = kb * kTK;
@@ -357,12 +359,10 @@ int launch_fold_tc(const FoldArgs &a, void *scratch, cudaStream_t st) {
   if (make_map(&mapA, A2, 2 * rows_a, k_pad) || make_map(&mapB, B2, (int)(2 * rows_b), k_pad))
     return -4;
   const size_t smem = kStageBytes + 1024;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(fold_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr = true;
-  }
+  // the attribute is per device: set it on every launch (cheap)
+  if (cudaFuncSetAttribute(fold_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -5;
   dim3 grid((unsigned)(rows_b / kTN), (unsigned)(rows_a / kTM));
   fold_tc_kernel<<<grid, kFoldThreads, smem, st>>>(mapA, mapB, a.K, k_pad, rows_a,
                                                    (int)rows_b, a.N, cols, a.out);

@@ -599,19 +599,53 @@ constexpr size_t kLikeScratchBytes = size_t(4) << 20;
 constexpr size_t kLikeScratchPerChannel = sizeof(double) + sizeof(int32_t);
 static __device__ __align__(256) unsigned char g_like_scratch[kLikeScratchBytes];
 
-// device address of g_like_scratch per device, looked up once with that
-// device current (the host-side name of the array is not a device address)
+// device address of g_like_scratch per device, looked up with that device
+// current (the host-side name of the array is not a device address) and
+// kept with the unique id of the context it belongs to: a context created
+// anew (after cudaDeviceReset) has a new id, and the address is looked up
+// again instead of reusing one from the destroyed context
 std::mutex g_like_scratch_mu;
 void *g_like_scratch_addr[64] = {};
+unsigned long long g_like_scratch_ctx[64] = {};
+
+using CtxGetCurrent = int (*)(void **);
+using CtxGetId = int (*)(void *, unsigned long long *);
+
+// the current context's unique id, through the driver entry points the
+// runtime hands out (no link-time dependency on the driver library); 0 if
+// they are unavailable
+unsigned long long current_context_id() {
+  static CtxGetCurrent get_cur = nullptr;
+  static CtxGetId get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<CtxGetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetId>(p);
+    looked = true;
+  }
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_cur && get_id && get_cur(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
 
 int like_scratch_address(void **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -4;
   std::lock_guard<std::mutex> lk(g_like_scratch_mu);
-  if (!g_like_scratch_addr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_like_scratch_addr[dev] || ctx == 0 || ctx != g_like_scratch_ctx[dev]) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_like_scratch) != cudaSuccess || p == nullptr) return -4;
     g_like_scratch_addr[dev] = p;
+    g_like_scratch_ctx[dev] = ctx;
   }
   *out = g_like_scratch_addr[dev];
   return 0;
