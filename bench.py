@@ -143,49 +143,105 @@ def shard_vectors(V, rank, world, seed=3):
     return SY.config3_vectors(V * world, seed=seed)[rank * V:(rank + 1) * V]
 
 
-# ------------------------------------------------------------------ GPU arm
-def run_gb300(args):
+# Instruction counts of the dominant kernel (integrate_kernel<double>), from one
+# ncu capture of one launch over the first 64 prior vectors of the benchmark's
+# draw (profiles/integrate_kernel_instruction_mix_64_vectors.md).  Thread
+# instructions: FP64 FLOP = 2 DFMA + DMUL + DADD, FP32 FLOP = 2 FFMA + FMUL +
+# FADD.  A launch over other vectors is scaled by its cost-model work (the
+# kernel's own counter) relative to the captured launch's.
+PIPE_COUNTS = {
+    "vectors": 64,
+    "cost_model_flop": 482067568128.0,
+    "fp64_flop": 2 * 6955209850 + 6428283081 + 2293872409,
+    "fp32_flop": 2 * 136060681846 + 46795769114 + 552848550742,
+    "dram_bytes": 745280768 + 1360537856,
+    "fp64_pipe_active": 0.593,
+    "fma_pipe_active": 0.274,
+    "issue_active": 0.406,
+    "duration_ms": 208.3,
+    "capture": "ncu --metrics (instruction classes, pipe activity, dram bytes) -k "
+               "regex:integrate_kernel -s 1 -c 1, python bench.py --vectors 64 --steps 1 "
+               "--warmup 3 --legs none",
+}
+
+
+def bench_config(V):
+    """The workload description both arms print (identical by construction)."""
+    return {"workload": WORKLOAD, "vectors_per_gpu": V,
+            "vectors": "config3_vectors(V, seed=3): the first V prior draws of seed 3 "
+                       "(sharded by rank under torchrun)",
+            "l2": "inputs and ray tables larger than L2 (129 MB) every step"}
+
+
+def gpu_data(model, device):
+    """Counts drawn from the GPU's model of the full-size configuration's
+    vector (the GPU arm).  The reference arm draws them from the oracle's
+    model of the same vector; the two expected-count sets agree to ~1e-12, so
+    the seeded Poisson draws are the same counts (checked in
+    tests/test_gpu_full_size.py)."""
     import torch
     from xpsi_gb300 import batch as BT
     from xpsi_gb300 import synthetic as SY
-    from xpsi_gb300._native import lib
-    rank, world = dist_init()
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    V = args.vectors
-    model, _ = build_workload(1)
-    # data: Poisson draws from the model of the full-size configuration's vector
-    ev = BT.BatchEvaluator(model, device=local)
+    ev = BT.BatchEvaluator(model, device=device)
     P0 = BT.prepare(model, SY.config2_vector(seed=1)[None, :])
     B0 = ev.upload(P0)
     ev.run(B0)
     torch.cuda.synchronize()
     folded = B0["folded"].cpu().numpy()
     SY.attach_data(model, [folded[0], folded[1]], P0.shifts[0])
+    return model
+
+
+def oracle_data(model, n_threads):
+    """Counts drawn from the oracle's model of the full-size configuration's
+    vector (the reference arm)."""
+    from oracle import pipeline as OP
+    from oracle import prepare as OPR
+    from xpsi_gb300 import synthetic as SY
+    P0 = OPR.prepare(model, SY.config2_vector(seed=1)[None, :], n_threads=n_threads)
+    _, _, stages = OP.loglike(model, P0, n_threads=n_threads, return_stages=True)
+    SY.attach_data(model, [stages[0]["folded"], stages[1]["folded"]], P0.shifts[0])
+    return model
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gb300(args):
+    import torch
+    from xpsi_gb300 import batch as BT
+    rank, world = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    V = args.vectors
+    cores = os.cpu_count() or 1
+    model, _ = build_workload(1)
+    gpu_data(model, local)
     ev = BT.BatchEvaluator(model, device=local)
     # each rank evaluates its own V vectors (independent parameter vectors)
     params = shard_vectors(V, rank, world)
     t0 = time.time()
     P = BT.prepare(model, params)
     t_mesh = time.time() - t0
-    B = ev.upload(P)
-    # three batches in flight on three streams, the steps rotating between
-    # them: one batch's FP64-bound stages run beside another's FP32-bound
+    # resident copies of the batch, the steps rotating over one CUDA stream
+    # each: one batch's FP64-bound stages run beside another's FP32-bound
     # integrator sums
-    Bs = [B, ev.upload(P), ev.upload(P)]
+    from xpsi_gb300.serving import estimate_bytes
+    per_batch = estimate_bytes(ev, P)
+    n_res = max(1, min(args.resident, int((150 << 30) // max(1, per_batch))))
+    Bs = [ev.upload(P) for _ in range(n_res)]
+    B = Bs[0]
     streams = [torch.cuda.Stream() for _ in Bs]
     flops = torch.zeros(1, dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream()
     # warm-up
     pipelined_steps(ev, Bs, streams, args.warmup)
     torch.cuda.synchronize()
-    # integrator time (CUDA events on the launching stream) and its
-    # algorithmic FLOPs for one step
+    # the integrator alone on one stream (CUDA events on the launching
+    # stream) and its cost-model work for one step
     probe = {"flops": flops}
     ev.run(B, probe=probe)
     torch.cuda.synchronize()
     int_ms = probe["start"].elapsed_time(probe["end"])
     int_flops = float(flops.item())
+    one_ms = single_stream_step(ev, B)
     # timed region
     barrier(world)
     torch.cuda.synchronize()
@@ -195,7 +251,10 @@ def run_gb300(args):
     barrier(world)
     ms = max_over_ranks(ms, world)
     st = ev.statuses(B)
+    plain_ll = B["loglike"].cpu().numpy().copy()
     value = V * world / (ms / 1e3)
+    del Bs, B
+    torch.cuda.empty_cache()
     # end to end through the public API from the host parameter vectors:
     # each step prepares the batch (cell budgets and derived quantities on
     # the host), copies its mesh descriptors to the device (pinned), builds
@@ -204,7 +263,7 @@ def run_gb300(args):
     Pg = BT.prepare(model, params, meshes="gpu")
     h2d = ev.h2d_bytes(Pg)
     d2h = V * (8 + 4)
-    e2e_steps = max(6, args.steps)
+    e2e_steps = max(2, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
@@ -215,6 +274,7 @@ def run_gb300(args):
     e2e_s = max_over_ranks(e2e_s, world)
     # the GPU mesh build of one batch alone (CUDA events around the upload,
     # whose launches are the mesh kernels and the descriptor copies)
+    stream = torch.cuda.current_stream()
     g0 = torch.cuda.Event(enable_timing=True)
     g1 = torch.cuda.Event(enable_timing=True)
     g0.record(stream)
@@ -222,6 +282,8 @@ def run_gb300(args):
     g1.record(stream)
     torch.cuda.synchronize()
     mesh_gpu_ms = g0.elapsed_time(g1)
+    del Bx
+    torch.cuda.empty_cache()
     t0 = time.perf_counter()
     BT.prepare(model, params, meshes="gpu")
     t_prep = time.perf_counter() - t0
@@ -230,69 +292,99 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded prior draws, "
-        "Poisson counts from the model)",
-        "config": {"workload": WORKLOAD,
-                   "vectors_per_gpu": V, "precision": "plain FP64",
-                   "l2": "inputs and ray tables larger than L2 (129 MB) every step",
-                   "streams": "three batches resident, steps rotating over three CUDA streams "
-                              "(events bracket all steps of all three)",
-                   "mesh_build_host_s": round(t_mesh, 3),
-                   "mesh_build_gpu_ms": round(mesh_gpu_ms, 2),
-                   "prepare_for_gpu_meshes_s": round(t_prep, 3),
-                   "status_counts": {str(k): int(v) for k, v in
-                                     zip(*np.unique(st, return_counts=True))}},
+        "Poisson counts from the model of the full-size configuration's vector)",
+        "config": bench_config(V),
+        "details": {"precision": "plain FP64 path (the drop-in's numerics), every vector "
+                                 "of the batch in one launch per stage",
+                    "streams": f"{n_res} copies of the batch resident, steps rotating over "
+                               f"{n_res} CUDA streams (events bracket all steps)",
+                    "ms_per_step_one_stream": one_ms,
+                    "mesh_build_host_s": round(t_mesh, 3),
+                    "mesh_build_gpu_ms": round(mesh_gpu_ms, 2),
+                    "prepare_for_gpu_meshes_s": round(t_prep, 3),
+                    "device_bytes_per_batch": per_batch,
+                    "status_counts": {str(k): int(v) for k, v in
+                                      zip(*np.unique(st, return_counts=True))}},
         "e2e": {"value": V * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "what": "from host parameter vectors: host cell budgets, pinned copies, GPU "
                         "meshes, the five stages, log L and statuses back to the host; "
-                        "BatchEvaluator.loglikelihood_pipelined, three batches in flight"},
+                        f"BatchEvaluator.loglikelihood_pipelined, {args.e2e_depth} batches "
+                        "in flight"},
         "gpu_launches": None,
         "clocks": clocks.summary(),
     }
     # kernels launched per step: rays 1, integrator 2 (+2 Num4D pre-pass/scan),
     # energy 1, fold 1, likelihood 2
     out["gpu_launches"] = args.steps * (1 + 4 + 1 + 1 + 2)
-    peak64 = fp64_peak(local)
-    achieved = int_flops / (int_ms / 1e3) / 1e12
-    out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64,
-                       "unit": "TFLOP/s", "frac": achieved / peak64 if peak64 else None,
-                       "traffic": None,
-                       "traffic_note": "DRAM bytes of this kernel from ncu at 8 vectors: 224 MB "
-                                       "read + 260 MB written per launch (0.64 % of peak "
-                                       "bandwidth), mostly the per-chunk partial sums, whose "
-                                       "size follows the chunk count rather than the vectors, "
-                                       "so it is not scaled to this launch",
-                       "pipes_ncu": {"fp64_pipe_active": 0.620, "fma_pipe_active": 0.273,
-                                     "issue_active": 0.407, "source": "ncu --set full of this "
-                                     "kernel at 8 vectors (profiles/)"},
-                       "kernel": "integrate_kernel",
-                       "kernel_ms": int_ms, "flops_per_launch": int_flops,
-                       "peak_source": "measured FP64 FMA probe on this GPU (not in "
-                       "MEASURED_PEAKS.json)", "hbm_peak_gbs": pk.get("hbm_gbs"),
-                       "hbm_peak_source": pk_kind,
-                       "note": "achieved counts the reference algorithm's FP64 operations "
-                               "(cost model of the path); the kernel computes them at "
-                               "FP64-class accuracy as double-float arithmetic on the "
-                               "FP32 pipes (64x the FP64 issue rate), so frac can exceed "
-                               "1 against the FP64 pipe's peak; pipe utilisation of this "
-                               "kernel is in profiles/"}
-    torch.cuda.synchronize()
-    plain_ll = B["loglike"].cpu().numpy().copy()
+    out["roofline"] = roofline(int_ms, int_flops, V)
     if rank == 0:
         legs = set(args.legs.split(",")) if args.legs != "all" else \
             {"mixed", "drop_in", "serving", "cpu"}
+        cpu = None
+        if "cpu" in legs:
+            cpu = cpu_baseline(args, model, params, plain_ll, st)
+            out["cpu_baseline"] = cpu
         if "mixed" in legs:
-            out["mixed"] = mixed_leg(model, P, plain_ll, st, args)
+            out["mixed"] = mixed_leg(model, P, plain_ll, st, args, cpu)
         if "drop_in" in legs:
             out["drop_in"] = drop_in_leg(model, P, min(V, args.drop_in_vectors))
             out["batched_vs_drop_in"] = value / out["drop_in"]["value"]
             if "mixed" in out:
                 out["mixed_vs_drop_in"] = out["mixed"]["value"] / out["drop_in"]["value"]
-        if "serving" in legs and args.serve_seconds > 0:
+        if "serving" in legs and args.serve_window > 0:
             out["serving"] = serving_leg(args)
-        if "cpu" in legs:
-            out["cpu_baseline"] = cpu_baseline(args, model, params)
+        if cpu is not None:
+            cpu.pop("_ll", None)
+            cpu.pop("_st", None)
         print(json.dumps(out))
+
+
+def single_stream_step(ev, B, reps=1):
+    """ms of one step of the batch on one stream, alone (CUDA events)."""
+    import torch
+    s = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        ev.run(B, stream=s)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def roofline(int_ms, int_flops, V):
+    """Per-pipe rates of the dominant kernel against the pipes' measured
+    FMA peaks: its FP64 and FP32 arithmetic (ncu instruction counts of the
+    captured launch, scaled to this launch by the cost-model work) over its
+    CUDA-event duration in this run."""
+    pk, pk_kind = peaks()
+    p64, p32 = pipe_peak(1), pipe_peak(0)
+    scale = int_flops / PIPE_COUNTS["cost_model_flop"] if int_flops > 0 else V / 64.0
+    sec = int_ms / 1e3
+    a64 = PIPE_COUNTS["fp64_flop"] * scale / sec / 1e12
+    a32 = PIPE_COUNTS["fp32_flop"] * scale / sec / 1e12
+    traffic = PIPE_COUNTS["dram_bytes"] * scale
+    return {"bound": "fp64", "achieved": a64, "peak": p64, "unit": "TFLOP/s", "frac": a64 / p64,
+            "traffic": traffic,
+            "pipes": {"fp64": {"achieved": a64, "peak": p64, "frac": a64 / p64,
+                               "pipe_active_ncu": PIPE_COUNTS["fp64_pipe_active"]},
+                      "fp32": {"achieved": a32, "peak": p32, "frac": a32 / p32,
+                               "pipe_active_ncu": PIPE_COUNTS["fma_pipe_active"]},
+                      "issue_active_ncu": PIPE_COUNTS["issue_active"]},
+            "kernel": "integrate_kernel<double>", "kernel_ms": int_ms,
+            "cost_model_flop_per_launch": int_flops,
+            "achieved_hbm_gbs": traffic / sec / 1e9, "hbm_peak_gbs": pk.get("hbm_gbs"),
+            "hbm_peak_source": pk_kind,
+            "peak_source": "measured here: FMA throughput probes of the FP64 and FP32 pipes "
+                           "(MEASURED_PEAKS.json has HBM and bf16 only)",
+            "counts_source": PIPE_COUNTS["capture"] + " (%d vectors; scaled by %.3f)"
+                             % (PIPE_COUNTS["vectors"], scale),
+            "note": "the binding pipe is FP64 (ncu: %.0f %% of active cycles, about half of "
+                    "its instructions compares and conversions); frac is its arithmetic "
+                    "rate over its FMA peak" % (100 * PIPE_COUNTS["fp64_pipe_active"])}
 
 
 def pipe_peak(fp64):
@@ -349,32 +441,43 @@ def pipelined_steps(ev, Bs, streams, steps):
     return e0.elapsed_time(e1) / max(1, steps)
 
 
-def mixed_leg(model, P, plain_ll, plain_st, args):
-    """Batched mixed-precision form on the same vectors: throughput and
-    |Delta log L| against the FP64 path."""
+def mixed_leg(model, P, plain_ll, plain_st, args, cpu=None):
+    """Batched mixed-precision form on the same vectors: throughput, and
+    |Delta log L| against the FP64 path on every vector and against the
+    oracle on the vectors the CPU leg evaluated."""
     import torch
     from xpsi_gb300 import batch as BT
     ev = BT.BatchEvaluator(model, precision="mixed")
-    B = ev.upload(P)
-    Bs = [B, ev.upload(P), ev.upload(P)]
+    Bs = [ev.upload(P) for _ in range(2)]
+    B = Bs[0]
     streams = [torch.cuda.Stream() for _ in Bs]
-    pipelined_steps(ev, Bs, streams, args.warmup)
-    ms = pipelined_steps(ev, Bs, streams, args.steps)
+    pipelined_steps(ev, Bs, streams, 1)
+    ms = pipelined_steps(ev, Bs, streams, max(2, min(args.steps, 4)))
     ll = B["loglike"].cpu().numpy()
     st = ev.statuses(B)
+    del Bs, B
+    torch.cuda.empty_cache()
     ok = (st == 0) & (plain_st == 0)
     d = np.abs(ll - plain_ll)[ok]
-    rel = d / np.abs(plain_ll[ok])
-    return {"value": P.V / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-            "precision": "FP32 atmosphere interpolation, Akima pieces and cell x phase sums; "
-                         "FP64 rays, knots, energy integration, fold and log L",
-            "dlogL_vs_fp64": {"median": float(np.median(d)) if d.size else None,
-                              "p99": float(np.percentile(d, 99)) if d.size else None,
-                              "max": float(d.max()) if d.size else None,
-                              "frac_within_1e-3": float((d <= 1e-3).mean()) if d.size else None,
-                              "median_relative": float(np.median(rel)) if d.size else None,
-                              "vectors": int(ok.sum())},
-            "status_equal": bool((st == plain_st).all())}
+    out = {"value": P.V / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+           "precision": "FP32 atmosphere interpolation, Akima pieces and cell x phase sums; "
+                        "tensor-core fold (3xTF32, FP32 accumulation); FP64 rays, knots, "
+                        "energy integration and log L",
+           "dlogL_vs_fp64": _dist(d),
+           "status_equal": bool((st == plain_st).all())}
+    if cpu is not None and cpu.get("_ll") is not None:
+        n = len(cpu["_ll"])
+        ok_o = (cpu["_st"] == 0) & (st[:n] == 0)
+        out["dlogL_vs_oracle"] = _dist(np.abs(ll[:n] - cpu["_ll"])[ok_o])
+    return out
+
+
+def _dist(d):
+    if d.size == 0:
+        return {"vectors": 0}
+    return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)),
+            "max": float(d.max()), "frac_within_1e-3": float((d <= 1e-3).mean()),
+            "vectors": int(d.size)}
 
 
 def drop_in_leg(model, P, n_vec):
@@ -436,14 +539,14 @@ def drop_in_leg(model, P, n_vec):
                     "(host arrays, H2D/D2H per call), FP64"}
 
 
-def serving_leg(args):
-    """Poisson request stream through the serving loop: even blackbody /
-    Num4D mix, sqrt_num_cells in {32, 64, 96}, num_leaves in {64, 128},
-    mixed-precision form; p50/p99 latency and throughput."""
+def serving_models():
+    """The serving configuration's model mix: blackbody (the small plain
+    configuration's kind) and Num4D (the full-size configuration's), each at
+    sqrt_num_cells 32, 64, 96 (max 128) and 64 or 128 leaves; data drawn from
+    each model's reference vector on the GPU."""
     import torch
     from xpsi_gb300 import batch as BT
     from xpsi_gb300 import synthetic as SY
-    from xpsi_gb300.serving import Server, poisson_stream
     models = {}
     for kind in ("bb", "num4d"):
         for sq in (32, 64, 96):
@@ -472,9 +575,18 @@ def serving_leg(args):
                 SY.attach_data(m, [f[h] for h in range(P0.H)], P0.shifts[0])
                 models[f"{kind}_{sq}_{nl}"] = (m, ref)
                 del ev, B0
+    return models
+
+
+def serve_once(models, rate, window, max_batch, precision, seed):
+    """Poisson arrivals at `rate` req/s for `window` s, batch sizes
+    log-uniform on [1, max_batch], models drawn evenly; returns the
+    serving record (all requests run to completion)."""
+    from xpsi_gb300 import synthetic as SY
+    from xpsi_gb300.serving import Server, poisson_stream
     names = sorted(models)
-    stream = poisson_stream(args.serve_rate, args.serve_seconds, args.serve_max_batch, seed=5)
-    rng = np.random.default_rng(5)
+    stream = poisson_stream(rate, window, max_batch, seed=seed)
+    rng = np.random.default_rng(seed)
     reqs = []
     for t, v in stream:
         name = names[rng.integers(len(names))]
@@ -488,7 +600,7 @@ def serving_leg(args):
             p = SY.config3_vectors(v, seed=int(rng.integers(1 << 30)))
         reqs.append((t, name, p))
     srv = Server({k: v[0] for k, v in models.items()}, hbm_budget=120 << 30, slots=4,
-                 precision="mixed", prep_threads=8)
+                 precision=precision, prep_threads=8)
     futs = []
     t0 = time.perf_counter()
     for t, name, p in reqs:
@@ -496,82 +608,107 @@ def serving_leg(args):
             time.sleep(0.0002)
         futs.append(srv.submit(name, p))
     for f in futs:
-        f.result(timeout=600)
+        f.result(timeout=1800)
     wall = time.perf_counter() - t0
     srv.close()
     lat = srv.latency_percentiles()
     nv = sum(p.shape[0] for _, _, p in reqs)
     return {"p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"], "requests": len(reqs),
             "vectors": nv, "throughput": nv / wall, "unit": UNIT, "wall_s": wall,
-            "arrivals": f"Poisson {args.serve_rate} req/s for {args.serve_seconds} s, "
-                        f"batch sizes log-uniform on [1, {args.serve_max_batch}]",
+            "arrivals": f"Poisson {rate} req/s for {window} s, batch sizes log-uniform on "
+                        f"[1, {max_batch}], {len(names)} models drawn evenly",
             "launches": srv.stats.launches, "merged_requests": srv.stats.merged_requests,
             "peak_concurrent_launches": srv.stats.peak_concurrency,
-            "peak_device_bytes_admitted": srv.stats.peak_bytes,
-            "models": len(names), "precision": "mixed"}
+            "peak_device_bytes_admitted": srv.stats.peak_bytes, "hbm_budget_bytes": 120 << 30,
+            "precision": precision}
+
+
+def serving_leg(args):
+    """The serving configuration: 200 req/s, batches log-uniform on [1, 4096]
+    (about 490 vectors per request), an even blackbody / Num4D mix over
+    sqrt_num_cells {32, 64, 96} x leaves {64, 128}, a 120 GB admission
+    budget, plain FP64 form (the form that meets |dlogL| <= 1e-3), over a
+    fixed arrival window.  It offers ~1e5 vectors/s, far beyond one GPU, so
+    latencies are queue-bound and the throughput is the saturation rate.
+    Beside it, a load one GPU sustains (40 req/s, batches 1-16)."""
+    models = serving_models()
+    sat = serve_once(models, args.serve_rate, args.serve_window, args.serve_max_batch,
+                     "plain", seed=5)
+    sat["what"] = "saturation: the serving configuration's arrival process over a fixed window"
+    sus = serve_once(models, 40.0, 2.0, 16, "plain", seed=6)
+    sus["what"] = "sustainable load"
+    return {"saturation": sat, "sustainable": sus}
+
 
 # ------------------------------------------------------------------ CPU legs
-def oracle_evals(model, params, n_threads, budget_s):
-    """Run the oracle over successive vectors until the time budget is used;
-    returns (evaluations, seconds)."""
-    from xpsi_gb300 import batch as BT
+def oracle_evals(model, params, n_threads, budget_s, start=0):
+    """The oracle over successive vectors (from `start`) until the time
+    budget is used, each from its parameter vector: the oracle's own
+    preparation (cell budgets and meshes included) and every restated
+    stage; returns (log L [n], status [n], seconds)."""
     from oracle import pipeline as OP
-    done, t_total = 0, 0.0
-    for v in range(params.shape[0]):
+    from oracle import prepare as OPR
+    lls, sts, t_total = [], [], 0.0
+    for v in range(start, params.shape[0]):
         t0 = time.perf_counter()
-        # the whole path from the parameter vector: cell budget and meshes
-        # (host C++ on all cores), then the restated stages
-        P = BT.prepare(model, params[v:v + 1], n_threads=n_threads)
-        OP.loglike(model, P, n_threads=n_threads)
+        P = OPR.prepare(model, params[v:v + 1], n_threads=n_threads)
+        ll, st = OP.loglike(model, P, n_threads=n_threads)
         t_total += time.perf_counter() - t0
-        done += 1
+        lls.append(ll[0])
+        sts.append(st[0])
         if t_total >= budget_s:
             break
-    return done, t_total
+    return np.array(lls), np.array(sts, dtype=np.int32), t_total
 
 
-def cpu_baseline(args, model, params):
+def cpu_baseline(args, model, params, plain_ll=None, plain_st=None):
+    """The oracle on the host cores over the first vectors of the batch, and
+    |Delta log L| of the GPU's plain path against it on those vectors."""
     cores = os.cpu_count() or 1
-    n, t = oracle_evals(model, params, cores, args.cpu_budget)
-    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} of the benchmark's prior vectors through the CPU restatement "
-                      f"(oracle/, OpenMP over parallels, {cores} threads), meshes included, "
-                      f"{t:.1f} s"}
+    ll, st, t = oracle_evals(model, params, cores, args.cpu_budget)
+    n = len(ll)
+    out = {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"the first {n} vectors of the batch through the oracle (oracle/: its "
+                     f"own meshes and every restated stage, OpenMP over parallels, {cores} "
+                     f"threads), {t:.1f} s", "_ll": ll, "_st": st}
+    if plain_ll is not None:
+        ok = (st == 0) & (plain_st[:n] == 0)
+        out["plain_vs_oracle"] = {"status_equal": bool((st == plain_st[:n]).all()),
+                                  **_dist(np.abs(plain_ll[:n] - ll)[ok])}
+    return out
 
 
 def run_reference(args):
     rank, world = dist_init()
     if rank != 0:
         return
-    from oracle import oracle as O  # noqa: F401
-    from oracle import pipeline as OP
-    from xpsi_gb300 import batch as BT
-    from xpsi_gb300 import synthetic as SY
-    model, _ = build_workload(1)
-    P0 = BT.prepare(model, SY.config2_vector(seed=1)[None, :])
-    _, _, stages = OP.loglike(model, P0, n_threads=os.cpu_count() or 1, return_stages=True)
-    SY.attach_data(model, [stages[0]["folded"], stages[1]["folded"]], P0.shifts[0])
-    params = SY.config3_vectors(args.vectors, seed=3)
     cores = os.cpu_count() or 1
+    model, _ = build_workload(1)
+    oracle_data(model, cores)
+    V = args.vectors
+    params = shard_vectors(V, 0, 1)
     per_step = max(1.0, args.cpu_budget / max(1, args.steps))
     for _ in range(args.warmup):
         oracle_evals(model, params[:1], cores, 0.0)
-    n_tot, t_tot = 0, 0.0
+    n_tot, t_tot, v0 = 0, 0.0, 0
     for s in range(args.steps):
-        n, t = oracle_evals(model, params[s:], cores, per_step)
-        n_tot += n
+        ll, st, t = oracle_evals(model, params, cores, per_step, start=v0 % V)
+        n_tot += len(ll)
+        v0 += len(ll)
         t_tot += t
     value = n_tot / t_tot
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_tot / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (seeded prior draws, Poisson counts from the model)",
-           "config": {"workload": WORKLOAD, "vectors_per_gpu": args.vectors,
-                      "vectors_sampled": n_tot},
+           "data": "synthetic (seeded prior draws, Poisson counts from the model of the "
+                   "full-size configuration's vector)",
+           "config": bench_config(V),
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{n_tot} prior vectors through the CPU restatement "
-                                      f"(OpenMP, {cores} threads), meshes included"},
+                            "sample": f"the first {n_tot} vectors of the batch through the "
+                                      f"oracle (its own meshes and every restated stage; "
+                                      f"OpenMP, {cores} threads), about {per_step:.1f} s per "
+                                      f"step"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -582,21 +719,24 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--vectors", type=int, default=256)
+    # the batched configuration: 4096 prior vectors in one launch
+    ap.add_argument("--vectors", type=int, default=4096)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     # comma-separated subset of mixed,drop_in,serving,cpu (or "all", "none"):
     # the legs run after the timed plain-path steps
     ap.add_argument("--legs", default="all")
-    ap.add_argument("--e2e-depth", type=int, default=3,
+    ap.add_argument("--resident", type=int, default=2,
+                    help="copies of the batch resident for the timed steps (one stream each)")
+    ap.add_argument("--e2e-depth", type=int, default=2,
                     help="batches in flight in the end-to-end leg")
+    ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--drop-in-vectors", type=int, default=8)
-    # the stream's shape (Poisson arrivals, log-uniform batch sizes, even
-    # model mix) at an offered load one GPU sustains; 200 req/s with batches
-    # up to 4096 offers ~1e5 vectors/s
-    ap.add_argument("--serve-rate", type=float, default=40.0)
-    ap.add_argument("--serve-seconds", type=float, default=2.0)
-    ap.add_argument("--serve-max-batch", type=int, default=16)
+    ap.add_argument("--drop-in-vectors", type=int, default=64)
+    # the serving configuration: Poisson arrivals at 200 req/s, batches
+    # log-uniform on [1, 4096], over a fixed arrival window
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-window", type=float, default=0.1)
+    ap.add_argument("--serve-max-batch", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

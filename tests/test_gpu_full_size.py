@@ -55,6 +55,20 @@ def workload(cuda):
                 stages={(s["v"], s["h"]): s for s in stages})
 
 
+def test_gpu_and_oracle_draw_the_same_counts(cuda, workload):
+    """The benchmark's arms draw their data from the GPU's and from the
+    oracle's model of the same vector: the seeded Poisson counts agree."""
+    model = SY.config2_model()
+    ev = BT.BatchEvaluator(model)
+    P0 = BT.prepare(model, SY.config2_vector(seed=1)[None, :])
+    B0 = ev.upload(P0)
+    ev.run(B0)
+    cuda.cuda.synchronize()
+    f = B0["folded"].cpu().numpy()
+    SY.attach_data(model, [f[0], f[1]], P0.shifts[0])
+    np.testing.assert_array_equal(model.data.counts, workload["model"].data.counts)
+
+
 def test_full_size_workload_has_polar_caps(workload):
     Ph = workload["Ph"]
     f = workload["f"]

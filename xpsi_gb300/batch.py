@@ -139,6 +139,21 @@ def param_names(model):
     return names
 
 
+def spacetime(mass, radius, frequency, cos_inclination, distance):
+    """The derived quantities of xpsi.Spacetime (Spacetime.py:110-187) from
+    its five parameters (solar masses, km, Hz, cos i, kpc): M (kg), r_g,
+    r_s, R, R_r_s, f, Omega, i, d, d_sq (SI), zeta and epsilon of the
+    universal relations (Morsink et al. 2007; AlGendy & Morsink 2014)."""
+    r_g = mass * _GM
+    M = mass * _GM * _CSQ / _G
+    R = radius * _KM
+    Omega = _2PI * frequency
+    d = distance * _KPC
+    return dict(M=M, r_g=r_g, r_s=2.0 * r_g, R=R, R_r_s=R / (2.0 * r_g), f=frequency,
+                Omega=Omega, i=math.acos(cos_inclination), d=d, d_sq=d * d, zeta=r_g / R,
+                epsilon=Omega ** 2.0 * R ** 3.0 / (_G * M))
+
+
 def _effective_gravity_bounds(R, zeta, eps):
     c = _C
     out = []
@@ -184,15 +199,10 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
         p = params[v]
         Msun, Rkm, f, cosi, Dkpc = (p[col[k]] for k in ("mass", "radius", "frequency",
                                                          "cos_inclination", "distance"))
-        r_g = Msun * _GM
-        r_s = 2.0 * r_g
-        R = Rkm * _KM
-        Mkg = Msun * _GM * _CSQ / _G
-        Om = _2PI * f
-        zeta = r_g / R
-        eps = Om ** 2.0 * R ** 3.0 / (_G * Mkg)
-        star = dict(r_s=r_s, R=R, Omega=Om, zeta=zeta, eps=eps, inclination=math.acos(cosi),
-                    d_sq=(Dkpc * _KPC) ** 2, f=f)
+        sp = spacetime(Msun, Rkm, f, cosi, Dkpc)
+        R, zeta, eps = sp["R"], sp["zeta"], sp["epsilon"]
+        star = dict(r_s=sp["r_s"], R=R, Omega=sp["Omega"], zeta=zeta, eps=eps,
+                    inclination=sp["i"], d_sq=sp["d_sq"], f=f)
         stars.append(star)
         if atm is not None and any(r.atm_ext == 2 for r in model.regions):
             # Photosphere.py:486-507
@@ -213,7 +223,8 @@ def prepare(model: Model, params: np.ndarray, n_threads: int = 0,
             else:
                 o_r = o_c = o_a = 0.0
             pend.append((AllocRequest(r.sqrt_num_cells ** 2, r.min_sqrt_num_cells,
-                                      r.max_sqrt_num_cells, R, Om, zeta, eps, 0, rad, 0.0,
+                                      r.max_sqrt_num_cells, R, sp["Omega"], zeta, eps, 0, rad,
+                                      0.0,
                                       colat, colat, -0.0, o_c, o_r, o_a),
                          dict(colat=colat, rad=rad, o_r=o_r, o_c=o_c, o_a=o_a),
                          dict(v=v, h=h, logT=logT, shift=shift, omit_azimuth=o_a,
