@@ -30,6 +30,11 @@ Cases
                  plain blackbody with a correction.
   gaussian       the Gaussian likelihoods of polarimetry.
   split          the split integrator with a synthetic 5-D split atmosphere.
+  energy_arrays  the integrators' energies over several wavebands (gaps, a
+                 maximum energy) and the waveband a response and channel range
+                 select.
+  beaming        the integrator with beaming options 1-3 on config1's and
+                 num4d_omit's inputs.
   config1        the blackbody workload of the small plain configuration
                  (M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot 1.0/0.075/6.1;
                  32 cells, 64 leaves, 512 rays, 64 energies; 300 x 64 response;
@@ -236,6 +241,96 @@ def meshes(xpsi):
         out[f"m{k}_effGrav"] = g
     out["n_members"] = len(members)
     save("meshes", **out)
+
+
+# beaming-modification parameters (abb, bbb, cbb, dbb, nimu) appended to the
+# cell vectors for the beaming fixture
+BEAM_PARAMS = (0.3, -0.2, 0.5, 0.3, 20.0)
+
+
+# waveband sets for the energy-array fixture: (num_energies, max_energy,
+# [(lower, upper, n_edges), ...])
+ENERGY_CASES = (
+    (64, None, [(0.1, 10.0, 65)]),
+    (100, None, [(0.3, 12.0, 40), (0.1, 3.0, 30)]),
+    (128, None, [(0.6, 10.0, 50), (0.1, 0.5, 20)]),
+    (200, None, [(2.2, 12.0, 30), (0.8, 2.0, 25), (0.2, 0.7, 10)]),
+    (200, 2.1, [(2.2, 12.0, 30), (0.8, 2.0, 25), (0.2, 0.7, 10)]),
+    (200, 1.5, [(2.2, 12.0, 30), (0.8, 2.0, 25), (0.2, 0.7, 10)]),
+    (128, 20.0, [(0.6, 10.0, 50), (0.1, 0.5, 20)]),
+    (90, None, [(0.5, 8.0, 17), (0.2, 0.9, 9), (8.5, 15.0, 12)]),
+)
+# (the reference subtracts the gaps' widths in keV from a log10 span, so
+# gaps are kept narrow here: wide ones drive its interval negative)
+
+
+def energy_arrays(xpsi):
+    """The reference's construct_energy_array (Signal.py:1092-1197) over the
+    waveband sets of ENERGY_CASES (overlapping bands, coverage gaps, a
+    maximum energy inside a gap, inside a band and above all bands), and its
+    Signal._identify_waveband (Signal.py:324-354) on responses whose edge
+    channels have leading and trailing zero columns."""
+    from types import SimpleNamespace
+    from xpsi.Signal import Signal, construct_energy_array
+
+    class _Sig:  # compared by identity, as list.remove in the reference needs
+        def __init__(self, e):
+            self.energy_edges = e
+    rng = np.random.default_rng(8)
+    out = {"n_cases": len(ENERGY_CASES)}
+    for c, (num, emax, bands) in enumerate(ENERGY_CASES):
+        sigs = []
+        for b, (lo, hi, n) in enumerate(bands):
+            e = np.sort(np.exp(rng.uniform(np.log(lo), np.log(hi), n)))
+            e[0], e[-1] = lo, hi
+            out[f"c{c}_band{b}"] = e
+            sigs.append(_Sig(e))
+        out[f"c{c}_energies"] = construct_energy_array(num, list(sigs), emax)
+    for c, (K, q, rng_ch) in enumerate(((40, 30, (0, 40)), (40, 30, (5, 33)), (25, 50, (3, 4)))):
+        M = rng.uniform(0.1, 1.0, (K, q))
+        M[:, :3] = 0.0
+        M[:, -4:] = 0.0
+        M[rng_ch[0], 3:6] = 0.0
+        M[rng_ch[1] - 1, -8:] = 0.0
+        edges = np.logspace(-1, 1, q + 1)
+        obj = SimpleNamespace(_data=SimpleNamespace(index_range=rng_ch),
+                              _instrument=SimpleNamespace(matrix=M, energy_edges=edges))
+        Signal._identify_waveband(obj)
+        out[f"w{c}_matrix"] = M
+        out[f"w{c}_edges"] = edges
+        out[f"w{c}_index_range"] = np.array(rng_ch)
+        out[f"w{c}_range"] = np.array(obj._input_interval_range)
+        out[f"w{c}_energy_edges"] = obj._energy_edges
+    out["n_wave"] = 3
+    save("energy_arrays", **out)
+
+
+def beaming(xpsi):
+    """The hot-region integrator with the reference's beaming options 1-3
+    (hot_wrapper.pyx:153-199) on config1's blackbody inputs and num4d_omit's
+    Num4D inputs (read from their fixtures), the cell vectors extended with
+    BEAM_PARAMS as columns 2-6."""
+    from xpsi.cellmesh.integrator_for_azimuthal_invariance import integrate
+    out = {"beam_params": np.array(BEAM_PARAMS)}
+    for case in ("config1", "num4d_omit"):
+        with np.load(os.path.join(HERE, case + ".npz")) as z:
+            f = {k: z[k] for k in z.files}
+        prm = np.ascontiguousarray(np.concatenate(
+            [f["params"], np.broadcast_to(np.array(BEAM_PARAMS), f["params"].shape[:2] + (5,))],
+            axis=2))
+        atm = ((f["atm_logT"], f["atm_logg"], f["atm_mu"], f["atm_logE"], f["atm_I"])
+               if case == "num4d_omit" else ())
+        for opt in (1, 2, 3):
+            st, flux = integrate(1, float(f["R"]), float(f["Omega"]), float(f["r_s"]),
+                                 float(f["inclination"]), f["cellArea"], f["radius"], f["u"],
+                                 f["theta"], f["phi"], prm, f["radiates"], None, int(f["N_R"]),
+                                 f["deflection"], f["cos_alpha"], f["lag"], f["maxDeflection"],
+                                 f["cos_gamma"], f["energies"], f["leaves"], f["phases"], atm,
+                                 None, int(f["atm_ext"]), None, opt,
+                                 int(f["image_order_limit"]) or None)
+            assert st == 0
+            out[f"{case}_opt{opt}"] = flux
+    save("beaming", **out)
 
 
 def num4d_omit(xpsi):
@@ -761,6 +856,8 @@ def main():
     split_iqu(xpsi)
     general_iqu(xpsi)
     interpolators(xpsi)
+    beaming(xpsi)
+    energy_arrays(xpsi)
 
 
 if __name__ == "__main__":

@@ -74,6 +74,86 @@ class ElsewhereSpec:
     image_order_limit: Optional[int] = None
 
 
+def identify_waveband(matrix, energy_edges, index_range=None):
+    """The input intervals a signal integrates over (Signal._identify_waveband,
+    Signal.py:324-354): from the data's channel range [a, b), the first input
+    column with a nonzero response in channel a and the last with one in
+    channel b - 1.  Returns ((first, end) input-interval range, the energy
+    edges [end - first + 1])."""
+    M = np.asarray(matrix)
+    a, b = (0, M.shape[0]) if index_range is None else index_range
+
+    def search(i, j, k):
+        while M[i, j] == 0.0:
+            j += k
+        return j
+
+    lo = search(a, 0, 1)
+    hi = M.shape[1] + search(b - 1, -1, -1) + 1
+    return (lo, hi), np.asarray(energy_edges)[lo:hi + 1]
+
+
+def construct_energy_array(num_energies, wavebands, max_energy=None):
+    """Photon energies for the integrators, distributed over the union of the
+    signals' wavebands (Signal.construct_energy_array, Signal.py:1092-1197).
+
+    wavebands: the energy-edge arrays of the signals (any order).  As the
+    reference does: the bands are ordered by upper limit; a gap between a
+    band's upper limit and the lowest lower limit of the bands above it is a
+    coverage gap; max_energy (if below the highest limit) caps the range,
+    falling to the bottom of a gap it lands in; the log10 span less the gaps'
+    widths (the reference subtracts the gaps' widths in keV, not in log10)
+    shares num_energies between the covered intervals, each getting
+    ceil(fraction x num_energies) log-spaced energies.  Returns them
+    ascending."""
+    bands = [np.asarray(e, dtype=np.float64) for e in wavebands]
+    if not bands:
+        raise ValueError("at least one waveband is needed")
+    ordered, gaps = [], []
+    remaining = list(bands)
+    MIN = None
+    while remaining:
+        k = 0
+        for i in range(1, len(remaining)):
+            if remaining[i][-1] > remaining[k][-1]:
+                k = i
+        top = remaining.pop(k)
+        ordered.append(top)
+        if len(ordered) > 1:
+            for e in ordered[:-1]:
+                if MIN is None or e[0] < MIN:
+                    MIN = e[0]
+            if top[-1] < MIN:
+                gaps.append((top[-1], MIN))
+    hi = ordered[0][-1]
+    if max_energy is not None and max_energy < hi:
+        MAX = max_energy
+        kept = []
+        for g in gaps:
+            if g[0] < MAX <= g[1]:
+                MAX = g[0]
+            if MAX > g[1]:
+                kept.append(g)
+        gaps = kept
+    else:
+        MAX = hi
+    for e in ordered:
+        if MIN is None or e[0] < MIN:
+            MIN = e[0]
+    interval = np.log10(MAX) - np.log10(MIN)
+    for g in gaps:
+        interval -= (g[1] - g[0])
+    energies = np.array([])
+    for i in range(len(gaps) + 1):
+        U = MAX if i == 0 else gaps[i - 1][0]
+        L = MIN if i == len(gaps) else gaps[i][1]
+        frac = (np.log10(U) - np.log10(L)) / interval
+        num = int(math.ceil(frac * num_energies))
+        energies = np.append(energies, np.logspace(np.log10(L), np.log10(U), int(num),
+                                                   base=10.0)[::-1])
+    return np.ascontiguousarray(energies[::-1])
+
+
 @dataclass
 class Instrument:
     matrix: np.ndarray               # [K, q] response (channels x input intervals)
@@ -113,10 +193,10 @@ class Model:
             if e.num_rays < 3:
                 raise ValueError("elsewhere num_rays must be at least 3")
         if self.energies is None:
-            e = self.instrument.energy_edges
-            # construct_energy_array for one waveband (Signal.py:1092-1197)
-            self.energies = np.logspace(math.log10(e[0]), math.log10(e[-1]),
-                                        int(math.ceil(self.num_energies)))
+            # the signal's waveband and the integrators' energies
+            # (Signal.py:324-354, 1092-1197; Likelihood.py:102-104)
+            _, edges = identify_waveband(self.instrument.matrix, self.instrument.energy_edges)
+            self.energies = construct_energy_array(self.num_energies, [edges])
         leaves = {r.num_leaves for r in self.regions}
         rays = {r.num_rays for r in self.regions}
         if len(leaves) != 1 or len(rays) != 1:
