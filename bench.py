@@ -578,7 +578,7 @@ def serving_models():
     return models
 
 
-def serve_once(models, rate, window, max_batch, precision, seed):
+def serve_once(models, rate, window, max_batch, precision, seed, deadline=300.0):
     """Poisson arrivals at `rate` req/s for `window` s, batch sizes
     log-uniform on [1, max_batch], models drawn evenly; returns the
     serving record (all requests run to completion)."""
@@ -607,10 +607,18 @@ def serve_once(models, rate, window, max_batch, precision, seed):
         while time.perf_counter() - t0 < t:
             time.sleep(0.0002)
         futs.append(srv.submit(name, p))
+    done = 0
     for f in futs:
-        f.result(timeout=1800)
+        left = deadline - (time.perf_counter() - t0)
+        try:
+            f.result(timeout=max(1.0, left))
+            done += 1
+        except Exception:  # noqa: BLE001 - recorded, the leg is bounded
+            break
     wall = time.perf_counter() - t0
     srv.close()
+    if done < len(futs):
+        return {"incomplete": f"{done} of {len(futs)} requests finished within {deadline} s"}
     lat = srv.latency_percentiles()
     nv = sum(p.shape[0] for _, _, p in reqs)
     return {"p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"], "requests": len(reqs),
@@ -714,6 +722,76 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def _cpu_worker(args):
+    """One single-threaded oracle process over its share of the vectors for
+    `seconds`: (evaluations, seconds)."""
+    model_kind, params, seconds = args
+    sys.path.insert(0, HERE)
+    from xpsi_gb300 import synthetic as SY
+    model = SY.config2_model() if model_kind == 2 else SY.config1_model()
+    if model_kind == 2:
+        oracle_data(model, 1)
+    else:
+        _oracle_data_config1(model, 1)
+    n, t = 0, 0.0
+    for v in range(params.shape[0]):
+        ll, st, dt = oracle_evals(model, params[v:v + 1], 1, 0.0)
+        n += 1
+        t += dt
+        if t >= seconds:
+            break
+    return n, t
+
+
+def _oracle_data_config1(model, n_threads):
+    from oracle import pipeline as OP
+    from oracle import prepare as OPR
+    from xpsi_gb300 import synthetic as SY
+    P0 = OPR.prepare(model, SY.config1_vector()[None, :], n_threads=n_threads)
+    _, _, stages = OP.loglike(model, P0, n_threads=n_threads, return_stages=True)
+    SY.attach_data(model, [stages[0]["folded"]], P0.shifts[0])
+    return model
+
+
+def run_cpu_configs(args):
+    """The reference path's CPU cost per configuration through the oracle
+    (meshes included) on this host: latency (one process on all cores,
+    median of repeated evaluations of the configuration's vector) and
+    throughput (one single-threaded process per core over distinct prior
+    vectors)."""
+    import multiprocessing as mp
+    from xpsi_gb300 import synthetic as SY
+    cores = os.cpu_count() or 1
+    out = {"cores": cores, "kind": "port (oracle/, its own meshes and every restated stage)"}
+    for kind in (1, 2):
+        model = SY.config1_model() if kind == 1 else SY.config2_model()
+        vec = SY.config1_vector() if kind == 1 else SY.config2_vector(seed=1)
+        (_oracle_data_config1 if kind == 1 else oracle_data)(model, cores)
+        lat = []
+        for _ in range(args.cpu_reps):
+            _, _, t = oracle_evals(model, vec[None, :], cores, 0.0)
+            lat.append(t)
+        if kind == 1:
+            rng = np.random.default_rng(3)
+            prm = np.repeat(vec[None, :], 64 * cores, axis=0)
+            prm[:, 5] = rng.uniform(0.5, 2.5, prm.shape[0])
+            prm[:, 6] = rng.uniform(0.03, 0.3, prm.shape[0])
+        else:
+            prm = SY.config3_vectors(64 * cores, seed=3)
+        shares = [(kind, prm[c::cores], args.cpu_budget) for c in range(cores)]
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_cpu_worker, shares)
+        n = sum(r[0] for r in res)
+        thr = sum(r[0] / r[1] for r in res if r[1] > 0)
+        out[f"config{kind}"] = {"latency_s_median": statistics.median(lat),
+                                "latency_samples": len(lat), "throughput_evals_per_s": thr,
+                                "throughput_evaluations": n,
+                                "throughput_vectors": "config 1: the vector with spot colatitude "
+                                "U(0.5, 2.5) and radius U(0.03, 0.3)" if kind == 1 else
+                                "config 3's prior draws (seed 3)"}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -737,8 +815,14 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-window", type=float, default=0.1)
     ap.add_argument("--serve-max-batch", type=int, default=4096)
+    # per-configuration CPU latency and throughput of the reference path
+    # (oracle) on this host, instead of the benchmark
+    ap.add_argument("--cpu-configs", action="store_true")
+    ap.add_argument("--cpu-reps", type=int, default=5)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.cpu_configs:
+        run_cpu_configs(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

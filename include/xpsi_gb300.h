@@ -32,7 +32,9 @@ extern "C" {
  * atmospheres); xgpu_integrate_stokes takes the I and Q tables of atm_ext 4
  * (Pol_Num2D), which xgpu_integrate and xgpu_integrate_general also take;
  * xgpu_integrate_general_stokes; xgpu_phase_interpolator, xgpu_energy_interpolator.
- * 4: xgpu_atmos_cache_invalidate. */
+ * 4: xgpu_atmos_cache_invalidate; xgpu_integrate takes beam_opt and xgpu_mesh
+ * carries it; xgpu_poisson_loglike_batch, xgpu_poisson_likelihood_given_background;
+ * xgpu_fold_batch_tc takes a status word; xgpu_fold_tc_timeout_selftest. */
 #define XGPU_ABI_VERSION 4
 
 /* Status words of the batched layer (per parameter vector). */
@@ -43,7 +45,8 @@ enum {
   XGPU_ATMOS_BOUNDS = 3,  /* Photosphere.py:486-507 */
   XGPU_QUAD_FAIL = 4,     /* vanished marginal integral -> random llzero */
   XGPU_SLIM_CUT = 5,      /* slim early exit */
-  XGPU_BAD_INPUT = 6
+  XGPU_BAD_INPUT = 6,
+  XGPU_DEVICE_TIMEOUT = 8 /* a bounded wait in a kernel ran out */
 };
 
 int xgpu_abi_version(void);
@@ -84,7 +87,10 @@ int xgpu_compute_rays(size_t N_u, double r_s, const double *r_s_over_R,
 
 /* Replaces xpsi.cellmesh.integrator_for_azimuthal_invariance.integrate
  * (xpsi/cellmesh/integrator_for_azimuthal_invariance.pyx:70-98) for uniform
- * hot regions: beam_opt 0, no disk (R_in >= 1e6).  atm_ext 1 = blackbody,
+ * hot regions with no disk (R_in >= 1e6).  beam_opt 0-3 as the reference's
+ * (hot_wrapper.pyx:153-199); options 1-3 read (abb, bbb, cbb, dbb, nimu) from
+ * parameters 2-6 of each parallel's first radiating cell (n_params >= 7),
+ * and option 3 takes atm_ext 1 or 2.  atm_ext 1 = blackbody,
  * 2 = Num4D (atmos required), 3 = the burst blackbody's intensity
  * (hot_BB_burst.pyx), 4 = Pol_Num2D's intensity (hot_Num2D.pyx:
  * atmos->mu, logE and intensity [nmu][nE] on (mu, log10 E/keV); the other
@@ -106,7 +112,7 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination,
                    size_t N_E, const double *energies, size_t N_L,
                    const double *leaves, size_t N_P, const double *phases,
                    int atm_ext, const xgpu_atmos4d *atmos, int else_atm_ext,
-                   int image_order_limit, double *flux);
+                   int image_order_limit, int beam_opt, double *flux);
 
 /* A split atmosphere (hot_Num5D_split.pyx:77-220): grids of t_e, t_bb,
  * tau, mu and E (electron rest energies), intensity [n0][n1][n2][n3][n4]. */
@@ -310,6 +316,11 @@ typedef struct {
   double omega, inclination;
   int32_t image_order_limit, atm_ext;
   int64_t flux_off;
+  /* beaming modification of the hot intensity (hot_wrapper.pyx:153-199):
+   * 0 none; 1, 2, 3 as the reference's beam_opt, reading (abb, bbb, cbb,
+   * dbb, nimu) from parameters 2-6 of the parallel's first radiating cell
+   * (n_params >= 7); 3 takes atm_ext 1 or 2; the mixed form takes 0 only. */
+  int32_t beam_opt, reserved;
 } xgpu_mesh;
 
 /* Ray tables for n_rows packed rows (per-row u and r_s).  When lag_C and
@@ -373,7 +384,16 @@ int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges,
  * class relative error ~1e-7).  Same arguments and layouts as
  * xgpu_fold_batch; the operand splits use stream-ordered scratch memory. */
 int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int ld,
-                       const double *in, double *out, void *stream);
+                       const double *in, double *out, int32_t *status, void *stream);
+/* status (device int32, may be NULL; the caller zeroes it) of
+ * xgpu_fold_batch_tc: 1 when a bounded wait on the TMA unit or the tensor
+ * core ran out (the tile is written as NaN), 2 when the second, bounded wait
+ * for the operations in flight ran out as well.  xgpu_fold_tc_timeout_selftest
+ * runs one tile whose producer issues nothing, so that both waits run out
+ * after a short limit without any copy or MMA in flight, and returns the
+ * status word it reported (2) in *status_out: the failure path checked
+ * without a GPU fault.  No counterpart in the reference. */
+int xgpu_fold_tc_timeout_selftest(int32_t *status_out);
 
 /* out[b][K][N] = matrix[K][0:q] @ in[b][q][N] for b < batch (FP64). */
 int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix,
@@ -645,6 +665,35 @@ int xgpu_expected_counts_batch(int n_sets, int K, int B, int H,
                                const int32_t *allow_negative,
                                const double *background, double *out,
                                void *stream);
+/* Poisson log-likelihood of data counts[K][B] (device) given the expected
+ * counts[n_sets][K][B] (star plus a known background, device) of n_sets
+ * evaluations, the core of xpsi.likelihoods._poisson_likelihood_given_background
+ * (xpsi/likelihoods/_poisson_likelihood_given_background.pyx:82-109):
+ * loglike[set] = sum_i (precomp[i] + sum_j over E_ij > 0 of d_ij log E_ij -
+ * E_ij), precomp (neg_sum_ln_data_factorial) may be NULL; n_penalty[set]
+ * counts the bins with E_ij <= 0 that are not d_ij == E_ij == 0, each of
+ * which the reference penalises by -1e90 (0.1 + 0.9 U(0, 1)) (left to the
+ * caller, as it is random). */
+int xgpu_poisson_loglike_batch(int n_sets, int K, int B, const double *expected,
+                               const double *counts, const double *precomp, double *loglike,
+                               int32_t *n_penalty, void *stream);
+
+/* Replaces the numerical part of
+ * xpsi.likelihoods._poisson_likelihood_given_background.poisson_likelihood_given_background
+ * (xpsi/likelihoods/_poisson_likelihood_given_background.pyx:14-109), HOST
+ * arrays: expected[K][B] = compute_expected_counts(exposure_time, phases,
+ * components, background, allow_negative) as xgpu_compute_expected_counts
+ * forms it, *loglike the log-likelihood before penalties, *n_penalty the
+ * number of penalised bins (see xgpu_poisson_loglike_batch). */
+int xgpu_poisson_likelihood_given_background(double exposure_time, size_t B,
+                                             const double *phases, size_t K,
+                                             const double *counts, size_t H,
+                                             const xgpu_component *components,
+                                             const double *background,
+                                             const double *neg_sum_ln_data_factorial,
+                                             const int32_t *allow_negative, double *expected,
+                                             double *loglike, int64_t *n_penalty);
+
 /* fail (device int32, may be NULL) is set to 1 if a draw hit the bound. */
 int xgpu_poisson_batch(int64_t n, const double *mean, double *out,
                        uint64_t seed, uint64_t offset, int32_t *fail,

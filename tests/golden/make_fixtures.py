@@ -33,6 +33,8 @@ Cases
   energy_arrays  the integrators' energies over several wavebands (gaps, a
                  maximum energy) and the waveband a response and channel range
                  select.
+  poisson_given_background  the Poisson likelihood with a known background
+                 on config1's signal and data.
   beaming        the integrator with beaming options 1-3 on config1's and
                  num4d_omit's inputs.
   config1        the blackbody workload of the small plain configuration
@@ -303,6 +305,38 @@ def energy_arrays(xpsi):
         out[f"w{c}_energy_edges"] = obj._energy_edges
     out["n_wave"] = 3
     save("energy_arrays", **out)
+
+
+def poisson_given_background(xpsi):
+    """The reference's poisson_likelihood_given_background
+    (_poisson_likelihood_given_background.pyx:14-113) on config1's registered
+    signal, data and phases: a background of 10 % of each channel's mean
+    source rate, with and without the data-factorial constants, and a case
+    whose first channels have no signal, no background and no counts (no
+    penalty).  (The penalty branch, :107-108, converts a 1-element array to
+    a C double, which numpy >= 2 refuses; the reference pins numpy < 2, so
+    that branch is not run here.)"""
+    from xpsi.likelihoods._poisson_likelihood_given_background import (
+        poisson_likelihood_given_background as plgb)
+    with np.load(os.path.join(HERE, "config1.npz")) as z:
+        f = {k: z[k] for k in z.files}
+    reg = np.ascontiguousarray(f["folded"])  # the registered count rates [K, N_P]
+    counts = np.ascontiguousarray(f["counts"].astype(np.float64))
+    B = f["phase_edges"].size - 1
+    bg = np.ascontiguousarray(np.repeat(0.1 * reg.mean(axis=1, keepdims=True), B, axis=1))
+    args = lambda r, c, b: (float(f["exposure"]), f["phase_edges"], c, [r], [f["comp_phases"]],
+                            np.ascontiguousarray(f["shifts"]), b)
+    out = dict(registered=reg, counts=counts, background=bg, exposure=f["exposure"],
+               phase_edges=f["phase_edges"], comp_phases=f["comp_phases"], shifts=f["shifts"],
+               precomp=f["precomp"])
+    out["ll_nopre"], out["expec"] = plgb(*args(reg, counts, bg))
+    out["ll_pre"], _ = plgb(*args(reg, counts, bg), f["precomp"])
+    r0, c0, b0 = reg.copy(), counts.copy(), bg.copy()
+    r0[:3] = 0.0
+    c0[:3] = 0.0
+    b0[:3] = 0.0
+    out["ll_zero"], out["expec_zero"] = plgb(*args(r0, c0, b0), f["precomp"])
+    save("poisson_given_background", **out)
 
 
 def beaming(xpsi):
@@ -858,6 +892,7 @@ def main():
     interpolators(xpsi)
     beaming(xpsi)
     energy_arrays(xpsi)
+    poisson_given_background(xpsi)
 
 
 if __name__ == "__main__":

@@ -33,10 +33,25 @@ def test_fold_tc_matches_fp64(cuda, K, q, N, batch):
     st = torch.cuda.current_stream().cuda_stream
     L = lib()
     check(L.xgpu_fold_batch(batch, K, q, N, M.data_ptr(), q, X.data_ptr(), ref.data_ptr(), st))
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
     check(L.xgpu_fold_batch_tc(batch, K, q, N, M.data_ptr(), q, X.data_ptr(), out.data_ptr(),
-                               st))
+                               status.data_ptr(), st))
     torch.cuda.synchronize()
+    assert int(status.item()) == 0
     a, r = out.cpu().numpy(), ref.cpu().numpy()
     assert np.isfinite(a).all()
     rel = np.max(np.abs(a - r) / np.max(np.abs(r), axis=2, keepdims=True))
     assert rel <= TOL
+
+
+def test_fold_tc_timeout_path_reports_status(cuda):
+    """The failure path without a fault: a tile whose producer issues no
+    copies lets both bounded waits run out; the kernel reports status 2,
+    frees its tensor memory and returns, and the context stays usable (a
+    regular fold afterwards is correct)."""
+    import ctypes
+    from xpsi_gb300._native import lib, check
+    st = ctypes.c_int32(-1)
+    check(lib().xgpu_fold_tc_timeout_selftest(ctypes.byref(st)))
+    assert st.value == 2
+    test_fold_tc_matches_fp64(cuda, 300, 64, 64, 1)

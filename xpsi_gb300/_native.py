@@ -93,7 +93,7 @@ class Atmos5D(C.Structure):
 class Mesh(C.Structure):
     _fields_ = [("S0", I32), ("S1", I32), ("row_off", I64), ("cell_off", I64),
                 ("omega", D), ("inclination", D), ("image_order_limit", I32),
-                ("atm_ext", I32), ("flux_off", I64)]
+                ("atm_ext", I32), ("flux_off", I64), ("beam_opt", I32), ("reserved", I32)]
 
 
 class IntegrateBatchData(C.Structure):
@@ -178,7 +178,7 @@ def _bind(L):
         "xgpu_compute_rays": (C.c_int, [SZ, D, P, P, SZ, P, P, P, P]),
         "xgpu_integrate": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ, SZ,
                                      P, P, P, P, P, SZ, P, SZ, P, SZ, P, C.c_int,
-                                     C.POINTER(Atmos4D), C.c_int, C.c_int, P]),
+                                     C.POINTER(Atmos4D), C.c_int, C.c_int, C.c_int, P]),
         "xgpu_integrate_split": (C.c_int, [D, D, D, D, SZ, SZ, P, P, P, P, P, P, SZ, P, P, SZ,
                                            SZ, P, P, P, P, P, SZ, P, SZ, P, SZ, P,
                                            C.POINTER(Atmos5D), C.c_int, C.c_int, P]),
@@ -200,7 +200,8 @@ def _bind(L):
         "xgpu_fold_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
                                       P, P]),
         "xgpu_fold_batch_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P,
-                                         P, P]),
+                                         P, P, P]),
+        "xgpu_fold_tc_timeout_selftest": (C.c_int, [P]),
         "xgpu_likelihood_batch": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
         "xgpu_likelihood_batch_static": (C.c_int, [C.POINTER(LikelihoodBatchData), P]),
         "xgpu_allocate_cells": (C.c_int, [SZ, SZ, SZ, D, D, D, D, C.c_int, D, D, D, D, D, D,
@@ -241,6 +242,10 @@ def _bind(L):
         "xgpu_expected_counts_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, D, P,
                                                  C.POINTER(Component), P, P, P, P]),
         "xgpu_poisson_batch": (C.c_int, [I64, P, P, C.c_uint64, C.c_uint64, P, P]),
+        "xgpu_poisson_loglike_batch": (C.c_int, [C.c_int, C.c_int, C.c_int, P, P, P, P, P, P]),
+        "xgpu_poisson_likelihood_given_background": (C.c_int, [D, SZ, P, SZ, P, SZ,
+                                                               C.POINTER(Component), P, P, P, P,
+                                                               P, P]),
         "xgpu_closed_cell_mesh": (C.c_int, [SZ, SZ, D, D, D, C.c_int, P, P, P, P, P, P, P]),
         "xgpu_closed_cell_mesh_many": (C.c_int, [C.c_int, C.POINTER(ClosedMeshRequest),
                                                  C.c_int]),
@@ -273,7 +278,8 @@ EXPORTED = ["xgpu_abi_version", "xgpu_last_error", "xgpu_compute_rays", "xgpu_in
             "xgpu_gaussian_loglike_batch", "xgpu_integrate_split",
             "xgpu_integrate_split_stokes", "xgpu_integrate_general_stokes",
             "xgpu_phase_interpolator", "xgpu_energy_interpolator",
-            "xgpu_atmos_cache_invalidate"]
+            "xgpu_atmos_cache_invalidate", "xgpu_poisson_loglike_batch",
+            "xgpu_poisson_likelihood_given_background", "xgpu_fold_tc_timeout_selftest"]
 
 
 ABI_VERSION = 4  # XGPU_ABI_VERSION of include/xpsi_gb300.h

@@ -46,7 +46,7 @@ _KPC = 3.08567758e19
 _2PI = 2.0 * math.pi
 
 STATUS_NAMES = {0: "ok", 1: "RayError", 2: "PulseError", 3: "AtmosError", 4: "QuadFail",
-                5: "SlimCut", 6: "BadInput", 7: "IntegrationError"}
+                5: "SlimCut", 6: "BadInput", 7: "IntegrationError", 8: "DeviceTimeout"}
 
 
 @dataclass
@@ -690,9 +690,17 @@ class BatchEvaluator:
         check(L.xgpu_energy_batch(n_m, N_E, N_P, self.log10edges.numel(), p(B["flux"]),
                                   p(B["off_in"]), p(self.log10E), p(self.log10edges),
                                   p(B["d_sq"]), p(B["integrated"]), p(B["off_out"]), 0, st))
-        fold = L.xgpu_fold_batch_tc if self.precision == "mixed" else L.xgpu_fold_batch
-        check(fold(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
-                                p(B["integrated"]), p(B["folded"]), st))
+        if self.precision == "mixed":
+            if "fold_status" not in B:
+                B["fold_status"] = self.torch.zeros(1, dtype=self.torch.int32, device=self.dev)
+            else:
+                B["fold_status"].zero_()
+            check(L.xgpu_fold_batch_tc(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
+                                       p(B["integrated"]), p(B["folded"]), p(B["fold_status"]),
+                                       st))
+        else:
+            check(L.xgpu_fold_batch(n_m, self.K, self.q, N_P, p(self.matrix), self.q,
+                                    p(B["integrated"]), p(B["folded"]), st))
         if not likelihood:
             return
         m = self.model
@@ -786,6 +794,10 @@ class BatchEvaluator:
             for v in np.nonzero(est)[0]:
                 if st[v] == 0:
                     st[v] = 7
+        if "fold_status" in B and int(B["fold_status"].item()) != 0:
+            # a bounded wait in the tensor-core fold ran out: every vector's
+            # folded signal is void
+            st[st == 0] = 8
         st[P.status != 0] = P.status[P.status != 0]
         return st
 

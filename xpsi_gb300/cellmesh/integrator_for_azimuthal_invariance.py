@@ -24,10 +24,13 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
     Returns (0, flux[N_E, N_P]) or (1, None) exactly as the reference does.
     Supported: blackbody (hot_atm_ext 1), numerical 4-D (2), the burst
     blackbody's intensity (3) and Pol_Num2D's intensity table (4,
-    hot_atmosphere = (mu, log10 E, I)) hot atmospheres
-    with beam_opt 0 and no disk (R_in >= 1e6), with or without the
-    correction for a blackbody elsewhere (else_atm_ext 1).  Other options raise NotImplementedError
-    rather than silently computing something else.
+    hot_atmosphere = (mu, log10 E, I)) hot atmospheres with no disk
+    (R_in >= 1e6), with or without the correction for a blackbody elsewhere
+    (else_atm_ext 1).  beam_opt 0-3 as the reference's (hot_wrapper.pyx:
+    153-199): options 1-3 read (abb, bbb, cbb, dbb, nimu) from
+    srcCellParams[..., 2:7]; option 3 takes hot_atm_ext 1 or 2.  Other
+    options raise NotImplementedError rather than silently computing
+    something else.
     """
     require_default_interpolants(phase=True, energy=False)
     corr = None
@@ -37,8 +40,14 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         corr = f64(correction_srcCellParams)
         if corr.ndim != 3 or corr.shape[:2] != f64(cellArea).shape:
             raise ValueError("correction_srcCellParams must be [rows, cells, n_params]")
-    if int(beam_opt) != 0:
-        raise NotImplementedError("beaming options 1-3 are not on the GPU path")
+    beam = int(beam_opt)
+    if beam not in (0, 1, 2, 3):
+        raise ValueError("beam_opt must be 0, 1, 2 or 3")
+    if beam == 3 and int(hot_atm_ext) not in (1, 2):
+        raise NotImplementedError("beam_opt 3 is on the GPU path for hot_atm_ext 1 and 2")
+    if beam and f64(srcCellParams).shape[-1] < 7:
+        raise ValueError("beaming options read srcCellParams[..., 2:7] (abb, bbb, cbb, dbb, "
+                         "nimu)")
     if R_in < 1e6:
         raise NotImplementedError("disk occultation is not on the GPU path")
     atm = int(hot_atm_ext)
@@ -75,7 +84,7 @@ def integrate(numThreads, R, omega, r_s, inclination, cellArea,
         ptr(arrs[5]), ptr(arrs[6]), ptr(arrs[7]), ptr(arrs[8]), E.size, ptr(E), Lv.size,
         ptr(Lv), P.size, ptr(P), atm, C.byref(atmos) if atmos is not None else None,
         int(else_atm_ext) if corr is not None else 0,
-        int(image_order_limit) if image_order_limit is not None else 0, ptr(flux)))
+        int(image_order_limit) if image_order_limit is not None else 0, beam, ptr(flux)))
     del keep
     if st != 0:
         return (ERROR, None)

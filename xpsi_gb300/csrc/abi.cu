@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -221,6 +222,17 @@ int xgpu_integrate_batch_mixed(int n_meshes, const xgpu_mesh *meshes, int64_t n_
 }  // extern "C"
 
 namespace {
+// XGPU_CELL_SUMS=runs selects the power-sum form of the FP64 integrator's
+// cell x phase sums instead of the per-cell form (the same sums, another
+// order of summation)
+bool wsum_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("XGPU_CELL_SUMS");
+    return e && std::string(e) == "runs";
+  }();
+  return on;
+}
+
 int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, int N_R,
                          int N_E, int N_L, int N_P, const xgpu_integrate_batch_data *d,
                          int target_ctas, void *stream, int mixed, int table2d) {
@@ -240,6 +252,16 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
     if (ext == 3 && mixed) return fail_msg("the mixed integrator takes atm_ext 1 or 2");
     if (ext != 1 && ext != 2 && ext != 3 && ext != 4 && ext != 6)
       return fail_msg("atm_ext must be 1 (BB) or 2 (Num4D)");
+  }
+  for (int m = 0; m < n_meshes; m++) {
+    const int b = meshes[m].beam_opt;
+    if (b < 0 || b > 3) return fail_msg("beam_opt must be 0, 1, 2 or 3");
+    if (b > 0 && mixed) return fail_msg("the mixed integrator takes beam_opt 0 only");
+    if (b > 0 && d->n_params < 7)
+      return fail_msg("beaming options read (abb, bbb, cbb, dbb, nimu) from parameters 2-6 of "
+                      "the cell vectors: n_params must be at least 7");
+    if (b == 3 && meshes[m].atm_ext != 1 && meshes[m].atm_ext != 2)
+      return fail_msg("beam_opt 3 (numerical renormalisation) takes atm_ext 1 or 2");
   }
   if (d->correction != nullptr && mixed)
     return fail_msg("the elsewhere correction is computed by the FP64 integrator only");
@@ -279,6 +301,17 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
       (rc = dalloc(dslab, (size_t)n_chunks * d->atmos.nmu * d->atmos.nE * sizeof(double), st)))
     return rc;
   CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
+  // run records of the FP64 form's power sums, per chunk (parallels of up
+  // to 1023 cells and 1024 leaves; beyond that the per-cell form runs)
+  Dev dwsum;
+  int w_cap = 0;
+  int max_cells = 0;
+  for (int m = 0; m < n_meshes; m++) max_cells = std::max(max_cells, (int)meshes[m].S1);
+  const bool use_w = !mixed && max_cells <= 1023 && N_L <= 1024 && wsum_enabled();
+  if (use_w) {
+    const size_t w_chunk = xg::integrate_wsum_bytes(N_P, max_cells, &w_cap);
+    if ((rc = dalloc(dwsum, (size_t)n_chunks * w_chunk, st))) return rc;
+  }
 
   xg::IntegrateArgs a{};
   a.n_members = n_meshes;
@@ -309,6 +342,8 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.flux = d->flux;
   a.flop_counter = d->flop_counter;
   a.slab = d->atmos.intensity != nullptr && !table2d ? dslab.as<double>() : nullptr;
+  a.wsum = use_w ? dwsum.as<unsigned char>() : nullptr;
+  a.w_cap = w_cap;
   a.mixed = mixed;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());
@@ -339,9 +374,9 @@ int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix, int ld
 }
 
 int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int ld,
-                       const double *in, double *out, void *stream) {
+                       const double *in, double *out, int32_t *status, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  xg::FoldArgs a{batch, K, q, N, matrix, ld, in, out};
+  xg::FoldArgs a{batch, K, q, N, matrix, ld, in, out, status};
   Dev scratch;
   int rc = dalloc(scratch, xg::fold_tc_scratch_bytes(a), st);
   if (rc) return rc;
@@ -349,6 +384,28 @@ int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int
   if (rc == -5) return fail_msg("could not set the tensor-core fold's shared-memory size");
   if (rc) return fail_msg("tensor-map encoding failed for the tensor-core fold");
   CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_fold_tc_timeout_selftest(int32_t *status_out) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  const int K = 8, q = 8, N = 8;
+  xg::FoldArgs a{1, K, q, N, nullptr, q, nullptr, nullptr, nullptr};
+  Dev dout, dst, scratch;
+  if ((rc = dalloc(dout, (size_t)K * N * 8, st)) || (rc = dalloc(dst, 4, st)) ||
+      (rc = dalloc(scratch, xg::fold_tc_scratch_bytes(a), st)))
+    return rc;
+  CK(cudaMemsetAsync(scratch.p, 0, xg::fold_tc_scratch_bytes(a), st));
+  CK(cudaMemsetAsync(dst.p, 0, 4, st));
+  a.out = dout.as<double>();
+  a.status = dst.as<int32_t>();
+  rc = xg::launch_fold_tc_timeout_selftest(a, scratch.p, st);
+  if (rc) return fail_msg("could not launch the tensor-core fold's timeout self-test");
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(status_out, dst.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
   return 0;
 }
 
@@ -502,7 +559,7 @@ int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
                    const double *maxDeflection, const double *cos_gamma, size_t N_E,
                    const double *energies, size_t N_L, const double *leaves, size_t N_P,
                    const double *phases, int atm_ext, const xg::Atmos4D &A,
-                   int else_atm_ext, int image_order_limit, double *flux) {
+                   int else_atm_ext, int image_order_limit, int beam_opt, double *flux) {
   int rc;
   if (n_params < 2) return fail_msg("srcCellParams needs at least 2 parameters per cell");
   if (correction && else_atm_ext != 1)
@@ -527,7 +584,7 @@ int integrate_host(cudaStream_t st, double omega, double inclination, size_t S0,
       (rc = dalloc(dst, 16, st)) || (rc = upload(drm, row_mesh.data(), S0, st)))
     return rc;
   xgpu_mesh mesh{(int32_t)S0, (int32_t)S1, 0, 0, omega, inclination, image_order_limit,
-                 atm_ext, 0};
+                 atm_ext, 0, beam_opt, 0};
   xgpu_integrate_batch_data d{};
   d.row_mesh = drm.as<int32_t>();
   d.radius = drad.as<double>(); d.u = du.as<double>(); d.cos_gamma = dcg.as<double>();
@@ -567,7 +624,7 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
                    const double *maxDeflection, const double *cos_gamma, size_t N_E,
                    const double *energies, size_t N_L, const double *leaves, size_t N_P,
                    const double *phases, int atm_ext, const xgpu_atmos4d *atmos,
-                   int else_atm_ext, int image_order_limit, double *flux) {
+                   int else_atm_ext, int image_order_limit, int beam_opt, double *flux) {
   cudaStream_t st;
   int rc;
   if ((rc = lib_stream(&st))) return rc;
@@ -583,7 +640,7 @@ int xgpu_integrate(double R, double omega, double r_s, double inclination, size_
                         phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
                         deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
                         N_L, leaves, N_P, phases, atm_ext, A, else_atm_ext, image_order_limit,
-                        flux);
+                        beam_opt, flux);
 }
 
 int xgpu_integrate_split(double R, double omega, double r_s, double inclination, size_t S0,
@@ -610,7 +667,8 @@ int xgpu_integrate_split(double R, double omega, double r_s, double inclination,
   return integrate_host(st, omega, inclination, S0, S1, cellArea, radius, r_s_over_r, theta,
                         phi, srcCellParams, n_params, radiates, correction, n_correction, N_R,
                         deflection, cos_alpha, lag, maxDeflection, cos_gamma, N_E, energies,
-                        N_L, leaves, N_P, phases, 6, A, else_atm_ext, image_order_limit, flux);
+                        N_L, leaves, N_P, phases, 6, A, else_atm_ext, image_order_limit, 0,
+                        flux);
 }
 
 }  // extern "C"
@@ -1280,6 +1338,60 @@ int xgpu_compute_expected_counts(double exposure_time, size_t B, const double *p
   if (rc) return rc;
   CK(cudaMemcpyAsync(out, dout.p, K * B * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int xgpu_poisson_loglike_batch(int n_sets, int K, int B, const double *expected,
+                               const double *counts, const double *precomp, double *loglike,
+                               int32_t *n_penalty, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_sets <= 0 || K <= 0) return 0;
+  if (B <= 0) return fail_msg("at least one phase bin is needed");
+  Dev dll, dpen;
+  int rc;
+  if ((rc = dalloc(dll, (size_t)n_sets * K * 8, st)) ||
+      (rc = dalloc(dpen, (size_t)n_sets * K * 4, st)))
+    return rc;
+  xg::PoissonArgs a{n_sets, K, B, expected, counts, precomp, dll.as<double>(),
+                    dpen.as<int32_t>(), loglike, n_penalty};
+  xg::launch_poisson_loglike(a, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int xgpu_poisson_likelihood_given_background(double exposure_time, size_t B,
+                                             const double *phases, size_t K,
+                                             const double *counts, size_t H,
+                                             const xgpu_component *components,
+                                             const double *background,
+                                             const double *neg_sum_ln_data_factorial,
+                                             const int32_t *allow_negative, double *expected,
+                                             double *loglike, int64_t *n_penalty) {
+  cudaStream_t st;
+  int rc;
+  if ((rc = lib_stream(&st))) return rc;
+  if (K == 0 || B == 0) {
+    *loglike = 0.0;
+    *n_penalty = 0;
+    return 0;
+  }
+  if ((rc = xgpu_compute_expected_counts(exposure_time, B, phases, K, H, components, background,
+                                         allow_negative, expected)))
+    return rc;
+  Dev dE, dC, dP, dL, dN;
+  if ((rc = upload(dE, expected, K * B, st)) || (rc = upload(dC, counts, K * B, st)) ||
+      (neg_sum_ln_data_factorial && (rc = upload(dP, neg_sum_ln_data_factorial, K, st))) ||
+      (rc = dalloc(dL, 8, st)) || (rc = dalloc(dN, 4, st)))
+    return rc;
+  rc = xgpu_poisson_loglike_batch(1, (int)K, (int)B, dE.as<double>(), dC.as<double>(),
+                                  neg_sum_ln_data_factorial ? dP.as<double>() : nullptr,
+                                  dL.as<double>(), dN.as<int32_t>(), st);
+  if (rc) return rc;
+  int32_t pen = 0;
+  CK(cudaMemcpyAsync(loglike, dL.p, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&pen, dN.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *n_penalty = pen;
   return 0;
 }
 

@@ -18,8 +18,9 @@
 // accumulator of 128 TMEM columns, committed to a second mbarrier; each
 // warp reads its 32 TMEM lanes (rows) with tcgen05.ld after every step and
 // sums the steps in registers, then stores FP64.  Every mbarrier wait is
-// bounded; on a timeout the tile is written as NaN and the kernel still
-// waits (bounded) for its copies and MMAs and frees its TMEM.
+// bounded; on a timeout the tile is written as NaN, the status word gets 1
+// (2 if the second, bounded wait for the copies and MMAs in flight runs out
+// as well) and the kernel frees its TMEM.
 #include <cuda.h>
 
 #include "common.cuh"
@@ -33,6 +34,7 @@ constexpr int kFoldThreads = 128;
 constexpr uint32_t kPartBytes = kTM * kTK * 4;  // one operand part: 128 rows x 128 B
 constexpr uint32_t kStageBytes = 4 * kPartBytes;
 constexpr long kSpinLimit = 1L << 22;
+constexpr long kSelfTestSpinLimit = 1L << 10;
 constexpr uint32_t kTmemCols = 128;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -60,8 +62,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 // bounded wait for the phase with the given parity; false on timeout
-__device__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (long i = 0; i < kSpinLimit; i++)
+__device__ bool mbar_wait(uint64_t *bar, uint32_t parity, long limit = kSpinLimit) {
+  for (long i = 0; i < limit; i++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -187,9 +189,12 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
 constexpr uint32_t kIdescTf32 =
     (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
 
+// selftest: the producer issues no copies and its waits give up after a
+// short limit (the timeout path, with nothing in flight)
 __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
     const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-    int K, int q_pad, int rows_a, int rows_b, int N, long cols, double *out) {
+    int K, int q_pad, int rows_a, int rows_b, int N, long cols, double *out, int32_t *status,
+    int selftest) {
   extern __shared__ __align__(1024) unsigned char fsm[];
   __shared__ __align__(8) uint64_t bar_full, bar_mma;
   __shared__ uint32_t s_tmem;
@@ -232,15 +237,19 @@ __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
   // the barrier that follows the write, so all threads leave together
   for (int kb = 0; kb < nkb; kb++) {
     if (threadIdx.x == 0) {
-      mbar_expect_tx(&bar_full, kStageBytes);
-      const int x = kb * kTK;
-      tma_load_2d(sA_hi, &mapA, x, m0, &bar_full);
-      tma_load_2d(sA_lo, &mapA, x, rows_a + m0, &bar_full);
-      tma_load_2d(sB_hi, &mapB, x, (int)n0, &bar_full);
-      tma_load_2d(sB_lo, &mapB, x, rows_b + (int)n0, &bar_full);
-      if (!mbar_wait(&bar_full, (uint32_t)(kb & 1))) {
+      const long limit = selftest ? kSelfTestSpinLimit : kSpinLimit;
+      if (!selftest) {
+        mbar_expect_tx(&bar_full, kStageBytes);
+        const int x = kb * kTK;
+        tma_load_2d(sA_hi, &mapA, x, m0, &bar_full);
+        tma_load_2d(sA_lo, &mapA, x, rows_a + m0, &bar_full);
+        tma_load_2d(sB_hi, &mapB, x, (int)n0, &bar_full);
+        tma_load_2d(sB_lo, &mapB, x, rows_b + (int)n0, &bar_full);
+      }
+      if (!mbar_wait(&bar_full, (uint32_t)(kb & 1), limit)) {
         s_fail = 1;
-        mbar_wait(&bar_full, (uint32_t)(kb & 1));  // let the copy land (bounded)
+        // let the copy land (bounded); if it does not, say so
+        if (!mbar_wait(&bar_full, (uint32_t)(kb & 1), limit)) s_fail = 2;
       }
     }
     __syncthreads();
@@ -259,7 +268,8 @@ __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
         mma_commit(&bar_mma);
         if (!mbar_wait(&bar_mma, (uint32_t)(step & 1))) {
           s_fail = 1;
-          mbar_wait(&bar_mma, (uint32_t)(step & 1));  // let the MMAs finish (bounded)
+          // let the MMAs finish (bounded); if they do not, say so
+          if (!mbar_wait(&bar_mma, (uint32_t)(step & 1))) s_fail = 2;
         }
       }
       tc_fence_before();
@@ -281,6 +291,7 @@ __global__ void __launch_bounds__(kFoldThreads) fold_tc_kernel(
   }
   tc_fence_after();
   const bool fail = s_fail != 0;
+  if (fail && threadIdx.x == 0 && status != nullptr) atomicMax(status, s_fail);
   if (m < K) {
 #pragma unroll
     for (int c = 0; c < kTN; c++) {
@@ -365,7 +376,29 @@ int launch_fold_tc(const FoldArgs &a, void *scratch, cudaStream_t st) {
     return -5;
   dim3 grid((unsigned)(rows_b / kTN), (unsigned)(rows_a / kTM));
   fold_tc_kernel<<<grid, kFoldThreads, smem, st>>>(mapA, mapB, a.K, k_pad, rows_a,
-                                                   (int)rows_b, a.N, cols, a.out);
+                                                   (int)rows_b, a.N, cols, a.out, a.status, 0);
+  return 0;
+}
+
+int launch_fold_tc_timeout_selftest(const FoldArgs &a, void *scratch, cudaStream_t st) {
+  if (a.batch <= 0 || a.K <= 0 || a.N <= 0 || a.status == nullptr) return -3;
+  const int rows_a = (a.K + kTM - 1) / kTM * kTM;
+  const long cols = (long)a.batch * a.N;
+  const long rows_b = (cols + kTN - 1) / kTN * kTN;
+  const int k_pad = (a.q + kTK - 1) / kTK * kTK;
+  float *A2 = static_cast<float *>(scratch);
+  float *B2 = A2 + (size_t)2 * rows_a * k_pad;
+  CUtensorMap mapA, mapB;
+  if (make_map(&mapA, A2, 2 * rows_a, k_pad) || make_map(&mapB, B2, (int)(2 * rows_b), k_pad))
+    return -4;
+  const size_t smem = kStageBytes + 1024;
+  if (cudaFuncSetAttribute(fold_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -5;
+  // one tile: its waits run out, the kernel reports and returns
+  fold_tc_kernel<<<dim3(1, 1), kFoldThreads, smem, st>>>(mapA, mapB, a.K, k_pad, rows_a,
+                                                         (int)rows_b, a.N, cols, a.out, a.status,
+                                                         1);
   return 0;
 }
 

@@ -809,6 +809,198 @@ __device__ __forceinline__ bool cell_phase_sums_df(const CP &cp, const AR &area,
 }
 
 // ---------------------------------------------------------------------------
+// Power-sum form of the FP64 path's cell x phase sums.  At a signal phase k
+// the cells of a parallel fall, in azimuth order, into runs of consecutive
+// radiating cells whose wrapped phase lies in the same knot interval iv (a
+// run ends where the interval changes).  Over a run every energy row
+// evaluates the same cubic piece, so
+//     sum_j A_j S_E(t_j) = y W0 + k1 W1 + k2 W2 + k3 W3,  Wp = sum_j A_j t_j^p,
+// and the power sums Wp depend on the geometry only: they are formed once
+// per (parallel, image) and reused by all N_E energies.  This holds where
+// the reference adds every value (the elsewhere correction) or where the
+// piece is positive on its whole interval; a piece that is <= 0 on its whole
+// interval adds nothing.  A piece whose sign changes inside its interval is
+// evaluated cell by cell over the run, with the reference's test (:593-594).
+// The sign of a piece on [0, h] is bounded by its Bernstein coefficients
+// (the curve lies in their convex hull), with a margin of 1e-5 of the
+// piece's scale so that rounding cannot flip the classification.
+//
+// Run records live in global scratch, per chunk: for cell half c (the two
+// halves of the parallel's cells are walked by different threads) and run r
+// of phase k, record (c w_cap + r) N_P + k (consecutive phases adjacent, so a
+// warp's tasks load them coalesced): two float4 with the float pairs of
+// W0, W1 and W2, W3, and an int with the interval (bits 0-9), the first
+// cell (bits 10-19) and the cell span (bits 20-29).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline size_t integrate_wsum_bytes_dev(int N_P, int cap) {
+  const size_t n = (size_t)2 * cap * N_P;
+  return (n * (2 * sizeof(float4) + sizeof(int)) + 255) & ~size_t(255);
+}
+
+struct WRuns {
+  float4 *wa, *wb;
+  int *meta;
+  int cap, N_P;
+  __device__ __forceinline__ size_t rec(int half, int r, int k) const {
+    return ((size_t)half * cap + r) * N_P + k;
+  }
+};
+
+__device__ __forceinline__ WRuns wruns_of(unsigned char *base, int cap, int N_P) {
+  const size_t n = (size_t)2 * cap * N_P;
+  WRuns w;
+  w.wa = reinterpret_cast<float4 *>(base);
+  w.wb = w.wa + n;
+  w.meta = reinterpret_cast<int *>(w.wb + n);
+  w.cap = cap;
+  w.N_P = N_P;
+  return w;
+}
+
+// piece classes: 0 adds nothing, 1 power sums, 2 cell by cell
+__device__ __forceinline__ uint8_t piece_class(const PieceDF &q, float h) {
+  const float y = q.y.h, a1 = q.k1.h * h, a2 = q.k2.h * h * h, a3 = q.k3.h * h * h * h;
+  const float scale = fabsf(y) + fabsf(a1) + fabsf(a2) + fabsf(a3);
+  if (scale == 0.0f) return 0;
+  const float b1 = y + a1 * (1.0f / 3.0f);
+  const float b2 = y + a1 * (2.0f / 3.0f) + a2 * (1.0f / 3.0f);
+  const float b3 = y + a1 + a2 + a3;
+  const float lo = fminf(fminf(y, b1), fminf(b2, b3));
+  const float hi = fmaxf(fmaxf(y, b1), fmaxf(b2, b3));
+  const float margin = 1.0e-5f * scale;
+  if (lo > margin) return 1;
+  if (hi < -margin) return 0;
+  return 2;
+}
+
+// the runs of signal phase k over cells [jb, je) of the parallel; returns
+// the number of runs written, or -1 when a cell phase cannot be wrapped
+// into the knot range (the reference's terminate)
+template <typename CP, typename AR>
+__device__ __forceinline__ int build_runs(const CP &cp, const AR &area, int jb, int je,
+                                          const int32_t *rad, const WRuns &w, int half, int k) {
+  int n = 0, cur = -1, j0 = 0, span = 0, hint = -1;
+  const DF zero{0.0f, 0.0f};
+  DF w0 = zero, w1 = zero, w2 = zero, w3 = zero;
+  auto flush = [&]() {
+    const size_t r = w.rec(half, n, k);
+    w.wa[r] = make_float4(w0.h, w0.l, w1.h, w1.l);
+    w.wb[r] = make_float4(w2.h, w2.l, w3.h, w3.l);
+    w.meta[r] = cur | (j0 << 10) | (span << 20);
+    n++;
+  };
+  for (int j = jb; j < je; j++) {
+    if (rad[j] != 1) continue;
+    DF t;
+    const int iv = cp(j, hint, t);
+    if (iv < 0) return -1;
+    hint = iv;
+    if (iv != cur) {
+      if (cur >= 0) flush();
+      cur = iv;
+      j0 = j;
+      w0 = w1 = w2 = w3 = zero;
+    }
+    const DF A = area(j);
+    const DF At = df_mul(A, t), At2 = df_mul(At, t), At3 = df_mul(At2, t);
+    w0 = df_add(w0, A);
+    w1 = df_add(w1, At);
+    w2 = df_add(w2, At2);
+    w3 = df_add(w3, At3);
+    span = j - j0 + 1;
+  }
+  if (cur >= 0) flush();
+  return n;
+}
+
+// the run's cells one by one (a piece whose sign changes on its interval)
+template <typename CP, typename AR>
+__device__ __noinline__ DF run_cells(const CP &cp, const AR &area, const int32_t *rad, int iv,
+                                     int j0, int span, const PieceDF &q, DF acc) {
+  for (int j = j0; j < j0 + span; j++) {
+    if (rad[j] != 1) continue;
+    DF t;
+    if (cp(j, iv, t) != iv) continue;
+    const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
+    if (sv.h > 0.0f) acc = df_fma(area(j), sv, acc);
+  }
+  return acc;
+}
+
+// sums at signal phase k for the energies pb .. pb+kEPT-1 of the chunk from
+// the power sums of its runs
+template <typename CP, typename AR>
+__device__ __forceinline__ void run_sums(const CP &cp, const AR &area, const int32_t *rad,
+                                         const WRuns &w, const int *nruns, int k,
+                                         const PieceDF *pc, const uint8_t *cls, int N_L, int pb,
+                                         int ne, DF (&acc)[kEPT]) {
+  for (int half = 0; half < 2; half++) {
+    const int n = nruns[half * w.N_P + k];
+    for (int r = 0; r < n; r++) {
+      const size_t ri = w.rec(half, r, k);
+      const float4 a4 = w.wa[ri], b4 = w.wb[ri];
+      const int meta = w.meta[ri];
+      const int iv = meta & 1023;
+      const DF W0{a4.x, a4.y}, W1{a4.z, a4.w}, W2{b4.x, b4.y}, W3{b4.z, b4.w};
+#pragma unroll
+      for (int e = 0; e < kEPT; e++) {
+        if (pb + e < ne) {
+          const int pi = (pb + e) * N_L + iv;
+          const uint8_t c = cls[pi];
+          if (c == 1) {
+            const PieceDF q = pc[pi];
+            acc[e] = df_fma(q.k3, W3, df_fma(q.k2, W2, df_fma(q.k1, W1, df_fma(q.y, W0, acc[e]))));
+          } else if (c == 2) {
+            acc[e] = run_cells(cp, area, rad, iv, (meta >> 10) & 1023, (meta >> 20) & 1023,
+                               pc[pi], acc[e]);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// beaming modification of the hot intensity I at energy E (the comoving
+// energy the atmosphere sees) and emission cosine mu, hot_wrapper.pyx:153-199:
+// 1: I (1 + abb E^cbb mu + bbb E^dbb mu^2); 2: the same with the analytical
+// normalisation 0.5 / (0.5 + abb E^cbb / 3 + bbb E^dbb / 4); 3: normalised by
+// the trapezoidal mu-integrals of I and of the modified I over nimu nodes
+// mu = 1/nimu, 2/nimu, ... (the reference's accumulated sums), eval_mu(mu)
+// giving the unmodified intensity there.  Negative results are 0.
+// ---------------------------------------------------------------------------
+template <typename EvalMu>
+__device__ double beamed_intensity(int opt, const double *b, double E, double mu, double I_hot,
+                                   const EvalMu &eval_mu) {
+  const double fa = b[0] * pow(E, b[2]), fb = b[1] * pow(E, b[3]);
+  double I = 0.0;
+  if (opt == 1) {
+    I = (1.0 + fa * mu + fb * (mu * mu)) * I_hot;
+  } else if (opt == 2) {
+    const double anorm = 0.5 / (0.5 + (1.0 / 3.0) * b[0] * pow(E, b[2]) +
+                                (1.0 / 4.0) * b[1] * pow(E, b[3]));
+    I = anorm * (1.0 + fa * mu + fb * (mu * mu)) * I_hot;
+  } else if (opt == 3) {
+    const double nimu = b[4];
+    const long n = nimu > 0.0 ? (long)nimu : 0;
+    double m = 0.0, nom = 0.0, den = 0.0;
+    for (long k = 0; k < n; k++) {
+      m = m + (1.0 / nimu);
+      const double dmu = (k == 0 || (double)k == nimu - 1.0) ? (0.5 / nimu) : (1.0 / nimu);
+      const double Ik = eval_mu(m);
+      const double fk = 1.0 + fa * m + fb * (m * m);
+      den = den + m * fk * Ik * dmu;
+      nom = nom + m * Ik * dmu;
+    }
+    if (are_equal(den, 0.0)) I = 0.0;
+    else I = (nom / den) * (1.0 + fa * mu + fb * (mu * mu)) * I_hot;
+  } else {
+    return I_hot;
+  }
+  return I < 0.0 ? 0.0 : I;
+}
+
+// ---------------------------------------------------------------------------
 // main integrator kernel: one CTA per chunk of parallels of one mesh
 // ---------------------------------------------------------------------------
 // WT = double: the plain FP64 drop-in.  WT = float: the mixed-precision form
@@ -839,6 +1031,16 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   GeoSmem g = carve(smem, N_L, EC, &coef, nmu, nEt, &as, (int)sizeof(PieceT<WT>), a.N_R);
   PieceT<WT> *co4 = reinterpret_cast<PieceT<WT> *>(coef);
   __shared__ int s_J, s_top, s_any, s_jalt;
+  // a beaming modification's (abb, bbb, cbb, dbb, nimu) for the parallel
+  __shared__ double s_beam[5];
+  // power-sum form (FP64 path with scratch): run counts per (cell half,
+  // signal phase) and the class of every piece of the chunk
+  const bool use_w = !kMixed && a.wsum != nullptr;
+  int *s_nruns = reinterpret_cast<int *>(g.sc_exp + EC);
+  uint8_t *s_cls = reinterpret_cast<uint8_t *>(s_nruns + 2 * N_P);
+  const WRuns wr = use_w ? wruns_of(a.wsum + (size_t)chunk * integrate_wsum_bytes_dev(N_P, a.w_cap),
+                                    a.w_cap, N_P)
+                         : WRuns{};
   double *slab = nullptr;
   float *slabf = nullptr;
   if (num4d) {
@@ -883,6 +1085,11 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     if (threadIdx.x == 0) {
       s_top = num4d ? (int)a.row_entry_top[row] : 0;
       s_any = 0;
+      // parameters 2-6 of the parallel's first radiating cell
+      if (M.beam_opt > 0) {
+        const double *vec = a.params + (M.cell_off + (int64_t)i * M.S1 + c.J) * a.n_params;
+        for (int b = 0; b < 5; b++) s_beam[b] = vec[2 + b];
+      }
     }
     __syncthreads();
     double E_eff = 0.0, p3 = 0.0;
@@ -1013,6 +1220,30 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         }
       }
       __syncthreads();
+      if (use_w) {
+        // the runs of every signal phase, each half of the cells by its own
+        // thread (energy independent: formed once per parallel and image)
+        const int hc = (M.S1 + 1) / 2;
+        const bool cached = M.S1 <= kMaxCellsF;
+        const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
+        for (int t = threadIdx.x; t < 2 * N_P; t += blockDim.x) {
+          const int k = t % N_P, half = t / N_P;
+          const double phd = a.phases[k];
+          const float ph = (float)phd;
+          const float tp = (float)kTwoPi;
+          const CellPhaseF cp{as.fphase, as.fphase_lo, N_L, as.fphase[0], as.fphase[N_L - 1], ph,
+                              (float)(phd - (double)ph), tp, (float)(kTwoPi - (double)tp),
+                              cached ? as.fcphi : nullptr, cached ? as.fcphi_lo : nullptr,
+                              cellPhi};
+          int n = build_runs(cp, ar, half * hc, min(M.S1, (half + 1) * hc), rad, wr, half, k);
+          if (n < 0) {
+            atomicExch(&a.member_status[m], (int)kPulseFail);
+            n = 0;
+          }
+          s_nruns[half * N_P + k] = n;
+        }
+        __syncthreads();
+      }
       if (threadIdx.x == 0 && a.flop_counter) {
         int Cr = 0;
         for (int j = 0; j < M.S1; j++) Cr += (rad[j] == 1);
@@ -1067,7 +1298,9 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                   // atm 6: E' = E / Z in electron rest energies (:457-458)
                   const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
                                           : g.lgE[pl] - g.lzs[s];
-                  if (p == 0 && g.clamp0[s]) {
+                  // with beaming option 3 every call is followed by calls up
+                  // to mu = 1, so no out-of-table mu is ever clamped
+                  if (p == 0 && g.clamp0[s] && M.beam_opt != 3) {
                     I_E = eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, g.ABB[s], true),
                                        v3, p3);
                   } else {
@@ -1084,10 +1317,40 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                 }
                 const double I_c =
                     corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
-                y = (WT)((I_E * norm - I_c) * g.GEOM[s]);
+                // with a beaming modification the raw intensity is kept here
+                // and modified in the pass below
+                y = (WT)(M.beam_opt > 0 ? I_E : (I_E * norm - I_c) * g.GEOM[s]);
               }
             }
             co4[pl * N_L + col].y = y;
+          }
+        }
+        if (!kMixed && M.beam_opt > 0) {
+          // the beaming modification (hot_wrapper.pyx:153-199) of every
+          // column intensity of the chunk, by the thread that formed it
+          for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+            const int pl = t / N_L, col = t - pl * N_L;
+            const int p = e0 + pl;
+            const int s = g.src[col];
+            if (s < 0) continue;
+            const double I_raw = (double)co4[pl * N_L + col].y;
+            double I_E;
+            if (num4d) {
+              const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951 : g.lgE[pl] - g.lzs[s];
+              const double Ep = erest ? v3 : a.energies[p] / g.Z[s];
+              I_E = beamed_intensity(M.beam_opt, s_beam, Ep, g.ABB[s], I_raw, [&](double mu_k) {
+                return eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, mu_k, false), v3,
+                                    p3);
+              });
+            } else {
+              const double Ep = a.energies[p] / g.Z[s];
+              const double I0 = eval_bb(Ep, kT);  // the blackbody has no mu dependence
+              I_E = beamed_intensity(M.beam_opt, s_beam, Ep, g.ABB[s], I_raw,
+                                     [&](double) { return I0; });
+            }
+            const double I_c =
+                corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
+            co4[pl * N_L + col].y = (WT)((I_E * norm - I_c) * g.GEOM[s]);
           }
         }
         __syncthreads();
@@ -1169,6 +1432,17 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             }
           }
           __syncthreads();
+          if (use_w) {
+            // every value is added with the elsewhere correction (:593-594)
+            for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+              const int iv = t % N_L;
+              uint8_t cl = 0;
+              if (iv < N_L - 1)
+                cl = corr ? 1 : piece_class(pc[t], as.fphase[iv + 1] - as.fphase[iv]);
+              s_cls[t] = cl;
+            }
+            __syncthreads();
+          }
         }
         // cell x phase accumulation (:571-598)
         for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
@@ -1200,8 +1474,12 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
 #pragma unroll
             for (int e = 0; e < kEPT; e++) acc[e] = DF{0.0f, 0.0f};
             const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
-            if (!cell_phase_sums_df(cp, ar, M.S1, rad, reinterpret_cast<const PieceDF *>(co4), N_L,
-                                    pb, ne, corr, acc)) {
+            if (use_w) {
+              run_sums(cp, ar, rad, wr, s_nruns, k, reinterpret_cast<const PieceDF *>(co4), s_cls,
+                       N_L, pb, ne, acc);
+            } else if (!cell_phase_sums_df(cp, ar, M.S1, rad,
+                                           reinterpret_cast<const PieceDF *>(co4), N_L, pb, ne,
+                                           corr, acc)) {
               atomicExch(&a.member_status[m], (int)kPulseFail);
               continue;
             }
@@ -1625,26 +1903,31 @@ static void launch_table_state(const IntegrateArgs &a, cudaStream_t st) {
   num4d_scan_kernel<<<(a.n_members + 127) / 128, 128, 0, st>>>(a);
 }
 
+size_t integrate_wsum_bytes(int N_P, int max_cells, int *w_cap) {
+  const int cap = (max_cells + 1) / 2;
+  if (w_cap) *w_cap = cap;
+  return integrate_wsum_bytes_dev(N_P, cap);
+}
+
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
   if (a.n_members <= 0) return;
   const int pb = a.mixed ? (int)sizeof(PieceT<float>) : (int)sizeof(PieceT<double>);
   Layout L = a.atmos.I ? make_layout(a.N_L, a.N_P, a.N_E, a.atmos.nmu, a.atmos.nE, pb, a.N_R)
                        : make_layout(a.N_L, a.N_P, a.N_E, 0, 0, pb, a.N_R);
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[a.mixed ? 1 : 0]) {
-    if (a.mixed)
-      cudaFuncSetAttribute(integrate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024);
-    else
-      cudaFuncSetAttribute(integrate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024);
-    attr_set[a.mixed ? 1 : 0] = true;
-  }
+  // run counts [2][N_P] and piece classes [EC][N_L] after the layout
+  const size_t bytes = L.bytes + (size_t)2 * a.N_P * sizeof(int) + (size_t)L.EC * a.N_L + 16;
+  // the attribute is per device: set it on every launch (cheap)
+  if (a.mixed)
+    cudaFuncSetAttribute(integrate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+  else
+    cudaFuncSetAttribute(integrate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
   if (a.atmos.I != nullptr) launch_table_state(a, st);
   if (a.mixed)
-    integrate_kernel<float><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
+    integrate_kernel<float><<<a.n_chunks, kThreads, bytes, st>>>(a);
   else
-    integrate_kernel<double><<<a.n_chunks, kThreads, L.bytes, st>>>(a);
+    integrate_kernel<double><<<a.n_chunks, kThreads, bytes, st>>>(a);
   dim3 grid((a.N_E * a.N_P + 255) / 256, a.n_members);
   reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
 }

@@ -34,6 +34,8 @@ struct MemberDesc {
   int32_t image_order_limit;  // 0: infer from the maximum deflection
   int32_t atm;                // 1 blackbody, 2 numerical 4-D table
   int64_t flux_off;           // offset of this member's [N_E][N_P] flux
+  int32_t beam_opt;           // beaming modification 0-3 (hot_wrapper.pyx:153-199)
+  int32_t reserved;
 };
 
 struct Atmos4D {
@@ -75,6 +77,10 @@ struct IntegrateArgs {
   double *flux;             // [..] at members[m].flux_off
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
   double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
+  // power sums of the cell x phase sums (FP64 form; scratch, or null for the
+  // per-cell form): per chunk 2 * w_cap * N_P run records, see integrator.cu
+  unsigned char *wsum = nullptr;
+  int w_cap = 0;            // runs per (cell half, signal phase)
   int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
   double *flux_q = nullptr, *flux_u = nullptr;  // Stokes Q, U (launch_stokes only)
   // Stokes Q of a 2-D table atmosphere (atm 4, 6; launch_stokes only):
@@ -91,6 +97,9 @@ struct SplitArgs {
 };
 void launch_split_reduce(const SplitArgs &a, cudaStream_t st);
 void launch_integrate(const IntegrateArgs &a, cudaStream_t st);
+// scratch bytes per chunk of the FP64 integrator's power sums for parallels
+// of at most max_cells cells (w_cap runs per cell half and signal phase)
+size_t integrate_wsum_bytes(int N_P, int max_cells, int *w_cap);
 // Stokes I (a.flux), Q, U for blackbody (1) and burst blackbody (3) members;
 // a.partial: stokes_partial_doubles(a) doubles, zeroed; a.chunk_* unused
 size_t stokes_partial_doubles(const IntegrateArgs &a);
@@ -121,6 +130,10 @@ struct FoldArgs {
   int ldM;
   const double *in;  // [batch][q][N]
   double *out;       // [batch][K][N]
+  // tensor-core form: set to 1 when a wait on the tensor core or the TMA
+  // unit timed out (the tile is written as NaN), 2 when the wait for the
+  // operations in flight timed out as well; may be null
+  int32_t *status = nullptr;
 };
 void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
 // tensor-core form (3xTF32 split products, FP32 accumulation in TMEM);
@@ -128,6 +141,11 @@ void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
 // Returns 0, or < 0 when the tile maps cannot be encoded.
 size_t fold_tc_scratch_bytes(const FoldArgs &a);
 int launch_fold_tc(const FoldArgs &a, void *scratch, cudaStream_t st);
+// the tensor-core fold's timeout path exercised without a fault: one tile
+// whose producer issues nothing, so its waits run out after a short limit;
+// the kernel reports through a.status (expected 2) and frees its tensor
+// memory.  a.K, a.q, a.N, a.batch small; scratch as launch_fold_tc.
+int launch_fold_tc_timeout_selftest(const FoldArgs &a, void *scratch, cudaStream_t st);
 double launch_peak_probe(int fp64, int blocks, int threads, int iters, void *out,
                          cudaStream_t st);
 
@@ -236,6 +254,23 @@ struct ExpectedArgs {
   double *out;                // [n_sets][K][B]
 };
 void launch_expected_counts(const ExpectedArgs &a, cudaStream_t st);
+// Poisson log-likelihood given the expected counts (star + known background)
+// of n_sets evaluations sharing one data set
+// (_poisson_likelihood_given_background.pyx:82-109): per set the channels'
+// constants plus sum_ij (d_ij log E_ij - E_ij) over E_ij > 0, and the count
+// of bins with E_ij <= 0 that are not (d_ij == 0 and E_ij == 0) (the
+// reference's randomised -1e90 penalty, applied by the host)
+struct PoissonArgs {
+  int n_sets, K, B;
+  const double *expected;   // [n_sets][K][B]
+  const double *counts;     // [K][B]
+  const double *precomp;    // [K] (neg_sum_ln_data_factorial) or null
+  double *chan_ll;          // [n_sets][K] scratch
+  int32_t *chan_pen;        // [n_sets][K] scratch
+  double *loglike;          // [n_sets]
+  int32_t *n_penalty;       // [n_sets]
+};
+void launch_poisson_loglike(const PoissonArgs &a, cudaStream_t st);
 struct PhaseIntArgs {
   int64_t rows;
   int n_phases, B;

@@ -238,7 +238,57 @@ __global__ void gaussian_kernel(int n_sets, int rows, int cols, const double *mo
   }
 }
 
+// one warp per (set, channel): lanes over the phase bins, the terms
+// reduced by a fixed butterfly
+__global__ void __launch_bounds__(32 * kSynWarps) poisson_channel_kernel(PoissonArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (int64_t)blockIdx.x * kSynWarps + (threadIdx.x >> 5);
+  if (w >= (int64_t)a.n_sets * a.K) return;
+  const int i = (int)(w % a.K);
+  const double *E = a.expected + w * a.B;
+  const double *d = a.counts + (int64_t)i * a.B;
+  double s = 0.0;
+  int pen = 0;
+  for (int j = lane; j < a.B; j += 32) {
+    const double e = E[j], c = d[j];
+    if (e > 0.0) s += c * log(e) - e;
+    else if (!(c == 0.0 && e == 0.0)) pen++;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    pen += __shfl_xor_sync(0xffffffffu, pen, o);
+  }
+  if (lane == 0) {
+    a.chan_ll[w] = s;
+    a.chan_pen[w] = pen;
+  }
+}
+
+// per set: the channels in order (constant term, then the channel's sum)
+__global__ void poisson_finish_kernel(PoissonArgs a) {
+  const int set = blockIdx.x * blockDim.x + threadIdx.x;
+  if (set >= a.n_sets) return;
+  double L = 0.0;
+  int pen = 0;
+  for (int i = 0; i < a.K; i++) {
+    if (a.precomp) L += a.precomp[i];
+    L += a.chan_ll[(int64_t)set * a.K + i];
+    pen += a.chan_pen[(int64_t)set * a.K + i];
+  }
+  a.loglike[set] = L;
+  a.n_penalty[set] = pen;
+}
+
 }  // namespace
+
+void launch_poisson_loglike(const PoissonArgs &a, cudaStream_t st) {
+  const int64_t warps = (int64_t)a.n_sets * a.K;
+  if (warps <= 0) return;
+  poisson_channel_kernel<<<(unsigned)((warps + kSynWarps - 1) / kSynWarps), 32 * kSynWarps, 0,
+                           st>>>(a);
+  poisson_finish_kernel<<<(a.n_sets + 127) / 128, 128, 0, st>>>(a);
+}
 
 void launch_gaussian(int n_sets, int rows, int cols, const double *model,
                      int64_t model_set_stride, int64_t model_row_stride, const double *data,

@@ -114,6 +114,28 @@ def config1_workload(n_channels=300, n_inputs=64, n_energies=64):
                 phase_edges=np.linspace(0.0, 1.0, 33), exposure=1.0e6)
 
 
+def config1_model():
+    """Model of the small plain configuration: one blackbody hot region
+    (sqrt_num_cells 32, min 10, max 80; 64 leaves, 512 rays), 64 energies,
+    the 300 x 64 response, 32 phase bins, exposure 1e6 s; data are attached
+    later (attach_data).  Its parameter vector is config1_vector()."""
+    from .batch import Data, HotRegionSpec, Instrument, Model
+    w = config1_workload()
+    return Model(regions=[HotRegionSpec(atm_ext=1, sqrt_num_cells=32, min_sqrt_num_cells=10,
+                                        max_sqrt_num_cells=80, num_leaves=64, num_rays=512)],
+                 instrument=Instrument(w["matrix"], w["input_edges"]),
+                 data=Data(np.zeros((300, 32), np.int32), w["phase_edges"], w["exposure"]),
+                 num_energies=64)
+
+
+def config1_vector():
+    """M 1.4, R 12 km, 300 Hz, i 1 rad, 1 kpc; spot colatitude 1.0, radius
+    0.075, log T 6.1, no phase shift."""
+    w = config1_workload()
+    return np.array([w["mass"], w["radius_km"], w["frequency"], math.cos(w["inclination"]),
+                     w["distance_kpc"], w["colatitude"], w["spot_radius"], w["logT"], 0.0])
+
+
 def poisson_data(registered, comp_phases, phase_edges, exposure, seed=20261203,
                  bg_fraction=0.1):
     """Counts [channels, bins]: Poisson draws of the source counts per phase
