@@ -10,7 +10,8 @@ that holds the reference checkout; the GPU host never runs it.
 Flags follow the reference's setup.py (-O3 -fopenmp) with FMA contraction
 switched off (-ffp-contract=off) so results do not depend on the host ISA.
 
-Usage:  python oracle/build_ref.py [--ref /root/reference] [-j N]
+Usage:  python oracle/build_ref.py --ref <reference checkout> [-j N]
+        (or the checkout in $XPSI_REFERENCE)
 """
 import argparse
 import os
@@ -60,13 +61,20 @@ def run(cmd):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("XPSI_REFERENCE"),
+                    help="the reference checkout (default: $XPSI_REFERENCE)")
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the reference checkout with --ref or $XPSI_REFERENCE")
     ref = os.path.abspath(args.ref)
     if not os.path.isdir(os.path.join(ref, "xpsi")):
         print("reference checkout not found; nothing to build")
         return 0
+    # the import harness finds the checkout these modules were built from
+    os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(OUT, "REFERENCE_PATH"), "w") as f:
+        f.write(ref + "\n")
     import numpy
     build = os.path.join(OUT, "build")
     os.makedirs(build, exist_ok=True)

@@ -28,12 +28,27 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("XPSI_REFERENCE", "/root/reference")
 BUILT = os.path.join(HERE, "_ref")
 
 
+def _reference_path():
+    """The checkout: $XPSI_REFERENCE, else the one oracle/build_ref.py built
+    from (recorded in oracle/_ref/REFERENCE_PATH), else none."""
+    env = os.environ.get("XPSI_REFERENCE")
+    if env:
+        return env
+    try:
+        with open(os.path.join(BUILT, "REFERENCE_PATH")) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
+REF = _reference_path()
+
+
 def available():
-    return (os.path.isdir(os.path.join(REF, "xpsi"))
+    return (bool(REF) and os.path.isdir(os.path.join(REF, "xpsi"))
             and os.path.isdir(os.path.join(BUILT, "xpsi", "cellmesh")))
 
 

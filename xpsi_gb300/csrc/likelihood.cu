@@ -508,27 +508,47 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   }
 }
 
+// (s, c) += x with Neumaier's compensation: s + c carries the sum to about
+// twice the working precision whatever the order of magnitudes
+__device__ __forceinline__ void comp_add(double &s, double &c, double x) {
+  const double t = s + x;
+  c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
 // per-evaluation sum over channels and the reference's early exits: one
 // warp per evaluation; the first flagged channel (lowest index) decides the
-// early exit (:677-684, :423-429), otherwise the channel terms are summed by
-// lane partials in a fixed order (bitwise reproducible)
+// early exit (:677-684, :423-429), otherwise the channel terms are summed
+// with compensation (each lane over its channels, then the lanes' sums and
+// corrections by a fixed butterfly: bitwise reproducible)
 __global__ void like_finalize_kernel(LikeArgs a) {
   const int lane = threadIdx.x & 31;
   const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (v >= a.n_vec) return;
-  double LL = 0.0;
+  double LL = 0.0, LLc = 0.0;
   int first = 0x7fffffff;
   for (int ch = lane; ch < a.K; ch += 32) {
     const size_t o = (size_t)v * a.K + ch;
     if (a.chan_flag[o] != 0) {
       if (ch < first) first = ch;
     } else {
-      LL += a.chan_ll[o];
+      comp_add(LL, LLc, a.chan_ll[o]);
     }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
-  LL = warp_sum(LL);
+  for (int o = 16; o > 0; o >>= 1) {
+    first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+    const double s2 = __shfl_xor_sync(0xffffffffu, LL, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, LLc, o);
+    // both lanes of a pair form the same (s, c): add the lower lane's pair
+    // to the higher's in a fixed order
+    double s = (lane & o) ? s2 : LL, c = (lane & o) ? c2 : LLc;
+    comp_add(s, c, (lane & o) ? LL : s2);
+    c += (lane & o) ? LLc : c2;
+    LL = s;
+    LLc = c;
+  }
+  LL = LL + LLc;
   int st = kOk;
   if (first != 0x7fffffff) {
     const int f = a.chan_flag[(size_t)v * a.K + first];
