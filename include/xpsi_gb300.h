@@ -335,7 +335,10 @@ int xgpu_rays_batch(int64_t n_rows, int N_R, const double *u,
 
 /* Integrator over n_meshes packed meshes.  `meshes` is a HOST array; every
  * other pointer is device memory.  flux receives [N_E][N_P] per mesh at
- * meshes[m].flux_off; mesh_status[m] gets XGPU_PULSE_FAIL on terminate. */
+ * meshes[m].flux_off; mesh_status[m] gets XGPU_PULSE_FAIL on terminate.
+ * The work is cut on the device into about 4 target_ctas chunks of
+ * consecutive parallels of equal estimated cost (images x radiating cells,
+ * the image counts from maxDeflection); target_ctas <= 0 takes 8 per SM. */
 typedef struct {
   const int32_t *row_mesh;
   const double *radius, *u, *cos_gamma, *theta0, *maxDeflection;

@@ -268,33 +268,28 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   if (d->correction != nullptr && d->n_correction < 1)
     return fail_msg("correction vectors need at least 1 parameter per cell");
   if (target_ctas <= 0) target_ctas = 8 * 152;
-  // chunks of consecutive parallels of one mesh, sized by estimated cost
-  // (cells per parallel) so that large meshes do not leave a long tail
-  double total_cost = 0.0;
-  for (int m = 0; m < n_meshes; m++) total_cost += (double)meshes[m].S0 * meshes[m].S1;
-  const double target_cost = std::max(1.0, total_cost / target_ctas);
-  std::vector<int64_t> r0, r1;
-  std::vector<int32_t> first(n_meshes + 1);
-  for (int m = 0; m < n_meshes; m++) {
-    first[m] = (int32_t)r0.size();
-    const int64_t rpc =
-        std::max<int64_t>(1, (int64_t)(target_cost / std::max(1, meshes[m].S1)));
-    for (int64_t s = 0; s < meshes[m].S0; s += rpc) {
-      r0.push_back(meshes[m].row_off + s);
-      r1.push_back(meshes[m].row_off + std::min<int64_t>(meshes[m].S0, s + rpc));
-    }
-  }
-  first[n_meshes] = (int32_t)r0.size();
-  int n_chunks = (int)r0.size();
-  Dev dm, dr0, dr1, dfirst, dpart, dstate;
+  // the chunks are planned on the device from the parallels' costs (image
+  // counts are known only after the ray tables): about 4 per CTA slot of
+  // the target, at most 2 target + members and at most one per parallel
+  // (integrator.cu)
+  const int64_t target_chunks = 4 * (int64_t)target_ctas;
+  const int64_t max_chunks = std::min<int64_t>(2 * target_chunks + n_meshes, n_rows) + 16;
+  if (max_chunks > (int64_t)INT32_MAX / 2) return fail_msg("too many meshes in one call");
+  const int n_chunks = (int)max_chunks;
+  Dev dm, dr0, dr1, dfirst, dorder, dcount, drowcost, dchunkcost, dpart, dstate;
   int rc;
   if ((rc = upload(dm, reinterpret_cast<const xg::MemberDesc *>(meshes), n_meshes, st))) return rc;
-  if ((rc = upload(dr0, r0.data(), r0.size(), st))) return rc;
-  if ((rc = upload(dr1, r1.data(), r1.size(), st))) return rc;
-  if ((rc = upload(dfirst, first.data(), first.size(), st))) return rc;
+  if ((rc = dalloc(dr0, (size_t)n_chunks * sizeof(int64_t), st)) ||
+      (rc = dalloc(dr1, (size_t)n_chunks * sizeof(int64_t), st)) ||
+      (rc = dalloc(dfirst, (size_t)(n_meshes + 1) * sizeof(int32_t), st)) ||
+      (rc = dalloc(dorder, (size_t)n_chunks * sizeof(int32_t), st)) ||
+      (rc = dalloc(dcount, sizeof(int32_t), st)) ||
+      (rc = dalloc(drowcost, (size_t)std::max<int64_t>(1, n_rows) * sizeof(float), st)) ||
+      (rc = dalloc(dchunkcost, (size_t)n_chunks * sizeof(float), st)))
+    return rc;
+  // each chunk's CTA zeroes its own partial before accumulating
   size_t part_n = (size_t)n_chunks * N_E * N_P;
   if ((rc = dalloc(dpart, part_n * sizeof(double), st))) return rc;
-  CK(cudaMemsetAsync(dpart.p, 0, part_n * sizeof(double), st));
   if ((rc = dalloc(dstate, (size_t)3 * n_rows + 16, st))) return rc;
   Dev dslab;
   if (d->atmos.intensity != nullptr && !table2d &&
@@ -331,11 +326,16 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.atmos = xg::Atmos4D{d->atmos.logT, d->atmos.logg, d->atmos.mu, d->atmos.logE,
                         d->atmos.intensity, (int)d->atmos.nT, (int)d->atmos.ng,
                         (int)d->atmos.nmu, (int)d->atmos.nE, d->atmos.intensity_f32};
-  a.n_chunks = n_chunks;
+  a.max_chunks = n_chunks;
+  a.target_chunks = (int)target_chunks;
   a.chunk_r0 = dr0.as<int64_t>();
   a.chunk_r1 = dr1.as<int64_t>();
   a.partial = dpart.as<double>();
   a.chunk_first = dfirst.as<int32_t>();
+  a.chunk_order = dorder.as<int32_t>();
+  a.chunk_count = dcount.as<int32_t>();
+  a.row_cost = drowcost.as<float>();
+  a.chunk_cost = dchunkcost.as<float>();
   uint8_t *sb = dstate.as<uint8_t>();
   a.row_has_eval = sb; a.row_last_top = sb + n_rows; a.row_entry_top = sb + 2 * n_rows;
   a.member_status = d->mesh_status;

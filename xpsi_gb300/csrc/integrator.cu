@@ -915,7 +915,7 @@ __device__ __forceinline__ int build_runs(const CP &cp, const AR &area, int jb, 
 
 // the run's cells one by one (a piece whose sign changes on its interval)
 template <typename CP, typename AR>
-__device__ __noinline__ DF run_cells(const CP &cp, const AR &area, const int32_t *rad, int iv,
+__device__ __forceinline__ DF run_cells(const CP &cp, const AR &area, const int32_t *rad, int iv,
                                      int j0, int span, const PieceDF &q, DF acc) {
   for (int j = j0; j < j0 + span; j++) {
     if (rad[j] != 1) continue;
@@ -928,35 +928,74 @@ __device__ __noinline__ DF run_cells(const CP &cp, const AR &area, const int32_t
 }
 
 // sums at signal phase k for the energies pb .. pb+kEPT-1 of the chunk from
-// the power sums of its runs
+// the power sums of its runs.  The lanes of a warp take consecutive phases,
+// so the r-th runs of neighbouring lanes lie in different intervals and
+// carry different piece classes: every energy's power-sum term is formed on
+// every lane and kept where the class is 1 (a select, no branch), and the
+// runs whose piece changes sign are only noted here and walked cell by cell
+// after the last run, so that one lane's cell walk does not hold up the
+// others run after run.  The next run's record is loaded before the current
+// one is used.
+constexpr int kDeferRuns = 24;  // sign-changing (run, energy) items noted per task
+
 template <typename CP, typename AR>
 __device__ __forceinline__ void run_sums(const CP &cp, const AR &area, const int32_t *rad,
                                          const WRuns &w, const int *nruns, int k,
                                          const PieceDF *pc, const uint8_t *cls, int N_L, int pb,
                                          int ne, DF (&acc)[kEPT]) {
+  uint32_t defer[kDeferRuns];
+  int nd = 0;
   for (int half = 0; half < 2; half++) {
     const int n = nruns[half * w.N_P + k];
+    float4 a4, b4;
+    int meta = 0;
+    if (n > 0) {
+      const size_t ri = w.rec(half, 0, k);
+      a4 = w.wa[ri];
+      b4 = w.wb[ri];
+      meta = w.meta[ri];
+    }
     for (int r = 0; r < n; r++) {
-      const size_t ri = w.rec(half, r, k);
-      const float4 a4 = w.wa[ri], b4 = w.wb[ri];
-      const int meta = w.meta[ri];
-      const int iv = meta & 1023;
       const DF W0{a4.x, a4.y}, W1{a4.z, a4.w}, W2{b4.x, b4.y}, W3{b4.z, b4.w};
+      const int iv = meta & 1023;
+      if (r + 1 < n) {
+        const size_t ri = w.rec(half, r + 1, k);
+        a4 = w.wa[ri];
+        b4 = w.wb[ri];
+        meta = w.meta[ri];
+      }
 #pragma unroll
       for (int e = 0; e < kEPT; e++) {
         if (pb + e < ne) {
           const int pi = (pb + e) * N_L + iv;
           const uint8_t c = cls[pi];
-          if (c == 1) {
-            const PieceDF q = pc[pi];
-            acc[e] = df_fma(q.k3, W3, df_fma(q.k2, W2, df_fma(q.k1, W1, df_fma(q.y, W0, acc[e]))));
-          } else if (c == 2) {
-            acc[e] = run_cells(cp, area, rad, iv, (meta >> 10) & 1023, (meta >> 20) & 1023,
-                               pc[pi], acc[e]);
+          const PieceDF q = pc[pi];
+          const DF v =
+              df_fma(q.k3, W3, df_fma(q.k2, W2, df_fma(q.k1, W1, df_fma(q.y, W0, acc[e]))));
+          if (c == 1) acc[e] = v;
+          if (c == 2) {
+            if (nd < kDeferRuns) {
+              defer[nd++] = (uint32_t)half | ((uint32_t)r << 1) | ((uint32_t)e << 12);
+            } else {
+              const int m = w.meta[w.rec(half, r, k)];
+              acc[e] = df_add(acc[e], run_cells(cp, area, rad, iv, (m >> 10) & 1023,
+                                                (m >> 20) & 1023, q, DF{0.0f, 0.0f}));
+            }
           }
         }
       }
     }
+  }
+  for (int d = 0; d < nd; d++) {
+    const uint32_t it = defer[d];
+    const int half = it & 1, r = (it >> 1) & 2047, ed = (int)(it >> 12);
+    const int m = w.meta[w.rec(half, r, k)];
+    const int iv = m & 1023;
+    const DF add = run_cells(cp, area, rad, iv, (m >> 10) & 1023, (m >> 20) & 1023,
+                             pc[(pb + ed) * N_L + iv], DF{0.0f, 0.0f});
+#pragma unroll
+    for (int e = 0; e < kEPT; e++)
+      if (e == ed) acc[e] = df_add(acc[e], add);
   }
 }
 
@@ -1010,7 +1049,8 @@ template <typename WT>
 __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a) {
   constexpr bool kMixed = std::is_same<WT, float>::value;
   extern __shared__ __align__(16) char smem[];
-  const int chunk = blockIdx.x;
+  if ((int)blockIdx.x >= *a.chunk_count) return;
+  const int chunk = a.chunk_order[blockIdx.x];
   const int64_t r0 = a.chunk_r0[chunk], r1 = a.chunk_r1[chunk];
   const int m = a.row_member[r0];
   const MemberDesc M = a.members[m];
@@ -1067,6 +1107,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   }
   const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
   double *part = a.partial + (size_t)chunk * N_E * N_P;
+  for (int t = threadIdx.x; t < N_E * N_P; t += blockDim.x) part[t] = 0.0;
+  __syncthreads();
   const double mu_max = num4d ? a.atmos.mu[a.atmos.nmu - 1] : 0.0;
   const double mu_top3 = num4d ? a.atmos.mu[a.atmos.nmu - 3] : 0.0;
   const int groups = EC / kEPT;
@@ -1873,6 +1915,166 @@ __global__ void split_reduce_kernel(SplitArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Work plan.  A parallel's cost is dominated by its images: each image
+// repeats the profile columns, the splines and the cell x phase sums, and a
+// star near the photon sphere (R -> 1.5 r_s) has rays deflected by several
+// pi, so its parallels carry up to ~8 images against the usual 1-2.  The
+// image count per parallel, ceil(max deflection / pi) (or the mesh's image
+// order limit), is known only after the ray tables are built on the device,
+// so the chunks are planned there:
+//   cost(parallel) = images x (kCostImage + radiating cells) + kCostRow
+// in units of one radiating cell's sums over one image (the fixed per-image
+// work -- columns, splines, leaf geometry -- measured at about 28 cells, the
+// per-parallel slab contraction at about 6), or 1 for a parallel with no
+// radiating cell.  The consecutive parallels of each mesh are cut greedily
+// into chunks of about total / target_chunks (a chunk closes before the
+// parallel that would take it past the target), which bounds the count by
+// 2 target_chunks + members.  The CTAs take the chunks heaviest first
+// (a counting sort on floor(log2 cost)), so the few heavy chunks start in
+// the first wave instead of forming the tail.  Chunk boundaries depend only
+// on the costs, so every result is independent of the order in which the
+// CTAs run.
+// ---------------------------------------------------------------------------
+constexpr float kCostImage = 28.0f;
+constexpr float kCostRow = 6.0f;
+constexpr int kPlanThreads = 1024;
+
+__global__ void row_cost_kernel(IntegrateArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= a.n_rows) return;
+  const MemberDesc M = a.members[a.row_member[row]];
+  const int64_t i = row - M.row_off;
+  const int32_t *rad = a.radiates + M.cell_off + i * M.S1;
+  int cr = 0;
+  for (int j = lane; j < M.S1; j += 32) cr += (rad[j] == 1);
+  for (int o = 16; o > 0; o >>= 1) cr += __shfl_xor_sync(0xffffffffu, cr, o);
+  if (lane == 0) {
+    float c = 1.0f;
+    if (cr > 0) {
+      const double md = a.maxDeflection[row];
+      int io = M.image_order_limit > 0 ? M.image_order_limit
+                                       : (md > 0.0 ? (int)ceil(md / kPi) : 1);
+      io = max(1, min(io, 64));
+      c = (float)io * (kCostImage + (float)cr) + kCostRow;
+    }
+    a.row_cost[row] = c;
+  }
+}
+
+// chunks of mesh m for a target cost: count (write == false) or write them
+// from index c0; returns the count
+__device__ int plan_mesh(const IntegrateArgs &a, int m, double target, bool write, int c0) {
+  const MemberDesc M = a.members[m];
+  int n = 0;
+  double acc = 0.0;
+  int64_t start = M.row_off;
+  for (int64_t s = 0; s < M.S0; s++) {
+    const int64_t row = M.row_off + s;
+    const double c = a.row_cost[row];
+    if (acc > 0.0 && acc + c > target) {
+      if (write) {
+        a.chunk_r0[c0 + n] = start;
+        a.chunk_r1[c0 + n] = row;
+        a.chunk_cost[c0 + n] = (float)acc;
+      }
+      n++;
+      acc = 0.0;
+      start = row;
+    }
+    acc += c;
+  }
+  if (M.S0 > 0) {
+    if (write) {
+      a.chunk_r0[c0 + n] = start;
+      a.chunk_r1[c0 + n] = M.row_off + M.S0;
+      a.chunk_cost[c0 + n] = (float)acc;
+    }
+    n++;
+  }
+  return n;
+}
+
+// exclusive scan of per-thread values over the block; returns the total
+__device__ int block_exclusive_scan(int v, int *s_buf, int &excl) {
+  const int t = threadIdx.x;
+  s_buf[t] = v;
+  __syncthreads();
+  for (int o = 1; o < kPlanThreads; o <<= 1) {
+    const int x = t >= o ? s_buf[t - o] : 0;
+    __syncthreads();
+    s_buf[t] += x;
+    __syncthreads();
+  }
+  excl = s_buf[t] - v;
+  const int total = s_buf[kPlanThreads - 1];
+  __syncthreads();
+  return total;
+}
+
+// one CTA of kPlanThreads threads
+__global__ void __launch_bounds__(kPlanThreads) plan_chunks_kernel(IntegrateArgs a) {
+  __shared__ double s_sum[kPlanThreads];
+  __shared__ int s_scan[kPlanThreads];
+  __shared__ int s_hist[64], s_cur[64];
+  const int t = threadIdx.x;
+  // total cost (fixed summation order)
+  double sum = 0.0;
+  for (int64_t r = t; r < a.n_rows; r += kPlanThreads) sum += a.row_cost[r];
+  s_sum[t] = sum;
+  __syncthreads();
+  for (int o = kPlanThreads / 2; o > 0; o >>= 1) {
+    if (t < o) s_sum[t] += s_sum[t + o];
+    __syncthreads();
+  }
+  double target = fmax(1.0, s_sum[0] / (double)max(1, a.target_chunks));
+  // meshes [m0, m1) of this thread
+  const int per = (a.n_members + kPlanThreads - 1) / kPlanThreads;
+  const int m0 = min(a.n_members, t * per), m1 = min(a.n_members, m0 + per);
+  int excl = 0, total = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    int cnt = 0;
+    for (int m = m0; m < m1; m++) cnt += plan_mesh(a, m, target, false, 0);
+    total = block_exclusive_scan(cnt, s_scan, excl);
+    if (total <= a.max_chunks) break;
+    // the bound cannot be exceeded in exact arithmetic; should rounding ever
+    // do it, one chunk per mesh fits
+    target = 1.0e300;
+  }
+  int c = excl;
+  for (int m = m0; m < m1; m++) {
+    a.chunk_first[m] = c;
+    c += plan_mesh(a, m, target, true, c);
+  }
+  if (t == 0) {
+    a.chunk_first[a.n_members] = total;
+    *a.chunk_count = total;
+  }
+  // heaviest first: counting sort on floor(log2 cost), descending
+  if (t < 64) s_hist[t] = 0;
+  __syncthreads();
+  for (int k = t; k < total; k += kPlanThreads) {
+    int e = 0;
+    frexpf(a.chunk_cost[k], &e);
+    atomicAdd(&s_hist[min(63, max(0, e))], 1);
+  }
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int b = 63; b >= 0; b--) {
+      s_cur[b] = run;
+      run += s_hist[b];
+    }
+  }
+  __syncthreads();
+  for (int k = t; k < total; k += kPlanThreads) {
+    int e = 0;
+    frexpf(a.chunk_cost[k], &e);
+    a.chunk_order[atomicAdd(&s_cur[min(63, max(0, e))], 1)] = k;
+  }
+}
+
 // ordered reduction of the chunk partials and the 1/(E keV) factor (:605-612)
 __global__ void reduce_flux_kernel(IntegrateArgs a) {
   const int m = blockIdx.y;
@@ -1916,18 +2118,20 @@ void launch_integrate(const IntegrateArgs &a, cudaStream_t st) {
                        : make_layout(a.N_L, a.N_P, a.N_E, 0, 0, pb, a.N_R);
   // run counts [2][N_P] and piece classes [EC][N_L] after the layout
   const size_t bytes = L.bytes + (size_t)2 * a.N_P * sizeof(int) + (size_t)L.EC * a.N_L + 16;
+  // the work plan from the parallels' costs (needs the ray tables)
+  if (a.n_rows > 0) row_cost_kernel<<<(unsigned)((a.n_rows * 32 + 255) / 256), 256, 0, st>>>(a);
+  plan_chunks_kernel<<<1, kPlanThreads, 0, st>>>(a);
   // the attribute is per device: set it on every launch (cheap)
-  if (a.mixed)
+  if (a.atmos.I != nullptr) launch_table_state(a, st);
+  if (a.mixed) {
     cudaFuncSetAttribute(integrate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
-  else
+    integrate_kernel<float><<<a.max_chunks, kThreads, bytes, st>>>(a);
+  } else {
     cudaFuncSetAttribute(integrate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
-  if (a.atmos.I != nullptr) launch_table_state(a, st);
-  if (a.mixed)
-    integrate_kernel<float><<<a.n_chunks, kThreads, bytes, st>>>(a);
-  else
-    integrate_kernel<double><<<a.n_chunks, kThreads, bytes, st>>>(a);
+    integrate_kernel<double><<<a.max_chunks, kThreads, bytes, st>>>(a);
+  }
   dim3 grid((a.N_E * a.N_P + 255) / 256, a.n_members);
   reduce_flux_kernel<<<grid, 256, 0, st>>>(a);
 }

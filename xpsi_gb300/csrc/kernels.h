@@ -66,17 +66,25 @@ struct IntegrateArgs {
   int N_E, N_L, N_P;
   const double *energies, *leaves, *phases;
   Atmos4D atmos;
-  // work chunks: chunk c covers rows [chunk_r0[c], chunk_r1[c]) of one member
-  int n_chunks;
-  const int64_t *chunk_r0, *chunk_r1;
-  double *partial;          // [n_chunks][N_E][N_P]
-  const int32_t *chunk_first;  // [n_members + 1] first chunk of each member
+  // work chunks, planned on the device from per-parallel costs before the
+  // integrator runs (integrator.cu, plan_chunks_kernel): chunk c covers rows
+  // [chunk_r0[c], chunk_r1[c]) of one member; the grid is max_chunks CTAs and
+  // CTA b takes chunk chunk_order[b] (heaviest first) while b < *chunk_count
+  int max_chunks;           // bound on the planned chunks (2 target + members)
+  int target_chunks;        // chunks the plan aims at
+  int64_t *chunk_r0, *chunk_r1;  // [max_chunks]
+  double *partial;          // [max_chunks][N_E][N_P], written by each chunk's CTA
+  int32_t *chunk_first;     // [n_members + 1] first chunk of each member
+  int32_t *chunk_order;     // [max_chunks]
+  int32_t *chunk_count;     // [1]
+  float *row_cost;          // [n_rows] scratch: estimated cost of each parallel
+  float *chunk_cost;        // [max_chunks] scratch
   // Num4D call-history state (see integrator.cu)
   uint8_t *row_has_eval, *row_last_top, *row_entry_top;  // [rows]
   int32_t *member_status;   // [n_members]
   double *flux;             // [..] at members[m].flux_off
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
-  double *slab;             // [n_chunks][nmu][nE] contracted Num4D table (scratch)
+  double *slab;             // [max_chunks][nmu][nE] contracted Num4D table (scratch)
   // power sums of the cell x phase sums (FP64 form; scratch, or null for the
   // per-cell form): per chunk 2 * w_cap * N_P run records, see integrator.cu
   unsigned char *wsum = nullptr;
