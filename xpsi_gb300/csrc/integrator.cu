@@ -297,6 +297,11 @@ struct AtmSmem {
   double *smu, *sE;      // inverse Lagrange denominators per stencil base, 4 each
   float *fgmu, *fgE, *fsmu, *fsE;  // FP32 copies for the mixed-precision form
   float *fgEo;           // [3 nE] offsets gE[b + i] - gE[b], i = 1..3 (mixed form)
+  // FP64 form with a contracted 4-D table: the offsets gE[b + i] - gE[b]
+  // (i = 1..3) and the inverse Lagrange denominators of the energy grid as
+  // double-float pairs (in the space of the mixed form's FP32 arrays and of sE)
+  DF *dgEo, *dsE;
+  int *xe;               // [nE] binary exponent of each energy column of the slab
   float *fphase;         // FP32 copy of the phase knots
   float *fphase_lo;      // phase knot minus its FP32 copy
   float *fcphi, *fcphi_lo;  // cell azimuths of the parallel as float pairs (<= kMaxCellsF)
@@ -417,6 +422,116 @@ __device__ __forceinline__ double eval_num4d_e(const Atmos4D &A, const AtmSmem &
   }
   if (I < 0.0) return 0.0;
   return I * p3;
+}
+
+// acc + a b in double-float, the sum held unnormalised in (s, c): s gathers
+// the rounded products through error-free sums, c the product and sum
+// errors; the caller renormalises once (two_sum of s and c)
+__device__ __forceinline__ void df_acc_mul(DF a, DF b, float &s, float &c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  float q;
+  two_sum(s, p, s, q);
+  c = __fadd_rn(c, __fadd_rn(q, e));
+}
+__device__ __forceinline__ DF df_norm(float s, float c) {
+  DF r;
+  two_sum(s, c, r.h, r.l);
+  return r;
+}
+
+// binary exponent x of |v| = f 2^x, f in [0.5, 1), from the bit pattern
+// (integer work); kZeroExp for zero and subnormal values
+constexpr int kZeroExp = -2100;
+__device__ __forceinline__ int binary_exponent(double v) {
+  const int e = (__double2hiint(v) >> 20) & 0x7ff;
+  return e == 0 ? kZeroExp : e - 1022;
+}
+// 2^x as a double from the bit pattern (0 below the normal range, the
+// largest power of two above it)
+__device__ __forceinline__ double pow2_double(int x) {
+  const int b = x + 1023;
+  if (b <= 0) return 0.0;
+  return __hiloint2double(min(b, 2046) << 20, 0);
+}
+// a double-float pair times 2^d, d <= 0 (exact down to the float range)
+__device__ __forceinline__ DF df_scale(DF a, int d) {
+  if (d < -125) return DF{0.0f, 0.0f};
+  const float f = __int_as_float((127 + d) << 23);
+  return DF{a.h * f, a.l * f};
+}
+
+// Num4D intensity of the FP64 form from a slab held as double-float pairs
+// whose energy-node columns are scaled by 2^-xe: the same stencils as
+// eval_num4d_e, with the energy coordinate's offset from the stencil base
+// formed in FP64 (as the reference's differences) and the Lagrange products
+// and the 4 x 4 contraction in double-float arithmetic (~2^-48 relative, on
+// the FP32 pipes).  The float pre-tests leave the FP64 comparisons to the
+// grid's ends and to ties of the rounded coordinate.  Returns the stencil
+// sum before the positive part (the caller clamps it at 0), in units of
+// `scale` (the largest of the four nodes' column scales).
+struct MuStencilDF {
+  int b2;
+  DF w2[4];
+};
+__device__ __forceinline__ MuStencilDF mu_stencil_df(const Atmos4D &A, const AtmSmem &as,
+                                                     double mu, bool clamp_mu) {
+  const MuStencil m = mu_stencil(A, as, mu, clamp_mu);
+  MuStencilDF d;
+  d.b2 = m.b2;
+#pragma unroll
+  for (int k = 0; k < 4; k++) d.w2[k] = df_split(m.w2[k]);
+  return d;
+}
+__device__ __forceinline__ DF eval_num4d_df(const Atmos4D &A, const AtmSmem &as, const DF *slab,
+                                            const MuStencilDF &m, double v3, double &scale) {
+  const int nE = A.nE;
+  float vf = (float)v3;
+  if (vf <= as.fgE[0] && v3 < as.gE[0]) {
+    v3 = as.gE[0];
+    vf = as.fgE[0];
+  }
+  if (vf >= as.fgE[nE - 1] && v3 > as.gE[nE - 1]) {
+    v3 = as.gE[nE - 1];
+    vf = as.fgE[nE - 1];
+  }
+  // stencil_base_guided with the FP64 step-down tested only where the
+  // rounded node does not lie below the rounded coordinate (g > v implies
+  // fg >= vf, rounding being monotone)
+  int lo = 0, hi = nE - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (as.fgE[mid] > vf) hi = mid; else lo = mid;
+  }
+  while (lo > 0 && as.fgE[lo] >= vf && as.gE[lo] > v3) lo--;
+  int b3 = lo - 1;
+  if (b3 < 0) b3 = 0;
+  if (b3 > nE - 4) b3 = nE - 4;
+  const DF u0 = df_split(v3 - as.gE[b3]);
+  const DF *o = as.dgEo + 3 * b3;
+  const DF u1 = df_sub(u0, o[0]), u2 = df_sub(u0, o[1]), u3 = df_sub(u0, o[2]);
+  const DF u01 = df_mul(u0, u1), u23 = df_mul(u2, u3);
+  const DF *S = as.dsE + 4 * b3;
+  // the nodes' column scales relative to the largest of the four (<= 1)
+  const int x0 = as.xe[b3], x1 = as.xe[b3 + 1], x2 = as.xe[b3 + 2], x3 = as.xe[b3 + 3];
+  const int xr = max(max(x0, x1), max(x2, x3));
+  scale = pow2_double(xr);
+  const DF w3[4] = {df_scale(df_mul(df_mul(u1, u23), S[0]), x0 - xr),
+                    df_scale(df_mul(df_mul(u0, u23), S[1]), x1 - xr),
+                    df_scale(df_mul(df_mul(u01, u3), S[2]), x2 - xr),
+                    df_scale(df_mul(df_mul(u01, u2), S[3]), x3 - xr)};
+  float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const DF *r = slab + (size_t)(m.b2 + k) * nE + b3;
+    float th = 0.0f, tl = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) df_acc_mul(w3[i], r[i], th, tl);
+    df_acc_mul(m.w2[k], df_norm(th, tl), sh, sl);
+  }
+  return df_norm(sh, sl);
 }
 
 // Akima piece (common.cuh akima_piece) in double-float arithmetic, with the
@@ -545,6 +660,7 @@ __host__ __device__ inline Layout make_layout(int N_L, int N_P, int N_E, int nmu
             + (size_t)(nmu + nE) * 5 * sizeof(double)  // Num4D grids + inverse denominators
             + (size_t)(nmu + nE) * 5 * sizeof(float)   // their FP32 copies (mixed form)
             + (size_t)3 * nE * sizeof(float)           // energy-grid node offsets (mixed)
+            + (size_t)nE * sizeof(int)                 // slab column exponents (FP64 form)
             + (size_t)(5 * N_L + 4 * kMaxCellsF + kMaxEnergiesF) * sizeof(float)
             + (size_t)N_R * sizeof(double)  // staged deflection table
             + (size_t)(ec + N_L) * sizeof(double)  // lgE, lzs
@@ -587,6 +703,11 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
     atm->fsmu = f; f += (size_t)4 * nmu;
     atm->fsE = f; f += (size_t)4 * nE;
     atm->fgEo = f; f += (size_t)3 * nE;
+    // the FP64 form's double-float energy-grid data reuse the mixed form's
+    // FP32 arrays (fsmu .. fgEo: 4 nmu + 7 nE floats >= 6 nE + 1) and sE
+    atm->dgEo = reinterpret_cast<DF *>((reinterpret_cast<uintptr_t>(atm->fsmu) + 7) &
+                                       ~uintptr_t(7));
+    atm->dsE = reinterpret_cast<DF *>(atm->sE);
     atm->fphase = f; f += N_L;
     atm->fphase_lo = f; f += N_L;
     atm->fcphi = f; f += kMaxCellsF;
@@ -597,6 +718,7 @@ __device__ GeoSmem carve(char *base, int N_L, int EC, double **coef, int nmu = 0
     atm->fabb = f; f += N_L;
     atm->fgeom = f; f += N_L;
     atm->fE = f; f += kMaxEnergiesF;
+    atm->xe = reinterpret_cast<int *>(f); f += nE;
     d = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(f) + 15) & ~uintptr_t(15));
   }
   int *ip = reinterpret_cast<int *>(d);
@@ -796,13 +918,18 @@ __device__ __forceinline__ bool cell_phase_sums_df(const CP &cp, const AR &area,
     if (iv < 0) return false;
     hint = iv;
     const DF A = area(j);
+    // every energy slot of the task is evaluated (slots past the chunk's
+    // energies read pieces of the coefficient area that the caller ignores)
+    // and the positive part is a select: no branch inside the cell, so the
+    // kEPT independent double-float chains interleave
 #pragma unroll
     for (int e = 0; e < kEPT; e++) {
-      if (pb + e < ne) {
-        const PieceDF q = pc[(pb + e) * N_L + iv];
-        const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
-        if (sv.h > 0.0f || add_all) acc[e] = df_fma(A, sv, acc[e]);
-      }
+      const PieceDF q = pc[(pb + e) * N_L + iv];
+      const DF sv = df_fma(t, df_fma(t, df_fma(t, q.k3, q.k2), q.k1), q.y);
+      const DF nx = df_fma(A, sv, acc[e]);
+      const bool take = add_all || sv.h > 0.0f;
+      acc[e].h = take ? nx.h : acc[e].h;
+      acc[e].l = take ? nx.l : acc[e].l;
     }
   }
   return true;
@@ -941,8 +1068,8 @@ constexpr int kDeferRuns = 24;  // sign-changing (run, energy) items noted per t
 template <typename CP, typename AR>
 __device__ __forceinline__ void run_sums(const CP &cp, const AR &area, const int32_t *rad,
                                          const WRuns &w, const int *nruns, int k,
-                                         const PieceDF *pc, const uint8_t *cls, int N_L, int pb,
-                                         int ne, DF (&acc)[kEPT]) {
+                                         const PieceDF *pc, const uint8_t *cls, int N_L, int EC,
+                                         int pb, int ne, DF (&acc)[kEPT]) {
   uint32_t defer[kDeferRuns];
   int nd = 0;
   for (int half = 0; half < 2; half++) {
@@ -966,13 +1093,16 @@ __device__ __forceinline__ void run_sums(const CP &cp, const AR &area, const int
       }
 #pragma unroll
       for (int e = 0; e < kEPT; e++) {
-        if (pb + e < ne) {
+        {  // slots past the chunk's energies have class 0
           const int pi = (pb + e) * N_L + iv;
-          const uint8_t c = cls[pi];
+          const uint8_t c = cls[iv * EC + pb + e];
           const PieceDF q = pc[pi];
-          const DF v =
-              df_fma(q.k3, W3, df_fma(q.k2, W2, df_fma(q.k1, W1, df_fma(q.y, W0, acc[e]))));
-          if (c == 1) acc[e] = v;
+          float sh = acc[e].h, sl = acc[e].l;
+          df_acc_mul(q.y, W0, sh, sl);
+          df_acc_mul(q.k1, W1, sh, sl);
+          df_acc_mul(q.k2, W2, sh, sl);
+          df_acc_mul(q.k3, W3, sh, sl);
+          if (c == 1) acc[e] = fast_two_sum(sh, sl);
           if (c == 2) {
             if (nd < kDeferRuns) {
               defer[nd++] = (uint32_t)half | ((uint32_t)r << 1) | ((uint32_t)e << 12);
@@ -1098,6 +1228,18 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     }
     slab = tab2 ? const_cast<double *>(a.atmos.I) : a.slab + (size_t)chunk * nmu * nEt;
     slabf = reinterpret_cast<float *>(slab);
+    if (!kMixed && !tab2) {
+      // the energy grid's node offsets and inverse denominators as
+      // double-float pairs for eval_num4d_df (sE converted in place)
+      for (int t = threadIdx.x; t < 3 * nEt; t += blockDim.x) {
+        const int b = t / 3, i = t - 3 * b + 1;
+        as.dgEo[t] = b + i < nEt ? df_split(as.gE[b + i] - as.gE[b]) : DF{0.0f, 0.0f};
+      }
+      for (int t = threadIdx.x; t < 4 * nEt; t += blockDim.x) {
+        const double v = as.sE[t];
+        as.dsE[t] = df_split(v);
+      }
+    }
     __syncthreads();
   }
   if (kMixed && !num4d) {
@@ -1173,6 +1315,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
         }
       } else {
         const double *base = a.atmos.I + bT * S0t + bg * S1t;
+        double mx = 0.0;
         for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
           double r = 0.0;
 #pragma unroll
@@ -1182,14 +1325,36 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                        wg[3] * __ldg(q + 3 * S1t);
             r += wT[ii] * u;
           }
-          if (kMixed) slabf[t] = (float)r;
-          else slab[t] = r;
+          if (kMixed) {
+            slabf[t] = (float)r;
+          } else {
+            slab[t] = r;
+            mx = fmax(mx, fabs(r));
+          }
+        }
+        if (!kMixed) {
+          // the FP64 form keeps the slab as double-float pairs, each energy
+          // node's column (all mu) scaled by 2^-xe[e] (exact), xe the binary
+          // exponent of its largest value, so that the pairs keep full
+          // relative precision across the table's exponential tail
+          for (int e = threadIdx.x; e < nEt; e += blockDim.x) as.xe[e] = kZeroExp;
+          __syncthreads();
+          for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x)
+            atomicMax(&as.xe[t % nEt], binary_exponent(slab[t]));
+          __syncthreads();
+          DF *slabd = reinterpret_cast<DF *>(slab);
+          for (int t = threadIdx.x; t < (int)S1t; t += blockDim.x) {
+            const double r = slab[t];
+            slabd[t] = df_split(r * pow2_double(-as.xe[t % nEt]));
+          }
         }
       }
       E_eff = (kKB / kKeV) * pow(10.0, c.vec0);
       p3 = pow(10.0, 3.0 * vT);
       __syncthreads();
     }
+    // the FP64 form's double-float slab (energy columns scaled by 2^-xe)
+    const DF *slabd = reinterpret_cast<const DF *>(slab);
     const double kT = (kKB / kKeV) * pow(10.0, c.vec0);
     const float kT_f = (float)kT;
     // mixed form: the FP32 roundings of the constant factors norm and
@@ -1307,6 +1472,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           int mu_col = -1;
           MuStencil ms{};
           MuStencilF msf{};
+          MuStencilDF msd{};
+          double col_factor = 0.0;  // norm 10^(3 log T) GEOM of the column
           for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
             const int pl = t / N_L, col = t - pl * N_L;
             const int p = e0 + pl;
@@ -1336,7 +1503,31 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                 y = (WT)((float)norm * I_E * as.fgeom[s]);
               } else {
                 double I_E;
-                if (num4d) {
+                bool done = false;
+                if (num4d && !tab2) {
+                  // the contracted 4-D table in double-float (eval_num4d_df);
+                  // with beaming option 3 every call is followed by calls up
+                  // to mu = 1, so no out-of-table mu is ever clamped
+                  const double v3 = g.lgE[pl] - g.lzs[s];
+                  if (s != mu_col) {
+                    msd = mu_stencil_df(a.atmos, as, g.ABB[s], false);
+                    col_factor = norm * p3 * g.GEOM[s];
+                    mu_col = s;
+                  }
+                  double scale;
+                  DF I = (p == 0 && g.clamp0[s] && M.beam_opt != 3)
+                             ? eval_num4d_df(a.atmos, as, slabd,
+                                             mu_stencil_df(a.atmos, as, g.ABB[s], true), v3,
+                                             scale)
+                             : eval_num4d_df(a.atmos, as, slabd, msd, v3, scale);
+                  if (I.h < 0.0f) I = DF{0.0f, 0.0f};
+                  if (M.beam_opt == 0 && !corr) {
+                    y = df_value(I) * scale * col_factor;
+                    done = true;
+                  } else {
+                    I_E = df_value(I) * scale * p3;
+                  }
+                } else if (num4d) {
                   // atm 6: E' = E / Z in electron rest energies (:457-458)
                   const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
                                           : g.lgE[pl] - g.lzs[s];
@@ -1357,11 +1548,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                   // the burst blackbody's limb darkening (hot_BB_burst.pyx)
                   if (M.atm == 3) I_E = I_E * (0.421 + 0.868 * g.ABB[s]);
                 }
-                const double I_c =
-                    corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
-                // with a beaming modification the raw intensity is kept here
-                // and modified in the pass below
-                y = (WT)(M.beam_opt > 0 ? I_E : (I_E * norm - I_c) * g.GEOM[s]);
+                if (!done) {
+                  const double I_c =
+                      corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
+                  // with a beaming modification the raw intensity is kept
+                  // here and modified in the pass below
+                  y = (WT)(M.beam_opt > 0 ? I_E : (I_E * norm - I_c) * g.GEOM[s]);
+                }
               }
             }
             co4[pl * N_L + col].y = y;
@@ -1381,8 +1574,13 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
               const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951 : g.lgE[pl] - g.lzs[s];
               const double Ep = erest ? v3 : a.energies[p] / g.Z[s];
               I_E = beamed_intensity(M.beam_opt, s_beam, Ep, g.ABB[s], I_raw, [&](double mu_k) {
-                return eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, mu_k, false), v3,
-                                    p3);
+                if (tab2)
+                  return eval_num4d_e(a.atmos, as, slab, mu_stencil(a.atmos, as, mu_k, false),
+                                      v3, p3);
+                double scale;
+                const DF I = eval_num4d_df(a.atmos, as, slabd,
+                                           mu_stencil_df(a.atmos, as, mu_k, false), v3, scale);
+                return I.h < 0.0f ? 0.0 : df_value(I) * scale * p3;
               });
             } else {
               const double Ep = a.energies[p] / g.Z[s];
@@ -1474,17 +1672,23 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             }
           }
           __syncthreads();
-          if (use_w) {
-            // every value is added with the elsewhere correction (:593-594)
-            for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
-              const int iv = t % N_L;
-              uint8_t cl = 0;
-              if (iv < N_L - 1)
-                cl = corr ? 1 : piece_class(pc[t], as.fphase[iv + 1] - as.fphase[iv]);
-              s_cls[t] = cl;
+          // the class of every piece for the power sums, [N_L][EC] (0
+          // beyond the chunk's energies); every nonzero value is added with
+          // the elsewhere correction (:593-594)
+          if (use_w) for (int t = threadIdx.x; t < EC * N_L; t += blockDim.x) {
+            const int iv = t / EC, pl = t - iv * EC;
+            uint8_t cl = 0;
+            if (pl < ne && iv < N_L - 1) {
+              const PieceDF &q = pc[pl * N_L + iv];
+              cl = piece_class(q, as.fphase[iv + 1] - as.fphase[iv]);
+              if (corr && cl == 0 &&
+                  (q.y.h != 0.0f || q.k1.h != 0.0f || q.k2.h != 0.0f || q.k3.h != 0.0f))
+                cl = 1;
+              if (corr) cl = cl ? 1 : 0;
             }
-            __syncthreads();
+            s_cls[t] = cl;
           }
+          if (use_w) __syncthreads();
         }
         // cell x phase accumulation (:571-598)
         for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
@@ -1518,7 +1722,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
             if (use_w) {
               run_sums(cp, ar, rad, wr, s_nruns, k, reinterpret_cast<const PieceDF *>(co4), s_cls,
-                       N_L, pb, ne, acc);
+                       N_L, EC, pb, ne, acc);
             } else if (!cell_phase_sums_df(cp, ar, M.S1, rad,
                                            reinterpret_cast<const PieceDF *>(co4), N_L, pb, ne,
                                            corr, acc)) {
