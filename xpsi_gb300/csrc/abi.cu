@@ -296,16 +296,27 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
       (rc = dalloc(dslab, (size_t)n_chunks * d->atmos.nmu * d->atmos.nE * sizeof(double), st)))
     return rc;
   CK(cudaMemsetAsync(d->mesh_status, 0, n_meshes * sizeof(int32_t), st));
-  // run records of the FP64 form's power sums, per chunk (parallels of up
-  // to 1023 cells and 1024 leaves; beyond that the per-cell form runs)
+  // run records of the FP64 form's power sums (parallels of up to 1023
+  // cells and 1024 leaves; beyond that the per-cell form runs)
   Dev dwsum;
   int w_cap = 0;
   int max_cells = 0;
   for (int m = 0; m < n_meshes; m++) max_cells = std::max(max_cells, (int)meshes[m].S1);
   const bool use_w = !mixed && max_cells <= 1023 && N_L <= 1024 && wsum_enabled();
+  // a slot per CTA that can be resident (at most 2 per SM), twice over
+  int w_slots = 0;
+  Dev dwbusy, dpart2;
   if (use_w) {
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    w_slots = 4 * std::max(1, sms);
     const size_t w_chunk = xg::integrate_wsum_bytes(N_P, max_cells, &w_cap);
-    if ((rc = dalloc(dwsum, (size_t)n_chunks * w_chunk, st))) return rc;
+    if ((rc = dalloc(dwsum, (size_t)w_slots * w_chunk, st)) ||
+        (rc = dalloc(dwbusy, (size_t)w_slots * sizeof(int32_t), st)) ||
+        (rc = dalloc(dpart2, part_n * sizeof(double), st)))
+      return rc;
+    CK(cudaMemsetAsync(dwbusy.p, 0, (size_t)w_slots * sizeof(int32_t), st));
   }
 
   xg::IntegrateArgs a{};
@@ -344,6 +355,9 @@ int integrate_batch_impl(int n_meshes, const xgpu_mesh *meshes, int64_t n_rows, 
   a.slab = d->atmos.intensity != nullptr && !table2d ? dslab.as<double>() : nullptr;
   a.wsum = use_w ? dwsum.as<unsigned char>() : nullptr;
   a.w_cap = w_cap;
+  a.w_slots = w_slots;
+  a.w_slot_busy = use_w ? dwbusy.as<int32_t>() : nullptr;
+  a.partial2 = use_w ? dpart2.as<double>() : nullptr;
   a.mixed = mixed;
   xg::launch_integrate(a, st);
   CK(cudaGetLastError());

@@ -1055,7 +1055,7 @@ __device__ __forceinline__ DF run_cells(const CP &cp, const AR &area, const int3
 }
 
 // sums at signal phase k for the energies pb .. pb+kEPT-1 of the chunk from
-// the power sums of its runs.  The lanes of a warp take consecutive phases,
+// the power sums of the runs of one half of the parallel's cells.  The lanes of a warp take consecutive phases,
 // so the r-th runs of neighbouring lanes lie in different intervals and
 // carry different piece classes: every energy's power-sum term is formed on
 // every lane and kept where the class is 1 (a select, no branch), and the
@@ -1067,58 +1067,54 @@ constexpr int kDeferRuns = 24;  // sign-changing (run, energy) items noted per t
 
 template <typename CP, typename AR>
 __device__ __forceinline__ void run_sums(const CP &cp, const AR &area, const int32_t *rad,
-                                         const WRuns &w, const int *nruns, int k,
+                                         const WRuns &w, const int *nruns, int k, int half,
                                          const PieceDF *pc, const uint8_t *cls, int N_L, int EC,
-                                         int pb, int ne, DF (&acc)[kEPT]) {
+                                         int pb, DF (&acc)[kEPT]) {
   uint32_t defer[kDeferRuns];
   int nd = 0;
-  for (int half = 0; half < 2; half++) {
-    const int n = nruns[half * w.N_P + k];
-    float4 a4, b4;
-    int meta = 0;
-    if (n > 0) {
-      const size_t ri = w.rec(half, 0, k);
+  const int n = nruns[half * w.N_P + k];
+  float4 a4, b4;
+  int meta = 0;
+  if (n > 0) {
+    const size_t ri = w.rec(half, 0, k);
+    a4 = w.wa[ri];
+    b4 = w.wb[ri];
+    meta = w.meta[ri];
+  }
+  for (int r = 0; r < n; r++) {
+    const DF W0{a4.x, a4.y}, W1{a4.z, a4.w}, W2{b4.x, b4.y}, W3{b4.z, b4.w};
+    const int iv = meta & 1023;
+    if (r + 1 < n) {
+      const size_t ri = w.rec(half, r + 1, k);
       a4 = w.wa[ri];
       b4 = w.wb[ri];
       meta = w.meta[ri];
     }
-    for (int r = 0; r < n; r++) {
-      const DF W0{a4.x, a4.y}, W1{a4.z, a4.w}, W2{b4.x, b4.y}, W3{b4.z, b4.w};
-      const int iv = meta & 1023;
-      if (r + 1 < n) {
-        const size_t ri = w.rec(half, r + 1, k);
-        a4 = w.wa[ri];
-        b4 = w.wb[ri];
-        meta = w.meta[ri];
-      }
+    // slots past the chunk's energies have class 0
 #pragma unroll
-      for (int e = 0; e < kEPT; e++) {
-        {  // slots past the chunk's energies have class 0
-          const int pi = (pb + e) * N_L + iv;
-          const uint8_t c = cls[iv * EC + pb + e];
-          const PieceDF q = pc[pi];
-          float sh = acc[e].h, sl = acc[e].l;
-          df_acc_mul(q.y, W0, sh, sl);
-          df_acc_mul(q.k1, W1, sh, sl);
-          df_acc_mul(q.k2, W2, sh, sl);
-          df_acc_mul(q.k3, W3, sh, sl);
-          if (c == 1) acc[e] = fast_two_sum(sh, sl);
-          if (c == 2) {
-            if (nd < kDeferRuns) {
-              defer[nd++] = (uint32_t)half | ((uint32_t)r << 1) | ((uint32_t)e << 12);
-            } else {
-              const int m = w.meta[w.rec(half, r, k)];
-              acc[e] = df_add(acc[e], run_cells(cp, area, rad, iv, (m >> 10) & 1023,
-                                                (m >> 20) & 1023, q, DF{0.0f, 0.0f}));
-            }
-          }
+    for (int e = 0; e < kEPT; e++) {
+      const uint8_t c = cls[iv * EC + pb + e];
+      const PieceDF q = pc[(pb + e) * N_L + iv];
+      float sh = acc[e].h, sl = acc[e].l;
+      df_acc_mul(q.y, W0, sh, sl);
+      df_acc_mul(q.k1, W1, sh, sl);
+      df_acc_mul(q.k2, W2, sh, sl);
+      df_acc_mul(q.k3, W3, sh, sl);
+      if (c == 1) acc[e] = fast_two_sum(sh, sl);
+      if (c == 2) {
+        if (nd < kDeferRuns) {
+          defer[nd++] = ((uint32_t)r << 4) | (uint32_t)e;
+        } else {
+          const int m = w.meta[w.rec(half, r, k)];
+          acc[e] = df_add(acc[e], run_cells(cp, area, rad, iv, (m >> 10) & 1023,
+                                            (m >> 20) & 1023, q, DF{0.0f, 0.0f}));
         }
       }
     }
   }
   for (int d = 0; d < nd; d++) {
     const uint32_t it = defer[d];
-    const int half = it & 1, r = (it >> 1) & 2047, ed = (int)(it >> 12);
+    const int r = (int)(it >> 4), ed = (int)(it & 15u);
     const int m = w.meta[w.rec(half, r, k)];
     const int iv = m & 1023;
     const DF add = run_cells(cp, area, rad, iv, (m >> 10) & 1023, (m >> 20) & 1023,
@@ -1204,11 +1200,28 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   // a beaming modification's (abb, bbb, cbb, dbb, nimu) for the parallel
   __shared__ double s_beam[5];
   // power-sum form (FP64 path with scratch): run counts per (cell half,
-  // signal phase) and the class of every piece of the chunk
-  const bool use_w = !kMixed && a.wsum != nullptr;
+  // signal phase) and the class of every piece of the chunk; the run
+  // records live in one of a.w_slots scratch slots, taken for the CTA's
+  // lifetime (at most 2 CTAs per SM are resident, the pool has more slots;
+  // a CTA that finds none after a bounded search runs the per-cell form)
+  __shared__ int s_wslot, s_next;
+  bool use_w = !kMixed && a.wsum != nullptr;
+  if (use_w) {
+    if (threadIdx.x == 0) {
+      int got = -1;
+      for (int i = 0; i < 4 * a.w_slots && got < 0; i++) {
+        const int sl = (int)((blockIdx.x + i) % a.w_slots);
+        if (atomicCAS(&a.w_slot_busy[sl], 0, 1) == 0) got = sl;
+      }
+      s_wslot = got;
+    }
+    __syncthreads();
+    use_w = s_wslot >= 0;
+  }
   int *s_nruns = reinterpret_cast<int *>(g.sc_exp + EC);
   uint8_t *s_cls = reinterpret_cast<uint8_t *>(s_nruns + 2 * N_P);
-  const WRuns wr = use_w ? wruns_of(a.wsum + (size_t)chunk * integrate_wsum_bytes_dev(N_P, a.w_cap),
+  const WRuns wr = use_w ? wruns_of(a.wsum + (size_t)s_wslot *
+                                                 integrate_wsum_bytes_dev(N_P, a.w_cap),
                                     a.w_cap, N_P)
                          : WRuns{};
   double *slab = nullptr;
@@ -1249,7 +1262,12 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
   }
   const double norm = num4d ? kErg / kHKeV : kErg * kPlanck;
   double *part = a.partial + (size_t)chunk * N_E * N_P;
-  for (int t = threadIdx.x; t < N_E * N_P; t += blockDim.x) part[t] = 0.0;
+  // the power sums' second cell half adds into its own partial
+  double *part2 = a.partial2 ? a.partial2 + (size_t)chunk * N_E * N_P : nullptr;
+  for (int t = threadIdx.x; t < N_E * N_P; t += blockDim.x) {
+    part[t] = 0.0;
+    if (part2) part2[t] = 0.0;
+  }
   __syncthreads();
   const double mu_max = num4d ? a.atmos.mu[a.atmos.nmu - 1] : 0.0;
   const double mu_top3 = num4d ? a.atmos.mu[a.atmos.nmu - 3] : 0.0;
@@ -1386,7 +1404,10 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
       __syncthreads();
       const int term = g.flags[0], invis = g.flags[1];
       if (term) {
-        if (threadIdx.x == 0) atomicExch(&a.member_status[m], (int)kPulseFail);
+        if (threadIdx.x == 0) {
+          atomicExch(&a.member_status[m], (int)kPulseFail);
+          if (use_w) atomicExch(&a.w_slot_busy[s_wslot], 0);
+        }
         return;
       }
       if (invis) break;
@@ -1688,10 +1709,23 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             }
             s_cls[t] = cl;
           }
+          if (threadIdx.x == 0) s_next = blockDim.x;
           if (use_w) __syncthreads();
         }
-        // cell x phase accumulation (:571-598)
-        for (int task = threadIdx.x; task < ntasks; task += blockDim.x) {
+        // cell x phase accumulation (:571-598).  The power-sum form splits
+        // each task into its two cell halves (units u < ntasks: half 0,
+        // u >= ntasks: half 1, adding into part2); a warp takes its first 32
+        // consecutive units by index and further blocks of 32 from a shared
+        // counter, so the uneven run counts of the phases even out over the
+        // CTA while a warp's lanes keep consecutive phases
+        const int nunits = use_w ? 2 * ntasks : ntasks;
+        const int lane = threadIdx.x & 31;
+        for (int u = threadIdx.x; u - lane < nunits;
+             u = use_w ? __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&s_next, 32) : 0, 0) + lane
+                       : u + (int)blockDim.x) {
+          if (u >= nunits) continue;
+          const int half = u >= ntasks ? 1 : 0;
+          const int task = u - half * ntasks;
           const int k = task % N_P, grp = task / N_P;
           const int pb = grp * kEPT;
           if (pb >= ne) continue;
@@ -1721,23 +1755,28 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
             for (int e = 0; e < kEPT; e++) acc[e] = DF{0.0f, 0.0f};
             const AreaDF ar{cached ? as.fcarea : nullptr, cached ? as.fcarea_lo : nullptr, cellA};
             if (use_w) {
-              run_sums(cp, ar, rad, wr, s_nruns, k, reinterpret_cast<const PieceDF *>(co4), s_cls,
-                       N_L, EC, pb, ne, acc);
+              run_sums(cp, ar, rad, wr, s_nruns, k, half,
+                       reinterpret_cast<const PieceDF *>(co4), s_cls, N_L, EC, pb, acc);
             } else if (!cell_phase_sums_df(cp, ar, M.S1, rad,
                                            reinterpret_cast<const PieceDF *>(co4), N_L, pb, ne,
                                            corr, acc)) {
               atomicExch(&a.member_status[m], (int)kPulseFail);
               continue;
             }
+            double *dst = half ? part2 : part;
 #pragma unroll
             for (int e = 0; e < kEPT; e++)
               if (pb + e < ne)
-                part[(size_t)(e0 + pb + e) * N_P + k] += ldexp(df_value(acc[e]), g.sc_exp[pb + e]);
+                dst[(size_t)(e0 + pb + e) * N_P + k] += ldexp(df_value(acc[e]), g.sc_exp[pb + e]);
           }
         }
         __syncthreads();
       }
     }
+  }
+  if (use_w) {
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(&a.w_slot_busy[s_wslot], 0);
   }
   if (threadIdx.x == 0 && a.flop_counter && flops > 0.0) atomicAdd(a.flop_counter, flops);
 }
@@ -2287,7 +2326,9 @@ __global__ void reduce_flux_kernel(IntegrateArgs a) {
   const int c0 = a.chunk_first[m], c1 = a.chunk_first[m + 1];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int c = c0; c < c1; c++) s += a.partial[(size_t)c * n + t];
+    for (int c = c0; c < c1; c++)
+      s += a.partial2 ? a.partial[(size_t)c * n + t] + a.partial2[(size_t)c * n + t]
+                      : a.partial[(size_t)c * n + t];
     const int p = t / a.N_P;
     a.flux[M.flux_off + t] = s / (a.energies[p] * kKeV);
   }

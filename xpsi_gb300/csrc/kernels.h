@@ -74,6 +74,7 @@ struct IntegrateArgs {
   int target_chunks;        // chunks the plan aims at
   int64_t *chunk_r0, *chunk_r1;  // [max_chunks]
   double *partial;          // [max_chunks][N_E][N_P], written by each chunk's CTA
+  double *partial2 = nullptr;  // the same for the power sums' second cell half, or null
   int32_t *chunk_first;     // [n_members + 1] first chunk of each member
   int32_t *chunk_order;     // [max_chunks]
   int32_t *chunk_count;     // [1]
@@ -86,9 +87,12 @@ struct IntegrateArgs {
   double *flop_counter;     // algorithmic FLOPs of the launch (atomic), or null
   double *slab;             // [max_chunks][nmu][nE] contracted Num4D table (scratch)
   // power sums of the cell x phase sums (FP64 form; scratch, or null for the
-  // per-cell form): per chunk 2 * w_cap * N_P run records, see integrator.cu
+  // per-cell form): w_slots slots of 2 * w_cap * N_P run records, a CTA
+  // holding one (w_slot_busy[slot] = 1) while it runs, see integrator.cu
   unsigned char *wsum = nullptr;
   int w_cap = 0;            // runs per (cell half, signal phase)
+  int w_slots = 0;
+  int32_t *w_slot_busy = nullptr;  // [w_slots], zero before the launch
   int mixed;                // 0: FP64 drop-in, 1: mixed-precision form
   double *flux_q = nullptr, *flux_u = nullptr;  // Stokes Q, U (launch_stokes only)
   // Stokes Q of a 2-D table atmosphere (atm 4, 6; launch_stokes only):
