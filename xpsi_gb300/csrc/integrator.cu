@@ -27,6 +27,7 @@
 // other energy extrapolates the last stencil.  The kernels reproduce the
 // reference's single-thread call order exactly: a geometry pre-pass and a
 // per-mesh scan hand each parallel the state its first evaluation sees.
+#include <climits>
 #include <type_traits>
 
 #include "common.cuh"
@@ -456,6 +457,40 @@ __device__ __forceinline__ double pow2_double(int x) {
   if (b <= 0) return 0.0;
   return __hiloint2double(min(b, 2046) << 20, 0);
 }
+// v 2^e, as ldexp(v, e) (one rounding at most), by a product with the
+// power of two where that is a normal double
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+  return (e >= -1022 && e <= 1023) ? v * pow2_double(e) : ldexp(v, e);
+}
+// the largest frexp exponent of |v| over a lane's values, from the bit
+// patterns (integer work): fold() each value, exponent() at the end gives
+// what frexp(max |v|) gives, 0 when the largest is 0, infinite or NaN
+// throughout (NaNs are skipped as fmax skips them; an infinity gives 0)
+struct MaxExponent {
+  int e = INT_MIN;
+  bool inf = false;
+  __device__ __forceinline__ void fold(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int f = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    if (f == 0x7ff) {
+      inf = inf || m == 0ull;
+    } else if (f != 0) {
+      e = max(e, f - 1022);
+    } else if (m != 0ull) {
+      e = max(e, -1010 - __clzll((long long)m));
+    }
+  }
+  __device__ __forceinline__ void merge_warp() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+      inf = __shfl_xor_sync(0xffffffffu, (int)inf, o) != 0 || inf;
+    }
+  }
+  __device__ __forceinline__ int exponent() const { return (inf || e == INT_MIN) ? 0 : e; }
+};
+
 // a double-float pair times 2^d, d <= 0 (exact down to the float range)
 __device__ __forceinline__ DF df_scale(DF a, int d) {
   if (d < -125) return DF{0.0f, 0.0f};
@@ -1654,20 +1689,16 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           // keep the row's full relative precision whatever its magnitude
           const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
           for (int pl = warp; pl < ne; pl += kThreads / 32) {
-            double mx = 0.0;
-            for (int col = lane; col < N_L; col += 32)
-              mx = fmax(mx, fabs((double)co4[pl * N_L + col].y));
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            int ex = 0;
-            if (mx > 0.0 && mx <= 1.7976931348623157e308) frexp(mx, &ex);
-            if (lane == 0) g.sc_exp[pl] = ex;
+            MaxExponent mx;
+            for (int col = lane; col < N_L; col += 32) mx.fold((double)co4[pl * N_L + col].y);
+            mx.merge_warp();
+            if (lane == 0) g.sc_exp[pl] = mx.exponent();
           }
           __syncthreads();
           PieceDF *pc = reinterpret_cast<PieceDF *>(co4);
           for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
             const double v = (double)co4[t].y;
-            pc[t].y = df_split(ldexp(v, -g.sc_exp[t / N_L]));
+            pc[t].y = df_split(scale_pow2(v, -g.sc_exp[t / N_L]));
           }
           __syncthreads();
           for (int t = threadIdx.x; t < ne * strips; t += blockDim.x) {
@@ -1767,7 +1798,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
 #pragma unroll
             for (int e = 0; e < kEPT; e++)
               if (pb + e < ne)
-                dst[(size_t)(e0 + pb + e) * N_P + k] += ldexp(df_value(acc[e]), g.sc_exp[pb + e]);
+                dst[(size_t)(e0 + pb + e) * N_P + k] +=
+                    scale_pow2(df_value(acc[e]), g.sc_exp[pb + e]);
           }
         }
         __syncthreads();
