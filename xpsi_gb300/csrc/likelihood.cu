@@ -17,9 +17,36 @@
 // integral :423-429).
 #include "common.cuh"
 #include "kernels.h"
+#include "log_table.h"
 
 namespace xg {
 namespace {
+
+// Natural logarithm of a positive, normal double-float m with a table:
+// m = 2^e f, f in [0.75, 1.5) (as df_log), then f = c (f / c) with c the
+// nearest node 0.75 + i / 128 (|f / c - 1| <= 1 / 192) and
+//   ln f = ln c + 2 atanh(s),  s = (f - c) / (f + c),  |s| <= 1 / 385,
+// the series 2 s (1 + s^2 / 3 + s^4 / 5) truncated below 1e-17 relative
+// (the s^4 / 5 term in float, its rounding ~1e-19); ln c from the table
+// (gen_log_table.py, float pairs).  About half the work of df_log's
+// 11-term series.  tab: the table in shared memory.
+__device__ __forceinline__ DF df_log_t(DF m, const DF *tab) {
+  const DF ln2{0.6931471824645996f, -1.9046542121259336e-09f};
+  const DF third{0.3333333432674408f, -9.934107758624577e-09f};
+  const int bits = __float_as_int(m.h);
+  int e = ((bits >> 23) & 0xff) - 127;
+  if ((bits & 0x7fffff) >= 0x400000) e += 1;
+  const float sc = __int_as_float((127 - e) << 23);
+  const DF f{__fmul_rn(m.h, sc), __fmul_rn(m.l, sc)};
+  int i = __float2int_rn((f.h - 0.75f) * 128.0f);
+  i = min(max(i, 0), XG_LOGT_N - 1);
+  const float c = 0.75f + (float)i * 0.0078125f;
+  const DF s = df_div(df_add(f, DF{-c, 0.0f}), df_add(f, DF{c, 0.0f}));
+  const DF s2 = df_mul(s, s);
+  const float s4_5 = __fmul_rn(__fmul_rn(s2.h, s2.h), 0.2f);
+  const DF p = df_add(DF{1.0f, 0.0f}, df_add(df_mul(s2, third), DF{s4_5, 0.0f}));
+  return df_add(df_fma(DF{(float)e, 0.0f}, ln2, tab[i]), df_mul(df_add(s, s), p));
+}
 
 constexpr int kWarps = 4;
 constexpr int kMaxB = 64;      // phase bins per channel held in shared memory
@@ -42,6 +69,7 @@ struct Marg {
   double Bi;
   const DF *q;
   const float *dataf;
+  const DF *logt;  // df_log_t's table (shared memory)
 };
 
 // :84-138, as the reference writes it
@@ -73,7 +101,7 @@ __device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
   for (int j = 0; j < m.n; j++) {
     const DF r = df_fma(dB, m.q[j], one);
     if (!(r.h > 0.0f)) return marginal_integrand_direct(m, B);
-    if (m.dataf[j] != 0.0f) acc = df_fma(DF{m.dataf[j], 0.0f}, df_log(r), acc);
+    if (m.dataf[j] != 0.0f) acc = df_fma(DF{m.dataf[j], 0.0f}, df_log_t(r, m.logt), acc);
   }
   return exp(df_value(acc) - (double)m.n * m.SCALE * dBd);
 }
@@ -324,6 +352,9 @@ __device__ double warp_marginal(const Marg &m, WarpSmem &w, int lane, double a, 
 
 __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   __shared__ WarpSmem ws[kWarps];
+  __shared__ DF s_logt[XG_LOGT_N];
+  for (int t = threadIdx.x; t < XG_LOGT_N; t += blockDim.x) s_logt[t] = DF{XG_LOGT[t][0], XG_LOGT[t][1]};
+  __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long gw = (long)blockIdx.x * kWarps + wid;
   if (gw >= (long)a.n_vec * a.K) return;
@@ -380,7 +411,7 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
     if (limit > 0.0) flag = 1;
   }
   const double *support = a.support + 2 * (size_t)ch;
-  Marg m{B, SCALE, T, 0.0, w.data, w.star, 0, 0.0, w.q, w.dataf};
+  Marg m{B, SCALE, T, 0.0, w.data, w.star, 0, 0.0, w.q, w.dataf, s_logt};
   double Bfinal = 0.0;
   if (!flag) {
     av_STAR /= n;
