@@ -152,13 +152,13 @@ def shard_vectors(V, rank, world, seed=3):
 PIPE_COUNTS = {
     "vectors": 64,
     "cost_model_flop": 482067568128.0,
-    "fp64_flop": 2 * 6955209850 + 6428283081 + 2293872409,
-    "fp32_flop": 2 * 136060681846 + 46795769114 + 552848550742,
-    "dram_bytes": 745280768 + 1360537856,
-    "fp64_pipe_active": 0.593,
-    "fma_pipe_active": 0.274,
-    "issue_active": 0.406,
-    "duration_ms": 208.3,
+    "fp64_flop": 2 * 3659919382 + 2194393971 + 2365114391,
+    "fp32_flop": 2 * 163498592549 + 57528786183 + 634940702172,
+    "dram_bytes": 987693312 + 2736122112,
+    "fp64_pipe_active": 0.571,
+    "fma_pipe_active": 0.380,
+    "issue_active": 0.533,
+    "duration_ms": 69.2,
     "capture": "ncu --metrics (instruction classes, pipe activity, dram bytes) -k "
                "regex:integrate_kernel -s 1 -c 1, python bench.py --vectors 64 --steps 1 "
                "--warmup 3 --legs none",
@@ -382,9 +382,13 @@ def roofline(int_ms, int_flops, V):
                            "(MEASURED_PEAKS.json has HBM and bf16 only)",
             "counts_source": PIPE_COUNTS["capture"] + " (%d vectors; scaled by %.3f)"
                              % (PIPE_COUNTS["vectors"], scale),
-            "note": "the binding pipe is FP64 (ncu: %.0f %% of active cycles, about half of "
-                    "its instructions compares and conversions); frac is its arithmetic "
-                    "rate over its FMA peak" % (100 * PIPE_COUNTS["fp64_pipe_active"])}
+            "note": "the busiest pipe is FP64 (ncu: %.0f %% of active cycles against %.0f %% "
+                    "for the FMA pipe; most FP64-pipe instructions are conversions, "
+                    "compares and the slab contraction); frac is its arithmetic rate over "
+                    "its FMA peak; issue is %.0f %% active, the kernel latency-bound on "
+                    "dependent double-float chains" % (100 * PIPE_COUNTS["fp64_pipe_active"],
+                                                     100 * PIPE_COUNTS["fma_pipe_active"],
+                                                     100 * PIPE_COUNTS["issue_active"])}
 
 
 def pipe_peak(fp64):
