@@ -114,6 +114,43 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// The Akima-periodic pieces of one component's pulse through (x[i], y[i]),
+// i < n, built once per warp: the chord slopes (lane-parallel) into ch[],
+// then each interval's (k1, k2, k3) into k1[], k2[], k3[] -- the same
+// operations on the same values as akima_periodic_integral, which forms
+// each piece again for every bin that reaches it.  Ends with __syncwarp.
+__device__ __forceinline__ void akima_pieces_warp(const double *x, const double *y, int n,
+                                                  double *ch, double *k1, double *k2,
+                                                  double *k3, int lane) {
+  for (int q = lane; q < n - 1; q += 32) ch[q] = (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
+  __syncwarp();
+  for (int i = lane; i < n - 1; i += 32) {
+    double a1, a2, a3;
+    akima_piece(ch[periodic_chord(i - 2, n)], ch[periodic_chord(i - 1, n)], ch[i],
+                ch[periodic_chord(i + 1, n)], ch[periodic_chord(i + 2, n)], x[i + 1] - x[i], a1,
+                a2, a3);
+    k1[i] = a1;
+    k2[i] = a2;
+    k3[i] = a3;
+  }
+  __syncwarp();
+}
+// akima_periodic_integral over [lo, hi] from the pieces of akima_pieces_warp
+__device__ __forceinline__ double akima_integral_pieces(const double *x, const double *y, int n,
+                                                        const double *k1, const double *k2,
+                                                        const double *k3, double lo, double hi) {
+  if (lo > hi || lo < x[0] || hi > x[n - 1]) return nan("");
+  if (lo == hi) return 0.0;
+  const int ia = locate(x, n, lo), ib = locate(x, n, hi);
+  double acc = 0.0;
+  for (int i = ia; i <= ib; i++) {
+    const double u = (i == ia) ? lo - x[i] : 0.0;
+    const double w = (i == ib) ? hi - x[i] : x[i + 1] - x[i];
+    acc += piece_integral(y[i], k1[i], k2[i], k3[i], u, w);
+  }
+  return acc;
+}
+
 // :140-173 (returns the step; writes the Gaussian width); lane-parallel over
 // the phase bins.  pow(s, 2.0) of the reference is s * s, as its C compiler
 // emits it.
@@ -364,10 +401,42 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   const double n = (double)B;
   const double SCALE = a.exposure / n;
   const double T = a.exposure;
-  // expected star count rate per phase bin (compute_expected_counts.pyx:66-197)
-  for (int j = lane; j < B; j += 32) {
-    double st = 0.0;
+  // expected star count rate per phase bin (compute_expected_counts.pyx:66-197).
+  // Each component's Akima pieces are built once by the warp (in the
+  // quadrature's interval lists, free until the marginal integral) and
+  // integrated over every bin; pulses longer than those lists take the
+  // per-bin form.
+  const bool warp_pieces = N_P > 1 && N_P - 1 <= kQagLimit;
+  for (int j = lane; j < B; j += 32) w.star[j] = 0.0;
+  if (warp_pieces) {
     for (int h = 0; h < a.H; h++) {
+      const double *pulse = a.signals + (((size_t)v * a.H + h) * a.K + ch) * N_P;
+      const double sh = a.shifts[(size_t)v * a.H + h];
+      const bool neg = a.allow_negative[h] == 1;
+      akima_pieces_warp(a.comp_phases, pulse, N_P, w.el, w.al, w.bl, w.rl, lane);
+      for (int j = lane; j < B; j += 32) {
+        double st = w.star[j];
+        double pa = a.phase_edges[j] + sh, pb = a.phase_edges[j + 1] + sh;
+        if (are_equal(pb - pa, 1.0)) { pa = 0.0; pb = 1.0; }
+        else { pa -= floor(pa); pb -= floor(pb); }
+        double val;
+        if (pa < pb) {
+          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, pa, pb);
+          if (val > 0.0 || neg) st += val;
+        } else {
+          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, pa, 1.0);
+          if (val > 0.0 || neg) st += val;
+          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, 0.0, pb);
+          if (val > 0.0 || neg) st += val;
+        }
+        w.star[j] = st;
+      }
+      __syncwarp();
+    }
+  }
+  for (int j = lane; j < B; j += 32) {
+    double st = w.star[j];
+    for (int h = 0; h < a.H && !warp_pieces; h++) {
       const double *pulse = a.signals + (((size_t)v * a.H + h) * a.K + ch) * N_P;
       const double sh = a.shifts[(size_t)v * a.H + h];
       const bool neg = a.allow_negative[h] == 1;
