@@ -393,7 +393,13 @@ struct CellIntegrand {
   double pa, pb;
   XG_HD double operator()(double theta) const {
     if (are_equal(theta, 0.0)) return 0.0;
-    double mu = cos(theta), st = sin(theta);
+    double mu, st;
+#ifdef __CUDA_ARCH__
+    sincos(theta, &st, &mu);  // one argument reduction for both
+#else
+    mu = cos(theta);
+    st = sin(theta);
+#endif
     double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
     double ft = f_theta(mu, radius, s.epsilon, s.zeta, s.shape);
     bool zero;
@@ -454,7 +460,13 @@ template <typename W>
 XG_QD double integrateSpot(double ta, double tb, const Star &s, const Region &g, W &w) {
   auto f = [&](double theta) -> double {
     if (are_equal(theta, 0.0)) return 0.0;
-    double mu = cos(theta), st = sin(theta);
+    double mu, st;
+#ifdef __CUDA_ARCH__
+    sincos(theta, &st, &mu);
+#else
+    mu = cos(theta);
+    st = sin(theta);
+#endif
     double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
     double ft = f_theta(mu, radius, s.epsilon, s.zeta, s.shape);
     bool zero;

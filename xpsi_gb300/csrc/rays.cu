@@ -182,7 +182,22 @@ __global__ void __launch_bounds__(128) rays_kernel(RaysArgs a) {
     L[j] = l;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // rays.pyx:322-371: a row whose values are all finite, in [0, 100 pi] and
+  // rising at the last ray needs no repair (the walk below changes nothing
+  // there); the CTA checks that in parallel and only other rows take the
+  // sequential walk
+  int bad = 0;
+  for (int j = 1 + threadIdx.x; j < N_R; j += blockDim.x) {
+    const double rp = D[j];
+    bad |= (isnan(rp) || rp < 0.0 || rp > 100.0 * kPi) ? 1 : 0;
+  }
+  const int any_bad = __syncthreads_or(bad);
+  if (!any_bad && threadIdx.x == 0) {
+    const int term = N_R >= 2 && !(D[N_R - 1] > D[N_R - 2]);
+    a.maxDeflection[row] = D[N_R - 1];
+    if (a.row_status) a.row_status[row] = term ? kRayFail : kOk;
+  }
+  if (any_bad && threadIdx.x == 0) {
     // rays.pyx:322-371, sequential NaN repair by linear interpolation
     int term = 0;
     int icount = 0, iidx = 0;
