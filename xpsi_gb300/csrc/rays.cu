@@ -4,12 +4,15 @@
 //
 // Work decomposition: one CTA per mesh row ("parallel"), one thread per ray;
 // each thread runs its 2 or 4 QUADPACK-QAG / Gauss-Kronrod-61 integrals to
-// epsrel 1e-12, the reference's quadrature problem: interval bookkeeping and
-// error control in FP64, every panel's integrand evaluations and weighted
-// sums in double-float arithmetic (FP32 pipes, ~1e-14 relative).  The
-// row's NaN repair (:333-369) is a short sequential walk done by one thread
-// after the CTA barrier.  Optionally the lag is calibrated in the same pass
-// (HotRegion.py:880-901: lag -= C(r), lag *= 2 pi f_mode).
+// epsrel 1e-12, the reference's quadrature problem, with the deflection and
+// lag integrals over the same interval taken as a pair (their integrands
+// share the square root, so each node is evaluated once for both):
+// interval bookkeeping and error control in FP64, every panel's integrand
+// evaluations and weighted sums in double-float arithmetic (FP32 pipes,
+// ~1e-14 relative).  The row's NaN repair (:333-369) is a sequential walk
+// done by one thread, for the rows that need one.  Optionally the lag is
+// calibrated in the same pass (HotRegion.py:880-901: lag -= C(r), lag *=
+// 2 pi f_mode).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -28,13 +31,6 @@ struct OutDef {
   }
   __device__ DF operator()(DF x) const { return df_div(x, root(x)); }
 };
-struct OutLag {
-  OutDef d;
-  __device__ DF operator()(DF x) const {
-    const DF f = d.root(x);
-    return df_div(x, df_fma(f, f, f));
-  }
-};
 struct InDef {
   DF q;  // 1 / (rc - 1)
   __device__ __forceinline__ DF value(DF x) const {
@@ -45,24 +41,186 @@ struct InDef {
   }
   __device__ DF operator()(DF x) const { return value(x); }
 };
-struct InLag {
+
+// The deflection and lag integrands of a ray share their square root (Out*)
+// or their inner value (In*): a pair evaluates both at each node once.
+struct OutPair {
+  OutDef d;
+  __device__ void operator()(DF x, DF &fd, DF &fl) const {
+    const DF f = d.root(x);
+    fd = df_div(x, f);
+    fl = df_div(x, df_fma(f, f, f));
+  }
+};
+struct InPair {
   InDef d;
-  __device__ DF operator()(DF x) const {
+  __device__ void operator()(DF x, DF &fd, DF &fl) const {
     const DF X = d.value(x);
-    return df_div(df_mul(X, X), df_add(x, X));
+    fd = X;
+    fl = df_div(df_mul(X, X), df_add(x, X));
   }
 };
 
-// QUADPACK QAG with the 61-point rule at relative 1e-12, limit 100
-// (rays.pyx:140-236), panels in double-float arithmetic
-template <typename F>
-__device__ __forceinline__ int q61(const F &f, double a, double b, double &r) {
-  double e;
-  auto panel = [&](double lo, double hi, double &res, double &err, double &ra, double &rc) {
-    gk_panel_df<XG_K61_HALF>(f, XG_K61_X2, XG_K61_WK2, XG_K61_WG2, lo, hi, res, err, ra, rc);
-  };
-  return qag_panels<100>(panel, a, b, 0.0, 1.0e-12, r, e);
+// gk_panel_df for the two integrands of a pair at once (the same nodes,
+// weights and error estimate per integrand)
+template <typename P>
+__device__ __forceinline__ void gk61_pair_panel(const P &pf, double a, double b, double res[2],
+                                                double err[2], double rabs[2], double rasc[2]) {
+  constexpr int NH = XG_K61_HALF - 1;
+  const double cd = 0.5 * (a + b), hd = 0.5 * (b - a);
+  const DF c = df_split(cd), h = df_split(hd);
+  float fv1[2][NH], fv2[2][NH];
+  DF fc[2];
+  pf(c, fc[0], fc[1]);
+  DF rk[2], rg[2];
+  float ra[2];
+  const DF wkc{XG_K61_WK2[2 * NH], XG_K61_WK2[2 * NH + 1]};
+  const DF wgc{XG_K61_WG2[2 * NH], XG_K61_WG2[2 * NH + 1]};
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    rk[q] = df_mul(wkc, fc[q]);
+    rg[q] = df_mul(wgc, fc[q]);
+    ra[q] = fabsf(rk[q].h);
+  }
+#pragma unroll 1
+  for (int j = 0; j < NH; j++) {
+    const DF dx = df_mul(h, DF{XG_K61_X2[2 * j], XG_K61_X2[2 * j + 1]});
+    DF f1[2], f2[2];
+    pf(df_sub(c, dx), f1[0], f1[1]);
+    pf(df_add(c, dx), f2[0], f2[1]);
+    const DF wk{XG_K61_WK2[2 * j], XG_K61_WK2[2 * j + 1]};
+    const DF wg{XG_K61_WG2[2 * j], XG_K61_WG2[2 * j + 1]};
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      fv1[q][j] = f1[q].h;
+      fv2[q][j] = f2[q].h;
+      const DF s2 = df_add(f1[q], f2[q]);
+      rk[q] = df_fma(wk, s2, rk[q]);
+      if (wg.h != 0.0f) rg[q] = df_fma(wg, s2, rg[q]);
+      ra[q] += wk.h * (fabsf(f1[q].h) + fabsf(f2[q].h));
+    }
+  }
+  const double ah = fabs(hd);
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const float mean = 0.5f * rk[q].h;
+    float rc = wkc.h * fabsf(fc[q].h - mean);
+#pragma unroll 1
+    for (int j = 0; j < NH; j++)
+      rc += XG_K61_WK2[2 * j] * (fabsf(fv1[q][j] - mean) + fabsf(fv2[q][j] - mean));
+    res[q] = df_value(rk[q]) * hd;
+    const double rad = (double)ra[q] * ah, rcd = (double)rc * ah;
+    double e = fabs(df_value(df_sub(rk[q], rg[q])) * hd);
+    if (rcd != 0.0 && e != 0.0) {
+      const double x = 200.0 * e / rcd, sc = x * sqrt(x);
+      e = sc < 1.0 ? rcd * sc : rcd;
+    }
+    if (rad > dmin / (50.0 * eps)) {
+      const double fl = 50.0 * eps * rad;
+      if (fl > e) e = fl;
+    }
+    err[q] = e;
+    rabs[q] = rad;
+    rasc[q] = rcd;
+  }
 }
+
+// QUADPACK QAG at relative 1e-12, limit 100 (rays.pyx:140-236) for the two
+// integrals of a pair over the same interval: the first panel's tests are
+// QUADPACK's for each integral, and while either error is above its
+// tolerance the interval whose larger error relative to its own tolerance
+// is largest is bisected (both integrals refined there).  Each integral is
+// thus at least as accurate as its own QAG run would leave it.  Statuses:
+// 0, 11 (limit), 18 (round-off), 21 (bad integrand), as qag_panels.
+template <typename P>
+__device__ int q61_pair(const P &pf, double a, double b, double &r1, double &r2) {
+  constexpr int LIMIT = 100;
+  const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+  const double epsrel = 1.0e-12;
+  double al[LIMIT], bl[LIMIT], rl[2][LIMIT], el[2][LIMIT];
+  double r0[2], e0[2], ra0[2], rc0[2];
+  gk61_pair_panel(pf, a, b, r0, e0, ra0, rc0);
+  bool done[2];
+  int st0[2];
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const double tol = epsrel * fabs(r0[q]);
+    st0[q] = -1;
+    if (e0[q] <= 50.0 * eps * ra0[q] && e0[q] > tol) st0[q] = 18;
+    else if ((e0[q] <= tol && e0[q] != rc0[q]) || e0[q] == 0.0) st0[q] = 0;
+    done[q] = st0[q] >= 0;
+  }
+  if (done[0] && done[1]) {
+    r1 = r0[0];
+    r2 = r0[1];
+    return st0[0] > st0[1] ? st0[0] : st0[1];
+  }
+  int size = 1;
+  al[0] = a; bl[0] = b;
+  rl[0][0] = r0[0]; el[0][0] = e0[0];
+  rl[1][0] = r0[1]; el[1][0] = e0[1];
+  double area[2] = {r0[0], r0[1]}, errsum[2] = {e0[0], e0[1]};
+  int rnd1 = 0, rnd2 = 0, fail = 0, iter = 1, k = 0;
+  auto tol_of = [&](int q) { return epsrel * fabs(area[q]); };
+  auto prio = [&](int i) {
+    const double t0 = fmax(tol_of(0), dmin), t1 = fmax(tol_of(1), dmin);
+    return fmax(el[0][i] / t0, el[1][i] / t1);
+  };
+  do {
+    const double ai = al[k], bi = bl[k];
+    const double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
+    double R1[2], E1[2], RA1[2], RC1[2], R2[2], E2[2], RA2[2], RC2[2];
+    gk61_pair_panel(pf, a1, b1, R1, E1, RA1, RC1);
+    gk61_pair_panel(pf, a2, b2, R2, E2, RA2, RC2);
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const double ri = rl[q][k], ei = el[q][k];
+      const double r12 = R1[q] + R2[q], e12 = E1[q] + E2[q];
+      errsum[q] += e12 - ei;
+      area[q] += r12 - ri;
+      if (RC1[q] != E1[q] && RC2[q] != E2[q]) {
+        if (fabs(ri - r12) <= 1.0e-5 * fabs(r12) && e12 >= 0.99 * ei) rnd1++;
+        if (iter >= 10 && e12 > ei) rnd2++;
+      }
+    }
+    const bool above = errsum[0] > tol_of(0) || errsum[1] > tol_of(1);
+    if (above) {
+      if (rnd1 >= 12 || rnd2 >= 40) fail = 2;
+      const double edge = (1.0 + 100.0 * eps) * (fabs(a2) + 1000.0 * dmin);
+      if (fabs(a1) <= edge && fabs(b2) <= edge) fail = 3;
+    }
+    const int nw = size++;
+    al[k] = a1; bl[k] = b1;
+    al[nw] = a2; bl[nw] = b2;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      rl[q][k] = R1[q]; el[q][k] = E1[q];
+      rl[q][nw] = R2[q]; el[q][nw] = E2[q];
+    }
+    k = 0;
+    double pk = prio(0);
+    for (int i = 1; i < size; i++) {
+      const double pi = prio(i);
+      if (pi > pk) { pk = pi; k = i; }
+    }
+    iter++;
+    if (!(iter < LIMIT && !fail && above)) break;
+  } while (true);
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = 0; i < size; i++) {
+    s0 += rl[0][i];
+    s1 += rl[1][i];
+  }
+  r1 = s0;
+  r2 = s1;
+  if (!(errsum[0] > tol_of(0) || errsum[1] > tol_of(1))) return 0;
+  if (fail == 2) return 18;
+  if (fail == 3) return 21;
+  if (iter == LIMIT) return 11;
+  return 5;
+}
+
 
 // rays.pyx:90-247; returns deflection in d, lag in seconds in l
 __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d, double &l) {
@@ -76,13 +234,8 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
   l = 0.0;
   if (b <= kBPhotonSphere) {
     const OutDef fd{df_split(1.0 - sas), df_split(sas), df_split(1.0 / (1.0 / u - 1.0))};
-    const OutLag fl{fd};
-    status = q61(fd, 0.0, 1.0, d);
+    status = q61_pair(OutPair{fd}, 0.0, 1.0, d, l);
     if (status == EFAILED) d = nan("");
-    if (status != EFAILED) {
-      status = q61(fl, 0.0, 1.0, l);
-      if (status == EFAILED) d = nan("");
-    }
     if (status != EFAILED) {
       d *= 2.0 * b * u;
       l *= 2.0 * b * b * u * r_s;
@@ -98,13 +251,8 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
     }
     if (isnan(wR)) wR = 0.0;
     const InDef fd{df_split(1.0 / (rc - 1.0))};
-    const InLag fl{fd};
-    status = q61(fd, wR, 1.0, d);
+    status = q61_pair(InPair{fd}, wR, 1.0, d, l);
     if (status == EFAILED) d = nan("");
-    if (status != EFAILED) {
-      status = q61(fl, wR, 1.0, l);
-      if (status == EFAILED) d = nan("");
-    }
     if (status != EFAILED) {
       d *= 2.0 * b / rc;
       l *= 2.0 * b * b * r_s / rc;
@@ -114,20 +262,11 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d,
     double wR = sqrt(1.0 - rc * u);
     if (isnan(wR)) wR = 0.0;
     const InDef fd{df_split(1.0 / (rc - 1.0))};
-    const InLag fl{fd};
     double d1, d0, l1, l0;
-    status = q61(fd, 0.0, 1.0, d1);
+    status = q61_pair(InPair{fd}, 0.0, 1.0, d1, l1);
     if (status == EFAILED) d = nan("");
     if (status != EFAILED) {
-      status = q61(fd, wR, 1.0, d0);
-      if (status == EFAILED) d = nan("");
-    }
-    if (status != EFAILED) {
-      status = q61(fl, 0.0, 1.0, l1);
-      if (status == EFAILED) d = nan("");
-    }
-    if (status != EFAILED) {
-      status = q61(fl, wR, 1.0, l0);
+      status = q61_pair(InPair{fd}, wR, 1.0, d0, l0);
       if (status == EFAILED) d = nan("");
     }
     if (status != EFAILED) {
