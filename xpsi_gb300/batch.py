@@ -470,6 +470,9 @@ class BatchEvaluator:
             raise NotImplementedError("the elsewhere correction is computed by the FP64 "
                                       "integrator only (precision 'plain')")
         self.precision = precision
+        # the integrator's work plan aims at about 4 x target_ctas chunks of
+        # parallels (xgpu_integrate_batch; 0: 8 per SM)
+        self.target_ctas = 0
         self.torch = torch
         self.model = model
         self.dev = torch.device("cuda", device)
@@ -668,7 +671,8 @@ class BatchEvaluator:
             probe["start"].record(strm)
         integ = L.xgpu_integrate_batch_mixed if self.precision == "mixed" \
             else L.xgpu_integrate_batch
-        check(integ(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P, C.byref(d), 0, st))
+        check(integ(n_m, P.meshes, P.n_rows, self.N_R, N_E, self.N_L, N_P, C.byref(d),
+                    int(self.target_ctas), st))
         if probe is not None:
             probe["end"].record(strm)
         if P.else_V:
