@@ -116,24 +116,53 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // The Akima-periodic pieces of one component's pulse through (x[i], y[i]),
 // i < n, built once per warp: the chord slopes (lane-parallel) into ch[],
-// then each interval's (k1, k2, k3) into k1[], k2[], k3[] -- the same
-// operations on the same values as akima_periodic_integral, which forms
-// each piece again for every bin that reaches it.  Ends with __syncwarp.
+// then each interval's (k1, k2, k3) into k1[], k2[], k3[] -- the operations
+// of akima_periodic_integral, which forms each piece again for every bin
+// that reaches it, with products by reciprocals in place of three of its
+// divisions.  Ends with __syncwarp.
 __device__ __forceinline__ void akima_pieces_warp(const double *x, const double *y, int n,
                                                   double *ch, double *k1, double *k2,
                                                   double *k3, int lane) {
   for (int q = lane; q < n - 1; q += 32) ch[q] = (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
   __syncwarp();
   for (int i = lane; i < n - 1; i += 32) {
-    double a1, a2, a3;
-    akima_piece(ch[periodic_chord(i - 2, n)], ch[periodic_chord(i - 1, n)], ch[i],
-                ch[periodic_chord(i + 1, n)], ch[periodic_chord(i + 2, n)], x[i + 1] - x[i], a1,
-                a2, a3);
-    k1[i] = a1;
-    k2[i] = a2;
-    k3[i] = a3;
+    // akima_piece with the interval's 1/h and 1/h^2 formed once (products
+    // instead of the two divisions; an ulp apart)
+    const double mm2 = ch[periodic_chord(i - 2, n)], mm1 = ch[periodic_chord(i - 1, n)];
+    const double m0 = ch[i], mp1 = ch[periodic_chord(i + 1, n)];
+    const double mp2 = ch[periodic_chord(i + 2, n)];
+    const double ih = 1.0 / (x[i + 1] - x[i]);
+    const double wl = fabs(mp1 - m0) + fabs(mm1 - mm2);
+    if (wl == 0.0) {
+      k1[i] = m0;
+      k2[i] = 0.0;
+      k3[i] = 0.0;
+      continue;
+    }
+    const double wr = fabs(mp2 - mp1) + fabs(m0 - mm1);
+    const double f = fabs(mm1 - mm2) / wl;
+    const double tl = (1.0 - f) * mm1 + f * m0;
+    double tr;
+    if (wr == 0.0) {
+      tr = m0;
+    } else {
+      const double g = fabs(m0 - mm1) / wr;
+      tr = (1.0 - g) * m0 + g * mp1;
+    }
+    k1[i] = tl;
+    k2[i] = (3.0 * m0 - 2.0 * tl - tr) * ih;
+    k3[i] = (tl + tr - 2.0 * m0) * (ih * ih);
   }
   __syncwarp();
+}
+// piece_integral with the divisions by 3 taken as products with 1/3 (an ulp
+// apart)
+__device__ __forceinline__ double piece_integral_m(double y0, double k1, double k2, double k3,
+                                                   double u, double w) {
+  constexpr double third = 1.0 / 3.0;
+  const double Fw = w * (y0 + w * (0.5 * k1 + w * (k2 * third + 0.25 * k3 * w)));
+  const double Fu = u * (y0 + u * (0.5 * k1 + u * (k2 * third + 0.25 * k3 * u)));
+  return Fw - Fu;
 }
 // akima_periodic_integral over [lo, hi] from the pieces of akima_pieces_warp
 __device__ __forceinline__ double akima_integral_pieces(const double *x, const double *y, int n,
@@ -146,7 +175,7 @@ __device__ __forceinline__ double akima_integral_pieces(const double *x, const d
   for (int i = ia; i <= ib; i++) {
     const double u = (i == ia) ? lo - x[i] : 0.0;
     const double w = (i == ib) ? hi - x[i] : x[i + 1] - x[i];
-    acc += piece_integral(y[i], k1[i], k2[i], k3[i], u, w);
+    acc += piece_integral_m(y[i], k1[i], k2[i], k3[i], u, w);
   }
   return acc;
 }
