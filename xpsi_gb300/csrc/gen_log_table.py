@@ -1,9 +1,13 @@
-"""Write the table of the double-float natural logarithm in likelihood.cu.
+"""Write the tables of the double-float logarithm and exponential in
+likelihood.cu.
 
 Nodes c_i = 0.75 + i / 128, i = 0..96 (exact in float), cover the reduced
 argument f in [0.75, 1.5); the table holds ln(c_i) as a float pair
 (high part the nearest float, low part the nearest float to the remainder),
-computed here to 50 digits.
+computed here to 50 digits.  For the exponential: 1 / n!, n = 0..13, as
+float pairs (the Taylor coefficients of exp on |r| <= ln 2 / 2), and
+ln 2 in three parts for the argument reduction k ln 2 (the first two with
+12 significant bits, so that k times each is exact for |k| < 2^11).
 
 Usage:  python gen_log_table.py OUT.h
 """
@@ -29,6 +33,23 @@ def main(out):
         hi, lo = pair(mp.log(c))
         lines.append("    {%.9ef, %.9ef}," % (hi, lo))
     lines.append("};")
+    lines.append("")
+    lines.append("#define XG_EXPT_N 14")
+    lines.append("static __constant__ const float XG_EXPT[XG_EXPT_N][2] = {")
+    for n in range(14):
+        hi, lo = pair(1 / mp.factorial(n))
+        lines.append("    {%.9ef, %.9ef}," % (hi, lo))
+    lines.append("};")
+    ln2 = mp.log(2)
+    c1 = mp.mpf(round(float(ln2) * 2**12)) / 2**12
+    c2 = mp.mpf(round(float(ln2 - c1) * 2**24)) / 2**24
+    c3 = ln2 - c1 - c2
+    lines.append("// ln 2 = XG_LN2_1 + XG_LN2_2 + XG_LN2_3")
+    lines.append("#define XG_LN2_1 %.9ef" % float(c1))
+    lines.append("#define XG_LN2_2 %.9ef" % float(c2))
+    h3, l3 = pair(c3)
+    lines.append("#define XG_LN2_3 %.9ef" % h3)
+    lines.append("#define XG_LN2_4 %.9ef" % l3)
     with open(out, "w") as f:
         f.write("\n".join(lines) + "\n")
 

@@ -48,6 +48,30 @@ __device__ __forceinline__ DF df_log_t(DF m, const DF *tab) {
   return df_add(df_fma(DF{(float)e, 0.0f}, ln2, tab[i]), df_mul(df_add(s, s), p));
 }
 
+// exp(x) of a double-float x, returned as a double: x = k ln 2 + r with
+// |r| <= ln 2 / 2 (ln 2 in parts, gen_log_table.py: k times the first two
+// exact for |k| < 2^11), exp(r) by its Taylor series through r^13 / 13! in
+// double-float (truncation below 4e-18 relative), then 2^k in FP64; 0 below
+// the double range, the FP64 exp beyond ln 2^1000.
+__device__ __forceinline__ double df_exp_d(DF x) {
+  if (x.h != x.h) return (double)x.h;
+  if (x.h < -760.0f) return 0.0;
+  if (x.h > 690.0f) return exp((double)x.h + (double)x.l);
+  const float kf = rintf(x.h * 1.44269504088896341f);
+  const int k = (int)kf;
+  DF r = df_add(x, DF{-kf * XG_LN2_1, 0.0f});
+  r = df_add(r, DF{-kf * XG_LN2_2, 0.0f});
+  r = df_fma(DF{-kf, 0.0f}, DF{XG_LN2_3, XG_LN2_4}, r);
+  DF p{XG_EXPT[XG_EXPT_N - 1][0], XG_EXPT[XG_EXPT_N - 1][1]};
+#pragma unroll
+  for (int n = XG_EXPT_N - 2; n >= 0; n--) p = df_fma(p, r, DF{XG_EXPT[n][0], XG_EXPT[n][1]});
+  // 2^k from the bit pattern, split in two factors to stay normal
+  const int k1 = k / 2, k2 = k - k1;
+  const double f1 = __hiloint2double((k1 + 1023) << 20, 0);
+  const double f2 = __hiloint2double((k2 + 1023) << 20, 0);
+  return df_value(p) * f1 * f2;
+}
+
 constexpr int kWarps = 4;
 constexpr int kMaxB = 64;      // phase bins per channel held in shared memory
 constexpr int kQagLimit = 256; // interval list of the marginal quadrature
@@ -70,6 +94,7 @@ struct Marg {
   const DF *q;
   const float *dataf;
   const DF *logt;  // df_log_t's table (shared memory)
+  DF nS;           // n SCALE as a pair (relative form)
 };
 
 // :84-138, as the reference writes it
@@ -88,8 +113,9 @@ __device__ __forceinline__ double marginal_integrand_direct(const Marg &m, doubl
 // A = x(Bi),
 //   x(B) - A = sum_j d_j log(c_j(B) / c_j(Bi)) - n SCALE (B - Bi),
 // whose terms are O(d_j |B - Bi| / c_j) instead of O(d_j log c_j): no
-// cancellation against A.  The ratio 1 + (B - Bi) SCALE / c_j(Bi) and its
-// logarithm are taken in double-float arithmetic (FP32 pipes); a node where
+// cancellation against A.  The ratio 1 + (B - Bi) SCALE / c_j(Bi), its
+// logarithm, the sum and its exponential are taken in double-float
+// arithmetic (FP32 pipes); a node where
 // some ratio is not positive (c_j(B) <= 0) takes the direct form, which
 // holds the reference's tests for that case.
 __device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
@@ -103,7 +129,7 @@ __device__ __forceinline__ double marginal_integrand(const Marg &m, double B) {
     if (!(r.h > 0.0f)) return marginal_integrand_direct(m, B);
     if (m.dataf[j] != 0.0f) acc = df_fma(DF{m.dataf[j], 0.0f}, df_log_t(r, m.logt), acc);
   }
-  return exp(df_value(acc) - (double)m.n * m.SCALE * dBd);
+  return df_exp_d(df_sub(acc, df_mul(m.nS, dB)));
 }
 
 // sum over the warp; the butterfly adds the same pairs in every lane, so all
@@ -601,6 +627,7 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
       if (__all_sync(0xffffffffu, pos)) {
         m.rel = 1;
         m.Bi = Bi;
+        m.nS = df_split((double)m.n * m.SCALE);
       }
       double result;
       if (dsum == 0.0) {
