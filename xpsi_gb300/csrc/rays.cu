@@ -223,13 +223,19 @@ __device__ int q61_pair(const P &pf, double a, double b, double &r1, double &r2)
 
 
 // rays.pyx:90-247; returns deflection in d, lag in seconds in l
-__device__ void ray_integrate(double cos_alpha, double r_s, double u, double &d, double &l) {
+// u_sq1u = u sqrt(1 - u), formed once per row (rays.pyx forms it per ray)
+__device__ void ray_integrate(double cos_alpha, double r_s, double u, double u_sq1u, double &d,
+                              double &l) {
   const int EFAILED = 5;
   int status = 0;
   double sas = 1.0 - cos_alpha * cos_alpha;
   double sa = sqrt(sas);
-  double alpha = acos(cos_alpha);
-  double b = sa / (u * sqrt(1.0 - u));
+  // alpha = acos(cos_alpha) enters only through alpha <= pi/2 and alpha >
+  // pi/2, which are cos_alpha >= 0 and cos_alpha < 0 except where acos
+  // rounds to pi/2 from a cosine a few ulps below zero: there it is formed
+  double alpha = cos_alpha >= 0.0 ? 0.0 : kPi;
+  if (fabs(cos_alpha) < 1.0e-15) alpha = acos(cos_alpha);
+  double b = sa / u_sq1u;
   d = 0.0;
   l = 0.0;
   if (b <= kBPhotonSphere) {
@@ -306,6 +312,7 @@ __global__ void __launch_bounds__(128) rays_kernel(RaysArgs a) {
   }
   __syncthreads();
   const double inc = s_inc;
+  const double u_sq1u = u * sqrt(1.0 - u);
   for (int j = threadIdx.x; j < N_R; j += blockDim.x) {
     double ca = 1.0 - (double)j * inc;
     if (j == 0) {
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(128) rays_kernel(RaysArgs a) {
     }
     CA[j] = ca;
     double d, l;
-    ray_integrate(ca, r_s, u, d, l);
+    ray_integrate(ca, r_s, u, u_sq1u, d, l);
     D[j] = d;  // raw values; repaired below
     L[j] = l;
   }
