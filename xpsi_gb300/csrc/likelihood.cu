@@ -212,9 +212,11 @@ __device__ __forceinline__ double akima_integral_pieces(const double *x, const d
 __device__ __forceinline__ double newton_delta(const Marg &m, double B, int lane, double &std) {
   double x = 0.0, y = 0.0;
   for (int j = lane; j < m.n; j += 32) {
-    const double s = m.star[j] + B;
-    y += m.data[j] / s;
-    x += m.data[j] / (s * s);
+    // d / s and d / s^2 from one reciprocal (an ulp from the two divisions)
+    const double is = 1.0 / (m.star[j] + B);
+    const double t = m.data[j] * is;
+    y += t;
+    x += t * is;
   }
   y = warp_sum(y);
   x = warp_sum(x);

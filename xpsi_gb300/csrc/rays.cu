@@ -223,6 +223,16 @@ __device__ int q61_pair(const P &pf, double a, double b, double &r1, double &r2)
 
 
 // rays.pyx:90-247; returns deflection in d, lag in seconds in l
+// the turning radius r_c / r_s of a ray of impact parameter b / r_s
+// (rays.pyx:156, :194): 2 b cos((atan(sqrt(4 b^2 / 27 - 1)) - pi) / 3) / sqrt 3,
+// the divisions by the constants 27, 3 and sqrt 3 taken as products with
+// their reciprocals (an ulp apart)
+__device__ __forceinline__ double turning_radius(double b) {
+  constexpr double i27 = 1.0 / 27.0, i3 = 1.0 / 3.0;
+  const double isq3 = 0.57735026918962576451;  // 1 / sqrt(3)
+  return 2.0 * b * cos((atan(sqrt(4.0 * b * b * i27 - 1.0)) - kPi) * i3) * isq3;
+}
+
 // u_sq1u = u sqrt(1 - u), formed once per row (rays.pyx forms it per ray)
 __device__ void ray_integrate(double cos_alpha, double r_s, double u, double u_sq1u, double &d,
                               double &l) {
@@ -252,7 +262,7 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double u_s
       rc = 1.0 / u;
       wR = 0.0;
     } else {
-      rc = 2.0 * b * cos((atan(sqrt(4.0 * b * b / 27.0 - 1.0)) - kPi) / 3.0) / sqrt(3.0);
+      rc = turning_radius(b);
       wR = sqrt(1.0 - rc * u);
     }
     if (isnan(wR)) wR = 0.0;
@@ -260,11 +270,12 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double u_s
     status = q61_pair(InPair{fd}, wR, 1.0, d, l);
     if (status == EFAILED) d = nan("");
     if (status != EFAILED) {
-      d *= 2.0 * b / rc;
-      l *= 2.0 * b * b * r_s / rc;
+      const double irc = 1.0 / rc;
+      d *= 2.0 * b * irc;
+      l *= 2.0 * b * b * r_s * irc;
     }
   } else if (alpha > kPi / 2.0) {
-    double rc = 2.0 * b * cos((atan(sqrt(4.0 * b * b / 27.0 - 1.0)) - kPi) / 3.0) / sqrt(3.0);
+    double rc = turning_radius(b);
     double wR = sqrt(1.0 - rc * u);
     if (isnan(wR)) wR = 0.0;
     const InDef fd{df_split(1.0 / (rc - 1.0))};
@@ -276,8 +287,9 @@ __device__ void ray_integrate(double cos_alpha, double r_s, double u, double u_s
       if (status == EFAILED) d = nan("");
     }
     if (status != EFAILED) {
-      d = 2.0 * b * (2.0 * d1 - d0) / rc;
-      l = 2.0 * b * b * r_s * (2.0 * l1 - l0) / rc;
+      const double irc = 1.0 / rc;
+      d = 2.0 * b * (2.0 * d1 - d0) * irc;
+      l = 2.0 * b * b * r_s * (2.0 * l1 - l0) * irc;
       double cor = 1.0 / u - rc + log((1.0 / u - 1.0) / (rc - 1.0));
       l += 2.0 * r_s * cor;
     }
