@@ -119,7 +119,9 @@ __device__ void leaf_geometry(const RowCtx &c, int I, int k, int N_L, int leaf_l
       steffen_eval(ax, ay, c.jalt + 1, cos_psi, nullptr, &deriv);
     } else {
       steffen_eval(mx, ArrY{c.CA}, N_R, psi, nullptr, &deriv);
-      deriv = exp(log(fabs(deriv)) - log(fabs(sin_psi)));
+      // the reference's exp(log|deriv| - log|sin psi|), as the quotient
+      // (the same zero, infinite and NaN cases; an ulp apart)
+      deriv = fabs(deriv) / fabs(sin_psi);
     }
     double plag;
     steffen_eval(mx, ArrY{c.LG}, N_R, psi, &plag, nullptr);
