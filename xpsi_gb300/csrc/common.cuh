@@ -363,6 +363,34 @@ __device__ __forceinline__ DF df_log(DF m) {
   return df_fma(DF{(float)e, 0.0f}, ln2, df_mul(df_add(s, s), p));
 }
 
+// Akima piece (akima_piece above) in double-float arithmetic, with the
+// divisions by h and h^2 taken as products with their reciprocals
+__device__ __forceinline__ DF df_abs(DF a) { return a.h < 0.0f ? df_neg(a) : a; }
+__device__ __forceinline__ void akima_piece_df(DF mm2, DF mm1, DF m0, DF mp1, DF mp2, DF ih,
+                                               DF ih2, DF &k1, DF &k2, DF &k3) {
+  const DF one{1.0f, 0.0f};
+  const DF wl = df_add(df_abs(df_sub(mp1, m0)), df_abs(df_sub(mm1, mm2)));
+  if (wl.h == 0.0f) {
+    k1 = m0;
+    k2 = k3 = DF{0.0f, 0.0f};
+    return;
+  }
+  const DF wr = df_add(df_abs(df_sub(mp2, mp1)), df_abs(df_sub(m0, mm1)));
+  const DF f = df_div(df_abs(df_sub(mm1, mm2)), wl);
+  const DF tl = df_fma(df_sub(one, f), mm1, df_mul(f, m0));
+  DF tr;
+  if (wr.h == 0.0f) {
+    tr = m0;
+  } else {
+    const DF gg = df_div(df_abs(df_sub(m0, mm1)), wr);
+    tr = df_fma(df_sub(one, gg), m0, df_mul(gg, mp1));
+  }
+  k1 = tl;
+  const DF m3 = df_add(df_add(m0, m0), m0);
+  k2 = df_mul(df_sub(df_sub(m3, df_add(tl, tl)), tr), ih);
+  k3 = df_mul(df_sub(df_add(tl, tr), df_add(m0, m0)), ih2);
+}
+
 // ---------------------------------------------------------------------
 // QUADPACK QAG with a Gauss-Kronrod rule, one thread per integral.  The
 // interval list lives in the caller-provided arrays (local memory).

@@ -15,6 +15,8 @@
 // terms are summed per evaluation in channel order by a second kernel, which
 // also applies the reference's early exits (slim cut :677-684, vanished
 // integral :423-429).
+#include <climits>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "log_table.h"
@@ -75,6 +77,7 @@ __device__ __forceinline__ double df_exp_d(DF x) {
 constexpr int kWarps = 4;
 constexpr int kMaxB = 64;      // phase bins per channel held in shared memory
 constexpr int kQagLimit = 256; // interval list of the marginal quadrature
+constexpr int kMaxPiecesPerLane = 8;  // pulse knots per lane in the warp's Akima build
 
 struct WarpSmem {
   double star[kMaxB];
@@ -141,67 +144,77 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // The Akima-periodic pieces of one component's pulse through (x[i], y[i]),
-// i < n, built once per warp: the chord slopes (lane-parallel) into ch[],
-// then each interval's (k1, k2, k3) into k1[], k2[], k3[] -- the operations
-// of akima_periodic_integral, which forms each piece again for every bin
-// that reaches it, with products by reciprocals in place of three of its
-// divisions.  Ends with __syncwarp.
-__device__ __forceinline__ void akima_pieces_warp(const double *x, const double *y, int n,
-                                                  double *ch, double *k1, double *k2,
-                                                  double *k3, int lane) {
-  for (int q = lane; q < n - 1; q += 32) ch[q] = (y[q + 1] - y[q]) / (x[q + 1] - x[q]);
+// i < n, built once per warp in double-float arithmetic: the pulse scaled
+// by 2^-e (e the binary exponent of its largest value, exact) into yd[],
+// the chord slopes into ch[], each interval's (k1, k2, k3) into k1[], k2[],
+// k3[] (akima_piece_df, 1/h and 1/h^2 from FP64), then yd[] over ch[] -- the
+// pieces akima_periodic_integral forms again for every bin that reaches
+// them, here once, on the FP32 pipes (~2^-48 relative).  Returns e; ends
+// with __syncwarp.
+__device__ __forceinline__ int akima_pieces_warp_df(const double *x, const double *y, int n,
+                                                    DF *ch, DF *k1, DF *k2, DF *k3, int lane) {
+  int e = INT_MIN;
+  bool inf = false;
+  for (int q = lane; q < n; q += 32) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(y[q]);
+    const int f = (int)((b >> 52) & 0x7ff);
+    if (f == 0x7ff) inf = true;
+    else if (f != 0) e = max(e, f - 1022);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    inf = __shfl_xor_sync(0xffffffffu, (int)inf, o) != 0 || inf;
+  }
+  if (inf || e == INT_MIN) e = 0;
+  // yd (in k3[] for now) and the chords
+  for (int q = lane; q < n; q += 32) k3[q] = df_split(ldexp(y[q], -e));
+  __syncwarp();
+  for (int q = lane; q < n - 1; q += 32)
+    ch[q] = df_mul(df_sub(k3[q + 1], k3[q]), df_split(1.0 / (x[q + 1] - x[q])));
+  __syncwarp();
+  DF yq[kMaxPiecesPerLane];
+  int c = 0;
+  for (int q = lane; q < n; q += 32) yq[c++] = k3[q];
   __syncwarp();
   for (int i = lane; i < n - 1; i += 32) {
-    // akima_piece with the interval's 1/h and 1/h^2 formed once (products
-    // instead of the two divisions; an ulp apart)
-    const double mm2 = ch[periodic_chord(i - 2, n)], mm1 = ch[periodic_chord(i - 1, n)];
-    const double m0 = ch[i], mp1 = ch[periodic_chord(i + 1, n)];
-    const double mp2 = ch[periodic_chord(i + 2, n)];
-    const double ih = 1.0 / (x[i + 1] - x[i]);
-    const double wl = fabs(mp1 - m0) + fabs(mm1 - mm2);
-    if (wl == 0.0) {
-      k1[i] = m0;
-      k2[i] = 0.0;
-      k3[i] = 0.0;
-      continue;
-    }
-    const double wr = fabs(mp2 - mp1) + fabs(m0 - mm1);
-    const double f = fabs(mm1 - mm2) / wl;
-    const double tl = (1.0 - f) * mm1 + f * m0;
-    double tr;
-    if (wr == 0.0) {
-      tr = m0;
-    } else {
-      const double g = fabs(m0 - mm1) / wr;
-      tr = (1.0 - g) * m0 + g * mp1;
-    }
-    k1[i] = tl;
-    k2[i] = (3.0 * m0 - 2.0 * tl - tr) * ih;
-    k3[i] = (tl + tr - 2.0 * m0) * (ih * ih);
+    const double h = x[i + 1] - x[i];
+    DF a1, a2, a3;
+    akima_piece_df(ch[periodic_chord(i - 2, n)], ch[periodic_chord(i - 1, n)], ch[i],
+                   ch[periodic_chord(i + 1, n)], ch[periodic_chord(i + 2, n)],
+                   df_split(1.0 / h), df_split(1.0 / (h * h)), a1, a2, a3);
+    k1[i] = a1;
+    k2[i] = a2;
+    k3[i] = a3;
   }
   __syncwarp();
+  c = 0;
+  for (int q = lane; q < n; q += 32) ch[q] = yq[c++];
+  __syncwarp();
+  return e;
 }
-// piece_integral with the divisions by 3 taken as products with 1/3 (an ulp
-// apart)
-__device__ __forceinline__ double piece_integral_m(double y0, double k1, double k2, double k3,
-                                                   double u, double w) {
-  constexpr double third = 1.0 / 3.0;
-  const double Fw = w * (y0 + w * (0.5 * k1 + w * (k2 * third + 0.25 * k3 * w)));
-  const double Fu = u * (y0 + u * (0.5 * k1 + u * (k2 * third + 0.25 * k3 * u)));
-  return Fw - Fu;
-}
-// akima_periodic_integral over [lo, hi] from the pieces of akima_pieces_warp
-__device__ __forceinline__ double akima_integral_pieces(const double *x, const double *y, int n,
-                                                        const double *k1, const double *k2,
-                                                        const double *k3, double lo, double hi) {
-  if (lo > hi || lo < x[0] || hi > x[n - 1]) return nan("");
-  if (lo == hi) return 0.0;
+// akima_periodic_integral over [lo, hi] from the pieces of
+// akima_pieces_warp_df (yd in yd[]), in units of 2^e
+__device__ __forceinline__ DF akima_integral_df(const double *x, const DF *yd, int n,
+                                                const DF *k1, const DF *k2, const DF *k3,
+                                                double lo, double hi) {
+  const DF third{0.3333333432674408f, -9.934107758624577e-09f};
   const int ia = locate(x, n, lo), ib = locate(x, n, hi);
-  double acc = 0.0;
+  DF acc{0.0f, 0.0f};
   for (int i = ia; i <= ib; i++) {
     const double u = (i == ia) ? lo - x[i] : 0.0;
     const double w = (i == ib) ? hi - x[i] : x[i + 1] - x[i];
-    acc += piece_integral_m(y[i], k1[i], k2[i], k3[i], u, w);
+    // F(t) = t (y + t (k1 / 2 + t (k2 / 3 + t k3 / 4))) at w and u
+    const DF c1{0.5f * k1[i].h, 0.5f * k1[i].l}, c3{0.25f * k3[i].h, 0.25f * k3[i].l};
+    const DF c2 = df_mul(k2[i], third);
+    DF F[2];
+    const double ts[2] = {w, u};
+#pragma unroll
+    for (int z = 0; z < 2; z++) {
+      const DF t = df_split(ts[z]);
+      F[z] = df_mul(t, df_fma(t, df_fma(t, df_fma(t, c3, c2), c1), yd[i]));
+    }
+    acc = df_add(acc, df_sub(F[0], F[1]));
   }
   return acc;
 }
@@ -463,27 +476,36 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   // quadrature's interval lists, free until the marginal integral) and
   // integrated over every bin; pulses longer than those lists take the
   // per-bin form.
-  const bool warp_pieces = N_P > 1 && N_P - 1 <= kQagLimit;
+  const bool warp_pieces = N_P > 1 && N_P <= kQagLimit && N_P <= 32 * kMaxPiecesPerLane;
   for (int j = lane; j < B; j += 32) w.star[j] = 0.0;
   if (warp_pieces) {
+    DF *yd = reinterpret_cast<DF *>(w.el), *k1 = reinterpret_cast<DF *>(w.al);
+    DF *k2 = reinterpret_cast<DF *>(w.bl), *k3 = reinterpret_cast<DF *>(w.rl);
+    const double *xs = a.comp_phases;
     for (int h = 0; h < a.H; h++) {
       const double *pulse = a.signals + (((size_t)v * a.H + h) * a.K + ch) * N_P;
       const double sh = a.shifts[(size_t)v * a.H + h];
       const bool neg = a.allow_negative[h] == 1;
-      akima_pieces_warp(a.comp_phases, pulse, N_P, w.el, w.al, w.bl, w.rl, lane);
+      const int ex = akima_pieces_warp_df(xs, pulse, N_P, yd, k1, k2, k3, lane);
       for (int j = lane; j < B; j += 32) {
         double st = w.star[j];
         double pa = a.phase_edges[j] + sh, pb = a.phase_edges[j + 1] + sh;
         if (are_equal(pb - pa, 1.0)) { pa = 0.0; pb = 1.0; }
         else { pa -= floor(pa); pb -= floor(pb); }
+        // the reference's argument checks (akima_periodic_integral)
+        auto piece = [&](double lo, double hi) -> double {
+          if (lo > hi || lo < xs[0] || hi > xs[N_P - 1]) return nan("");
+          if (lo == hi) return 0.0;
+          return ldexp(df_value(akima_integral_df(xs, yd, N_P, k1, k2, k3, lo, hi)), ex);
+        };
         double val;
         if (pa < pb) {
-          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, pa, pb);
+          val = piece(pa, pb);
           if (val > 0.0 || neg) st += val;
         } else {
-          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, pa, 1.0);
+          val = piece(pa, 1.0);
           if (val > 0.0 || neg) st += val;
-          val = akima_integral_pieces(a.comp_phases, pulse, N_P, w.al, w.bl, w.rl, 0.0, pb);
+          val = piece(0.0, pb);
           if (val > 0.0 || neg) st += val;
         }
         w.star[j] = st;
