@@ -147,12 +147,14 @@ __device__ __forceinline__ double warp_sum(double v) {
 // i < n, built once per warp in double-float arithmetic: the pulse scaled
 // by 2^-e (e the binary exponent of its largest value, exact) into yd[],
 // the chord slopes into ch[], each interval's (k1, k2, k3) into k1[], k2[],
-// k3[] (akima_piece_df, 1/h and 1/h^2 from FP64), then yd[] over ch[] -- the
+// k3[] (akima_piece_df, with the grid's 1/h and 1/h^2 from ih[], ih2[]), then
+// yd[] over ch[] -- the
 // pieces akima_periodic_integral forms again for every bin that reaches
 // them, here once, on the FP32 pipes (~2^-48 relative).  Returns e; ends
 // with __syncwarp.
 __device__ __forceinline__ int akima_pieces_warp_df(const double *x, const double *y, int n,
-                                                    DF *ch, DF *k1, DF *k2, DF *k3, int lane) {
+                                                    const DF *ih, const DF *ih2, DF *ch, DF *k1,
+                                                    DF *k2, DF *k3, int lane) {
   int e = INT_MIN;
   bool inf = false;
   for (int q = lane; q < n; q += 32) {
@@ -171,18 +173,17 @@ __device__ __forceinline__ int akima_pieces_warp_df(const double *x, const doubl
   for (int q = lane; q < n; q += 32) k3[q] = df_split(ldexp(y[q], -e));
   __syncwarp();
   for (int q = lane; q < n - 1; q += 32)
-    ch[q] = df_mul(df_sub(k3[q + 1], k3[q]), df_split(1.0 / (x[q + 1] - x[q])));
+    ch[q] = df_mul(df_sub(k3[q + 1], k3[q]), ih[q]);
   __syncwarp();
   DF yq[kMaxPiecesPerLane];
   int c = 0;
   for (int q = lane; q < n; q += 32) yq[c++] = k3[q];
   __syncwarp();
   for (int i = lane; i < n - 1; i += 32) {
-    const double h = x[i + 1] - x[i];
     DF a1, a2, a3;
     akima_piece_df(ch[periodic_chord(i - 2, n)], ch[periodic_chord(i - 1, n)], ch[i],
-                   ch[periodic_chord(i + 1, n)], ch[periodic_chord(i + 2, n)],
-                   df_split(1.0 / h), df_split(1.0 / (h * h)), a1, a2, a3);
+                   ch[periodic_chord(i + 1, n)], ch[periodic_chord(i + 2, n)], ih[i], ih2[i],
+                   a1, a2, a3);
     k1[i] = a1;
     k2[i] = a2;
     k3[i] = a3;
@@ -460,7 +461,14 @@ __device__ double warp_marginal(const Marg &m, WarpSmem &w, int lane, double a, 
 __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
   __shared__ WarpSmem ws[kWarps];
   __shared__ DF s_logt[XG_LOGT_N];
+  // the phase grid's 1 / h and 1 / h^2 as pairs, shared by the warps' Akima builds
+  __shared__ DF s_ih[kQagLimit], s_ih2[kQagLimit];
   for (int t = threadIdx.x; t < XG_LOGT_N; t += blockDim.x) s_logt[t] = DF{XG_LOGT[t][0], XG_LOGT[t][1]};
+  for (int t = threadIdx.x; t < a.N_P - 1 && t < kQagLimit; t += blockDim.x) {
+    const double h = a.comp_phases[t + 1] - a.comp_phases[t];
+    s_ih[t] = df_split(1.0 / h);
+    s_ih2[t] = df_split(1.0 / (h * h));
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long gw = (long)blockIdx.x * kWarps + wid;
@@ -486,7 +494,7 @@ __global__ void __launch_bounds__(32 * kWarps) like_channel_kernel(LikeArgs a) {
       const double *pulse = a.signals + (((size_t)v * a.H + h) * a.K + ch) * N_P;
       const double sh = a.shifts[(size_t)v * a.H + h];
       const bool neg = a.allow_negative[h] == 1;
-      const int ex = akima_pieces_warp_df(xs, pulse, N_P, yd, k1, k2, k3, lane);
+      const int ex = akima_pieces_warp_df(xs, pulse, N_P, s_ih, s_ih2, yd, k1, k2, k3, lane);
       for (int j = lane; j < B; j += 32) {
         double st = w.star[j];
         double pa = a.phase_edges[j] + sh, pb = a.phase_edges[j + 1] + sh;
