@@ -398,7 +398,12 @@ int xgpu_fold_batch_tc(int batch, int K, int q, int N, const double *matrix, int
  * without a GPU fault.  No counterpart in the reference. */
 int xgpu_fold_tc_timeout_selftest(int32_t *status_out);
 
-/* out[b][K][N] = matrix[K][0:q] @ in[b][q][N] for b < batch (FP64). */
+/* out[b][K][N] = matrix[K][0:q] @ in[b][q][N] for b < batch, FP64-class:
+ * each row of the matrix and each column of in[b] is scaled by a power of two
+ * and split into a pair of floats, and the products and sums run in
+ * double-float arithmetic (~1e-14 of the sum of the terms' magnitudes; an
+ * infinite input gives NaN where it reaches).  Stream-ordered scratch of
+ * about the size of in plus 8 K q bytes. */
 int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix,
                     int ld, const double *in, double *out, void *stream);
 

@@ -381,8 +381,12 @@ int xgpu_energy_batch(int n_signals, int N_E, int N_P, int n_edges, const double
 
 int xgpu_fold_batch(int batch, int K, int q, int N, const double *matrix, int ld,
                     const double *in, double *out, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   xg::FoldArgs a{batch, K, q, N, matrix, ld, in, out};
-  xg::launch_fold_f64(a, static_cast<cudaStream_t>(stream));
+  Dev scratch;
+  int rc = dalloc(scratch, xg::fold_scratch_bytes(a), st);
+  if (rc) return rc;
+  xg::launch_fold(a, scratch.p, st);
   CK(cudaGetLastError());
   return 0;
 }

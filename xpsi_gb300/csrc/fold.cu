@@ -1,8 +1,30 @@
-// fold.cu -- K5 (FP64 form): the instrument-response fold
+// fold.cu -- K5: the instrument-response fold
 // signals[K][N] = M[K][q] @ integrated[q][N], replacing Instrument.__call__
 // (xpsi/Instrument.py:163-197, a numpy dot).  All likelihood evaluations in a
-// batch share M, so the batch is one GEMM over N = batch * phases columns.
-// FP64 tiles of 64 x 64 in shared memory, 4 x 4 outputs per thread.
+// batch share M, so the batch is one launch over (column tile, row tile,
+// member).
+//
+// Double-float form.  On this GPU the FP64 pipe issues at 1/64 of the FP32
+// rate and an FP64 GEMM runs at that pipe's peak, so the products and sums run
+// in double-float arithmetic on the FP32 pipes:
+//  1. fold_rows_kernel: every row of M times a power of two 2^sM[k] that puts
+//     its largest magnitude in [2^(T-1), 2^T), split into a float pair and
+//     stored transposed (q-major) for the tile loads;
+//  2. fold_cols_kernel: every column of every member's input likewise,
+//     2^sX[b][n];
+//  3. fold_df_kernel: 64 x 64 output tiles, 4 x 4 outputs per thread.  Per
+//     term the product's rounding error comes from an FMA (plus both cross
+//     terms), the rounded products are summed by error-free two-sums into s
+//     and every error into c; (s, c) is renormalised after each 16 terms; the
+//     result, (s + c) in FP64, is scaled back by 2^-(sM[k] + sX[b][n]).
+// T = floor((127 - ceil(log2 q)) / 2): every product stays below 2^(2T) and
+// every partial sum below 2^127, inside the float range.  A product keeps its
+// full accuracy down to 2^(2T-101) (below that its rounding error is a
+// subnormal float), 2^-220 of the largest possible product.  Each output
+// carries ~q 2^-48 of the sum of its terms' magnitudes at worst, ~1e-14 of it
+// in practice -- FP64-class, where a plain FP64 sum carries ~q 2^-53.
+// Infinite inputs give NaN in the outputs they reach (the product error
+// inf - inf), NaNs propagate.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -10,60 +32,176 @@ namespace xg {
 namespace {
 
 constexpr int TM = 64, TN = 64, TK = 16;
+constexpr int kFoldThreads = 256;
+constexpr int kRowsPerCta = kFoldThreads / 32;
+constexpr int kColGroups = kFoldThreads / 32;
 
-__global__ void __launch_bounds__(256) fold_f64_kernel(FoldArgs a) {
-  __shared__ double sA[TK][TM + 1];
-  __shared__ double sB[TK][TN + 1];
+int fold_target_exponent(int q) {
+  int lg = 0;
+  while (lg < 31 && (1ll << lg) < (long long)q) lg++;
+  return (127 - lg) / 2;
+}
+
+struct FoldScratch {
+  float2 *mt;  // [q][K] scaled row splits of M, transposed
+  int *sm;     // [K]
+  float2 *xs;  // [batch][q][N] scaled column splits of the input
+  int *sx;     // [batch][N]
+};
+
+size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+FoldScratch carve(const FoldArgs &a, void *scratch) {
+  char *p = static_cast<char *>(scratch);
+  FoldScratch f;
+  f.mt = reinterpret_cast<float2 *>(p);
+  p += align16(sizeof(float2) * (size_t)a.q * a.K);
+  f.sm = reinterpret_cast<int *>(p);
+  p += align16(sizeof(int) * (size_t)a.K);
+  f.xs = reinterpret_cast<float2 *>(p);
+  p += align16(sizeof(float2) * (size_t)a.batch * a.q * a.N);
+  f.sx = reinterpret_cast<int *>(p);
+  return f;
+}
+
+__device__ __forceinline__ float2 scaled_split(double v, int s) {
+  const DF d = df_split(scale_pow2(v, s));
+  return make_float2(d.h, d.l);
+}
+
+// one warp per row of M
+__global__ void __launch_bounds__(kFoldThreads) fold_rows_kernel(FoldArgs a, FoldScratch f,
+                                                                 int T) {
+  const int lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kRowsPerCta + (threadIdx.x >> 5);
+  if (k >= a.K) return;
+  const double *row = a.M + (size_t)k * a.ldM;
+  MaxExponent mx;
+  for (int c = lane; c < a.q; c += 32) mx.fold(row[c]);
+  mx.merge_warp();
+  const int s = T - mx.exponent();
+  for (int c = lane; c < a.q; c += 32) f.mt[(size_t)c * a.K + k] = scaled_split(row[c], s);
+  if (lane == 0) f.sm[k] = s;
+}
+
+// one CTA per (member, 32 columns): lane = column, warp = a stride-8 share
+// of the q rows
+__global__ void __launch_bounds__(kFoldThreads) fold_cols_kernel(FoldArgs a, FoldScratch f,
+                                                                 int T) {
+  __shared__ int s_e[kColGroups][32];
+  __shared__ int s_inf[kColGroups][32];
+  __shared__ int s_s[32];
+  const int b = blockIdx.y;
+  const int col = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int n = blockIdx.x * 32 + col;
+  const double *In = a.in + (size_t)b * a.q * a.N;
+  MaxExponent mx;
+  if (n < a.N)
+    for (int r = g; r < a.q; r += kColGroups) mx.fold(In[(size_t)r * a.N + n]);
+  s_e[g][col] = mx.e;
+  s_inf[g][col] = mx.inf ? 1 : 0;
+  __syncthreads();
+  if (g == 0) {
+    for (int w = 1; w < kColGroups; w++) {
+      mx.e = max(mx.e, s_e[w][col]);
+      mx.inf = mx.inf || s_inf[w][col] != 0;
+    }
+    s_s[col] = T - mx.exponent();
+  }
+  __syncthreads();
+  if (n >= a.N) return;
+  const int s = s_s[col];
+  float2 *Xs = f.xs + (size_t)b * a.q * a.N;
+  for (int r = g; r < a.q; r += kColGroups)
+    Xs[(size_t)r * a.N + n] = scaled_split(In[(size_t)r * a.N + n], s);
+  if (g == 0) f.sx[(size_t)b * a.N + n] = s;
+}
+
+__global__ void __launch_bounds__(kFoldThreads) fold_df_kernel(FoldArgs a, FoldScratch f) {
+  __shared__ float2 sA[TK][TM];
+  __shared__ float2 sB[TK][TN];
   const int b = blockIdx.z;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
-  const double *In = a.in + (size_t)b * a.q * a.N;
-  double *Out = a.out + (size_t)b * a.K * a.N;
+  const float2 *Xs = f.xs + (size_t)b * a.q * a.N;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
+  float s[4][4], c[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) s[i][j] = c[i][j] = 0.0f;
+  const float2 zero = make_float2(0.0f, 0.0f);
   for (int k0 = 0; k0 < a.q; k0 += TK) {
-    for (int t = threadIdx.x; t < TK * TM; t += 256) {
-      int kk = t % TK, mm = t / TK;
-      int gm = m0 + mm, gk = k0 + kk;
-      sA[kk][mm] = (gm < a.K && gk < a.q) ? a.M[(size_t)gm * a.ldM + gk] : 0.0;
+    for (int t = threadIdx.x; t < TK * TM; t += kFoldThreads) {
+      const int kk = t / TM, mm = t % TM;
+      const int gm = m0 + mm, gk = k0 + kk;
+      sA[kk][mm] = (gm < a.K && gk < a.q) ? f.mt[(size_t)gk * a.K + gm] : zero;
     }
-    for (int t = threadIdx.x; t < TK * TN; t += 256) {
-      int nn = t % TN, kk = t / TN;
-      int gn = n0 + nn, gk = k0 + kk;
-      sB[kk][nn] = (gn < a.N && gk < a.q) ? In[(size_t)gk * a.N + gn] : 0.0;
+    for (int t = threadIdx.x; t < TK * TN; t += kFoldThreads) {
+      const int kk = t / TN, nn = t % TN;
+      const int gn = n0 + nn, gk = k0 + kk;
+      sB[kk][nn] = (gn < a.N && gk < a.q) ? Xs[(size_t)gk * a.N + gn] : zero;
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < TK; kk++) {
-      double av[4], bv[4];
+      DF av[4], bv[4];
 #pragma unroll
-      for (int i = 0; i < 4; i++) av[i] = sA[kk][ty + 16 * i];
+      for (int i = 0; i < 4; i++) {
+        const float2 v = sA[kk][ty + 16 * i];
+        av[i] = DF{v.x, v.y};
+      }
 #pragma unroll
-      for (int j = 0; j < 4; j++) bv[j] = sB[kk][tx + 16 * j];
+      for (int j = 0; j < 4; j++) {
+        const float2 v = sB[kk][tx + 16 * j];
+        bv[j] = DF{v.x, v.y};
+      }
 #pragma unroll
       for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] += av[i] * bv[j];
+        for (int j = 0; j < 4; j++) df_acc_mul(av[i], bv[j], s[i][j], c[i][j]);
     }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const DF r = df_norm(s[i][j], c[i][j]);
+        s[i][j] = r.h;
+        c[i][j] = r.l;
+      }
     __syncthreads();
   }
+  double *Out = a.out + (size_t)b * a.K * a.N;
+  const int *sx = f.sx + (size_t)b * a.N;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
-    int gm = m0 + ty + 16 * i;
+    const int gm = m0 + ty + 16 * i;
     if (gm >= a.K) continue;
+    const int sm = f.sm[gm];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      int gn = n0 + tx + 16 * j;
-      if (gn < a.N) Out[(size_t)gm * a.N + gn] = acc[i][j];
+      const int gn = n0 + tx + 16 * j;
+      if (gn < a.N)
+        Out[(size_t)gm * a.N + gn] = scale_pow2((double)s[i][j] + (double)c[i][j], -(sm + sx[gn]));
     }
   }
 }
 
 }  // namespace
 
-void launch_fold_f64(const FoldArgs &a, cudaStream_t st) {
-  if (a.batch <= 0) return;
+size_t fold_scratch_bytes(const FoldArgs &a) {
+  return align16(sizeof(float2) * (size_t)a.q * a.K) + align16(sizeof(int) * (size_t)a.K) +
+         align16(sizeof(float2) * (size_t)a.batch * a.q * a.N) +
+         align16(sizeof(int) * (size_t)a.batch * a.N);
+}
+
+void launch_fold(const FoldArgs &a, void *scratch, cudaStream_t st) {
+  if (a.batch <= 0 || a.K <= 0 || a.N <= 0) return;
+  const FoldScratch f = carve(a, scratch);
+  const int T = fold_target_exponent(a.q);
+  fold_rows_kernel<<<(a.K + kRowsPerCta - 1) / kRowsPerCta, kFoldThreads, 0, st>>>(a, f, T);
+  fold_cols_kernel<<<dim3((a.N + 31) / 32, a.batch), kFoldThreads, 0, st>>>(a, f, T);
   dim3 grid((a.N + TN - 1) / TN, (a.K + TM - 1) / TM, a.batch);
-  fold_f64_kernel<<<grid, 256, 0, st>>>(a);
+  fold_df_kernel<<<grid, kFoldThreads, 0, st>>>(a, f);
 }
 
 }  // namespace xg

@@ -427,72 +427,6 @@ __device__ __forceinline__ double eval_num4d_e(const Atmos4D &A, const AtmSmem &
   return I * p3;
 }
 
-// acc + a b in double-float, the sum held unnormalised in (s, c): s gathers
-// the rounded products through error-free sums, c the product and sum
-// errors; the caller renormalises once (two_sum of s and c)
-__device__ __forceinline__ void df_acc_mul(DF a, DF b, float &s, float &c) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  float q;
-  two_sum(s, p, s, q);
-  c = __fadd_rn(c, __fadd_rn(q, e));
-}
-__device__ __forceinline__ DF df_norm(float s, float c) {
-  DF r;
-  two_sum(s, c, r.h, r.l);
-  return r;
-}
-
-// binary exponent x of |v| = f 2^x, f in [0.5, 1), from the bit pattern
-// (integer work); kZeroExp for zero and subnormal values
-constexpr int kZeroExp = -2100;
-__device__ __forceinline__ int binary_exponent(double v) {
-  const int e = (__double2hiint(v) >> 20) & 0x7ff;
-  return e == 0 ? kZeroExp : e - 1022;
-}
-// 2^x as a double from the bit pattern (0 below the normal range, the
-// largest power of two above it)
-__device__ __forceinline__ double pow2_double(int x) {
-  const int b = x + 1023;
-  if (b <= 0) return 0.0;
-  return __hiloint2double(min(b, 2046) << 20, 0);
-}
-// v 2^e, as ldexp(v, e) (one rounding at most), by a product with the
-// power of two where that is a normal double
-__device__ __forceinline__ double scale_pow2(double v, int e) {
-  return (e >= -1022 && e <= 1023) ? v * pow2_double(e) : ldexp(v, e);
-}
-// the largest frexp exponent of |v| over a lane's values, from the bit
-// patterns (integer work): fold() each value, exponent() at the end gives
-// what frexp(max |v|) gives, 0 when the largest is 0, infinite or NaN
-// throughout (NaNs are skipped as fmax skips them; an infinity gives 0)
-struct MaxExponent {
-  int e = INT_MIN;
-  bool inf = false;
-  __device__ __forceinline__ void fold(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const int f = (int)((b >> 52) & 0x7ff);
-    const unsigned long long m = b & 0xfffffffffffffull;
-    if (f == 0x7ff) {
-      inf = inf || m == 0ull;
-    } else if (f != 0) {
-      e = max(e, f - 1022);
-    } else if (m != 0ull) {
-      e = max(e, -1010 - __clzll((long long)m));
-    }
-  }
-  __device__ __forceinline__ void merge_warp() {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-      inf = __shfl_xor_sync(0xffffffffu, (int)inf, o) != 0 || inf;
-    }
-  }
-  __device__ __forceinline__ int exponent() const { return (inf || e == INT_MIN) ? 0 : e; }
-};
-
 // a double-float pair times 2^d, d <= 0 (exact down to the float range)
 __device__ __forceinline__ DF df_scale(DF a, int d) {
   if (d < -125) return DF{0.0f, 0.0f};

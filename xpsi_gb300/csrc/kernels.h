@@ -147,7 +147,10 @@ struct FoldArgs {
   // operations in flight timed out as well; may be null
   int32_t *status = nullptr;
 };
-void launch_fold_f64(const FoldArgs &a, cudaStream_t st);
+// double-float form (FP64-class): scratch is fold_scratch_bytes(a) bytes of
+// device memory, 16-byte aligned
+size_t fold_scratch_bytes(const FoldArgs &a);
+void launch_fold(const FoldArgs &a, void *scratch, cudaStream_t st);
 // tensor-core form (3xTF32 split products, FP32 accumulation in TMEM);
 // scratch: fold_tc_scratch_bytes(a) bytes of device memory, 16-byte aligned.
 // Returns 0, or < 0 when the tile maps cannot be encoded.

@@ -359,19 +359,25 @@ __global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, in
 }
 
 // one group of 16 lanes per queued cell: the area quadrature of a cell cut
-// by a boundary
+// by a boundary.  The groups take the next queued cell from a shared counter
+// (n_queue[1]) when they finish one, as the cells' costs differ by 5x or
+// more (10-50 bisection steps); each cell's result is independent of which
+// group integrates it.
 constexpr int kBoundaryWarps = 4;
 __global__ void __launch_bounds__(32 * kBoundaryWarps) mesh_boundary_kernel(
     const MeshJob *jobs, int n_mesh, xgpu_mesh_batch_out o, const double *row_tmp,
-    const int64_t *queue, const unsigned *n_queue) {
+    const int64_t *queue, unsigned *n_queue) {
   __shared__ WarpList lists[2 * kBoundaryWarps];
   const int lane = threadIdx.x & 31, half = lane / kGrp;
   const int grp = (threadIdx.x >> 5) * 2 + half;
   const Grp gp{lane - half * kGrp, 0xFFFFu << (kGrp * half)};
   WarpList &L = lists[grp];
-  const unsigned n = *n_queue;
-  const unsigned stride = gridDim.x * kBoundaryWarps * 2;
-  for (unsigned q = blockIdx.x * kBoundaryWarps * 2 + grp; q < n; q += stride) {
+  const unsigned n = n_queue[0];
+  for (;;) {
+    unsigned q = 0;
+    if (gp.l == 0) q = atomicAdd(&n_queue[1], 1u);
+    q = __shfl_sync(gp.mask, q, half * kGrp);
+    if (q >= n) break;
     const int64_t c = queue[q];
     const int m = mesh_of_cell(jobs, n_mesh, c);
     const MeshJob &J = jobs[m];
@@ -437,14 +443,14 @@ extern "C" int xgpu_mesh_batch(int n, const xgpu_mesh_member *members, int64_t n
       cudaMallocAsync(&row_tmp, sizeof(double) * 4 * (size_t)n_rows, st) != cudaSuccess ||
       cudaMallocAsync(&mesh_tmp, sizeof(double) * 2 * (size_t)n, st) != cudaSuccess ||
       cudaMallocAsync(&queue, sizeof(int64_t) * (size_t)n_cells, st) != cudaSuccess ||
-      cudaMallocAsync(&n_queue, sizeof(unsigned), st) != cudaSuccess) {
+      cudaMallocAsync(&n_queue, 2 * sizeof(unsigned), st) != cudaSuccess) {
     cudaFreeAsync(d_jobs, st);
     return -5;
   }
   // (a copy from pageable memory has been staged when cudaMemcpyAsync
   // returns, so the host jobs may go out of scope)
   cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(MeshJob) * (size_t)n, cudaMemcpyHostToDevice, st);
-  cudaMemsetAsync(n_queue, 0, sizeof(unsigned), st);
+  cudaMemsetAsync(n_queue, 0, 2 * sizeof(unsigned), st);  // queue length, next cell
   mesh_table_kernel<<<dim3((kAreaTab + 127) / 128, (unsigned)n), 128, 0, st>>>(d_jobs, tab);
   const size_t smem = sizeof(double) * (kAreaTab + S_max);
   mesh_rows_kernel<<<(unsigned)n, 128, smem, st>>>(d_jobs, tab, *out, row_tmp, mesh_tmp);
