@@ -184,6 +184,16 @@ XG_HD inline double f_theta(double mu, double radius, double epsilon, double zet
   if (shape == 0) return d / (radius * sqrt(1.0 - 2.0 * zeta / radius));
   return 0.0;
 }
+// f_theta^2 for the surface element sqrt(1 + f^2) of the area integrands:
+// (2 eps c mu sin theta)^2 / (r (r - 2 zeta)), the same quantity without
+// f_theta's two square roots and two divisions; sin_theta is sqrt(1 - mu^2)
+// for theta in [0, pi], and accurate near the poles where 1 - mu^2 cancels
+XG_HD inline double f_theta_sq(double mu, double sin_theta, double radius, double epsilon,
+                               double zeta, int shape) {
+  if (shape != 0) return 0.0;
+  const double d = 2.0 * epsilon * (-0.788 + 1.030 * zeta) * mu * sin_theta;
+  return d * d / (radius * (radius - 2.0 * zeta));
+}
 // effective_gravity_universal.pyx:10-71
 XG_HD inline double effectiveGravity(double mu, double R_eq, double x, double epsilon, int shape) {
   double g_0 = x * C_LIGHT * C_LIGHT / (R_eq * sqrt(1.0 - 2.0 * x));
@@ -400,12 +410,14 @@ struct CellIntegrand {
     mu = cos(theta);
     st = sin(theta);
 #endif
-    double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
-    double ft = f_theta(mu, radius, s.epsilon, s.zeta, s.shape);
     bool zero;
-    double dphi = ring_extent(theta, mu, st, g, true, pa, pb, zero);
-    if (zero) return 0.0;
-    return dphi * radius * radius * sqrt(1.0 + ft * ft) * st;
+    const double dphi = ring_extent(theta, mu, st, g, true, pa, pb, zero);
+    // outside the cell's share of the ring the integrand is 0 (a zero
+    // extent times the finite surface factor): the factor is not formed
+    if (zero || dphi == 0.0) return 0.0;
+    const double radius = radiusNormalised(mu, s.epsilon, s.zeta, s.shape);
+    const double ft2 = f_theta_sq(mu, st, radius, s.epsilon, s.zeta, s.shape);
+    return dphi * radius * radius * sqrt(1.0 + ft2) * st;
   }
 };
 
