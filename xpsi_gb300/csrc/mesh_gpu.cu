@@ -245,9 +245,16 @@ __device__ double grp_qag21(const F &f, double a, double b, double epsabs, doubl
       }
     }
     __syncwarp(g.mask);
+    // the interval of largest error, compared by bit pattern: the errors are
+    // non-negative, so their patterns order as 64-bit integers like the
+    // values (the integer pipe instead of FP64 compares; the first of equal
+    // errors wins, as before)
     k = 0;
-    for (int i = 1; i < size; i++)
-      if (L.el[i] > L.el[k]) k = i;
+    long long ek = __double_as_longlong(L.el[0]);
+    for (int i = 1; i < size; i++) {
+      const long long e = __double_as_longlong(L.el[i]);
+      if (e > ek) { ek = e; k = i; }
+    }
     iter++;
   } while (iter < kWarpList && !fail && errsum > tol);
   double sum = 0.0;

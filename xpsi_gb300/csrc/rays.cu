@@ -163,10 +163,9 @@ __device__ int q61_pair(const P &pf, double a, double b, double &r1, double &r2)
   double area[2] = {r0[0], r0[1]}, errsum[2] = {e0[0], e0[1]};
   int rnd1 = 0, rnd2 = 0, fail = 0, iter = 1, k = 0;
   auto tol_of = [&](int q) { return epsrel * fabs(area[q]); };
-  auto prio = [&](int i) {
-    const double t0 = fmax(tol_of(0), dmin), t1 = fmax(tol_of(1), dmin);
-    return fmax(el[0][i] / t0, el[1][i] / t1);
-  };
+  // an interval's priority: the larger of its two errors over their
+  // tolerances (the reciprocals taken once per bisection step)
+  auto prio = [&](int i, double i0, double i1) { return fmax(el[0][i] * i0, el[1][i] * i1); };
   do {
     const double ai = al[k], bi = bl[k];
     const double a1 = ai, b1 = 0.5 * (ai + bi), a2 = b1, b2 = bi;
@@ -199,9 +198,10 @@ __device__ int q61_pair(const P &pf, double a, double b, double &r1, double &r2)
       rl[q][nw] = R2[q]; el[q][nw] = E2[q];
     }
     k = 0;
-    double pk = prio(0);
+    const double i0 = 1.0 / fmax(tol_of(0), dmin), i1 = 1.0 / fmax(tol_of(1), dmin);
+    double pk = prio(0, i0, i1);
     for (int i = 1; i < size; i++) {
-      const double pi = prio(i);
+      const double pi = prio(i, i0, i1);
       if (pi > pk) { pk = pi; k = i; }
     }
     iter++;
