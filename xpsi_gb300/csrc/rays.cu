@@ -111,10 +111,16 @@ __device__ __forceinline__ void gk61_pair_panel(const P &pf, double a, double b,
       rc += XG_K61_WK2[2 * j] * (fabsf(fv1[q][j] - mean) + fabsf(fv2[q][j] - mean));
     res[q] = df_value(rk[q]) * hd;
     const double rad = (double)ra[q] * ah, rcd = (double)rc * ah;
-    double e = fabs(df_value(df_sub(rk[q], rg[q])) * hd);
-    if (rcd != 0.0 && e != 0.0) {
-      const double x = 200.0 * e / rcd, sc = x * sqrt(x);
-      e = sc < 1.0 ? rcd * sc : rcd;
+    // QUADPACK's err = rasc min(1, (200 |K - G| / rasc)^1.5): the ratio is
+    // free of the half-width (it cancels), so it is formed in float from the
+    // double-float and float sums; only the product with rasc is FP64
+    const DF dk = df_sub(rk[q], rg[q]);
+    double e;
+    if (rc != 0.0f && dk.h != 0.0f) {
+      const float x = 200.0f * fabsf(dk.h) / rc, sc = x * sqrtf(x);
+      e = sc < 1.0f ? rcd * (double)sc : rcd;
+    } else {
+      e = fabs(df_value(dk) * hd);
     }
     if (rad > dmin / (50.0 * eps)) {
       const double fl = 50.0 * eps * rad;
