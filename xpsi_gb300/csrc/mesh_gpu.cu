@@ -151,7 +151,7 @@ __device__ __forceinline__ WPanel k21_finish(double rk, double rg, double ra, do
   rc *= ah;
   double e = fabs((rk - rg) * h);
   if (rc != 0.0 && e != 0.0) {
-    const double sc = pow(200.0 * e / rc, 1.5);
+    const double x = 200.0 * e / rc, sc = x * sqrt(x);  // x^1.5 without pow
     e = sc < 1.0 ? rc * sc : rc;
   }
   const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(128) mesh_cells_kernel(const MeshJob *jobs, in
 // more (10-50 bisection steps); each cell's result is independent of which
 // group integrates it.
 constexpr int kBoundaryWarps = 4;
-__global__ void __launch_bounds__(32 * kBoundaryWarps) mesh_boundary_kernel(
+__global__ void __launch_bounds__(32 * kBoundaryWarps, 4) mesh_boundary_kernel(
     const MeshJob *jobs, int n_mesh, xgpu_mesh_batch_out o, const double *row_tmp,
     const int64_t *queue, unsigned *n_queue) {
   __shared__ WarpList lists[2 * kBoundaryWarps];

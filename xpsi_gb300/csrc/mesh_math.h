@@ -64,7 +64,7 @@ XG_QD void gk21(const F &f, double a, double b, double &res, double &err, double
   rc *= ah;
   double e = fabs((rk - rg) * h);
   if (rc != 0.0 && e != 0.0) {
-    double sc = pow(200.0 * e / rc, 1.5);
+    const double x = 200.0 * e / rc, sc = x * sqrt(x);  // x^1.5 without pow
     e = sc < 1.0 ? rc * sc : rc;
   }
   const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
