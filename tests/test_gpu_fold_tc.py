@@ -1,5 +1,5 @@
 """The tensor-core fold (tcgen05, 3xTF32 split products, FP32 accumulation)
-against the FP64 fold on the same inputs: FP32-class agreement, 1e-6 of
+against the FP64-class (double-float) fold on the same inputs: FP32-class agreement, 1e-6 of
 each output row's largest value, on shapes that exercise the padding of
 every tile dimension (channels, columns across signals, input intervals)."""
 import numpy as np
