@@ -456,8 +456,10 @@ __device__ __forceinline__ MuStencilDF mu_stencil_df(const Atmos4D &A, const Atm
   for (int k = 0; k < 4; k++) d.w2[k] = df_split(m.w2[k]);
   return d;
 }
-__device__ __forceinline__ DF eval_num4d_df(const Atmos4D &A, const AtmSmem &as, const DF *slab,
-                                            const MuStencilDF &m, double v3, double &scale) {
+// the contracted table's value at (mu stencil m, v3) as a double-float times
+// 2^xr (xr the largest column exponent of the energy stencil)
+__device__ __forceinline__ DF eval_num4d_dfx(const Atmos4D &A, const AtmSmem &as, const DF *slab,
+                                             const MuStencilDF &m, double v3, int &xr) {
   const int nE = A.nE;
   float vf = (float)v3;
   if (vf <= as.fgE[0] && v3 < as.gE[0]) {
@@ -487,8 +489,7 @@ __device__ __forceinline__ DF eval_num4d_df(const Atmos4D &A, const AtmSmem &as,
   const DF *S = as.dsE + 4 * b3;
   // the nodes' column scales relative to the largest of the four (<= 1)
   const int x0 = as.xe[b3], x1 = as.xe[b3 + 1], x2 = as.xe[b3 + 2], x3 = as.xe[b3 + 3];
-  const int xr = max(max(x0, x1), max(x2, x3));
-  scale = pow2_double(xr);
+  xr = max(max(x0, x1), max(x2, x3));
   const DF w3[4] = {df_scale(df_mul(df_mul(u1, u23), S[0]), x0 - xr),
                     df_scale(df_mul(df_mul(u0, u23), S[1]), x1 - xr),
                     df_scale(df_mul(df_mul(u01, u3), S[2]), x2 - xr),
@@ -503,6 +504,26 @@ __device__ __forceinline__ DF eval_num4d_df(const Atmos4D &A, const AtmSmem &as,
     df_acc_mul(m.w2[k], df_norm(th, tl), sh, sl);
   }
   return df_norm(sh, sl);
+}
+// the same with the factor 2^xr returned as a double
+__device__ __forceinline__ DF eval_num4d_df(const Atmos4D &A, const AtmSmem &as, const DF *slab,
+                                            const MuStencilDF &m, double v3, double &scale) {
+  int xr;
+  const DF v = eval_num4d_dfx(A, as, slab, m, v3, xr);
+  scale = pow2_double(xr);
+  return v;
+}
+// binary exponent x of |f| = m 2^x, m in [0.5, 1), of a nonzero finite float
+// from its bit pattern
+__device__ __forceinline__ int float_exponent(float f) {
+  const int b = (__float_as_int(f) >> 23) & 0xff;
+  return b != 0 ? b - 126 : -149 + (32 - __clz(__float_as_int(f) & 0x7fffff));
+}
+// a double-float times 2^d (0 where 2^d leaves the float range)
+__device__ __forceinline__ DF df_times_pow2(DF a, int d) {
+  if (d < -126 || d > 127) return DF{0.0f, 0.0f};
+  const float f = __int_as_float((127 + d) << 23);
+  return DF{a.h * f, a.l * f};
 }
 
 // FP32 forms for the mixed-precision integrator
@@ -1327,6 +1348,10 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
     // the elsewhere correction's blackbody temperature at the parallel's
     // first radiating cell (:469-476)
     const bool corr = !kMixed && a.correction != nullptr;
+    // the plain Num4D columns without beaming or correction keep their
+    // intensities as double-float mantissas with exponents up to the row
+    // scaling (uniform over the CTA: a chunk is one mesh's rows)
+    const bool dfy = !kMixed && num4d && !tab2 && M.beam_opt == 0 && !corr;
     const double kT_c =
         corr ? (kKB / kKeV) *
                    pow(10.0, a.correction[(M.cell_off + (int64_t)i * M.S1 + c.J) * a.n_correction])
@@ -1438,6 +1463,8 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           MuStencilF msf{};
           MuStencilDF msd{};
           double col_factor = 0.0;  // norm 10^(3 log T) GEOM of the column
+          DF cf_m{0.0f, 0.0f};      // col_factor = cf_m 2^cf_x (dfy form)
+          int cf_x = 0;
           for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
             const int pl = t / N_L, col = t - pl * N_L;
             const int p = e0 + pl;
@@ -1467,7 +1494,6 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                 y = (WT)((float)norm * I_E * as.fgeom[s]);
               } else {
                 double I_E;
-                bool done = false;
                 if (num4d && !tab2) {
                   // the contracted 4-D table in double-float (eval_num4d_df);
                   // with beaming option 3 every call is followed by calls up
@@ -1476,21 +1502,30 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                   if (s != mu_col) {
                     msd = mu_stencil_df(a.atmos, as, g.ABB[s], false);
                     col_factor = norm * p3 * g.GEOM[s];
+                    if (dfy) {
+                      MaxExponent mx;
+                      mx.fold(col_factor);
+                      cf_x = mx.exponent();
+                      cf_m = df_split(scale_pow2(col_factor, -cf_x));
+                    }
                     mu_col = s;
                   }
-                  double scale;
+                  int xr;
                   DF I = (p == 0 && g.clamp0[s] && M.beam_opt != 3)
-                             ? eval_num4d_df(a.atmos, as, slabd,
-                                             mu_stencil_df(a.atmos, as, g.ABB[s], true), v3,
-                                             scale)
-                             : eval_num4d_df(a.atmos, as, slabd, msd, v3, scale);
+                             ? eval_num4d_dfx(a.atmos, as, slabd,
+                                              mu_stencil_df(a.atmos, as, g.ABB[s], true), v3,
+                                              xr)
+                             : eval_num4d_dfx(a.atmos, as, slabd, msd, v3, xr);
                   if (I.h < 0.0f) I = DF{0.0f, 0.0f};
-                  if (M.beam_opt == 0 && !corr) {
-                    y = df_value(I) * scale * col_factor;
-                    done = true;
-                  } else {
-                    I_E = df_value(I) * scale * p3;
+                  if (dfy) {
+                    // y = I 2^xr col_factor kept as a double-float mantissa
+                    // and an exponent (no round trip through FP64)
+                    Piece &o = co4[pl * N_L + col];
+                    *reinterpret_cast<DF *>(&o.y) = df_mul(I, cf_m);
+                    *reinterpret_cast<int *>(&o.k1) = xr + cf_x;
+                    continue;
                   }
+                  I_E = df_value(I) * pow2_double(xr) * p3;
                 } else if (num4d) {
                   // atm 6: E' = E / Z in electron rest energies (:457-458)
                   const double v3 = erest ? (g.lgE[pl] / g.lzs[s]) * 0.001956951
@@ -1512,7 +1547,7 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
                   // the burst blackbody's limb darkening (hot_BB_burst.pyx)
                   if (M.atm == 3) I_E = I_E * (0.421 + 0.868 * g.ABB[s]);
                 }
-                if (!done) {
+                {
                   const double I_c =
                       corr ? eval_bb(a.energies[p] / g.Z[s], kT_c) * (kErg * kPlanck) : 0.0;
                   // with a beaming modification the raw intensity is kept
@@ -1596,17 +1631,42 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(IntegrateArgs a)
           // largest profile value lies in [0.5, 1): double-float values then
           // keep the row's full relative precision whatever its magnitude
           const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-          for (int pl = warp; pl < ne; pl += kThreads / 32) {
-            MaxExponent mx;
-            for (int col = lane; col < N_L; col += 32) mx.fold((double)co4[pl * N_L + col].y);
-            mx.merge_warp();
-            if (lane == 0) g.sc_exp[pl] = mx.exponent();
-          }
-          __syncthreads();
           PieceDF *pc = reinterpret_cast<PieceDF *>(co4);
-          for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
-            const double v = (double)co4[t].y;
-            pc[t].y = df_split(scale_pow2(v, -g.sc_exp[t / N_L]));
+          if (dfy) {
+            // values m 2^x (mantissa in the y slot, exponent in k1's): the
+            // row's largest exponent from the bits, then each value times
+            // 2^(x - that) in float arithmetic (exact)
+            for (int pl = warp; pl < ne; pl += kThreads / 32) {
+              MaxExponent mx;
+              for (int col = lane; col < N_L; col += 32) {
+                const Piece &o = co4[pl * N_L + col];
+                const float h = reinterpret_cast<const DF *>(&o.y)->h;
+                if (h != 0.0f && h == h) {
+                  if (isinf(h)) mx.inf = true;
+                  else mx.e = max(mx.e, *reinterpret_cast<const int *>(&o.k1) + float_exponent(h));
+                }
+              }
+              mx.merge_warp();
+              if (lane == 0) g.sc_exp[pl] = mx.exponent();
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+              const DF m = *reinterpret_cast<const DF *>(&co4[t].y);
+              const int x = *reinterpret_cast<const int *>(&co4[t].k1);
+              pc[t].y = m.h == 0.0f ? DF{0.0f, 0.0f} : df_times_pow2(m, x - g.sc_exp[t / N_L]);
+            }
+          } else {
+            for (int pl = warp; pl < ne; pl += kThreads / 32) {
+              MaxExponent mx;
+              for (int col = lane; col < N_L; col += 32) mx.fold((double)co4[pl * N_L + col].y);
+              mx.merge_warp();
+              if (lane == 0) g.sc_exp[pl] = mx.exponent();
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < ne * N_L; t += blockDim.x) {
+              const double v = (double)co4[t].y;
+              pc[t].y = df_split(scale_pow2(v, -g.sc_exp[t / N_L]));
+            }
           }
           __syncthreads();
           for (int t = threadIdx.x; t < ne * strips; t += blockDim.x) {
