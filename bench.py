@@ -152,13 +152,13 @@ def shard_vectors(V, rank, world, seed=3):
 PIPE_COUNTS = {
     "vectors": 64,
     "cost_model_flop": 482067568128.0,
-    "fp64_flop": 2 * 3659919382 + 2194393971 + 2365114391,
-    "fp32_flop": 2 * 163498592549 + 57528786183 + 634940702172,
-    "dram_bytes": 987693312 + 2736122112,
-    "fp64_pipe_active": 0.571,
-    "fma_pipe_active": 0.380,
-    "issue_active": 0.533,
-    "duration_ms": 69.2,
+    "fp64_flop": 2 * 3645276754 + 1588912815 + 1953852419,
+    "fp32_flop": 2 * 164095141825 + 58059214755 + 635536874448,
+    "dram_bytes": 969295104 + 2730820608,
+    "fp64_pipe_active": 0.530,
+    "fma_pipe_active": 0.389,
+    "issue_active": 0.547,
+    "duration_ms": 68.3,
     "capture": "ncu --metrics (instruction classes, pipe activity, dram bytes) -k "
                "regex:integrate_kernel -s 1 -c 1, python bench.py --vectors 64 --steps 1 "
                "--warmup 3 --legs none",
