@@ -5,7 +5,7 @@
 // (the packing of xpsi/HotRegion.py:774-1017 / Likelihood.py:297-432 that
 // the host path does in numpy).
 //
-// Three launches over all meshes of the batch:
+// Four launches over all meshes of the batch:
 //   1. the 1000-point table of area(colat..lims[1]) per mesh, one thread per
 //      entry (1000 independent adaptive quadratures);
 //   2. per mesh: the cell area and the S - 1 parallels (one thread, the
@@ -14,10 +14,11 @@
 //   3. one thread per cell: the corner / centre membership tests; cells
 //      wholly inside or outside get their area at once, cells cut by a
 //      region boundary (~1 %) are queued;
-//   4. one warp per queued cell: its area quadrature, warp-cooperative (the
-//      21 or 42 Gauss-Kronrod nodes of a step over the lanes, the rule's
-//      sums reduced lane-parallel, the interval list in shared memory) --
-//      the same adaptive scheme the host builder runs serially.
+//   4. one group of 16 lanes per queued cell, taken from a shared counter:
+//      its area quadrature, group-cooperative (the 21 or 42 Gauss-Kronrod
+//      nodes of a step over the lanes, the rule's sums reduced lane-parallel,
+//      the interval list in shared memory) -- the same adaptive scheme the
+//      host builder runs serially.
 // The per-thread quadratures of steps 1-2 keep their interval list (128
 // intervals) in local memory; the host builder's limit of 4000 gives bitwise
 // the same meshes (these integrals converge in far fewer intervals).
