@@ -314,9 +314,11 @@ def run_gb300(args):
         "gpu_launches": None,
         "clocks": clocks.summary(),
     }
-    # kernels launched per step: rays 1, integrator 2 (+2 Num4D pre-pass/scan),
-    # energy 1, fold 1, likelihood 2
-    out["gpu_launches"] = args.steps * (1 + 4 + 1 + 1 + 2)
+    # kernels launched per step (the ncu launch list of this bench): rays 1;
+    # integrator 6 (row costs, chunk plan, Num4D pre-pass and scan, the
+    # integration, the ordered reduction); energy 1; fold 3 (row and column
+    # splits, the double-float product); likelihood 2
+    out["gpu_launches"] = args.steps * (1 + 6 + 1 + 3 + 2)
     out["roofline"] = roofline(int_ms, int_flops, V)
     if rank == 0:
         legs = set(args.legs.split(",")) if args.legs != "all" else \
